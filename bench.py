@@ -1,0 +1,308 @@
+"""Frequency points per second of the mom25d sweep path on GB300.
+
+Workload: the 7-section stepped-impedance low-pass (eps_r 3.55, h 0.508 mm,
+widths 4.0/0.3 mm, lengths from default_rng(0), mesh 0.35/0.05 mm ->
+N = 5943 unknowns), its 101 frequencies 0.5-8 GHz taken in turn. One step =
+one frequency point of Solver.sweep: Green's tables, impedance fill, LU +
+solve of the 2 port excitations, de-embedding to S, all on the GPU.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64] [--impl reference]
+
+value: points/s with the mesh, test blocks and port data already on the
+device (the `mixed` path: complex64 fill + LU, fp64 refinement). e2e: the
+same through the public API (Solver construction + sweep, host arrays in,
+S and the currents back on the host). Under torchrun each rank sweeps its
+own frequencies (weak scaling, no collective in the path). --impl
+reference times the CPU oracle (numpy restatement of mom25d's own path) on
+the host cores on a bounded sample of each point.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "freq points/s at N~6k (mixed + fp64 refinement vs plain fp64), |dS| <= 1e-5"
+UNIT = "points/s"
+WORKLOAD = {"workload": "stepped-impedance LPF, 7 sections, eps_r 3.55 h 0.508 mm, mesh 0.35/0.05 mm",
+            "N": 5943, "triangles": 4134, "ports": 2, "freqs": "101 points 0.5-8 GHz, taken in turn"}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi samples (SM clock, throttle reasons) during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in self.rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def build_workload(api):
+    from mom25d_gb300 import workloads
+
+    return workloads.build(api, "lpf")
+
+
+def lu_flops(n, nrhs=2):
+    """Complex LU (8/3 n^3 real flops) + the two triangular solves (8 n^2 nrhs)."""
+    return 8.0 / 3.0 * n ** 3 + 8.0 * n * n * nrhs
+
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    import mom25d_gb300 as G
+    from mom25d_gb300 import engine as E
+    from mom25d_gb300.solver import Solver
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lay, st, mesh, freqs = build_workload(G)
+    n = mesh.n_unknowns
+    my = [freqs[(rank * args.steps + i) % len(freqs)] for i in range(args.steps + args.warmup)]
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident: geometry, ports uploaded before the timed region
+    sol = Solver(mesh, st, verbose=False, precision=args.precision, device=local)
+    sol.geometry()
+    sol.port_data()
+    lib, ctx = sol.ctx.lib, sol.ctx.h
+    for f in my[:args.warmup]:
+        sol.point(f)
+    import ctypes as C
+
+    ms = (C.c_double * 11)()
+    cnt = (C.c_longlong * 11)()
+    E.check(lib.m25_ctx_timing(ctx, 1, ms, cnt))  # reset + enable the stage timers
+    barrier()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for f in my[args.warmup:]:
+            sol.point(f)
+        sol.ctx.synchronize()
+        barrier()
+        dt = time.perf_counter() - t0
+    E.check(lib.m25_ctx_timing(ctx, 0, ms, cnt))
+    stages = dict(zip(["greens", "fill", "gather", "via", "lu_panel", "lu_laswp", "lu_trsm", "lu_gemm", "trsv",
+                       "refine", "deembed"], [round(v / args.steps, 4) for v in ms]))
+    launches = {k: int(c) for k, c in zip(stages, cnt)}
+    geo = sol.geometry_stats()
+    sol.close()
+    # ---- e2e through the public API: host arrays in, S + currents out
+    barrier()
+    t0 = time.perf_counter()
+    sol2 = Solver(mesh, st, verbose=False, precision=args.precision, device=local)
+    r = sol2.sweep(my[args.warmup:], keep_currents=True)
+    torch.cuda.synchronize()
+    barrier()
+    dt_e2e = time.perf_counter() - t0
+    sol2.close()
+    # fp64 reference point of the engine itself (same kernels, fp64 fill + LU)
+    t64 = None
+    if args.precision != "fp64" and args.fp64_points > 0:
+        s64 = Solver(mesh, st, verbose=False, precision="fp64", device=local)
+        s64.geometry()
+        s64.port_data()
+        s64.point(my[0])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for f in my[1:1 + args.fp64_points]:
+            s64.point(f)
+        torch.cuda.synchronize()
+        t64 = (time.perf_counter() - t0) / args.fp64_points
+        s64.close()
+    # max over ranks
+    tt = torch.tensor([dt, dt_e2e], dtype=torch.float64, device="cuda")
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    dt, dt_e2e = float(tt[0]), float(tt[1])
+    if rank != 0:
+        return None
+    value = world * args.steps / dt
+    step_ms = dt / args.steps * 1e3
+    # roofline: the LU trailing update (tensor path) or, on the SIMT path,
+    # the fill; algorithmic flops per step over the stage's event time
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    lu_ms = stages["lu_gemm"]
+    gemm_flops = 8.0 / 3.0 * n ** 3  # the trailing updates carry ~all of the LU's flops
+    achieved = gemm_flops / (lu_ms * 1e-3) / 1e12 if lu_ms else None
+    bf16 = peaks.get("bf16_tflops_sustained") or 1700.0
+    roof = {"kernel": "lu trailing update (complex64, per step)", "bound": "tensor",
+            "achieved": round(achieved, 2) if achieved else None, "peak": bf16, "unit": "TFLOP/s",
+            "frac": round(achieved / bf16, 4) if achieved else None, "traffic": None,
+            "peak_source": "MEASURED_PEAKS.json bf16 sustained" if peaks else "fallback 1.7 PFLOP/s"}
+    h2d = (mesh.verts.nbytes + mesh.tri_basis.nbytes // 2 + mesh.tri_sign.nbytes + mesh.edge_len.nbytes) / args.steps
+    d2h = n * 2 * 16 + 4 * 16
+    out = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(step_ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64+c128" if args.precision == "mixed" else "c128", "data": "synthetic",
+        "config": dict(WORKLOAD, precision=args.precision, l2="inputs > L2 (Z 283 MB, fill scratch 1.2 GB per step)"),
+        "e2e": {"value": round(world * args.steps / dt_e2e, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "stages_ms_per_step": stages, "gpu_launches": int(sum(launches.values())),
+        "fp64_ms_per_point": round(t64 * 1e3, 2) if t64 else None,
+        "speedup_vs_fp64": round(t64 / (dt / args.steps), 2) if t64 else None,
+        "roofline": roof, "clocks": clk.summary(), "geometry": geo,
+        "refine_steps": r.info["refine_steps"][:4] if r.info else None,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(samples=1)
+    return out
+
+
+def cpu_sample_point(sw, f, block_frac=0.2):
+    """Oracle time of one frequency point: Green's tables + fill of a fraction
+    of the test blocks (scaled to all of them) + LU + de-embedding."""
+    from oracle import sweep as O
+
+    t0 = time.perf_counter()
+    kern = sw.kernels(f)
+    t1 = time.perf_counter()
+    geo = sw.geom
+    nb = len(geo.blocks)
+    k = max(1, int(block_frac * nb))
+    full = geo.blocks
+    geo.blocks = full[:k]
+    try:
+        Z = O.fill(geo, kern, 2 * np.pi * f, sw.stack.surface_impedance(f))
+    finally:
+        geo.blocks = full
+    t2 = time.perf_counter()
+    Z = Z + np.eye(Z.shape[0]) * (1e-3 + np.abs(np.diag(Z)).max())  # partial fill: keep the LU well posed
+    x = O.dense_solve(Z, sw.excitations())
+    t3 = time.perf_counter()
+    q = O.charges(sw.mesh, x, kern.omega)
+    try:
+        sw.deembed(f, kern, x, q)
+    except Exception:  # noqa: BLE001 - the partial Z gives a meaningless fit; its time still counts
+        pass
+    t4 = time.perf_counter()
+    return (t1 - t0) + (t2 - t1) * nb / k + (t3 - t2) + (t4 - t3)
+
+
+def cpu_baseline(samples=1):
+    import mom25d_gb300 as G
+    from oracle import sweep as O
+
+    lay, st, mesh, freqs = build_workload(G)
+    sw = O.Sweep(mesh, st)
+    ts = [cpu_sample_point(sw, freqs[50 + i]) for i in range(samples)]
+    sec = float(np.mean(ts))
+    cores = os.cpu_count()
+    return {"value": round(1.0 / sec, 5), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{samples} point(s) of the workload: Green's tables, LU and de-embedding in full, fill timed "
+                      "on 20% of the 130 test blocks and scaled; numpy/scipy with OpenBLAS on all host threads"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    import mom25d_gb300 as G
+    from oracle import sweep as O
+
+    lay, st, mesh, freqs = build_workload(G)
+    sw = O.Sweep(mesh, st)
+    for i in range(args.warmup):
+        cpu_sample_point(sw, freqs[i % len(freqs)], block_frac=0.05)
+    ts = [cpu_sample_point(sw, freqs[(args.warmup + i) % len(freqs)], block_frac=0.05) for i in range(args.steps)]
+    sec = float(np.sum(ts))
+    value = args.steps / sec
+    return {"metric": METRIC, "value": round(value, 5), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(sec / args.steps * 1e3, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic", "impl": "reference",
+            "config": dict(WORKLOAD, precision="fp64 (numpy / scipy LAPACK)"),
+            "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                             "sample": "per step one frequency point: tables, LU, de-embedding in full, fill on 5% "
+                                       "of the test blocks scaled to all"},
+            "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=12)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--fp64-points", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        out = run_ours(args, rank, world, local)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,199 @@
+/*
+ * C ABI of the GB300 (sm_103a) engine for mom25d's per-frequency sweep path:
+ * Green's-function tabulation, RWG impedance fill, dense complex LU factor +
+ * solve, and port de-embedding to S-parameters.
+ *
+ * Every call returns an int status (M25_OK or an M25_ERR_* code); the text
+ * of the last error of the calling thread is m25_last_error(). No C++
+ * exception crosses this boundary. Array arguments are plain pointers with
+ * sizes; "host" arrays are ordinary CPU memory, "device" arrays are CUDA
+ * device pointers on the context's device. Complex numbers are interleaved
+ * (re, im) pairs of double (complex128) or float (complex64), row-major.
+ *
+ * Reference interfaces replaced (paths inside the mom25d project):
+ *   m25_geometry_create  AssemblyGeometry.__init__  Engine/mom25d/solver.py:321-426
+ *   m25_greens_create    GroundedSlabGreens          Engine/mom25d/greens.py:205-318
+ *                        LayeredGreens               Engine/mom25d/layered.py:217-405
+ *   m25_assemble         assemble                    Engine/mom25d/solver.py:429-524
+ *                        _via_blocks                 Engine/mom25d/solver.py:527-566
+ *   m25_dense_solve      _dense_solve                Engine/mom25d/solver.py:11-23
+ *   m25_deembed          Solver.sweep de-embedding   Engine/mom25d/solver.py:1276-1325
+ *                        (charges 1076-1091, line_voltage 1101-1125, PortModel 604-610,
+ *                         fit_waves 618-670, _reciprocal_z0 1357-1427)
+ */
+#ifndef M25_H
+#define M25_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  M25_OK = 0,
+  M25_ERR_VALUE = 1,   /* bad argument or model (mom25d raises ValueError) */
+  M25_ERR_MEMORY = 2,  /* device memory exhausted (MemoryError) */
+  M25_ERR_CUDA = 3,    /* CUDA runtime failure (RuntimeError) */
+  M25_ERR_NUMERIC = 4  /* singular matrix, non-converged refinement (RuntimeError) */
+};
+
+enum { M25_FP64 = 0, M25_MIXED = 1 };          /* arithmetic of fill + LU */
+enum { M25_ON_HOST = 0, M25_ON_DEVICE = 1 };    /* where array arguments live */
+
+typedef struct m25_ctx m25_ctx;
+typedef struct m25_geom m25_geom;
+typedef struct m25_greens m25_greens;
+
+const char* m25_last_error(void);
+int m25_version(void);
+
+/* One context per host thread: a device, a CUDA stream, a workspace. */
+int m25_ctx_create(int device, m25_ctx** out);
+int m25_ctx_destroy(m25_ctx* ctx);
+int m25_ctx_synchronize(m25_ctx* ctx);
+void* m25_ctx_stream(m25_ctx* ctx); /* the cudaStream_t every call of this context runs on */
+
+/* Stage timers: CUDA events recorded on the context's stream around the
+ * kernels of each stage (the verbose green / fill / solve timers of
+ * Engine/mom25d/solver.py:1023-1026, per kernel class). Copies the
+ * accumulated milliseconds and launch counts of the M25_STAGES stages to the
+ * outputs (either may be NULL), then enable = 1 / 0 resets and switches the
+ * timers on / off, enable = -1 only reads. Stages, in order: greens, fill,
+ * gather, via, lu_panel, lu_laswp, lu_trsm, lu_gemm, trsv, refine, deembed. */
+#define M25_STAGES 11
+int m25_ctx_timing(m25_ctx* ctx, int enable, double* ms_out, long long* count_out);
+
+/* ------------------------------------------------------------------ mesh */
+typedef struct {
+  int32_t nt, nb, nlev;       /* triangles, RWG bases, metal levels */
+  const double* verts;        /* (nt,3,2) counter-clockwise vertices [m] */
+  const int32_t* tri_basis;   /* (nt,3) basis of the edge opposite vertex i, -1 on a boundary */
+  const double* tri_sign;     /* (nt,3) +1 (T+), -1 (T-), 0 */
+  const double* edge_len;     /* (nb) */
+  const int32_t* tri_layer;   /* (nt) level index */
+  const double* level_z;      /* (nlev) level heights [m] */
+  const int32_t* edge_tri;    /* (nb,2) T+, T- of each basis */
+  const int32_t* edge_loc;    /* (nb,2) local index of the edge in T+, T- */
+  int32_t nblocks;            /* test blocks: <= 32 Morton-ordered triangles of one level */
+  const int32_t* block_tris;  /* (nblocks,32) triangle per slot, -1 empty */
+  int32_t nv;                 /* via segments (unknowns nb .. nb+nv-1) */
+  int32_t npad;               /* triangles attached to via ends */
+  const int32_t* pad_tris;    /* (npad) */
+  const int32_t* seg_pad_off; /* (nv+1) CSR offsets into seg_pad / seg_pad_w */
+  const int32_t* seg_pad;     /* pad index per entry */
+  const double* seg_pad_w;    /* +1/A_top or -1/A_bottom per entry */
+  const int32_t* seg_end_lev; /* (nv,2) level of the top / bottom end charge, -1 none */
+  const double* seg_span;     /* (nv,2) z bottom, z top [m] */
+  const double* seg_xy;       /* (nv,2) via centre [m] */
+  const double* seg_drill;    /* (nv) */
+  double near_factor, far_factor; /* 3, 10 in mom25d */
+} m25_mesh_desc;
+
+/* Uploads the mesh, builds the frequency-independent fill data on the
+ * device: quadrature points, near/mid/far classes per (test block, source
+ * triangle), closed-form 1/R integrals of the near pairs. Host arrays. */
+int m25_geometry_create(m25_ctx* ctx, const m25_mesh_desc* desc, m25_geom** out);
+int m25_geometry_destroy(m25_geom* g);
+/* out[0..3] = near, mid, far (test triangle, source triangle) pairs; bytes of near-pair data */
+int m25_geometry_stats(m25_geom* g, int64_t* out4);
+
+/* ---------------------------------------------------------- Green's tables */
+typedef struct {
+  double freq;
+  int32_t nlayer;             /* dielectric layers, bottom to top (air above) */
+  const double* layer_t;
+  const double* layer_eps;
+  const double* layer_tand;
+  int32_t nlev;               /* metal levels of the mesh */
+  const int32_t* lev_iface;   /* interface index 1..nlayer of each level */
+  const double* lev_z;        /* height of each level [m] */
+  int32_t single;             /* 1: one slab, metal on top (closed-form slab kernels) */
+  double zs_ground_re, zs_ground_im; /* ground-plane surface impedance (0: PEC) */
+  double stack_h;             /* total stack height [m] */
+  int32_t nk_c, nk_r;         /* Sommerfeld path: lifted arc points, real-axis points */
+  const double* kc;           /* (nk_c,2) complex points */
+  const double* wc;           /* (nk_c,2) complex weights */
+  const double* kr;           /* (nk_r) */
+  const double* wr;           /* (nk_r) */
+  int32_t nrho;
+  const double* rho;          /* (nrho) tabulation radii, rho[0] = 0 */
+  double kbig;                /* spectral sample for layered leading terms (15 / t_min) */
+} m25_greens_desc;
+
+int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* desc, m25_greens** out);
+int m25_greens_destroy(m25_greens* g);
+/* Host copies: S (3,nlev,nlev,nrho) complex128 [S_A, S_V, S_W]; c (3,nlev,nlev)
+ * complex128 leading coefficients; coef (nlev*nlev, nrho-1, 4, 3) complex128
+ * not-a-knot cubic coefficients (highest power first). Any may be NULL. */
+int m25_greens_tables(m25_greens* g, double* S, double* c, double* coef);
+
+/* ----------------------------------------------------------------- fill */
+/* Z (n x n, n = nb + nv) of the MPIE Galerkin fill, symmetrised. precision
+ * M25_FP64 writes complex128, M25_MIXED complex64 (fp32 arithmetic). Z is
+ * host or device memory (where); ldz its row stride in elements. */
+int m25_assemble(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, double zs_re, double zs_im,
+                 double zsv_re, double zsv_im, int precision, void* Z, int64_t ldz, int where);
+
+/* ---------------------------------------------------------------- solve */
+/* Z X = B for an n x n complex128 Z (overwritten by its LU factors when on
+ * the device, as mom25d's _dense_solve overwrites Z) and nrhs right-hand
+ * sides B (n x nrhs complex128, row-major). precision M25_FP64: LU with
+ * partial pivoting in fp64; M25_MIXED: complex64 LU (tensor-core trailing
+ * updates) and fp64 iterative refinement against Z to tol (relative
+ * residual) in at most max_iter steps. info[0] = refinement steps taken,
+ * info[1] = 0 or the first zero pivot (1-based). */
+int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precision, void* Z, const void* B, void* X,
+                    int where, double tol, int32_t max_iter, int32_t* info);
+
+/* ----------------------------------------------------------- de-embedding */
+typedef struct {
+  int32_t nport;               /* feed ports P */
+  int32_t ngroup;              /* ports sharing a line (same width, level): one wave fit each */
+  const int32_t* group_of;     /* (P) group index */
+  const int32_t* port_level;   /* (P) mesh level of each feed */
+  const int32_t* ns;           /* (P) fit-window cuts per port */
+  const double* s;             /* concatenated cut positions [m] */
+  const int32_t* cut_off;      /* (sum ns + 1) CSR over cut edges */
+  const int32_t* cut_edge;     /* RWG index per entry */
+  const double* cut_w;         /* sign * edge length per entry */
+  const int32_t* nvpt;         /* (P) voltage points per port (ns * 8) */
+  const double* vpts;          /* concatenated (x, y) voltage points */
+  const double* beta0;         /* (ngroup) Kirschning-Jansen initial phase constant */
+  int32_t lossless;            /* 1: bounded Brent on beta; 0: Nelder-Mead on gamma */
+  const double* bounds;        /* (ngroup,2) beta search bounds (lossless) */
+  double v_weight;             /* voltage residual weight (1) */
+  const double* excitation;    /* (nport, n) delta-gap excitation vectors (PortModel.excitation) */
+} m25_port_desc;
+
+typedef struct m25_ports m25_ports;
+int m25_ports_create(m25_ctx* ctx, m25_geom* geom, const m25_port_desc* desc, m25_ports** out);
+int m25_ports_destroy(m25_ports* p);
+
+/* From the solution x (n x P complex128, device or host per where) at one
+ * frequency: S (P,P) referenced to the extracted line impedances, z0 (P),
+ * gamma (P), z0_line (P), fit residual (P), all host complex128 / float64.
+ * beta0 overrides the per-group initial guess (NULL: from the port desc). */
+int m25_deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* ports, const void* x, int where,
+                const double* beta0, double* S, double* z0, double* gamma, double* z0_line, double* resid);
+
+/* One frequency point of Solver.sweep (Engine/mom25d/solver.py:1273-1325) with
+ * every intermediate on the device: fill (precision), solve of the port
+ * excitations, de-embedding. x_out (n, P) complex128 host copy of the
+ * currents or NULL; S, z0, gamma, z0_line, resid as m25_deembed; info[0]
+ * refinement steps, info[1] zero pivot. */
+int m25_sweep_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* ports, double zs_re, double zs_im,
+                    double zsv_re, double zsv_im, int precision, const double* beta0, double tol, int32_t max_iter,
+                    double* x_out, double* S, double* z0, double* gamma, double* z0_line, double* resid,
+                    int32_t* info);
+
+/* Diagnostics of the last m25_deembed: phi (sum nvpt, P) complex128 line
+ * voltages, q (nt, P) complex128 triangle charges, I and V (sum ns, P)
+ * complex128 cut currents / voltages. NULL skips an output. */
+int m25_deembed_debug(m25_ctx* ctx, m25_ports* ports, double* phi, double* q, double* I, double* V);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* M25_H */

@@ -1,0 +1,243 @@
+// C ABI glue: contexts, error text, workspace, and the drivers of the fill
+// (m25_assemble) and of the dense solve (m25_dense_solve).
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "m25_internal.h"
+
+namespace m25 {
+
+static thread_local std::string g_err;
+void set_error(const std::string& msg) { g_err = msg; }
+const char* last_error() { return g_err.c_str(); }
+
+int DevBuf::ensure(size_t n) {
+  if (n <= bytes) return M25_OK;
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+  cudaError_t e = cudaMalloc(&p, n);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    set_error(std::string("workspace cudaMalloc(") + std::to_string(n) + " B): " + cudaGetErrorString(e));
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? M25_ERR_MEMORY : M25_ERR_CUDA;
+  }
+  bytes = n;
+  return M25_OK;
+}
+
+void DevBuf::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+}
+
+// fill.cu
+template <class T>
+int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, void* Z, int64_t ldz, int where);
+
+// lu.cu
+template <class T> int lu_factor(m25_ctx*, cx<T>*, int64_t, int, int32_t*, int, bool, int*);
+template <class T> int lu_solve(m25_ctx*, const cx<T>*, int64_t, int, const int32_t*, const cx<T>*, int, cx<T>*);
+template <class TZ>
+int refine(m25_ctx*, int, int, const cx<TZ>*, int64_t, const zf*, const int32_t*, const zd*, zd*, double, int, int*);
+void cast_to_z32(m25_ctx*, const zd*, int64_t, zf*, int64_t, int, int);
+bool lu_tc_available();
+
+}  // namespace m25
+
+using namespace m25;
+
+extern "C" const char* m25_last_error(void) { return last_error(); }
+extern "C" int m25_version(void) { return 1; }
+
+extern "C" int m25_ctx_create(int device, m25_ctx** out) {
+  if (!out) {
+    set_error("m25_ctx_create: null out");
+    return M25_ERR_VALUE;
+  }
+  int ndev = 0;
+  M25_CUDA(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev) {
+    set_error("m25_ctx_create: no such CUDA device");
+    return M25_ERR_VALUE;
+  }
+  M25_CUDA(cudaSetDevice(device));
+  m25_ctx* c = new m25_ctx();
+  c->device = device;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    set_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    return M25_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  *out = c;
+  return M25_OK;
+}
+
+extern "C" int m25_ctx_destroy(m25_ctx* c) {
+  if (!c) return M25_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (DevBuf* b : {&c->H, &c->Zw, &c->Zlu, &c->Bw, &c->Xw, &c->Rw, &c->Dw, &c->ipiv, &c->scratch, &c->deemb,
+                    &c->Zsweep, &c->Xsweep})
+    b->release();
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return M25_OK;
+}
+
+extern "C" int m25_ctx_synchronize(m25_ctx* c) {
+  if (!c) {
+    set_error("m25_ctx_synchronize: null context");
+    return M25_ERR_VALUE;
+  }
+  M25_CUDA(cudaStreamSynchronize(c->stream));
+  return M25_OK;
+}
+
+extern "C" void* m25_ctx_stream(m25_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+namespace m25 {
+cudaEvent_t take_event(m25_ctx* c) {
+  if (!c->event_pool.empty()) {
+    cudaEvent_t e = c->event_pool.back();
+    c->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+}  // namespace m25
+
+extern "C" int m25_ctx_timing(m25_ctx* c, int enable, double* ms_out, long long* count_out) {
+  if (!c) {
+    set_error("m25_ctx_timing: null context");
+    return M25_ERR_VALUE;
+  }
+  M25_CUDA(cudaStreamSynchronize(c->stream));
+  for (auto& m : c->marks) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, m.a, m.b) == cudaSuccess) {
+      c->stage_ms[m.stage] += ms;
+      c->stage_n[m.stage] += 1;
+    }
+    c->event_pool.push_back(m.a);
+    c->event_pool.push_back(m.b);
+  }
+  c->marks.clear();
+  for (int s = 0; s < ST_COUNT; ++s) {
+    if (ms_out) ms_out[s] = c->stage_ms[s];
+    if (count_out) count_out[s] = c->stage_n[s];
+  }
+  if (enable >= 0) {
+    // any change of the switch starts a new accumulation
+    for (int s = 0; s < ST_COUNT; ++s) {
+      c->stage_ms[s] = 0;
+      c->stage_n[s] = 0;
+    }
+    c->timing = enable != 0;
+  }
+  return M25_OK;
+}
+
+extern "C" int m25_assemble(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, double zs_re, double zs_im, double zsv_re,
+                            double zsv_im, int precision, void* Z, int64_t ldz, int where) {
+  if (!ctx || !geom || !gr || !Z) {
+    set_error("m25_assemble: null argument");
+    return M25_ERR_VALUE;
+  }
+  if (gr->nlev != geom->nlev) {
+    set_error("m25_assemble: Green's tables and mesh have different level counts");
+    return M25_ERR_VALUE;
+  }
+  const int n = geom->nb + geom->nv;
+  if (ldz < n) {
+    set_error("m25_assemble: ldz < n");
+    return M25_ERR_VALUE;
+  }
+  M25_CUDA(cudaSetDevice(ctx->device));
+  if (precision == M25_FP64)
+    return fill_driver<double>(ctx, geom, gr, zd(zs_re, zs_im), zd(zsv_re, zsv_im), Z, ldz, where);
+  if (precision == M25_MIXED)
+    return fill_driver<float>(ctx, geom, gr, zd(zs_re, zs_im), zd(zsv_re, zsv_im), Z, ldz, where);
+  set_error("m25_assemble: precision must be M25_FP64 or M25_MIXED");
+  return M25_ERR_VALUE;
+}
+
+extern "C" int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precision, void* Z, const void* B, void* X,
+                               int where, double tol, int32_t max_iter, int32_t* info) {
+  if (!ctx || !Z || !B || !X || n <= 0 || nrhs <= 0 || nrhs > 8) {
+    set_error("m25_dense_solve: bad argument (1 <= nrhs <= 8)");
+    return M25_ERR_VALUE;
+  }
+  M25_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  const size_t nn = (size_t)n * n, nr = (size_t)n * nrhs;
+  int rc;
+  if ((rc = ctx->ipiv.ensure(sizeof(int32_t) * n))) return rc;
+  if ((rc = ctx->Bw.ensure(sizeof(zd) * nr))) return rc;
+  if ((rc = ctx->Xw.ensure(sizeof(zd) * nr))) return rc;
+  zd* Bd = ctx->Bw.as<zd>();
+  zd* Xd = ctx->Xw.as<zd>();
+  M25_CUDA(cudaMemcpyAsync(Bd, B, sizeof(zd) * nr, where == M25_ON_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st));
+  int zinfo = 0, steps = 0;
+  if (precision == M25_FP64) {
+    zd* Zd = static_cast<zd*>(Z);
+    if (where == M25_ON_HOST) {
+      if ((rc = ctx->Zw.ensure(sizeof(zd) * nn))) return rc;
+      Zd = ctx->Zw.as<zd>();
+      M25_CUDA(cudaMemcpyAsync(Zd, Z, sizeof(zd) * nn, cudaMemcpyHostToDevice, st));
+    }
+    if ((rc = lu_factor<double>(ctx, Zd, n, n, ctx->ipiv.as<int32_t>(), 64, false, &zinfo))) return rc;
+    if (zinfo) {
+      if (info) { info[0] = 0; info[1] = zinfo; }
+      set_error("m25_dense_solve: exactly singular matrix (zero pivot)");
+      return M25_ERR_NUMERIC;
+    }
+    if ((rc = lu_solve<double>(ctx, Zd, n, n, ctx->ipiv.as<int32_t>(), Bd, nrhs, Xd))) return rc;
+  } else if (precision == M25_MIXED || precision == 2) {
+    // M25_MIXED: Z is the complex64 fill; 2: Z is complex128 (cast for the LU)
+    if ((rc = ctx->Zlu.ensure(sizeof(zf) * nn))) return rc;
+    zf* LU = ctx->Zlu.as<zf>();
+    const void* Zres = Z;
+    if (where == M25_ON_HOST) {
+      size_t zb = (precision == M25_MIXED ? sizeof(zf) : sizeof(zd)) * nn;
+      if ((rc = ctx->Zw.ensure(zb))) return rc;
+      M25_CUDA(cudaMemcpyAsync(ctx->Zw.p, Z, zb, cudaMemcpyHostToDevice, st));
+      Zres = ctx->Zw.p;
+    }
+    if (precision == M25_MIXED)
+      M25_CUDA(cudaMemcpyAsync(LU, Zres, sizeof(zf) * nn, cudaMemcpyDeviceToDevice, st));
+    else
+      cast_to_z32(ctx, static_cast<const zd*>(Zres), n, LU, n, n, n);
+    if ((rc = lu_factor<float>(ctx, LU, n, n, ctx->ipiv.as<int32_t>(), 128, lu_tc_available(), &zinfo))) return rc;
+    if (zinfo) {
+      if (info) { info[0] = 0; info[1] = zinfo; }
+      set_error("m25_dense_solve: zero pivot in the complex64 LU");
+      return M25_ERR_NUMERIC;
+    }
+    if (precision == M25_MIXED)
+      rc = refine<float>(ctx, n, nrhs, static_cast<const zf*>(Zres), n, LU, ctx->ipiv.as<int32_t>(), Bd, Xd, tol,
+                         max_iter, &steps);
+    else
+      rc = refine<double>(ctx, n, nrhs, static_cast<const zd*>(Zres), n, LU, ctx->ipiv.as<int32_t>(), Bd, Xd, tol,
+                          max_iter, &steps);
+    if (rc) return rc;
+  } else {
+    set_error("m25_dense_solve: unknown precision");
+    return M25_ERR_VALUE;
+  }
+  M25_CUDA(cudaMemcpyAsync(X, Xd, sizeof(zd) * nr, where == M25_ON_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
+  M25_CUDA(cudaStreamSynchronize(st));
+  if (info) {
+    info[0] = steps;
+    info[1] = 0;
+  }
+  return M25_OK;
+}

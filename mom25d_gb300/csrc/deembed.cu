@@ -1,0 +1,699 @@
+// Port de-embedding on the device (Engine/mom25d/solver.py:1276-1325):
+// triangle charges (1076-1091), line voltages at the feed sample points
+// (1101-1125), cut currents and voltages (PortModel, 604-610), the wave fit
+// (fit_waves, 618-670: Nelder-Mead on gamma with per-dataset 2x2 least
+// squares) and S with reciprocity-fitted reference impedances (1316-1325,
+// 1357-1427).
+#include <cmath>
+#include <vector>
+
+#include "m25_integrals.cuh"
+#include "m25_internal.h"
+
+namespace m25 {
+
+constexpr int kMaxPorts = 8;
+constexpr int kMaxSamples = 128;  // fit-window cuts per port
+
+// charge density per triangle, q = -div J / (jw)
+__global__ void charges_kernel(int nt, int nb, int P, const TriData<double>* __restrict__ td,
+                               const int32_t* __restrict__ tri_basis, const zd* __restrict__ x, double omega,
+                               zd* __restrict__ q) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  const zd jw(0.0, omega);
+  for (int e = 0; e < P; ++e) {
+    zd div(0.0);
+    for (int i = 0; i < 3; ++i) {
+      int b = tri_basis[3 * t + i];
+      if (b >= 0) div += x[(int64_t)b * P + e] * td[t].cV[i];
+    }
+    q[(int64_t)t * P + e] = -div / jw;
+  }
+}
+
+// via segments drain their upper triangles and feed their lower ones
+__global__ void via_charges_kernel(int nv, int nb, int P, const int32_t* __restrict__ seg_pad_off,
+                                   const int32_t* __restrict__ seg_pad, const double* __restrict__ seg_pad_w,
+                                   const int32_t* __restrict__ pad_tris, const zd* __restrict__ x, double omega,
+                                   zd* __restrict__ q) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nv) return;
+  const zd jw(0.0, omega);
+  for (int e = seg_pad_off[k]; e < seg_pad_off[k + 1]; ++e) {
+    int t = pad_tris[seg_pad[e]];
+    for (int c = 0; c < P; ++c) {
+      zd v = -(x[(int64_t)(nb + k) * P + c] * seg_pad_w[e]) / jw;
+      atomicAdd(&q[(int64_t)t * P + c].re, v.re);
+      atomicAdd(&q[(int64_t)t * P + c].im, v.im);
+    }
+  }
+}
+
+__device__ inline zd spline_w(const double* __restrict__ rho, int n, const zd* __restrict__ coef, int pair, double r) {
+  int i;
+  if (r < rho[1]) i = 0;
+  else if (r >= rho[n - 2]) i = n - 2;
+  else {
+    int lo = 1, hi = n - 2;
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (r < rho[mid]) hi = mid; else lo = mid;
+    }
+    i = lo;
+  }
+  double dx = r - rho[i];
+  const zd* c = coef + ((size_t)pair * (n - 1) + i) * 12;
+  double z = dx, z2 = dx * dx, z3 = z2 * dx;
+  return c[3 * 3 + 2] + c[2 * 3 + 2] * z + c[1 * 3 + 2] * z2 + c[0 * 3 + 2] * z3;
+}
+
+// phi[m][e] = (1/eps0) sum_t [sum_k w_k S_W(|p_m - r_k|) + c_W I0(t, p_m) / 4pi] q[t][e]
+__global__ void line_voltage_kernel(int nt, int P, int L, const double* __restrict__ pts,
+                                    const int32_t* __restrict__ pt_level, const double* __restrict__ cen,
+                                    const TriData<double>* __restrict__ td, const int32_t* __restrict__ tri_layer,
+                                    const double* __restrict__ level_z, int nrho, const double* __restrict__ rho,
+                                    const zd* __restrict__ coef, const zd* __restrict__ cW, const zd* __restrict__ q,
+                                    zd* __restrict__ phi) {
+  int m = blockIdx.x;
+  int li = pt_level[m];
+  double px = pts[2 * m], py = pts[2 * m + 1];
+  zd acc[kMaxPorts];
+  for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+    int ls = tri_layer[t];
+    int pair = li * L + ls;
+    const TriData<double>& T = td[t];
+    double ox = px - cen[2 * t], oy = py - cen[2 * t + 1];
+    zd k0w(0.0);
+    for (int k = 0; k < 7; ++k) {
+      double dx = ox - T.q7[k][0], dy = oy - T.q7[k][1];
+      k0w += spline_w(rho, nrho, coef, pair, sqrt(dx * dx + dy * dy)) * T.w7[k];
+    }
+    zd cw = cW[pair];
+    if (cw.re != 0.0 || cw.im != 0.0) {
+      double I0, I1x, I1y;
+      potential_integrals(T.v, ox, oy, fabs(level_z[li] - level_z[ls]), I0, I1x, I1y);
+      k0w += cw * (I0 / (4.0 * kPi));
+    }
+    for (int e = 0; e < P; ++e) acc[e] += k0w * q[(int64_t)t * P + e];
+  }
+  __shared__ double red[32][2];
+  const double ie0 = 1.0 / eps0();
+  for (int e = 0; e < P; ++e) {
+    double a = acc[e].re, b = acc[e].im;
+    for (int o = 16; o; o >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, o);
+      b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      red[threadIdx.x >> 5][0] = a;
+      red[threadIdx.x >> 5][1] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double sa = 0, sb = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        sa += red[w][0];
+        sb += red[w][1];
+      }
+      phi[(int64_t)m * P + e] = zd(sa, sb) * ie0;
+    }
+    __syncthreads();
+  }
+}
+
+// cut currents I[c][e] = sum sign len x and cut voltages V[c][e] = mean of phi over its 8 points
+__global__ void cuts_kernel(int ncut, int P, const int32_t* __restrict__ cut_off, const int32_t* __restrict__ cut_edge,
+                            const double* __restrict__ cut_w, const zd* __restrict__ x, const zd* __restrict__ phi,
+                            int nper, zd* __restrict__ I, zd* __restrict__ V) {
+  int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= ncut * P) return;
+  int c = gid / P, e = gid % P;
+  zd s(0.0);
+  for (int k = cut_off[c]; k < cut_off[c + 1]; ++k) s += x[(int64_t)cut_edge[k] * P + e] * cut_w[k];
+  I[gid] = s;
+  zd v(0.0);
+  for (int k = 0; k < nper; ++k) v += phi[((int64_t)c * nper + k) * P + e];
+  V[gid] = v / double(nper);
+}
+
+// ------------------------------------------------------------------ fit
+struct FitArgs {
+  int P, ngroup;
+  int group_of[kMaxPorts];
+  int ns[kMaxPorts];
+  int s_off[kMaxPorts];     // offset of port p's cuts in s / I / V rows
+  double beta0[kMaxPorts];  // per group
+  double v_weight;
+  const double* s;          // concatenated cut positions
+  const zd* I;              // (sum ns, P)
+  const zd* V;              // (sum ns, P)
+  zd* A;                    // (P, P) incident amplitudes
+  zd* B;                    // (P, P)
+  zd* gamma;                // (P)
+  zd* zline;                // (P)
+  double* resid;            // (P)
+  int* iters;               // (ngroup) Nelder-Mead iterations
+  zd* S;                    // (P, P)
+  double* z0;               // (P)
+};
+
+__device__ inline double warp_sum(double v) {
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ inline zd warp_sum(zd v) { return zd(warp_sum(v.re), warp_sum(v.im)); }
+
+// Residual of the wave model at gamma for the datasets of one group (all lanes
+// of the warp return the same value); optionally stores coefficients, z0.
+__device__ double wave_objective(const FitArgs& a, int grp, zd g, double Inrm, double Vnrm, bool store) {
+  const int lane = threadIdx.x & 31;
+  double res = 0.0;
+  zd UV(0.0);
+  double UU = 0.0;
+  constexpr int kPer = kMaxSamples / 32;
+  zd U[kMaxPorts * kMaxPorts][kPer];
+  int nd = 0;
+  for (int p = 0; p < a.P; ++p) {
+    if (a.group_of[p] != grp) continue;
+    for (int e = 0; e < a.P; ++e, ++nd) {
+      const int ns = a.ns[p], off = a.s_off[p];
+      zd ep[kPer], em[kPer], Iv[kPer];
+      double n11 = 0;
+      for (int u = 0; u < kPer; ++u) {
+        int i = lane + 32 * u;
+        if (i < ns) {
+          double s = a.s[off + i];
+          ep[u] = cexp(g * s);
+          em[u] = cexp(-g * s);
+          Iv[u] = a.I[(int64_t)(off + i) * a.P + e];
+          n11 += norm2(ep[u]);
+        } else {
+          ep[u] = em[u] = Iv[u] = zd(0.0);
+        }
+      }
+      // two-column least squares by modified Gram-Schmidt with one re-orthogonalisation
+      double r11 = sqrt(warp_sum(n11));
+      zd q1[kPer];
+      zd r12(0.0);
+      for (int u = 0; u < kPer; ++u) {
+        q1[u] = ep[u] / r11;
+        r12 += conj(q1[u]) * em[u];
+      }
+      r12 = warp_sum(r12);
+      zd v[kPer];
+      zd r12b(0.0);
+      for (int u = 0; u < kPer; ++u) {
+        v[u] = em[u] - r12 * q1[u];
+        r12b += conj(q1[u]) * v[u];
+      }
+      r12b = warp_sum(r12b);
+      double n22 = 0;
+      for (int u = 0; u < kPer; ++u) {
+        v[u] -= r12b * q1[u];
+        n22 += norm2(v[u]);
+      }
+      r12 += r12b;
+      double r22 = sqrt(warp_sum(n22));
+      zd b1(0.0), b2(0.0);
+      for (int u = 0; u < kPer; ++u) {
+        b1 += conj(q1[u]) * Iv[u];
+        b2 += conj(v[u] / r22) * Iv[u];
+      }
+      b1 = warp_sum(b1);
+      b2 = warp_sum(b2);
+      zd c1 = b2 / zd(r22);
+      zd c0 = (b1 - r12 * c1) / zd(r11);
+      double rr = 0;
+      for (int u = 0; u < kPer; ++u) {
+        zd d = c0 * ep[u] + c1 * em[u] - Iv[u];
+        rr += norm2(d);
+        U[nd][u] = c0 * ep[u] - c1 * em[u];
+        if (lane + 32 * u < ns) {
+          zd Vv = a.V[(int64_t)(off + lane + 32 * u) * a.P + e];
+          UV += conj(U[nd][u]) * Vv;
+          UU += norm2(U[nd][u]);
+        }
+      }
+      res += warp_sum(rr) / Inrm;
+      if (store && lane == 0) {
+        a.A[p * a.P + e] = c0;
+        a.B[p * a.P + e] = c1;
+      }
+    }
+  }
+  zd z0 = warp_sum(UV) / zd(warp_sum(UU));
+  double rv = 0;
+  nd = 0;
+  for (int p = 0; p < a.P; ++p) {
+    if (a.group_of[p] != grp) continue;
+    for (int e = 0; e < a.P; ++e, ++nd) {
+      const int ns = a.ns[p], off = a.s_off[p];
+      for (int u = 0; u < kPer; ++u)
+        if (lane + 32 * u < ns) {
+          zd Vv = a.V[(int64_t)(off + lane + 32 * u) * a.P + e];
+          rv += norm2(Vv - z0 * U[nd][u]);
+        }
+    }
+  }
+  res += a.v_weight * warp_sum(rv) / Vnrm;
+  if (store && lane == 0)
+    for (int p = 0; p < a.P; ++p)
+      if (a.group_of[p] == grp) a.zline[p] = z0;
+  return res;
+}
+
+// One warp per port group: Nelder-Mead with scipy's coefficients (reflection
+// 1, expansion 2, contraction 0.5, shrink 0.5), initial simplex 5 % steps,
+// stopping when the simplex spans <= xatol and its values <= fatol.
+__global__ void fit_kernel(FitArgs a) {
+  const int grp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (grp < a.ngroup) {
+    const double scale = fabs(a.beta0[grp]);
+    double Inrm = 0, Vnrm = 0;
+    for (int p = 0; p < a.P; ++p) {
+      if (a.group_of[p] != grp) continue;
+      for (int i = lane; i < a.ns[p]; i += 32)
+        for (int e = 0; e < a.P; ++e) {
+          Inrm += norm2(a.I[(int64_t)(a.s_off[p] + i) * a.P + e]);
+          Vnrm += norm2(a.V[(int64_t)(a.s_off[p] + i) * a.P + e]);
+        }
+    }
+    Inrm = warp_sum(Inrm);
+    Vnrm = warp_sum(Vnrm);
+    auto f = [&](double x0, double x1) { return wave_objective(a, grp, zd(scale * x0, scale * x1), Inrm, Vnrm, false); };
+    const double xatol = 1e-10, fatol = 1e-16;
+    double sim[3][2], fs[3];
+    // gamma0 = 1e-3 b0 + j b0, scaled by |b0|
+    double x0 = 1e-3 * a.beta0[grp] / scale, x1 = a.beta0[grp] / scale;
+    sim[0][0] = x0; sim[0][1] = x1;
+    sim[1][0] = x0 != 0 ? 1.05 * x0 : 0.00025; sim[1][1] = x1;
+    sim[2][0] = x0; sim[2][1] = x1 != 0 ? 1.05 * x1 : 0.00025;
+    for (int k = 0; k < 3; ++k) fs[k] = f(sim[k][0], sim[k][1]);
+    auto sort3 = [&]() {  // stable insertion sort by value
+      for (int i = 1; i < 3; ++i)
+        for (int j = i; j > 0 && fs[j] < fs[j - 1]; --j) {
+          double t = fs[j]; fs[j] = fs[j - 1]; fs[j - 1] = t;
+          for (int d = 0; d < 2; ++d) { double u = sim[j][d]; sim[j][d] = sim[j - 1][d]; sim[j - 1][d] = u; }
+        }
+    };
+    sort3();
+    int it = 1;
+    while (it < 4000) {
+      double dx = 0, df = 0;
+      for (int k = 1; k < 3; ++k) {
+        dx = fmax(dx, fmax(fabs(sim[k][0] - sim[0][0]), fabs(sim[k][1] - sim[0][1])));
+        df = fmax(df, fabs(fs[0] - fs[k]));
+      }
+      if (dx <= xatol && df <= fatol) break;
+      double xb[2], xr[2];
+      for (int d = 0; d < 2; ++d) {
+        xb[d] = (sim[0][d] + sim[1][d]) / 2.0;
+        xr[d] = 2.0 * xb[d] - sim[2][d];
+      }
+      double fr = f(xr[0], xr[1]);
+      bool shrink = false;
+      if (fr < fs[0]) {
+        double xe[2] = {3.0 * xb[0] - 2.0 * sim[2][0], 3.0 * xb[1] - 2.0 * sim[2][1]};
+        double fe = f(xe[0], xe[1]);
+        if (fe < fr) { sim[2][0] = xe[0]; sim[2][1] = xe[1]; fs[2] = fe; }
+        else { sim[2][0] = xr[0]; sim[2][1] = xr[1]; fs[2] = fr; }
+      } else if (fr < fs[1]) {
+        sim[2][0] = xr[0]; sim[2][1] = xr[1]; fs[2] = fr;
+      } else if (fr < fs[2]) {
+        double xc[2] = {1.5 * xb[0] - 0.5 * sim[2][0], 1.5 * xb[1] - 0.5 * sim[2][1]};
+        double fc = f(xc[0], xc[1]);
+        if (fc <= fr) { sim[2][0] = xc[0]; sim[2][1] = xc[1]; fs[2] = fc; }
+        else shrink = true;
+      } else {
+        double xc[2] = {0.5 * xb[0] + 0.5 * sim[2][0], 0.5 * xb[1] + 0.5 * sim[2][1]};
+        double fc = f(xc[0], xc[1]);
+        if (fc < fs[2]) { sim[2][0] = xc[0]; sim[2][1] = xc[1]; fs[2] = fc; }
+        else shrink = true;
+      }
+      if (shrink)
+        for (int j = 1; j < 3; ++j) {
+          for (int d = 0; d < 2; ++d) sim[j][d] = sim[0][d] + 0.5 * (sim[j][d] - sim[0][d]);
+          fs[j] = f(sim[j][0], sim[j][1]);
+        }
+      ++it;
+      sort3();
+    }
+    zd g(scale * sim[0][0], scale * sim[0][1]);
+    double res = wave_objective(a, grp, g, Inrm, Vnrm, true);
+    if (lane == 0) {
+      a.iters[grp] = it;
+      for (int p = 0; p < a.P; ++p)
+        if (a.group_of[p] == grp) {
+          a.gamma[p] = g;
+          a.resid[p] = sqrt(res);
+        }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  // SI = -B A^-1 (Gauss-Jordan with partial pivoting on [A^T | -B^T]: X^T = A^-T (-B^T))
+  const int P = a.P;
+  zd M[kMaxPorts][2 * kMaxPorts];
+  for (int i = 0; i < P; ++i)
+    for (int j = 0; j < P; ++j) {
+      M[i][j] = a.A[j * P + i];          // A^T
+      M[i][P + j] = -a.B[j * P + i];     // -B^T
+    }
+  for (int c = 0; c < P; ++c) {
+    int pr = c;
+    for (int r = c + 1; r < P; ++r)
+      if (cabs(M[r][c]) > cabs(M[pr][c])) pr = r;
+    for (int j = 0; j < 2 * P; ++j) { zd t = M[c][j]; M[c][j] = M[pr][j]; M[pr][j] = t; }
+    zd piv = M[c][c];
+    for (int j = 0; j < 2 * P; ++j) M[c][j] = M[c][j] / piv;
+    for (int r = 0; r < P; ++r)
+      if (r != c) {
+        zd f = M[r][c];
+        for (int j = 0; j < 2 * P; ++j) M[r][j] -= f * M[c][j];
+      }
+  }
+  zd SI[kMaxPorts][kMaxPorts];
+  for (int i = 0; i < P; ++i)
+    for (int j = 0; j < P; ++j) SI[i][j] = M[j][P + i];
+  // reference impedances: reciprocity between groups + scalar-potential level
+  double z[kMaxPorts];
+  const int G = a.ngroup;
+  if (G == 1) {
+    for (int p = 0; p < P; ++p) z[p] = a.zline[p].re;
+  } else {
+    // weighted least squares on log z per group, normal equations
+    double NtN[kMaxPorts][kMaxPorts] = {}, Ntb[kMaxPorts] = {};
+    auto add_row = [&](const double* r, double rhs, double w) {
+      for (int i = 0; i < G; ++i) {
+        Ntb[i] += w * r[i] * rhs;
+        for (int j = 0; j < G; ++j) NtN[i][j] += w * r[i] * r[j];
+      }
+    };
+    for (int i = 0; i < P; ++i)
+      for (int j = i + 1; j < P; ++j) {
+        int gi = a.group_of[i], gj = a.group_of[j];
+        if (gi == gj) continue;
+        double w = fmin(cabs(SI[i][j]), cabs(SI[j][i]));
+        w *= w;
+        if (w > 0) {
+          double r[kMaxPorts] = {};
+          r[gi] = 1;
+          r[gj] = -1;
+          add_row(r, log(cabs(SI[j][i] / SI[i][j])), w);
+        }
+      }
+    double meanlog_all = 0;
+    for (int k = 0; k < G; ++k) {
+      double s = 0;
+      int c = 0;
+      for (int p = 0; p < P; ++p)
+        if (a.group_of[p] == k) { s += a.zline[p].re; ++c; }
+      double r[kMaxPorts] = {};
+      r[k] = 1;
+      add_row(r, log(s / c), 1e-4);
+    }
+    for (int p = 0; p < P; ++p) meanlog_all += log(a.zline[p].re);
+    meanlog_all /= P;
+    // solve NtN x = Ntb (symmetric positive definite, Gaussian elimination)
+    double x[kMaxPorts];
+    for (int c = 0; c < G; ++c)
+      for (int r = c + 1; r < G; ++r) {
+        double f = NtN[r][c] / NtN[c][c];
+        for (int j = c; j < G; ++j) NtN[r][j] -= f * NtN[c][j];
+        Ntb[r] -= f * Ntb[c];
+      }
+    for (int c = G - 1; c >= 0; --c) {
+      double s = Ntb[c];
+      for (int j = c + 1; j < G; ++j) s -= NtN[c][j] * x[j];
+      x[c] = s / NtN[c][c];
+    }
+    double meang = 0;
+    for (int p = 0; p < P; ++p) meang += x[a.group_of[p]];
+    meang /= P;
+    for (int p = 0; p < P; ++p) z[p] = exp(x[a.group_of[p]] + meanlog_all - meang);
+  }
+  for (int i = 0; i < P; ++i) {
+    a.z0[i] = z[i];
+    for (int j = 0; j < P; ++j) a.S[i * P + j] = SI[i][j] * (sqrt(z[i]) / sqrt(z[j]));
+  }
+}
+
+}  // namespace m25
+
+using namespace m25;
+
+struct m25_ports {
+  m25_ctx* ctx = nullptr;
+  int P = 0, ngroup = 0, nvpt_tot = 0, ncut = 0, lossless = 0;
+  double v_weight = 1.0;
+  std::vector<int> group_of, ns, s_off, port_level, nvpt;
+  std::vector<double> beta0;
+  double* s = nullptr;
+  int32_t* cut_off = nullptr;
+  int32_t* cut_edge = nullptr;
+  double* cut_w = nullptr;
+  double* vpts = nullptr;
+  int32_t* vpt_level = nullptr;
+  // per-call buffers
+  zd *q = nullptr, *phi = nullptr, *I = nullptr, *V = nullptr, *x = nullptr, *out = nullptr;
+  zd* Bexc = nullptr;  // (n, P) excitation columns
+  int* iters = nullptr;
+  int nt = 0, n = 0;
+  std::vector<void*> allocs;
+};
+
+extern "C" int m25_ports_create(m25_ctx* ctx, m25_geom* geom, const m25_port_desc* d, m25_ports** out) {
+  if (!ctx || !geom || !d || !out) {
+    set_error("m25_ports_create: null argument");
+    return M25_ERR_VALUE;
+  }
+  if (d->nport < 1 || d->nport > kMaxPorts || d->ngroup < 1 || d->ngroup > d->nport) {
+    set_error("m25_ports_create: 1..8 ports, 1..nport groups");
+    return M25_ERR_VALUE;
+  }
+  if (d->lossless) {
+    set_error("m25_ports_create: lossless stacks (bounded beta search) are not supported by this engine");
+    return M25_ERR_VALUE;
+  }
+  m25_ports* p = new m25_ports();
+  p->ctx = ctx;
+  p->P = d->nport;
+  p->ngroup = d->ngroup;
+  p->v_weight = d->v_weight;
+  p->nt = geom->nt;
+  p->n = geom->nb + geom->nv;
+  int tot_s = 0, tot_v = 0;
+  for (int i = 0; i < p->P; ++i) {
+    if (d->group_of[i] < 0 || d->group_of[i] >= d->ngroup || d->ns[i] < 2 || d->ns[i] > kMaxSamples ||
+        d->nvpt[i] != 8 * d->ns[i] || d->port_level[i] < 0 || d->port_level[i] >= geom->nlev) {
+      set_error("m25_ports_create: bad port description (2..128 cuts, 8 voltage points per cut)");
+      delete p;
+      return M25_ERR_VALUE;
+    }
+    p->group_of.push_back(d->group_of[i]);
+    p->ns.push_back(d->ns[i]);
+    p->s_off.push_back(tot_s);
+    p->port_level.push_back(d->port_level[i]);
+    p->nvpt.push_back(d->nvpt[i]);
+    tot_s += d->ns[i];
+    tot_v += d->nvpt[i];
+  }
+  for (int gi = 0; gi < d->ngroup; ++gi) p->beta0.push_back(d->beta0 ? d->beta0[gi] : 0.0);
+  p->ncut = tot_s;
+  p->nvpt_tot = tot_v;
+  int nent = d->cut_off[tot_s];
+  for (int i = 0; i < nent; ++i)
+    if (d->cut_edge[i] < 0 || d->cut_edge[i] >= p->n) {
+      set_error("m25_ports_create: cut edge out of range");
+      delete p;
+      return M25_ERR_VALUE;
+    }
+  std::vector<int32_t> vlev(tot_v);
+  {
+    int o = 0;
+    for (int i = 0; i < p->P; ++i)
+      for (int k = 0; k < d->nvpt[i]; ++k) vlev[o++] = d->port_level[i];
+  }
+  cudaStream_t st = ctx->stream;
+  int rc = M25_OK;
+#define TRY(x)         \
+  do {                 \
+    rc = (x);          \
+    if (rc) goto fail; \
+  } while (0)
+  TRY(alloc(p->allocs, (void**)&p->s, sizeof(double) * tot_s));
+  TRY(alloc(p->allocs, (void**)&p->cut_off, sizeof(int32_t) * (tot_s + 1)));
+  TRY(alloc(p->allocs, (void**)&p->cut_edge, sizeof(int32_t) * std::max(nent, 1)));
+  TRY(alloc(p->allocs, (void**)&p->cut_w, sizeof(double) * std::max(nent, 1)));
+  TRY(alloc(p->allocs, (void**)&p->vpts, sizeof(double) * 2 * tot_v));
+  TRY(alloc(p->allocs, (void**)&p->vpt_level, sizeof(int32_t) * tot_v));
+  TRY(alloc(p->allocs, (void**)&p->q, sizeof(zd) * (size_t)geom->nt * p->P));
+  TRY(alloc(p->allocs, (void**)&p->phi, sizeof(zd) * (size_t)tot_v * p->P));
+  TRY(alloc(p->allocs, (void**)&p->I, sizeof(zd) * (size_t)tot_s * p->P));
+  TRY(alloc(p->allocs, (void**)&p->V, sizeof(zd) * (size_t)tot_s * p->P));
+  TRY(alloc(p->allocs, (void**)&p->x, sizeof(zd) * (size_t)p->n * p->P));
+  TRY(alloc(p->allocs, (void**)&p->out, sizeof(zd) * (size_t)(4 * kMaxPorts * kMaxPorts + 8 * kMaxPorts)));
+  TRY(alloc(p->allocs, (void**)&p->iters, sizeof(int) * kMaxPorts));
+  TRY(alloc(p->allocs, (void**)&p->Bexc, sizeof(zd) * (size_t)p->n * p->P));
+  if (d->excitation) {
+    std::vector<zd> hb((size_t)p->n * p->P);
+    for (int i = 0; i < p->n; ++i)
+      for (int e = 0; e < p->P; ++e) hb[(size_t)i * p->P + e] = zd(d->excitation[(size_t)e * p->n + i], 0.0);
+    M25_CUDA(cudaMemcpy(p->Bexc, hb.data(), sizeof(zd) * hb.size(), cudaMemcpyHostToDevice));
+  } else {
+    M25_CUDA(cudaMemset(p->Bexc, 0, sizeof(zd) * (size_t)p->n * p->P));
+  }
+  M25_CUDA(cudaMemcpyAsync(p->s, d->s, sizeof(double) * tot_s, cudaMemcpyHostToDevice, st));
+  M25_CUDA(cudaMemcpyAsync(p->cut_off, d->cut_off, sizeof(int32_t) * (tot_s + 1), cudaMemcpyHostToDevice, st));
+  M25_CUDA(cudaMemcpyAsync(p->cut_edge, d->cut_edge, sizeof(int32_t) * nent, cudaMemcpyHostToDevice, st));
+  M25_CUDA(cudaMemcpyAsync(p->cut_w, d->cut_w, sizeof(double) * nent, cudaMemcpyHostToDevice, st));
+  M25_CUDA(cudaMemcpyAsync(p->vpts, d->vpts, sizeof(double) * 2 * tot_v, cudaMemcpyHostToDevice, st));
+  M25_CUDA(cudaMemcpyAsync(p->vpt_level, vlev.data(), sizeof(int32_t) * tot_v, cudaMemcpyHostToDevice, st));
+  M25_CUDA(cudaStreamSynchronize(st));
+  *out = p;
+  return M25_OK;
+fail:
+  free_all(p->allocs);
+  delete p;
+  return rc;
+#undef TRY
+}
+
+extern "C" int m25_ports_destroy(m25_ports* p) {
+  if (!p) return M25_OK;
+  cudaStreamSynchronize(p->ctx->stream);
+  free_all(p->allocs);
+  delete p;
+  return M25_OK;
+}
+
+extern "C" int m25_deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, const void* x, int where,
+                           const double* beta0, double* S, double* z0, double* gamma, double* z0_line, double* resid) {
+  if (!ctx || !geom || !gr || !p || !x) {
+    set_error("m25_deembed: null argument");
+    return M25_ERR_VALUE;
+  }
+  if (gr->nlev != geom->nlev) {
+    set_error("m25_deembed: Green's tables and mesh have different level counts");
+    return M25_ERR_VALUE;
+  }
+  cudaStream_t st = ctx->stream;
+  const int P = p->P, L = geom->nlev;
+  const zd* xd = static_cast<const zd*>(x);
+  if (where == M25_ON_HOST) {
+    M25_CUDA(cudaMemcpyAsync(p->x, x, sizeof(zd) * (size_t)p->n * P, cudaMemcpyHostToDevice, st));
+    xd = p->x;
+  }
+  StageTimer tm(ctx, ST_DEEMBED);
+  charges_kernel<<<(geom->nt + 127) / 128, 128, 0, st>>>(geom->nt, geom->nb, P, geom->td64, geom->tri_basis, xd,
+                                                         gr->omega, p->q);
+  if (geom->nv)
+    via_charges_kernel<<<(geom->nv + 63) / 64, 64, 0, st>>>(geom->nv, geom->nb, P, geom->seg_pad_off, geom->seg_pad,
+                                                            geom->seg_pad_w, geom->pad_tris, xd, gr->omega, p->q);
+  // W leading coefficients per pair
+  zd* cW = reinterpret_cast<zd*>(p->out) + 4 * kMaxPorts * kMaxPorts;
+  {
+    std::vector<zd> hc(L * L);
+    for (int i = 0; i < L * L; ++i) hc[i] = gr->lead_h[2 * L * L + i];
+    M25_CUDA(cudaMemcpyAsync(cW, hc.data(), sizeof(zd) * L * L, cudaMemcpyHostToDevice, st));
+  }
+  line_voltage_kernel<<<p->nvpt_tot, 256, 0, st>>>(geom->nt, P, L, p->vpts, p->vpt_level, geom->cen, geom->td64,
+                                                   geom->tri_layer, geom->level_z, gr->nrho, gr->rho,
+                                                   reinterpret_cast<const zd*>(gr->coef), cW, p->q, p->phi);
+  cuts_kernel<<<(p->ncut * P + 127) / 128, 128, 0, st>>>(p->ncut, P, p->cut_off, p->cut_edge, p->cut_w, xd, p->phi, 8,
+                                                         p->I, p->V);
+  FitArgs fa;
+  fa.P = P;
+  fa.ngroup = p->ngroup;
+  for (int i = 0; i < P; ++i) {
+    fa.group_of[i] = p->group_of[i];
+    fa.ns[i] = p->ns[i];
+    fa.s_off[i] = p->s_off[i];
+  }
+  for (int gi = 0; gi < p->ngroup; ++gi) fa.beta0[gi] = beta0 ? beta0[gi] : p->beta0[gi];
+  fa.v_weight = p->v_weight;
+  fa.s = p->s;
+  fa.I = p->I;
+  fa.V = p->V;
+  zd* o = reinterpret_cast<zd*>(p->out);
+  fa.A = o;
+  fa.B = o + kMaxPorts * kMaxPorts;
+  fa.S = o + 2 * kMaxPorts * kMaxPorts;
+  fa.gamma = o + 3 * kMaxPorts * kMaxPorts;
+  fa.zline = fa.gamma + kMaxPorts;
+  fa.resid = reinterpret_cast<double*>(fa.zline + kMaxPorts);
+  fa.z0 = fa.resid + kMaxPorts;
+  fa.iters = p->iters;
+  fit_kernel<<<1, 32 * p->ngroup, 0, st>>>(fa);
+  M25_CHECK_LAUNCH();
+  std::vector<zd> h(4 * kMaxPorts * kMaxPorts);
+  M25_CUDA(cudaMemcpyAsync(h.data(), p->out, sizeof(zd) * h.size(), cudaMemcpyDeviceToHost, st));
+  M25_CUDA(cudaStreamSynchronize(st));
+  const zd* hS = h.data() + 2 * kMaxPorts * kMaxPorts;
+  const zd* hg = h.data() + 3 * kMaxPorts * kMaxPorts;
+  const zd* hz = hg + kMaxPorts;
+  const double* hr = reinterpret_cast<const double*>(hz + kMaxPorts);
+  const double* hz0 = hr + kMaxPorts;
+  for (int i = 0; i < P; ++i) {
+    for (int j = 0; j < P; ++j) {
+      if (S) {
+        S[2 * (i * P + j)] = hS[i * P + j].re;
+        S[2 * (i * P + j) + 1] = hS[i * P + j].im;
+      }
+    }
+    if (gamma) { gamma[2 * i] = hg[i].re; gamma[2 * i + 1] = hg[i].im; }
+    if (z0_line) { z0_line[2 * i] = hz[i].re; z0_line[2 * i + 1] = hz[i].im; }
+    if (resid) resid[i] = hr[i];
+    if (z0) z0[i] = hz0[i];
+  }
+  return M25_OK;
+}
+
+extern "C" int m25_deembed_debug(m25_ctx* ctx, m25_ports* p, double* phi, double* q, double* I, double* V) {
+  if (!ctx || !p) {
+    set_error("m25_deembed_debug: null argument");
+    return M25_ERR_VALUE;
+  }
+  M25_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (phi) M25_CUDA(cudaMemcpy(phi, p->phi, sizeof(zd) * (size_t)p->nvpt_tot * p->P, cudaMemcpyDeviceToHost));
+  if (q) M25_CUDA(cudaMemcpy(q, p->q, sizeof(zd) * (size_t)p->nt * p->P, cudaMemcpyDeviceToHost));
+  if (I) M25_CUDA(cudaMemcpy(I, p->I, sizeof(zd) * (size_t)p->ncut * p->P, cudaMemcpyDeviceToHost));
+  if (V) M25_CUDA(cudaMemcpy(V, p->V, sizeof(zd) * (size_t)p->ncut * p->P, cudaMemcpyDeviceToHost));
+  return M25_OK;
+}
+
+extern "C" int m25_sweep_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, double zs_re, double zs_im,
+                               double zsv_re, double zsv_im, int precision, const double* beta0, double tol,
+                               int32_t max_iter, double* x_out, double* S, double* z0, double* gamma, double* z0_line,
+                               double* resid, int32_t* info) {
+  if (!ctx || !geom || !gr || !p) {
+    set_error("m25_sweep_point: null argument");
+    return M25_ERR_VALUE;
+  }
+  if (precision != M25_FP64 && precision != M25_MIXED) {
+    set_error("m25_sweep_point: precision must be M25_FP64 or M25_MIXED");
+    return M25_ERR_VALUE;
+  }
+  const int n = geom->nb + geom->nv, P = p->P;
+  const size_t esz = precision == M25_FP64 ? sizeof(zd) : sizeof(zf);
+  int rc;
+  if ((rc = ctx->Zsweep.ensure(esz * (size_t)n * n))) return rc;
+  if ((rc = ctx->Xsweep.ensure(sizeof(zd) * (size_t)n * P))) return rc;
+  if ((rc = m25_assemble(ctx, geom, gr, zs_re, zs_im, zsv_re, zsv_im, precision, ctx->Zsweep.p, n, M25_ON_DEVICE)))
+    return rc;
+  int32_t inf[2] = {0, 0};
+  if ((rc = m25_dense_solve(ctx, n, P, precision, ctx->Zsweep.p, p->Bexc, ctx->Xsweep.p, M25_ON_DEVICE, tol, max_iter,
+                            inf)))
+    return rc;
+  if (info) {
+    info[0] = inf[0];
+    info[1] = inf[1];
+  }
+  if ((rc = m25_deembed(ctx, geom, gr, p, ctx->Xsweep.p, M25_ON_DEVICE, beta0, S, z0, gamma, z0_line, resid)))
+    return rc;
+  if (x_out) {
+    M25_CUDA(cudaMemcpy(x_out, ctx->Xsweep.p, sizeof(zd) * (size_t)n * P, cudaMemcpyDeviceToHost));
+  }
+  return M25_OK;
+}

@@ -1,0 +1,505 @@
+// MPIE / RWG impedance fill (Engine/mom25d/solver.py:429-524 and the
+// compiled form of the same fill, Engine/mom25d/_fast.py:82-158):
+//
+//   Z_mn = jw mu0 <f_m, gA * f_n> + 1/(jw eps0) <div f_m, gV * div f_n> + Zs <f_m, f_n>
+//
+// Stage 1 (fill_tri_kernel): one CTA per test block of 32 Morton-ordered
+// triangles of one level, one warp lane per test triangle; the warps walk the
+// source triangles, so every lane of a warp sees the same source and the same
+// near/mid/far class (no divergence). Each (test, source) triangle pair gives
+// a 3x3 block of half-basis values, written to the scratch H laid out
+// [source half-basis][test half-basis slot] so the 32 lanes store one
+// contiguous run per source half-basis.
+// Stage 2 (gather_kernel): each RWG entry sums its 2 x 2 half-basis values
+// and the symmetrisation 0.5 (Z + Z^T) is applied, so every Z entry has a
+// single writer (no atomics).
+// Stage 3 (via_rows_kernel, via_block_kernel): rows / columns of the via
+// segment unknowns (Engine/mom25d/solver.py:527-566).
+#include <algorithm>
+#include <type_traits>
+#include <vector>
+
+#include "m25_internal.h"
+
+namespace m25 {
+
+template <class T>
+struct FillArgs {
+  int nt, nb, nlev, nblocks, n_src_chunk;
+  const TriData<T>* td;
+  const double* cen;
+  const int32_t* tri_layer;
+  const int32_t* block_tris;
+  const int32_t* block_level;
+  const int32_t* cls;
+  const T* stat;
+  const int32_t* pad_pos;
+  int nrho;
+  const T* rho;        // (nrho)
+  const T* coef;       // (L*L, nrho-1, 4, 3) complex: A, V, W
+  cx<T> lead[kMaxLevSq][2];  // cA, cV of pair (lt*L + ls)
+  T dz[kMaxLevSq];
+  cx<T> jwmu, inv_jwe, zs;
+  cx<T>* H;            // (3 nt, ldh)
+  int64_t ldh;
+  cx<T>* IVpad;        // (npad, nt)
+};
+
+// scipy PPoly interval: x[i] <= r < x[i+1], clamped to the end intervals.
+template <class T>
+__device__ __forceinline__ int find_interval(const T* __restrict__ x, int n, T r) {
+  if (r < x[1]) return 0;
+  if (r >= x[n - 2]) return n - 2;
+  int lo = 1, hi = n - 2;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (r < x[mid]) hi = mid; else lo = mid;
+  }
+  return lo;
+}
+
+// Smooth parts S_A, S_V at radius r from the shared-memory table of one pair:
+// sum_p c[3-p] (r - x_i)^p, the order PPoly evaluates.
+template <class T>
+__device__ __forceinline__ void spline_av(const T* __restrict__ xs, const T* __restrict__ tab, int n, T r,
+                                          cx<T>& sa, cx<T>& sv) {
+  int i = find_interval(xs, n, r);
+  T dx = r - xs[i];
+  const T* c = tab + (size_t)i * 16;  // [power 0..3][A re, A im, V re, V im], highest power first
+  T z = dx, z2 = dx * dx, z3 = z2 * dx;
+  sa.re = c[12] + c[8] * z + c[4] * z2 + c[0] * z3;
+  sa.im = c[13] + c[9] * z + c[5] * z2 + c[1] * z3;
+  sv.re = c[14] + c[10] * z + c[6] * z2 + c[2] * z3;
+  sv.im = c[15] + c[11] * z + c[7] * z2 + c[3] * z3;
+}
+
+template <class T, int NQ, bool NEAR>
+__device__ __forceinline__ void source_pass(const FillArgs<T>& a, const TriData<T>& S, T dcx, T dcy,
+                                            const T (&tq)[7][2], const T (&tw)[7], const T* xs, const T* tab,
+                                            cx<T> cA, cx<T> cV, T dz, const T* st, int lane, cx<T> (&Q)[3],
+                                            cx<T> (&Px)[3], cx<T> (&Py)[3], cx<T>& IV, const T (&tv)[3][2]) {
+  const T inv4pi = T(1.0 / (4.0 * kPi));
+  T sq[NQ][2], sw[NQ];
+#pragma unroll
+  for (int l = 0; l < NQ; ++l) {
+    if (NQ == 7) {
+      sq[l][0] = S.q7[l][0];
+      sq[l][1] = S.q7[l][1];
+      sw[l] = S.w7[l];
+    } else if (NQ == 3) {
+      sq[l][0] = S.q3[l][0];
+      sq[l][1] = S.q3[l][1];
+      sw[l] = S.w3[l];
+    } else {
+      sq[l][0] = T(0);
+      sq[l][1] = T(0);
+      sw[l] = S.area;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    cx<T> K0A, K1x, K1y, K0V;
+    if (NEAR) {
+      T s0 = st[(0 * 7 + k) * 32 + lane], s1x = st[(1 * 7 + k) * 32 + lane], s2y = st[(2 * 7 + k) * 32 + lane];
+      K0A = cA * s0;
+      K1x = cA * s1x;
+      K1y = cA * s2y;
+      K0V = cV * s0;
+    }
+    // test point relative to the source centroid
+    const T rx = dcx + tq[k][0], ry = dcy + tq[k][1];
+#pragma unroll
+    for (int l = 0; l < NQ; ++l) {
+      T ddx = rx - sq[l][0], ddy = ry - sq[l][1];
+      T R = sqrt(ddx * ddx + ddy * ddy);
+      cx<T> sa, sv;
+      spline_av(xs, tab, a.nrho, R, sa, sv);
+      if (!NEAR) {
+        T inv = inv4pi / (dz == T(0) ? R : sqrt(R * R + dz * dz));
+        sa += cA * inv;
+        sv += cV * inv;
+      }
+      cx<T> saw = sa * sw[l];
+      K0A += saw;
+      K1x += saw * sq[l][0];
+      K1y += saw * sq[l][1];
+      K0V += sv * sw[l];
+    }
+    const T wk = tw[k];
+    IV += K0V * wk;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      // w_k (r_k - a_i), lengths about the test centroid
+      T ax = wk * (tq[k][0] - tv[i][0]), ay = wk * (tq[k][1] - tv[i][1]);
+      Q[i] += K1x * ax + K1y * ay;
+      Px[i] += K0A * ax;
+      Py[i] += K0A * ay;
+    }
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int blk = blockIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int L = a.nlev;
+  const int lt = a.block_level[blk];
+  const int n = a.nrho;
+  // tables of the pairs (lt, ls): radii, then per source level (n-1) x 16 values [A, V]
+  T* xs = reinterpret_cast<T*>(smem_raw);
+  T* tabs = xs + ((n + 3) & ~3);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i] = a.rho[i];
+  for (int ls = 0; ls < L; ++ls) {
+    const cx<T>* src = reinterpret_cast<const cx<T>*>(a.coef) + (size_t)(lt * L + ls) * (n - 1) * 12;
+    T* dst = tabs + (size_t)ls * (n - 1) * 16;
+    for (int e = threadIdx.x; e < (n - 1) * 8; e += blockDim.x) {
+      int iv = e >> 3, r = e & 7, p = r >> 1, which = r & 1;  // power p, kernel A(0) / V(1)
+      cx<T> v = src[((size_t)iv * 4 + p) * 3 + which];
+      dst[(size_t)iv * 16 + p * 4 + which * 2] = v.re;
+      dst[(size_t)iv * 16 + p * 4 + which * 2 + 1] = v.im;
+    }
+  }
+  __syncthreads();
+
+  const int t = a.block_tris[blk * 32 + lane];
+  const bool active = t >= 0;
+  const int tt = active ? t : a.block_tris[blk * 32];
+  T tq[7][2], tw[7], tv[3][2], tcA[3], tcV[3];
+  {
+    const TriData<T>& A = a.td[tt];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      tq[k][0] = A.q7[k][0];
+      tq[k][1] = A.q7[k][1];
+      tw[k] = A.w7[k];
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      tv[i][0] = A.v[i][0];
+      tv[i][1] = A.v[i][1];
+      tcA[i] = A.cA[i];
+      tcV[i] = A.cV[i];
+    }
+  }
+  const double tcx = a.cen[2 * tt], tcy = a.cen[2 * tt + 1];
+  const int pad = active ? a.pad_pos[tt] : -1;
+  const int64_t col0 = (int64_t)(blk * 32 + lane) * 3;
+
+  const int s_begin = blockIdx.y * a.n_src_chunk;
+  const int s_end = min(a.nt, s_begin + a.n_src_chunk);
+  for (int s = s_begin + warp; s < s_end; s += nwarp) {
+    const int code = a.cls[(int64_t)blk * a.nt + s];
+    const int ls = a.tri_layer[s];
+    const TriData<T>& S = a.td[s];
+    const T dcx = T(tcx - a.cen[2 * s]), dcy = T(tcy - a.cen[2 * s + 1]);
+    const T* tab = tabs + (size_t)ls * (n - 1) * 16;
+    const cx<T> cA = a.lead[lt * L + ls][0], cV = a.lead[lt * L + ls][1];
+    const T dz = a.dz[lt * L + ls];
+    cx<T> Q[3], Px[3], Py[3], IV;
+    if (code >= 0) {
+      source_pass<T, 7, true>(a, S, dcx, dcy, tq, tw, xs, tab, cA, cV, dz, a.stat + (int64_t)code * 672, lane, Q, Px,
+                              Py, IV, tv);
+    } else if (code == -1) {
+      source_pass<T, 3, false>(a, S, dcx, dcy, tq, tw, xs, tab, cA, cV, dz, nullptr, lane, Q, Px, Py, IV, tv);
+    } else {
+      source_pass<T, 1, false>(a, S, dcx, dcy, tq, tw, xs, tab, cA, cV, dz, nullptr, lane, Q, Px, Py, IV, tv);
+    }
+    // IA[i][j] = Q_i - (b_j - c_s) . P_i ; vals = jw mu cA cA IA + inv_jwe cV cV IV
+    cx<T> out[3][3];
+    T scA[3], scV[3], bx[3], by[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      scA[j] = S.cA[j];
+      scV[j] = S.cV[j];
+      bx[j] = S.v[j][0];
+      by[j] = S.v[j][1];
+    }
+    const cx<T> ivt = a.inv_jwe * IV;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        cx<T> IA = Q[i] - (Px[i] * bx[j] + Py[i] * by[j]);
+        out[i][j] = a.jwmu * IA * (tcA[i] * scA[j]) + ivt * (tcV[i] * scV[j]);
+      }
+    if (active && s == t && (a.zs.re != T(0) || a.zs.im != T(0))) {
+      // conductor loss: Zs Int_T (r - a_i).(r - a_j) dS cA_i cA_j
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          T gsum = T(0);
+#pragma unroll
+          for (int k = 0; k < 7; ++k)
+            gsum += tw[k] * ((tq[k][0] - tv[i][0]) * (tq[k][0] - tv[j][0]) + (tq[k][1] - tv[i][1]) * (tq[k][1] - tv[j][1]));
+          out[i][j] += a.zs * (gsum * tcA[i] * tcA[j]);
+        }
+    }
+    if (active) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        cx<T>* row = a.H + (int64_t)(3 * s + j) * a.ldh + col0;
+        row[0] = out[0][j];
+        row[1] = out[1][j];
+        row[2] = out[2][j];
+      }
+      if (pad >= 0) a.IVpad[(int64_t)pad * a.nt + s] = IV;
+    }
+  }
+}
+
+// Z[m][n] = 0.5 (Zr[m][n] + Zr[n][m]), Zr[m][n] = sum over the two triangles
+// of m (test) and of n (source) of H[3 t_n + j_n][slot(t_m) * 3 + i_m].
+template <class T, class TO>
+__global__ void gather_kernel(int nb, const cx<T>* __restrict__ H, int64_t ldh, const int32_t* __restrict__ etri,
+                              const int32_t* __restrict__ eloc, const int32_t* __restrict__ tpos,
+                              cx<TO>* __restrict__ Z, int64_t ldz) {
+  int nn = blockIdx.x * blockDim.x + threadIdx.x;
+  int m = blockIdx.y;
+  if (nn >= nb) return;
+  int64_t rm[2], cm[2], rn[2], cn[2];
+#pragma unroll
+  for (int a = 0; a < 2; ++a) {
+    int tmi = etri[2 * m + a], lmi = eloc[2 * m + a];
+    int tni = etri[2 * nn + a], lni = eloc[2 * nn + a];
+    rm[a] = 3 * (int64_t)tmi + lmi;
+    cm[a] = 3 * (int64_t)tpos[tmi] + lmi;
+    rn[a] = 3 * (int64_t)tni + lni;
+    cn[a] = 3 * (int64_t)tpos[tni] + lni;
+  }
+  cx<T> s1, s2;
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      s1 += H[rn[b] * ldh + cm[a]];  // test m, source n
+      s2 += H[rm[a] * ldh + cn[b]];  // test n, source m
+    }
+  cx<T> z = (s1 + s2) * T(0.5);
+  Z[(int64_t)m * ldz + nn] = cx<TO>(z);
+}
+
+// Via rows: Zvb[k][n] = inv_jwe sum_pad D[pad][k] sum_{T of n} cV IV(pad, T)
+// (written to row nb+k and column nb+k).
+template <class T, class TO>
+__global__ void via_rows_kernel(int nb, int nv, int nt, const cx<T>* __restrict__ IVpad,
+                                const int32_t* __restrict__ seg_pad_off, const int32_t* __restrict__ seg_pad,
+                                const double* __restrict__ seg_pad_w, const int32_t* __restrict__ etri,
+                                const int32_t* __restrict__ eloc, const TriData<T>* __restrict__ td, cx<T> inv_jwe,
+                                cx<TO>* __restrict__ Z, int64_t ldz) {
+  int nn = blockIdx.x * blockDim.x + threadIdx.x;
+  int k = blockIdx.y;
+  if (nn >= nb || k >= nv) return;
+  int ta = etri[2 * nn], la = eloc[2 * nn], tb = etri[2 * nn + 1], lb = eloc[2 * nn + 1];
+  T ca = td[ta].cV[la], cb = td[tb].cV[lb];
+  cx<T> acc;
+  for (int e = seg_pad_off[k]; e < seg_pad_off[k + 1]; ++e) {
+    int p = seg_pad[e];
+    cx<T> y = IVpad[(int64_t)p * nt + ta] * ca + IVpad[(int64_t)p * nt + tb] * cb;
+    acc += y * T(seg_pad_w[e]);
+  }
+  cx<TO> z(inv_jwe * acc);
+  Z[(int64_t)(nb + k) * ldz + nn] = z;
+  Z[(int64_t)nn * ldz + nb + k] = z;
+}
+
+__device__ inline double filament_f(double s, double d) { return s * asinh(s / d) - sqrt(s * s + d * d); }
+
+// Grover's partial mutual inductance of parallel z filaments [a1,a2], [b1,b2]
+// at lateral distance d.
+__device__ inline double filament_mutual_z(double a1, double a2, double b1, double b2, double d) {
+  return kMu0 / (4.0 * kPi) *
+         (filament_f(a2 - b1, d) - filament_f(a2 - b2, d) - filament_f(a1 - b1, d) + filament_f(a1 - b2, d));
+}
+
+// Via-via block (Engine/mom25d/solver.py:527-566 with the open-section case
+// of via_impedance, 125-199): charge coupling through gV, removal of the
+// Im gV(0) part of the segment end charges, quasi-static inductance of the
+// segments and their ground images, via-wall loss.
+template <class T, class TO>
+__global__ void via_block_kernel(int nb, int nv, int nt, int L, const cx<T>* __restrict__ IVpad,
+                                 const int32_t* __restrict__ pad_tris, const int32_t* __restrict__ seg_pad_off,
+                                 const int32_t* __restrict__ seg_pad, const double* __restrict__ seg_pad_w,
+                                 const int32_t* __restrict__ seg_end_lev, const double* __restrict__ seg_span,
+                                 const double* __restrict__ seg_xy, const double* __restrict__ seg_drill,
+                                 const double* __restrict__ im_gv0, double omega, zd zsv, double h_sec,
+                                 cx<TO>* __restrict__ Z, int64_t ldz) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int m = blockIdx.y;
+  if (k >= nv || m >= nv) return;
+  const zd inv_jwe = zd(1.0) / zd(0.0, omega * eps0());
+  // charge part, both orders (the matrix is symmetrised)
+  zd acc[2];
+  for (int o = 0; o < 2; ++o) {
+    int r = o == 0 ? k : m, c = o == 0 ? m : k;
+    zd s(0.0);
+    for (int e = seg_pad_off[r]; e < seg_pad_off[r + 1]; ++e)
+      for (int f = seg_pad_off[c]; f < seg_pad_off[c + 1]; ++f) {
+        cx<T> iv = IVpad[(int64_t)seg_pad[e] * nt + pad_tris[seg_pad[f]]];
+        s += zd(double(iv.re), double(iv.im)) * (seg_pad_w[e] * seg_pad_w[f]);
+      }
+    // Im gV(0) of the end charges
+    double im = 0.0;
+    for (int a = 0; a < 2; ++a)
+      for (int b = 0; b < 2; ++b) {
+        int la = seg_end_lev[2 * r + a], lb = seg_end_lev[2 * c + b];
+        if (la < 0 || lb < 0) continue;
+        double sa = a == 0 ? 1.0 : -1.0, sb = b == 0 ? 1.0 : -1.0;
+        im += sa * sb * im_gv0[la * L + lb];
+      }
+    acc[o] = inv_jwe * s - inv_jwe * zd(0.0, im);
+  }
+  zd z = (acc[0] + acc[1]) * 0.5;
+  // inductance of the vertical currents (+ images in the ground plane)
+  double dx = seg_xy[2 * k] - seg_xy[2 * m], dy = seg_xy[2 * k + 1] - seg_xy[2 * m + 1];
+  double rk = 0.5 * seg_drill[k], rm = 0.5 * seg_drill[m];
+  double rho = sqrt(dx * dx + dy * dy);
+  if (rho < 1e-12) rho = fmin(rk, rm);
+  if (k == m) rho = rk;
+  double p1 = fmin(fmax(seg_span[2 * k], 0.0), h_sec), p2 = fmin(fmax(seg_span[2 * k + 1], 0.0), h_sec);
+  double q1 = fmin(fmax(seg_span[2 * m], 0.0), h_sec), q2 = fmin(fmax(seg_span[2 * m + 1], 0.0), h_sec);
+  double Lkm = filament_mutual_z(p1, p2, q1, q2, rho) + filament_mutual_z(p1, p2, -q2, -q1, rho);
+  double Lmk = filament_mutual_z(q1, q2, p1, p2, rho) + filament_mutual_z(q1, q2, -p2, -p1, rho);
+  z += zd(0.0, omega) * (0.5 * (Lkm + Lmk));
+  if (k == m && (zsv.re != 0.0 || zsv.im != 0.0)) {
+    double len = seg_span[2 * k + 1] - seg_span[2 * k];
+    z += zsv * (len / (kPi * seg_drill[k]));
+  }
+  Z[(int64_t)(nb + k) * ldz + nb + m] = cx<TO>(cx<T>(T(z.re), T(z.im)));
+}
+
+// Im gV at rho0 (0 between levels, 1e-6 h on a level) for every level pair.
+__global__ void im_gv0_kernel(int L, int nrho, const double* __restrict__ rho, const zd* __restrict__ coef,
+                              const zd* __restrict__ lead, const double* __restrict__ dzp, double h,
+                              double* __restrict__ out) {
+  int p = threadIdx.x;
+  if (p >= L * L) return;
+  double dz = dzp[p];
+  double r = dz != 0.0 ? 0.0 : 1e-6 * h;
+  int i = find_interval(rho, nrho, r);
+  double dx = r - rho[i];
+  const zd* c = coef + ((size_t)p * (nrho - 1) + i) * 12;
+  zd v = c[3 * 3 + 1] + c[2 * 3 + 1] * dx + c[1 * 3 + 1] * (dx * dx) + c[0 * 3 + 1] * (dx * dx * dx);
+  double R = sqrt(r * r + dz * dz);
+  zd g = lead[p] / (4.0 * kPi * R) + v;
+  out[p] = g.im;
+}
+
+// Stage 1 + 2 + 3 on the context's stream; Z is host or device memory.
+template <class T>
+int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, void* Zout, int64_t ldz, int where) {
+  cudaStream_t st = ctx->stream;
+  const int nt = geom->nt, nb = geom->nb, nv = geom->nv, L = geom->nlev, n = nb + nv;
+  const int nrho = gr->nrho;
+  const int64_t ldh = (int64_t)geom->nblocks * 96;
+  int rc;
+  if ((rc = ctx->H.ensure(sizeof(cx<T>) * (size_t)3 * nt * ldh + sizeof(cx<T>) * (size_t)std::max(geom->npad, 1) * nt +
+                          sizeof(double) * 16)))
+    return rc;
+  cx<T>* H = ctx->H.as<cx<T>>();
+  cx<T>* IVpad = H + (size_t)3 * nt * ldh;
+  double* imgv = reinterpret_cast<double*>(IVpad + (size_t)std::max(geom->npad, 1) * nt);
+  cx<T>* Z = static_cast<cx<T>*>(Zout);
+  int64_t ldzd = ldz;
+  if (where == M25_ON_HOST) {
+    if ((rc = ctx->Zw.ensure(sizeof(cx<T>) * (size_t)n * n))) return rc;
+    Z = ctx->Zw.as<cx<T>>();
+    ldzd = n;
+  }
+  FillArgs<T> a;
+  a.nt = nt;
+  a.nb = nb;
+  a.nlev = L;
+  a.nblocks = geom->nblocks;
+  a.td = std::is_same<T, double>::value ? reinterpret_cast<const TriData<T>*>(geom->td64)
+                                        : reinterpret_cast<const TriData<T>*>(geom->td32);
+  a.cen = geom->cen;
+  a.tri_layer = geom->tri_layer;
+  a.block_tris = geom->block_tris;
+  a.block_level = geom->block_level;
+  a.cls = geom->cls;
+  a.stat = std::is_same<T, double>::value ? reinterpret_cast<const T*>(geom->stat64)
+                                          : reinterpret_cast<const T*>(geom->stat32);
+  a.pad_pos = geom->pad_pos;
+  a.nrho = nrho;
+  a.rho = std::is_same<T, double>::value ? reinterpret_cast<const T*>(gr->rho) : reinterpret_cast<const T*>(gr->rho32);
+  a.coef = std::is_same<T, double>::value ? reinterpret_cast<const T*>(gr->coef)
+                                          : reinterpret_cast<const T*>(gr->coef32);
+  for (int p = 0; p < L * L; ++p) {
+    zd ca = gr->lead_h[0 * L * L + p], cv = gr->lead_h[1 * L * L + p];
+    a.lead[p][0] = cx<T>(T(ca.re), T(ca.im));
+    a.lead[p][1] = cx<T>(T(cv.re), T(cv.im));
+    a.dz[p] = T(gr->dz_h[p]);
+  }
+  const double omega = gr->omega;
+  zd jwmu(0.0, omega * kMu0);
+  zd inv_jwe = zd(1.0) / zd(0.0, omega * eps0());
+  a.jwmu = cx<T>(T(jwmu.re), T(jwmu.im));
+  a.inv_jwe = cx<T>(T(inv_jwe.re), T(inv_jwe.im));
+  a.zs = cx<T>(T(zs.re), T(zs.im));
+  a.H = H;
+  a.ldh = ldh;
+  a.IVpad = IVpad;
+  size_t smem = sizeof(T) * (((nrho + 3) & ~3) + (size_t)L * (nrho - 1) * 16);
+  if (smem > 220 * 1024) {
+    set_error("m25_assemble: Green's tables too large for shared memory (reduce rho_max or levels)");
+    return M25_ERR_VALUE;
+  }
+  M25_CUDA(cudaFuncSetAttribute(fill_tri_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 1;
+  M25_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fill_tri_kernel<T>, 256, smem));
+  int want = std::max(1, 2 * occ * ctx->num_sms);
+  int nchunk = std::max(1, std::min((want + geom->nblocks - 1) / geom->nblocks, (nt + 7) / 8));
+  a.n_src_chunk = (nt + nchunk - 1) / nchunk;
+  nchunk = (nt + a.n_src_chunk - 1) / a.n_src_chunk;
+  if (nv) M25_CUDA(cudaMemsetAsync(IVpad, 0, sizeof(cx<T>) * (size_t)geom->npad * nt, st));
+  {
+    StageTimer tm(ctx, ST_FILL);
+    fill_tri_kernel<T><<<dim3(geom->nblocks, nchunk), 256, smem, st>>>(a);
+  }
+  M25_CHECK_LAUNCH();
+  {
+  StageTimer tm(ctx, ST_GATHER);
+  gather_kernel<T, T><<<dim3((nb + 127) / 128, nb), 128, 0, st>>>(nb, H, ldh, geom->edge_tri, geom->edge_loc,
+                                                                 geom->tpos, Z, ldzd);
+  }
+  M25_CHECK_LAUNCH();
+  if (nv) {
+    zd* lead_dev = reinterpret_cast<zd*>(imgv + 9);  // unused slot guard
+    (void)lead_dev;
+    // Im gV(rho0) per level pair from the double tables
+    std::vector<zd> hv(L * L);
+    std::vector<double> hdz(L * L);
+    for (int p = 0; p < L * L; ++p) {
+      hv[p] = gr->lead_h[1 * L * L + p];
+      hdz[p] = gr->dz_h[p];
+    }
+    if ((rc = ctx->Dw.ensure(sizeof(zd) * 2 * kMaxLevSq))) return rc;
+    zd* dv = ctx->Dw.as<zd>();
+    double* ddz = reinterpret_cast<double*>(dv + kMaxLevSq);
+    M25_CUDA(cudaMemcpyAsync(dv, hv.data(), sizeof(zd) * L * L, cudaMemcpyHostToDevice, st));
+    M25_CUDA(cudaMemcpyAsync(ddz, hdz.data(), sizeof(double) * L * L, cudaMemcpyHostToDevice, st));
+    StageTimer tm(ctx, ST_VIA);
+    im_gv0_kernel<<<1, 32, 0, st>>>(L, nrho, gr->rho, reinterpret_cast<const zd*>(gr->coef), dv, ddz, gr->stack_h,
+                                    imgv);
+    via_rows_kernel<T, T><<<dim3((nb + 127) / 128, nv), 128, 0, st>>>(
+        nb, nv, nt, IVpad, geom->seg_pad_off, geom->seg_pad, geom->seg_pad_w, geom->edge_tri, geom->edge_loc, a.td,
+        a.inv_jwe, Z, ldzd);
+    via_block_kernel<T, T><<<dim3((nv + 31) / 32, nv), 32, 0, st>>>(
+        nb, nv, nt, L, IVpad, geom->pad_tris, geom->seg_pad_off, geom->seg_pad, geom->seg_pad_w, geom->seg_end_lev,
+        geom->seg_span, geom->seg_xy, geom->seg_drill, imgv, omega, zsv, gr->stack_h, Z, ldzd);
+    M25_CHECK_LAUNCH();
+  }
+  if (where == M25_ON_HOST) {
+    M25_CUDA(cudaMemcpy2DAsync(Zout, sizeof(cx<T>) * ldz, Z, sizeof(cx<T>) * n, sizeof(cx<T>) * n, n,
+                               cudaMemcpyDeviceToHost, st));
+    M25_CUDA(cudaStreamSynchronize(st));
+  }
+  return M25_OK;
+}
+
+template int fill_driver<double>(m25_ctx*, m25_geom*, m25_greens*, zd, zd, void*, int64_t, int);
+template int fill_driver<float>(m25_ctx*, m25_geom*, m25_greens*, zd, zd, void*, int64_t, int);
+
+}  // namespace m25

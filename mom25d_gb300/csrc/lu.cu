@@ -1,0 +1,657 @@
+// Dense complex LU with partial pivoting and the triangular solves, the
+// GPU replacement of mom25d's _dense_solve (Engine/mom25d/solver.py:11-23,
+// LAPACK zgetrf / zgetrs through scipy).
+//
+// Right-looking blocked factorisation of a row-major matrix, per panel of
+// nb columns:
+//   panel_kernel   cooperative grid: each CTA keeps a slice of the panel
+//                  rows in shared memory; one bounded grid barrier per
+//                  column (pivot search |re| + |im| as izamax, swap, scale,
+//                  rank-1 update of the panel)
+//   laswp_kernel   the panel's row interchanges on the other columns
+//   trsm_kernel    U12 = L11^-1 A12
+//   gemm_kernel    A22 -= L21 U12 (SIMT), or the tcgen05 tensor-core path
+//                  for complex64 (lu_tc.cu)
+// Solve: permutation, blocked forward / backward substitution. The mixed
+// path refines in fp64: r = B - Z X, X += LU32^-1 r.
+#include <algorithm>
+#include <vector>
+
+#include "m25_internal.h"
+
+namespace m25 {
+
+constexpr long long kBarrierSpinLimit = 1LL << 25;  // ~1 s of polling, then give up
+
+// Grid-wide barrier for a cooperative launch. Every wait is bounded: on
+// timeout the CTA raises *err and the caller returns.
+__device__ inline bool grid_sync(unsigned* count, unsigned* gen, unsigned nblocks, int* err) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* vgen = gen;
+    unsigned g0 = *vgen;
+    __threadfence();
+    unsigned arrived = atomicAdd(count, 1u);
+    if (arrived == nblocks - 1) {
+      atomicExch(count, 0u);
+      __threadfence();
+      atomicAdd(gen, 1u);
+    } else {
+      long long it = 0;
+      while (*vgen == g0) {
+        if (++it > kBarrierSpinLimit || *(volatile int*)err) {
+          atomicExch(err, 1);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *(volatile int*)err == 0;
+}
+
+template <class T>
+struct PanelArgs {
+  cx<T>* A;
+  int64_t lda;
+  int n, k0, nb, rows_per_cta;
+  int32_t* ipiv;      // absolute pivot row per factored row
+  cx<T>* cand;        // (2, G, nb) candidate pivot rows
+  T* candval;         // (2, G)
+  int* candidx;       // (2, G)
+  cx<T>* rowj;        // (2, nb) row k0+j before the swap
+  unsigned* bar;      // count, generation
+  int* err;           // barrier timeout
+  int* info;          // first zero pivot (1-based), 0 if none
+};
+
+template <class T>
+__global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int G = gridDim.x, g = blockIdx.x, nb = a.nb;
+  const int r0 = a.k0 + g * a.rows_per_cta;
+  const int r1 = min(a.n, r0 + a.rows_per_cta);
+  const int R = max(0, r1 - r0);
+  cx<T>* P = reinterpret_cast<cx<T>*>(smem_raw);      // (rows_per_cta, nb)
+  cx<T>* urow = P + (size_t)a.rows_per_cta * nb;        // (nb)
+  __shared__ T red_v[8];
+  __shared__ int red_i[8];
+  __shared__ int piv_sh;
+  for (int e = threadIdx.x; e < R * nb; e += blockDim.x) {
+    int r = e / nb, c = e % nb;
+    P[e] = a.A[(int64_t)(r0 + r) * a.lda + a.k0 + c];
+  }
+  __syncthreads();
+  for (int j = 0; j < nb; ++j) {
+    const int row_j = a.k0 + j;
+    const int par = j & 1;
+    // local pivot candidate: max |re|+|im|, first index on ties
+    T best = T(-1);
+    int bi = -1;
+    for (int r = threadIdx.x; r < R; r += blockDim.x) {
+      if (r0 + r < row_j) continue;
+      T v = cabs1(P[r * nb + j]);
+      if (v > best) {
+        best = v;
+        bi = r0 + r;
+      }
+    }
+    for (int o = 16; o; o >>= 1) {
+      T ov = __shfl_down_sync(0xffffffffu, best, o);
+      int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      if (oi >= 0 && (ov > best || (ov == best && (bi < 0 || oi < bi)))) {
+        best = ov;
+        bi = oi;
+      }
+    }
+    if ((threadIdx.x & 31) == 0) {
+      red_v[threadIdx.x >> 5] = best;
+      red_i[threadIdx.x >> 5] = bi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T bv = T(-1);
+      int bidx = -1;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        int oi = red_i[w];
+        T ov = red_v[w];
+        if (oi >= 0 && (ov > bv || (ov == bv && (bidx < 0 || oi < bidx)))) {
+          bv = ov;
+          bidx = oi;
+        }
+      }
+      a.candval[par * G + g] = bv;
+      a.candidx[par * G + g] = bidx;
+      piv_sh = bidx;
+    }
+    __syncthreads();
+    {
+      int bidx = piv_sh;
+      if (bidx >= 0)
+        for (int c = threadIdx.x; c < nb; c += blockDim.x)
+          a.cand[((size_t)par * G + g) * nb + c] = P[(bidx - r0) * nb + c];
+      if (row_j >= r0 && row_j < r1)
+        for (int c = threadIdx.x; c < nb; c += blockDim.x) a.rowj[par * nb + c] = P[(row_j - r0) * nb + c];
+    }
+    if (!grid_sync(a.bar, a.bar + 1, G, a.err)) return;
+    // global pivot
+    if (threadIdx.x == 0) {
+      T bv = T(-1);
+      int bidx = -1, bg = -1;
+      for (int q = 0; q < G; ++q) {
+        int oi = *(volatile int*)&a.candidx[par * G + q];
+        T ov = *(volatile T*)&a.candval[par * G + q];
+        if (oi >= 0 && (ov > bv || (ov == bv && (bidx < 0 || oi < bidx)))) {
+          bv = ov;
+          bidx = oi;
+          bg = q;
+        }
+      }
+      if (bidx < 0 || bv == T(0)) {
+        if (g == 0 && *a.info == 0) *a.info = row_j + 1;
+        bidx = row_j;
+        bg = -1;
+      }
+      piv_sh = bidx;
+      red_i[0] = bg;
+      if (g == 0) a.ipiv[row_j] = bidx;
+    }
+    __syncthreads();
+    const int p = piv_sh, pg = red_i[0];
+    for (int c = threadIdx.x; c < nb; c += blockDim.x) {
+      if (pg >= 0) {
+        volatile cx<T>* src = &a.cand[((size_t)par * G + pg) * nb + c];
+        urow[c] = cx<T>(src->re, src->im);
+      } else if (row_j >= r0 && row_j < r1) {
+        urow[c] = P[(row_j - r0) * nb + c];
+      }
+    }
+    __syncthreads();
+    if (pg < 0 && !(row_j >= r0 && row_j < r1)) {
+      // zero pivot owned elsewhere: take the row from the published copy
+      for (int c = threadIdx.x; c < nb; c += blockDim.x) {
+        volatile cx<T>* src = &a.rowj[par * nb + c];
+        urow[c] = cx<T>(src->re, src->im);
+      }
+      __syncthreads();
+    }
+    if (p != row_j) {
+      if (p >= r0 && p < r1)
+        for (int c = threadIdx.x; c < nb; c += blockDim.x) {
+          volatile cx<T>* src = &a.rowj[par * nb + c];
+          P[(p - r0) * nb + c] = cx<T>(src->re, src->im);
+        }
+      if (row_j >= r0 && row_j < r1)
+        for (int c = threadIdx.x; c < nb; c += blockDim.x) P[(row_j - r0) * nb + c] = urow[c];
+    }
+    __syncthreads();
+    const cx<T> piv = urow[j];
+    const bool zero = piv.re == T(0) && piv.im == T(0);
+    // multipliers, then the rank-1 update of the panel's remaining columns
+    if (!zero)
+      for (int r = threadIdx.x; r < R; r += blockDim.x)
+        if (r0 + r > row_j) P[r * nb + j] = P[r * nb + j] / piv;
+    __syncthreads();
+    const int w = nb - j - 1;
+    if (w > 0)
+      for (int e = threadIdx.x; e < R * w; e += blockDim.x) {
+        int r = e / w, c = j + 1 + e % w;
+        if (r0 + r > row_j) P[r * nb + c] -= P[r * nb + j] * urow[c];
+      }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < R * nb; e += blockDim.x) {
+    int r = e / nb, c = e % nb;
+    a.A[(int64_t)(r0 + r) * a.lda + a.k0 + c] = P[e];
+  }
+}
+
+// Row interchanges of rows k0..k0+nb-1 applied to the columns outside the panel.
+template <class T>
+__global__ void laswp_kernel(cx<T>* A, int64_t lda, int n, int k0, int nb, const int32_t* __restrict__ ipiv) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n || (c >= k0 && c < k0 + nb)) return;
+  for (int j = 0; j < nb; ++j) {
+    int r = k0 + j, p = ipiv[r];
+    if (p != r) {
+      cx<T> t = A[(int64_t)r * lda + c];
+      A[(int64_t)r * lda + c] = A[(int64_t)p * lda + c];
+      A[(int64_t)p * lda + c] = t;
+    }
+  }
+}
+
+// U12 = L11^-1 A12 for a column chunk of 32 per CTA (L11 unit lower).
+template <class T>
+__global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, int64_t lda, int n, int k0, int nb) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<T>* Ls = reinterpret_cast<cx<T>*>(smem_raw);  // (nb, nb)
+  cx<T>* X = Ls + (size_t)nb * nb;                  // (nb, 32)
+  const int c0 = k0 + nb + blockIdx.x * 32;
+  const int cw = min(32, n - c0);
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    int r = e / nb, c = e % nb;
+    Ls[e] = A[(int64_t)(k0 + r) * lda + k0 + c];
+  }
+  for (int e = threadIdx.x; e < nb * 32; e += blockDim.x) {
+    int r = e >> 5, c = e & 31;
+    X[e] = c < cw ? A[(int64_t)(k0 + r) * lda + c0 + c] : cx<T>();
+  }
+  __syncthreads();
+  for (int t = 0; t < nb - 1; ++t) {
+    for (int e = threadIdx.x; e < (nb - 1 - t) * 32; e += blockDim.x) {
+      int r = t + 1 + (e >> 5), c = e & 31;
+      X[r * 32 + c] -= Ls[r * nb + t] * X[t * 32 + c];
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < nb * 32; e += blockDim.x) {
+    int r = e >> 5, c = e & 31;
+    if (c < cw) A[(int64_t)(k0 + r) * lda + c0 + c] = X[e];
+  }
+}
+
+// C[r][c] -= sum_t Lp[r][t] Up[t][c] over rows / cols >= off, t < nb:
+// 64 x 64 tile per CTA, 4 x 4 complex outputs per thread.
+template <class T>
+__global__ void __launch_bounds__(256) gemm_kernel(cx<T>* A, int64_t lda, int n, int k0, int nb) {
+  const int off = k0 + nb;
+  const int row0 = off + blockIdx.y * 64, col0 = off + blockIdx.x * 64;
+  __shared__ cx<T> As[16][64 + 1];
+  __shared__ cx<T> Bs[16][64];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  cx<T> acc[4][4];
+  for (int t0 = 0; t0 < nb; t0 += 16) {
+    for (int e = threadIdx.x; e < 16 * 64; e += 256) {
+      int r = e >> 4, t = e & 15;  // As[t][r] = L[row0 + r][k0 + t0 + t]
+      int gr = row0 + r, gt = t0 + t;
+      As[t][r] = (gr < n && gt < nb) ? A[(int64_t)gr * lda + k0 + gt] : cx<T>();
+      int t2 = e >> 6, c = e & 63;  // Bs[t][c] = U[k0 + t0 + t][col0 + c]
+      int gc = col0 + c, gt2 = t0 + t2;
+      Bs[t2][c] = (gc < n && gt2 < nb) ? A[(int64_t)(k0 + gt2) * lda + gc] : cx<T>();
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int t = 0; t < 16; ++t) {
+      cx<T> a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[t][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[t][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          acc[i][j].re += a[i].re * b[j].re - a[i].im * b[j].im;
+          acc[i][j].im += a[i].re * b[j].im + a[i].im * b[j].re;
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int r = row0 + ty + 16 * i, c = col0 + tx + 16 * j;
+      if (r < n && c < n) A[(int64_t)r * lda + c] -= acc[i][j];
+    }
+}
+
+// perm from the interchange list (sequential in shared memory), then the
+// gather Bp[i] = B[perm[i]].
+template <class T>
+__global__ void permute_kernel(int n, int nrhs, const int32_t* __restrict__ ipiv, const cx<T>* __restrict__ B,
+                               cx<T>* __restrict__ Bp) {
+  extern __shared__ int perm[];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = i;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int i = 0; i < n; ++i) {
+      int p = ipiv[i];
+      if (p != i && p >= 0 && p < n) {
+        int t = perm[i];
+        perm[i] = perm[p];
+        perm[p] = t;
+      }
+    }
+  __syncthreads();
+  for (int e = threadIdx.x; e < n * nrhs; e += blockDim.x) {
+    int i = e / nrhs, c = e % nrhs;
+    Bp[e] = B[(int64_t)perm[i] * nrhs + c];
+  }
+}
+
+// Triangular solve of one diagonal block (rows b0..b0+bs-1) in one CTA;
+// lower: unit diagonal, forward; upper: backward with the diagonal.
+template <class T>
+__global__ void trsv_block_kernel(const cx<T>* __restrict__ A, int64_t lda, int b0, int bs, int nrhs, int upper,
+                                  cx<T>* __restrict__ X) {
+  __shared__ cx<T> xs[64][8];
+  for (int e = threadIdx.x; e < bs * nrhs; e += blockDim.x) xs[e / nrhs][e % nrhs] = X[(int64_t)(b0 + e / nrhs) * nrhs + e % nrhs];
+  __syncthreads();
+  if (!upper) {
+    for (int t = 0; t < bs; ++t) {
+      for (int e = threadIdx.x; e < (bs - 1 - t) * nrhs; e += blockDim.x) {
+        int r = t + 1 + e / nrhs, c = e % nrhs;
+        xs[r][c] -= A[(int64_t)(b0 + r) * lda + b0 + t] * xs[t][c];
+      }
+      __syncthreads();
+    }
+  } else {
+    for (int t = bs - 1; t >= 0; --t) {
+      if (threadIdx.x < nrhs) xs[t][threadIdx.x] = xs[t][threadIdx.x] / A[(int64_t)(b0 + t) * lda + b0 + t];
+      __syncthreads();
+      for (int e = threadIdx.x; e < t * nrhs; e += blockDim.x) {
+        int r = e / nrhs, c = e % nrhs;
+        xs[r][c] -= A[(int64_t)(b0 + r) * lda + b0 + t] * xs[t][c];
+      }
+      __syncthreads();
+    }
+  }
+  for (int e = threadIdx.x; e < bs * nrhs; e += blockDim.x) X[(int64_t)(b0 + e / nrhs) * nrhs + e % nrhs] = xs[e / nrhs][e % nrhs];
+}
+
+// X[r] -= A[r][b0:b0+bs] X[b0:b0+bs] for the rows r in [r_lo, r_hi): one warp per row.
+template <class T>
+__global__ void trsv_update_kernel(const cx<T>* __restrict__ A, int64_t lda, int b0, int bs, int nrhs, int r_lo,
+                                   int r_hi, cx<T>* __restrict__ X) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  int r = r_lo + warp;
+  if (r >= r_hi) return;
+  cx<T> acc[8];
+  for (int t = lane; t < bs; t += 32) {
+    cx<T> l = A[(int64_t)r * lda + b0 + t];
+    for (int c = 0; c < nrhs; ++c) acc[c] += l * X[(int64_t)(b0 + t) * nrhs + c];
+  }
+  for (int c = 0; c < nrhs; ++c) {
+    T re = acc[c].re, im = acc[c].im;
+    for (int o = 16; o; o >>= 1) {
+      re += __shfl_down_sync(0xffffffffu, re, o);
+      im += __shfl_down_sync(0xffffffffu, im, o);
+    }
+    if (lane == 0) X[(int64_t)r * nrhs + c] -= cx<T>(re, im);
+  }
+}
+
+// r = B - Z X in fp64 (Z complex128 or complex64); one warp per row; also
+// the max-abs of r per row for the stopping test.
+template <class TZ>
+__global__ void residual_kernel(int n, int nrhs, const cx<TZ>* __restrict__ Z, int64_t ldz,
+                                const zd* __restrict__ B, const zd* __restrict__ X, zd* __restrict__ Rr,
+                                double* __restrict__ rmax) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  zd acc[8];
+  for (int t = lane; t < n; t += 32) {
+    cx<TZ> zz = Z[(int64_t)warp * ldz + t];
+    zd z(double(zz.re), double(zz.im));
+    for (int c = 0; c < nrhs; ++c) acc[c] += z * X[(int64_t)t * nrhs + c];
+  }
+  double m = 0;
+  for (int c = 0; c < nrhs; ++c) {
+    double re = acc[c].re, im = acc[c].im;
+    for (int o = 16; o; o >>= 1) {
+      re += __shfl_down_sync(0xffffffffu, re, o);
+      im += __shfl_down_sync(0xffffffffu, im, o);
+    }
+    if (lane == 0) {
+      zd r = B[(int64_t)warp * nrhs + c] - zd(re, im);
+      Rr[(int64_t)warp * nrhs + c] = r;
+      m = fmax(m, cabs1(r));
+    }
+  }
+  if (lane == 0) rmax[warp] = m;
+}
+
+__global__ void cast_z64_to_z32(const zd* __restrict__ a, int64_t lda, zf* __restrict__ b, int64_t ldb, int n,
+                                int m) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)n * m) return;
+  int64_t r = e / m, c = e % m;
+  zd v = a[r * lda + c];
+  b[r * ldb + c] = zf(float(v.re), float(v.im));
+}
+
+__global__ void scale_to_z32(int64_t n, const zd* __restrict__ r, double s, zf* __restrict__ o) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) o[e] = zf(float(r[e].re * s), float(r[e].im * s));
+}
+
+__global__ void axpy_z32(int64_t n, const zf* __restrict__ d, double s, zd* __restrict__ x) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) x[e] += zd(double(d[e].re) * s, double(d[e].im) * s);
+}
+
+__global__ void max_reduce(int n, const double* __restrict__ v, double* __restrict__ out) {
+  __shared__ double sh[32];
+  double m = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, v[i]);
+  for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, sh[w]);
+    *out = r;
+  }
+}
+
+// ----------------------------------------------------------------- drivers
+int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int nb);  // lu_tc.cu
+bool lu_tc_available();
+
+template <class T>
+int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb, bool use_tc, int* info_host) {
+  cudaStream_t st = ctx->stream;
+  // panel workspace
+  int bps_max = 0;
+  size_t panel_smem = 0;
+  int G = 0, rows = 0;
+  const size_t extra = (size_t)nb * sizeof(cx<T>);
+  // pick the widest grid whose slices fit: rows_per_cta = ceil(m / G)
+  auto fits = [&](int g, int m, size_t& smem) {
+    int rpc = (m + g - 1) / g;
+    smem = (size_t)rpc * nb * sizeof(cx<T>) + extra;
+    return smem <= 200 * 1024;
+  };
+  M25_CUDA(cudaFuncSetAttribute(panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+  {
+    size_t smem_t = (size_t)nb * nb * sizeof(cx<T>) + (size_t)nb * 32 * sizeof(cx<T>);
+    M25_CUDA(cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
+  }
+  (void)bps_max;
+  (void)rows;
+  int Gmax = 4 * ctx->num_sms;
+  int rc = ctx->scratch.ensure(sizeof(cx<T>) * 2 * (size_t)Gmax * nb + sizeof(T) * 2 * Gmax + sizeof(int) * 2 * Gmax +
+                               sizeof(cx<T>) * 2 * nb + 64);
+  if (rc) return rc;
+  char* base = ctx->scratch.as<char>();
+  unsigned* bar = reinterpret_cast<unsigned*>(base);
+  int* err = reinterpret_cast<int*>(base + 8);
+  int* info = reinterpret_cast<int*>(base + 12);
+  cx<T>* cand = reinterpret_cast<cx<T>*>(base + 64);
+  T* candval = reinterpret_cast<T*>(cand + 2 * (size_t)Gmax * nb);
+  int* candidx = reinterpret_cast<int*>(candval + 2 * Gmax);
+  cx<T>* rowj = reinterpret_cast<cx<T>*>(candidx + 2 * Gmax);
+  M25_CUDA(cudaMemsetAsync(base, 0, 64, st));
+  for (int k0 = 0; k0 < n; k0 += nb) {
+    const int w = std::min(nb, n - k0);
+    const int m = n - k0;
+    // grid size: as many CTAs as can be co-resident, each with >= 1 row
+    int occ = 0;
+    G = std::min(m, ctx->num_sms);
+    fits(G, m, panel_smem);
+    for (int bps = 4; bps >= 1; --bps) {
+      int g = std::min(m, bps * ctx->num_sms);
+      size_t smem;
+      if (!fits(g, m, smem)) continue;
+      M25_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, panel_kernel<T>, 256, smem));
+      if (occ * ctx->num_sms >= g) {
+        G = g;
+        panel_smem = smem;
+        break;
+      }
+    }
+    if (!fits(G, m, panel_smem)) {
+      set_error("dense LU: matrix too large for the panel slices in shared memory");
+      return M25_ERR_VALUE;
+    }
+    M25_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, panel_kernel<T>, 256, panel_smem));
+    if (occ * ctx->num_sms < G) {
+      set_error("dense LU: cooperative panel grid does not fit on the device");
+      return M25_ERR_VALUE;
+    }
+    PanelArgs<T> pa;
+    pa.A = A;
+    pa.lda = lda;
+    pa.n = n;
+    pa.k0 = k0;
+    pa.nb = w;
+    pa.rows_per_cta = (m + G - 1) / G;
+    pa.ipiv = ipiv;
+    pa.cand = cand;
+    pa.candval = candval;
+    pa.candidx = candidx;
+    pa.rowj = rowj;
+    pa.bar = bar;
+    pa.err = err;
+    pa.info = info;
+    void* args[] = {&pa};
+    {
+      StageTimer tm(ctx, ST_PANEL);
+      M25_CUDA(cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(G), dim3(256), args, panel_smem, st));
+    }
+    if (n > w) {
+      StageTimer tm(ctx, ST_LASWP);
+      laswp_kernel<T><<<(n + 255) / 256, 256, 0, st>>>(A, lda, n, k0, w, ipiv);
+    }
+    if (k0 + w < n) {
+      int ncol = n - k0 - w;
+      size_t smem_t = (size_t)w * w * sizeof(cx<T>) + (size_t)w * 32 * sizeof(cx<T>);
+      {
+        StageTimer tm(ctx, ST_TRSM);
+        trsm_kernel<T><<<(ncol + 31) / 32, 256, smem_t, st>>>(A, lda, n, k0, w);
+      }
+      StageTimer tm(ctx, ST_GEMM);
+      if (use_tc) {
+        rc = lu_gemm_tc(ctx, reinterpret_cast<zf*>(A), lda, n, k0, w);
+        if (rc) return rc;
+      } else {
+        dim3 grid((ncol + 63) / 64, (ncol + 63) / 64);
+        gemm_kernel<T><<<grid, 256, 0, st>>>(A, lda, n, k0, w);
+      }
+    }
+    M25_CHECK_LAUNCH();
+  }
+  int hflags[3];
+  M25_CUDA(cudaMemcpyAsync(hflags, base + 8, 8, cudaMemcpyDeviceToHost, st));
+  M25_CUDA(cudaStreamSynchronize(st));
+  if (hflags[0]) {
+    set_error("dense LU: grid barrier timed out");
+    return M25_ERR_CUDA;
+  }
+  *info_host = hflags[1];
+  return M25_OK;
+}
+
+template <class T>
+int lu_solve(m25_ctx* ctx, const cx<T>* A, int64_t lda, int n, const int32_t* ipiv, const cx<T>* B, int nrhs,
+             cx<T>* X) {
+  cudaStream_t st = ctx->stream;
+  if (nrhs > 8) {
+    set_error("dense solve: at most 8 right-hand sides per call");
+    return M25_ERR_VALUE;
+  }
+  if ((size_t)n * sizeof(int) > 200 * 1024) {
+    set_error("dense solve: n too large for the permutation in shared memory");
+    return M25_ERR_VALUE;
+  }
+  M25_CUDA(cudaFuncSetAttribute(permute_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  StageTimer tm(ctx, ST_TRSV);
+  permute_kernel<T><<<1, 1024, n * sizeof(int), st>>>(n, nrhs, ipiv, B, X);
+  const int bs = 64;
+  for (int b0 = 0; b0 < n; b0 += bs) {
+    int w = std::min(bs, n - b0);
+    trsv_block_kernel<T><<<1, 256, 0, st>>>(A, lda, b0, w, nrhs, 0, X);
+    if (b0 + w < n) {
+      int rows = n - b0 - w;
+      trsv_update_kernel<T><<<(rows * 32 + 255) / 256, 256, 0, st>>>(A, lda, b0, w, nrhs, b0 + w, n, X);
+    }
+  }
+  for (int b0 = ((n - 1) / bs) * bs; b0 >= 0; b0 -= bs) {
+    int w = std::min(bs, n - b0);
+    trsv_block_kernel<T><<<1, 256, 0, st>>>(A, lda, b0, w, nrhs, 1, X);
+    if (b0 > 0) trsv_update_kernel<T><<<(b0 * 32 + 255) / 256, 256, 0, st>>>(A, lda, b0, w, nrhs, 0, b0, X);
+  }
+  M25_CHECK_LAUNCH();
+  return M25_OK;
+}
+
+template int lu_factor<double>(m25_ctx*, zd*, int64_t, int, int32_t*, int, bool, int*);
+template int lu_factor<float>(m25_ctx*, zf*, int64_t, int, int32_t*, int, bool, int*);
+template int lu_solve<double>(m25_ctx*, const zd*, int64_t, int, const int32_t*, const zd*, int, zd*);
+template int lu_solve<float>(m25_ctx*, const zf*, int64_t, int, const int32_t*, const zf*, int, zf*);
+
+// Mixed solve: LU32 of Z (already factored in Zlu), fp64 refinement against Zres.
+template <class TZ>
+int refine(m25_ctx* ctx, int n, int nrhs, const cx<TZ>* Zres, int64_t ldz, const zf* LU, const int32_t* ipiv,
+           const zd* B, zd* X, double tol, int max_iter, int* steps) {
+  cudaStream_t st = ctx->stream;
+  size_t nn = (size_t)n * nrhs;
+  int rc = ctx->Rw.ensure(nn * sizeof(zd) + nn * 2 * sizeof(zf) + (n + 2) * sizeof(double));
+  if (rc) return rc;
+  zd* R = ctx->Rw.as<zd>();
+  zf* r32 = reinterpret_cast<zf*>(R + nn);
+  zf* d32 = r32 + nn;
+  double* rmax = reinterpret_cast<double*>(d32 + nn);
+  double* gmax = rmax + n;
+  // |B| for the relative residual
+  double bmax = 0;
+  {
+    std::vector<zd> hb(nn);
+    M25_CUDA(cudaMemcpyAsync(hb.data(), B, nn * sizeof(zd), cudaMemcpyDeviceToHost, st));
+    M25_CUDA(cudaStreamSynchronize(st));
+    for (auto& v : hb) bmax = std::max(bmax, cabs1(v));
+  }
+  if (bmax == 0) bmax = 1;
+  // X = 0: first pass solves B itself
+  M25_CUDA(cudaMemsetAsync(X, 0, nn * sizeof(zd), st));
+  *steps = 0;
+  for (int it = 0; it <= max_iter; ++it) {
+    {
+      StageTimer tm(ctx, ST_REFINE);
+      residual_kernel<TZ><<<(n * 32 + 255) / 256, 256, 0, st>>>(n, nrhs, Zres, ldz, B, X, R, rmax);
+      max_reduce<<<1, 1024, 0, st>>>(n, rmax, gmax);
+    }
+    double hmax = 0;
+    M25_CUDA(cudaMemcpyAsync(&hmax, gmax, sizeof(double), cudaMemcpyDeviceToHost, st));
+    M25_CUDA(cudaStreamSynchronize(st));
+    if (hmax / bmax <= tol) break;
+    if (it == max_iter) {
+      set_error("mixed solve: iterative refinement did not reach the tolerance");
+      return M25_ERR_NUMERIC;
+    }
+    double s = 1.0 / hmax;  // keep the fp32 right-hand side O(1)
+    scale_to_z32<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(nn, R, s, r32);
+    rc = lu_solve<float>(ctx, LU, n, n, ipiv, r32, nrhs, d32);
+    if (rc) return rc;
+    axpy_z32<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(nn, d32, hmax, X);
+    *steps = it + 1;
+  }
+  M25_CHECK_LAUNCH();
+  return M25_OK;
+}
+
+template int refine<double>(m25_ctx*, int, int, const zd*, int64_t, const zf*, const int32_t*, const zd*, zd*, double,
+                            int, int*);
+template int refine<float>(m25_ctx*, int, int, const zf*, int64_t, const zf*, const int32_t*, const zd*, zd*, double,
+                           int, int*);
+
+void cast_to_z32(m25_ctx* ctx, const zd* a, int64_t lda, zf* b, int64_t ldb, int n, int m) {
+  int64_t tot = (int64_t)n * m;
+  cast_z64_to_z32<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(a, lda, b, ldb, n, m);
+}
+
+}  // namespace m25

@@ -1,0 +1,158 @@
+"""ctypes binding of the CUDA engine's C ABI (include/m25.h).
+
+The shared library is built in-tree (mom25d_gb300/build.py). There is no
+CPU fallback: loading fails loudly when the library or a CUDA device is
+missing. Status codes map to the exceptions mom25d raises for the same
+conditions (ValueError, MemoryError, RuntimeError).
+"""
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libm25.so")
+
+M25_OK, M25_ERR_VALUE, M25_ERR_MEMORY, M25_ERR_CUDA, M25_ERR_NUMERIC = range(5)
+M25_FP64, M25_MIXED = 0, 1
+M25_ON_HOST, M25_ON_DEVICE = 0, 1
+
+EXPORTS = ("m25_last_error", "m25_version", "m25_ctx_create", "m25_ctx_destroy", "m25_ctx_synchronize",
+           "m25_ctx_stream", "m25_geometry_create", "m25_geometry_destroy", "m25_geometry_stats",
+           "m25_greens_create", "m25_greens_destroy", "m25_greens_tables", "m25_assemble", "m25_dense_solve",
+           "m25_ports_create", "m25_ports_destroy", "m25_deembed", "m25_sweep_point", "m25_deembed_debug",
+           "m25_ctx_timing")
+
+_i32p = C.POINTER(C.c_int32)
+_f64p = C.POINTER(C.c_double)
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("nt", C.c_int32), ("nb", C.c_int32), ("nlev", C.c_int32),
+                ("verts", _f64p), ("tri_basis", _i32p), ("tri_sign", _f64p), ("edge_len", _f64p),
+                ("tri_layer", _i32p), ("level_z", _f64p), ("edge_tri", _i32p), ("edge_loc", _i32p),
+                ("nblocks", C.c_int32), ("block_tris", _i32p),
+                ("nv", C.c_int32), ("npad", C.c_int32), ("pad_tris", _i32p), ("seg_pad_off", _i32p),
+                ("seg_pad", _i32p), ("seg_pad_w", _f64p), ("seg_end_lev", _i32p), ("seg_span", _f64p),
+                ("seg_xy", _f64p), ("seg_drill", _f64p), ("near_factor", C.c_double), ("far_factor", C.c_double)]
+
+
+class GreensDesc(C.Structure):
+    _fields_ = [("freq", C.c_double), ("nlayer", C.c_int32), ("layer_t", _f64p), ("layer_eps", _f64p),
+                ("layer_tand", _f64p), ("nlev", C.c_int32), ("lev_iface", _i32p), ("lev_z", _f64p),
+                ("single", C.c_int32), ("zs_ground_re", C.c_double), ("zs_ground_im", C.c_double),
+                ("stack_h", C.c_double), ("nk_c", C.c_int32), ("nk_r", C.c_int32), ("kc", _f64p), ("wc", _f64p),
+                ("kr", _f64p), ("wr", _f64p), ("nrho", C.c_int32), ("rho", _f64p), ("kbig", C.c_double)]
+
+
+class PortDesc(C.Structure):
+    _fields_ = [("nport", C.c_int32), ("ngroup", C.c_int32), ("group_of", _i32p), ("port_level", _i32p),
+                ("ns", _i32p), ("s", _f64p), ("cut_off", _i32p), ("cut_edge", _i32p), ("cut_w", _f64p),
+                ("nvpt", _i32p), ("vpts", _f64p), ("beta0", _f64p), ("lossless", C.c_int32), ("bounds", _f64p),
+                ("v_weight", C.c_double), ("excitation", _f64p)]
+
+
+_lib = None
+
+
+def load():
+    """The engine library (built on demand when nvcc is present)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from . import build
+
+        build.build()
+    lib = C.CDLL(LIB_PATH)
+    for name in EXPORTS:
+        getattr(lib, name)  # every declared entry point must be exported
+    lib.m25_last_error.restype = C.c_char_p
+    lib.m25_ctx_stream.restype = C.c_void_p
+    vp = C.c_void_p
+    lib.m25_ctx_create.argtypes = [C.c_int, C.POINTER(vp)]
+    for f in ("m25_ctx_destroy", "m25_ctx_synchronize", "m25_geometry_destroy", "m25_greens_destroy",
+              "m25_ports_destroy"):
+        getattr(lib, f).argtypes = [vp]
+    lib.m25_geometry_create.argtypes = [vp, C.POINTER(MeshDesc), C.POINTER(vp)]
+    lib.m25_geometry_stats.argtypes = [vp, C.POINTER(C.c_int64)]
+    lib.m25_greens_create.argtypes = [vp, C.POINTER(GreensDesc), C.POINTER(vp)]
+    lib.m25_greens_tables.argtypes = [vp, _f64p, _f64p, _f64p]
+    d = C.c_double
+    lib.m25_assemble.argtypes = [vp, vp, vp, d, d, d, d, C.c_int, vp, C.c_int64, C.c_int]
+    lib.m25_dense_solve.argtypes = [vp, C.c_int32, C.c_int32, C.c_int, vp, vp, vp, C.c_int, d, C.c_int32, _i32p]
+    lib.m25_ports_create.argtypes = [vp, vp, C.POINTER(PortDesc), C.POINTER(vp)]
+    lib.m25_deembed.argtypes = [vp, vp, vp, vp, vp, C.c_int, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p]
+    lib.m25_sweep_point.argtypes = [vp, vp, vp, vp, d, d, d, d, C.c_int, _f64p, d, C.c_int32, _f64p, _f64p, _f64p,
+                                    _f64p, _f64p, _f64p, _i32p]
+    lib.m25_deembed_debug.argtypes = [vp, vp, _f64p, _f64p, _f64p, _f64p]
+    lib.m25_ctx_timing.argtypes = [vp, C.c_int, _f64p, C.POINTER(C.c_longlong)]
+    _lib = lib
+    return lib
+
+
+def check(rc):
+    if rc == M25_OK:
+        return
+    msg = load().m25_last_error().decode(errors="replace")
+    if rc == M25_ERR_VALUE:
+        raise ValueError(msg)
+    if rc == M25_ERR_MEMORY:
+        raise MemoryError(msg)
+    raise RuntimeError(msg)
+
+
+def ptr(a, ctype=C.c_double):
+    return a.ctypes.data_as(C.POINTER(ctype)) if a is not None else None
+
+
+def i32(a):
+    return np.ascontiguousarray(a, np.int32)
+
+
+def f64(a):
+    return np.ascontiguousarray(a, np.float64)
+
+
+class Context:
+    """One engine context: a CUDA device and stream plus a reusable workspace."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = C.c_void_p()
+        check(self.lib.m25_ctx_create(int(device), C.byref(h)))
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.m25_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
+
+    def synchronize(self):
+        check(self.lib.m25_ctx_synchronize(self.h))
+
+
+class Handle:
+    """Owner of a device object (geometry, Green's tables, ports)."""
+
+    def __init__(self, ctx, h, destroy, keep=()):
+        self.ctx, self.h, self._destroy, self._keep = ctx, h, destroy, keep
+
+    def close(self):
+        if self.h:
+            self._destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass

@@ -1,0 +1,542 @@
+"""Solver / sweep API of mom25d (Engine/mom25d/solver.py:673-1335) on the
+GB300 engine.
+
+The Python layer keeps mom25d's objects and their meaning (Solver, sweep,
+SweepResult, PortModel data, port groups, checkpoint keys) and prepares the
+small frequency-independent host arrays: test blocks, port cuts and voltage
+points, the Sommerfeld path and tabulation radii of each frequency. Every
+per-frequency computation of the sweep path runs on the GPU through the C
+ABI: Green's tables, impedance fill, LU + solve, de-embedding. There is no
+CPU fallback; without the CUDA library or a device the constructor raises.
+"""
+
+import ctypes as C
+import os
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import analytic
+from . import engine as E
+from .constants import C0, EPS0, MU0
+
+# ------------------------------------------------------------- host prep
+_A1, _B1 = 0.059715871789770, 0.470142064105115
+_A2, _B2 = 0.797426985353087, 0.101286507323456
+TRI7_BARY = np.array([[1 / 3, 1 / 3, 1 / 3], [_A1, _B1, _B1], [_B1, _A1, _B1], [_B1, _B1, _A1],
+                      [_A2, _B2, _B2], [_B2, _A2, _B2], [_B2, _B2, _A2]])
+TRI7_W = np.array([0.225] + [0.132394152788506] * 3 + [0.125939180544827] * 3)
+
+
+def morton_order(xy):
+    """Z-order of points on a 16-bit lattice over their bounding square
+    (ties keep input order); mom25d groups its test triangles the same way
+    (Engine/mom25d/solver.py:294-304), which fixes the near/mid/far blocks."""
+    span = max(float(np.ptp(xy, 0).max()), 1e-30)
+    q = ((xy - xy.min(0)) / span * 65535).astype(np.uint64)
+
+    def interleave(v):
+        for shift, mask in ((8, 0x00FF00FF), (4, 0x0F0F0F0F), (2, 0x33333333), (1, 0x55555555)):
+            v = (v | (v << np.uint64(shift))) & np.uint64(mask)
+        return v
+
+    return np.argsort(interleave(q[:, 0]) | (interleave(q[:, 1]) << np.uint64(1)), kind="stable")
+
+
+def test_blocks(mesh, block=32):
+    """(nblocks, 32) triangle slots: per level, Morton order, blocks of 32."""
+    out = []
+    tl = mesh.tri_layer
+    for lt in range(len(mesh.layer_names)):
+        on = np.nonzero(tl == lt)[0]
+        if not on.size:
+            continue
+        order = on[morton_order(mesh.centroid[on])]
+        for p0 in range(0, order.size, block):
+            row = -np.ones(block, np.int32)
+            pb = order[p0:p0 + block]
+            row[:pb.size] = pb
+            out.append(row)
+    return np.stack(out)
+
+
+def gauss_panels(a, b, n_panels, order):
+    x, w = np.polynomial.legendre.leggauss(order)
+    edges = np.linspace(a, b, n_panels + 1)
+    half = 0.5 * np.diff(edges)
+    mid = 0.5 * (edges[1:] + edges[:-1])
+    return (mid[:, None] + half[:, None] * x).ravel(), (half[:, None] * w).ravel()
+
+
+def sommerfeld_path(k0, kref, tmin, rho_max, order=12):
+    """Lifted arc k = t + j a sin(pi t / T) over [0, T] (Gauss-Legendre panels)
+    and the real axis [T, kmax]: T = 1.3 kref + k0, a = min(k0/2, 1/rho_max)
+    (Engine/mom25d/greens.py:261-278, layered.py:343-358)."""
+    T = 1.3 * kref + k0
+    a = min(0.5 * k0, 1.0 / rho_max)
+    n1 = int(np.clip(np.ceil(2 * T / a), 100, 3000))
+    t, w = gauss_panels(0.0, T, n1, order)
+    kc = t + 1j * a * np.sin(np.pi * t / T)
+    wc = w * (1 + 1j * a * np.pi / T * np.cos(np.pi * t / T))
+    kmax = max(40 * kref, 20.0 / tmin, T * 1.5)
+    dk = min(np.pi / rho_max, 0.5 / tmin, kref)
+    n2 = int(np.ceil((kmax - T) / dk))
+    kr, wr = gauss_panels(T, kmax, n2, 8)
+    return kc, wc, kr, wr
+
+
+def tabulation_radii(rho_max, lam, tmin):
+    """rho grid: steps min(lambda/80, max(t_min/25, rho/25)) up to rho_max
+    (Engine/mom25d/greens.py:298-306)."""
+    r = [0.0]
+    while r[-1] < rho_max:
+        r.append(r[-1] + min(lam / 80, max(tmin / 25, r[-1] / 25)))
+    return np.array(r)
+
+
+class Greens:
+    """Green's tables of one frequency on the device (GroundedSlabGreens /
+    LayeredGreens): rho grid, S_A/S_V/S_W tables, cubic coefficients."""
+
+    def __init__(self, solver, freq):
+        st, mesh = solver.stack, solver.mesh
+        self.freq = float(freq)
+        self.omega = 2 * np.pi * freq
+        self.k0 = k0 = self.omega / C0
+        layers = st.layers
+        eps = np.array([d.eps_r * (1 - 1j * d.tand) for d in layers])
+        kk = k0 * np.sqrt(eps)
+        t = np.array([d.t for d in layers], float)
+        single = solver.single
+        kref = abs(kk[0]) if single else np.abs(kk).max()
+        tmin = t[0] if single else t.min()
+        kc, wc, kr, wr = sommerfeld_path(k0, kref, tmin, solver.rho_max)
+        self.rho = tabulation_radii(solver.rho_max, 2 * np.pi / kref, tmin)
+        zg = st.surface_impedance(freq) if st.ground_loss else 0.0
+        zg = complex(zg)
+        self.levels = list(mesh.layer_names)
+        L = len(self.levels)
+        arrs = dict(lt=E.f64(t), le=E.f64([d.eps_r for d in layers]), ld=E.f64([d.tand for d in layers]),
+                    il=E.i32([st.metals[n] for n in self.levels]), lz=E.f64(solver.zl),
+                    kc=E.f64(np.stack([kc.real, kc.imag], 1)), wc=E.f64(np.stack([wc.real, wc.imag], 1)),
+                    kr=E.f64(kr), wr=E.f64(wr), rho=E.f64(self.rho))
+        d = E.GreensDesc(self.freq, len(layers), E.ptr(arrs["lt"]), E.ptr(arrs["le"]), E.ptr(arrs["ld"]), L,
+                         E.ptr(arrs["il"], C.c_int32), E.ptr(arrs["lz"]), int(single), zg.real, zg.imag,
+                         float(st.z[-1]), kc.size, kr.size, E.ptr(arrs["kc"]), E.ptr(arrs["wc"]), E.ptr(arrs["kr"]),
+                         E.ptr(arrs["wr"]), self.rho.size, E.ptr(arrs["rho"]), 15.0 / t.min())
+        h = C.c_void_p()
+        E.check(solver.ctx.lib.m25_greens_create(solver.ctx.h, C.byref(d), C.byref(h)))
+        self._h = E.Handle(solver.ctx, h, solver.ctx.lib.m25_greens_destroy)
+        self.nlev = L
+        self.h = h
+
+    def tables(self):
+        """(S (3,L,L,nrho), c (3,L,L), coef (L*L, nrho-1, 4, 3)) complex128 host copies."""
+        L, n = self.nlev, self.rho.size
+        S = np.zeros((3, L, L, n), complex)
+        c = np.zeros((3, L, L), complex)
+        coef = np.zeros((L * L, n - 1, 4, 3), complex)
+        E.check(self._h.ctx.lib.m25_greens_tables(self.h, E.ptr(S.view(np.float64)), E.ptr(c.view(np.float64)),
+                                                  E.ptr(coef.view(np.float64))))
+        return S, c, coef
+
+    def close(self):
+        self._h.close()
+
+
+class PortModel:
+    """Delta-gap excitation, fit-window cuts and line-voltage sample points of
+    one feed (Engine/mom25d/solver.py:570-610)."""
+
+    def __init__(self, mesh, port, h):
+        margin = port.margin if port.margin is not None else max(1.5 * port.width, 4 * h)
+        s = mesh.cut_positions(port)
+        s = s[(s >= margin - 1e-12) & (s <= port.s_gap - margin + 1e-12)]
+        if s.size < 4:
+            raise ValueError(f"port {port.name}: feed line too short or mesh too coarse "
+                             f"({s.size} sample cuts in the fitting window "
+                             f"[{margin * 1e3:.3g}, {(port.s_gap - margin) * 1e3:.3g}] mm)")
+        self.port = port
+        self.s = s
+        self.cuts = [mesh.cut_edges(port, si) for si in s]
+        idx, sgn = mesh.cut_edges(port, port.s_gap)
+        if idx.size == 0:
+            raise ValueError(f"port {port.name}: no mesh edges on the gap cut")
+        self.excitation = np.zeros(mesh.n_unknowns)
+        self.excitation[idx] = sgn * mesh.edge_len[idx]
+        self.len = mesh.edge_len
+        allcuts = mesh.cut_positions(port)
+        k = np.searchsorted(allcuts, s)
+        lo = s - allcuts[np.maximum(k - 1, 0)]
+        hi = allcuts[np.minimum(k + 1, allcuts.size - 1)] - s
+        d = 0.5 * np.minimum(np.where(lo > 0, lo, np.inf), np.where(hi > 0, hi, np.inf))
+        frac = np.array([-0.3, -0.1, 0.1, 0.3])
+        along = np.stack([s - d, s + d], 1)
+        self.vpts = port.point(along[:, :, None], frac * port.width).reshape(-1, 2)
+        self.nper = 2 * frac.size
+
+
+@dataclass
+class SweepResult:
+    freqs: np.ndarray
+    S: np.ndarray  # (F,P,P), referenced to each port's line impedance z0
+    z0: np.ndarray  # (F,P)
+    gamma: np.ndarray  # (F,P)
+    z0_line: np.ndarray  # (F,P)
+    fit_residual: np.ndarray  # (F,P)
+    port_names: list
+    currents: list = None
+    info: dict = None
+
+    @property
+    def eeff(self):
+        k0 = 2 * np.pi * self.freqs / C0
+        return (self.gamma.imag / k0[:, None]) ** 2
+
+    def renormalize(self, zref=50.0):
+        """S-parameters referenced to a common real impedance zref."""
+        out = np.empty_like(self.S)
+        eye = np.eye(self.S.shape[1])
+        for f, S in enumerate(self.S):
+            sq = np.diag(np.sqrt(self.z0[f]))
+            Zm = sq @ (eye + S) @ np.linalg.inv(eye - S) @ sq
+            out[f] = (Zm - zref * eye) @ np.linalg.inv(Zm + zref * eye)
+        return out
+
+    def db(self, i, j, S=None):
+        S = self.S if S is None else S
+        return 20 * np.log10(np.abs(S[:, i, j]))
+
+    def write_touchstone(self, path, zref=50.0):
+        S = self.S if zref is None else self.renormalize(zref)
+        z = zref if zref is not None else float(np.mean(self.z0))
+        n = S.shape[1]
+        with open(path, "w") as fh:
+            fh.write(f"! mom25d_gb300 2.5D MoM. ports: {', '.join(self.port_names)}\n")
+            fh.write(f"# HZ S RI R {z:g}\n")
+            for f, Sf in zip(self.freqs, S):
+                vals = Sf.T.ravel() if n == 2 else Sf.ravel()
+                fh.write(f"{f:.9e} " + " ".join(f"{v.real:.9e} {v.imag:.9e}" for v in vals) + "\n")
+
+
+PRECISIONS = {"fp64": E.M25_FP64, "mixed": E.M25_MIXED}
+
+
+class Solver:
+    """mom25d.Solver on the GB300 engine.
+
+    mesh      : a Mesh with RWG data, via segments and port cuts (this
+                package's grid mesher, or mom25d's own Mesh object)
+    substrate : Substrate or Stackup (open top, no inner planes)
+    method    : "dense" (the only method of this engine; "auto" maps to it)
+    precision : "fp64" (fill + LU in fp64) or "mixed" (complex64 fill and
+                LU, fp64 iterative refinement; tolerance refine_tol)
+    """
+
+    def __init__(self, mesh, substrate, z0=None, verbose=True, method="dense", v_weight=None, precision="fp64",
+                 device=0, refine_tol=1e-12, max_refine=20):
+        if method not in ("auto", "dense"):
+            raise ValueError("this engine implements method='dense' only")
+        if precision not in PRECISIONS:
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.mesh = mesh
+        self.sub = substrate
+        self.stack = st = substrate if hasattr(substrate, "layers") else substrate.to_stackup()
+        missing = [n for n in mesh.layer_names if n not in st.metals]
+        if missing:
+            raise ValueError(f"mesh layers {missing} are not metal levels of the stackup {list(st.metals)}")
+        if getattr(mesh, "n_frills", 0) or getattr(mesh, "n_ap", 0) or getattr(mesh, "n_walls", 0):
+            raise ValueError("antipads, plane apertures and thick metal are not part of this engine")
+        self.single = len(st.layers) == 1 and st.top == "air" and list(mesh.layer_names) == ["top"]
+        self.zl = np.array([st.level_z(n) for n in mesh.layer_names])
+        order = sorted(list(mesh.layer_names), key=st.level_z)
+        if getattr(mesh, "level_order", None) != order:
+            mesh.assign_levels(order)
+        self.ports = mesh.layout.ports
+        if not self.ports:
+            raise ValueError("layout has no ports")
+        if getattr(mesh.layout, "lumped", None) or getattr(mesh.layout, "internal_ports", None):
+            raise ValueError("lumped components and internal ports are not part of this engine")
+        self.method = "dense"
+        self.precision = precision
+        self.refine_tol, self.max_refine = refine_tol, max_refine
+        self.z0_fixed = None if z0 is None else np.asarray(z0, float)
+        v = mesh.nodes
+        self.rho_max = 1.02 * np.hypot(*(v.max(0) - v.min(0)))
+        self.verbose = verbose
+        self.v_weight = 1.0 if v_weight is None else float(v_weight)
+        self.pm = [PortModel(mesh, p, st.level_h(p.layer)) for p in self.ports]
+        self.groups = {}
+        for p, port in enumerate(self.ports):
+            hp = st.level_h(port.layer)
+            key = (round(port.width / hp, 9), port.layer,
+                   port.ground.key(hp) if port.ground is not None else None, port.z0_from)
+            self.groups.setdefault(key, []).append(p)
+        if st.lossless:
+            raise ValueError("lossless stacks (bounded beta search) are not supported by this engine")
+        self.ctx = E.Context(device)
+        self._geom = None
+        self._ports = None
+
+    # ----------------------------------------------------------- device data
+    def geometry(self):
+        """Device copy of the mesh + near/mid/far classes + closed-form near integrals."""
+        if self._geom is not None:
+            return self._geom
+        m, st = self.mesh, self.stack
+        blocks = test_blocks(m)
+        nt, nb = len(m.tris), m.n_basis
+        segs = m.via_segments
+        nv = len(segs)
+        lev = {n: i for i, n in enumerate(m.layer_names)}
+        zmap = {n: st.level_z(n) for n in m.layer_names}
+        zmap["gnd"] = 0.0
+        arrs = dict(verts=E.f64(m.verts), tb=E.i32(m.tri_basis), ts=E.f64(m.tri_sign), el=E.f64(m.edge_len),
+                    tl=E.i32(m.tri_layer), lz=E.f64(self.zl), et=E.i32(np.stack([m.tp, m.tm], 1)),
+                    eloc=E.i32(np.stack([m.vp, m.vm], 1)), blocks=E.i32(blocks))
+        if nv:
+            tris = [g[e] for g in segs for e in ("top_tris", "bottom_tris") if g[e] is not None]
+            pad = np.unique(np.concatenate(tris))
+            pos = -np.ones(nt, int)
+            pos[pad] = np.arange(pad.size)
+            off, ent, w, endlev, span, xy, drill = [0], [], [], [], [], [], []
+            for g in segs:
+                for key, sg in (("top_tris", 1.0), ("bottom_tris", -1.0)):
+                    t = g[key]
+                    if t is not None:
+                        a = m.area[t].sum()
+                        ent += list(pos[t])
+                        w += [sg / a] * len(t)
+                off.append(len(ent))
+                endlev.append([m.tri_layer[g["top_tris"][0]] if g["top_tris"] is not None else -1,
+                               m.tri_layer[g["bottom_tris"][0]] if g["bottom_tris"] is not None else -1])
+                span.append([zmap[g["bottom"]], zmap[g["top"]]])
+                v = m.vias[g["via"]]
+                xy.append(v.xy)
+                drill.append(v.drill)
+            arrs.update(pad=E.i32(pad), off=E.i32(off), ent=E.i32(ent), w=E.f64(w), endlev=E.i32(endlev),
+                        span=E.f64(span), xy=E.f64(xy), drill=E.f64(drill))
+        g = lambda k, t=C.c_double: E.ptr(arrs[k], t) if k in arrs else None  # noqa: E731
+        i = C.c_int32
+        d = E.MeshDesc(nt, nb, len(m.layer_names), g("verts"), g("tb", i), g("ts"), g("el"), g("tl", i), g("lz"),
+                       g("et", i), g("eloc", i), blocks.shape[0], g("blocks", i), nv,
+                       int(arrs["pad"].size) if nv else 0, g("pad", i), g("off", i), g("ent", i), g("w"),
+                       g("endlev", i), g("span"), g("xy"), g("drill"), 3.0, 10.0)
+        h = C.c_void_p()
+        E.check(self.ctx.lib.m25_geometry_create(self.ctx.h, C.byref(d), C.byref(h)))
+        self._geom = E.Handle(self.ctx, h, self.ctx.lib.m25_geometry_destroy)
+        return self._geom
+
+    def geometry_stats(self):
+        out = (C.c_int64 * 4)()
+        E.check(self.ctx.lib.m25_geometry_stats(self.geometry().h, out))
+        return dict(near_pairs=out[0], mid_pairs=out[1], far_pairs=out[2], near_bytes=out[3])
+
+    def port_data(self):
+        if self._ports is not None:
+            return self._ports
+        m = self.mesh
+        groups = list(self.groups.values())
+        gid = np.zeros(len(self.ports), int)
+        for k, mem in enumerate(groups):
+            gid[mem] = k
+        cut_off, cut_edge, cut_w = [0], [], []
+        for pm in self.pm:
+            for idx, sg in pm.cuts:
+                cut_edge += list(idx)
+                cut_w += list(sg * m.edge_len[idx])
+                cut_off.append(len(cut_edge))
+        lev = [m.layer_names.index(p.layer) for p in self.ports]
+        arrs = dict(gid=E.i32(gid), lev=E.i32(lev), ns=E.i32([pm.s.size for pm in self.pm]),
+                    s=E.f64(np.concatenate([pm.s for pm in self.pm])), off=E.i32(cut_off), edge=E.i32(cut_edge),
+                    w=E.f64(cut_w), nvpt=E.i32([len(pm.vpts) for pm in self.pm]),
+                    vpts=E.f64(np.concatenate([pm.vpts for pm in self.pm])),
+                    exc=E.f64(np.stack([pm.excitation for pm in self.pm])))
+        i = C.c_int32
+        d = E.PortDesc(len(self.ports), len(groups), E.ptr(arrs["gid"], i), E.ptr(arrs["lev"], i),
+                       E.ptr(arrs["ns"], i), E.ptr(arrs["s"]), E.ptr(arrs["off"], i), E.ptr(arrs["edge"], i),
+                       E.ptr(arrs["w"]), E.ptr(arrs["nvpt"], i), E.ptr(arrs["vpts"]), None, 0, None,
+                       self.v_weight, E.ptr(arrs["exc"]))
+        h = C.c_void_p()
+        E.check(self.ctx.lib.m25_ports_create(self.ctx.h, self.geometry().h, C.byref(d), C.byref(h)))
+        self._ports = E.Handle(self.ctx, h, self.ctx.lib.m25_ports_destroy)
+        return self._ports
+
+    # ---------------------------------------------------------------- path
+    def greens(self, freq):
+        return Greens(self, freq)
+
+    def surface_impedance(self, freq):
+        return self.stack.surface_impedance(freq)
+
+    def beta0(self, f):
+        """Kirschning-Jansen phase constant per port group (the fit's start)."""
+        out = []
+        for members in self.groups.values():
+            port = self.ports[members[0]]
+            hp = self.stack.level_h(port.layer)
+            out.append(float(analytic.beta(port.width, hp, self.stack.eps_below(port.layer), f)))
+        return np.array(out)
+
+    def impedance(self, freq, greens=None, precision=None):
+        """The MoM impedance matrix at freq as a host array (complex128 for
+        fp64, complex64 for mixed)."""
+        g = greens or self.greens(freq)
+        prec = PRECISIONS[precision or self.precision]
+        n = self.mesh.n_unknowns
+        Z = np.zeros((n, n), np.complex128 if prec == E.M25_FP64 else np.complex64)
+        zs = complex(self.surface_impedance(freq))
+        E.check(self.ctx.lib.m25_assemble(self.ctx.h, self.geometry().h, g.h, zs.real, zs.imag, zs.real, zs.imag,
+                                          prec, Z.ctypes.data, n, E.M25_ON_HOST))
+        return Z
+
+    def port_excitations(self):
+        return np.stack([pm.excitation for pm in self.pm], 1)
+
+    def solve_currents(self, freq, excitations=None, greens=None, Z=None):
+        """RWG (+ via segment) coefficients (N, Nexc) for the given excitations
+        (default: one 1 V delta gap per port)."""
+        g = greens or self.greens(freq)
+        if Z is None:
+            Z = self.impedance(freq, g)
+        B = self.port_excitations() if excitations is None else excitations
+        return dense_solve(Z, B, precision=self.precision, ctx=self.ctx, tol=self.refine_tol,
+                           max_iter=self.max_refine)
+
+    def point(self, f, keep_currents=False):
+        """One frequency of the sweep on the device: (S, z0, gamma, z0_line, residual, x or None, info)."""
+        g = self.greens(f)
+        P = len(self.ports)
+        n = self.mesh.n_unknowns
+        S = np.zeros((P, P), complex)
+        z0 = np.zeros(P)
+        gam = np.zeros(P, complex)
+        zl = np.zeros(P, complex)
+        res = np.zeros(P)
+        x = np.zeros((n, P), complex) if keep_currents else None
+        info = np.zeros(2, np.int32)
+        zs = complex(self.surface_impedance(f))
+        b0 = E.f64(self.beta0(f))
+        F = lambda a: E.ptr(a.view(np.float64)) if a is not None else None  # noqa: E731
+        E.check(self.ctx.lib.m25_sweep_point(
+            self.ctx.h, self.geometry().h, g.h, self.port_data().h, zs.real, zs.imag, zs.real, zs.imag,
+            PRECISIONS[self.precision], E.ptr(b0), self.refine_tol, self.max_refine, F(x), F(S), E.ptr(z0), F(gam),
+            F(zl), E.ptr(res), E.ptr(info, C.c_int32)))
+        g.close()
+        if self.z0_fixed is not None:
+            d0 = np.sqrt(z0)
+            SI = S * d0[None, :] / d0[:, None]
+            z0 = self.z0_fixed.copy()
+            d = np.sqrt(z0)
+            S = d[:, None] * SI / d[None, :]
+        return S, z0, gam, zl, res, x, dict(refine_steps=int(info[0]))
+
+    def last_deembed(self):
+        """Intermediates of the last de-embedding on the device: triangle
+        charges q (Nt,P), line voltages phi (M,P), cut currents I and cut
+        voltages V (sum Ns, P)."""
+        P = len(self.ports)
+        M = sum(len(pm.vpts) for pm in self.pm)
+        ns = sum(pm.s.size for pm in self.pm)
+        q = np.zeros((len(self.mesh.tris), P), complex)
+        phi = np.zeros((M, P), complex)
+        I = np.zeros((ns, P), complex)
+        V = np.zeros((ns, P), complex)
+        F = lambda a: E.ptr(a.view(np.float64))  # noqa: E731
+        E.check(self.ctx.lib.m25_deembed_debug(self.ctx.h, self.port_data().h, F(phi), F(q), F(I), F(V)))
+        return q, phi, I, V
+
+    def _checkpoint_key(self, freqs):
+        m = self.mesh
+        return np.array([len(freqs), float(np.sum(freqs)), float(m.n_unknowns), float(np.sum(m.nodes)),
+                         float(np.sum(m.nodes ** 2)), float(len(m.tris)), 0.0])
+
+    def sweep(self, freqs, keep_currents=False, interp=None, values=None, checkpoint=None, wait_memory=None):
+        """S-parameters at freqs (exact fill at every frequency). checkpoint:
+        an .npz rewritten atomically after every frequency; a restarted sweep
+        with the same frequencies and mesh resumes from it."""
+        if interp not in (None, "auto"):
+            raise ValueError("this engine fills every frequency exactly (interp=None)")
+        freqs = np.atleast_1d(np.asarray(freqs, float))
+        nf, P = len(freqs), len(self.ports)
+        S = np.zeros((nf, P, P), complex)
+        gam = np.zeros((nf, P), complex)
+        zl = np.zeros((nf, P), complex)
+        zr = np.zeros((nf, P))
+        res = np.zeros((nf, P))
+        cur = [None] * nf
+        done = np.zeros(nf, bool)
+        key = self._checkpoint_key(freqs) if checkpoint else None
+        if checkpoint and os.path.exists(checkpoint) and not keep_currents:
+            try:
+                ck = np.load(checkpoint)
+                if ck["key"].shape == key.shape and np.allclose(ck["key"], key, rtol=1e-12, atol=0) \
+                        and ck["S"].shape == S.shape:
+                    done = ck["done"].astype(bool)
+                    S[:], gam[:], zl[:], zr[:], res[:] = (ck[k] for k in ("S", "gam", "zl", "zr", "res"))
+            except Exception as exc:  # noqa: BLE001 - unreadable: start afresh
+                if self.verbose:
+                    print(f" checkpoint: unreadable ({exc}); starting afresh", flush=True)
+                done[:] = False
+        steps = []
+        t0 = time.time()
+        for fi, f in enumerate(freqs):
+            if done[fi]:
+                continue
+            S[fi], zr[fi], gam[fi], zl[fi], res[fi], x, inf = self.point(f, keep_currents)
+            steps.append(inf["refine_steps"])
+            cur[fi] = x
+            done[fi] = True
+            if self.verbose:
+                print(f"PROGRESS {int(done.sum())}/{nf}", flush=True)
+            if checkpoint:
+                tmp = checkpoint + ".tmp.npz"
+                np.savez(tmp, key=key, done=done, S=S, gam=gam, zl=zl, zr=zr, res=res)
+                os.replace(tmp, checkpoint)
+        info = dict(seconds=time.time() - t0, refine_steps=steps)
+        return SweepResult(freqs, S, zr, gam, zl, res, [p.name for p in self.ports],
+                           cur if keep_currents else None, info)
+
+    def close(self):
+        for h in (self._ports, self._geom):
+            if h is not None:
+                h.close()
+        self._ports = self._geom = None
+        self.ctx.close()
+
+
+def assemble(solver, freq, precision="fp64"):
+    """mom25d's assemble(mesh, greens, zs, geom=...) for a Solver's mesh: the
+    impedance matrix at freq (host array)."""
+    return solver.impedance(freq, precision=precision)
+
+
+_default_ctx = None
+
+
+def dense_solve(Z, B, precision="fp64", ctx=None, tol=1e-12, max_iter=20):
+    """Z X = B on the GPU (mom25d's _dense_solve): LU with partial pivoting in
+    fp64, or complex64 LU + fp64 iterative refinement ("mixed"). Z is
+    complex128 (or complex64 for "mixed": the complex64 fill)."""
+    global _default_ctx
+    if ctx is None:
+        if _default_ctx is None:
+            _default_ctx = E.Context(0)
+        ctx = _default_ctx
+    Z = np.ascontiguousarray(Z)
+    n = Z.shape[0]
+    B = np.ascontiguousarray(np.asarray(B).reshape(n, -1), np.complex128)
+    X = np.zeros_like(B)
+    if precision == "fp64":
+        prec = E.M25_FP64
+        Z = np.ascontiguousarray(Z, np.complex128)
+    elif Z.dtype == np.complex64:
+        prec = E.M25_MIXED
+    else:
+        prec = 2
+        Z = np.ascontiguousarray(Z, np.complex128)
+    info = np.zeros(2, np.int32)
+    E.check(ctx.lib.m25_dense_solve(ctx.h, n, B.shape[1], prec, Z.ctypes.data, B.ctypes.data, X.ctypes.data,
+                                    E.M25_ON_HOST, tol, max_iter, E.ptr(info, C.c_int32)))
+    return X

@@ -1,0 +1,131 @@
+"""The sweep workloads this engine is measured and checked on.
+
+Each builder takes an `api` namespace with mom25d's layout classes
+(`Layout`, `Substrate`, `Stackup`, `Dielectric`, `CoplanarGround`) so the
+same geometry can be built with this package or with mom25d itself, and
+returns (layout, stack, mesh keyword arguments, frequencies [Hz]).
+
+  tee        open-stub tee, eps_r 3.55 / 0.508 mm, mesh 0.5/0.08 mm, 37 f 1-10 GHz (N = 1085)
+  lpf        7-section stepped-impedance low-pass 4.0/0.3 mm (seeded lengths), 101 f 0.5-8 GHz;
+             mesh 0.35/0.05 mm gives N = 5943, the N ~ 6k headline case
+  bandpass   seeded edge-coupled-line band-pass variants, 128 f 1-12 GHz
+  via        two-layer microstrip -> via -> inner line, 2 x 0.254 mm eps_r 3.66 (N = 3789)
+  gcpw       30 mm grounded CPW with via fences on 0.508 mm eps_r 3.55, 64 f 1-20 GHz
+  line       short through line (small N, test case)
+  shunt_via  short line with a via to ground (small N, test case)
+"""
+
+import numpy as np
+
+mm = 1e-3
+GHz = 1e9
+ER, H, TAND, SIGMA = 3.55, 0.508 * mm, 0.0027, 5.8e7
+
+
+def tee(api):
+    W = 1.137 * mm
+    lay = api.Layout()
+    lay.add_rect(-W / 2 - 2 * mm, -W / 2, W / 2 + 2 * mm, W / 2)
+    lay.add_rect(-W / 2, W / 2, W / 2, W / 2 + 6.6 * mm)
+    lay.add_port("P1", ref=(-W / 2 - 2 * mm, 0), direction="-x", width=W, length=15 * mm)
+    lay.add_port("P2", ref=(W / 2 + 2 * mm, 0), direction="+x", width=W, length=15 * mm)
+    sub = api.Substrate(eps_r=ER, h=H, tand=TAND, sigma=SIGMA)
+    return lay, sub, dict(max_cell=0.5 * mm, edge_cell=0.08 * mm), np.linspace(1, 10, 37) * GHz
+
+
+def lpf(api, max_cell=0.35 * mm, edge_cell=0.05 * mm, seed=0):
+    widths = [4.0 * mm if k % 2 == 0 else 0.3 * mm for k in range(7)]
+    lengths = np.random.default_rng(seed).uniform(2.5, 5.0, 7) * mm
+    lay = api.Layout()
+    x = 0.0
+    for w, l in zip(widths, lengths):
+        lay.add_rect(x, -w / 2, x + l, w / 2)
+        x += l
+    W0 = 1.1366 * mm
+    lay.add_port("P1", (0.0, 0.0), "-x", W0, 15 * mm)
+    lay.add_port("P2", (x, 0.0), "+x", W0, 15 * mm)
+    sub = api.Substrate(eps_r=ER, h=H, tand=TAND, sigma=SIGMA)
+    return lay, sub, dict(max_cell=max_cell, edge_cell=edge_cell), np.linspace(0.5, 8, 101) * GHz
+
+
+def bandpass(api, k=0, max_cell=None, edge_cell=0.05 * mm):
+    """Edge-coupled half-wave band-pass variant k: gap U(0.1, 0.4) mm,
+    width U(0.8, 1.4) mm, 3-5 coupled sections, each a pair of
+    quarter-wave-long rectangles offset along x."""
+    rng = np.random.default_rng(k)
+    gap = rng.uniform(0.1, 0.4) * mm
+    W = rng.uniform(0.8, 1.4) * mm
+    nsec = int(rng.integers(3, 6))
+    L = 4.2 * mm  # ~quarter wave at 10 GHz on eps_eff ~2.7
+    lay = api.Layout()
+    x, y = 0.0, 0.0
+    W0 = 1.1366 * mm
+    for s in range(nsec + 1):
+        lay.add_rect(x, y - W / 2, x + 2 * L, y + W / 2)
+        x += L
+        y += W + gap
+    lay.add_port("P1", (0.0, 0.0), "-x", W, 8 * mm)
+    lay.add_port("P2", (x + L, y - W - gap), "+x", W, 8 * mm)
+    sub = api.Substrate(eps_r=ER, h=H, tand=TAND, sigma=SIGMA)
+    mc = max_cell if max_cell is not None else 0.45 * mm
+    return lay, sub, dict(max_cell=mc, edge_cell=edge_cell), np.linspace(1, 12, 128) * GHz
+
+
+def via(api):
+    ER2, H1, H2 = 3.66, 0.254 * mm, 0.254 * mm
+    WT, WI = 1.1122 * mm, 0.45 * mm
+    REF, FEED = 3 * mm, 12 * mm
+    lay = api.Layout()
+    lay.add_rect(-REF, -WT / 2, 0, WT / 2, layer="top")
+    lay.add_rect(0, -WI / 2, REF, WI / 2, layer="inner")
+    lay.add_port("P1", (-REF, 0), "-x", WT, FEED, layer="top")
+    lay.add_port("P2", (REF, 0), "+x", WI, FEED, layer="inner")
+    lay.add_via(0, 0, drill=0.3 * mm, pad=0.6 * mm, top="top", bottom="inner")
+    st = api.Stackup([api.Dielectric(H1, ER2, 0.0037), api.Dielectric(H2, ER2, 0.0037)],
+                     {"inner": 1, "top": 2}, sigma=SIGMA)
+    return lay, st, dict(max_cell=0.2 * mm, edge_cell=0.05 * mm), np.linspace(1, 20, 20) * GHz
+
+
+def gcpw(api, max_cell=0.15 * mm, edge_cell=0.04 * mm):
+    W, G, WG = 1.137 * mm, 0.2 * mm, 1.2 * mm
+    lay = api.Layout()
+    lay.add_rect(-15 * mm, -W / 2, 15 * mm, W / 2)
+    for sg in (1, -1):
+        y0 = sg * (W / 2 + G)
+        lay.add_rect(-15 * mm, y0, 15 * mm, y0 + sg * WG)
+        for x in np.arange(-14.5, 15.0, 1.0) * mm:
+            lay.add_via(x, y0 + sg * WG / 2, drill=0.3 * mm, pad=0.5 * mm)
+    cg = api.CoplanarGround(G, WG, via_pitch=1 * mm, via_drill=0.3 * mm, via_pad=0.5 * mm)
+    lay.add_port("P1", (-15 * mm, 0), "-x", W, 6 * mm, ground=cg)
+    lay.add_port("P2", (15 * mm, 0), "+x", W, 6 * mm, ground=cg)
+    sub = api.Substrate(eps_r=ER, h=H, tand=TAND, sigma=SIGMA)
+    return lay, sub, dict(max_cell=max_cell, edge_cell=edge_cell), np.linspace(1, 20, 64) * GHz
+
+
+def line(api, length=4 * mm, cell=0.5 * mm):
+    W = 1.137 * mm
+    lay = api.Layout()
+    lay.add_rect(0, -W / 2, length, W / 2)
+    lay.add_port("P1", (0, 0), "-x", W, 8 * mm)
+    lay.add_port("P2", (length, 0), "+x", W, 8 * mm)
+    sub = api.Substrate(eps_r=ER, h=H, tand=TAND, sigma=SIGMA)
+    return lay, sub, dict(max_cell=cell, edge_cell=0.15 * mm), np.array([2.0, 7.0]) * GHz
+
+
+def shunt_via(api):
+    W = 0.5561 * mm
+    lay = api.Layout()
+    lay.add_rect(-2 * mm, -W / 2, 2 * mm, W / 2)
+    lay.add_port("P1", (-2 * mm, 0), "-x", W, 4 * mm)
+    lay.add_port("P2", (2 * mm, 0), "+x", W, 4 * mm)
+    lay.add_via(0, 0, drill=0.3 * mm, pad=W)
+    sub = api.Substrate(3.66, 0.254 * mm, 0.003, SIGMA)
+    return lay, sub, dict(max_cell=0.35 * mm, edge_cell=0.08 * mm), np.array([3.0, 9.0]) * GHz
+
+
+BUILDERS = dict(tee=tee, lpf=lpf, bandpass=bandpass, via=via, gcpw=gcpw, line=line, shunt_via=shunt_via)
+
+
+def build(api, name, **kw):
+    lay, stack, mkw, freqs = BUILDERS[name](api, **kw)
+    return lay, stack, lay.mesh(**mkw), freqs

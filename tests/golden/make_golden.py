@@ -1,0 +1,148 @@
+"""Generate the golden fixtures of this directory by running mom25d itself.
+
+Run in a container where the mom25d sources are importable (they are read
+from /root/reference/Engine); the fixtures are committed so that tests on
+machines without mom25d compare against them:
+
+    python tests/golden/make_golden.py [--quick]
+
+Every case uses the sweep settings the parity tests assume: method="dense"
+(dense LU) and interp=None (an exact fill at every frequency).
+"""
+
+import argparse
+import hashlib
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", ".."))
+sys.path.insert(0, "/root/reference/Engine")
+
+import mom25d as ref  # noqa: E402
+from mom25d import solver as ref_solver  # noqa: E402
+from mom25d.integrals import potential_integrals  # noqa: E402
+
+from mom25d_gb300 import workloads  # noqa: E402
+
+
+def mesh_digest(m):
+    h = hashlib.sha256()
+    for a in (m.nodes, m.tris, m.tri_basis, m.tri_sign, m.edge_len, m.tri_layer):
+        h.update(np.ascontiguousarray(a).tobytes())
+    for s in m.via_segments:
+        h.update(repr((s["via"], s["top"], s["bottom"])).encode())
+        for k in ("top_tris", "bottom_tris"):
+            if s[k] is not None:
+                h.update(np.asarray(s[k], np.int64).tobytes())
+    return h.hexdigest()
+
+
+def solve_point(sol, f):
+    """Everything the sweep computes at one frequency, step by step."""
+    g = sol.greens(f)
+    Z = sol.impedance(f, g)
+    x = sol.solve_currents(f, greens=g, Z=Z.copy())
+    q = sol.charges(x, g.omega)
+    return g, Z, x, q
+
+
+def sweep(sol, freqs):
+    t = time.time()
+    r = sol.sweep(freqs, interp=None)
+    return r, time.time() - t
+
+
+def result_arrays(r, prefix=""):
+    return {prefix + "S": r.S, prefix + "z0": r.z0, prefix + "gamma": r.gamma, prefix + "z0_line": r.z0_line,
+            prefix + "fit_residual": r.fit_residual, prefix + "S50": r.renormalize(50)}
+
+
+def case(name, freqs_full=None, zfull=False, zrows=None, sweep_freqs=None, kw=None):
+    lay, stack, mkw, freqs = workloads.BUILDERS[name](ref, **(kw or {}))
+    m = lay.mesh(**mkw)
+    sol = ref.Solver(m, stack, verbose=False, method="dense")
+    out = dict(N=m.n_unknowns, Nt=len(m.tris), mesh_sha=mesh_digest(m), rho_max=sol.rho_max)
+    f0 = freqs[0] if sweep_freqs is None else sweep_freqs[0]
+    g, Z, x, q = solve_point(sol, f0)
+    out["f0"] = f0
+    if zfull:
+        out["Z"] = Z
+    if zrows is not None:
+        rows = np.unique(np.r_[zrows, m.n_unknowns - 1])
+        out["Z_rows_idx"] = rows
+        out["Z_rows"] = Z[rows]
+        out["Z_diag"] = np.diag(Z).copy()
+    out["x"] = x
+    out["q"] = q
+    if sol.single:
+        out["rho_tab"] = g.rho_tab
+        out["SA_tab"], out["SV_tab"], out["SW_tab"] = g.SA_tab, g.SV_tab, g.SW_tab
+        out["spl_c"], out["splw_c"] = g._spl.c, g._splw.c
+        out["cv"] = g.cv
+    else:
+        out["rho_tab"] = g.rho_tab
+        L = len(g.levels)
+        for i in range(L):
+            for j in range(L):
+                p = g.pair(i, j)
+                out[f"pair{i}{j}_c"] = np.array([p.cA, p.cV, p.cW], complex)
+                out[f"pair{i}{j}_dz"] = p.dz
+                out[f"pair{i}{j}_spl_c"] = p._spl.c
+                out[f"pair{i}{j}_splw_c"] = p._splw.c
+    sf = freqs if sweep_freqs is None else np.asarray(sweep_freqs)
+    r, dt = sweep(sol, sf)
+    out["freqs"] = sf
+    out["sweep_seconds"] = dt
+    out.update(result_arrays(r))
+    np.savez_compressed(os.path.join(HERE, f"{name}{'_' + str(kw['k']) if kw and 'k' in kw else ''}.npz"), **out)
+    print(f"{name}: N={m.n_unknowns} Nt={len(m.tris)} {len(sf)} freqs {dt:.1f} s ({dt / len(sf):.2f} s/pt)", flush=True)
+
+
+def kernels():
+    """Known-answer vectors for the closed-form integrals and the slab kernels."""
+    rng = np.random.default_rng(1)
+    V = rng.uniform(-1e-3, 1e-3, (6, 3, 2))
+    e1, e2 = V[:, 1] - V[:, 0], V[:, 2] - V[:, 0]
+    cw = (e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0]) < 0
+    V[cw] = V[cw][:, [0, 2, 1]]
+    r = rng.uniform(-2e-3, 2e-3, (9, 2))
+    r[0] = V[0, 0]  # observer on a vertex
+    r[1] = 0.5 * (V[1, 0] + V[1, 1])  # on an edge
+    out = dict(V=V, r=r)
+    for d in (0.0, 0.254e-3):
+        I0, I1 = potential_integrals(V, r, d)
+        out[f"I0_{d:g}"], out[f"I1_{d:g}"] = I0, I1
+    g = ref.GroundedSlabGreens(5e9, 3.55, 0.508e-3, 0.0027, rho_max=0.03, zs_ground=0.02 + 0.02j)
+    R = np.geomspace(1e-6, 0.03, 40)
+    out["slab_R"] = R
+    out["slab_gA"], out["slab_gV"], out["slab_gW"] = g.gA(R), g.gV(R), g.gW(R)
+    out["slab_rho_tab"] = g.rho_tab
+    out["slab_SA"], out["slab_SV"], out["slab_SW"] = g.SA_tab, g.SV_tab, g.SW_tab
+    L = ref_solver.via_inductance([ref.Via((0, 0), 0.3e-3), ref.Via((1e-3, 0.2e-3), 0.2e-3)], 0.508e-3)
+    out["via_L"] = L
+    np.savez_compressed(os.path.join(HERE, "kernels.npz"), **out)
+    print("kernels: done", flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--quick", action="store_true", help="small cases only")
+    args = ap.parse_args()
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "4")
+    kernels()
+    case("line", zrows=np.arange(0, 546, 37))
+    case("shunt_via", zrows=np.arange(0, 492, 41))
+    if args.quick:
+        return
+    case("tee", zrows=np.arange(0, 1085, 97))
+    case("via", zrows=np.arange(0, 3789, 379), sweep_freqs=[2e9, 10e9, 18e9])
+    case("bandpass", kw=dict(k=0), zrows=np.arange(0, 1524, 211), sweep_freqs=[3e9, 9e9])
+    case("lpf", zrows=np.arange(0, 5943, 743), sweep_freqs=[0.5e9, 4e9, 8e9])
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,130 @@
+"""CPU tests: the grid mesher and the oracle against fixtures generated by
+running mom25d itself (tests/golden/make_golden.py)."""
+
+import hashlib
+
+import numpy as np
+import pytest
+
+import mom25d_gb300 as G
+from mom25d_gb300 import workloads
+from oracle import kernels as K
+from oracle import sweep as O
+
+from conftest import golden
+
+
+def mesh_digest(m):
+    h = hashlib.sha256()
+    for a in (m.nodes, m.tris, m.tri_basis, m.tri_sign, m.edge_len, m.tri_layer):
+        h.update(np.ascontiguousarray(a).tobytes())
+    for s in m.via_segments:
+        h.update(repr((s["via"], s["top"], s["bottom"])).encode())
+        for k in ("top_tris", "bottom_tris"):
+            if s[k] is not None:
+                h.update(np.asarray(s[k], np.int64).tobytes())
+    return h.hexdigest()
+
+
+@pytest.mark.parametrize("name", ["line", "shunt_via", "tee", "via", "lpf", "bandpass_0"])
+def test_mesh_identical_to_reference(name):
+    g = golden(name)
+    base = name.split("_")[0] if name.startswith("bandpass") else name
+    kw = {"k": 0} if name.startswith("bandpass") else {}
+    lay, st, m, _ = workloads.build(G, base, **kw)
+    stack = st if hasattr(st, "layers") else st.to_stackup()
+    m.assign_levels(sorted(m.layer_names, key=stack.level_z))
+    assert m.n_unknowns == int(g["N"]) and len(m.tris) == int(g["Nt"])
+    assert mesh_digest(m) == str(g["mesh_sha"])
+
+
+def test_potential_integrals_known_answers():
+    g = golden("kernels")
+    for d in (0.0, 0.254e-3):
+        I0, I1 = K.potential_integrals(g["V"], g["r"], d)
+        np.testing.assert_allclose(I0, g[f"I0_{d:g}"], rtol=1e-13, atol=1e-20)
+        np.testing.assert_allclose(I1, g[f"I1_{d:g}"], rtol=1e-13, atol=1e-20)
+
+
+def test_potential_integrals_vs_brute_force():
+    """Closed form against a fine midpoint rule (the reference's own check, 2e-3)."""
+    V = np.array([[[0, 0], [1.0, 0.2], [0.3, 0.9]]])
+    r = np.array([[0.4, 0.3], [2.0, -0.5], [0.5, 0.1]])
+    I0, I1 = K.potential_integrals(V, r)
+    n = 600
+    u, v = np.meshgrid((np.arange(n) + 0.5) / n, (np.arange(n) + 0.5) / n)
+    msk = u + v < 1
+    e1, e2 = V[0, 1] - V[0, 0], V[0, 2] - V[0, 0]
+    P = V[0, 0] + u[msk, None] * e1 + v[msk, None] * e2
+    w = 0.5 * abs(e1[0] * e2[1] - e1[1] * e2[0]) / msk.sum()
+    for k in range(len(r)):
+        d = P - r[k]
+        R = np.hypot(d[:, 0], d[:, 1])
+        assert I0[0, k] == pytest.approx((w / R).sum(), rel=4e-3)
+
+
+def test_slab_kernels_match_reference():
+    g = golden("kernels")
+    s = K.SlabKernels(5e9, 3.55, 0.508e-3, 0.0027, rho_max=0.03, zs_ground=0.02 + 0.02j)
+    np.testing.assert_array_equal(s.rho_tab, g["slab_rho_tab"])
+    for a, b in ((s.SA, g["slab_SA"]), (s.SV, g["slab_SV"]), (s.SW, g["slab_SW"])):
+        assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max()
+    R = g["slab_R"]
+    p = s.pair()
+    for a, b in ((p.gA(R), g["slab_gA"]), (p.gV(R), g["slab_gV"]), (p.gW(R), g["slab_gW"])):
+        assert np.max(np.abs(a - b) * 4 * np.pi * R) < 1e-12
+
+
+def test_air_slab_equals_images():
+    """eps_r = 1 over ground: source plus negative image (the reference's test, 1e-6)."""
+    h = 0.5e-3
+    for f in (1e9, 10e9):
+        s = K.SlabKernels(f, 1.0, h, rho_max=0.06)
+        k = s.k0
+        R = np.array([1e-5, 1e-4, 5e-4, 2e-3, 1e-2, 0.03, 0.06])
+        R2 = np.sqrt(R ** 2 + 4 * h ** 2)
+        exact = (np.exp(-1j * k * R) / R - np.exp(-1j * k * R2) / R2) / (4 * np.pi)
+        p = s.pair()
+        assert np.max(np.abs(p.gA(R) - exact) * 4 * np.pi * R) < 1e-6
+        assert np.max(np.abs(p.gV(R) - exact) * 4 * np.pi * R) < 1e-6
+
+
+def test_layered_one_layer_equals_slab():
+    f = 3e9
+    s = K.SlabKernels(f, 3.55, 0.508e-3, 0.002, rho_max=0.04)
+    lk = K.LayeredKernels(f, [(0.508e-3, 3.55, 0.002)], [1], [0.508e-3], rho_max=0.04)
+    R = np.array([1e-5, 1e-4, 5e-4, 2e-3, 1e-2, 0.03])
+    for a, b in ((lk.pair(0, 0).gA(R), s.pair().gA(R)), (lk.pair(0, 0).gV(R), s.pair().gV(R)),
+                 (lk.pair(0, 0).gW(R), s.pair().gW(R))):
+        assert np.max(np.abs(a - b) * 4 * np.pi * R) < 1e-12
+
+
+def test_via_inductance_known_answer():
+    g = golden("kernels")
+    vias = [G.Via((0, 0), 0.3e-3), G.Via((1e-3, 0.2e-3), 0.2e-3)]
+    spans = np.array([[0.0, 0.508e-3], [0.0, 0.508e-3]])
+    L = O.via_block_L(vias, spans, (0.0, 0.508e-3))
+    np.testing.assert_allclose(L, g["via_L"], rtol=1e-13)
+
+
+@pytest.mark.parametrize("name", ["line", "shunt_via"])
+def test_oracle_fill_and_sweep_match_reference(name):
+    g = golden(name)
+    lay, st, m, _ = workloads.build(G, name)
+    sw = O.Sweep(m, st)
+    f0 = float(g["f0"])
+    Z = sw.impedance(f0)
+    if "Z" in g.files:
+        assert np.abs(Z - g["Z"]).max() <= 1e-13 * np.abs(g["Z"]).max()
+    else:
+        rows = g["Z_rows_idx"]
+        assert np.abs(Z[rows] - g["Z_rows"]).max() <= 1e-13 * np.abs(g["Z_rows"]).max()
+        assert np.abs(np.diag(Z) - g["Z_diag"]).max() <= 1e-13 * np.abs(g["Z_diag"]).max()
+    x = O.dense_solve(Z.copy(), sw.excitations())
+    # the currents agree to ~cond(Z) x 1e-16 (cond ~1e7 with the shunt via)
+    assert np.abs(x - g["x"]).max() <= 1e-8 * np.abs(g["x"]).max()
+    S, z0, gam, zl, res = sw.sweep(g["freqs"])
+    # the reference's own Nelder-Mead wave fit moves gamma by ~4e-8 under 1e-15
+    # perturbations of its inputs: S agrees to that floor, not to 1e-9
+    assert np.abs(S - g["S"]).max() < 1e-6
+    assert np.abs(gam - g["gamma"]).max() < 1e-6 * np.abs(g["gamma"]).max()

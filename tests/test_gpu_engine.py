@@ -1,0 +1,233 @@
+"""GPU parity tests: the CUDA engine against the CPU oracle and against
+fixtures made by running mom25d (tests/golden). Tolerances are written in
+each test; fp64 stages must agree to rounding, the mixed path to 1e-5 in S.
+"""
+
+import numpy as np
+import pytest
+
+import mom25d_gb300 as G
+from mom25d_gb300 import workloads
+from mom25d_gb300.solver import Solver, dense_solve
+from oracle import sweep as O
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def build(name, **kw):
+    lay, st, m, freqs = workloads.build(G, name, **kw)
+    return lay, st, m, freqs
+
+
+@pytest.fixture(scope="module")
+def line(gpu):
+    lay, st, m, freqs = build("line")
+    sol = Solver(m, st, verbose=False)
+    yield sol, O.Sweep(m, st)
+    sol.close()
+
+
+@pytest.fixture(scope="module")
+def shunt(gpu):
+    lay, st, m, freqs = build("shunt_via")
+    sol = Solver(m, st, verbose=False)
+    yield sol, O.Sweep(m, st)
+    sol.close()
+
+
+# ---------------------------------------------------------------- Green's tables
+@pytest.mark.parametrize("f", [0.5e9, 7e9, 20e9])
+def test_slab_tables_match_oracle(line, f):
+    sol, ref = line
+    g = sol.greens(f)
+    S, c, coef = g.tables()
+    k = ref.kernels(f)
+    np.testing.assert_array_equal(g.rho, k.rho_tab)
+    for m, tab in enumerate((k.SA, k.SV, k.SW)):
+        err = np.abs(S[m, 0, 0] - tab).max() / np.abs(tab).max()
+        assert err < 1e-12, (m, err)
+    # cubic coefficients against scipy's not-a-knot spline
+    c_ref = k.pair().spl.c  # (4, n-1, 2)
+    for m in range(2):
+        err = np.abs(coef[0, :, :, m] - c_ref[:, :, m].T).max() / np.abs(c_ref[:, :, m]).max()
+        assert err < 1e-9, (m, err)
+    np.testing.assert_allclose(c[1, 0, 0], k.cv, rtol=1e-15)
+    g.close()
+
+
+def test_layered_tables_match_oracle(gpu):
+    lay, st, m, _ = build("via")
+    sol = Solver(m, st, verbose=False)
+    ref = O.Sweep(m, st)
+    f = 10e9
+    g = sol.greens(f)
+    S, c, coef = g.tables()
+    k = ref.kernels(f)
+    np.testing.assert_array_equal(g.rho, k.rho_tab)
+    L = len(m.layer_names)
+    for i in range(L):
+        for j in range(L):
+            p = k.pair(i, j)
+            np.testing.assert_allclose(c[:, i, j], [p.cA, p.cV, p.cW], rtol=1e-12, atol=1e-14)
+            for mm, tab in enumerate((p.spl(g.rho)[:, 0], p.spl(g.rho)[:, 1], p.splw(g.rho))):
+                err = np.abs(S[mm, i, j] - tab).max() / np.abs(tab).max()
+                assert err < 1e-11, (i, j, mm, err)
+    g.close()
+    sol.close()
+
+
+# ------------------------------------------------------------------------ fill
+@pytest.mark.parametrize("f", [2e9, 7e9])
+def test_fill_fp64_matches_oracle(line, f):
+    sol, ref = line
+    Z = sol.impedance(f)
+    Zo = ref.impedance(f)
+    assert np.abs(Z - Zo).max() <= 1e-12 * np.abs(Zo).max()
+    assert np.abs(Z - Z.T).max() == 0.0  # symmetric by construction
+
+
+def test_fill_with_via_matches_oracle(shunt):
+    sol, ref = shunt
+    f = 3e9
+    Z = sol.impedance(f)
+    Zo = ref.impedance(f)
+    scale = np.abs(Zo).max()
+    nb = sol.mesh.n_basis
+    assert np.abs(Z[:nb, :nb] - Zo[:nb, :nb]).max() <= 1e-12 * scale
+    # via rows and the via-via block
+    assert np.abs(Z[nb:] - Zo[nb:]).max() <= 1e-11 * np.abs(Zo[nb:]).max()
+
+
+@pytest.mark.parametrize("name", ["tee", "via", "bandpass_0", "lpf"])
+def test_fill_fp64_matches_reference_rows(gpu, name):
+    g = golden(name)
+    base = "bandpass" if name.startswith("bandpass") else name
+    kw = {"k": 0} if name.startswith("bandpass") else {}
+    lay, st, m, _ = build(base, **kw)
+    sol = Solver(m, st, verbose=False)
+    Z = sol.impedance(float(g["f0"]))
+    rows = g["Z_rows_idx"]
+    assert np.abs(Z[rows] - g["Z_rows"]).max() <= 1e-11 * np.abs(g["Z_rows"]).max()
+    assert np.abs(np.diag(Z) - g["Z_diag"]).max() <= 1e-11 * np.abs(g["Z_diag"]).max()
+    sol.close()
+
+
+def test_fill_mixed_close_to_fp64(line):
+    sol, _ = line
+    f = 7e9
+    Z64 = sol.impedance(f, precision="fp64")
+    Z32 = sol.impedance(f, precision="mixed")
+    assert Z32.dtype == np.complex64
+    assert np.abs(Z32 - Z64).max() <= 3e-6 * np.abs(Z64).max()
+
+
+# ----------------------------------------------------------------------- solve
+@pytest.mark.parametrize("n", [1, 2, 63, 65, 130, 700])
+def test_dense_solve_fp64_vs_lapack(gpu, n):
+    rng = np.random.default_rng(n)
+    A = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    A += n * np.eye(n) * (0.3 + 0.1j)
+    B = rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2))
+    X = dense_solve(A, B)
+    Xr = np.linalg.solve(A, B)
+    assert np.abs(X - Xr).max() <= 1e-12 * np.abs(Xr).max()
+
+
+def test_dense_solve_needs_pivoting(gpu):
+    # zero leading diagonal: partial pivoting is required
+    rng = np.random.default_rng(3)
+    n = 200
+    A = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    A[0, 0] = 0
+    A[:5, :5] = 0
+    B = rng.standard_normal((n, 1)) + 0j
+    X = dense_solve(A, B)
+    assert np.abs(A @ X - B).max() <= 1e-10 * np.abs(B).max()
+
+
+@pytest.mark.parametrize("n", [64, 300, 1000])
+def test_dense_solve_mixed_refines_to_fp64(gpu, n):
+    rng = np.random.default_rng(n + 1)
+    A = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    A += 3 * np.sqrt(n) * np.eye(n)
+    B = rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2))
+    X = dense_solve(A, B, precision="mixed", tol=1e-13)
+    Xr = np.linalg.solve(A, B)
+    assert np.abs(X - Xr).max() <= 1e-11 * np.abs(Xr).max()
+
+
+def test_singular_matrix_raises(gpu):
+    A = np.zeros((10, 10), complex)
+    with pytest.raises(RuntimeError):
+        dense_solve(A, np.ones((10, 1)))
+
+
+# --------------------------------------------------------------------- sweeps
+def test_line_sweep_fp64_matches_reference(line):
+    sol, ref = line
+    g = golden("line")
+    r = sol.sweep(g["freqs"])
+    # floor: the reference's own Nelder-Mead fit reproduces gamma to ~4e-8
+    assert np.abs(r.S - g["S"]).max() < 1e-6
+    assert np.abs(r.gamma - g["gamma"]).max() < 1e-6 * np.abs(g["gamma"]).max()
+    assert np.abs(r.z0 - g["z0"]).max() < 1e-5 * np.abs(g["z0"]).max()
+    assert np.abs(r.renormalize(50) - g["S50"]).max() < 1e-6
+
+
+def test_deembed_stages_match_oracle(line):
+    sol, ref = line
+    f = 7e9
+    S, z0, gam, zl, res, x, _ = sol.point(f, keep_currents=True)
+    q, phi, I, V = sol.last_deembed()
+    k = ref.kernels(f)
+    Zo = ref.impedance(f, k)
+    xo = O.dense_solve(Zo, ref.excitations())
+    assert np.abs(x - xo).max() <= 1e-10 * np.abs(xo).max()
+    qo = O.charges(sol.mesh, x, 2 * np.pi * f)
+    assert np.abs(q - qo).max() <= 1e-12 * np.abs(qo).max()
+    pts = np.concatenate([pm.vpts for pm in ref.pm])
+    phio = O.line_voltage(sol.mesh, k, q, pts, "top")
+    assert np.abs(phi - phio).max() <= 1e-11 * np.abs(phio).max()
+    Io = np.concatenate([pm.currents(x) for pm in ref.pm])
+    assert np.abs(I - Io).max() <= 1e-13 * np.abs(Io).max()
+    So = ref.deembed(f, k, x, q)[0]
+    assert np.abs(S - So).max() < 1e-6
+
+
+def test_shunt_via_sweep_matches_reference(shunt):
+    sol, _ = shunt
+    g = golden("shunt_via")
+    r = sol.sweep(g["freqs"])
+    assert np.abs(r.S - g["S"]).max() < 1e-6
+
+
+def test_tee_sweep_matches_reference(gpu):
+    g = golden("tee")
+    lay, st, m, _ = build("tee")
+    idx = [0, 12, 24, 36]
+    for prec, tol in (("fp64", 1e-6), ("mixed", 1e-5)):
+        sol = Solver(m, st, verbose=False, precision=prec)
+        r = sol.sweep(g["freqs"][idx])
+        assert np.abs(r.S - g["S"][idx]).max() < tol, prec
+        sol.close()
+
+
+def test_via_transition_sweep_matches_reference(gpu):
+    g = golden("via")
+    lay, st, m, _ = build("via")
+    sol = Solver(m, st, verbose=False)
+    r = sol.sweep(g["freqs"])
+    assert np.abs(r.S - g["S"]).max() < 1e-6
+    sol.close()
+
+
+def test_bad_mesh_is_rejected(gpu):
+    lay, st, m, _ = build("line")
+    m.tri_basis = m.tri_basis.copy()
+    m.tri_basis[0, 0] = 10 ** 6
+    sol = Solver(m, st, verbose=False)
+    with pytest.raises(ValueError):
+        sol.geometry()
+    sol.close()
