@@ -38,7 +38,10 @@ enum {
   M25_ERR_NUMERIC = 4  /* singular matrix, non-converged refinement (RuntimeError) */
 };
 
-enum { M25_FP64 = 0, M25_MIXED = 1 };          /* arithmetic of fill + LU */
+/* Arithmetic of the path. M25_FP64: fp64 fill, fp64 LU. M25_MIXED: fp64 fill,
+ * complex64 LU, fp64 GMRES refinement against the fp64 Z. M25_MIXED_FILL32:
+ * fp32 fill (complex64 Z), complex64 LU, fp64 refinement against that Z. */
+enum { M25_FP64 = 0, M25_MIXED = 1, M25_MIXED_FILL32 = 2 };
 enum { M25_ON_HOST = 0, M25_ON_DEVICE = 1 };    /* where array arguments live */
 
 typedef struct m25_ctx m25_ctx;
@@ -130,8 +133,9 @@ int m25_greens_tables(m25_greens* g, double* S, double* c, double* coef);
 
 /* ----------------------------------------------------------------- fill */
 /* Z (n x n, n = nb + nv) of the MPIE Galerkin fill, symmetrised. precision
- * M25_FP64 writes complex128, M25_MIXED complex64 (fp32 arithmetic). Z is
- * host or device memory (where); ldz its row stride in elements. */
+ * M25_FP64 and M25_MIXED write complex128 (fp64 arithmetic), M25_MIXED_FILL32
+ * complex64 (fp32 arithmetic). Z is host or device memory (where); ldz its
+ * row stride in elements. */
 int m25_assemble(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, double zs_re, double zs_im,
                  double zsv_re, double zsv_im, int precision, void* Z, int64_t ldz, int where);
 
@@ -139,9 +143,10 @@ int m25_assemble(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, double zs_re, dou
 /* Z X = B for an n x n complex128 Z (overwritten by its LU factors when on
  * the device, as mom25d's _dense_solve overwrites Z) and nrhs right-hand
  * sides B (n x nrhs complex128, row-major). precision M25_FP64: LU with
- * partial pivoting in fp64; M25_MIXED: complex64 LU (tensor-core trailing
- * updates) and fp64 iterative refinement against Z to tol (relative
- * residual) in at most max_iter steps. info[0] = refinement steps taken,
+ * partial pivoting in fp64 (Z complex128); M25_MIXED: Z complex128, LU of its
+ * complex64 copy, fp64 GMRES refinement against Z until the normwise backward
+ * error |r| / (|Z| |x| + |b|) <= tol within max_iter GMRES steps;
+ * M25_MIXED_FILL32: the same with a complex64 Z. info[0] = GMRES steps,
  * info[1] = 0 or the first zero pivot (1-based). */
 int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precision, void* Z, const void* B, void* X,
                     int where, double tol, int32_t max_iter, int32_t* info);

@@ -162,11 +162,11 @@ extern "C" int m25_assemble(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, double
     return M25_ERR_VALUE;
   }
   M25_CUDA(cudaSetDevice(ctx->device));
-  if (precision == M25_FP64)
+  if (precision == M25_FP64 || precision == M25_MIXED)
     return fill_driver<double>(ctx, geom, gr, zd(zs_re, zs_im), zd(zsv_re, zsv_im), Z, ldz, where);
-  if (precision == M25_MIXED)
+  if (precision == M25_MIXED_FILL32)
     return fill_driver<float>(ctx, geom, gr, zd(zs_re, zs_im), zd(zsv_re, zsv_im), Z, ldz, where);
-  set_error("m25_assemble: precision must be M25_FP64 or M25_MIXED");
+  set_error("m25_assemble: unknown precision");
   return M25_ERR_VALUE;
 }
 
@@ -201,18 +201,18 @@ extern "C" int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precis
       return M25_ERR_NUMERIC;
     }
     if ((rc = lu_solve<double>(ctx, Zd, n, n, ctx->ipiv.as<int32_t>(), Bd, nrhs, Xd))) return rc;
-  } else if (precision == M25_MIXED || precision == 2) {
-    // M25_MIXED: Z is the complex64 fill; 2: Z is complex128 (cast for the LU)
+  } else if (precision == M25_MIXED || precision == M25_MIXED_FILL32) {
+    // M25_MIXED: Z complex128 (cast for the LU); M25_MIXED_FILL32: Z is the complex64 fill
     if ((rc = ctx->Zlu.ensure(sizeof(zf) * nn))) return rc;
     zf* LU = ctx->Zlu.as<zf>();
     const void* Zres = Z;
     if (where == M25_ON_HOST) {
-      size_t zb = (precision == M25_MIXED ? sizeof(zf) : sizeof(zd)) * nn;
+      size_t zb = (precision == M25_MIXED_FILL32 ? sizeof(zf) : sizeof(zd)) * nn;
       if ((rc = ctx->Zw.ensure(zb))) return rc;
       M25_CUDA(cudaMemcpyAsync(ctx->Zw.p, Z, zb, cudaMemcpyHostToDevice, st));
       Zres = ctx->Zw.p;
     }
-    if (precision == M25_MIXED)
+    if (precision == M25_MIXED_FILL32)
       M25_CUDA(cudaMemcpyAsync(LU, Zres, sizeof(zf) * nn, cudaMemcpyDeviceToDevice, st));
     else
       cast_to_z32(ctx, static_cast<const zd*>(Zres), n, LU, n, n, n);
@@ -222,7 +222,7 @@ extern "C" int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precis
       set_error("m25_dense_solve: zero pivot in the complex64 LU");
       return M25_ERR_NUMERIC;
     }
-    if (precision == M25_MIXED)
+    if (precision == M25_MIXED_FILL32)
       rc = refine<float>(ctx, n, nrhs, static_cast<const zf*>(Zres), n, LU, ctx->ipiv.as<int32_t>(), Bd, Xd, tol,
                          max_iter, &steps);
     else

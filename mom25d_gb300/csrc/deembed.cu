@@ -671,12 +671,12 @@ extern "C" int m25_sweep_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25
     set_error("m25_sweep_point: null argument");
     return M25_ERR_VALUE;
   }
-  if (precision != M25_FP64 && precision != M25_MIXED) {
-    set_error("m25_sweep_point: precision must be M25_FP64 or M25_MIXED");
+  if (precision != M25_FP64 && precision != M25_MIXED && precision != M25_MIXED_FILL32) {
+    set_error("m25_sweep_point: unknown precision");
     return M25_ERR_VALUE;
   }
   const int n = geom->nb + geom->nv, P = p->P;
-  const size_t esz = precision == M25_FP64 ? sizeof(zd) : sizeof(zf);
+  const size_t esz = precision == M25_MIXED_FILL32 ? sizeof(zf) : sizeof(zd);
   int rc;
   if ((rc = ctx->Zsweep.ensure(esz * (size_t)n * n))) return rc;
   if ((rc = ctx->Xsweep.ensure(sizeof(zd) * (size_t)n * P))) return rc;

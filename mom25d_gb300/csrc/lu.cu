@@ -594,52 +594,320 @@ template int lu_factor<float>(m25_ctx*, zf*, int64_t, int, int32_t*, int, bool, 
 template int lu_solve<double>(m25_ctx*, const zd*, int64_t, int, const int32_t*, const zd*, int, zd*);
 template int lu_solve<float>(m25_ctx*, const zf*, int64_t, int, const int32_t*, const zf*, int, zf*);
 
-// Mixed solve: LU32 of Z (already factored in Zlu), fp64 refinement against Zres.
+// ------------------------------------------------ GMRES iterative refinement
+// Right-hand sides are handled in lockstep (one column per rhs).
+
+// Y[t][c] = sum_k Z[t][k] X[k][c] in fp64, one warp per row
 template <class TZ>
-int refine(m25_ctx* ctx, int n, int nrhs, const cx<TZ>* Zres, int64_t ldz, const zf* LU, const int32_t* ipiv,
+__global__ void matvec_kernel(int n, int P, const cx<TZ>* __restrict__ Z, int64_t ldz, const zd* __restrict__ X,
+                              zd* __restrict__ Y) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  zd acc[8];
+  for (int t = lane; t < n; t += 32) {
+    cx<TZ> zz = Z[(int64_t)warp * ldz + t];
+    zd z(double(zz.re), double(zz.im));
+    for (int c = 0; c < P; ++c) acc[c] += z * X[(int64_t)t * P + c];
+  }
+  for (int c = 0; c < P; ++c) {
+    double re = acc[c].re, im = acc[c].im;
+    for (int o = 16; o; o >>= 1) {
+      re += __shfl_down_sync(0xffffffffu, re, o);
+      im += __shfl_down_sync(0xffffffffu, im, o);
+    }
+    if (lane == 0) Y[(int64_t)warp * P + c] = zd(re, im);
+  }
+}
+
+// h[i][c] = sum_t conj(V_i[t][c]) W[t][c] for i < nvec: one CTA per i
+__global__ void dots_kernel(int n, int P, const zd* __restrict__ V, int64_t vstride, const zd* __restrict__ W,
+                            zd* __restrict__ h) {
+  int i = blockIdx.x;
+  const zd* Vi = V + (int64_t)i * vstride;
+  zd acc[8];
+  for (int t = threadIdx.x; t < n; t += blockDim.x)
+    for (int c = 0; c < P; ++c) acc[c] += conj(Vi[(int64_t)t * P + c]) * W[(int64_t)t * P + c];
+  __shared__ double red[32][2];
+  for (int c = 0; c < P; ++c) {
+    double re = acc[c].re, im = acc[c].im;
+    for (int o = 16; o; o >>= 1) {
+      re += __shfl_down_sync(0xffffffffu, re, o);
+      im += __shfl_down_sync(0xffffffffu, im, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      red[threadIdx.x >> 5][0] = re;
+      red[threadIdx.x >> 5][1] = im;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double a = 0, b = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        a += red[w][0];
+        b += red[w][1];
+      }
+      h[i * P + c] = zd(a, b);
+    }
+    __syncthreads();
+  }
+}
+
+// W[t][c] -= sum_{i < nvec} V_i[t][c] h[i][c]
+__global__ void orth_update_kernel(int n, int P, int nvec, const zd* __restrict__ V, int64_t vstride,
+                                   const zd* __restrict__ h, zd* __restrict__ W) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)n * P) return;
+  int c = int(e % P);
+  zd s = W[e];
+  for (int i = 0; i < nvec; ++i) s -= V[(int64_t)i * vstride + e] * h[i * P + c];
+  W[e] = s;
+}
+
+// per-column squared 2-norms: out[c] (one CTA)
+__global__ void norms_kernel(int n, int P, const zd* __restrict__ W, double* __restrict__ out) {
+  double acc[8] = {};
+  for (int t = threadIdx.x; t < n; t += blockDim.x)
+    for (int c = 0; c < P; ++c) acc[c] += norm2(W[(int64_t)t * P + c]);
+  __shared__ double red[32];
+  for (int c = 0; c < P; ++c) {
+    double v = acc[c];
+    for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+      out[c] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// out[t][c] = in[t][c] * s[c] (s complex per column)
+__global__ void col_scale_kernel(int64_t n, int P, const zd* __restrict__ in, const zd* __restrict__ s,
+                                 zd* __restrict__ out) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n * P) out[e] = in[e] * s[e % P];
+}
+
+// X[t][c] += sum_i V_i[t][c] y[i][c]
+__global__ void combine_kernel(int n, int P, int nvec, const zd* __restrict__ V, int64_t vstride,
+                               const zd* __restrict__ y, zd* __restrict__ X) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)n * P) return;
+  int c = int(e % P);
+  zd s(0.0);
+  for (int i = 0; i < nvec; ++i) s += V[(int64_t)i * vstride + e] * y[i * P + c];
+  X[e] += s;
+}
+
+// max over rows of sum |Z[t][k]| (infinity norm), one warp per row + atomicMax on the bits
+template <class TZ>
+__global__ void rownorm_kernel(int n, const cx<TZ>* __restrict__ Z, int64_t ldz, unsigned long long* __restrict__ out) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  double s = 0;
+  for (int t = lane; t < n; t += 32) {
+    cx<TZ> z = Z[(int64_t)warp * ldz + t];
+    s += hypot(double(z.re), double(z.im));
+  }
+  for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) atomicMax(out, (unsigned long long)__double_as_longlong(s));  // s >= 0: bit order = value order
+}
+
+__global__ void z64_to_z32_scaled(int64_t n, const zd* __restrict__ a, double s, zf* __restrict__ o) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) o[e] = zf(float(a[e].re * s), float(a[e].im * s));
+}
+__global__ void z32_to_z64_scaled(int64_t n, const zf* __restrict__ a, double s, zd* __restrict__ o) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) o[e] = zd(double(a[e].re) * s, double(a[e].im) * s);
+}
+__global__ void maxabs_kernel(int64_t n, const zd* __restrict__ a, double* __restrict__ out) {
+  double m = 0;
+  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) m = fmax(m, cabs1(a[e]));
+  __shared__ double red[32];
+  for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, red[w]);
+    *out = r;
+  }
+}
+
+// Restarted GMRES in fp64 on Z x = B, left-preconditioned by the complex64 LU
+// (GMRES-based iterative refinement, Carson & Higham 2017): converges where
+// classical refinement with a low-precision LU stalls (cond(Z) u32 >~ 1).
+// tol: relative 2-norm residual per column; max_iter: total GMRES steps.
+template <class TZ>
+int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* LU, const int32_t* ipiv,
            const zd* B, zd* X, double tol, int max_iter, int* steps) {
   cudaStream_t st = ctx->stream;
-  size_t nn = (size_t)n * nrhs;
-  int rc = ctx->Rw.ensure(nn * sizeof(zd) + nn * 2 * sizeof(zf) + (n + 2) * sizeof(double));
+  const int m = std::min(30, std::max(1, max_iter));
+  const size_t np = (size_t)n * P;
+  int rc = ctx->Rw.ensure(sizeof(zd) * np * (m + 3) + sizeof(zf) * np * 2 + sizeof(double) * 64 +
+                          sizeof(zd) * (size_t)(m + 2) * P * 2);
   if (rc) return rc;
-  zd* R = ctx->Rw.as<zd>();
-  zf* r32 = reinterpret_cast<zf*>(R + nn);
-  zf* d32 = r32 + nn;
-  double* rmax = reinterpret_cast<double*>(d32 + nn);
-  double* gmax = rmax + n;
-  // |B| for the relative residual
-  double bmax = 0;
+  zd* V = ctx->Rw.as<zd>();           // (m+1) basis vectors
+  zd* W = V + np * (m + 1);           // work vector
+  zd* R = W + np;                     // residual
+  zf* r32 = reinterpret_cast<zf*>(R + np);
+  zf* d32 = r32 + np;
+  double* dsc = reinterpret_cast<double*>(d32 + np);  // scalars
+  zd* hdev = reinterpret_cast<zd*>(dsc + 64);
+  zd* ydev = hdev + (size_t)(m + 2) * P;
+  const unsigned g1 = (unsigned)((np + 255) / 256);
+  const unsigned gw = (unsigned)(((size_t)n * 32 + 255) / 256);
+  StageTimer tm(ctx, ST_REFINE);
+  // apply M^-1: out = LU32^-1 in (scaled to O(1) in complex64)
+  auto precond = [&](const zd* in, zd* out) -> int {
+    maxabs_kernel<<<1, 1024, 0, st>>>((int64_t)np, in, dsc);
+    double s = 0;
+    M25_CUDA(cudaMemcpyAsync(&s, dsc, sizeof(double), cudaMemcpyDeviceToHost, st));
+    M25_CUDA(cudaStreamSynchronize(st));
+    if (s == 0) s = 1;
+    z64_to_z32_scaled<<<g1, 256, 0, st>>>((int64_t)np, in, 1.0 / s, r32);
+    int r = lu_solve<float>(ctx, LU, n, n, ipiv, r32, P, d32);
+    if (r) return r;
+    z32_to_z64_scaled<<<g1, 256, 0, st>>>((int64_t)np, d32, s, out);
+    return M25_OK;
+  };
+  auto col_norms = [&](const zd* v, std::vector<double>& out) -> int {
+    norms_kernel<<<1, 1024, 0, st>>>(n, P, v, dsc);
+    out.assign(P, 0.0);
+    M25_CUDA(cudaMemcpyAsync(out.data(), dsc, sizeof(double) * P, cudaMemcpyDeviceToHost, st));
+    M25_CUDA(cudaStreamSynchronize(st));
+    for (auto& x : out) x = sqrt(x);
+    return M25_OK;
+  };
+  std::vector<double> bn, rn, xn;
+  if ((rc = col_norms(B, bn))) return rc;
+  double znorm = 0;
   {
-    std::vector<zd> hb(nn);
-    M25_CUDA(cudaMemcpyAsync(hb.data(), B, nn * sizeof(zd), cudaMemcpyDeviceToHost, st));
+    unsigned long long* zb = reinterpret_cast<unsigned long long*>(dsc + 32);
+    M25_CUDA(cudaMemsetAsync(zb, 0, sizeof(unsigned long long), st));
+    rownorm_kernel<TZ><<<gw, 256, 0, st>>>(n, Z, ldz, zb);
+    M25_CUDA(cudaMemcpyAsync(&znorm, zb, sizeof(double), cudaMemcpyDeviceToHost, st));
     M25_CUDA(cudaStreamSynchronize(st));
-    for (auto& v : hb) bmax = std::max(bmax, cabs1(v));
   }
-  if (bmax == 0) bmax = 1;
-  // X = 0: first pass solves B itself
-  M25_CUDA(cudaMemsetAsync(X, 0, nn * sizeof(zd), st));
-  *steps = 0;
-  for (int it = 0; it <= max_iter; ++it) {
+  double prev_worst = INFINITY;
+  M25_CUDA(cudaMemsetAsync(X, 0, np * sizeof(zd), st));
+  int total = 0;
+  std::vector<zd> hh((size_t)(m + 2) * P), H((size_t)(m + 1) * m * P), g((size_t)(m + 1) * P), cs(m * P), sn(m * P);
+  for (int outer = 0; outer < 50; ++outer) {
+    // true residual
+    matvec_kernel<TZ><<<gw, 256, 0, st>>>(n, P, Z, ldz, X, W);
     {
-      StageTimer tm(ctx, ST_REFINE);
-      residual_kernel<TZ><<<(n * 32 + 255) / 256, 256, 0, st>>>(n, nrhs, Zres, ldz, B, X, R, rmax);
-      max_reduce<<<1, 1024, 0, st>>>(n, rmax, gmax);
+      // R = B - W
+      std::vector<zd> minus1(P, zd(-1.0));
+      M25_CUDA(cudaMemcpyAsync(ydev, minus1.data(), sizeof(zd) * P, cudaMemcpyHostToDevice, st));
+      col_scale_kernel<<<g1, 256, 0, st>>>((int64_t)n, P, W, ydev, R);
+      M25_CUDA(cudaMemcpyAsync(W, B, np * sizeof(zd), cudaMemcpyDeviceToDevice, st));
+      combine_kernel<<<g1, 256, 0, st>>>(n, P, 0, V, (int64_t)np, ydev, W);
     }
-    double hmax = 0;
-    M25_CUDA(cudaMemcpyAsync(&hmax, gmax, sizeof(double), cudaMemcpyDeviceToHost, st));
-    M25_CUDA(cudaStreamSynchronize(st));
-    if (hmax / bmax <= tol) break;
-    if (it == max_iter) {
-      set_error("mixed solve: iterative refinement did not reach the tolerance");
+    // R = B - Z X : W holds B now, R holds -Z X
+    {
+      std::vector<zd> one(P, zd(1.0));
+      M25_CUDA(cudaMemcpyAsync(ydev, one.data(), sizeof(zd) * P, cudaMemcpyHostToDevice, st));
+      combine_kernel<<<g1, 256, 0, st>>>(n, P, 1, W, 0, ydev, R);  // R += W
+    }
+    if ((rc = col_norms(R, rn))) return rc;
+    if ((rc = col_norms(X, xn))) return rc;
+    // normwise backward error |r| / (|Z| |x| + |b|) per column
+    double worst = 0;
+    for (int c = 0; c < P; ++c) {
+      double den = znorm * xn[c] + bn[c];
+      worst = std::max(worst, den > 0 ? rn[c] / den : 0.0);
+    }
+    if (worst <= tol) break;
+    const bool stalled = worst > 0.5 * prev_worst;
+    if (total >= max_iter || stalled) {
+      if (worst <= 1e3 * tol && outer > 0) break;  // at the fp64 floor
+      set_error("mixed solve: GMRES refinement did not reach the tolerance (backward error " +
+                std::to_string(worst) + ")");
       return M25_ERR_NUMERIC;
     }
-    double s = 1.0 / hmax;  // keep the fp32 right-hand side O(1)
-    scale_to_z32<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(nn, R, s, r32);
-    rc = lu_solve<float>(ctx, LU, n, n, ipiv, r32, nrhs, d32);
-    if (rc) return rc;
-    axpy_z32<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(nn, d32, hmax, X);
-    *steps = it + 1;
+    prev_worst = worst;
+    // preconditioned start vector
+    if ((rc = precond(R, W))) return rc;
+    std::vector<double> beta;
+    if ((rc = col_norms(W, beta))) return rc;
+    {
+      std::vector<zd> inv(P);
+      for (int c = 0; c < P; ++c) inv[c] = zd(beta[c] > 0 ? 1.0 / beta[c] : 0.0);
+      M25_CUDA(cudaMemcpyAsync(ydev, inv.data(), sizeof(zd) * P, cudaMemcpyHostToDevice, st));
+      col_scale_kernel<<<g1, 256, 0, st>>>((int64_t)n, P, W, ydev, V);
+    }
+    std::fill(g.begin(), g.end(), zd(0.0));
+    for (int c = 0; c < P; ++c) g[c] = zd(beta[c]);
+    int k = 0;
+    for (; k < m && total < max_iter; ++k, ++total) {
+      zd* vk = V + np * k;
+      matvec_kernel<TZ><<<gw, 256, 0, st>>>(n, P, Z, ldz, vk, R);
+      if ((rc = precond(R, W))) return rc;
+      // classical Gram-Schmidt, twice
+      std::fill(hh.begin(), hh.end(), zd(0.0));
+      for (int pass = 0; pass < 2; ++pass) {
+        dots_kernel<<<k + 1, 256, 0, st>>>(n, P, V, (int64_t)np, W, hdev);
+        orth_update_kernel<<<g1, 256, 0, st>>>(n, P, k + 1, V, (int64_t)np, hdev, W);
+        std::vector<zd> tmp((size_t)(k + 1) * P);
+        M25_CUDA(cudaMemcpyAsync(tmp.data(), hdev, sizeof(zd) * tmp.size(), cudaMemcpyDeviceToHost, st));
+        M25_CUDA(cudaStreamSynchronize(st));
+        for (size_t i = 0; i < tmp.size(); ++i) hh[i] += tmp[i];
+      }
+      std::vector<double> wn;
+      if ((rc = col_norms(W, wn))) return rc;
+      {
+        std::vector<zd> inv(P);
+        for (int c = 0; c < P; ++c) inv[c] = zd(wn[c] > 0 ? 1.0 / wn[c] : 0.0);
+        M25_CUDA(cudaMemcpyAsync(ydev, inv.data(), sizeof(zd) * P, cudaMemcpyHostToDevice, st));
+        col_scale_kernel<<<g1, 256, 0, st>>>((int64_t)n, P, W, ydev, V + np * (k + 1));
+      }
+      double worst_est = 0;
+      for (int c = 0; c < P; ++c) {
+        // column k of the Hessenberg matrix, rotated by the previous Givens rotations
+        std::vector<zd> col(k + 2);
+        for (int i = 0; i <= k; ++i) col[i] = hh[(size_t)i * P + c];
+        col[k + 1] = zd(wn[c]);
+        for (int i = 0; i < k; ++i) {
+          zd a = col[i], b = col[i + 1];
+          zd cI = cs[(size_t)i * P + c], sI = sn[(size_t)i * P + c];
+          col[i] = conj(cI) * a + conj(sI) * b;
+          col[i + 1] = -sI * a + cI * b;
+        }
+        double r = sqrt(norm2(col[k]) + norm2(col[k + 1]));
+        zd cN = r > 0 ? col[k] / zd(r) : zd(1.0), sN = r > 0 ? col[k + 1] / zd(r) : zd(0.0);
+        cs[(size_t)k * P + c] = cN;
+        sn[(size_t)k * P + c] = sN;
+        col[k] = zd(r);
+        col[k + 1] = zd(0.0);
+        for (int i = 0; i <= k; ++i) H[((size_t)i * m + k) * P + c] = col[i];
+        zd gk = g[(size_t)k * P + c];
+        g[(size_t)k * P + c] = conj(cN) * gk;
+        g[(size_t)(k + 1) * P + c] = -sN * gk;
+        double est = cabs(g[(size_t)(k + 1) * P + c]) / (beta[c] > 0 ? beta[c] : 1.0);
+        worst_est = std::max(worst_est, beta[c] > 0 ? est : 0.0);
+      }
+      if (worst_est <= 1e-13) {
+        ++k;
+        ++total;
+        break;
+      }
+    }
+    // y = H^-1 g (upper triangular), X += V y
+    std::vector<zd> y((size_t)k * P, zd(0.0));
+    for (int c = 0; c < P; ++c)
+      for (int i = k - 1; i >= 0; --i) {
+        zd s = g[(size_t)i * P + c];
+        for (int j = i + 1; j < k; ++j) s -= H[((size_t)i * m + j) * P + c] * y[(size_t)j * P + c];
+        zd d = H[((size_t)i * m + i) * P + c];
+        y[(size_t)i * P + c] = (d.re != 0 || d.im != 0) ? s / d : zd(0.0);
+      }
+    M25_CUDA(cudaMemcpyAsync(ydev, y.data(), sizeof(zd) * y.size(), cudaMemcpyHostToDevice, st));
+    combine_kernel<<<g1, 256, 0, st>>>(n, P, k, V, (int64_t)np, ydev, X);
   }
+  *steps = total;
   M25_CHECK_LAUNCH();
   return M25_OK;
 }

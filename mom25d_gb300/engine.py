@@ -6,8 +6,11 @@ missing. Status codes map to the exceptions mom25d raises for the same
 conditions (ValueError, MemoryError, RuntimeError).
 """
 
+import atexit
 import ctypes as C
 import os
+import sys
+import weakref
 
 import numpy as np
 
@@ -15,7 +18,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libm25.so")
 
 M25_OK, M25_ERR_VALUE, M25_ERR_MEMORY, M25_ERR_CUDA, M25_ERR_NUMERIC = range(5)
-M25_FP64, M25_MIXED = 0, 1
+M25_FP64, M25_MIXED, M25_MIXED_FILL32 = 0, 1, 2
 M25_ON_HOST, M25_ON_DEVICE = 0, 1
 
 EXPORTS = ("m25_last_error", "m25_version", "m25_ctx_create", "m25_ctx_destroy", "m25_ctx_synchronize",
@@ -115,8 +118,12 @@ def f64(a):
     return np.ascontiguousarray(a, np.float64)
 
 
+_live_contexts = weakref.WeakSet()
+
+
 class Context:
-    """One engine context: a CUDA device and stream plus a reusable workspace."""
+    """One engine context: a CUDA device and stream plus a reusable workspace.
+    Device objects created in it (Handle) are released before it."""
 
     def __init__(self, device=0):
         self.lib = load()
@@ -124,34 +131,53 @@ class Context:
         check(self.lib.m25_ctx_create(int(device), C.byref(h)))
         self.h = h
         self.device = device
+        self.handles = weakref.WeakSet()
+        _live_contexts.add(self)
 
     def close(self):
         if getattr(self, "h", None):
+            for hd in list(self.handles):
+                hd.close()
             self.lib.m25_ctx_destroy(self.h)
             self.h = None
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             self.close()
-        except Exception:  # noqa: BLE001 - interpreter shutdown
+        except Exception:  # noqa: BLE001
             pass
 
     def synchronize(self):
         check(self.lib.m25_ctx_synchronize(self.h))
 
 
-class Handle:
-    """Owner of a device object (geometry, Green's tables, ports)."""
+@atexit.register
+def _close_all():
+    # before the CUDA runtime's own teardown
+    for c in list(_live_contexts):
+        try:
+            c.close()
+        except Exception:  # noqa: BLE001
+            pass
 
-    def __init__(self, ctx, h, destroy, keep=()):
-        self.ctx, self.h, self._destroy, self._keep = ctx, h, destroy, keep
+
+class Handle:
+    """Owner of a device object (geometry, Green's tables, ports) of a Context."""
+
+    def __init__(self, ctx, h, destroy):
+        self.ctx, self.h, self._destroy = ctx, h, destroy
+        ctx.handles.add(self)
 
     def close(self):
-        if self.h:
+        if self.h and self.ctx.h:
             self._destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:  # noqa: BLE001

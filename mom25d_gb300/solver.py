@@ -220,7 +220,7 @@ class SweepResult:
                 fh.write(f"{f:.9e} " + " ".join(f"{v.real:.9e} {v.imag:.9e}" for v in vals) + "\n")
 
 
-PRECISIONS = {"fp64": E.M25_FP64, "mixed": E.M25_MIXED}
+PRECISIONS = {"fp64": E.M25_FP64, "mixed": E.M25_MIXED, "mixed_fill32": E.M25_MIXED_FILL32}
 
 
 class Solver:
@@ -230,16 +230,18 @@ class Solver:
                 package's grid mesher, or mom25d's own Mesh object)
     substrate : Substrate or Stackup (open top, no inner planes)
     method    : "dense" (the only method of this engine; "auto" maps to it)
-    precision : "fp64" (fill + LU in fp64) or "mixed" (complex64 fill and
-                LU, fp64 iterative refinement; tolerance refine_tol)
+    precision : "fp64" (fill + LU in fp64), "mixed" (fp64 fill, complex64 LU,
+                fp64 GMRES refinement to the normwise backward error
+                refine_tol) or "mixed_fill32" (fp32 fill too: faster fill,
+                larger error in S at low frequency)
     """
 
     def __init__(self, mesh, substrate, z0=None, verbose=True, method="dense", v_weight=None, precision="fp64",
-                 device=0, refine_tol=1e-12, max_refine=20):
+                 device=0, refine_tol=1e-14, max_refine=60):
         if method not in ("auto", "dense"):
             raise ValueError("this engine implements method='dense' only")
         if precision not in PRECISIONS:
-            raise ValueError("precision must be 'fp64' or 'mixed'")
+            raise ValueError("precision must be 'fp64', 'mixed' or 'mixed_fill32'")
         self.mesh = mesh
         self.sub = substrate
         self.stack = st = substrate if hasattr(substrate, "layers") else substrate.to_stackup()
@@ -385,7 +387,7 @@ class Solver:
         g = greens or self.greens(freq)
         prec = PRECISIONS[precision or self.precision]
         n = self.mesh.n_unknowns
-        Z = np.zeros((n, n), np.complex128 if prec == E.M25_FP64 else np.complex64)
+        Z = np.zeros((n, n), np.complex64 if prec == E.M25_MIXED_FILL32 else np.complex128)
         zs = complex(self.surface_impedance(freq))
         E.check(self.ctx.lib.m25_assemble(self.ctx.h, self.geometry().h, g.h, zs.real, zs.imag, zs.real, zs.imag,
                                           prec, Z.ctypes.data, n, E.M25_ON_HOST))
@@ -515,10 +517,10 @@ def assemble(solver, freq, precision="fp64"):
 _default_ctx = None
 
 
-def dense_solve(Z, B, precision="fp64", ctx=None, tol=1e-12, max_iter=20):
+def dense_solve(Z, B, precision="fp64", ctx=None, tol=1e-14, max_iter=60):
     """Z X = B on the GPU (mom25d's _dense_solve): LU with partial pivoting in
-    fp64, or complex64 LU + fp64 iterative refinement ("mixed"). Z is
-    complex128 (or complex64 for "mixed": the complex64 fill)."""
+    fp64, or ("mixed") a complex64 LU with fp64 GMRES refinement against Z
+    (complex128, or complex64 when Z comes from the fp32 fill)."""
     global _default_ctx
     if ctx is None:
         if _default_ctx is None:
@@ -532,9 +534,9 @@ def dense_solve(Z, B, precision="fp64", ctx=None, tol=1e-12, max_iter=20):
         prec = E.M25_FP64
         Z = np.ascontiguousarray(Z, np.complex128)
     elif Z.dtype == np.complex64:
-        prec = E.M25_MIXED
+        prec = E.M25_MIXED_FILL32
     else:
-        prec = 2
+        prec = E.M25_MIXED
         Z = np.ascontiguousarray(Z, np.complex128)
     info = np.zeros(2, np.int32)
     E.check(ctx.lib.m25_dense_solve(ctx.h, n, B.shape[1], prec, Z.ctypes.data, B.ctypes.data, X.ctypes.data,

@@ -48,11 +48,18 @@ def test_slab_tables_match_oracle(line, f):
     for m, tab in enumerate((k.SA, k.SV, k.SW)):
         err = np.abs(S[m, 0, 0] - tab).max() / np.abs(tab).max()
         assert err < 1e-12, (m, err)
-    # cubic coefficients against scipy's not-a-knot spline
+    # cubic coefficients against scipy's not-a-knot spline (the cubic term
+    # carries the cancellation of the slope system: 1e-8), and the spline
+    # values between the nodes (1e-12)
     c_ref = k.pair().spl.c  # (4, n-1, 2)
     for m in range(2):
         err = np.abs(coef[0, :, :, m] - c_ref[:, :, m].T).max() / np.abs(c_ref[:, :, m]).max()
-        assert err < 1e-9, (m, err)
+        assert err < 1e-8, (m, err)
+        mid = 0.5 * (g.rho[1:] + g.rho[:-1])
+        dx = (mid - g.rho[:-1])[:, None] ** np.arange(3, -1, -1)[None]
+        val = np.sum(coef[0, :, :, m] * dx, 1)
+        ref_val = k.pair().spl(mid)[:, m]
+        assert np.abs(val - ref_val).max() < 1e-12 * np.abs(ref_val).max()
     np.testing.assert_allclose(c[1, 0, 0], k.cv, rtol=1e-15)
     g.close()
 
@@ -85,7 +92,7 @@ def test_fill_fp64_matches_oracle(line, f):
     Z = sol.impedance(f)
     Zo = ref.impedance(f)
     assert np.abs(Z - Zo).max() <= 1e-12 * np.abs(Zo).max()
-    assert np.abs(Z - Z.T).max() == 0.0  # symmetric by construction
+    assert np.abs(Z - Z.T).max() <= 1e-15 * np.abs(Z).max()  # symmetrised in the gather
 
 
 def test_fill_with_via_matches_oracle(shunt):
@@ -118,7 +125,7 @@ def test_fill_mixed_close_to_fp64(line):
     sol, _ = line
     f = 7e9
     Z64 = sol.impedance(f, precision="fp64")
-    Z32 = sol.impedance(f, precision="mixed")
+    Z32 = sol.impedance(f, precision="mixed_fill32")
     assert Z32.dtype == np.complex64
     assert np.abs(Z32 - Z64).max() <= 3e-6 * np.abs(Z64).max()
 
@@ -153,9 +160,26 @@ def test_dense_solve_mixed_refines_to_fp64(gpu, n):
     A = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
     A += 3 * np.sqrt(n) * np.eye(n)
     B = rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2))
-    X = dense_solve(A, B, precision="mixed", tol=1e-13)
+    X = dense_solve(A, B, precision="mixed", tol=1e-15)
     Xr = np.linalg.solve(A, B)
-    assert np.abs(X - Xr).max() <= 1e-11 * np.abs(Xr).max()
+    assert np.abs(X - Xr).max() <= 1e-12 * np.abs(Xr).max()
+
+
+def test_dense_solve_mixed_ill_conditioned(gpu):
+    """cond ~1e9: beyond classical refinement with a complex64 LU (cond u32 >> 1);
+    GMRES refinement still reaches the fp64 solution's accuracy."""
+    rng = np.random.default_rng(7)
+    n = 400
+    U, _ = np.linalg.qr(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    Vm, _ = np.linalg.qr(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    s = np.logspace(0, -9, n)
+    A = (U * s) @ Vm.conj().T
+    B = rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2))
+    X = dense_solve(A, B, precision="mixed")
+    Xr = np.linalg.solve(A, B)
+    assert np.abs(X - Xr).max() <= 1e-5 * np.abs(Xr).max()
+    r = A @ X - B
+    assert np.linalg.norm(r) <= 1e-13 * (np.abs(A).sum(1).max() * np.linalg.norm(X) + np.linalg.norm(B))
 
 
 def test_singular_matrix_raises(gpu):
@@ -207,10 +231,24 @@ def test_tee_sweep_matches_reference(gpu):
     g = golden("tee")
     lay, st, m, _ = build("tee")
     idx = [0, 12, 24, 36]
-    for prec, tol in (("fp64", 1e-6), ("mixed", 1e-5)):
+    # fp64 and mixed (fp64 fill, complex64 LU + fp64 GMRES refinement) are
+    # held to the reference's fit floor; the all-fp32 fill loses the
+    # low-frequency scalar-potential cancellation (~1e-4 at 1 GHz)
+    for prec, tol in (("fp64", 1e-6), ("mixed", 1e-6), ("mixed_fill32", 3e-4)):
         sol = Solver(m, st, verbose=False, precision=prec)
         r = sol.sweep(g["freqs"][idx])
         assert np.abs(r.S - g["S"][idx]).max() < tol, prec
+        sol.close()
+
+
+def test_lpf_headline_workload_matches_reference(gpu):
+    """N = 5943, 0.5 / 4 / 8 GHz: fp64 to the fit floor, mixed within 1e-5."""
+    g = golden("lpf")
+    lay, st, m, _ = build("lpf")
+    for prec, tol in (("fp64", 1e-6), ("mixed", 1e-5)):
+        sol = Solver(m, st, verbose=False, precision=prec)
+        r = sol.sweep(g["freqs"])
+        assert np.abs(r.S - g["S"]).max() < tol, prec
         sol.close()
 
 
