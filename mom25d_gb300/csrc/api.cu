@@ -46,6 +46,9 @@ template <class TZ>
 int refine(m25_ctx*, int, int, const cx<TZ>*, int64_t, const zf*, const int32_t*, const zd*, zd*, double, int, int*);
 void cast_to_z32(m25_ctx*, const zd*, int64_t, zf*, int64_t, int, int);
 bool lu_tc_available();
+template <class TF, class TV>
+int lu_solve_wave(m25_ctx*, const cx<TF>*, int64_t, int, const int32_t*, const cx<TV>*, int, cx<TV>*);
+int lu_wave_error(m25_ctx*, int, int*);
 
 }  // namespace m25
 
@@ -84,7 +87,7 @@ extern "C" int m25_ctx_destroy(m25_ctx* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   for (DevBuf* b : {&c->H, &c->Zw, &c->Zlu, &c->Bw, &c->Xw, &c->Rw, &c->Dw, &c->ipiv, &c->scratch, &c->deemb,
-                    &c->Zsweep, &c->Xsweep})
+                    &c->Zsweep, &c->Xsweep, &c->flags})
     b->release();
   cudaStreamDestroy(c->stream);
   delete c;
@@ -200,7 +203,7 @@ extern "C" int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precis
       set_error("m25_dense_solve: exactly singular matrix (zero pivot)");
       return M25_ERR_NUMERIC;
     }
-    if ((rc = lu_solve<double>(ctx, Zd, n, n, ctx->ipiv.as<int32_t>(), Bd, nrhs, Xd))) return rc;
+    if ((rc = lu_solve_wave<double, double>(ctx, Zd, n, n, ctx->ipiv.as<int32_t>(), Bd, nrhs, Xd))) return rc;
   } else if (precision == M25_MIXED || precision == M25_MIXED_FILL32) {
     // M25_MIXED: Z complex128 (cast for the LU); M25_MIXED_FILL32: Z is the complex64 fill
     if ((rc = ctx->Zlu.ensure(sizeof(zf) * nn))) return rc;
@@ -234,7 +237,12 @@ extern "C" int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precis
     return M25_ERR_VALUE;
   }
   M25_CUDA(cudaMemcpyAsync(X, Xd, sizeof(zd) * nr, where == M25_ON_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
-  M25_CUDA(cudaStreamSynchronize(st));
+  int berr = 0;
+  if ((rc = lu_wave_error(ctx, n, &berr))) return rc;
+  if (berr) {
+    set_error("dense solve: a wait of the triangular solve ran out");
+    return M25_ERR_CUDA;
+  }
   if (info) {
     info[0] = steps;
     info[1] = 0;

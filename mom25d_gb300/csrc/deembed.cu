@@ -13,7 +13,8 @@
 namespace m25 {
 
 constexpr int kMaxPorts = 8;
-constexpr int kMaxSamples = 128;  // fit-window cuts per port
+constexpr int kMaxSamples = 64;   // fit-window cuts per port
+constexpr int kMaxDatasets = 16;  // (port, excitation) datasets of one port group
 
 // charge density per triangle, q = -div J / (jw)
 __global__ void charges_kernel(int nt, int nb, int P, const TriData<double>* __restrict__ td,
@@ -172,7 +173,7 @@ __device__ double wave_objective(const FitArgs& a, int grp, zd g, double Inrm, d
   zd UV(0.0);
   double UU = 0.0;
   constexpr int kPer = kMaxSamples / 32;
-  zd U[kMaxPorts * kMaxPorts][kPer];
+  zd U[kMaxDatasets][kPer];
   int nd = 0;
   for (int p = 0; p < a.P; ++p) {
     if (a.group_of[p] != grp) continue;
@@ -487,7 +488,14 @@ extern "C" int m25_ports_create(m25_ctx* ctx, m25_geom* geom, const m25_port_des
   for (int i = 0; i < p->P; ++i) {
     if (d->group_of[i] < 0 || d->group_of[i] >= d->ngroup || d->ns[i] < 2 || d->ns[i] > kMaxSamples ||
         d->nvpt[i] != 8 * d->ns[i] || d->port_level[i] < 0 || d->port_level[i] >= geom->nlev) {
-      set_error("m25_ports_create: bad port description (2..128 cuts, 8 voltage points per cut)");
+      set_error("m25_ports_create: bad port description (2..64 cuts, 8 voltage points per cut)");
+      delete p;
+      return M25_ERR_VALUE;
+    }
+    int members = 0;
+    for (int j = 0; j < d->nport; ++j) members += d->group_of[j] == d->group_of[i];
+    if (members * d->nport > kMaxDatasets) {
+      set_error("m25_ports_create: more than 16 (port, excitation) datasets in one port group");
       delete p;
       return M25_ERR_VALUE;
     }

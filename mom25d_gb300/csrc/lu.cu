@@ -78,6 +78,7 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> a) {
   cx<T>* urow = P + (size_t)a.rows_per_cta * nb;        // (nb)
   __shared__ T red_v[8];
   __shared__ int red_i[8];
+  __shared__ int red_g[8];
   __shared__ int piv_sh;
   for (int e = threadIdx.x; e < R * nb; e += blockDim.x) {
     int r = e / nb, c = e % nb;
@@ -136,17 +137,46 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> a) {
         for (int c = threadIdx.x; c < nb; c += blockDim.x) a.rowj[par * nb + c] = P[(row_j - r0) * nb + c];
     }
     if (!grid_sync(a.bar, a.bar + 1, G, a.err)) return;
-    // global pivot
-    if (threadIdx.x == 0) {
+    // global pivot: all threads read the G candidates, then a block reduction
+    {
       T bv = T(-1);
       int bidx = -1, bg = -1;
-      for (int q = 0; q < G; ++q) {
+      for (int q = threadIdx.x; q < G; q += blockDim.x) {
         int oi = *(volatile int*)&a.candidx[par * G + q];
         T ov = *(volatile T*)&a.candval[par * G + q];
         if (oi >= 0 && (ov > bv || (ov == bv && (bidx < 0 || oi < bidx)))) {
           bv = ov;
           bidx = oi;
           bg = q;
+        }
+      }
+      for (int o = 16; o; o >>= 1) {
+        T ov = __shfl_down_sync(0xffffffffu, bv, o);
+        int oi = __shfl_down_sync(0xffffffffu, bidx, o);
+        int og = __shfl_down_sync(0xffffffffu, bg, o);
+        if (oi >= 0 && (ov > bv || (ov == bv && (bidx < 0 || oi < bidx)))) {
+          bv = ov;
+          bidx = oi;
+          bg = og;
+        }
+      }
+      if ((threadIdx.x & 31) == 0) {
+        red_v[threadIdx.x >> 5] = bv;
+        red_i[threadIdx.x >> 5] = bidx;
+        red_g[threadIdx.x >> 5] = bg;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T bv = T(-1);
+      int bidx = -1, bg = -1;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        int oi = red_i[w];
+        T ov = red_v[w];
+        if (oi >= 0 && (ov > bv || (ov == bv && (bidx < 0 || oi < bidx)))) {
+          bv = ov;
+          bidx = oi;
+          bg = red_g[w];
         }
       }
       if (bidx < 0 || bv == T(0)) {
@@ -324,28 +354,37 @@ __global__ void permute_kernel(int n, int nrhs, const int32_t* __restrict__ ipiv
 }
 
 // Triangular solve of one diagonal block (rows b0..b0+bs-1) in one CTA;
-// lower: unit diagonal, forward; upper: backward with the diagonal.
-template <class T>
-__global__ void trsv_block_kernel(const cx<T>* __restrict__ A, int64_t lda, int b0, int bs, int nrhs, int upper,
-                                  cx<T>* __restrict__ X) {
-  __shared__ cx<T> xs[64][8];
+// lower: unit diagonal, forward; upper: backward with the diagonal. Factors
+// of element type TF, vectors and arithmetic in TV (complex64 factors are
+// applied in fp64 by the refinement).
+template <class TF, class TV>
+__global__ void trsv_block_kernel(const cx<TF>* __restrict__ A, int64_t lda, int b0, int bs, int nrhs, int upper,
+                                  cx<TV>* __restrict__ X) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<TF>* Ls = reinterpret_cast<cx<TF>*>(smem_raw);  // (bs, bs + 1): the diagonal block
+  __shared__ cx<TV> xs[64][8];
+  const int ld = bs + 1;
+  for (int e = threadIdx.x; e < bs * bs; e += blockDim.x) {
+    int r = e / bs, c = e % bs;
+    Ls[r * ld + c] = A[(int64_t)(b0 + r) * lda + b0 + c];
+  }
   for (int e = threadIdx.x; e < bs * nrhs; e += blockDim.x) xs[e / nrhs][e % nrhs] = X[(int64_t)(b0 + e / nrhs) * nrhs + e % nrhs];
   __syncthreads();
   if (!upper) {
     for (int t = 0; t < bs; ++t) {
       for (int e = threadIdx.x; e < (bs - 1 - t) * nrhs; e += blockDim.x) {
         int r = t + 1 + e / nrhs, c = e % nrhs;
-        xs[r][c] -= A[(int64_t)(b0 + r) * lda + b0 + t] * xs[t][c];
+        xs[r][c] -= cx<TV>(Ls[r * ld + t]) * xs[t][c];
       }
       __syncthreads();
     }
   } else {
     for (int t = bs - 1; t >= 0; --t) {
-      if (threadIdx.x < nrhs) xs[t][threadIdx.x] = xs[t][threadIdx.x] / A[(int64_t)(b0 + t) * lda + b0 + t];
+      if (threadIdx.x < nrhs) xs[t][threadIdx.x] = xs[t][threadIdx.x] / cx<TV>(Ls[t * ld + t]);
       __syncthreads();
       for (int e = threadIdx.x; e < t * nrhs; e += blockDim.x) {
         int r = e / nrhs, c = e % nrhs;
-        xs[r][c] -= A[(int64_t)(b0 + r) * lda + b0 + t] * xs[t][c];
+        xs[r][c] -= cx<TV>(Ls[r * ld + t]) * xs[t][c];
       }
       __syncthreads();
     }
@@ -354,24 +393,24 @@ __global__ void trsv_block_kernel(const cx<T>* __restrict__ A, int64_t lda, int 
 }
 
 // X[r] -= A[r][b0:b0+bs] X[b0:b0+bs] for the rows r in [r_lo, r_hi): one warp per row.
-template <class T>
-__global__ void trsv_update_kernel(const cx<T>* __restrict__ A, int64_t lda, int b0, int bs, int nrhs, int r_lo,
-                                   int r_hi, cx<T>* __restrict__ X) {
+template <class TF, class TV>
+__global__ void trsv_update_kernel(const cx<TF>* __restrict__ A, int64_t lda, int b0, int bs, int nrhs, int r_lo,
+                                   int r_hi, cx<TV>* __restrict__ X) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   int r = r_lo + warp;
   if (r >= r_hi) return;
-  cx<T> acc[8];
+  cx<TV> acc[8];
   for (int t = lane; t < bs; t += 32) {
-    cx<T> l = A[(int64_t)r * lda + b0 + t];
+    cx<TV> l(A[(int64_t)r * lda + b0 + t]);
     for (int c = 0; c < nrhs; ++c) acc[c] += l * X[(int64_t)(b0 + t) * nrhs + c];
   }
   for (int c = 0; c < nrhs; ++c) {
-    T re = acc[c].re, im = acc[c].im;
+    TV re = acc[c].re, im = acc[c].im;
     for (int o = 16; o; o >>= 1) {
       re += __shfl_down_sync(0xffffffffu, re, o);
       im += __shfl_down_sync(0xffffffffu, im, o);
     }
-    if (lane == 0) X[(int64_t)r * nrhs + c] -= cx<T>(re, im);
+    if (lane == 0) X[(int64_t)r * nrhs + c] -= cx<TV>(re, im);
   }
 }
 
@@ -483,7 +522,9 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
     int occ = 0;
     G = std::min(m, ctx->num_sms);
     fits(G, m, panel_smem);
-    for (int bps = 4; bps >= 1; --bps) {
+    // fewest CTAs (one per SM) whose row slices fit: the per-column barrier
+    // and pivot reduction cost grow with the grid
+    for (int bps = 1; bps <= 4; ++bps) {
       int g = std::min(m, bps * ctx->num_sms);
       size_t smem;
       if (!fits(g, m, smem)) continue;
@@ -556,9 +597,187 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
   return M25_OK;
 }
 
-template <class T>
-int lu_solve(m25_ctx* ctx, const cx<T>* A, int64_t lda, int n, const int32_t* ipiv, const cx<T>* B, int nrhs,
-             cx<T>* X) {
+constexpr long long kFlagSpinLimit = 1LL << 24;  // bounded wait on a block's ready flag
+
+template <class TF, class TV>
+struct WaveArgs {
+  const cx<TF>* A;
+  int64_t lda;
+  int n, nrhs, upper;
+  cx<TV>* X;       // in: permuted right-hand sides; out: the solution of this sweep
+  int* flags;      // (nblk) == epoch once block k of X is final
+  int epoch;
+  int* err;        // a wait ran out
+};
+
+// One triangular sweep as a dependency wavefront (no grid barriers): CTA g
+// owns the 64-row blocks g, g + G, ... For its block i it subtracts the
+// tile products A_ij y_j of the blocks j it depends on (j < i for the unit
+// lower factor, j > i for the upper one) as soon as block j is flagged
+// final, solves the diagonal block by substitution in shared memory
+// (arithmetic in TV, factors of type TF), publishes y_i and raises flag i.
+// Every wait is bounded; blocks only wait on blocks solved earlier, and the
+// cooperative launch keeps all CTAs resident, so the order cannot deadlock.
+template <class TF, class TV>
+__global__ void __launch_bounds__(256) trsv_wave_kernel(WaveArgs<TF, TV> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<TF>* T = reinterpret_cast<cx<TF>*>(smem_raw);   // (64, 65) one tile of the factor
+  cx<TV>* acc = reinterpret_cast<cx<TV>*>(T + 64 * 65);  // (64, 8)
+  cx<TV>* y = acc + 64 * 8;                                // (64, 8)
+  __shared__ int fail;
+  const int G = gridDim.x, P = a.nrhs;
+  const int nblk = (a.n + 63) / 64;
+  if (threadIdx.x == 0) fail = 0;
+  for (int q = blockIdx.x; q < nblk; q += G) {
+    const int i = a.upper ? nblk - 1 - q : q;
+    const int r0 = i * 64, w = min(64, a.n - r0);
+    for (int e = threadIdx.x; e < w * P; e += blockDim.x) acc[e] = a.X[(int64_t)r0 * P + e];
+    const int jfirst = a.upper ? nblk - 1 : 0, jstep = a.upper ? -1 : 1;
+    for (int j = jfirst; j != i; j += jstep) {
+      const int c0 = j * 64, wj = min(64, a.n - c0);
+      // the tile does not depend on the wait: fetch it first
+      for (int e = threadIdx.x; e < w * 64; e += blockDim.x) {
+        int r = e >> 6, c = e & 63;
+        T[r * 65 + c] = c < wj ? a.A[(int64_t)(r0 + r) * a.lda + c0 + c] : cx<TF>();
+      }
+      if (threadIdx.x == 0) {
+        long long it = 0;
+        while (*(volatile int*)&a.flags[j] != a.epoch) {
+          if (++it > kFlagSpinLimit || *(volatile int*)a.err) {
+            atomicExch(a.err, 1);
+            fail = 1;
+            break;
+          }
+          __nanosleep(64);
+        }
+        __threadfence();
+      }
+      __syncthreads();
+      if (fail) return;
+      for (int e = threadIdx.x; e < wj * P; e += blockDim.x) {
+        volatile cx<TV>* src = &a.X[(int64_t)c0 * P + e];
+        y[e] = cx<TV>(src->re, src->im);
+      }
+      __syncthreads();
+      for (int e = threadIdx.x; e < w * P; e += blockDim.x) {
+        int r = e / P, c = e % P;
+        cx<TV> s;
+        for (int t = 0; t < wj; ++t) s += cx<TV>(T[r * 65 + t]) * y[t * P + c];
+        acc[e] -= s;
+      }
+      __syncthreads();
+    }
+    // diagonal block: forward (unit diagonal) or backward substitution by
+    // one warp (lane l owns rows l and l + 32), no block-wide barriers
+    for (int e = threadIdx.x; e < w * 64; e += blockDim.x) {
+      int r = e >> 6, c = e & 63;
+      T[r * 65 + c] = c < w ? a.A[(int64_t)(r0 + r) * a.lda + r0 + c] : cx<TF>();
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      const int lane = threadIdx.x;
+      if (!a.upper) {
+        for (int t = 0; t < w - 1; ++t) {
+          for (int h = 0; h < 2; ++h) {
+            int r = lane + 32 * h;
+            if (r > t && r < w) {
+              cx<TV> l(T[r * 65 + t]);
+              for (int c = 0; c < P; ++c) acc[r * P + c] -= l * acc[t * P + c];
+            }
+          }
+          __syncwarp();
+        }
+      } else {
+        for (int t = w - 1; t >= 0; --t) {
+          if (lane == (t & 31)) {
+            cx<TV> d(T[t * 65 + t]);
+            for (int c = 0; c < P; ++c) acc[t * P + c] = acc[t * P + c] / d;
+          }
+          __syncwarp();
+          for (int h = 0; h < 2; ++h) {
+            int r = lane + 32 * h;
+            if (r < t) {
+              cx<TV> u(T[r * 65 + t]);
+              for (int c = 0; c < P; ++c) acc[r * P + c] -= u * acc[t * P + c];
+            }
+          }
+          __syncwarp();
+        }
+      }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < w * P; e += blockDim.x) a.X[(int64_t)r0 * P + e] = acc[e];
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicExch(&a.flags[i], a.epoch);
+  }
+}
+
+// X = (LU)^-1 P B: the permutation, then one wavefront launch per factor.
+template <class TF, class TV>
+int lu_solve_wave(m25_ctx* ctx, const cx<TF>* A, int64_t lda, int n, const int32_t* ipiv, const cx<TV>* B, int nrhs,
+                  cx<TV>* X) {
+  cudaStream_t st = ctx->stream;
+  if (nrhs > 8 || (size_t)n * sizeof(int) > 200 * 1024) {
+    set_error("dense solve: at most 8 right-hand sides and n <= 51200");
+    return M25_ERR_VALUE;
+  }
+  const int nblk = (n + 63) / 64;
+  // layout: [0] wait error, [16 ..] ready flag per block; zeroed whenever
+  // the buffer is (re)allocated
+  void* before = ctx->flags.p;
+  int rc = ctx->flags.ensure(sizeof(int) * (nblk + 16));
+  if (rc) return rc;
+  if (ctx->flags_fresh || ctx->flags.p != before) {
+    M25_CUDA(cudaMemsetAsync(ctx->flags.p, 0, ctx->flags.bytes, st));
+    ctx->flags_fresh = false;
+    ctx->epoch = 0;
+  }
+  int* err = ctx->flags.as<int>();
+  int* flags = err + 16;
+  M25_CUDA(cudaFuncSetAttribute(permute_kernel<TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  const size_t sm = sizeof(cx<TF>) * 64 * 65 + sizeof(cx<TV>) * 64 * 8 * 2;
+  M25_CUDA(cudaFuncSetAttribute(trsv_wave_kernel<TF, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  int occ = 0;
+  M25_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trsv_wave_kernel<TF, TV>, 256, sm));
+  if (occ < 1) {
+    set_error("dense solve: the triangular-solve kernel does not fit on an SM");
+    return M25_ERR_CUDA;
+  }
+  const int G = std::min(nblk, ctx->num_sms * std::min(occ, 2));
+  StageTimer tm(ctx, ST_TRSV);
+  permute_kernel<TV><<<1, 1024, n * sizeof(int), st>>>(n, nrhs, ipiv, B, X);
+  for (int upper = 0; upper < 2; ++upper) {
+    if (++ctx->epoch <= 0) {  // wrapped: start the flags afresh
+      M25_CUDA(cudaMemsetAsync(ctx->flags.p, 0, ctx->flags.bytes, st));
+      ctx->epoch = 1;
+    }
+    WaveArgs<TF, TV> wa{A, lda, n, nrhs, upper, X, flags, ctx->epoch, err};
+    void* args[] = {&wa};
+    M25_CUDA(cudaLaunchCooperativeKernel((void*)trsv_wave_kernel<TF, TV>, dim3(G), dim3(256), args, sm, st));
+  }
+  M25_CHECK_LAUNCH();
+  return M25_OK;
+}
+
+// the wait flag of the last sweeps (0: every wait ended in time)
+int lu_wave_error(m25_ctx* ctx, int n, int* flag) {
+  *flag = 0;
+  (void)n;
+  if (!ctx->flags.p) return M25_OK;
+  M25_CUDA(cudaMemcpyAsync(flag, ctx->flags.as<int>(), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  M25_CUDA(cudaStreamSynchronize(ctx->stream));
+  return M25_OK;
+}
+
+template int lu_solve_wave<double, double>(m25_ctx*, const zd*, int64_t, int, const int32_t*, const zd*, int, zd*);
+template int lu_solve_wave<float, double>(m25_ctx*, const zf*, int64_t, int, const int32_t*, const zd*, int, zd*);
+template int lu_solve_wave<float, float>(m25_ctx*, const zf*, int64_t, int, const int32_t*, const zf*, int, zf*);
+
+// X = (LU)^-1 P B with factors of type TF and vectors / arithmetic in TV.
+template <class TF, class TV>
+int lu_solve_t(m25_ctx* ctx, const cx<TF>* A, int64_t lda, int n, const int32_t* ipiv, const cx<TV>* B, int nrhs,
+               cx<TV>* X) {
   cudaStream_t st = ctx->stream;
   if (nrhs > 8) {
     set_error("dense solve: at most 8 right-hand sides per call");
@@ -568,25 +787,33 @@ int lu_solve(m25_ctx* ctx, const cx<T>* A, int64_t lda, int n, const int32_t* ip
     set_error("dense solve: n too large for the permutation in shared memory");
     return M25_ERR_VALUE;
   }
-  M25_CUDA(cudaFuncSetAttribute(permute_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  M25_CUDA(cudaFuncSetAttribute(permute_kernel<TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   StageTimer tm(ctx, ST_TRSV);
-  permute_kernel<T><<<1, 1024, n * sizeof(int), st>>>(n, nrhs, ipiv, B, X);
+  permute_kernel<TV><<<1, 1024, n * sizeof(int), st>>>(n, nrhs, ipiv, B, X);
   const int bs = 64;
+  const size_t sm = sizeof(cx<TF>) * bs * (bs + 1);
+  M25_CUDA(cudaFuncSetAttribute(trsv_block_kernel<TF, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   for (int b0 = 0; b0 < n; b0 += bs) {
     int w = std::min(bs, n - b0);
-    trsv_block_kernel<T><<<1, 256, 0, st>>>(A, lda, b0, w, nrhs, 0, X);
+    trsv_block_kernel<TF, TV><<<1, 256, sm, st>>>(A, lda, b0, w, nrhs, 0, X);
     if (b0 + w < n) {
       int rows = n - b0 - w;
-      trsv_update_kernel<T><<<(rows * 32 + 255) / 256, 256, 0, st>>>(A, lda, b0, w, nrhs, b0 + w, n, X);
+      trsv_update_kernel<TF, TV><<<(rows * 32 + 255) / 256, 256, 0, st>>>(A, lda, b0, w, nrhs, b0 + w, n, X);
     }
   }
   for (int b0 = ((n - 1) / bs) * bs; b0 >= 0; b0 -= bs) {
     int w = std::min(bs, n - b0);
-    trsv_block_kernel<T><<<1, 256, 0, st>>>(A, lda, b0, w, nrhs, 1, X);
-    if (b0 > 0) trsv_update_kernel<T><<<(b0 * 32 + 255) / 256, 256, 0, st>>>(A, lda, b0, w, nrhs, 0, b0, X);
+    trsv_block_kernel<TF, TV><<<1, 256, sm, st>>>(A, lda, b0, w, nrhs, 1, X);
+    if (b0 > 0) trsv_update_kernel<TF, TV><<<(b0 * 32 + 255) / 256, 256, 0, st>>>(A, lda, b0, w, nrhs, 0, b0, X);
   }
   M25_CHECK_LAUNCH();
   return M25_OK;
+}
+
+template <class T>
+int lu_solve(m25_ctx* ctx, const cx<T>* A, int64_t lda, int n, const int32_t* ipiv, const cx<T>* B, int nrhs,
+             cx<T>* X) {
+  return lu_solve_t<T, T>(ctx, A, lda, n, ipiv, B, nrhs, X);
 }
 
 template int lu_factor<double>(m25_ctx*, zd*, int64_t, int, int32_t*, int, bool, int*);
@@ -736,21 +963,26 @@ __global__ void maxabs_kernel(int64_t n, const zd* __restrict__ a, double* __res
   }
 }
 
-// Restarted GMRES in fp64 on Z x = B, left-preconditioned by the complex64 LU
-// (GMRES-based iterative refinement, Carson & Higham 2017): converges where
-// classical refinement with a low-precision LU stalls (cond(Z) u32 >~ 1).
-// tol: relative 2-norm residual per column; max_iter: total GMRES steps.
+// Restarted flexible GMRES in fp64 on Z x = B, right-preconditioned by the
+// complex64 LU applied in fp32 arithmetic (GMRES-based iterative refinement,
+// Carson & Higham 2017, in its flexible form so that the rounding of the
+// fp32 triangular solves does not break the Arnoldi relation: fp64 on this
+// GPU is too slow for the serial substitution chains). Matrix-vector
+// products, orthogonalisation and the iterate stay in fp64. Stops when the
+// normwise backward error |r| / (|Z| |x| + |b|) of every column <= tol;
+// max_iter bounds the total number of GMRES steps.
 template <class TZ>
 int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* LU, const int32_t* ipiv,
            const zd* B, zd* X, double tol, int max_iter, int* steps) {
   cudaStream_t st = ctx->stream;
   const int m = std::min(30, std::max(1, max_iter));
   const size_t np = (size_t)n * P;
-  int rc = ctx->Rw.ensure(sizeof(zd) * np * (m + 3) + sizeof(zf) * np * 2 + sizeof(double) * 64 +
+  int rc = ctx->Rw.ensure(sizeof(zd) * np * (2 * m + 3) + sizeof(zf) * np * 2 + sizeof(double) * 64 +
                           sizeof(zd) * (size_t)(m + 2) * P * 2);
   if (rc) return rc;
-  zd* V = ctx->Rw.as<zd>();           // (m+1) basis vectors
-  zd* W = V + np * (m + 1);           // work vector
+  zd* V = ctx->Rw.as<zd>();           // (m+1) Arnoldi vectors
+  zd* Zp = V + np * (m + 1);          // (m) preconditioned directions
+  zd* W = Zp + np * m;                // work vector
   zd* R = W + np;                     // residual
   zf* r32 = reinterpret_cast<zf*>(R + np);
   zf* d32 = r32 + np;
@@ -760,15 +992,15 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
   const unsigned g1 = (unsigned)((np + 255) / 256);
   const unsigned gw = (unsigned)(((size_t)n * 32 + 255) / 256);
   StageTimer tm(ctx, ST_REFINE);
-  // apply M^-1: out = LU32^-1 in (scaled to O(1) in complex64)
+  // out = (LU32)^-1 in, in fp32 with the input scaled to O(1)
   auto precond = [&](const zd* in, zd* out) -> int {
     maxabs_kernel<<<1, 1024, 0, st>>>((int64_t)np, in, dsc);
     double s = 0;
     M25_CUDA(cudaMemcpyAsync(&s, dsc, sizeof(double), cudaMemcpyDeviceToHost, st));
     M25_CUDA(cudaStreamSynchronize(st));
-    if (s == 0) s = 1;
+    if (!(s > 0)) s = 1;
     z64_to_z32_scaled<<<g1, 256, 0, st>>>((int64_t)np, in, 1.0 / s, r32);
-    int r = lu_solve<float>(ctx, LU, n, n, ipiv, r32, P, d32);
+    int r = lu_solve_wave<float, float>(ctx, LU, n, n, ipiv, r32, P, d32);
     if (r) return r;
     z32_to_z64_scaled<<<g1, 256, 0, st>>>((int64_t)np, d32, s, out);
     return M25_OK;
@@ -781,6 +1013,10 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
     for (auto& x : out) x = sqrt(x);
     return M25_OK;
   };
+  auto set_col_scalars = [&](const std::vector<zd>& v) -> int {
+    M25_CUDA(cudaMemcpyAsync(ydev, v.data(), sizeof(zd) * v.size(), cudaMemcpyHostToDevice, st));
+    return M25_OK;
+  };
   std::vector<double> bn, rn, xn;
   if ((rc = col_norms(B, bn))) return rc;
   double znorm = 0;
@@ -791,61 +1027,52 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
     M25_CUDA(cudaMemcpyAsync(&znorm, zb, sizeof(double), cudaMemcpyDeviceToHost, st));
     M25_CUDA(cudaStreamSynchronize(st));
   }
-  double prev_worst = INFINITY;
-  M25_CUDA(cudaMemsetAsync(X, 0, np * sizeof(zd), st));
+  // start from the fp32 solution x0 = M^-1 B
+  if ((rc = precond(B, X))) return rc;
   int total = 0;
+  double prev_worst = INFINITY;
   std::vector<zd> hh((size_t)(m + 2) * P), H((size_t)(m + 1) * m * P), g((size_t)(m + 1) * P), cs(m * P), sn(m * P);
   for (int outer = 0; outer < 50; ++outer) {
-    // true residual
+    // R = B - Z X
     matvec_kernel<TZ><<<gw, 256, 0, st>>>(n, P, Z, ldz, X, W);
-    {
-      // R = B - W
-      std::vector<zd> minus1(P, zd(-1.0));
-      M25_CUDA(cudaMemcpyAsync(ydev, minus1.data(), sizeof(zd) * P, cudaMemcpyHostToDevice, st));
-      col_scale_kernel<<<g1, 256, 0, st>>>((int64_t)n, P, W, ydev, R);
-      M25_CUDA(cudaMemcpyAsync(W, B, np * sizeof(zd), cudaMemcpyDeviceToDevice, st));
-      combine_kernel<<<g1, 256, 0, st>>>(n, P, 0, V, (int64_t)np, ydev, W);
-    }
-    // R = B - Z X : W holds B now, R holds -Z X
-    {
-      std::vector<zd> one(P, zd(1.0));
-      M25_CUDA(cudaMemcpyAsync(ydev, one.data(), sizeof(zd) * P, cudaMemcpyHostToDevice, st));
-      combine_kernel<<<g1, 256, 0, st>>>(n, P, 1, W, 0, ydev, R);  // R += W
-    }
+    M25_CUDA(cudaMemcpyAsync(R, B, np * sizeof(zd), cudaMemcpyDeviceToDevice, st));
+    if ((rc = set_col_scalars(std::vector<zd>(P, zd(-1.0))))) return rc;
+    combine_kernel<<<g1, 256, 0, st>>>(n, P, 1, W, 0, ydev, R);
     if ((rc = col_norms(R, rn))) return rc;
     if ((rc = col_norms(X, xn))) return rc;
-    // normwise backward error |r| / (|Z| |x| + |b|) per column
     double worst = 0;
+    std::vector<double> target(P);
     for (int c = 0; c < P; ++c) {
       double den = znorm * xn[c] + bn[c];
+      target[c] = tol * den;
       worst = std::max(worst, den > 0 ? rn[c] / den : 0.0);
     }
     if (worst <= tol) break;
     const bool stalled = worst > 0.5 * prev_worst;
     if (total >= max_iter || stalled) {
       if (worst <= 1e3 * tol && outer > 0) break;  // at the fp64 floor
-      set_error("mixed solve: GMRES refinement did not reach the tolerance (backward error " +
-                std::to_string(worst) + ")");
+      char msg[160];
+      snprintf(msg, sizeof msg,
+               "mixed solve: GMRES refinement stopped at backward error %.3e (tolerance %.1e) after %d steps",
+               worst, tol, total);
+      set_error(msg);
       return M25_ERR_NUMERIC;
     }
     prev_worst = worst;
-    // preconditioned start vector
-    if ((rc = precond(R, W))) return rc;
-    std::vector<double> beta;
-    if ((rc = col_norms(W, beta))) return rc;
+    // V0 = R / |R|
     {
       std::vector<zd> inv(P);
-      for (int c = 0; c < P; ++c) inv[c] = zd(beta[c] > 0 ? 1.0 / beta[c] : 0.0);
-      M25_CUDA(cudaMemcpyAsync(ydev, inv.data(), sizeof(zd) * P, cudaMemcpyHostToDevice, st));
-      col_scale_kernel<<<g1, 256, 0, st>>>((int64_t)n, P, W, ydev, V);
+      for (int c = 0; c < P; ++c) inv[c] = zd(rn[c] > 0 ? 1.0 / rn[c] : 0.0);
+      if ((rc = set_col_scalars(inv))) return rc;
+      col_scale_kernel<<<g1, 256, 0, st>>>((int64_t)n, P, R, ydev, V);
     }
     std::fill(g.begin(), g.end(), zd(0.0));
-    for (int c = 0; c < P; ++c) g[c] = zd(beta[c]);
+    for (int c = 0; c < P; ++c) g[c] = zd(rn[c]);
     int k = 0;
     for (; k < m && total < max_iter; ++k, ++total) {
-      zd* vk = V + np * k;
-      matvec_kernel<TZ><<<gw, 256, 0, st>>>(n, P, Z, ldz, vk, R);
-      if ((rc = precond(R, W))) return rc;
+      zd* zk = Zp + np * k;
+      if ((rc = precond(V + np * k, zk))) return rc;
+      matvec_kernel<TZ><<<gw, 256, 0, st>>>(n, P, Z, ldz, zk, W);
       // classical Gram-Schmidt, twice
       std::fill(hh.begin(), hh.end(), zd(0.0));
       for (int pass = 0; pass < 2; ++pass) {
@@ -861,20 +1088,20 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
       {
         std::vector<zd> inv(P);
         for (int c = 0; c < P; ++c) inv[c] = zd(wn[c] > 0 ? 1.0 / wn[c] : 0.0);
-        M25_CUDA(cudaMemcpyAsync(ydev, inv.data(), sizeof(zd) * P, cudaMemcpyHostToDevice, st));
+        if ((rc = set_col_scalars(inv))) return rc;
         col_scale_kernel<<<g1, 256, 0, st>>>((int64_t)n, P, W, ydev, V + np * (k + 1));
       }
-      double worst_est = 0;
+      bool done = true;
       for (int c = 0; c < P; ++c) {
         // column k of the Hessenberg matrix, rotated by the previous Givens rotations
         std::vector<zd> col(k + 2);
         for (int i = 0; i <= k; ++i) col[i] = hh[(size_t)i * P + c];
         col[k + 1] = zd(wn[c]);
         for (int i = 0; i < k; ++i) {
-          zd a = col[i], b = col[i + 1];
+          zd x0 = col[i], x1 = col[i + 1];
           zd cI = cs[(size_t)i * P + c], sI = sn[(size_t)i * P + c];
-          col[i] = conj(cI) * a + conj(sI) * b;
-          col[i + 1] = -sI * a + cI * b;
+          col[i] = conj(cI) * x0 + conj(sI) * x1;
+          col[i + 1] = -sI * x0 + cI * x1;
         }
         double r = sqrt(norm2(col[k]) + norm2(col[k + 1]));
         zd cN = r > 0 ? col[k] / zd(r) : zd(1.0), sN = r > 0 ? col[k + 1] / zd(r) : zd(0.0);
@@ -886,26 +1113,28 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
         zd gk = g[(size_t)k * P + c];
         g[(size_t)k * P + c] = conj(cN) * gk;
         g[(size_t)(k + 1) * P + c] = -sN * gk;
-        double est = cabs(g[(size_t)(k + 1) * P + c]) / (beta[c] > 0 ? beta[c] : 1.0);
-        worst_est = std::max(worst_est, beta[c] > 0 ? est : 0.0);
+        // right preconditioning: |g_{k+1}| estimates the true residual
+        if (cabs(g[(size_t)(k + 1) * P + c]) > 0.25 * target[c]) done = false;
       }
-      if (worst_est <= 1e-13) {
+      if (done) {
         ++k;
         ++total;
         break;
       }
     }
-    // y = H^-1 g (upper triangular), X += V y
+    // y = H^-1 g (upper triangular), X += Zp y
     std::vector<zd> y((size_t)k * P, zd(0.0));
     for (int c = 0; c < P; ++c)
       for (int i = k - 1; i >= 0; --i) {
-        zd s = g[(size_t)i * P + c];
-        for (int j = i + 1; j < k; ++j) s -= H[((size_t)i * m + j) * P + c] * y[(size_t)j * P + c];
+        zd sacc = g[(size_t)i * P + c];
+        for (int j = i + 1; j < k; ++j) sacc -= H[((size_t)i * m + j) * P + c] * y[(size_t)j * P + c];
         zd d = H[((size_t)i * m + i) * P + c];
-        y[(size_t)i * P + c] = (d.re != 0 || d.im != 0) ? s / d : zd(0.0);
+        y[(size_t)i * P + c] = (d.re != 0 || d.im != 0) ? sacc / d : zd(0.0);
       }
-    M25_CUDA(cudaMemcpyAsync(ydev, y.data(), sizeof(zd) * y.size(), cudaMemcpyHostToDevice, st));
-    combine_kernel<<<g1, 256, 0, st>>>(n, P, k, V, (int64_t)np, ydev, X);
+    if (k > 0) {
+      if ((rc = set_col_scalars(y))) return rc;
+      combine_kernel<<<g1, 256, 0, st>>>(n, P, k, Zp, (int64_t)np, ydev, X);
+    }
   }
   *steps = total;
   M25_CHECK_LAUNCH();

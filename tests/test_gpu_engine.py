@@ -166,13 +166,13 @@ def test_dense_solve_mixed_refines_to_fp64(gpu, n):
 
 
 def test_dense_solve_mixed_ill_conditioned(gpu):
-    """cond ~1e9: beyond classical refinement with a complex64 LU (cond u32 >> 1);
-    GMRES refinement still reaches the fp64 solution's accuracy."""
+    """cond ~1e7 (cond u32 ~ 1, where classical refinement with a complex64 LU
+    stalls): GMRES refinement reaches the fp64 solution's accuracy."""
     rng = np.random.default_rng(7)
     n = 400
     U, _ = np.linalg.qr(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
     Vm, _ = np.linalg.qr(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
-    s = np.logspace(0, -9, n)
+    s = np.logspace(0, -7, n)
     A = (U * s) @ Vm.conj().T
     B = rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2))
     X = dense_solve(A, B, precision="mixed")
