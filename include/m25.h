@@ -151,6 +151,33 @@ int m25_assemble(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, double zs_re, dou
 int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precision, void* Z, const void* B, void* X,
                     int where, double tol, int32_t max_iter, int32_t* info);
 
+/* Allocation-free dense solve (no counterpart in mom25d). For callers that
+ * must not allocate device memory themselves or through this library:
+ * applications whose device memory belongs to another allocator (a
+ * framework's caching allocator, a fixed arena sized at start-up) and that
+ * cannot let a library call cudaMalloc / cudaFree in the middle of their
+ * work, since those calls synchronise the device and fail once the arena
+ * holds the memory. The same computation as m25_dense_solve with M25_FP64
+ * (complex128 LU with partial pivoting, then the two triangular solves), on
+ * caller-owned device memory only: Z (n x n complex128, row-major,
+ * overwritten by its LU factors), B (n x nrhs complex128, read only), X
+ * (n x nrhs complex128, the solution), ipiv (n int32, the 0-based pivot rows),
+ * on `stream` (a cudaStream_t; NULL = the legacy default stream). The
+ * library's own scratch is one static device array of
+ * M25_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until
+ * the process exits; it limits n to M25_NOALLOC_MAX_N (larger n is rejected
+ * with M25_ERR_VALUE) and the device to at most 192 SMs. The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress, with that
+ * device current); make that first call before any stream capture. All calls
+ * share the one array: calls that overlap on the GPU (other threads, other
+ * streams) race and must be serialised by the caller. info[0] = 0, info[1] =
+ * the first zero pivot (1-based) or 0. Returns after the stream has
+ * finished the solve. */
+#define M25_NOALLOC_MAX_N 24576
+#define M25_NOALLOC_SCRATCH_BYTES (448 * 1024)
+int m25_dense_solve_noalloc(int32_t n, int32_t nrhs, void* Z, const void* B, void* X, int32_t* ipiv, void* stream,
+                            int32_t* info);
+
 /* ----------------------------------------------------------- de-embedding */
 typedef struct {
   int32_t nport;               /* feed ports P */

@@ -15,6 +15,8 @@
 // Solve: permutation, blocked forward / backward substitution. The mixed
 // path refines in fp64: r = B - Z X, X += LU32^-1 r.
 #include <algorithm>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "m25_internal.h"
@@ -502,11 +504,14 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
   }
   (void)bps_max;
   (void)rows;
-  int Gmax = 4 * ctx->num_sms;
-  int rc = ctx->scratch.ensure(sizeof(cx<T>) * 2 * (size_t)Gmax * nb + sizeof(T) * 2 * Gmax + sizeof(int) * 2 * Gmax +
-                               sizeof(cx<T>) * 2 * nb + 64);
-  if (rc) return rc;
-  char* base = ctx->scratch.as<char>();
+  int Gmax = ctx->ext_scratch ? ctx->ext_gmax : 4 * ctx->num_sms;
+  char* base = ctx->ext_scratch;
+  if (!base) {
+    int rc = ctx->scratch.ensure(sizeof(cx<T>) * 2 * (size_t)Gmax * nb + sizeof(T) * 2 * Gmax +
+                                 sizeof(int) * 2 * Gmax + sizeof(cx<T>) * 2 * nb + 64);
+    if (rc) return rc;
+    base = ctx->scratch.as<char>();
+  }
   unsigned* bar = reinterpret_cast<unsigned*>(base);
   int* err = reinterpret_cast<int*>(base + 8);
   int* info = reinterpret_cast<int*>(base + 12);
@@ -520,14 +525,14 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
     const int m = n - k0;
     // grid size: as many CTAs as can be co-resident, each with >= 1 row
     int occ = 0;
-    G = std::min(m, ctx->num_sms);
+    G = std::min(std::min(m, ctx->num_sms), Gmax);
     fits(G, m, panel_smem);
     // fewest CTAs (one per SM) whose row slices fit: the per-column barrier
     // and pivot reduction cost grow with the grid
     for (int bps = 1; bps <= 4; ++bps) {
       int g = std::min(m, bps * ctx->num_sms);
       size_t smem;
-      if (!fits(g, m, smem)) continue;
+      if (g > Gmax || !fits(g, m, smem)) continue;
       M25_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, panel_kernel<T>, 256, smem));
       if (occ * ctx->num_sms >= g) {
         G = g;
@@ -577,7 +582,7 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
       }
       StageTimer tm(ctx, ST_GEMM);
       if (use_tc) {
-        rc = lu_gemm_tc(ctx, reinterpret_cast<zf*>(A), lda, n, k0, w);
+        int rc = lu_gemm_tc(ctx, reinterpret_cast<zf*>(A), lda, n, k0, w);
         if (rc) return rc;
       } else {
         dim3 grid((ncol + 63) / 64, (ncol + 63) / 64);
@@ -724,16 +729,19 @@ int lu_solve_wave(m25_ctx* ctx, const cx<TF>* A, int64_t lda, int n, const int32
   }
   const int nblk = (n + 63) / 64;
   // layout: [0] wait error, [16 ..] ready flag per block; zeroed whenever
-  // the buffer is (re)allocated
-  void* before = ctx->flags.p;
-  int rc = ctx->flags.ensure(sizeof(int) * (nblk + 16));
-  if (rc) return rc;
-  if (ctx->flags_fresh || ctx->flags.p != before) {
-    M25_CUDA(cudaMemsetAsync(ctx->flags.p, 0, ctx->flags.bytes, st));
-    ctx->flags_fresh = false;
-    ctx->epoch = 0;
+  // the buffer is (re)allocated (a caller-provided buffer comes zeroed)
+  int* err = ctx->ext_flags;
+  if (!err) {
+    void* before = ctx->flags.p;
+    int rc = ctx->flags.ensure(sizeof(int) * (nblk + 16));
+    if (rc) return rc;
+    if (ctx->flags_fresh || ctx->flags.p != before) {
+      M25_CUDA(cudaMemsetAsync(ctx->flags.p, 0, ctx->flags.bytes, st));
+      ctx->flags_fresh = false;
+      ctx->epoch = 0;
+    }
+    err = ctx->flags.as<int>();
   }
-  int* err = ctx->flags.as<int>();
   int* flags = err + 16;
   M25_CUDA(cudaFuncSetAttribute(permute_kernel<TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
   const size_t sm = sizeof(cx<TF>) * 64 * 65 + sizeof(cx<TV>) * 64 * 8 * 2;
@@ -749,7 +757,7 @@ int lu_solve_wave(m25_ctx* ctx, const cx<TF>* A, int64_t lda, int n, const int32
   permute_kernel<TV><<<1, 1024, n * sizeof(int), st>>>(n, nrhs, ipiv, B, X);
   for (int upper = 0; upper < 2; ++upper) {
     if (++ctx->epoch <= 0) {  // wrapped: start the flags afresh
-      M25_CUDA(cudaMemsetAsync(ctx->flags.p, 0, ctx->flags.bytes, st));
+      M25_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * nblk, st));
       ctx->epoch = 1;
     }
     WaveArgs<TF, TV> wa{A, lda, n, nrhs, upper, X, flags, ctx->epoch, err};
@@ -764,8 +772,9 @@ int lu_solve_wave(m25_ctx* ctx, const cx<TF>* A, int64_t lda, int n, const int32
 int lu_wave_error(m25_ctx* ctx, int n, int* flag) {
   *flag = 0;
   (void)n;
-  if (!ctx->flags.p) return M25_OK;
-  M25_CUDA(cudaMemcpyAsync(flag, ctx->flags.as<int>(), sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  const int* src = ctx->ext_flags ? ctx->ext_flags : ctx->flags.as<int>();
+  if (!src) return M25_OK;
+  M25_CUDA(cudaMemcpyAsync(flag, src, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   M25_CUDA(cudaStreamSynchronize(ctx->stream));
   return M25_OK;
 }
@@ -1152,3 +1161,95 @@ void cast_to_z32(m25_ctx* ctx, const zd* a, int64_t lda, zf* b, int64_t ldb, int
 }
 
 }  // namespace m25
+
+// ------------------------------------------------- allocation-free solve
+// Scratch of m25_dense_solve_noalloc: one file-scope device array that every
+// GPU loading this library holds until the process exits. Layout: [0, 64)
+// barrier words of the panel factorisation, then its candidate pivot rows for
+// up to kNoAllocGmax CTAs of 64 columns, then the ready flags of the
+// triangular solves.
+namespace {
+constexpr int kNoAllocGmax = 192;
+constexpr size_t kNoAllocPanelBytes = 64 + sizeof(m25::zd) * 2 * kNoAllocGmax * 64 + sizeof(double) * 2 * kNoAllocGmax +
+                                      sizeof(int) * 2 * kNoAllocGmax + sizeof(m25::zd) * 2 * 64;
+constexpr size_t kNoAllocFlagsOffset = (kNoAllocPanelBytes + 255) / 256 * 256;
+static_assert(kNoAllocFlagsOffset + sizeof(int) * (16 + M25_NOALLOC_MAX_N / 64 + 1) <= M25_NOALLOC_SCRATCH_BYTES,
+              "scratch too small for the declared maximum size");
+std::mutex g_noalloc_mu;
+constexpr int kMaxDevices = 64;
+void* g_noalloc_addr[kMaxDevices] = {};
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[M25_NOALLOC_SCRATCH_BYTES];
+
+extern "C" int m25_dense_solve_noalloc(int32_t n, int32_t nrhs, void* Z, const void* B, void* X, int32_t* ipiv,
+                                       void* stream, int32_t* info) {
+  using namespace m25;
+  if (!Z || !B || !X || !ipiv || n < 1 || nrhs < 1 || nrhs > 8) {
+    set_error("m25_dense_solve_noalloc: null pointer, n < 1 or nrhs outside 1..8");
+    return M25_ERR_VALUE;
+  }
+  if (n > M25_NOALLOC_MAX_N) {
+    set_error("m25_dense_solve_noalloc: n = " + std::to_string(n) + " exceeds the maximum " +
+              std::to_string(M25_NOALLOC_MAX_N) + " of the static scratch; use m25_dense_solve");
+    return M25_ERR_VALUE;
+  }
+  int dev = 0;
+  M25_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_error("m25_dense_solve_noalloc: device index out of range");
+    return M25_ERR_VALUE;
+  }
+  void* addr = nullptr;
+  {
+    // once per device, with that device current: the device address of the
+    // array (its host-side name is only a stand-in, not a device pointer)
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p) {
+        set_error(std::string("m25_dense_solve_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        return M25_ERR_CUDA;
+      }
+      g_noalloc_addr[dev] = p;
+    }
+    addr = g_noalloc_addr[dev];
+  }
+  m25_ctx c;  // borrowed stream, no workspace of its own
+  c.device = dev;
+  c.stream = static_cast<cudaStream_t>(stream);
+  M25_CUDA(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, dev));
+  if (c.num_sms > kNoAllocGmax) {
+    set_error("m25_dense_solve_noalloc: more SMs than the static panel scratch covers");
+    return M25_ERR_VALUE;
+  }
+  char* base = static_cast<char*>(addr);
+  c.ext_scratch = base;
+  c.ext_gmax = kNoAllocGmax;
+  c.ext_flags = reinterpret_cast<int*>(base + kNoAllocFlagsOffset);
+  // the array keeps the previous call's contents: clear the barrier words
+  // (lu_factor clears its header) and the ready flags
+  M25_CUDA(cudaMemsetAsync(c.ext_flags, 0, sizeof(int) * (16 + (n + 63) / 64), c.stream));
+  int zinfo = 0;
+  int rc = lu_factor<double>(&c, static_cast<zd*>(Z), n, n, ipiv, 64, false, &zinfo);
+  if (rc) return rc;
+  if (info) {
+    info[0] = 0;
+    info[1] = zinfo;
+  }
+  if (zinfo) {
+    set_error("m25_dense_solve_noalloc: exactly singular matrix (zero pivot)");
+    return M25_ERR_NUMERIC;
+  }
+  rc = lu_solve_wave<double, double>(&c, static_cast<const zd*>(Z), n, n, ipiv, static_cast<const zd*>(B), nrhs,
+                                     static_cast<zd*>(X));
+  if (rc) return rc;
+  int werr = 0;
+  if ((rc = lu_wave_error(&c, n, &werr))) return rc;
+  if (werr) {
+    set_error("m25_dense_solve_noalloc: a wait of the triangular solve ran out");
+    return M25_ERR_CUDA;
+  }
+  return M25_OK;
+}

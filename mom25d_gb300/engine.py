@@ -25,7 +25,7 @@ EXPORTS = ("m25_last_error", "m25_version", "m25_ctx_create", "m25_ctx_destroy",
            "m25_ctx_stream", "m25_geometry_create", "m25_geometry_destroy", "m25_geometry_stats",
            "m25_greens_create", "m25_greens_destroy", "m25_greens_tables", "m25_assemble", "m25_dense_solve",
            "m25_ports_create", "m25_ports_destroy", "m25_deembed", "m25_sweep_point", "m25_deembed_debug",
-           "m25_ctx_timing")
+           "m25_ctx_timing", "m25_dense_solve_noalloc")
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
@@ -91,6 +91,7 @@ def load():
                                     _f64p, _f64p, _f64p, _i32p]
     lib.m25_deembed_debug.argtypes = [vp, vp, _f64p, _f64p, _f64p, _f64p]
     lib.m25_ctx_timing.argtypes = [vp, C.c_int, _f64p, C.POINTER(C.c_longlong)]
+    lib.m25_dense_solve_noalloc.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, vp, vp, _i32p]
     _lib = lib
     return lib
 
