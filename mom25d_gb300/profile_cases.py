@@ -1,0 +1,58 @@
+"""Small, self-contained runs of single engine stages, for profiler captures.
+
+    python -m mom25d_gb300.profile_cases fill  --workload bandpass --precision fp64 [--reps 2]
+    python -m mom25d_gb300.profile_cases point --workload lpf --precision mixed [--reps 1]
+
+`fill` builds the mesh geometry and one frequency's Green's tables, then
+runs the impedance fill `reps` times (device output, no host copy);
+`point` runs `reps` full frequency points (tables, fill, LU + solve,
+de-embedding). Each exits non-zero on any engine error.
+"""
+
+import argparse
+import ctypes as C
+
+import numpy as np
+
+from . import engine as E
+from . import workloads
+from .solver import PRECISIONS, Solver
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("mode", choices=["fill", "point"])
+    ap.add_argument("--workload", default="bandpass")
+    ap.add_argument("--precision", default="fp64", choices=list(PRECISIONS))
+    ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--freq", type=float, default=None, help="Hz (default: the workload's middle frequency)")
+    args = ap.parse_args()
+    import mom25d_gb300 as G
+
+    kw = {"k": 0} if args.workload == "bandpass" else {}
+    lay, st, mesh, freqs = workloads.build(G, args.workload, **kw)
+    f = args.freq or float(freqs[len(freqs) // 2])
+    sol = Solver(mesh, st, verbose=False, precision=args.precision)
+    if args.mode == "fill":
+        import torch
+
+        n = mesh.n_unknowns
+        dtype = torch.complex64 if args.precision == "mixed_fill32" else torch.complex128
+        Z = torch.empty((n, n), dtype=dtype, device="cuda")
+        g = sol.greens(f)
+        zs = complex(sol.surface_impedance(f))
+        for _ in range(args.reps):
+            E.check(sol.ctx.lib.m25_assemble(sol.ctx.h, sol.geometry().h, g.h, zs.real, zs.imag, zs.real, zs.imag,
+                                             PRECISIONS[args.precision], C.c_void_p(Z.data_ptr()), n,
+                                             E.M25_ON_DEVICE))
+        sol.ctx.synchronize()
+        print(f"fill ok: N={n} |Z|max={float(Z.abs().max()):.3e}")
+    else:
+        for _ in range(args.reps):
+            S = sol.point(f)[0]
+        print(f"point ok: N={mesh.n_unknowns} S11={np.round(S[0, 0], 6)}")
+    sol.close()
+
+
+if __name__ == "__main__":
+    main()
