@@ -177,55 +177,65 @@ __device__ double wave_objective(const FitArgs& a, int grp, zd g, double Inrm, d
   int nd = 0;
   for (int p = 0; p < a.P; ++p) {
     if (a.group_of[p] != grp) continue;
+    const int ns = a.ns[p], off = a.s_off[p];
+    // e^{+-g s} and the QR of [e^{gs}, e^{-gs}] depend on the port only:
+    // shared by its P excitations
+    zd ep[kPer], em[kPer], q1[kPer], q2[kPer];
+    double n11 = 0;
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      int i = lane + 32 * u;
+      if (i < ns) {
+        double sv = a.s[off + i];
+        ep[u] = cexp(g * sv);
+        em[u] = cexp(-g * sv);
+        n11 += norm2(ep[u]);
+      } else {
+        ep[u] = em[u] = zd(0.0);
+      }
+    }
+    // two-column least squares by modified Gram-Schmidt with one re-orthogonalisation
+    const double r11 = sqrt(warp_sum(n11));
+    zd r12(0.0);
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      q1[u] = ep[u] / r11;
+      r12 += conj(q1[u]) * em[u];
+    }
+    r12 = warp_sum(r12);
+    zd r12b(0.0);
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      q2[u] = em[u] - r12 * q1[u];
+      r12b += conj(q1[u]) * q2[u];
+    }
+    r12b = warp_sum(r12b);
+    double n22 = 0;
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      q2[u] -= r12b * q1[u];
+      n22 += norm2(q2[u]);
+    }
+    r12 += r12b;
+    const double r22 = sqrt(warp_sum(n22));
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) q2[u] = q2[u] / r22;
     for (int e = 0; e < a.P; ++e, ++nd) {
-      const int ns = a.ns[p], off = a.s_off[p];
-      zd ep[kPer], em[kPer], Iv[kPer];
-      double n11 = 0;
+      zd Iv[kPer];
+      zd b1(0.0), b2(0.0);
+#pragma unroll
       for (int u = 0; u < kPer; ++u) {
         int i = lane + 32 * u;
-        if (i < ns) {
-          double s = a.s[off + i];
-          ep[u] = cexp(g * s);
-          em[u] = cexp(-g * s);
-          Iv[u] = a.I[(int64_t)(off + i) * a.P + e];
-          n11 += norm2(ep[u]);
-        } else {
-          ep[u] = em[u] = Iv[u] = zd(0.0);
-        }
-      }
-      // two-column least squares by modified Gram-Schmidt with one re-orthogonalisation
-      double r11 = sqrt(warp_sum(n11));
-      zd q1[kPer];
-      zd r12(0.0);
-      for (int u = 0; u < kPer; ++u) {
-        q1[u] = ep[u] / r11;
-        r12 += conj(q1[u]) * em[u];
-      }
-      r12 = warp_sum(r12);
-      zd v[kPer];
-      zd r12b(0.0);
-      for (int u = 0; u < kPer; ++u) {
-        v[u] = em[u] - r12 * q1[u];
-        r12b += conj(q1[u]) * v[u];
-      }
-      r12b = warp_sum(r12b);
-      double n22 = 0;
-      for (int u = 0; u < kPer; ++u) {
-        v[u] -= r12b * q1[u];
-        n22 += norm2(v[u]);
-      }
-      r12 += r12b;
-      double r22 = sqrt(warp_sum(n22));
-      zd b1(0.0), b2(0.0);
-      for (int u = 0; u < kPer; ++u) {
+        Iv[u] = i < ns ? a.I[(int64_t)(off + i) * a.P + e] : zd(0.0);
         b1 += conj(q1[u]) * Iv[u];
-        b2 += conj(v[u] / r22) * Iv[u];
+        b2 += conj(q2[u]) * Iv[u];
       }
       b1 = warp_sum(b1);
       b2 = warp_sum(b2);
-      zd c1 = b2 / zd(r22);
-      zd c0 = (b1 - r12 * c1) / zd(r11);
+      const zd c1 = b2 / zd(r22);
+      const zd c0 = (b1 - r12 * c1) / zd(r11);
       double rr = 0;
+#pragma unroll
       for (int u = 0; u < kPer; ++u) {
         zd d = c0 * ep[u] + c1 * em[u] - Iv[u];
         rr += norm2(d);
@@ -248,8 +258,9 @@ __device__ double wave_objective(const FitArgs& a, int grp, zd g, double Inrm, d
   nd = 0;
   for (int p = 0; p < a.P; ++p) {
     if (a.group_of[p] != grp) continue;
+    const int ns = a.ns[p], off = a.s_off[p];
     for (int e = 0; e < a.P; ++e, ++nd) {
-      const int ns = a.ns[p], off = a.s_off[p];
+#pragma unroll
       for (int u = 0; u < kPer; ++u)
         if (lane + 32 * u < ns) {
           zd Vv = a.V[(int64_t)(off + lane + 32 * u) * a.P + e];

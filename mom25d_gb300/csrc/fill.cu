@@ -25,7 +25,7 @@ namespace m25 {
 
 template <class T>
 struct FillArgs {
-  int nt, nb, nlev, nblocks, n_src_chunk;
+  int nt, nb, nlev, nblocks, n_src_chunk, n_chunks;
   const TriData<T>* td;
   const double* cen;
   const int32_t* tri_layer;
@@ -141,26 +141,34 @@ __device__ __forceinline__ void source_pass(const FillArgs<T>& a, const TriData<
 template <class T>
 __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int blk = blockIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   const int L = a.nlev;
-  const int lt = a.block_level[blk];
   const int n = a.nrho;
   // tables of the pairs (lt, ls): radii, then per source level (n-1) x 16 values [A, V]
   T* xs = reinterpret_cast<T*>(smem_raw);
   T* tabs = xs + ((n + 3) & ~3);
   for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i] = a.rho[i];
-  for (int ls = 0; ls < L; ++ls) {
-    const cx<T>* src = reinterpret_cast<const cx<T>*>(a.coef) + (size_t)(lt * L + ls) * (n - 1) * 12;
-    T* dst = tabs + (size_t)ls * (n - 1) * 16;
-    for (int e = threadIdx.x; e < (n - 1) * 8; e += blockDim.x) {
-      int iv = e >> 3, r = e & 7, p = r >> 1, which = r & 1;  // power p, kernel A(0) / V(1)
-      cx<T> v = src[((size_t)iv * 4 + p) * 3 + which];
-      dst[(size_t)iv * 16 + p * 4 + which * 2] = v.re;
-      dst[(size_t)iv * 16 + p * 4 + which * 2 + 1] = v.im;
+  int loaded = -1;
+  // persistent grid: work items (test block, source chunk) taken round-robin
+  const int nitems = a.nblocks * a.n_chunks;
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+  const int blk = item / a.n_chunks, chunk = item % a.n_chunks;
+  const int lt = a.block_level[blk];
+  if (lt != loaded) {  // same for the whole CTA
+    __syncthreads();
+    for (int ls = 0; ls < L; ++ls) {
+      const cx<T>* src = reinterpret_cast<const cx<T>*>(a.coef) + (size_t)(lt * L + ls) * (n - 1) * 12;
+      T* dst = tabs + (size_t)ls * (n - 1) * 16;
+      for (int e = threadIdx.x; e < (n - 1) * 8; e += blockDim.x) {
+        int iv = e >> 3, r = e & 7, p = r >> 1, which = r & 1;  // power p, kernel A(0) / V(1)
+        cx<T> v = src[((size_t)iv * 4 + p) * 3 + which];
+        dst[(size_t)iv * 16 + p * 4 + which * 2] = v.re;
+        dst[(size_t)iv * 16 + p * 4 + which * 2 + 1] = v.im;
+      }
     }
+    __syncthreads();
+    loaded = lt;
   }
-  __syncthreads();
 
   const int t = a.block_tris[blk * 32 + lane];
   const bool active = t >= 0;
@@ -186,7 +194,7 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
   const int pad = active ? a.pad_pos[tt] : -1;
   const int64_t col0 = (int64_t)(blk * 32 + lane) * 3;
 
-  const int s_begin = blockIdx.y * a.n_src_chunk;
+  const int s_begin = chunk * a.n_src_chunk;
   const int s_end = min(a.nt, s_begin + a.n_src_chunk);
   for (int s = s_begin + warp; s < s_end; s += nwarp) {
     const int code = a.cls[(int64_t)blk * a.nt + s];
@@ -247,6 +255,7 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
       if (pad >= 0) a.IVpad[(int64_t)pad * a.nt + s] = IV;
     }
   }
+  }  // work items
 }
 
 // Z[m][n] = 0.5 (Zr[m][n] + Zr[n][m]), Zr[m][n] = sum over the two triangles
@@ -449,14 +458,17 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   M25_CUDA(cudaFuncSetAttribute(fill_tri_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int occ = 1;
   M25_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fill_tri_kernel<T>, 256, smem));
-  int want = std::max(1, 2 * occ * ctx->num_sms);
-  int nchunk = std::max(1, std::min((want + geom->nblocks - 1) / geom->nblocks, (nt + 7) / 8));
+  // persistent grid (a whole number of waves); ~16 work items per CTA of at
+  // least 64 sources each keep the round-robin tail short
+  const int grid = std::max(1, occ) * ctx->num_sms;
+  int nchunk = std::max(1, std::min((16 * grid + geom->nblocks - 1) / geom->nblocks, (nt + 63) / 64));
   a.n_src_chunk = (nt + nchunk - 1) / nchunk;
   nchunk = (nt + a.n_src_chunk - 1) / a.n_src_chunk;
+  a.n_chunks = nchunk;
   if (nv) M25_CUDA(cudaMemsetAsync(IVpad, 0, sizeof(cx<T>) * (size_t)geom->npad * nt, st));
   {
     StageTimer tm(ctx, ST_FILL);
-    fill_tri_kernel<T><<<dim3(geom->nblocks, nchunk), 256, smem, st>>>(a);
+    fill_tri_kernel<T><<<std::min(grid, geom->nblocks * nchunk), 256, smem, st>>>(a);
   }
   M25_CHECK_LAUNCH();
   {

@@ -626,9 +626,10 @@ struct WaveArgs {
 template <class TF, class TV>
 __global__ void __launch_bounds__(256) trsv_wave_kernel(WaveArgs<TF, TV> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<TF>* T = reinterpret_cast<cx<TF>*>(smem_raw);   // (64, 65) one tile of the factor
-  cx<TV>* acc = reinterpret_cast<cx<TV>*>(T + 64 * 65);  // (64, 8)
-  cx<TV>* y = acc + 64 * 8;                                // (64, 8)
+  cx<TF>* T = reinterpret_cast<cx<TF>*>(smem_raw);   // (64, 65) one off-diagonal tile of the factor
+  cx<TF>* Dg = T + 64 * 65;                          // (64, 65) the diagonal tile, fetched up front
+  cx<TV>* acc = reinterpret_cast<cx<TV>*>(Dg + 64 * 65);  // (64, 8)
+  cx<TV>* y = acc + 64 * 8;                                 // (64, 8)
   __shared__ int fail;
   const int G = gridDim.x, P = a.nrhs;
   const int nblk = (a.n + 63) / 64;
@@ -637,6 +638,10 @@ __global__ void __launch_bounds__(256) trsv_wave_kernel(WaveArgs<TF, TV> a) {
     const int i = a.upper ? nblk - 1 - q : q;
     const int r0 = i * 64, w = min(64, a.n - r0);
     for (int e = threadIdx.x; e < w * P; e += blockDim.x) acc[e] = a.X[(int64_t)r0 * P + e];
+    for (int e = threadIdx.x; e < w * 64; e += blockDim.x) {
+      int r = e >> 6, c = e & 63;
+      Dg[r * 65 + c] = c < w ? a.A[(int64_t)(r0 + r) * a.lda + r0 + c] : cx<TF>();
+    }
     const int jfirst = a.upper ? nblk - 1 : 0, jstep = a.upper ? -1 : 1;
     for (int j = jfirst; j != i; j += jstep) {
       const int c0 = j * 64, wj = min(64, a.n - c0);
@@ -674,10 +679,6 @@ __global__ void __launch_bounds__(256) trsv_wave_kernel(WaveArgs<TF, TV> a) {
     }
     // diagonal block: forward (unit diagonal) or backward substitution by
     // one warp (lane l owns rows l and l + 32), no block-wide barriers
-    for (int e = threadIdx.x; e < w * 64; e += blockDim.x) {
-      int r = e >> 6, c = e & 63;
-      T[r * 65 + c] = c < w ? a.A[(int64_t)(r0 + r) * a.lda + r0 + c] : cx<TF>();
-    }
     __syncthreads();
     if (threadIdx.x < 32) {
       const int lane = threadIdx.x;
@@ -686,7 +687,7 @@ __global__ void __launch_bounds__(256) trsv_wave_kernel(WaveArgs<TF, TV> a) {
           for (int h = 0; h < 2; ++h) {
             int r = lane + 32 * h;
             if (r > t && r < w) {
-              cx<TV> l(T[r * 65 + t]);
+              cx<TV> l(Dg[r * 65 + t]);
               for (int c = 0; c < P; ++c) acc[r * P + c] -= l * acc[t * P + c];
             }
           }
@@ -695,14 +696,14 @@ __global__ void __launch_bounds__(256) trsv_wave_kernel(WaveArgs<TF, TV> a) {
       } else {
         for (int t = w - 1; t >= 0; --t) {
           if (lane == (t & 31)) {
-            cx<TV> d(T[t * 65 + t]);
+            cx<TV> d(Dg[t * 65 + t]);
             for (int c = 0; c < P; ++c) acc[t * P + c] = acc[t * P + c] / d;
           }
           __syncwarp();
           for (int h = 0; h < 2; ++h) {
             int r = lane + 32 * h;
             if (r < t) {
-              cx<TV> u(T[r * 65 + t]);
+              cx<TV> u(Dg[r * 65 + t]);
               for (int c = 0; c < P; ++c) acc[r * P + c] -= u * acc[t * P + c];
             }
           }
@@ -744,7 +745,7 @@ int lu_solve_wave(m25_ctx* ctx, const cx<TF>* A, int64_t lda, int n, const int32
   }
   int* flags = err + 16;
   M25_CUDA(cudaFuncSetAttribute(permute_kernel<TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  const size_t sm = sizeof(cx<TF>) * 64 * 65 + sizeof(cx<TV>) * 64 * 8 * 2;
+  const size_t sm = sizeof(cx<TF>) * 64 * 65 * 2 + sizeof(cx<TV>) * 64 * 8 * 2;
   M25_CUDA(cudaFuncSetAttribute(trsv_wave_kernel<TF, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   int occ = 0;
   M25_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trsv_wave_kernel<TF, TV>, 256, sm));
@@ -833,18 +834,22 @@ template int lu_solve<float>(m25_ctx*, const zf*, int64_t, int, const int32_t*, 
 // ------------------------------------------------ GMRES iterative refinement
 // Right-hand sides are handled in lockstep (one column per rhs).
 
-// Y[t][c] = sum_k Z[t][k] X[k][c] in fp64, one warp per row
-template <class TZ>
-__global__ void matvec_kernel(int n, int P, const cx<TZ>* __restrict__ Z, int64_t ldz, const zd* __restrict__ X,
-                              zd* __restrict__ Y) {
+// Y[t][c] = sum_k Z[t][k] X[k][c] in fp64, one warp per row; P (the number of
+// right-hand sides) is a template argument so the accumulators stay in registers
+template <class TZ, int P>
+__global__ void matvec_kernel_p(int n, const cx<TZ>* __restrict__ Z, int64_t ldz, const zd* __restrict__ X,
+                                zd* __restrict__ Y) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= n) return;
-  zd acc[8];
+  zd acc[P];
+  const cx<TZ>* row = Z + (int64_t)warp * ldz;
   for (int t = lane; t < n; t += 32) {
-    cx<TZ> zz = Z[(int64_t)warp * ldz + t];
+    cx<TZ> zz = row[t];
     zd z(double(zz.re), double(zz.im));
+#pragma unroll
     for (int c = 0; c < P; ++c) acc[c] += z * X[(int64_t)t * P + c];
   }
+#pragma unroll
   for (int c = 0; c < P; ++c) {
     double re = acc[c].re, im = acc[c].im;
     for (int o = 16; o; o >>= 1) {
@@ -852,6 +857,22 @@ __global__ void matvec_kernel(int n, int P, const cx<TZ>* __restrict__ Z, int64_
       im += __shfl_down_sync(0xffffffffu, im, o);
     }
     if (lane == 0) Y[(int64_t)warp * P + c] = zd(re, im);
+  }
+}
+
+template <class TZ>
+void matvec(int n, int P, const cx<TZ>* Z, int64_t ldz, const zd* X, zd* Y, cudaStream_t st) {
+  const unsigned g = (unsigned)(((size_t)n * 32 + 255) / 256);
+  switch (P) {
+    case 1: matvec_kernel_p<TZ, 1><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
+    case 2: matvec_kernel_p<TZ, 2><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
+    case 3: matvec_kernel_p<TZ, 3><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
+    case 4: matvec_kernel_p<TZ, 4><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
+    case 5: matvec_kernel_p<TZ, 5><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
+    case 6: matvec_kernel_p<TZ, 6><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
+    case 7: matvec_kernel_p<TZ, 7><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
+    case 8: matvec_kernel_p<TZ, 8><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
+    default: break;  // 1 <= P <= 8 is checked by the callers
   }
 }
 
@@ -1043,7 +1064,7 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
   std::vector<zd> hh((size_t)(m + 2) * P), H((size_t)(m + 1) * m * P), g((size_t)(m + 1) * P), cs(m * P), sn(m * P);
   for (int outer = 0; outer < 50; ++outer) {
     // R = B - Z X
-    matvec_kernel<TZ><<<gw, 256, 0, st>>>(n, P, Z, ldz, X, W);
+    matvec<TZ>(n, P, Z, ldz, X, W, st);
     M25_CUDA(cudaMemcpyAsync(R, B, np * sizeof(zd), cudaMemcpyDeviceToDevice, st));
     if ((rc = set_col_scalars(std::vector<zd>(P, zd(-1.0))))) return rc;
     combine_kernel<<<g1, 256, 0, st>>>(n, P, 1, W, 0, ydev, R);
@@ -1081,7 +1102,7 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
     for (; k < m && total < max_iter; ++k, ++total) {
       zd* zk = Zp + np * k;
       if ((rc = precond(V + np * k, zk))) return rc;
-      matvec_kernel<TZ><<<gw, 256, 0, st>>>(n, P, Z, ldz, zk, W);
+      matvec<TZ>(n, P, Z, ldz, zk, W, st);
       // classical Gram-Schmidt, twice
       std::fill(hh.begin(), hh.end(), zd(0.0));
       for (int pass = 0; pass < 2; ++pass) {
