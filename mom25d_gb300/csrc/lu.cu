@@ -526,10 +526,13 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
     // grid size: as many CTAs as can be co-resident, each with >= 1 row
     int occ = 0;
     G = std::min(std::min(m, ctx->num_sms), Gmax);
+    // M25_PANEL_CTAS: fixed panel grid (a tuning knob; 0 or unset = automatic)
+    static const int forced = getenv("M25_PANEL_CTAS") ? atoi(getenv("M25_PANEL_CTAS")) : 0;
+    if (forced > 0) G = std::min(std::min(m, forced), Gmax);
     fits(G, m, panel_smem);
     // fewest CTAs (one per SM) whose row slices fit: the per-column barrier
     // and pivot reduction cost grow with the grid
-    for (int bps = 1; bps <= 4; ++bps) {
+    for (int bps = 1; bps <= 4 && forced <= 0; ++bps) {
       int g = std::min(m, bps * ctx->num_sms);
       size_t smem;
       if (g > Gmax || !fits(g, m, smem)) continue;
@@ -623,11 +626,39 @@ struct WaveArgs {
 // (arithmetic in TV, factors of type TF), publishes y_i and raises flag i.
 // Every wait is bounded; blocks only wait on blocks solved earlier, and the
 // cooperative launch keeps all CTAs resident, so the order cannot deadlock.
+// asynchronous global -> shared copy of one element (8 or 16 bytes); a
+// column outside the matrix is zero-filled without reading global memory
+template <int BYTES>
+__device__ __forceinline__ void cp_async_elem(void* dst, const void* src, bool valid) {
+  unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  int n = valid ? BYTES : 0;
+  if (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(n));
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(n));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// fetch the w x 64 tile at (r0, c0) (columns >= wc zero) into a (64, 65) shared buffer
+template <class TF>
+__device__ __forceinline__ void fetch_tile(cx<TF>* dst, const cx<TF>* A, int64_t lda, int r0, int c0, int w, int wc) {
+  for (int e = threadIdx.x; e < w * 64; e += blockDim.x) {
+    int r = e >> 6, c = e & 63;
+    const cx<TF>* src = A + (int64_t)(r0 + r) * lda + c0 + (c < wc ? c : 0);
+    cp_async_elem<sizeof(cx<TF>)>(&dst[r * 65 + c], src, c < wc);
+  }
+  cp_async_commit();
+}
+
 template <class TF, class TV>
 __global__ void __launch_bounds__(256) trsv_wave_kernel(WaveArgs<TF, TV> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<TF>* T = reinterpret_cast<cx<TF>*>(smem_raw);   // (64, 65) one off-diagonal tile of the factor
-  cx<TF>* Dg = T + 64 * 65;                          // (64, 65) the diagonal tile, fetched up front
+  cx<TF>* Tb[2];
+  Tb[0] = reinterpret_cast<cx<TF>*>(smem_raw);              // (64, 65) off-diagonal tiles, double buffered
+  Tb[1] = Tb[0] + 64 * 65;
+  cx<TF>* Dg = Tb[1] + 64 * 65;                             // (64, 65) the diagonal tile
   cx<TV>* acc = reinterpret_cast<cx<TV>*>(Dg + 64 * 65);  // (64, 8)
   cx<TV>* y = acc + 64 * 8;                                 // (64, 8)
   __shared__ int fail;
@@ -638,17 +669,21 @@ __global__ void __launch_bounds__(256) trsv_wave_kernel(WaveArgs<TF, TV> a) {
     const int i = a.upper ? nblk - 1 - q : q;
     const int r0 = i * 64, w = min(64, a.n - r0);
     for (int e = threadIdx.x; e < w * P; e += blockDim.x) acc[e] = a.X[(int64_t)r0 * P + e];
-    for (int e = threadIdx.x; e < w * 64; e += blockDim.x) {
-      int r = e >> 6, c = e & 63;
-      Dg[r * 65 + c] = c < w ? a.A[(int64_t)(r0 + r) * a.lda + r0 + c] : cx<TF>();
+    fetch_tile(Dg, a.A, a.lda, r0, r0, w, w);
+    // dependencies in order: j = 0 .. i-1 (lower) or nblk-1 .. i+1 (upper)
+    const int ndep = a.upper ? nblk - 1 - i : i;
+    auto dep = [&](int d) { return a.upper ? nblk - 1 - d : d; };
+    if (ndep > 0) {
+      const int j0 = dep(0);
+      fetch_tile(Tb[0], a.A, a.lda, r0, j0 * 64, w, min(64, a.n - j0 * 64));
     }
-    const int jfirst = a.upper ? nblk - 1 : 0, jstep = a.upper ? -1 : 1;
-    for (int j = jfirst; j != i; j += jstep) {
-      const int c0 = j * 64, wj = min(64, a.n - c0);
-      // the tile does not depend on the wait: fetch it first
-      for (int e = threadIdx.x; e < w * 64; e += blockDim.x) {
-        int r = e >> 6, c = e & 63;
-        T[r * 65 + c] = c < wj ? a.A[(int64_t)(r0 + r) * a.lda + c0 + c] : cx<TF>();
+    for (int d = 0; d < ndep; ++d) {
+      const int j = dep(d), c0 = j * 64, wj = min(64, a.n - c0);
+      cx<TF>* T = Tb[d & 1];
+      const bool more = d + 1 < ndep;
+      if (more) {  // next tile in flight while this one is used
+        const int jn = dep(d + 1);
+        fetch_tile(Tb[(d + 1) & 1], a.A, a.lda, r0, jn * 64, w, min(64, a.n - jn * 64));
       }
       if (threadIdx.x == 0) {
         long long it = 0;
@@ -658,12 +693,16 @@ __global__ void __launch_bounds__(256) trsv_wave_kernel(WaveArgs<TF, TV> a) {
             fail = 1;
             break;
           }
-          __nanosleep(64);
+          __nanosleep(32);
         }
         __threadfence();
       }
+      if (more) cp_async_wait<1>(); else cp_async_wait<0>();
       __syncthreads();
-      if (fail) return;
+      if (fail) {
+        cp_async_wait<0>();
+        return;
+      }
       for (int e = threadIdx.x; e < wj * P; e += blockDim.x) {
         volatile cx<TV>* src = &a.X[(int64_t)c0 * P + e];
         y[e] = cx<TV>(src->re, src->im);
@@ -677,9 +716,10 @@ __global__ void __launch_bounds__(256) trsv_wave_kernel(WaveArgs<TF, TV> a) {
       }
       __syncthreads();
     }
+    cp_async_wait<0>();
+    __syncthreads();
     // diagonal block: forward (unit diagonal) or backward substitution by
     // one warp (lane l owns rows l and l + 32), no block-wide barriers
-    __syncthreads();
     if (threadIdx.x < 32) {
       const int lane = threadIdx.x;
       if (!a.upper) {
@@ -696,8 +736,8 @@ __global__ void __launch_bounds__(256) trsv_wave_kernel(WaveArgs<TF, TV> a) {
       } else {
         for (int t = w - 1; t >= 0; --t) {
           if (lane == (t & 31)) {
-            cx<TV> d(Dg[t * 65 + t]);
-            for (int c = 0; c < P; ++c) acc[t * P + c] = acc[t * P + c] / d;
+            cx<TV> dd(Dg[t * 65 + t]);
+            for (int c = 0; c < P; ++c) acc[t * P + c] = acc[t * P + c] / dd;
           }
           __syncwarp();
           for (int h = 0; h < 2; ++h) {
@@ -745,7 +785,7 @@ int lu_solve_wave(m25_ctx* ctx, const cx<TF>* A, int64_t lda, int n, const int32
   }
   int* flags = err + 16;
   M25_CUDA(cudaFuncSetAttribute(permute_kernel<TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  const size_t sm = sizeof(cx<TF>) * 64 * 65 * 2 + sizeof(cx<TV>) * 64 * 8 * 2;
+  const size_t sm = sizeof(cx<TF>) * 64 * 65 * 3 + sizeof(cx<TV>) * 64 * 8 * 2;
   M25_CUDA(cudaFuncSetAttribute(trsv_wave_kernel<TF, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   int occ = 0;
   M25_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trsv_wave_kernel<TF, TV>, 256, sm));
