@@ -151,6 +151,17 @@ int m25_assemble(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, double zs_re, dou
 int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precision, void* Z, const void* B, void* X,
                     int where, double tol, int32_t max_iter, int32_t* info);
 
+/* In-place LU factorisation with partial pivoting of an n x n row-major matrix
+ * (scipy.linalg.lu_factor, used by _dense_solve, Engine/mom25d/solver.py:23):
+ * precision M25_FP64 factors complex128, M25_MIXED complex64 (trailing
+ * updates on the tensor cores unless flags & M25_LU_NO_TENSOR_CORES). On
+ * return A holds L (unit lower, strictly below the diagonal) and U, ipiv the
+ * 0-based row interchanges (row i swapped with ipiv[i], in order). A and ipiv
+ * are host or device memory (where). info = first zero pivot (1-based) or 0. */
+#define M25_LU_NO_TENSOR_CORES 1
+int m25_lu_factor(m25_ctx* ctx, int32_t n, int precision, void* A, int64_t lda, int32_t* ipiv, int where,
+                  int32_t flags, int32_t* info);
+
 /* Allocation-free dense solve (no counterpart in mom25d). For callers that
  * must not allocate device memory themselves or through this library:
  * applications whose device memory belongs to another allocator (a

@@ -173,6 +173,41 @@ extern "C" int m25_assemble(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, double
   return M25_ERR_VALUE;
 }
 
+extern "C" int m25_lu_factor(m25_ctx* ctx, int32_t n, int precision, void* A, int64_t lda, int32_t* ipiv, int where,
+                             int32_t flags, int32_t* info) {
+  if (!ctx || !A || !ipiv || n <= 0 || lda < n || (precision != M25_FP64 && precision != M25_MIXED)) {
+    set_error("m25_lu_factor: bad argument");
+    return M25_ERR_VALUE;
+  }
+  M25_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  const size_t esz = precision == M25_FP64 ? sizeof(zd) : sizeof(zf);
+  void* Ad = A;
+  int32_t* pd = ipiv;
+  int rc;
+  if (where == M25_ON_HOST) {
+    if ((rc = ctx->Zw.ensure(esz * (size_t)n * lda))) return rc;
+    if ((rc = ctx->ipiv.ensure(sizeof(int32_t) * n))) return rc;
+    Ad = ctx->Zw.p;
+    pd = ctx->ipiv.as<int32_t>();
+    M25_CUDA(cudaMemcpyAsync(Ad, A, esz * (size_t)n * lda, cudaMemcpyHostToDevice, st));
+  }
+  int zinfo = 0;
+  if (precision == M25_FP64)
+    rc = lu_factor<double>(ctx, static_cast<zd*>(Ad), lda, n, pd, 64, false, &zinfo);
+  else
+    rc = lu_factor<float>(ctx, static_cast<zf*>(Ad), lda, n, pd, 128,
+                          lu_tc_available() && !(flags & M25_LU_NO_TENSOR_CORES), &zinfo);
+  if (rc) return rc;
+  if (where == M25_ON_HOST) {
+    M25_CUDA(cudaMemcpyAsync(A, Ad, esz * (size_t)n * lda, cudaMemcpyDeviceToHost, st));
+    M25_CUDA(cudaMemcpyAsync(ipiv, pd, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+  }
+  M25_CUDA(cudaStreamSynchronize(st));
+  if (info) *info = zinfo;
+  return M25_OK;
+}
+
 extern "C" int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precision, void* Z, const void* B, void* X,
                                int where, double tol, int32_t max_iter, int32_t* info) {
   if (!ctx || !Z || !B || !X || n <= 0 || nrhs <= 0 || nrhs > 8) {

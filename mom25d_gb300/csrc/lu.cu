@@ -481,6 +481,8 @@ __global__ void max_reduce(int n, const double* __restrict__ v, double* __restri
 
 // ----------------------------------------------------------------- drivers
 int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int nb);  // lu_tc.cu
+int lu_tc_prepare(m25_ctx* ctx, int n, int nb);
+int lu_tc_error(m25_ctx* ctx, int* flag);
 bool lu_tc_available();
 
 template <class T>
@@ -520,6 +522,10 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
   int* candidx = reinterpret_cast<int*>(candval + 2 * Gmax);
   cx<T>* rowj = reinterpret_cast<cx<T>*>(candidx + 2 * Gmax);
   M25_CUDA(cudaMemsetAsync(base, 0, 64, st));
+  if (use_tc) {
+    int rc = lu_tc_prepare(ctx, n, nb);
+    if (rc) return rc;
+  }
   for (int k0 = 0; k0 < n; k0 += nb) {
     const int w = std::min(nb, n - k0);
     const int m = n - k0;
@@ -600,6 +606,15 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
   if (hflags[0]) {
     set_error("dense LU: grid barrier timed out");
     return M25_ERR_CUDA;
+  }
+  if (use_tc) {
+    int tcerr = 0;
+    int rc = lu_tc_error(ctx, &tcerr);
+    if (rc) return rc;
+    if (tcerr) {
+      set_error("dense LU: a wait of the tensor-core update ran out");
+      return M25_ERR_CUDA;
+    }
   }
   *info_host = hflags[1];
   return M25_OK;

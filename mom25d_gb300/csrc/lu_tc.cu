@@ -1,13 +1,501 @@
-// Tensor-core trailing update of the complex64 LU (tcgen05), see below.
+// Tensor-core (tcgen05) trailing update of the complex64 LU:
+//
+//   A22 -= L21 U12          (complex, interleaved re/im, row-major, lda)
+//
+// written as one real GEMM on the interleaved storage: C (m x 2n') -=
+// A (m x 2K) B (2K x 2n') with A the interleaved conj(L21) and B rows
+// (U, -iU) alternating, which gives Re and Im of L U in the even and odd
+// columns of C. Each fp32 operand is split into tf32 hi + lo parts and the
+// three products lo.hi + hi.lo + hi.hi are concatenated along K (3xTF32) so
+// one kind::tf32 GEMM with K3 = 3 P (P = 2K rounded up to 64) does the update.
+//
+// The tensor cores round their fp32 accumulation with a bias, so a long
+// accumulation chain loses about four bits against fp32 fused multiply-adds.
+// The K loop is therefore cut into chunks of a few k-blocks: each chunk is
+// accumulated afresh in one of two TMEM buffers and the epilogue warps add the
+// chunk results into fp32 registers with round-to-nearest (the accumulation
+// outside the tensor cores of Ootomo & Yokota, 2022), which keeps the update
+// at the accuracy of the SIMT one.
+//
+// Kernel (persistent, one CTA per SM, 320 threads): warp 0 issues TMA loads of
+// 128B-swizzled K-major tiles (A 128 x 32, B 192 x 32 fp32) into a 3-stage
+// mbarrier ring; warp 1 owns the TMEM (two 128 x 192 fp32 buffers) and one
+// elected thread issues tcgen05.mma (M 128, N 192, K 8); warps 2-9 prefetch
+// the tile of C into shared memory (cp.async) when the tile starts, read the
+// chunk results with tcgen05.ld and sum them, and at the end of the tile
+// apply C -= sum in shared memory and store C with coalesced rows, so that the
+// HBM latency of the read-modify-write of C hides behind the MMAs. Every
+// mbarrier wait is bounded in iterations and wall-clock time; on a timeout
+// the CTA raises an error word, stops all roles, waits (bounded) for its TMA
+// copies and MMAs, frees its TMEM and returns.
+#include <cuda.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+
 #include "m25_internal.h"
 
 namespace m25 {
 
-bool lu_tc_available() { return false; }
+namespace {
 
-int lu_gemm_tc(m25_ctx*, zf*, int64_t, int, int, int) {
-  set_error("tensor-core LU update not built");
-  return M25_ERR_CUDA;
+constexpr int kBM = 128, kBN = 192, kBK = 32, kStages = 3;
+constexpr int kTmemCols = 512, kBufStride = 256;  // two accumulators, 256 columns apart
+constexpr int kTileA = kBM * kBK * 4, kTileB = kBN * kBK * 4, kStageBytes = kTileA + kTileB;
+constexpr int kEpiWarps = 8, kThreads = 64 + 32 * kEpiWarps;
+constexpr int kCTileBytes = kBM * kBN * 4;  // the tile of C, prefetched while the MMAs run
+constexpr int kSmemBytes = kStages * kStageBytes + kCTileBytes + 1024;
+constexpr long long kWaitLimit = 1LL << 24;
+constexpr unsigned long long kWaitNs = 200ull * 1000 * 1000;  // 200 ms wall clock per wait
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+// Bounded wait for the phase with the given parity: false on a timeout (an
+// iteration limit and a wall-clock limit) or, when abort is given, as soon as
+// another role of the CTA has raised it.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, const volatile int* abort = nullptr) {
+  uint32_t addr = smem_u32(bar);
+  unsigned long long t0;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t0));
+  for (long long it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (abort && *abort) return false;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    if (t - t0 > kWaitNs) return false;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::
+          "r"(smem_u32(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;            // leading-dimension offset (unused with this swizzle)
+  d |= (uint64_t)(1024 >> 4) << 32;  // stride between 8-row groups
+  d |= (uint64_t)1 << 46;            // descriptor version
+  d |= (uint64_t)2 << 61;            // 128-byte swizzle
+  return d;
+}
+
+// instruction descriptor: D f32, A and B tf32, both K-major, N = kBN, M = 128
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kBN >> 3) << 17) |
+                            ((uint32_t)(kBM >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+struct TcArgs {
+  float* C;        // fp32 view of the complex matrix at the trailing block's origin
+  int64_t ldc;     // in floats
+  int M, N, K3;    // rows, real columns, packed K (multiple of 32)
+  int tiles_m, ntiles;
+  int chunk;       // k-blocks accumulated afresh in TMEM before the register sum
+  int* err;
+};
+
+// one CTA per SM; 10 warps put three on one SM sub-partition, which caps a
+// thread at 168 registers (96 running sums per epilogue thread fit)
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-byte alignment of the swizzled tiles
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  float* ctile = reinterpret_cast<float*>(base + kStages * kStageBytes);  // [kBM][kBN], swizzled
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], tfull[2], tempty[2], done;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag, n_issued, n_consumed, skip;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nk = a.K3 / kBK;
+  const int nch = (nk + a.chunk - 1) / a.chunk;
+  // an earlier CTA gave up: leave before taking TMEM
+  if (threadIdx.x == 0) skip = *(volatile int*)a.err;
+  __syncthreads();
+  if (skip) return;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], kEpiWarps);
+    }
+    mbar_init(&done, 1);
+    abort_flag = 0;
+    n_issued = 0;
+    n_consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];\n" ::"l"(&tmA) : "memory");
+    asm volatile("prefetch.tensormap [%0];\n" ::"l"(&tmB) : "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  volatile int* abort_v = &abort_flag;
+
+  if (warp == 0) {
+    // TMA producer
+    if (lane == 0) {
+      int it = 0;
+      for (int t = blockIdx.x; t < a.ntiles && !*abort_v; t += gridDim.x) {
+        const int m0 = (t % a.tiles_m) * kBM, n0 = (t / a.tiles_m) * kBN;
+        for (int kb = 0; kb < nk; ++kb, ++it) {
+          const int s = it % kStages;
+          if (it >= kStages && !mbar_wait(&empty[s], ((it / kStages) - 1) & 1, abort_v)) {
+            *abort_v = 1;
+            break;
+          }
+          unsigned char* sa = base + s * kStageBytes;
+          mbar_expect_tx(&full[s], kStageBytes);
+          tma_load_2d(sa, &tmA, kb * kBK, m0, &full[s]);
+          tma_load_2d(sa + kTileA, &tmB, kb * kBK, n0, &full[s]);
+          n_issued = it + 1;
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // MMA issuer
+    if (lane == 0) {
+      int it = 0, ch = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
+        for (int c = 0; c < nch && ok; ++c, ++ch) {
+          const int b = ch & 1;
+          if (ch >= 2 && !mbar_wait(&tempty[b], ((ch >> 1) - 1) & 1, abort_v)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          const uint32_t acc = tmem + (uint32_t)(b * kBufStride);
+          const int kb1 = min(nk, (c + 1) * a.chunk);
+          for (int kb = c * a.chunk; kb < kb1; ++kb, ++it) {
+            const int s = it % kStages;
+            if (!mbar_wait(&full[s], (it / kStages) & 1, abort_v)) {
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t sa = smem_u32(base + s * kStageBytes), sb = sa + kTileA;
+#pragma unroll
+            for (int k = 0; k < kBK / 8; ++k)  // 8 tf32 = 32 bytes per MMA
+              mma_tf32(acc, smem_desc(sa + 32 * k), smem_desc(sb + 32 * k), (kb > c * a.chunk || k) ? 1u : 0u);
+            mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
+            n_consumed = it + 1;
+          }
+          if (ok) mma_commit(&tfull[b]);
+        }
+      }
+      if (!ok) *abort_v = 1;
+      mma_commit(&done);  // arrives once every MMA issued above has completed
+    }
+  } else {
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31, columns h * 96 .. + 95,
+    // and owns that 32 x 96 block of the C tile in shared memory. The block is
+    // stored with its columns XOR-swizzled by the row within each group of 32,
+    // so that both a row per lane and a row per warp are free of bank conflicts.
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    auto cidx = [&](int r, int c) { return r * kBN + ((c & ~31) | ((c & 31) ^ (r & 31))); };
+    int ch = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
+      const int m0 = (t % a.tiles_m) * kBM, n0 = (t / a.tiles_m) * kBN;
+      // prefetch this warp's block of C (4-byte copies: C rows need only be 8-byte aligned)
+      for (int i = 0; i < 32; ++i) {
+        const int r = q * 32 + i, row = m0 + r;
+#pragma unroll
+        for (int k = 0; k < kBN / 64; ++k) {
+          const int c = h * (kBN / 2) + k * 32 + lane;
+          if (row < a.M && n0 + c < a.N) {
+            const float* src = a.C + (int64_t)row * a.ldc + n0 + c;
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_u32(ctile + cidx(r, c))), "l"(src)
+                         : "memory");
+          }
+        }
+      }
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+      float sum[kBN / 2];
+#pragma unroll
+      for (int j = 0; j < kBN / 2; ++j) sum[j] = 0.f;
+      for (int c = 0; c < nch; ++c, ++ch) {
+        const int b = ch & 1;
+        ok = __all_sync(0xffffffffu, mbar_wait(&tfull[b], (ch >> 1) & 1, abort_v));
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll
+        for (int g = 0; g < kBN / 32; ++g) {
+          uint32_t r[16];
+          const uint32_t taddr =
+              tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kBufStride + h * (kBN / 2) + g * 16);
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                "=r"(r[15])
+              : "r"(taddr));
+          asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+          for (int j = 0; j < 16; ++j) sum[g * 16 + j] += __uint_as_float(r[j]);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&tempty[b]);
+      }
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+      __syncwarp();
+      if (!ok) break;
+      // C -= sum in shared memory (row per lane), then coalesced stores (row per warp)
+      {
+        const int r = q * 32 + lane;
+#pragma unroll
+        for (int j = 0; j < kBN / 2; ++j) ctile[cidx(r, h * (kBN / 2) + j)] -= sum[j];
+      }
+      __syncwarp();
+      for (int i = 0; i < 32; ++i) {
+        const int r = q * 32 + i, row = m0 + r;
+#pragma unroll
+        for (int k = 0; k < kBN / 64; ++k) {
+          const int c = h * (kBN / 2) + k * 32 + lane;
+          if (row < a.M && n0 + c < a.N) a.C[(int64_t)row * a.ldc + n0 + c] = ctile[cidx(r, c)];
+        }
+      }
+      __syncwarp();
+    }
+    if (!ok) *abort_v = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (abort_flag) {
+      atomicExch(a.err, 1);
+      // copies still in flight land before the CTA leaves (bounded waits)
+      for (int i = n_consumed; i < n_issued; ++i) mbar_wait(&full[i % kStages], (i / kStages) & 1);
+    }
+    mbar_wait(&done, 0);
+  }
+  // teardown: all MMAs and loads have completed; free the accumulators
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTmemCols));
+  }
+}
+
+__device__ __forceinline__ float tf32_round(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// A3[r][s P + j] for the trailing rows, planes s = [hi | lo | hi] of the
+// interleaved conj(L21) (j = 2 t + f: f = 0 real part, 1 minus imaginary part)
+__global__ void pack_a_kernel(const zf* __restrict__ LU, int64_t lda, int k0, int w, int m, int P,
+                              float* __restrict__ A3) {
+  const int K3p = 3 * P;
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)m * K3p) return;
+  int r = int(e / K3p), k3 = int(e % K3p);
+  int s = k3 / P, j = k3 % P, t = j >> 1;
+  float out = 0.f;
+  if (t < w) {
+    zf L = LU[(int64_t)(k0 + w + r) * lda + k0 + t];
+    float v = (j & 1) ? -L.im : L.re;
+    float hi = tf32_round(v);
+    out = s == 1 ? tf32_round(v - hi) : hi;
+  }
+  A3[e] = out;
+}
+
+// B3t[c2][s P + j] for the trailing real columns c2 = 2 c + e, planes
+// s = [lo | hi | hi] of the rows (U, -iU); the two small products come first.
+// One block transposes a 32 (t) x 32 (c) complex tile of U12 through shared
+// memory so that both the reads of U and the writes of B3t are coalesced.
+__global__ void __launch_bounds__(256) pack_b_kernel(const zf* __restrict__ LU, int64_t lda, int k0, int w, int m,
+                                                     int P, float* __restrict__ B3) {
+  __shared__ zf tile[32][33];
+  const int K3p = 3 * P;
+  const int c0 = blockIdx.x * 32, t0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int i = ty; i < 32; i += 8) {
+    const int t = t0 + i, c = c0 + tx;
+    tile[i][tx] = (t < w && c < m) ? LU[(int64_t)(k0 + t) * lda + k0 + w + c] : zf{0.f, 0.f};
+  }
+  __syncthreads();
+  // 3 planes x 64 real columns x 64 floats (32 t x 2 parts)
+  for (int idx = threadIdx.x; idx < 3 * 64 * 64; idx += 256) {
+    const int j = idx & 63, row = idx >> 6;
+    const int s = row >> 6, c2l = row & 63;
+    const int c = c2l >> 1, ee = c2l & 1, t = j >> 1, f = j & 1;
+    if (c0 + c >= m) continue;
+    const zf U = tile[t][c];
+    const float v = ee == 0 ? (f == 0 ? U.re : U.im) : (f == 0 ? U.im : -U.re);
+    const float hi = tf32_round(v);
+    B3[(int64_t)(2 * c0 + c2l) * K3p + s * P + 2 * t0 + j] = s == 0 ? tf32_round(v - hi) : hi;
+  }
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+int make_map(CUtensorMap* map, const float* ptr, int rows, int cols_k, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) {
+    set_error("tensor-core LU: cuTensorMapEncodeTiled is not available");
+    return M25_ERR_CUDA;
+  }
+  cuuint64_t dims[2] = {(cuuint64_t)cols_k, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)cols_k * sizeof(float)};
+  cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(ptr), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("tensor-core LU: cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return M25_ERR_CUDA;
+  }
+  return M25_OK;
+}
+
+}  // namespace
+
+bool lu_tc_available() {
+  static int avail = -1;
+  if (avail < 0) {
+    int dev = 0, major = 0, minor = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    const char* off = getenv("M25_NO_TENSOR_CORES");
+    avail = (major == 10 && minor == 3 && encode_fn() != nullptr && !(off && *off == '1')) ? 1 : 0;
+  }
+  return avail == 1;
+}
+
+// packed width of one plane for a panel of w complex columns
+inline int plane_width(int w) { return (2 * w + 63) / 64 * 64; }
+
+// Operand buffer for the factorisation of an n x n matrix with panels of
+// nb: [0, 256) error word, then the packed A3 and B3 of the largest update.
+int lu_tc_prepare(m25_ctx* ctx, int n, int nb) {
+  const int m = std::max(n - nb, 1);
+  const int K3p = 3 * plane_width(nb);
+  const size_t abytes = sizeof(float) * (size_t)m * K3p, bbytes = sizeof(float) * (size_t)2 * m * K3p;
+  int rc = ctx->Dw.ensure(256 + ((abytes + 255) & ~(size_t)255) + bbytes);
+  if (rc) return rc;
+  M25_CUDA(cudaMemsetAsync(ctx->Dw.p, 0, 256, ctx->stream));
+  return M25_OK;
+}
+
+int lu_tc_error(m25_ctx* ctx, int* flag) {
+  *flag = 0;
+  M25_CUDA(cudaMemcpyAsync(flag, ctx->Dw.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  M25_CUDA(cudaStreamSynchronize(ctx->stream));
+  return M25_OK;
+}
+
+// A22 -= L21 U12 for the panel at k0 of width w (complex64, in place);
+// lu_tc_prepare has sized the operand buffer for this factorisation.
+int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w) {
+  cudaStream_t st = ctx->stream;
+  const int m = n - k0 - w;  // trailing rows = trailing columns
+  if (m <= 0) return M25_OK;
+  const int P = plane_width(w), K3p = 3 * P;
+  const int n2 = 2 * m;
+  const size_t abytes = sizeof(float) * (size_t)m * K3p, bbytes = sizeof(float) * (size_t)n2 * K3p;
+  if (256 + ((abytes + 255) & ~(size_t)255) + bbytes > ctx->Dw.bytes) {
+    set_error("tensor-core LU: operand buffer not prepared for this size");
+    return M25_ERR_VALUE;
+  }
+  int* err = ctx->Dw.as<int>();
+  float* A3 = reinterpret_cast<float*>(ctx->Dw.as<char>() + 256);
+  float* B3 = reinterpret_cast<float*>(reinterpret_cast<char*>(A3) + ((abytes + 255) & ~(size_t)255));
+  {
+    int64_t ta = (int64_t)m * K3p;
+    pack_a_kernel<<<(unsigned)((ta + 255) / 256), 256, 0, st>>>(A, lda, k0, w, m, P, A3);
+    dim3 gb((m + 31) / 32, P / 64);
+    pack_b_kernel<<<gb, 256, 0, st>>>(A, lda, k0, w, m, P, B3);
+  }
+  CUtensorMap ma, mb;
+  int rc;
+  if ((rc = make_map(&ma, A3, m, K3p, kBM))) return rc;
+  if ((rc = make_map(&mb, B3, n2, K3p, kBN))) return rc;
+  static int n_sm = 0, chunk = 0;
+  if (!n_sm) {
+    int dev = 0;
+    M25_CUDA(cudaGetDevice(&dev));
+    M25_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+    const char* e = getenv("M25_TC_CHUNK");
+    chunk = e ? std::max(1, atoi(e)) : 2;
+  }
+  TcArgs ta;
+  ta.C = reinterpret_cast<float*>(A + (int64_t)(k0 + w) * lda + k0 + w);
+  ta.ldc = 2 * lda;
+  ta.M = m;
+  ta.N = n2;
+  ta.K3 = K3p;
+  ta.tiles_m = (m + kBM - 1) / kBM;
+  ta.ntiles = ta.tiles_m * ((n2 + kBN - 1) / kBN);
+  ta.chunk = chunk;
+  ta.err = err;
+  M25_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+  tc_gemm_kernel<<<std::min(ta.ntiles, n_sm), kThreads, kSmemBytes, st>>>(ma, mb, ta);
+  M25_CHECK_LAUNCH();
+  return M25_OK;
 }
 
 }  // namespace m25

@@ -19,13 +19,14 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libm25.so")
 
 M25_OK, M25_ERR_VALUE, M25_ERR_MEMORY, M25_ERR_CUDA, M25_ERR_NUMERIC = range(5)
 M25_FP64, M25_MIXED, M25_MIXED_FILL32 = 0, 1, 2
+M25_LU_NO_TENSOR_CORES = 1
 M25_ON_HOST, M25_ON_DEVICE = 0, 1
 
 EXPORTS = ("m25_last_error", "m25_version", "m25_ctx_create", "m25_ctx_destroy", "m25_ctx_synchronize",
            "m25_ctx_stream", "m25_geometry_create", "m25_geometry_destroy", "m25_geometry_stats",
            "m25_greens_create", "m25_greens_destroy", "m25_greens_tables", "m25_assemble", "m25_dense_solve",
            "m25_ports_create", "m25_ports_destroy", "m25_deembed", "m25_sweep_point", "m25_deembed_debug",
-           "m25_ctx_timing", "m25_dense_solve_noalloc")
+           "m25_ctx_timing", "m25_dense_solve_noalloc", "m25_lu_factor")
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
@@ -92,6 +93,7 @@ def load():
     lib.m25_deembed_debug.argtypes = [vp, vp, _f64p, _f64p, _f64p, _f64p]
     lib.m25_ctx_timing.argtypes = [vp, C.c_int, _f64p, C.POINTER(C.c_longlong)]
     lib.m25_dense_solve_noalloc.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, vp, vp, _i32p]
+    lib.m25_lu_factor.argtypes = [vp, C.c_int32, C.c_int, vp, C.c_int64, _i32p, C.c_int, C.c_int32, _i32p]
     _lib = lib
     return lib
 

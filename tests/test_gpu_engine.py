@@ -269,3 +269,46 @@ def test_bad_mesh_is_rejected(gpu):
     with pytest.raises(ValueError):
         sol.geometry()
     sol.close()
+
+
+# ------------------------------------------------ LU factors, tensor cores
+def _lu_reconstruct(F, piv):
+    n = F.shape[0]
+    L = np.tril(F, -1) + np.eye(n)
+    U = np.triu(F)
+    perm = np.arange(n)
+    for i, p in enumerate(piv):
+        perm[[i, p]] = perm[[p, i]]
+    return L @ U, perm
+
+
+@pytest.mark.parametrize("n", [300, 1000, 1301])
+def test_lu_complex64_tensor_cores_reconstruct(gpu, n):
+    """complex64 LU with tcgen05 3xTF32 trailing updates: P L U = A to fp32
+    accuracy. The tensor cores' fp32 accumulation rounds differently from
+    SIMT fused multiply-adds, so the bound against the SIMT factorisation is
+    a factor of 16; a wrong tile or operand split gives O(1) errors. (The
+    pivot sequences may part where two candidates tie to rounding, so the
+    factors themselves are not compared.)"""
+    import ctypes as C
+
+    from mom25d_gb300 import engine as E
+
+    ctx = E.Context(0)
+    rng = np.random.default_rng(n)
+    A = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))).astype(np.complex64)
+    errs = {}
+    for flags in (0, E.M25_LU_NO_TENSOR_CORES):
+        F = A.copy()
+        piv = np.zeros(n, np.int32)
+        info = np.zeros(1, np.int32)
+        E.check(ctx.lib.m25_lu_factor(ctx.h, n, E.M25_MIXED, F.ctypes.data, n, E.ptr(piv, C.c_int32), E.M25_ON_HOST,
+                                      flags, E.ptr(info, C.c_int32)))
+        LU, perm = _lu_reconstruct(F.astype(np.complex128), piv)
+        err = np.abs(LU - A[perm]).max() / np.abs(A).max()
+        assert info[0] == 0
+        assert err < 5e-5 * np.sqrt(n / 300), (flags, err)
+        errs[flags] = err
+    print("P L U - A, tensor cores / SIMT:", errs)
+    assert errs[0] <= 16 * errs[E.M25_LU_NO_TENSOR_CORES], errs
+    ctx.close()
