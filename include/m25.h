@@ -185,7 +185,7 @@ int m25_lu_factor(m25_ctx* ctx, int32_t n, int precision, void* A, int64_t lda, 
  * the first zero pivot (1-based) or 0. Returns after the stream has
  * finished the solve. */
 #define M25_NOALLOC_MAX_N 24576
-#define M25_NOALLOC_SCRATCH_BYTES (448 * 1024)
+#define M25_NOALLOC_SCRATCH_BYTES (512 * 1024)
 int m25_dense_solve_noalloc(int32_t n, int32_t nrhs, void* Z, const void* B, void* X, int32_t* ipiv, void* stream,
                             int32_t* info);
 

@@ -41,13 +41,13 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
 
 // lu.cu
 template <class T> int lu_factor(m25_ctx*, cx<T>*, int64_t, int, int32_t*, int, bool, int*);
-template <class T> int lu_solve(m25_ctx*, const cx<T>*, int64_t, int, const int32_t*, const cx<T>*, int, cx<T>*);
 template <class TZ>
 int refine(m25_ctx*, int, int, const cx<TZ>*, int64_t, const zf*, const int32_t*, const zd*, zd*, double, int, int*);
 void cast_to_z32(m25_ctx*, const zd*, int64_t, zf*, int64_t, int, int);
 bool lu_tc_available();
 template <class TF, class TV>
-int lu_solve_wave(m25_ctx*, const cx<TF>*, int64_t, int, const int32_t*, const cx<TV>*, int, cx<TV>*);
+int lu_solve_wave(m25_ctx*, const cx<TF>*, int64_t, int, const int32_t*, const cx<TV>*, int, cx<TV>*,
+                  const int32_t* perm = nullptr);
 int lu_wave_error(m25_ctx*, int, int*);
 
 }  // namespace m25

@@ -331,11 +331,10 @@ __global__ void __launch_bounds__(256) gemm_kernel(cx<T>* A, int64_t lda, int n,
     }
 }
 
-// perm from the interchange list (sequential in shared memory), then the
-// gather Bp[i] = B[perm[i]].
-template <class T>
-__global__ void permute_kernel(int n, int nrhs, const int32_t* __restrict__ ipiv, const cx<T>* __restrict__ B,
-                               cx<T>* __restrict__ Bp) {
+// perm from the interchange list: perm[i] = the original row that ends in
+// row i after the interchanges (sequential in shared memory, one thread;
+// built once per factorisation)
+__global__ void perm_kernel(int n, const int32_t* __restrict__ ipiv, int32_t* __restrict__ perm_out) {
   extern __shared__ int perm[];
   for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = i;
   __syncthreads();
@@ -349,101 +348,17 @@ __global__ void permute_kernel(int n, int nrhs, const int32_t* __restrict__ ipiv
       }
     }
   __syncthreads();
-  for (int e = threadIdx.x; e < n * nrhs; e += blockDim.x) {
-    int i = e / nrhs, c = e % nrhs;
-    Bp[e] = B[(int64_t)perm[i] * nrhs + c];
-  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) perm_out[i] = perm[i];
 }
 
-// Triangular solve of one diagonal block (rows b0..b0+bs-1) in one CTA;
-// lower: unit diagonal, forward; upper: backward with the diagonal. Factors
-// of element type TF, vectors and arithmetic in TV (complex64 factors are
-// applied in fp64 by the refinement).
-template <class TF, class TV>
-__global__ void trsv_block_kernel(const cx<TF>* __restrict__ A, int64_t lda, int b0, int bs, int nrhs, int upper,
-                                  cx<TV>* __restrict__ X) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<TF>* Ls = reinterpret_cast<cx<TF>*>(smem_raw);  // (bs, bs + 1): the diagonal block
-  __shared__ cx<TV> xs[64][8];
-  const int ld = bs + 1;
-  for (int e = threadIdx.x; e < bs * bs; e += blockDim.x) {
-    int r = e / bs, c = e % bs;
-    Ls[r * ld + c] = A[(int64_t)(b0 + r) * lda + b0 + c];
-  }
-  for (int e = threadIdx.x; e < bs * nrhs; e += blockDim.x) xs[e / nrhs][e % nrhs] = X[(int64_t)(b0 + e / nrhs) * nrhs + e % nrhs];
-  __syncthreads();
-  if (!upper) {
-    for (int t = 0; t < bs; ++t) {
-      for (int e = threadIdx.x; e < (bs - 1 - t) * nrhs; e += blockDim.x) {
-        int r = t + 1 + e / nrhs, c = e % nrhs;
-        xs[r][c] -= cx<TV>(Ls[r * ld + t]) * xs[t][c];
-      }
-      __syncthreads();
-    }
-  } else {
-    for (int t = bs - 1; t >= 0; --t) {
-      if (threadIdx.x < nrhs) xs[t][threadIdx.x] = xs[t][threadIdx.x] / cx<TV>(Ls[t * ld + t]);
-      __syncthreads();
-      for (int e = threadIdx.x; e < t * nrhs; e += blockDim.x) {
-        int r = e / nrhs, c = e % nrhs;
-        xs[r][c] -= cx<TV>(Ls[r * ld + t]) * xs[t][c];
-      }
-      __syncthreads();
-    }
-  }
-  for (int e = threadIdx.x; e < bs * nrhs; e += blockDim.x) X[(int64_t)(b0 + e / nrhs) * nrhs + e % nrhs] = xs[e / nrhs][e % nrhs];
-}
-
-// X[r] -= A[r][b0:b0+bs] X[b0:b0+bs] for the rows r in [r_lo, r_hi): one warp per row.
-template <class TF, class TV>
-__global__ void trsv_update_kernel(const cx<TF>* __restrict__ A, int64_t lda, int b0, int bs, int nrhs, int r_lo,
-                                   int r_hi, cx<TV>* __restrict__ X) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  int r = r_lo + warp;
-  if (r >= r_hi) return;
-  cx<TV> acc[8];
-  for (int t = lane; t < bs; t += 32) {
-    cx<TV> l(A[(int64_t)r * lda + b0 + t]);
-    for (int c = 0; c < nrhs; ++c) acc[c] += l * X[(int64_t)(b0 + t) * nrhs + c];
-  }
-  for (int c = 0; c < nrhs; ++c) {
-    TV re = acc[c].re, im = acc[c].im;
-    for (int o = 16; o; o >>= 1) {
-      re += __shfl_down_sync(0xffffffffu, re, o);
-      im += __shfl_down_sync(0xffffffffu, im, o);
-    }
-    if (lane == 0) X[(int64_t)r * nrhs + c] -= cx<TV>(re, im);
-  }
-}
-
-// r = B - Z X in fp64 (Z complex128 or complex64); one warp per row; also
-// the max-abs of r per row for the stopping test.
-template <class TZ>
-__global__ void residual_kernel(int n, int nrhs, const cx<TZ>* __restrict__ Z, int64_t ldz,
-                                const zd* __restrict__ B, const zd* __restrict__ X, zd* __restrict__ Rr,
-                                double* __restrict__ rmax) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (warp >= n) return;
-  zd acc[8];
-  for (int t = lane; t < n; t += 32) {
-    cx<TZ> zz = Z[(int64_t)warp * ldz + t];
-    zd z(double(zz.re), double(zz.im));
-    for (int c = 0; c < nrhs; ++c) acc[c] += z * X[(int64_t)t * nrhs + c];
-  }
-  double m = 0;
-  for (int c = 0; c < nrhs; ++c) {
-    double re = acc[c].re, im = acc[c].im;
-    for (int o = 16; o; o >>= 1) {
-      re += __shfl_down_sync(0xffffffffu, re, o);
-      im += __shfl_down_sync(0xffffffffu, im, o);
-    }
-    if (lane == 0) {
-      zd r = B[(int64_t)warp * nrhs + c] - zd(re, im);
-      Rr[(int64_t)warp * nrhs + c] = r;
-      m = fmax(m, cabs1(r));
-    }
-  }
-  if (lane == 0) rmax[warp] = m;
+// Bp[i] = B[perm[i]] for every right-hand side
+template <class T>
+__global__ void gather_rows_kernel(int n, int nrhs, const int32_t* __restrict__ perm, const cx<T>* __restrict__ B,
+                                   cx<T>* __restrict__ Bp) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)n * nrhs) return;
+  int i = int(e / nrhs), c = int(e % nrhs);
+  Bp[e] = B[(int64_t)perm[i] * nrhs + c];
 }
 
 __global__ void cast_z64_to_z32(const zd* __restrict__ a, int64_t lda, zf* __restrict__ b, int64_t ldb, int n,
@@ -453,30 +368,6 @@ __global__ void cast_z64_to_z32(const zd* __restrict__ a, int64_t lda, zf* __res
   int64_t r = e / m, c = e % m;
   zd v = a[r * lda + c];
   b[r * ldb + c] = zf(float(v.re), float(v.im));
-}
-
-__global__ void scale_to_z32(int64_t n, const zd* __restrict__ r, double s, zf* __restrict__ o) {
-  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < n) o[e] = zf(float(r[e].re * s), float(r[e].im * s));
-}
-
-__global__ void axpy_z32(int64_t n, const zf* __restrict__ d, double s, zd* __restrict__ x) {
-  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < n) x[e] += zd(double(d[e].re) * s, double(d[e].im) * s);
-}
-
-__global__ void max_reduce(int n, const double* __restrict__ v, double* __restrict__ out) {
-  __shared__ double sh[32];
-  double m = 0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, v[i]);
-  for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double r = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, sh[w]);
-    *out = r;
-  }
 }
 
 // ----------------------------------------------------------------- drivers
@@ -628,19 +519,16 @@ struct WaveArgs {
   int64_t lda;
   int n, nrhs, upper;
   cx<TV>* X;       // in: permuted right-hand sides; out: the solution of this sweep
-  int* flags;      // (nblk) == epoch once block k of X is final
+  int* flags;      // (nblk) == epoch once block k of X is final (complex128 vectors)
   int epoch;
   int* err;        // a wait ran out
+  // complex64 vectors: the solved values published with the sweep's epoch in
+  // every 8-byte word, (epoch << 32) | bits of re, then the same for im, so
+  // a reader can poll the data itself (aligned 8-byte accesses are single-copy
+  // atomic); replaces the ready flags and their fences
+  unsigned long long* Yt;
 };
 
-// One triangular sweep as a dependency wavefront (no grid barriers): CTA g
-// owns the 64-row blocks g, g + G, ... For its block i it subtracts the
-// tile products A_ij y_j of the blocks j it depends on (j < i for the unit
-// lower factor, j > i for the upper one) as soon as block j is flagged
-// final, solves the diagonal block by substitution in shared memory
-// (arithmetic in TV, factors of type TF), publishes y_i and raises flag i.
-// Every wait is bounded; blocks only wait on blocks solved earlier, and the
-// cooperative launch keeps all CTAs resident, so the order cannot deadlock.
 // asynchronous global -> shared copy of one element (8 or 16 bytes); a
 // column outside the matrix is zero-filled without reading global memory
 template <int BYTES>
@@ -656,140 +544,339 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
-// fetch the w x 64 tile at (r0, c0) (columns >= wc zero) into a (64, 65) shared buffer
+constexpr int kTileLd = 65;  // padded row of a 64-wide tile in shared memory
+
+// fetch the w x 64 tile at (r0, c0) (columns >= wc zero) into a (64, 65) shared buffer; one commit group
 template <class TF>
 __device__ __forceinline__ void fetch_tile(cx<TF>* dst, const cx<TF>* A, int64_t lda, int r0, int c0, int w, int wc) {
   for (int e = threadIdx.x; e < w * 64; e += blockDim.x) {
     int r = e >> 6, c = e & 63;
     const cx<TF>* src = A + (int64_t)(r0 + r) * lda + c0 + (c < wc ? c : 0);
-    cp_async_elem<sizeof(cx<TF>)>(&dst[r * 65 + c], src, c < wc);
+    cp_async_elem<sizeof(cx<TF>)>(&dst[r * kTileLd + c], src, c < wc);
   }
   cp_async_commit();
 }
 
+// the diagonal w x w tile at (r0, r0), transposed: DgT[c * 65 + r] = A[r0 + r][r0 + c]; one commit group
+template <class TF>
+__device__ __forceinline__ void fetch_diag_t(cx<TF>* DgT, const cx<TF>* A, int64_t lda, int r0, int w) {
+  for (int e = threadIdx.x; e < w * 64; e += blockDim.x) {
+    int r = e >> 6, c = e & 63;
+    const cx<TF>* src = A + (int64_t)(r0 + r) * lda + r0 + (c < w ? c : 0);
+    cp_async_elem<sizeof(cx<TF>)>(&DgT[c * kTileLd + r], src, c < w);
+  }
+  cp_async_commit();
+}
+
+// Substitution on the diagonal block by one warp, in registers: lane l owns
+// the rows 2l and 2l + 1, so each round the owner of a pair of rows solves
+// both locally and broadcasts them with one round of shuffles (32 rounds for
+// 64 rows). Lower: unit diagonal, forward; upper: backward with the
+// reciprocal diagonal dinv. PT right-hand sides as a compile-time count (8:
+// up to 8, the count P checked at run time). acc (rows x P) in and out.
+template <class TF, class TV, int PT>
+__device__ __forceinline__ void diag_solve(int lane, int w, int P, int upper, const cx<TF>* DgT, const cx<TV>* dinv,
+                                           cx<TV>* acc) {
+  const int ra = 2 * lane, rb = ra + 1;
+  cx<TV> va[PT], vb[PT];
+#pragma unroll
+  for (int c = 0; c < PT; ++c) {
+    const bool ok = PT < 8 || c < P;
+    va[c] = (ok && ra < w) ? acc[ra * P + c] : cx<TV>();
+    vb[c] = (ok && rb < w) ? acc[rb * P + c] : cx<TV>();
+  }
+  const int npair = (w + 1) >> 1;
+  // factor of row r at column col: 0 outside the block and outside the triangle
+  auto F = [&](int r, int col) -> cx<TV> {
+    const bool in = r < w && col < w && (upper ? r < col : r > col);
+    return in ? cx<TV>(DgT[min(col, 63) * kTileLd + r]) : cx<TV>();
+  };
+  struct Fac {
+    cx<TV> aA, aB, bA, bB, da, db;  // row ra / rb at column 2k / 2k + 1; reciprocal diagonals of the pair
+  };
+  auto load = [&](int k) {
+    Fac f;
+    const int ca = 2 * k, cb = ca + 1;
+    f.aA = F(ra, ca);
+    f.aB = F(ra, cb);
+    f.bA = F(rb, ca);
+    f.bB = F(rb, cb);
+    if (upper) {
+      f.da = dinv[min(ca, 63)];
+      f.db = cb < w ? dinv[cb] : cx<TV>();
+    }
+    return f;
+  };
+  if (!upper) {
+    Fac nx = load(0);
+    for (int k = 0; k < npair; ++k) {
+      const Fac f = nx;
+      nx = load(min(k + 1, npair - 1));
+      const bool mine = lane == k;
+#pragma unroll
+      for (int c = 0; c < PT; ++c) {
+        if (PT == 8 && c >= P) continue;
+        // owner (lane k): x_2k is final, x_2k+1 = v_2k+1 - L[2k+1][2k] x_2k
+        const cx<TV> xa_own = va[c];
+        const cx<TV> xb_own = vb[c] - f.bA * va[c];
+        const cx<TV> xa(__shfl_sync(0xffffffffu, xa_own.re, k), __shfl_sync(0xffffffffu, xa_own.im, k));
+        const cx<TV> xb(__shfl_sync(0xffffffffu, xb_own.re, k), __shfl_sync(0xffffffffu, xb_own.im, k));
+        // rows below the pair; the owner keeps the two values it broadcast
+        va[c] = mine ? xa : va[c] - (f.aA * xa + f.aB * xb);
+        vb[c] = mine ? xb : vb[c] - (f.bA * xa + f.bB * xb);
+      }
+    }
+  } else {
+    Fac nx = load(npair - 1);
+    for (int k = npair - 1; k >= 0; --k) {
+      const Fac f = nx;
+      nx = load(max(k - 1, 0));
+      const bool mine = lane == k;
+#pragma unroll
+      for (int c = 0; c < PT; ++c) {
+        if (PT == 8 && c >= P) continue;
+        // owner: x_2k+1 = v_2k+1 / d, then x_2k = (v_2k - U[2k][2k+1] x_2k+1) / d
+        const cx<TV> xb_own = vb[c] * f.db;
+        const cx<TV> xa_own = (va[c] - f.aB * xb_own) * f.da;
+        const cx<TV> xa(__shfl_sync(0xffffffffu, xa_own.re, k), __shfl_sync(0xffffffffu, xa_own.im, k));
+        const cx<TV> xb(__shfl_sync(0xffffffffu, xb_own.re, k), __shfl_sync(0xffffffffu, xb_own.im, k));
+        va[c] = mine ? xa : va[c] - (f.aA * xa + f.aB * xb);
+        vb[c] = mine ? xb : vb[c] - (f.bA * xa + f.bB * xb);
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < PT; ++c) {
+    if (PT == 8 && c >= P) continue;
+    if (ra < w) acc[ra * P + c] = va[c];
+    if (rb < w) acc[rb * P + c] = vb[c];
+  }
+  __syncwarp();
+}
+
+// tiles in flight per CTA: 4 complex64 or 2 complex128 tiles
+template <class TF>
+constexpr int wave_stages() {
+  return sizeof(cx<TF>) == 8 ? 4 : 2;
+}
+constexpr int kYtWords = 64 * 8 * 2;  // tagged words of one block of y (64 rows, up to 8 right-hand sides)
 template <class TF, class TV>
-__global__ void __launch_bounds__(256) trsv_wave_kernel(WaveArgs<TF, TV> a) {
+constexpr size_t wave_smem() {
+  return sizeof(cx<TF>) * 64 * kTileLd * (1 + wave_stages<TF>()) + sizeof(cx<TV>) * (64 * 8 * 2 + 64) +
+         (sizeof(TV) == 4 ? sizeof(unsigned long long) * kYtWords * wave_stages<TF>() : 0);
+}
+
+// One triangular sweep as a dependency wavefront (no grid barriers): CTA g
+// owns the 64-row blocks g, g + G, ... For its block i it subtracts the
+// tile products A_ij y_j of the blocks j it depends on (j < i for the unit
+// lower factor, j > i for the upper one, in the order they become final) as
+// soon as block j is flagged final, solves the diagonal block by
+// substitution, publishes y_i and raises flag i. The off-diagonal tiles
+// stream through a ring of cp.async stages so that a CTA's backlog of tiles
+// never holds up the chain; the chain step itself is the flag round trip,
+// one 64 x 64 tile product and the substitution, which one warp runs in
+// registers (lane l owns rows l and l + 32; each solved row is broadcast with
+// shuffles; the upper sweep multiplies by the reciprocal diagonal). Every
+// wait is bounded; blocks only wait on blocks solved earlier, and the
+// cooperative launch keeps all CTAs resident, so the order cannot deadlock.
+template <class TF, class TV>
+__global__ void __launch_bounds__(256, 1) trsv_wave_kernel(WaveArgs<TF, TV> a) {
+  constexpr int S = wave_stages<TF>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<TF>* Tb[2];
-  Tb[0] = reinterpret_cast<cx<TF>*>(smem_raw);              // (64, 65) off-diagonal tiles, double buffered
-  Tb[1] = Tb[0] + 64 * 65;
-  cx<TF>* Dg = Tb[1] + 64 * 65;                             // (64, 65) the diagonal tile
-  cx<TV>* acc = reinterpret_cast<cx<TV>*>(Dg + 64 * 65);  // (64, 8)
-  cx<TV>* y = acc + 64 * 8;                                 // (64, 8)
+  cx<TF>* Dg = reinterpret_cast<cx<TF>*>(smem_raw);  // (64, 65) diagonal tile, transposed
+  cx<TF>* ring = Dg + 64 * kTileLd;                   // S x (64, 65) off-diagonal tiles
+  cx<TV>* acc = reinterpret_cast<cx<TV>*>(ring + S * 64 * kTileLd);  // (64, P)
+  cx<TV>* y = acc + 64 * 8;                                            // (64, P)
+  cx<TV>* dinv = y + 64 * 8;                                           // (64) reciprocal diagonal
+  constexpr bool kTagged = sizeof(TV) == 4;
+  unsigned long long* yring = reinterpret_cast<unsigned long long*>(dinv + 64);  // S x kYtWords (tagged)
+  const unsigned tag = (unsigned)a.epoch;
   __shared__ int fail;
-  const int G = gridDim.x, P = a.nrhs;
+  const int G = gridDim.x, P = a.nrhs, tid = threadIdx.x;
   const int nblk = (a.n + 63) / 64;
-  if (threadIdx.x == 0) fail = 0;
+  if (tid == 0) fail = 0;
+  __syncthreads();
   for (int q = blockIdx.x; q < nblk; q += G) {
     const int i = a.upper ? nblk - 1 - q : q;
     const int r0 = i * 64, w = min(64, a.n - r0);
-    for (int e = threadIdx.x; e < w * P; e += blockDim.x) acc[e] = a.X[(int64_t)r0 * P + e];
-    fetch_tile(Dg, a.A, a.lda, r0, r0, w, w);
-    // dependencies in order: j = 0 .. i-1 (lower) or nblk-1 .. i+1 (upper)
+    // dependencies in the order they become final: j = 0 .. i-1 (lower) or nblk-1 .. i+1 (upper)
     const int ndep = a.upper ? nblk - 1 - i : i;
     auto dep = [&](int d) { return a.upper ? nblk - 1 - d : d; };
-    if (ndep > 0) {
-      const int j0 = dep(0);
-      fetch_tile(Tb[0], a.A, a.lda, r0, j0 * 64, w, min(64, a.n - j0 * 64));
+    // the tile of dependency d (and, for tagged vectors, the published y_j as
+    // it stands now) into ring slot d % S; one commit group per dependency
+    auto fetch_dep = [&](int d) {
+      const int j = dep(d), wj = min(64, a.n - j * 64);
+      if constexpr (kTagged) {
+        unsigned long long* ys = yring + (d % S) * kYtWords;
+        for (int e = threadIdx.x; e < wj * P; e += blockDim.x)  // 16 bytes = one complex value, L2 only
+          cp_async_elem<16>(ys + 2 * e, a.Yt + ((int64_t)j * 64 * P + e) * 2, true);
+      }
+      fetch_tile(ring + (d % S) * 64 * kTileLd, a.A, a.lda, r0, j * 64, w, wj);
+    };
+    // commit groups: the diagonal tile, then one per dependency (dependency d is group d + 1)
+    fetch_diag_t(Dg, a.A, a.lda, r0, w);
+    for (int d = 0; d < S; ++d) {
+      if (d < ndep) fetch_dep(d);
+      else cp_async_commit();
     }
+    for (int e = tid; e < w * P; e += blockDim.x) acc[e] = a.X[(int64_t)r0 * P + e];
     for (int d = 0; d < ndep; ++d) {
       const int j = dep(d), c0 = j * 64, wj = min(64, a.n - c0);
-      cx<TF>* T = Tb[d & 1];
-      const bool more = d + 1 < ndep;
-      if (more) {  // next tile in flight while this one is used
-        const int jn = dep(d + 1);
-        fetch_tile(Tb[(d + 1) & 1], a.A, a.lda, r0, jn * 64, w, min(64, a.n - jn * 64));
-      }
-      if (threadIdx.x == 0) {
-        long long it = 0;
-        while (*(volatile int*)&a.flags[j] != a.epoch) {
-          if (++it > kFlagSpinLimit || *(volatile int*)a.err) {
-            atomicExch(a.err, 1);
-            fail = 1;
-            break;
+      const cx<TF>* T = ring + (d % S) * 64 * kTileLd;
+      if constexpr (kTagged) {
+        cp_async_wait<S - 1>();  // tile d and the prefetched y_j have landed
+        __syncthreads();
+        // words of y_j not yet final when prefetched are polled until they carry this sweep's tag
+        const unsigned long long* ys = yring + (d % S) * kYtWords;
+        bool bad = false;
+        for (int e = tid; e < 64 * P * 2; e += blockDim.x) {
+          float f = 0.f;
+          if (e < wj * P * 2) {
+            unsigned long long v = ys[e];
+            if ((unsigned)(v >> 32) != tag) {
+              const volatile unsigned long long* g = a.Yt + (int64_t)j * 64 * P * 2 + e;
+              long long it = 0;
+              while (true) {
+                v = *g;
+                if ((unsigned)(v >> 32) == tag) break;
+                if (++it > kFlagSpinLimit || *(volatile int*)a.err) {
+                  bad = true;
+                  break;
+                }
+                __nanosleep(20);
+              }
+            }
+            f = __uint_as_float((unsigned)v);
           }
-          __nanosleep(32);
+          if (e & 1) y[e >> 1].im = f;
+          else y[e >> 1].re = f;
         }
-        __threadfence();
+        if (__syncthreads_or(bad)) {
+          if (tid == 0) atomicExch(a.err, 1);
+          cp_async_wait<0>();
+          return;
+        }
+      } else {
+        if (tid == 0) {
+          long long it = 0;
+          while (*(volatile int*)&a.flags[j] != a.epoch) {
+            if (++it > kFlagSpinLimit || *(volatile int*)a.err) {
+              atomicExch(a.err, 1);
+              fail = 1;
+              break;
+            }
+            __nanosleep(32);
+          }
+          __threadfence();
+        }
+        cp_async_wait<S - 1>();  // tile d has landed
+        __syncthreads();
+        if (fail) {
+          cp_async_wait<0>();
+          return;
+        }
+        for (int e = tid; e < 64 * P; e += blockDim.x) {
+          if (e < wj * P) {
+            volatile cx<TV>* src = &a.X[(int64_t)c0 * P + e];
+            y[e] = cx<TV>(src->re, src->im);
+          } else {
+            y[e] = cx<TV>();
+          }
+        }
+        __syncthreads();
       }
-      if (more) cp_async_wait<1>(); else cp_async_wait<0>();
-      __syncthreads();
-      if (fail) {
-        cp_async_wait<0>();
-        return;
+      for (int e = tid; e < w * P; e += blockDim.x) {
+        const int r = e / P, c = e % P;
+        const cx<TF>* Tr = T + r * kTileLd;
+        cx<TV> s0, s1, s2, s3;
+#pragma unroll 4
+        for (int t = 0; t < 64; t += 4) {
+          s0 += cx<TV>(Tr[t]) * y[t * P + c];
+          s1 += cx<TV>(Tr[t + 1]) * y[(t + 1) * P + c];
+          s2 += cx<TV>(Tr[t + 2]) * y[(t + 2) * P + c];
+          s3 += cx<TV>(Tr[t + 3]) * y[(t + 3) * P + c];
+        }
+        acc[e] -= (s0 + s1) + (s2 + s3);
       }
-      for (int e = threadIdx.x; e < wj * P; e += blockDim.x) {
-        volatile cx<TV>* src = &a.X[(int64_t)c0 * P + e];
-        y[e] = cx<TV>(src->re, src->im);
-      }
-      __syncthreads();
-      for (int e = threadIdx.x; e < w * P; e += blockDim.x) {
-        int r = e / P, c = e % P;
-        cx<TV> s;
-        for (int t = 0; t < wj; ++t) s += cx<TV>(T[r * 65 + t]) * y[t * P + c];
-        acc[e] -= s;
-      }
-      __syncthreads();
+      __syncthreads();  // the stage of tile d is free again
+      if (d + S < ndep) fetch_dep(d + S);
+      else cp_async_commit();
     }
     cp_async_wait<0>();
     __syncthreads();
-    // diagonal block: forward (unit diagonal) or backward substitution by
-    // one warp (lane l owns rows l and l + 32), no block-wide barriers
-    if (threadIdx.x < 32) {
-      const int lane = threadIdx.x;
-      if (!a.upper) {
-        for (int t = 0; t < w - 1; ++t) {
-          for (int h = 0; h < 2; ++h) {
-            int r = lane + 32 * h;
-            if (r > t && r < w) {
-              cx<TV> l(Dg[r * 65 + t]);
-              for (int c = 0; c < P; ++c) acc[r * P + c] -= l * acc[t * P + c];
-            }
-          }
-          __syncwarp();
-        }
-      } else {
-        for (int t = w - 1; t >= 0; --t) {
-          if (lane == (t & 31)) {
-            cx<TV> dd(Dg[t * 65 + t]);
-            for (int c = 0; c < P; ++c) acc[t * P + c] = acc[t * P + c] / dd;
-          }
-          __syncwarp();
-          for (int h = 0; h < 2; ++h) {
-            int r = lane + 32 * h;
-            if (r < t) {
-              cx<TV> u(Dg[r * 65 + t]);
-              for (int c = 0; c < P; ++c) acc[r * P + c] -= u * acc[t * P + c];
-            }
-          }
-          __syncwarp();
-        }
-      }
+    if (a.upper && tid < w) {
+      const cx<TV> dd(Dg[tid * kTileLd + tid]);
+      const TV m2 = dd.re * dd.re + dd.im * dd.im;
+      dinv[tid] = cx<TV>(dd.re / m2, -dd.im / m2);
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < w * P; e += blockDim.x) a.X[(int64_t)r0 * P + e] = acc[e];
-    __threadfence();
+    // diagonal block by warp 0, then publish y_i
+    if (tid < 32) {
+      const int lane = tid;
+      switch (P) {
+        case 1: diag_solve<TF, TV, 1>(lane, w, P, a.upper, Dg, dinv, acc); break;
+        case 2: diag_solve<TF, TV, 2>(lane, w, P, a.upper, Dg, dinv, acc); break;
+        case 3: diag_solve<TF, TV, 3>(lane, w, P, a.upper, Dg, dinv, acc); break;
+        case 4: diag_solve<TF, TV, 4>(lane, w, P, a.upper, Dg, dinv, acc); break;
+        default: diag_solve<TF, TV, 8>(lane, w, P, a.upper, Dg, dinv, acc); break;
+      }
+      if constexpr (kTagged) {
+        // publish first (the chain waits on it), then the plain copy for the next sweep
+        const unsigned long long hi = (unsigned long long)tag << 32;
+        volatile unsigned long long* yt = a.Yt + (int64_t)r0 * P * 2;
+        for (int e = lane; e < w * P; e += 32) {
+          const cx<TV> v = acc[e];
+          yt[2 * e] = hi | __float_as_uint((float)v.re);
+          yt[2 * e + 1] = hi | __float_as_uint((float)v.im);
+        }
+      }
+      for (int e = lane; e < w * P; e += 32) a.X[(int64_t)r0 * P + e] = acc[e];
+      if constexpr (!kTagged) __threadfence();
+    }
     __syncthreads();
-    if (threadIdx.x == 0) atomicExch(&a.flags[i], a.epoch);
+    if constexpr (!kTagged) {
+      if (tid == 0) atomicExch(&a.flags[i], a.epoch);
+    }
   }
 }
 
-// X = (LU)^-1 P B: the permutation, then one wavefront launch per factor.
+// perm (n ints, device) of the interchanges in ipiv; once per factorisation
+int lu_make_perm(m25_ctx* ctx, int n, const int32_t* ipiv, int32_t* perm) {
+  if ((size_t)n * sizeof(int) > 200 * 1024) {
+    set_error("dense solve: n <= 51200");
+    return M25_ERR_VALUE;
+  }
+  M25_CUDA(cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  perm_kernel<<<1, 1024, n * sizeof(int), ctx->stream>>>(n, ipiv, perm);
+  M25_CHECK_LAUNCH();
+  return M25_OK;
+}
+
+// X = (LU)^-1 P B: the permutation (from ipiv, or the precomputed perm when
+// given), then one wavefront launch per factor.
 template <class TF, class TV>
 int lu_solve_wave(m25_ctx* ctx, const cx<TF>* A, int64_t lda, int n, const int32_t* ipiv, const cx<TV>* B, int nrhs,
-                  cx<TV>* X) {
+                  cx<TV>* X, const int32_t* perm) {
   cudaStream_t st = ctx->stream;
   if (nrhs > 8 || (size_t)n * sizeof(int) > 200 * 1024) {
     set_error("dense solve: at most 8 right-hand sides and n <= 51200");
     return M25_ERR_VALUE;
   }
   const int nblk = (n + 63) / 64;
-  // layout: [0] wait error, [16 ..] ready flag per block; zeroed whenever
-  // the buffer is (re)allocated (a caller-provided buffer comes zeroed)
+  // layout: [0] wait error, [16 ..] ready flag per block, then the
+  // permutation when it is built here; zeroed whenever the buffer is
+  // (re)allocated (a caller-provided buffer comes zeroed)
+  // then (complex64 vectors) the tagged copy of y, 16 bytes per value
+  const bool tagged = sizeof(TV) == 4;
+  const size_t yt_off = ((sizeof(int) * (nblk + 16 + n)) + 255) / 256 * 256;
   int* err = ctx->ext_flags;
+  if (tagged && err) {
+    set_error("dense solve: complex64 vectors need the context's flag buffer");
+    return M25_ERR_VALUE;
+  }
   if (!err) {
     void* before = ctx->flags.p;
-    int rc = ctx->flags.ensure(sizeof(int) * (nblk + 16));
+    int rc = ctx->flags.ensure(yt_off + (tagged ? sizeof(unsigned long long) * 2 * (size_t)n * 8 : 0));
     if (rc) return rc;
     if (ctx->flags_fresh || ctx->flags.p != before) {
       M25_CUDA(cudaMemsetAsync(ctx->flags.p, 0, ctx->flags.bytes, st));
@@ -799,8 +886,17 @@ int lu_solve_wave(m25_ctx* ctx, const cx<TF>* A, int64_t lda, int n, const int32
     err = ctx->flags.as<int>();
   }
   int* flags = err + 16;
-  M25_CUDA(cudaFuncSetAttribute(permute_kernel<TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  const size_t sm = sizeof(cx<TF>) * 64 * 65 * 3 + sizeof(cx<TV>) * 64 * 8 * 2;
+  unsigned long long* Yt =
+      tagged ? reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(err) + yt_off) : nullptr;
+  if (!Yt && ctx->yt_off && sizeof(int) * (nblk + 16 + n) > ctx->yt_off)
+    ctx->yt_off = 0;  // this call's permutation reaches into the tagged copy of an earlier one
+  if (Yt && ctx->yt_off != yt_off) {
+    // the tagged copy moved (another n): what the buffer held there before
+    // (permutations, flags) must not pass for a tag of this sweep
+    M25_CUDA(cudaMemsetAsync(Yt, 0, sizeof(unsigned long long) * 2 * (size_t)n * 8, st));
+    ctx->yt_off = yt_off;
+  }
+  const size_t sm = wave_smem<TF, TV>();
   M25_CUDA(cudaFuncSetAttribute(trsv_wave_kernel<TF, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   int occ = 0;
   M25_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, trsv_wave_kernel<TF, TV>, 256, sm));
@@ -808,15 +904,29 @@ int lu_solve_wave(m25_ctx* ctx, const cx<TF>* A, int64_t lda, int n, const int32
     set_error("dense solve: the triangular-solve kernel does not fit on an SM");
     return M25_ERR_CUDA;
   }
-  const int G = std::min(nblk, ctx->num_sms * std::min(occ, 2));
+  const int G = std::min(nblk, ctx->num_sms * occ);
   StageTimer tm(ctx, ST_TRSV);
-  permute_kernel<TV><<<1, 1024, n * sizeof(int), st>>>(n, nrhs, ipiv, B, X);
+  if (!perm) {
+    if (ctx->ext_flags) {  // no room for a permutation in a caller-provided flag buffer
+      set_error("dense solve: a precomputed permutation is required here");
+      return M25_ERR_VALUE;
+    }
+    int32_t* pbuf = flags + nblk;
+    int rc = lu_make_perm(ctx, n, ipiv, pbuf);
+    if (rc) return rc;
+    perm = pbuf;
+  }
+  {
+    const int64_t tot = (int64_t)n * nrhs;
+    gather_rows_kernel<TV><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(n, nrhs, perm, B, X);
+  }
   for (int upper = 0; upper < 2; ++upper) {
-    if (++ctx->epoch <= 0) {  // wrapped: start the flags afresh
+    if (++ctx->epoch <= 0) {  // wrapped: start the flags (and tags) afresh
       M25_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * nblk, st));
+      if (Yt) M25_CUDA(cudaMemsetAsync(Yt, 0, sizeof(unsigned long long) * 2 * (size_t)n * 8, st));
       ctx->epoch = 1;
     }
-    WaveArgs<TF, TV> wa{A, lda, n, nrhs, upper, X, flags, ctx->epoch, err};
+    WaveArgs<TF, TV> wa{A, lda, n, nrhs, upper, X, flags, ctx->epoch, err, Yt};
     void* args[] = {&wa};
     M25_CUDA(cudaLaunchCooperativeKernel((void*)trsv_wave_kernel<TF, TV>, dim3(G), dim3(256), args, sm, st));
   }
@@ -835,56 +945,15 @@ int lu_wave_error(m25_ctx* ctx, int n, int* flag) {
   return M25_OK;
 }
 
-template int lu_solve_wave<double, double>(m25_ctx*, const zd*, int64_t, int, const int32_t*, const zd*, int, zd*);
-template int lu_solve_wave<float, double>(m25_ctx*, const zf*, int64_t, int, const int32_t*, const zd*, int, zd*);
-template int lu_solve_wave<float, float>(m25_ctx*, const zf*, int64_t, int, const int32_t*, const zf*, int, zf*);
-
-// X = (LU)^-1 P B with factors of type TF and vectors / arithmetic in TV.
-template <class TF, class TV>
-int lu_solve_t(m25_ctx* ctx, const cx<TF>* A, int64_t lda, int n, const int32_t* ipiv, const cx<TV>* B, int nrhs,
-               cx<TV>* X) {
-  cudaStream_t st = ctx->stream;
-  if (nrhs > 8) {
-    set_error("dense solve: at most 8 right-hand sides per call");
-    return M25_ERR_VALUE;
-  }
-  if ((size_t)n * sizeof(int) > 200 * 1024) {
-    set_error("dense solve: n too large for the permutation in shared memory");
-    return M25_ERR_VALUE;
-  }
-  M25_CUDA(cudaFuncSetAttribute(permute_kernel<TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  StageTimer tm(ctx, ST_TRSV);
-  permute_kernel<TV><<<1, 1024, n * sizeof(int), st>>>(n, nrhs, ipiv, B, X);
-  const int bs = 64;
-  const size_t sm = sizeof(cx<TF>) * bs * (bs + 1);
-  M25_CUDA(cudaFuncSetAttribute(trsv_block_kernel<TF, TV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  for (int b0 = 0; b0 < n; b0 += bs) {
-    int w = std::min(bs, n - b0);
-    trsv_block_kernel<TF, TV><<<1, 256, sm, st>>>(A, lda, b0, w, nrhs, 0, X);
-    if (b0 + w < n) {
-      int rows = n - b0 - w;
-      trsv_update_kernel<TF, TV><<<(rows * 32 + 255) / 256, 256, 0, st>>>(A, lda, b0, w, nrhs, b0 + w, n, X);
-    }
-  }
-  for (int b0 = ((n - 1) / bs) * bs; b0 >= 0; b0 -= bs) {
-    int w = std::min(bs, n - b0);
-    trsv_block_kernel<TF, TV><<<1, 256, sm, st>>>(A, lda, b0, w, nrhs, 1, X);
-    if (b0 > 0) trsv_update_kernel<TF, TV><<<(b0 * 32 + 255) / 256, 256, 0, st>>>(A, lda, b0, w, nrhs, 0, b0, X);
-  }
-  M25_CHECK_LAUNCH();
-  return M25_OK;
-}
-
-template <class T>
-int lu_solve(m25_ctx* ctx, const cx<T>* A, int64_t lda, int n, const int32_t* ipiv, const cx<T>* B, int nrhs,
-             cx<T>* X) {
-  return lu_solve_t<T, T>(ctx, A, lda, n, ipiv, B, nrhs, X);
-}
+template int lu_solve_wave<double, double>(m25_ctx*, const zd*, int64_t, int, const int32_t*, const zd*, int, zd*,
+                                           const int32_t*);
+template int lu_solve_wave<float, double>(m25_ctx*, const zf*, int64_t, int, const int32_t*, const zd*, int, zd*,
+                                          const int32_t*);
+template int lu_solve_wave<float, float>(m25_ctx*, const zf*, int64_t, int, const int32_t*, const zf*, int, zf*,
+                                         const int32_t*);
 
 template int lu_factor<double>(m25_ctx*, zd*, int64_t, int, int32_t*, int, bool, int*);
 template int lu_factor<float>(m25_ctx*, zf*, int64_t, int, int32_t*, int, bool, int*);
-template int lu_solve<double>(m25_ctx*, const zd*, int64_t, int, const int32_t*, const zd*, int, zd*);
-template int lu_solve<float>(m25_ctx*, const zf*, int64_t, int, const int32_t*, const zf*, int, zf*);
 
 // ------------------------------------------------ GMRES iterative refinement
 // Right-hand sides are handled in lockstep (one column per rhs).
@@ -1063,7 +1132,7 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
   const int m = std::min(30, std::max(1, max_iter));
   const size_t np = (size_t)n * P;
   int rc = ctx->Rw.ensure(sizeof(zd) * np * (2 * m + 3) + sizeof(zf) * np * 2 + sizeof(double) * 64 +
-                          sizeof(zd) * (size_t)(m + 2) * P * 2);
+                          sizeof(zd) * (size_t)(m + 2) * P * 2 + sizeof(int32_t) * n);
   if (rc) return rc;
   zd* V = ctx->Rw.as<zd>();           // (m+1) Arnoldi vectors
   zd* Zp = V + np * (m + 1);          // (m) preconditioned directions
@@ -1074,6 +1143,7 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
   double* dsc = reinterpret_cast<double*>(d32 + np);  // scalars
   zd* hdev = reinterpret_cast<zd*>(dsc + 64);
   zd* ydev = hdev + (size_t)(m + 2) * P;
+  int32_t* perm = reinterpret_cast<int32_t*>(ydev + (size_t)(m + 2) * P);  // row permutation of the LU
   const unsigned g1 = (unsigned)((np + 255) / 256);
   const unsigned gw = (unsigned)(((size_t)n * 32 + 255) / 256);
   StageTimer tm(ctx, ST_REFINE);
@@ -1085,7 +1155,7 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
     M25_CUDA(cudaStreamSynchronize(st));
     if (!(s > 0)) s = 1;
     z64_to_z32_scaled<<<g1, 256, 0, st>>>((int64_t)np, in, 1.0 / s, r32);
-    int r = lu_solve_wave<float, float>(ctx, LU, n, n, ipiv, r32, P, d32);
+    int r = lu_solve_wave<float, float>(ctx, LU, n, n, ipiv, r32, P, d32, perm);
     if (r) return r;
     z32_to_z64_scaled<<<g1, 256, 0, st>>>((int64_t)np, d32, s, out);
     return M25_OK;
@@ -1102,6 +1172,7 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
     M25_CUDA(cudaMemcpyAsync(ydev, v.data(), sizeof(zd) * v.size(), cudaMemcpyHostToDevice, st));
     return M25_OK;
   };
+  if ((rc = lu_make_perm(ctx, n, ipiv, perm))) return rc;
   std::vector<double> bn, rn, xn;
   if ((rc = col_norms(B, bn))) return rc;
   double znorm = 0;
@@ -1243,13 +1314,15 @@ void cast_to_z32(m25_ctx* ctx, const zd* a, int64_t lda, zf* b, int64_t ldb, int
 // GPU loading this library holds until the process exits. Layout: [0, 64)
 // barrier words of the panel factorisation, then its candidate pivot rows for
 // up to kNoAllocGmax CTAs of 64 columns, then the ready flags of the
-// triangular solves.
+// triangular solves, then the row permutation of the factorisation.
 namespace {
 constexpr int kNoAllocGmax = 192;
 constexpr size_t kNoAllocPanelBytes = 64 + sizeof(m25::zd) * 2 * kNoAllocGmax * 64 + sizeof(double) * 2 * kNoAllocGmax +
                                       sizeof(int) * 2 * kNoAllocGmax + sizeof(m25::zd) * 2 * 64;
 constexpr size_t kNoAllocFlagsOffset = (kNoAllocPanelBytes + 255) / 256 * 256;
-static_assert(kNoAllocFlagsOffset + sizeof(int) * (16 + M25_NOALLOC_MAX_N / 64 + 1) <= M25_NOALLOC_SCRATCH_BYTES,
+constexpr size_t kNoAllocPermOffset =
+    (kNoAllocFlagsOffset + sizeof(int) * (16 + M25_NOALLOC_MAX_N / 64 + 1) + 255) / 256 * 256;
+static_assert(kNoAllocPermOffset + sizeof(int) * M25_NOALLOC_MAX_N <= M25_NOALLOC_SCRATCH_BYTES,
               "scratch too small for the declared maximum size");
 std::mutex g_noalloc_mu;
 constexpr int kMaxDevices = 64;
@@ -1318,8 +1391,10 @@ extern "C" int m25_dense_solve_noalloc(int32_t n, int32_t nrhs, void* Z, const v
     set_error("m25_dense_solve_noalloc: exactly singular matrix (zero pivot)");
     return M25_ERR_NUMERIC;
   }
+  int32_t* perm = reinterpret_cast<int32_t*>(base + kNoAllocPermOffset);
+  if ((rc = lu_make_perm(&c, n, ipiv, perm))) return rc;
   rc = lu_solve_wave<double, double>(&c, static_cast<const zd*>(Z), n, n, ipiv, static_cast<const zd*>(B), nrhs,
-                                     static_cast<zd*>(X));
+                                     static_cast<zd*>(X), perm);
   if (rc) return rc;
   int werr = 0;
   if ((rc = lu_wave_error(&c, n, &werr))) return rc;

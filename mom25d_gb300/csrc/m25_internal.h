@@ -60,6 +60,7 @@ struct m25_ctx {
   m25::DevBuf H, Zw, Zlu, Bw, Xw, Rw, Dw, ipiv, scratch, deemb, Zsweep, Xsweep, flags;
   bool flags_fresh = true;  // the ready flags of the triangular solves need zeroing
   int epoch = 0;            // value of a ready flag in the current sweep
+  size_t yt_off = 0;        // offset of the tagged vector copy in the flag buffer (0: not placed yet)
   // caller-provided scratch instead of the workspace buffers (LU panel
   // candidates + barrier words; triangular-solve flags, already zeroed)
   char* ext_scratch = nullptr;
