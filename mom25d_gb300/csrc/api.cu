@@ -50,6 +50,10 @@ int lu_solve_wave(m25_ctx*, const cx<TF>*, int64_t, int, const int32_t*, const c
                   const int32_t* perm = nullptr);
 int lu_wave_error(m25_ctx*, int, int*);
 
+// panel width of the complex64 LU: 64 columns keep the panel of up to ~7000
+// trailing rows in the shared memory of one 16-CTA cluster
+constexpr int kPanelZ64 = 64;
+
 }  // namespace m25
 
 using namespace m25;
@@ -196,7 +200,7 @@ extern "C" int m25_lu_factor(m25_ctx* ctx, int32_t n, int precision, void* A, in
   if (precision == M25_FP64)
     rc = lu_factor<double>(ctx, static_cast<zd*>(Ad), lda, n, pd, 64, false, &zinfo);
   else
-    rc = lu_factor<float>(ctx, static_cast<zf*>(Ad), lda, n, pd, 128,
+    rc = lu_factor<float>(ctx, static_cast<zf*>(Ad), lda, n, pd, kPanelZ64,
                           lu_tc_available() && !(flags & M25_LU_NO_TENSOR_CORES), &zinfo);
   if (rc) return rc;
   if (where == M25_ON_HOST) {
@@ -254,7 +258,8 @@ extern "C" int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precis
       M25_CUDA(cudaMemcpyAsync(LU, Zres, sizeof(zf) * nn, cudaMemcpyDeviceToDevice, st));
     else
       cast_to_z32(ctx, static_cast<const zd*>(Zres), n, LU, n, n, n);
-    if ((rc = lu_factor<float>(ctx, LU, n, n, ctx->ipiv.as<int32_t>(), 128, lu_tc_available(), &zinfo))) return rc;
+    if ((rc = lu_factor<float>(ctx, LU, n, n, ctx->ipiv.as<int32_t>(), kPanelZ64, lu_tc_available(), &zinfo)))
+      return rc;
     if (zinfo) {
       if (info) { info[0] = 0; info[1] = zinfo; }
       set_error("m25_dense_solve: zero pivot in the complex64 LU");

@@ -240,6 +240,237 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> a) {
   }
 }
 
+// ------------------------------------------------ panel on one CTA cluster
+// For trailing sizes whose panel fits in the shared memory of one cluster of
+// kPanelCluster CTAs (16, the largest cluster size; about 6500 rows of
+// 64 complex64 columns), the panel is factored without global barriers. CTA q
+// of the cluster keeps rows k0 + q R .. + R - 1 in shared memory. Per column
+// j, every CTA pushes its pivot candidate (value, row index and the whole
+// row) into the shared memory of all 16 CTAs, and the owner of row j pushes
+// row j as well; one hardware cluster barrier later every CTA holds all it
+// needs locally: it picks the pivot (max |re| + |im|, first index on ties,
+// as panel_kernel), the two owners swap rows p and j in place, and every CTA
+// scales and updates its own rows, finding the next column's candidate while
+// it updates. The pushed data is double-buffered by column parity: a CTA can
+// only write column j + 2's buffers after every CTA has passed column j + 1's
+// barrier, that is, after all reads of column j's buffers.
+constexpr int kPanelCluster = 16;
+constexpr int kPanelLd = 65;  // padded row of the panel in shared memory
+
+template <class T>
+struct ClusterPanelArgs {
+  cx<T>* A;
+  int64_t lda;
+  int n, k0, nb, rows_per_cta;
+  int32_t* ipiv;
+  int* info;
+};
+
+template <class T>
+struct alignas(16) PivCand {
+  T val;
+  int idx;
+};
+
+template <class T>
+constexpr size_t cluster_panel_smem(int R) {
+  // rows + candidate rows (2 x 16 x 64) + row j (2 x 64)
+  return sizeof(cx<T>) * ((size_t)R * kPanelLd + 2 * kPanelCluster * 64 + 2 * 64);
+}
+
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+  return r;
+}
+// the address of a shared variable of this CTA in the shared memory of cluster CTA rank
+__device__ __forceinline__ uint32_t dsmem(const void* p, uint32_t rank) {
+  uint32_t a = (uint32_t)__cvta_generic_to_shared(p), r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_dsmem(uint32_t a, cx<float> v) {
+  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};\n" ::"r"(a), "f"(v.re), "f"(v.im) : "memory");
+}
+__device__ __forceinline__ void st_dsmem(uint32_t a, cx<double> v) {
+  asm volatile("st.shared::cluster.v2.f64 [%0], {%1, %2};\n" ::"r"(a), "d"(v.re), "d"(v.im) : "memory");
+}
+__device__ __forceinline__ void st_dsmem(uint32_t a, PivCand<float> v) {
+  asm volatile("st.shared::cluster.v2.b32 [%0], {%1, %2};\n" ::"r"(a), "r"(__float_as_uint(v.val)), "r"(v.idx)
+               : "memory");
+}
+__device__ __forceinline__ void st_dsmem(uint32_t a, PivCand<double> v) {
+  asm volatile("st.shared::cluster.f64 [%0], %1;\n\tst.shared::cluster.s32 [%0+8], %2;\n" ::"r"(a), "d"(v.val),
+               "r"(v.idx)
+               : "memory");
+}
+
+// better candidate: larger value, first index on ties
+template <class T>
+__device__ __forceinline__ bool piv_better(T ov, int oi, T v, int i) {
+  return oi >= 0 && (ov > v || (ov == v && (i < 0 || oi < i)));
+}
+
+constexpr int kPanelThreads = 512;
+constexpr int kPanelGroups = kPanelThreads / 64;  // row groups of the update's 2-D map
+
+template <class T>
+__global__ void __launch_bounds__(kPanelThreads, 1) panel_cluster_kernel(ClusterPanelArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int q = (int)cluster_rank(), nb = a.nb, R = a.rows_per_cta, tid = threadIdx.x;
+  const int r0 = a.k0 + q * R;
+  const int r1 = min(a.n, r0 + R);
+  const int Rq = max(0, r1 - r0);
+  cx<T>* P = reinterpret_cast<cx<T>*>(smem_raw);          // (R, kPanelLd) this CTA's rows
+  cx<T>* crow = P + (size_t)R * kPanelLd;                   // (2, 16, 64) pushed candidate rows
+  cx<T>* jrow = crow + 2 * kPanelCluster * 64;              // (2, 64) pushed row k0 + j
+  __shared__ PivCand<T> cand[2][kPanelCluster];             // pushed candidates
+  __shared__ T gmax_v[kPanelGroups];
+  __shared__ int gmax_i[kPanelGroups];
+  for (int e = tid; e < Rq * 64; e += blockDim.x) {
+    const int r = e >> 6, c = e & 63;
+    if (c < nb) P[r * kPanelLd + c] = a.A[(int64_t)(r0 + r) * a.lda + a.k0 + c];
+  }
+  // 2-D map of the update: column uc, rows ug, ug + kPanelGroups, ...
+  const int uc = tid & 63, ug = tid >> 6;
+  __syncthreads();
+  // candidate of column 0 (afterwards found during each update)
+  if (uc == 0) {
+    T bv = T(-1);
+    int bi = -1;
+    for (int r = ug; r < Rq; r += kPanelGroups) {
+      const T v = cabs1(P[r * kPanelLd]);
+      if (v > bv) {
+        bv = v;
+        bi = r0 + r;
+      }
+    }
+    gmax_v[ug] = bv;
+    gmax_i[ug] = bi;
+  }
+  __syncthreads();
+  cluster_sync_all();  // every CTA of the cluster runs before the first remote store
+  for (int j = 0; j < nb; ++j) {
+    const int row_j = a.k0 + j, par = j & 1;
+    const int qj = j / R;
+    // this CTA's candidate for column j (rows >= row_j)
+    T bv = T(-1);
+    int bi = -1;
+#pragma unroll
+    for (int g = 0; g < kPanelGroups; ++g)
+      if (piv_better(gmax_v[g], gmax_i[g], bv, bi)) {
+        bv = gmax_v[g];
+        bi = gmax_i[g];
+      }
+    // push: candidate, candidate row, and row j from its owner, to all 16 CTAs
+    if (tid < kPanelCluster) st_dsmem(dsmem(&cand[par][q], tid), PivCand<T>{bv, bi});
+    if (bi >= 0)
+      for (int e = tid; e < kPanelCluster * 64; e += blockDim.x) {
+        const int dst = e >> 6, c = e & 63;
+        if (c < nb) st_dsmem(dsmem(&crow[(par * kPanelCluster + q) * 64 + c], dst), P[(bi - r0) * kPanelLd + c]);
+      }
+    if (q == qj)
+      for (int e = tid; e < kPanelCluster * 64; e += blockDim.x) {
+        const int dst = e >> 6, c = e & 63;
+        if (c < nb) st_dsmem(dsmem(&jrow[par * 64 + c], dst), P[(row_j - r0) * kPanelLd + c]);
+      }
+    cluster_sync_all();  // all pushes of column j visible
+    // every thread picks the pivot from the 16 local candidates
+    T v = T(-1);
+    int p = -1, src = -1;
+#pragma unroll
+    for (int k = 0; k < kPanelCluster; ++k) {
+      const PivCand<T> c = cand[par][k];
+      if (piv_better(c.val, c.idx, v, p)) {
+        v = c.val;
+        p = c.idx;
+        src = k;
+      }
+    }
+    if (p < 0 || v == T(0)) {  // zero column: no interchange, no scaling
+      if (tid == 0 && q == 0 && *a.info == 0) *a.info = row_j + 1;
+      p = row_j;
+      src = -1;
+    }
+    if (tid == 0 && q == 0) a.ipiv[row_j] = p;
+    const cx<T>* urow = src >= 0 ? crow + (par * kPanelCluster + src) * 64 : jrow + par * 64;
+    if (p != row_j) {
+      if (p >= r0 && p < r1)
+        for (int c = tid; c < nb; c += blockDim.x) P[(p - r0) * kPanelLd + c] = jrow[par * 64 + c];
+      if (q == qj)
+        for (int c = tid; c < nb; c += blockDim.x) P[(row_j - r0) * kPanelLd + c] = urow[c];
+    }
+    __syncthreads();
+    // multipliers (rows below row j), by the reciprocal pivot
+    if (src >= 0) {
+      const cx<T> pv = urow[j];
+      const T m2 = pv.re * pv.re + pv.im * pv.im;
+      const cx<T> rp(pv.re / m2, -pv.im / m2);
+      for (int r = tid; r < Rq; r += blockDim.x)
+        if (r0 + r > row_j) P[r * kPanelLd + j] = P[r * kPanelLd + j] * rp;
+    }
+    __syncthreads();
+    // rank-1 update of the columns right of j, four rows at a time (loads
+    // first); the threads of column j + 1 track the next candidate
+    {
+      T gv = T(-1);
+      int gi = -1;
+      if (uc > j && uc < nb) {
+        const cx<T> u = urow[uc];
+        // first row below row j in this group
+        int r = ug;
+        const int rlo = row_j + 1 - r0;
+        if (r < rlo) r += (rlo - r + kPanelGroups - 1) / kPanelGroups * kPanelGroups;
+        for (; r + 3 * kPanelGroups < Rq; r += 4 * kPanelGroups) {
+          cx<T> x[4], m[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            x[i] = P[(r + i * kPanelGroups) * kPanelLd + uc];
+            m[i] = P[(r + i * kPanelGroups) * kPanelLd + j];
+          }
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            x[i] -= m[i] * u;
+            P[(r + i * kPanelGroups) * kPanelLd + uc] = x[i];
+          }
+          if (uc == j + 1)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              const T cv = cabs1(x[i]);
+              if (cv > gv) {
+                gv = cv;
+                gi = r0 + r + i * kPanelGroups;
+              }
+            }
+        }
+        for (; r < Rq; r += kPanelGroups) {
+          const cx<T> x = P[r * kPanelLd + uc] - P[r * kPanelLd + j] * u;
+          P[r * kPanelLd + uc] = x;
+          if (uc == j + 1) {
+            const T cv = cabs1(x);
+            if (cv > gv) {
+              gv = cv;
+              gi = r0 + r;
+            }
+          }
+        }
+      }
+      if (uc == j + 1) {
+        gmax_v[ug] = gv;
+        gmax_i[ug] = gi;
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < Rq * 64; e += blockDim.x) {
+    const int r = e >> 6, c = e & 63;
+    if (c < nb) a.A[(int64_t)(r0 + r) * a.lda + a.k0 + c] = P[r * kPanelLd + c];
+  }
+}
+
 // Row interchanges of rows k0..k0+nb-1 applied to the columns outside the panel.
 template <class T>
 __global__ void laswp_kernel(cx<T>* A, int64_t lda, int n, int k0, int nb, const int32_t* __restrict__ ipiv) {
@@ -417,9 +648,63 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
     int rc = lu_tc_prepare(ctx, n, nb);
     if (rc) return rc;
   }
+  // the cluster panel: largest trailing size whose rows fit in 16 CTAs
+  int cluster_rows = 0;
+  {
+    static int ok = -1;
+    int optin = 0;
+    M25_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    const size_t avail = (size_t)optin - 1024;  // static shared variables
+    const int R = nb > 64 ? 0
+                          : (int)((avail - cluster_panel_smem<T>(0)) / ((size_t)kPanelLd * sizeof(cx<T>)));
+    if (ok < 0) {
+      ok = 0;
+      const char* off = getenv("M25_NO_CLUSTER_PANEL");
+      if (!(off && *off == '1') &&
+          cudaFuncSetAttribute(panel_cluster_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+              cudaSuccess &&
+          cudaFuncSetAttribute(panel_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)avail) ==
+              cudaSuccess) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = kPanelCluster;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(kPanelCluster);
+        cfg.blockDim = dim3(kPanelThreads);
+        cfg.dynamicSmemBytes = avail;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, panel_cluster_kernel<T>, &cfg) == cudaSuccess && nclusters > 0)
+          ok = 1;
+      }
+      cudaGetLastError();  // a refused attribute only means: no cluster panel
+    }
+    if (ok == 1 && R > 0) cluster_rows = kPanelCluster * R;
+  }
   for (int k0 = 0; k0 < n; k0 += nb) {
     const int w = std::min(nb, n - k0);
     const int m = n - k0;
+    if (m <= cluster_rows) {
+      ClusterPanelArgs<T> ca{A, lda, n, k0, w, (m + kPanelCluster - 1) / kPanelCluster, ipiv, info};
+      const size_t smem = cluster_panel_smem<T>(ca.rows_per_cta);
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = kPanelCluster;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3(kPanelCluster);
+      cfg.blockDim = dim3(kPanelThreads);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = st;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      StageTimer tm(ctx, ST_PANEL);
+      M25_CUDA(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T>, ca));
+    } else {
     // grid size: as many CTAs as can be co-resident, each with >= 1 row
     int occ = 0;
     G = std::min(std::min(m, ctx->num_sms), Gmax);
@@ -468,6 +753,7 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
     {
       StageTimer tm(ctx, ST_PANEL);
       M25_CUDA(cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(G), dim3(256), args, panel_smem, st));
+    }
     }
     if (n > w) {
       StageTimer tm(ctx, ST_LASWP);
