@@ -58,12 +58,36 @@ __device__ __forceinline__ int find_interval(const T* __restrict__ x, int n, T r
   return lo;
 }
 
+// The same interval with the search in fp32 on a rounded copy xf of the
+// radii (the fp64 pipe of this GPU is the fill's bottleneck): rounding is
+// monotone and the radii are far apart against fp32 resolution, so the fp32
+// index is the fp64 one or one above it; one fp64 comparison settles it.
+template <class T>
+__device__ __forceinline__ int find_interval_f(const T* __restrict__ x, const float* __restrict__ xf, int n, T r) {
+  const float rf = (float)r;
+  int lo;
+  if (rf < xf[1]) {
+    lo = 0;
+  } else if (rf >= xf[n - 2]) {
+    lo = n - 2;
+  } else {
+    lo = 1;
+    int hi = n - 2;
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (rf < xf[mid]) hi = mid; else lo = mid;
+    }
+  }
+  if (lo > 0 && r < x[lo]) --lo;
+  return lo;
+}
+
 // Smooth parts S_A, S_V at radius r from the shared-memory table of one pair:
 // sum_p c[3-p] (r - x_i)^p, the order PPoly evaluates.
 template <class T>
-__device__ __forceinline__ void spline_av(const T* __restrict__ xs, const T* __restrict__ tab, int n, T r,
-                                          cx<T>& sa, cx<T>& sv) {
-  int i = find_interval(xs, n, r);
+__device__ __forceinline__ void spline_av(const T* __restrict__ xs, const float* __restrict__ xf,
+                                          const T* __restrict__ tab, int n, T r, cx<T>& sa, cx<T>& sv) {
+  int i = find_interval_f(xs, xf, n, r);
   T dx = r - xs[i];
   const T* c = tab + (size_t)i * 16;  // [power 0..3][A re, A im, V re, V im], highest power first
   T z = dx, z2 = dx * dx, z3 = z2 * dx;
@@ -75,7 +99,8 @@ __device__ __forceinline__ void spline_av(const T* __restrict__ xs, const T* __r
 
 template <class T, int NQ, bool NEAR>
 __device__ __forceinline__ void source_pass(const FillArgs<T>& a, const TriData<T>& S, T dcx, T dcy,
-                                            const T (&tq)[7][2], const T (&tw)[7], const T* xs, const T* tab,
+                                            const T (&tq)[7][2], const T (&tw)[7], const T* xs, const float* xf,
+                                            const T* tab,
                                             cx<T> cA, cx<T> cV, T dz, const T* st, int lane, cx<T> (&Q)[3],
                                             cx<T> (&Px)[3], cx<T> (&Py)[3], cx<T>& IV, const T (&tv)[3][2]) {
   const T inv4pi = T(1.0 / (4.0 * kPi));
@@ -111,18 +136,28 @@ __device__ __forceinline__ void source_pass(const FillArgs<T>& a, const TriData<
 #pragma unroll
     for (int l = 0; l < NQ; ++l) {
       T ddx = rx - sq[l][0], ddy = ry - sq[l][1];
-      T R = sqrt(ddx * ddx + ddy * ddy);
+      const T R2 = ddx * ddx + ddy * ddy;
+      T R, inv = T(0);
+      if (NEAR) {
+        R = sqrt(R2);  // may be 0 (coincident points of a self pair)
+      } else {
+        // distinct triangles: one reciprocal square root gives R and 1/R
+        const T ri = rsqrt(R2);
+        R = R2 * ri;
+        inv = inv4pi * (dz == T(0) ? ri : rsqrt(R2 + dz * dz));
+      }
       cx<T> sa, sv;
-      spline_av(xs, tab, a.nrho, R, sa, sv);
+      spline_av(xs, xf, tab, a.nrho, R, sa, sv);
       if (!NEAR) {
-        T inv = inv4pi / (dz == T(0) ? R : sqrt(R * R + dz * dz));
         sa += cA * inv;
         sv += cV * inv;
       }
       cx<T> saw = sa * sw[l];
       K0A += saw;
-      K1x += saw * sq[l][0];
-      K1y += saw * sq[l][1];
+      if (NQ > 1) {  // the one-point rule sits on the centroid: no first moments
+        K1x += saw * sq[l][0];
+        K1y += saw * sq[l][1];
+      }
       K0V += sv * sw[l];
     }
     const T wk = tw[k];
@@ -147,7 +182,11 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
   // tables of the pairs (lt, ls): radii, then per source level (n-1) x 16 values [A, V]
   T* xs = reinterpret_cast<T*>(smem_raw);
   T* tabs = xs + ((n + 3) & ~3);
-  for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i] = a.rho[i];
+  float* xf = reinterpret_cast<float*>(tabs + (size_t)L * (n - 1) * 16);  // radii rounded to fp32
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    xs[i] = a.rho[i];
+    xf[i] = (float)a.rho[i];
+  }
   int loaded = -1;
   // persistent grid: work items (test block, source chunk) taken round-robin
   const int nitems = a.nblocks * a.n_chunks;
@@ -206,14 +245,16 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
     const T dz = a.dz[lt * L + ls];
     cx<T> Q[3], Px[3], Py[3], IV;
     if (code >= 0) {
-      source_pass<T, 7, true>(a, S, dcx, dcy, tq, tw, xs, tab, cA, cV, dz, a.stat + (int64_t)code * 672, lane, Q, Px,
-                              Py, IV, tv);
+      source_pass<T, 7, true>(a, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, a.stat + (int64_t)code * 672, lane, Q,
+                              Px, Py, IV, tv);
     } else if (code == -1) {
-      source_pass<T, 3, false>(a, S, dcx, dcy, tq, tw, xs, tab, cA, cV, dz, nullptr, lane, Q, Px, Py, IV, tv);
+      source_pass<T, 3, false>(a, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, nullptr, lane, Q, Px, Py, IV, tv);
     } else {
-      source_pass<T, 1, false>(a, S, dcx, dcy, tq, tw, xs, tab, cA, cV, dz, nullptr, lane, Q, Px, Py, IV, tv);
+      source_pass<T, 1, false>(a, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, nullptr, lane, Q, Px, Py, IV, tv);
     }
-    // IA[i][j] = Q_i - (b_j - c_s) . P_i ; vals = jw mu cA cA IA + inv_jwe cV cV IV
+    // IA[i][j] = Q_i - (b_j - c_s) . P_i ; vals = jw mu cA cA IA + inv_jwe cV cV IV,
+    // with the test triangle's factors jw mu cA_i, inv_jwe cV_i applied to
+    // Q, P and IV once per i instead of once per (i, j)
     cx<T> out[3][3];
     T scA[3], scV[3], bx[3], by[3];
 #pragma unroll
@@ -223,14 +264,13 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
       bx[j] = S.v[j][0];
       by[j] = S.v[j][1];
     }
-    const cx<T> ivt = a.inv_jwe * IV;
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i) {
+      const cx<T> ja = a.jwmu * tcA[i], jv = a.inv_jwe * tcV[i];
+      const cx<T> JQ = ja * Q[i], JPx = ja * Px[i], JPy = ja * Py[i], JV = jv * IV;
 #pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        cx<T> IA = Q[i] - (Px[i] * bx[j] + Py[i] * by[j]);
-        out[i][j] = a.jwmu * IA * (tcA[i] * scA[j]) + ivt * (tcV[i] * scV[j]);
-      }
+      for (int j = 0; j < 3; ++j) out[i][j] = (JQ - (JPx * bx[j] + JPy * by[j])) * scA[j] + JV * scV[j];
+    }
     if (active && s == t && (a.zs.re != T(0) || a.zs.im != T(0))) {
       // conductor loss: Zs Int_T (r - a_i).(r - a_j) dS cA_i cA_j
 #pragma unroll
@@ -450,7 +490,7 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   a.H = H;
   a.ldh = ldh;
   a.IVpad = IVpad;
-  size_t smem = sizeof(T) * (((nrho + 3) & ~3) + (size_t)L * (nrho - 1) * 16);
+  size_t smem = sizeof(T) * (((nrho + 3) & ~3) + (size_t)L * (nrho - 1) * 16) + sizeof(float) * nrho;
   if (smem > 220 * 1024) {
     set_error("m25_assemble: Green's tables too large for shared memory (reduce rho_max or levels)");
     return M25_ERR_VALUE;

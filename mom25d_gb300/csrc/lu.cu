@@ -264,6 +264,7 @@ struct ClusterPanelArgs {
   int n, k0, nb, rows_per_cta;
   int32_t* ipiv;
   int* info;
+  int* err;  // a wait for pushed data ran out
 };
 
 template <class T>
@@ -292,20 +293,61 @@ __device__ __forceinline__ uint32_t dsmem(const void* p, uint32_t rank) {
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(a), "r"(rank));
   return r;
 }
-__device__ __forceinline__ void st_dsmem(uint32_t a, cx<float> v) {
-  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};\n" ::"r"(a), "f"(v.re), "f"(v.im) : "memory");
-}
-__device__ __forceinline__ void st_dsmem(uint32_t a, cx<double> v) {
-  asm volatile("st.shared::cluster.v2.f64 [%0], {%1, %2};\n" ::"r"(a), "d"(v.re), "d"(v.im) : "memory");
-}
-__device__ __forceinline__ void st_dsmem(uint32_t a, PivCand<float> v) {
-  asm volatile("st.shared::cluster.v2.b32 [%0], {%1, %2};\n" ::"r"(a), "r"(__float_as_uint(v.val)), "r"(v.idx)
+// remote store that completes its bytes on the destination CTA's mbarrier
+__device__ __forceinline__ void st_async(uint32_t a, cx<float> v, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];\n" ::"r"(a),
+               "f"(v.re), "f"(v.im), "r"(bar)
                : "memory");
 }
-__device__ __forceinline__ void st_dsmem(uint32_t a, PivCand<double> v) {
-  asm volatile("st.shared::cluster.f64 [%0], %1;\n\tst.shared::cluster.s32 [%0+8], %2;\n" ::"r"(a), "d"(v.val),
-               "r"(v.idx)
+__device__ __forceinline__ void st_async(uint32_t a, cx<double> v, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f64 [%0], {%1, %2}, [%3];\n" ::"r"(a),
+               "d"(v.re), "d"(v.im), "r"(bar)
                : "memory");
+}
+__device__ __forceinline__ void st_async(uint32_t a, PivCand<float> v, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.b32 [%0], {%1, %2}, [%3];\n" ::"r"(a),
+               "r"(__float_as_uint(v.val)), "r"(v.idx), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void st_async(uint32_t a, PivCand<double> v, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.b64 [%0], {%1, %2}, [%3];\n" ::"r"(a),
+               "l"(__double_as_longlong(v.val)), "l"((long long)v.idx), "r"(bar)
+               : "memory");
+}
+// bytes of one pushed candidate record
+template <class T>
+constexpr int cand_push_bytes() {
+  return sizeof(T) == 4 ? 8 : 16;
+}
+__device__ __forceinline__ void cl_mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"((uint32_t)__cvta_generic_to_shared(bar)), "r"(count));
+}
+__device__ __forceinline__ void cl_mbar_expect(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(
+                   (uint32_t)__cvta_generic_to_shared(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// bounded wait (iterations and wall clock) for the phase of the given parity
+// of a barrier completed by remote transactions; false on a timeout
+__device__ __forceinline__ bool cl_mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t addr = (uint32_t)__cvta_generic_to_shared(bar);
+  unsigned long long t0;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t0));
+  for (long long it = 0; it < kBarrierSpinLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    if (t - t0 > 500ull * 1000 * 1000) return false;
+  }
+  return false;
 }
 
 // better candidate: larger value, first index on ties
@@ -330,6 +372,12 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_cluster_kernel(Cluster
   __shared__ PivCand<T> cand[2][kPanelCluster];             // pushed candidates
   __shared__ T gmax_v[kPanelGroups];
   __shared__ int gmax_i[kPanelGroups];
+  __shared__ __align__(8) uint64_t colbar[2];  // per column parity: completed by the 16 CTAs' pushes
+  if (tid == 0) {
+    cl_mbar_init(&colbar[0], 1);
+    cl_mbar_init(&colbar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
   for (int e = tid; e < Rq * 64; e += blockDim.x) {
     const int r = e >> 6, c = e & 63;
     if (c < nb) P[r * kPanelLd + c] = a.A[(int64_t)(r0 + r) * a.lda + a.k0 + c];
@@ -352,7 +400,9 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_cluster_kernel(Cluster
     gmax_i[ug] = bi;
   }
   __syncthreads();
-  cluster_sync_all();  // every CTA of the cluster runs before the first remote store
+  cluster_sync_all();  // every CTA runs, with its barriers set up, before the first push
+  // bytes pushed into each CTA per column: 16 candidates, 16 rows, row j
+  const uint32_t expect = kPanelCluster * (cand_push_bytes<T>() + nb * (int)sizeof(cx<T>)) + nb * sizeof(cx<T>);
   for (int j = 0; j < nb; ++j) {
     const int row_j = a.k0 + j, par = j & 1;
     const int qj = j / R;
@@ -365,19 +415,29 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_cluster_kernel(Cluster
         bv = gmax_v[g];
         bi = gmax_i[g];
       }
-    // push: candidate, candidate row, and row j from its owner, to all 16 CTAs
-    if (tid < kPanelCluster) st_dsmem(dsmem(&cand[par][q], tid), PivCand<T>{bv, bi});
-    if (bi >= 0)
-      for (int e = tid; e < kPanelCluster * 64; e += blockDim.x) {
-        const int dst = e >> 6, c = e & 63;
-        if (c < nb) st_dsmem(dsmem(&crow[(par * kPanelCluster + q) * 64 + c], dst), P[(bi - r0) * kPanelLd + c]);
-      }
+    // push: candidate, candidate row (zeros without a candidate), and row j
+    // from its owner, into all 16 CTAs; each store completes its bytes on
+    // the destination's barrier of this column's parity
+    if (tid == 0) cl_mbar_expect(&colbar[par], expect);
+    if (tid < kPanelCluster) st_async(dsmem(&cand[par][q], tid), PivCand<T>{bv, bi}, dsmem(&colbar[par], tid));
+    for (int e = tid; e < kPanelCluster * 64; e += blockDim.x) {
+      const int dst = e >> 6, c = e & 63;
+      if (c < nb)
+        st_async(dsmem(&crow[(par * kPanelCluster + q) * 64 + c], dst),
+                 bi >= 0 ? P[(bi - r0) * kPanelLd + c] : cx<T>(), dsmem(&colbar[par], dst));
+    }
     if (q == qj)
       for (int e = tid; e < kPanelCluster * 64; e += blockDim.x) {
         const int dst = e >> 6, c = e & 63;
-        if (c < nb) st_dsmem(dsmem(&jrow[par * 64 + c], dst), P[(row_j - r0) * kPanelLd + c]);
+        if (c < nb)
+          st_async(dsmem(&jrow[par * 64 + c], dst), P[(row_j - r0) * kPanelLd + c], dsmem(&colbar[par], dst));
       }
-    cluster_sync_all();  // all pushes of column j visible
+    // wait until all of column j's pushes have landed here
+    const bool got = cl_mbar_wait(&colbar[par], (j >> 1) & 1);
+    if (__syncthreads_or(!got)) {
+      if (tid == 0) atomicExch(a.err, 1);
+      break;
+    }
     // every thread picks the pivot from the 16 local candidates
     T v = T(-1);
     int p = -1, src = -1;
@@ -469,6 +529,8 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_cluster_kernel(Cluster
     const int r = e >> 6, c = e & 63;
     if (c < nb) a.A[(int64_t)(r0 + r) * a.lda + a.k0 + c] = P[r * kPanelLd + c];
   }
+  // no CTA leaves while a peer may still store into its shared memory
+  cluster_sync_all();
 }
 
 // Row interchanges of rows k0..k0+nb-1 applied to the columns outside the panel.
@@ -688,7 +750,7 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
     const int w = std::min(nb, n - k0);
     const int m = n - k0;
     if (m <= cluster_rows) {
-      ClusterPanelArgs<T> ca{A, lda, n, k0, w, (m + kPanelCluster - 1) / kPanelCluster, ipiv, info};
+      ClusterPanelArgs<T> ca{A, lda, n, k0, w, (m + kPanelCluster - 1) / kPanelCluster, ipiv, info, err};
       const size_t smem = cluster_panel_smem<T>(ca.rows_per_cta);
       cudaLaunchConfig_t cfg = {};
       cudaLaunchAttribute at[1];
@@ -781,7 +843,7 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
   M25_CUDA(cudaMemcpyAsync(hflags, base + 8, 8, cudaMemcpyDeviceToHost, st));
   M25_CUDA(cudaStreamSynchronize(st));
   if (hflags[0]) {
-    set_error("dense LU: grid barrier timed out");
+    set_error("dense LU: a wait of the panel factorisation ran out");
     return M25_ERR_CUDA;
   }
   if (use_tc) {
