@@ -188,8 +188,10 @@ __device__ double wave_objective(const FitArgs& a, int grp, zd g, double Inrm, d
       if (i < ns) {
         double sv = a.s[off + i];
         ep[u] = cexp(g * sv);
-        em[u] = cexp(-g * sv);
-        n11 += norm2(ep[u]);
+        // e^{-g s} = 1 / e^{g s}: one reciprocal instead of a second exp and sincos
+        const double m2 = norm2(ep[u]);
+        em[u] = zd(ep[u].re / m2, -ep[u].im / m2);
+        n11 += m2;
       } else {
         ep[u] = em[u] = zd(0.0);
       }
@@ -275,82 +277,119 @@ __device__ double wave_objective(const FitArgs& a, int grp, zd g, double Inrm, d
   return res;
 }
 
-// One warp per port group: Nelder-Mead with scipy's coefficients (reflection
-// 1, expansion 2, contraction 0.5, shrink 0.5), initial simplex 5 % steps,
-// stopping when the simplex spans <= xatol and its values <= fatol.
-__global__ void fit_kernel(FitArgs a) {
-  const int grp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (grp < a.ngroup) {
-    const double scale = fabs(a.beta0[grp]);
-    double Inrm = 0, Vnrm = 0;
-    for (int p = 0; p < a.P; ++p) {
-      if (a.group_of[p] != grp) continue;
-      for (int i = lane; i < a.ns[p]; i += 32)
-        for (int e = 0; e < a.P; ++e) {
-          Inrm += norm2(a.I[(int64_t)(a.s_off[p] + i) * a.P + e]);
-          Vnrm += norm2(a.V[(int64_t)(a.s_off[p] + i) * a.P + e]);
-        }
-    }
-    Inrm = warp_sum(Inrm);
-    Vnrm = warp_sum(Vnrm);
-    auto f = [&](double x0, double x1) { return wave_objective(a, grp, zd(scale * x0, scale * x1), Inrm, Vnrm, false); };
-    const double xatol = 1e-10, fatol = 1e-16;
-    double sim[3][2], fs[3];
-    // gamma0 = 1e-3 b0 + j b0, scaled by |b0|
-    double x0 = 1e-3 * a.beta0[grp] / scale, x1 = a.beta0[grp] / scale;
-    sim[0][0] = x0; sim[0][1] = x1;
-    sim[1][0] = x0 != 0 ? 1.05 * x0 : 0.00025; sim[1][1] = x1;
-    sim[2][0] = x0; sim[2][1] = x1 != 0 ? 1.05 * x1 : 0.00025;
-    for (int k = 0; k < 3; ++k) fs[k] = f(sim[k][0], sim[k][1]);
-    auto sort3 = [&]() {  // stable insertion sort by value
-      for (int i = 1; i < 3; ++i)
-        for (int j = i; j > 0 && fs[j] < fs[j - 1]; --j) {
-          double t = fs[j]; fs[j] = fs[j - 1]; fs[j - 1] = t;
-          for (int d = 0; d < 2; ++d) { double u = sim[j][d]; sim[j][d] = sim[j - 1][d]; sim[j - 1][d] = u; }
-        }
-    };
-    sort3();
-    int it = 1;
-    while (it < 4000) {
-      double dx = 0, df = 0;
-      for (int k = 1; k < 3; ++k) {
-        dx = fmax(dx, fmax(fabs(sim[k][0] - sim[0][0]), fabs(sim[k][1] - sim[0][1])));
-        df = fmax(df, fabs(fs[0] - fs[k]));
+// One CTA of four warps per port group: Nelder-Mead with scipy's
+// coefficients (reflection 1, expansion 2, contraction 0.5, shrink 0.5),
+// initial simplex 5 % steps, stopping when the simplex spans <= xatol and its
+// values <= fatol. Each iteration evaluates its four possible trial points
+// (reflection, expansion, outside and inside contraction) at once, one warp
+// each (one SM sub-partition and its fp64 unit each), and then takes scipy's
+// decisions on those values: the objective is a pure function, so the
+// simplex follows the sequential method's path exactly, in about half the
+// sequential rounds of objective evaluations.
+constexpr int kFitWarps = 4;
+
+__global__ void __launch_bounds__(32 * kFitWarps) fit_kernel(FitArgs a) {
+  const int grp = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ double pts[kFitWarps][2];
+  __shared__ double vals[kFitWarps];
+  if (grp >= a.ngroup) return;
+  const double scale = fabs(a.beta0[grp]);
+  double Inrm = 0, Vnrm = 0;
+  for (int p = 0; p < a.P; ++p) {
+    if (a.group_of[p] != grp) continue;
+    for (int i = lane; i < a.ns[p]; i += 32)
+      for (int e = 0; e < a.P; ++e) {
+        Inrm += norm2(a.I[(int64_t)(a.s_off[p] + i) * a.P + e]);
+        Vnrm += norm2(a.V[(int64_t)(a.s_off[p] + i) * a.P + e]);
       }
-      if (dx <= xatol && df <= fatol) break;
-      double xb[2], xr[2];
+  }
+  Inrm = warp_sum(Inrm);
+  Vnrm = warp_sum(Vnrm);
+  // objective values of the first n points of pts, one warp per point
+  auto round = [&](int n) {
+    __syncthreads();
+    if (warp < n) {
+      const double v = wave_objective(a, grp, zd(scale * pts[warp][0], scale * pts[warp][1]), Inrm, Vnrm, false);
+      if (lane == 0) vals[warp] = v;
+    }
+    __syncthreads();
+  };
+  const double xatol = 1e-10, fatol = 1e-16;
+  double sim[3][2], fs[3];
+  // gamma0 = 1e-3 b0 + j b0, scaled by |b0|
+  const double x0 = 1e-3 * a.beta0[grp] / scale, x1 = a.beta0[grp] / scale;
+  sim[0][0] = x0; sim[0][1] = x1;
+  sim[1][0] = x0 != 0 ? 1.05 * x0 : 0.00025; sim[1][1] = x1;
+  sim[2][0] = x0; sim[2][1] = x1 != 0 ? 1.05 * x1 : 0.00025;
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 3; ++k) {
+      pts[k][0] = sim[k][0];
+      pts[k][1] = sim[k][1];
+    }
+  round(3);
+  for (int k = 0; k < 3; ++k) fs[k] = vals[k];
+  auto sort3 = [&]() {  // stable insertion sort by value
+    for (int i = 1; i < 3; ++i)
+      for (int j = i; j > 0 && fs[j] < fs[j - 1]; --j) {
+        double t = fs[j]; fs[j] = fs[j - 1]; fs[j - 1] = t;
+        for (int d = 0; d < 2; ++d) { double u = sim[j][d]; sim[j][d] = sim[j - 1][d]; sim[j - 1][d] = u; }
+      }
+  };
+  sort3();
+  int it = 1;
+  while (it < 4000) {
+    double dx = 0, df = 0;
+    for (int k = 1; k < 3; ++k) {
+      dx = fmax(dx, fmax(fabs(sim[k][0] - sim[0][0]), fabs(sim[k][1] - sim[0][1])));
+      df = fmax(df, fabs(fs[0] - fs[k]));
+    }
+    if (dx <= xatol && df <= fatol) break;
+    double xb[2], xr[2], xe[2], xo[2], xi[2];
+    for (int d = 0; d < 2; ++d) {
+      xb[d] = (sim[0][d] + sim[1][d]) / 2.0;
+      xr[d] = 2.0 * xb[d] - sim[2][d];
+      xe[d] = 3.0 * xb[d] - 2.0 * sim[2][d];
+      xo[d] = 1.5 * xb[d] - 0.5 * sim[2][d];
+      xi[d] = 0.5 * xb[d] + 0.5 * sim[2][d];
+    }
+    if (threadIdx.x == 0)
       for (int d = 0; d < 2; ++d) {
-        xb[d] = (sim[0][d] + sim[1][d]) / 2.0;
-        xr[d] = 2.0 * xb[d] - sim[2][d];
+        pts[0][d] = xr[d];
+        pts[1][d] = xe[d];
+        pts[2][d] = xo[d];
+        pts[3][d] = xi[d];
       }
-      double fr = f(xr[0], xr[1]);
-      bool shrink = false;
-      if (fr < fs[0]) {
-        double xe[2] = {3.0 * xb[0] - 2.0 * sim[2][0], 3.0 * xb[1] - 2.0 * sim[2][1]};
-        double fe = f(xe[0], xe[1]);
-        if (fe < fr) { sim[2][0] = xe[0]; sim[2][1] = xe[1]; fs[2] = fe; }
-        else { sim[2][0] = xr[0]; sim[2][1] = xr[1]; fs[2] = fr; }
-      } else if (fr < fs[1]) {
-        sim[2][0] = xr[0]; sim[2][1] = xr[1]; fs[2] = fr;
-      } else if (fr < fs[2]) {
-        double xc[2] = {1.5 * xb[0] - 0.5 * sim[2][0], 1.5 * xb[1] - 0.5 * sim[2][1]};
-        double fc = f(xc[0], xc[1]);
-        if (fc <= fr) { sim[2][0] = xc[0]; sim[2][1] = xc[1]; fs[2] = fc; }
-        else shrink = true;
-      } else {
-        double xc[2] = {0.5 * xb[0] + 0.5 * sim[2][0], 0.5 * xb[1] + 0.5 * sim[2][1]};
-        double fc = f(xc[0], xc[1]);
-        if (fc < fs[2]) { sim[2][0] = xc[0]; sim[2][1] = xc[1]; fs[2] = fc; }
-        else shrink = true;
-      }
-      if (shrink)
-        for (int j = 1; j < 3; ++j) {
-          for (int d = 0; d < 2; ++d) sim[j][d] = sim[0][d] + 0.5 * (sim[j][d] - sim[0][d]);
-          fs[j] = f(sim[j][0], sim[j][1]);
-        }
-      ++it;
-      sort3();
+    round(4);
+    const double fr = vals[0], fe = vals[1], fo = vals[2], fi = vals[3];
+    bool shrink = false;
+    if (fr < fs[0]) {
+      if (fe < fr) { sim[2][0] = xe[0]; sim[2][1] = xe[1]; fs[2] = fe; }
+      else { sim[2][0] = xr[0]; sim[2][1] = xr[1]; fs[2] = fr; }
+    } else if (fr < fs[1]) {
+      sim[2][0] = xr[0]; sim[2][1] = xr[1]; fs[2] = fr;
+    } else if (fr < fs[2]) {
+      if (fo <= fr) { sim[2][0] = xo[0]; sim[2][1] = xo[1]; fs[2] = fo; }
+      else shrink = true;
+    } else {
+      if (fi < fs[2]) { sim[2][0] = xi[0]; sim[2][1] = xi[1]; fs[2] = fi; }
+      else shrink = true;
     }
+    if (shrink) {
+      for (int j = 1; j < 3; ++j)
+        for (int d = 0; d < 2; ++d) sim[j][d] = sim[0][d] + 0.5 * (sim[j][d] - sim[0][d]);
+      if (threadIdx.x == 0)
+        for (int j = 1; j < 3; ++j) {
+          pts[j - 1][0] = sim[j][0];
+          pts[j - 1][1] = sim[j][1];
+        }
+      round(2);
+      fs[1] = vals[0];
+      fs[2] = vals[1];
+    }
+    ++it;
+    sort3();
+  }
+  if (warp == 0) {
     zd g(scale * sim[0][0], scale * sim[0][1]);
     double res = wave_objective(a, grp, g, Inrm, Vnrm, true);
     if (lane == 0) {
@@ -362,7 +401,10 @@ __global__ void fit_kernel(FitArgs a) {
         }
     }
   }
-  __syncthreads();
+}
+
+// After the fits of all groups: SI = -B A^-1, the reference impedances and S.
+__global__ void fit_finish_kernel(FitArgs a) {
   if (threadIdx.x != 0) return;
   // SI = -B A^-1 (Gauss-Jordan with partial pivoting on [A^T | -B^T]: X^T = A^-T (-B^T))
   const int P = a.P;
@@ -644,7 +686,8 @@ extern "C" int m25_deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_por
   fa.resid = reinterpret_cast<double*>(fa.zline + kMaxPorts);
   fa.z0 = fa.resid + kMaxPorts;
   fa.iters = p->iters;
-  fit_kernel<<<1, 32 * p->ngroup, 0, st>>>(fa);
+  fit_kernel<<<p->ngroup, 32 * kFitWarps, 0, st>>>(fa);
+  fit_finish_kernel<<<1, 32, 0, st>>>(fa);
   M25_CHECK_LAUNCH();
   std::vector<zd> h(4 * kMaxPorts * kMaxPorts);
   M25_CUDA(cudaMemcpyAsync(h.data(), p->out, sizeof(zd) * h.size(), cudaMemcpyDeviceToHost, st));

@@ -104,6 +104,7 @@ __device__ __forceinline__ void source_pass(const FillArgs<T>& a, const TriData<
                                             cx<T> cA, cx<T> cV, T dz, const T* st, int lane, cx<T> (&Q)[3],
                                             cx<T> (&Px)[3], cx<T> (&Py)[3], cx<T>& IV, const T (&tv)[3][2]) {
   const T inv4pi = T(1.0 / (4.0 * kPi));
+  cx<T> S0, SX, SY, T0, T1, T2;  // sums of w_k K over the test points k, weighted by 1, x_k, y_k
   T sq[NQ][2], sw[NQ];
 #pragma unroll
   for (int l = 0; l < NQ; ++l) {
@@ -160,16 +161,24 @@ __device__ __forceinline__ void source_pass(const FillArgs<T>& a, const TriData<
       }
       K0V += sv * sw[l];
     }
-    const T wk = tw[k];
+    // sums over the test points; the vertex terms a_i are applied once below
+    const T wk = tw[k], wx = wk * tq[k][0], wy = wk * tq[k][1];
     IV += K0V * wk;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      // w_k (r_k - a_i), lengths about the test centroid
-      T ax = wk * (tq[k][0] - tv[i][0]), ay = wk * (tq[k][1] - tv[i][1]);
-      Q[i] += K1x * ax + K1y * ay;
-      Px[i] += K0A * ax;
-      Py[i] += K0A * ay;
+    S0 += K0A * wk;
+    SX += K0A * wx;
+    SY += K0A * wy;
+    if (NEAR || NQ > 1) {  // the one-point rule has no first moments
+      T1 += K1x * wk;
+      T2 += K1y * wk;
+      T0 += K1x * wx + K1y * wy;
     }
+  }
+  // sum_k w_k (r_k - a_i) K, lengths about the test centroid
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    Px[i] = SX - S0 * tv[i][0];
+    Py[i] = SY - S0 * tv[i][1];
+    Q[i] = T0 - (T1 * tv[i][0] + T2 * tv[i][1]);
   }
 }
 
