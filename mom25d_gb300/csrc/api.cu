@@ -41,9 +41,9 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
 
 // lu.cu
 template <class T> int lu_factor(m25_ctx*, cx<T>*, int64_t, int, int32_t*, int, bool, int*);
-template <class TZ>
-int refine(m25_ctx*, int, int, const cx<TZ>*, int64_t, const zf*, const int32_t*, const zd*, zd*, double, int, int*);
-void cast_to_z32(m25_ctx*, const zd*, int64_t, zf*, int64_t, int, int);
+int refine(m25_ctx*, int, int, const zf*, const zf*, int64_t, const zf*, const int32_t*, const zd*, zd*, double, int,
+           int*);
+void split_to_z32(m25_ctx*, const zd*, int64_t, zf*, zf*, zf*, int64_t, int, int);
 bool lu_tc_available();
 template <class TF, class TV>
 int lu_solve_wave(m25_ctx*, const cx<TF>*, int64_t, int, const int32_t*, const cx<TV>*, int, cx<TV>*,
@@ -254,10 +254,19 @@ extern "C" int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precis
       M25_CUDA(cudaMemcpyAsync(ctx->Zw.p, Z, zb, cudaMemcpyHostToDevice, st));
       Zres = ctx->Zw.p;
     }
-    if (precision == M25_MIXED_FILL32)
+    // Z for the residuals as complex64 planes Zh + Zl (fp64-level products on
+    // the fp32 pipes); Zh is also the LU's input
+    const zf* Zh = static_cast<const zf*>(Zres);
+    const zf* Zl = nullptr;
+    if (precision == M25_MIXED_FILL32) {
       M25_CUDA(cudaMemcpyAsync(LU, Zres, sizeof(zf) * nn, cudaMemcpyDeviceToDevice, st));
-    else
-      cast_to_z32(ctx, static_cast<const zd*>(Zres), n, LU, n, n, n);
+    } else {
+      if ((rc = ctx->Zsplit.ensure(sizeof(zf) * 2 * nn))) return rc;
+      zf* h = ctx->Zsplit.as<zf>();
+      split_to_z32(ctx, static_cast<const zd*>(Zres), n, LU, h, h + nn, n, n, n);
+      Zh = h;
+      Zl = h + nn;
+    }
     if ((rc = lu_factor<float>(ctx, LU, n, n, ctx->ipiv.as<int32_t>(), kPanelZ64, lu_tc_available(), &zinfo)))
       return rc;
     if (zinfo) {
@@ -265,12 +274,7 @@ extern "C" int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precis
       set_error("m25_dense_solve: zero pivot in the complex64 LU");
       return M25_ERR_NUMERIC;
     }
-    if (precision == M25_MIXED_FILL32)
-      rc = refine<float>(ctx, n, nrhs, static_cast<const zf*>(Zres), n, LU, ctx->ipiv.as<int32_t>(), Bd, Xd, tol,
-                         max_iter, &steps);
-    else
-      rc = refine<double>(ctx, n, nrhs, static_cast<const zd*>(Zres), n, LU, ctx->ipiv.as<int32_t>(), Bd, Xd, tol,
-                          max_iter, &steps);
+    rc = refine(ctx, n, nrhs, Zh, Zl, n, LU, ctx->ipiv.as<int32_t>(), Bd, Xd, tol, max_iter, &steps);
     if (rc) return rc;
   } else {
     set_error("m25_dense_solve: unknown precision");

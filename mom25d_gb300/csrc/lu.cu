@@ -654,15 +654,6 @@ __global__ void gather_rows_kernel(int n, int nrhs, const int32_t* __restrict__ 
   Bp[e] = B[(int64_t)perm[i] * nrhs + c];
 }
 
-__global__ void cast_z64_to_z32(const zd* __restrict__ a, int64_t lda, zf* __restrict__ b, int64_t ldb, int n,
-                                int m) {
-  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (int64_t)n * m) return;
-  int64_t r = e / m, c = e % m;
-  zd v = a[r * lda + c];
-  b[r * ldb + c] = zf(float(v.re), float(v.im));
-}
-
 // ----------------------------------------------------------------- drivers
 int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int nb);  // lu_tc.cu
 int lu_tc_prepare(m25_ctx* ctx, int n, int nb);
@@ -1306,46 +1297,132 @@ template int lu_factor<float>(m25_ctx*, zf*, int64_t, int, int32_t*, int, bool, 
 // ------------------------------------------------ GMRES iterative refinement
 // Right-hand sides are handled in lockstep (one column per rhs).
 
-// Y[t][c] = sum_k Z[t][k] X[k][c] in fp64, one warp per row; P (the number of
-// right-hand sides) is a template argument so the accumulators stay in registers
-template <class TZ, int P>
-__global__ void matvec_kernel_p(int n, const cx<TZ>* __restrict__ Z, int64_t ldz, const zd* __restrict__ X,
-                                zd* __restrict__ Y) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (warp >= n) return;
-  zd acc[P];
-  const cx<TZ>* row = Z + (int64_t)warp * ldz;
-  for (int t = lane; t < n; t += 32) {
-    cx<TZ> zz = row[t];
-    zd z(double(zz.re), double(zz.im));
+// ---- fp64-accurate products on the fp32 pipes. GB300's fp64 rate makes an
+// fp64 matrix-vector product arithmetic-bound (~0.8 ms at N = 5943); here
+// Z is held as two complex64 planes, Z = Zh + Zl (Zl = fp32(Z - Zh)), the
+// vectors likewise, and the dot products use the error-free transforms of
+// Ogita, Rump & Oishi ("Accurate sum and dot product", 2005): the FMA
+// two-product and Knuth's two-sum, with the cross terms Zh Xl + Zl Xh and the
+// rounding errors summed in fp32. The result is as accurate as a dot product
+// in about 2^-48 relative precision, read from the same HBM bytes as the
+// complex128 matrix.
+__device__ __forceinline__ void dot2_acc(float& s, float& c, float ah, float al, float bh, float bl) {
+  const float p = ah * bh;
+  const float ep = fmaf(ah, bh, -p);
+  const float t = s + p;
+  const float z = t - s;
+  const float es = (s - (t - z)) + (p - z);
+  s = t;
+  c += (ep + es) + fmaf(ah, bl, al * bh);
+}
+
+// Y = Z X for ROWS rows per warp; Zl may be absent (LO false: Z is exact in complex64)
+template <int P, int ROWS, bool LO>
+__global__ void __launch_bounds__(256) matvec_df_kernel(int n, const zf* __restrict__ Zh, const zf* __restrict__ Zl,
+                                                        int64_t ldz, const zf* __restrict__ Xh,
+                                                        const zf* __restrict__ Xl, zd* __restrict__ Y) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int r0 = warp * ROWS;
+  if (r0 >= n) return;
+  float s[ROWS][P][2], cc[ROWS][P][2];
 #pragma unroll
-    for (int c = 0; c < P; ++c) acc[c] += z * X[(int64_t)t * P + c];
+  for (int r = 0; r < ROWS; ++r)
+#pragma unroll
+    for (int c = 0; c < P; ++c) s[r][c][0] = s[r][c][1] = cc[r][c][0] = cc[r][c][1] = 0.f;
+  for (int t = lane; t < n; t += 32) {
+    zf xh[P], xl[P];
+#pragma unroll
+    for (int c = 0; c < P; ++c) {
+      xh[c] = Xh[(int64_t)t * P + c];
+      xl[c] = Xl[(int64_t)t * P + c];
+    }
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+      if (r0 + r >= n) break;
+      const zf zh = Zh[(int64_t)(r0 + r) * ldz + t];
+      const zf zl = LO ? Zl[(int64_t)(r0 + r) * ldz + t] : zf();
+#pragma unroll
+      for (int c = 0; c < P; ++c) {
+        dot2_acc(s[r][c][0], cc[r][c][0], zh.re, zl.re, xh[c].re, xl[c].re);
+        dot2_acc(s[r][c][0], cc[r][c][0], zh.im, zl.im, -xh[c].im, -xl[c].im);
+        dot2_acc(s[r][c][1], cc[r][c][1], zh.re, zl.re, xh[c].im, xl[c].im);
+        dot2_acc(s[r][c][1], cc[r][c][1], zh.im, zl.im, xh[c].re, xl[c].re);
+      }
+    }
   }
 #pragma unroll
-  for (int c = 0; c < P; ++c) {
-    double re = acc[c].re, im = acc[c].im;
-    for (int o = 16; o; o >>= 1) {
-      re += __shfl_down_sync(0xffffffffu, re, o);
-      im += __shfl_down_sync(0xffffffffu, im, o);
+  for (int r = 0; r < ROWS; ++r) {
+    if (r0 + r >= n) break;
+#pragma unroll
+    for (int c = 0; c < P; ++c) {
+      double v[2];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        float a = s[r][c][q], e = cc[r][c][q];
+        for (int o = 16; o; o >>= 1) {
+          const float b = __shfl_down_sync(0xffffffffu, a, o), f = __shfl_down_sync(0xffffffffu, e, o);
+          const float t = a + b, z = t - a;
+          e += f + ((a - (t - z)) + (b - z));
+          a = t;
+        }
+        v[q] = (double)a + (double)e;
+      }
+      if (lane == 0) Y[(int64_t)(r0 + r) * P + c] = zd(v[0], v[1]);
     }
-    if (lane == 0) Y[(int64_t)warp * P + c] = zd(re, im);
   }
 }
 
-template <class TZ>
-void matvec(int n, int P, const cx<TZ>* Z, int64_t ldz, const zd* X, zd* Y, cudaStream_t st) {
-  const unsigned g = (unsigned)(((size_t)n * 32 + 255) / 256);
+// hi / lo complex64 planes of complex128 values: hi = fp32(x), lo = fp32(x - hi)
+__global__ void split_z64_kernel(int64_t n, const zd* __restrict__ X, zf* __restrict__ Xh, zf* __restrict__ Xl) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const zd x = X[e];
+  const float hr = (float)x.re, hi = (float)x.im;
+  Xh[e] = zf(hr, hi);
+  Xl[e] = zf((float)(x.re - (double)hr), (float)(x.im - (double)hi));
+}
+
+// the same for an n x m block of a matrix (leading dimensions lda / ldb),
+// also writing the hi plane to a second destination (the LU's input)
+__global__ void split_matrix_kernel(const zd* __restrict__ a, int64_t lda, zf* __restrict__ lu, zf* __restrict__ h,
+                                    zf* __restrict__ l, int64_t ldb, int n, int m) {
+  int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)n * m) return;
+  const int64_t r = e / m, c = e % m;
+  const zd x = a[r * lda + c];
+  const float hr = (float)x.re, hi = (float)x.im;
+  const zf hv(hr, hi);
+  lu[r * ldb + c] = hv;
+  h[r * ldb + c] = hv;
+  l[r * ldb + c] = zf((float)(x.re - (double)hr), (float)(x.im - (double)hi));
+}
+
+// Y = (Zh + Zl) X in fp64-level accuracy; Xw holds the split X (2 n P complex64)
+void matvec_df(int n, int P, const zf* Zh, const zf* Zl, int64_t ldz, const zd* X, zf* Xw, zd* Y, cudaStream_t st) {
+  const int64_t np = (int64_t)n * P;
+  split_z64_kernel<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(np, X, Xw, Xw + np);
+  const zf* Xh = Xw;
+  const zf* Xl = Xw + np;
+#define M25_MVDF(PP, RR)                                                                                       \
+  do {                                                                                                         \
+    const unsigned g = (unsigned)(((size_t)(n + RR - 1) / RR * 32 + 255) / 256);                               \
+    if (Zl)                                                                                                    \
+      matvec_df_kernel<PP, RR, true><<<g, 256, 0, st>>>(n, Zh, Zl, ldz, Xh, Xl, Y);                            \
+    else                                                                                                       \
+      matvec_df_kernel<PP, RR, false><<<g, 256, 0, st>>>(n, Zh, Zl, ldz, Xh, Xl, Y);                           \
+  } while (0)
   switch (P) {
-    case 1: matvec_kernel_p<TZ, 1><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
-    case 2: matvec_kernel_p<TZ, 2><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
-    case 3: matvec_kernel_p<TZ, 3><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
-    case 4: matvec_kernel_p<TZ, 4><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
-    case 5: matvec_kernel_p<TZ, 5><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
-    case 6: matvec_kernel_p<TZ, 6><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
-    case 7: matvec_kernel_p<TZ, 7><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
-    case 8: matvec_kernel_p<TZ, 8><<<g, 256, 0, st>>>(n, Z, ldz, X, Y); break;
+    case 1: M25_MVDF(1, 4); break;
+    case 2: M25_MVDF(2, 4); break;
+    case 3: M25_MVDF(3, 2); break;
+    case 4: M25_MVDF(4, 2); break;
+    case 5: M25_MVDF(5, 1); break;
+    case 6: M25_MVDF(6, 1); break;
+    case 7: M25_MVDF(7, 1); break;
+    case 8: M25_MVDF(8, 1); break;
     default: break;  // 1 <= P <= 8 is checked by the callers
   }
+#undef M25_MVDF
 }
 
 // h[i][c] = sum_t conj(V_i[t][c]) W[t][c] for i < nvec: one CTA per i
@@ -1429,26 +1506,31 @@ __global__ void combine_kernel(int n, int P, int nvec, const zd* __restrict__ V,
   X[e] += s;
 }
 
-// max over rows of sum |Z[t][k]| (infinity norm), one warp per row + atomicMax on the bits
-template <class TZ>
-__global__ void rownorm_kernel(int n, const cx<TZ>* __restrict__ Z, int64_t ldz, unsigned long long* __restrict__ out) {
+// max over rows of sum |Z[t][k]| (infinity norm; it only scales the stopping
+// test, so fp32 from the hi plane), one warp per row + atomicMax on the bits
+__global__ void rownorm_kernel(int n, const zf* __restrict__ Z, int64_t ldz, unsigned long long* __restrict__ out) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= n) return;
-  double s = 0;
+  float s = 0;
   for (int t = lane; t < n; t += 32) {
-    cx<TZ> z = Z[(int64_t)warp * ldz + t];
-    s += hypot(double(z.re), double(z.im));
+    const zf z = Z[(int64_t)warp * ldz + t];
+    s += sqrtf(z.re * z.re + z.im * z.im);
   }
   for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-  if (lane == 0) atomicMax(out, (unsigned long long)__double_as_longlong(s));  // s >= 0: bit order = value order
+  if (lane == 0) atomicMax(out, (unsigned long long)__double_as_longlong((double)s));  // s >= 0: bit order = value order
 }
 
-__global__ void z64_to_z32_scaled(int64_t n, const zd* __restrict__ a, double s, zf* __restrict__ o) {
+// o = a / s and back, s = *sp (a device scalar; 1 when it is not positive)
+__global__ void z64_to_z32_scaled(int64_t n, const zd* __restrict__ a, const double* __restrict__ sp,
+                                  zf* __restrict__ o) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const double s = *sp > 0 ? 1.0 / *sp : 1.0;
   if (e < n) o[e] = zf(float(a[e].re * s), float(a[e].im * s));
 }
-__global__ void z32_to_z64_scaled(int64_t n, const zf* __restrict__ a, double s, zd* __restrict__ o) {
+__global__ void z32_to_z64_scaled(int64_t n, const zf* __restrict__ a, const double* __restrict__ sp,
+                                  zd* __restrict__ o) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const double s = *sp > 0 ? *sp : 1.0;
   if (e < n) o[e] = zd(double(a[e].re) * s, double(a[e].im) * s);
 }
 __global__ void maxabs_kernel(int64_t n, const zd* __restrict__ a, double* __restrict__ out) {
@@ -1469,17 +1551,18 @@ __global__ void maxabs_kernel(int64_t n, const zd* __restrict__ a, double* __res
 // complex64 LU applied in fp32 arithmetic (GMRES-based iterative refinement,
 // Carson & Higham 2017, in its flexible form so that the rounding of the
 // fp32 triangular solves does not break the Arnoldi relation: fp64 on this
-// GPU is too slow for the serial substitution chains). Matrix-vector
-// products, orthogonalisation and the iterate stay in fp64. Stops when the
-// normwise backward error |r| / (|Z| |x| + |b|) of every column <= tol;
-// max_iter bounds the total number of GMRES steps.
-template <class TZ>
-int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* LU, const int32_t* ipiv,
+// GPU is too slow for the serial substitution chains). Orthogonalisation and
+// the iterate stay in fp64; the matrix-vector products use Z = Zh + Zl, two
+// complex64 planes, with fp64-level accuracy on the fp32 pipes (matvec_df;
+// Zl absent when Z is itself complex64). Stops when the normwise backward
+// error |r| / (|Z| |x| + |b|) of every column <= tol; max_iter bounds the
+// total number of GMRES steps.
+int refine(m25_ctx* ctx, int n, int P, const zf* Zh, const zf* Zl, int64_t ldz, const zf* LU, const int32_t* ipiv,
            const zd* B, zd* X, double tol, int max_iter, int* steps) {
   cudaStream_t st = ctx->stream;
   const int m = std::min(30, std::max(1, max_iter));
   const size_t np = (size_t)n * P;
-  int rc = ctx->Rw.ensure(sizeof(zd) * np * (2 * m + 3) + sizeof(zf) * np * 2 + sizeof(double) * 64 +
+  int rc = ctx->Rw.ensure(sizeof(zd) * np * (2 * m + 3) + sizeof(zf) * np * 4 + sizeof(double) * 64 +
                           sizeof(zd) * (size_t)(m + 2) * P * 2 + sizeof(int32_t) * n);
   if (rc) return rc;
   zd* V = ctx->Rw.as<zd>();           // (m+1) Arnoldi vectors
@@ -1491,21 +1574,20 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
   double* dsc = reinterpret_cast<double*>(d32 + np);  // scalars
   zd* hdev = reinterpret_cast<zd*>(dsc + 64);
   zd* ydev = hdev + (size_t)(m + 2) * P;
-  int32_t* perm = reinterpret_cast<int32_t*>(ydev + (size_t)(m + 2) * P);  // row permutation of the LU
+  zf* xsplit = reinterpret_cast<zf*>(ydev + (size_t)(m + 2) * P);  // (2 n P) hi / lo planes of a vector
+  int32_t* perm = reinterpret_cast<int32_t*>(xsplit + 2 * np);       // row permutation of the LU
   const unsigned g1 = (unsigned)((np + 255) / 256);
   const unsigned gw = (unsigned)(((size_t)n * 32 + 255) / 256);
   StageTimer tm(ctx, ST_REFINE);
-  // out = (LU32)^-1 in, in fp32 with the input scaled to O(1)
+  // out = (LU32)^-1 in, in fp32 with the input scaled to O(1) by its
+  // largest entry (kept on the device: no host round trip)
+  double* pscale = dsc + 48;
   auto precond = [&](const zd* in, zd* out) -> int {
-    maxabs_kernel<<<1, 1024, 0, st>>>((int64_t)np, in, dsc);
-    double s = 0;
-    M25_CUDA(cudaMemcpyAsync(&s, dsc, sizeof(double), cudaMemcpyDeviceToHost, st));
-    M25_CUDA(cudaStreamSynchronize(st));
-    if (!(s > 0)) s = 1;
-    z64_to_z32_scaled<<<g1, 256, 0, st>>>((int64_t)np, in, 1.0 / s, r32);
+    maxabs_kernel<<<1, 1024, 0, st>>>((int64_t)np, in, pscale);
+    z64_to_z32_scaled<<<g1, 256, 0, st>>>((int64_t)np, in, pscale, r32);
     int r = lu_solve_wave<float, float>(ctx, LU, n, n, ipiv, r32, P, d32, perm);
     if (r) return r;
-    z32_to_z64_scaled<<<g1, 256, 0, st>>>((int64_t)np, d32, s, out);
+    z32_to_z64_scaled<<<g1, 256, 0, st>>>((int64_t)np, d32, pscale, out);
     return M25_OK;
   };
   auto col_norms = [&](const zd* v, std::vector<double>& out) -> int {
@@ -1527,7 +1609,7 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
   {
     unsigned long long* zb = reinterpret_cast<unsigned long long*>(dsc + 32);
     M25_CUDA(cudaMemsetAsync(zb, 0, sizeof(unsigned long long), st));
-    rownorm_kernel<TZ><<<gw, 256, 0, st>>>(n, Z, ldz, zb);
+    rownorm_kernel<<<gw, 256, 0, st>>>(n, Zh, ldz, zb);
     M25_CUDA(cudaMemcpyAsync(&znorm, zb, sizeof(double), cudaMemcpyDeviceToHost, st));
     M25_CUDA(cudaStreamSynchronize(st));
   }
@@ -1538,7 +1620,7 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
   std::vector<zd> hh((size_t)(m + 2) * P), H((size_t)(m + 1) * m * P), g((size_t)(m + 1) * P), cs(m * P), sn(m * P);
   for (int outer = 0; outer < 50; ++outer) {
     // R = B - Z X
-    matvec<TZ>(n, P, Z, ldz, X, W, st);
+    matvec_df(n, P, Zh, Zl, ldz, X, xsplit, W, st);
     M25_CUDA(cudaMemcpyAsync(R, B, np * sizeof(zd), cudaMemcpyDeviceToDevice, st));
     if ((rc = set_col_scalars(std::vector<zd>(P, zd(-1.0))))) return rc;
     combine_kernel<<<g1, 256, 0, st>>>(n, P, 1, W, 0, ydev, R);
@@ -1576,7 +1658,7 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
     for (; k < m && total < max_iter; ++k, ++total) {
       zd* zk = Zp + np * k;
       if ((rc = precond(V + np * k, zk))) return rc;
-      matvec<TZ>(n, P, Z, ldz, zk, W, st);
+      matvec_df(n, P, Zh, Zl, ldz, zk, xsplit, W, st);
       // classical Gram-Schmidt, twice
       std::fill(hh.begin(), hh.end(), zd(0.0));
       for (int pass = 0; pass < 2; ++pass) {
@@ -1645,14 +1727,11 @@ int refine(m25_ctx* ctx, int n, int P, const cx<TZ>* Z, int64_t ldz, const zf* L
   return M25_OK;
 }
 
-template int refine<double>(m25_ctx*, int, int, const zd*, int64_t, const zf*, const int32_t*, const zd*, zd*, double,
-                            int, int*);
-template int refine<float>(m25_ctx*, int, int, const zf*, int64_t, const zf*, const int32_t*, const zd*, zd*, double,
-                           int, int*);
 
-void cast_to_z32(m25_ctx* ctx, const zd* a, int64_t lda, zf* b, int64_t ldb, int n, int m) {
+
+void split_to_z32(m25_ctx* ctx, const zd* a, int64_t lda, zf* lu, zf* h, zf* l, int64_t ldb, int n, int m) {
   int64_t tot = (int64_t)n * m;
-  cast_z64_to_z32<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(a, lda, b, ldb, n, m);
+  split_matrix_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(a, lda, lu, h, l, ldb, n, m);
 }
 
 }  // namespace m25

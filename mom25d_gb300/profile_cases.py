@@ -2,11 +2,14 @@
 
     python -m mom25d_gb300.profile_cases fill  --workload bandpass --precision fp64 [--reps 2]
     python -m mom25d_gb300.profile_cases point --workload lpf --precision mixed [--reps 1]
+    python -m mom25d_gb300.profile_cases lu --n 4096 [--simt] [--reps 1]
 
 `fill` builds the mesh geometry and one frequency's Green's tables, then
 runs the impedance fill `reps` times (device output, no host copy);
 `point` runs `reps` full frequency points (tables, fill, LU + solve,
-de-embedding). Each exits non-zero on any engine error.
+de-embedding); `lu` factors a seeded random n x n complex64 matrix on the
+device (tensor-core trailing updates unless --simt). Each exits non-zero on
+any engine error.
 """
 
 import argparse
@@ -21,12 +24,16 @@ from .solver import PRECISIONS, Solver
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("mode", choices=["fill", "point"])
+    ap.add_argument("mode", choices=["fill", "point", "lu"])
+    ap.add_argument("--n", type=int, default=4096, help="matrix size of the lu mode")
+    ap.add_argument("--simt", action="store_true", help="lu mode: SIMT trailing updates")
     ap.add_argument("--workload", default="bandpass")
     ap.add_argument("--precision", default="fp64", choices=list(PRECISIONS))
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--freq", type=float, default=None, help="Hz (default: the workload's middle frequency)")
     args = ap.parse_args()
+    if args.mode == "lu":
+        return lu_case(args)
     import mom25d_gb300 as G
 
     kw = {"k": 0} if args.workload == "bandpass" else {}
@@ -52,6 +59,26 @@ def main():
             S = sol.point(f)[0]
         print(f"point ok: N={mesh.n_unknowns} S11={np.round(S[0, 0], 6)}")
     sol.close()
+
+
+def lu_case(args):
+    import torch
+
+    n = args.n
+    ctx = E.Context(0)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    A0 = torch.randn((n, n), dtype=torch.complex64, device="cuda", generator=g)
+    piv = torch.empty(n, dtype=torch.int32, device="cuda")
+    info = np.zeros(1, np.int32)
+    flags = E.M25_LU_NO_TENSOR_CORES if args.simt else 0
+    for _ in range(args.reps):
+        A = A0.clone()
+        E.check(ctx.lib.m25_lu_factor(ctx.h, n, E.M25_MIXED, C.c_void_p(A.data_ptr()), n,
+                                      C.cast(C.c_void_p(piv.data_ptr()), C.POINTER(C.c_int32)), E.M25_ON_DEVICE, flags,
+                                      E.ptr(info, C.c_int32)))
+    ctx.synchronize()
+    print(f"lu ok: n={n} info={int(info[0])} tensor_cores={not args.simt}")
+    ctx.close()
 
 
 if __name__ == "__main__":
