@@ -907,42 +907,35 @@ __device__ __forceinline__ void fetch_diag_t(cx<TF>* DgT, const cx<TF>* A, int64
   cp_async_commit();
 }
 
-// Substitution on the diagonal block by one warp, in registers: lane l owns
-// the rows 2l and 2l + 1, so each round the owner of a pair of rows solves
-// both locally and broadcasts them with one round of shuffles (32 rounds for
-// 64 rows). Lower: unit diagonal, forward; upper: backward with the
-// reciprocal diagonal dinv. PT right-hand sides as a compile-time count (8:
-// up to 8, the count P checked at run time). acc (rows x P) in and out.
-template <class TF, class TV, int PT>
-__device__ __forceinline__ void diag_solve(int lane, int w, int P, int upper, const cx<TF>* DgT, const cx<TV>* dinv,
-                                           cx<TV>* acc) {
+// Substitution on the diagonal block by one warp for one right-hand side c,
+// in registers: lane l owns the rows 2l and 2l + 1, so each round the owner of
+// a pair of rows solves both locally and broadcasts them with one round of
+// shuffles (32 rounds for 64 rows). DgT is the transposed diagonal tile
+// already masked to the triangle of this sweep (zeros elsewhere and outside
+// the block), dinv the reciprocal diagonal (zero outside the block), so the
+// rounds load factors without any test. Lower: unit diagonal, forward; upper:
+// backward. acc (rows x P) in and out, column c.
+template <class TF, class TV>
+__device__ __forceinline__ void diag_solve1(int lane, int w, int P, int c, int upper, const cx<TF>* DgT,
+                                            const cx<TV>* dinv, cx<TV>* acc) {
   const int ra = 2 * lane, rb = ra + 1;
-  cx<TV> va[PT], vb[PT];
-#pragma unroll
-  for (int c = 0; c < PT; ++c) {
-    const bool ok = PT < 8 || c < P;
-    va[c] = (ok && ra < w) ? acc[ra * P + c] : cx<TV>();
-    vb[c] = (ok && rb < w) ? acc[rb * P + c] : cx<TV>();
-  }
+  cx<TV> va = ra < w ? acc[ra * P + c] : cx<TV>();
+  cx<TV> vb = rb < w ? acc[rb * P + c] : cx<TV>();
   const int npair = (w + 1) >> 1;
-  // factor of row r at column col: 0 outside the block and outside the triangle
-  auto F = [&](int r, int col) -> cx<TV> {
-    const bool in = r < w && col < w && (upper ? r < col : r > col);
-    return in ? cx<TV>(DgT[min(col, 63) * kTileLd + r]) : cx<TV>();
-  };
   struct Fac {
     cx<TV> aA, aB, bA, bB, da, db;  // row ra / rb at column 2k / 2k + 1; reciprocal diagonals of the pair
   };
   auto load = [&](int k) {
     Fac f;
-    const int ca = 2 * k, cb = ca + 1;
-    f.aA = F(ra, ca);
-    f.aB = F(ra, cb);
-    f.bA = F(rb, ca);
-    f.bB = F(rb, cb);
+    const cx<TF>* ca = DgT + (2 * k) * kTileLd;
+    const cx<TF>* cb = ca + kTileLd;
+    f.aA = cx<TV>(ca[ra]);
+    f.bA = cx<TV>(ca[rb]);
+    f.aB = cx<TV>(cb[ra]);
+    f.bB = cx<TV>(cb[rb]);
     if (upper) {
-      f.da = dinv[min(ca, 63)];
-      f.db = cb < w ? dinv[cb] : cx<TV>();
+      f.da = dinv[2 * k];
+      f.db = dinv[2 * k + 1];
     }
     return f;
   };
@@ -952,18 +945,13 @@ __device__ __forceinline__ void diag_solve(int lane, int w, int P, int upper, co
       const Fac f = nx;
       nx = load(min(k + 1, npair - 1));
       const bool mine = lane == k;
-#pragma unroll
-      for (int c = 0; c < PT; ++c) {
-        if (PT == 8 && c >= P) continue;
-        // owner (lane k): x_2k is final, x_2k+1 = v_2k+1 - L[2k+1][2k] x_2k
-        const cx<TV> xa_own = va[c];
-        const cx<TV> xb_own = vb[c] - f.bA * va[c];
-        const cx<TV> xa(__shfl_sync(0xffffffffu, xa_own.re, k), __shfl_sync(0xffffffffu, xa_own.im, k));
-        const cx<TV> xb(__shfl_sync(0xffffffffu, xb_own.re, k), __shfl_sync(0xffffffffu, xb_own.im, k));
-        // rows below the pair; the owner keeps the two values it broadcast
-        va[c] = mine ? xa : va[c] - (f.aA * xa + f.aB * xb);
-        vb[c] = mine ? xb : vb[c] - (f.bA * xa + f.bB * xb);
-      }
+      // owner (lane k): x_2k is final, x_2k+1 = v_2k+1 - L[2k+1][2k] x_2k
+      const cx<TV> xb_own = vb - f.bA * va;
+      const cx<TV> xa(__shfl_sync(0xffffffffu, va.re, k), __shfl_sync(0xffffffffu, va.im, k));
+      const cx<TV> xb(__shfl_sync(0xffffffffu, xb_own.re, k), __shfl_sync(0xffffffffu, xb_own.im, k));
+      // rows below the pair; the owner keeps the two values it broadcast
+      va = mine ? xa : va - (f.aA * xa + f.aB * xb);
+      vb = mine ? xb : vb - (f.bA * xa + f.bB * xb);
     }
   } else {
     Fac nx = load(npair - 1);
@@ -971,26 +959,17 @@ __device__ __forceinline__ void diag_solve(int lane, int w, int P, int upper, co
       const Fac f = nx;
       nx = load(max(k - 1, 0));
       const bool mine = lane == k;
-#pragma unroll
-      for (int c = 0; c < PT; ++c) {
-        if (PT == 8 && c >= P) continue;
-        // owner: x_2k+1 = v_2k+1 / d, then x_2k = (v_2k - U[2k][2k+1] x_2k+1) / d
-        const cx<TV> xb_own = vb[c] * f.db;
-        const cx<TV> xa_own = (va[c] - f.aB * xb_own) * f.da;
-        const cx<TV> xa(__shfl_sync(0xffffffffu, xa_own.re, k), __shfl_sync(0xffffffffu, xa_own.im, k));
-        const cx<TV> xb(__shfl_sync(0xffffffffu, xb_own.re, k), __shfl_sync(0xffffffffu, xb_own.im, k));
-        va[c] = mine ? xa : va[c] - (f.aA * xa + f.aB * xb);
-        vb[c] = mine ? xb : vb[c] - (f.bA * xa + f.bB * xb);
-      }
+      // owner: x_2k+1 = v_2k+1 / d, then x_2k = (v_2k - U[2k][2k+1] x_2k+1) / d
+      const cx<TV> xb_own = vb * f.db;
+      const cx<TV> xa_own = (va - f.aB * xb_own) * f.da;
+      const cx<TV> xa(__shfl_sync(0xffffffffu, xa_own.re, k), __shfl_sync(0xffffffffu, xa_own.im, k));
+      const cx<TV> xb(__shfl_sync(0xffffffffu, xb_own.re, k), __shfl_sync(0xffffffffu, xb_own.im, k));
+      va = mine ? xa : va - (f.aA * xa + f.aB * xb);
+      vb = mine ? xb : vb - (f.bA * xa + f.bB * xb);
     }
   }
-#pragma unroll
-  for (int c = 0; c < PT; ++c) {
-    if (PT == 8 && c >= P) continue;
-    if (ra < w) acc[ra * P + c] = va[c];
-    if (rb < w) acc[rb * P + c] = vb[c];
-  }
-  __syncwarp();
+  if (ra < w) acc[ra * P + c] = va;
+  if (rb < w) acc[rb * P + c] = vb;
 }
 
 // tiles in flight per CTA: 4 complex64 or 2 complex128 tiles
@@ -1059,12 +1038,33 @@ __global__ void __launch_bounds__(256, 1) trsv_wave_kernel(WaveArgs<TF, TV> a) {
       else cp_async_commit();
     }
     for (int e = tid; e < w * P; e += blockDim.x) acc[e] = a.X[(int64_t)r0 * P + e];
+    // reciprocal diagonal (zero outside the block), then the tile masked to
+    // this sweep's triangle (zero elsewhere); the first step's barrier
+    // separates the two, the next barrier publishes the result
+    auto prep_diag = [&]() {
+      if (tid < 64) {
+        cx<TV> di;
+        if (a.upper && tid < w) {
+          const cx<TV> dd(Dg[tid * kTileLd + tid]);
+          const TV m2 = dd.re * dd.re + dd.im * dd.im;
+          di = cx<TV>(dd.re / m2, -dd.im / m2);
+        }
+        dinv[tid] = di;
+      }
+      __syncthreads();
+      for (int e = tid; e < 64 * 64; e += blockDim.x) {
+        const int col = e >> 6, r = e & 63;
+        const bool keep = r < w && col < w && (a.upper ? r < col : r > col);
+        if (!keep) Dg[col * kTileLd + r] = cx<TF>();
+      }
+    };
     for (int d = 0; d < ndep; ++d) {
       const int j = dep(d), c0 = j * 64, wj = min(64, a.n - c0);
       const cx<TF>* T = ring + (d % S) * 64 * kTileLd;
       if constexpr (kTagged) {
         cp_async_wait<S - 1>();  // tile d and the prefetched y_j have landed
         __syncthreads();
+        if (d == 0) prep_diag();  // the diagonal tile (group 0) is in: mask it while the chain runs
         // words of y_j not yet final when prefetched are polled until they carry this sweep's tag
         const unsigned long long* ys = yring + (d % S) * kYtWords;
         bool bad = false;
@@ -1110,6 +1110,7 @@ __global__ void __launch_bounds__(256, 1) trsv_wave_kernel(WaveArgs<TF, TV> a) {
         }
         cp_async_wait<S - 1>();  // tile d has landed
         __syncthreads();
+        if (d == 0) prep_diag();
         if (fail) {
           cp_async_wait<0>();
           return;
@@ -1143,22 +1144,16 @@ __global__ void __launch_bounds__(256, 1) trsv_wave_kernel(WaveArgs<TF, TV> a) {
     }
     cp_async_wait<0>();
     __syncthreads();
-    if (a.upper && tid < w) {
-      const cx<TV> dd(Dg[tid * kTileLd + tid]);
-      const TV m2 = dd.re * dd.re + dd.im * dd.im;
-      dinv[tid] = cx<TV>(dd.re / m2, -dd.im / m2);
+    if (ndep == 0) {
+      prep_diag();
+      __syncthreads();
     }
+    // diagonal block: warp c solves right-hand side c (P <= 8 warps in parallel)
+    const int warp = tid >> 5, lane = tid & 31;
+    if (warp < P) diag_solve1<TF, TV>(lane, w, P, warp, a.upper, Dg, dinv, acc);
     __syncthreads();
-    // diagonal block by warp 0, then publish y_i
+    // publish y_i (warp 0)
     if (tid < 32) {
-      const int lane = tid;
-      switch (P) {
-        case 1: diag_solve<TF, TV, 1>(lane, w, P, a.upper, Dg, dinv, acc); break;
-        case 2: diag_solve<TF, TV, 2>(lane, w, P, a.upper, Dg, dinv, acc); break;
-        case 3: diag_solve<TF, TV, 3>(lane, w, P, a.upper, Dg, dinv, acc); break;
-        case 4: diag_solve<TF, TV, 4>(lane, w, P, a.upper, Dg, dinv, acc); break;
-        default: diag_solve<TF, TV, 8>(lane, w, P, a.upper, Dg, dinv, acc); break;
-      }
       if constexpr (kTagged) {
         // publish first (the chain waits on it), then the plain copy for the next sweep
         const unsigned long long hi = (unsigned long long)tag << 32;
