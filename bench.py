@@ -9,9 +9,12 @@ solve of the 2 port excitations, de-embedding to S, all on the GPU.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64] [--impl reference]
 
 value: points/s with the mesh, test blocks and port data already on the
-device (the `mixed` path: complex64 fill + LU, fp64 refinement). e2e: the
-same through the public API (Solver construction + sweep, host arrays in,
-S and the currents back on the host). Under torchrun each rank sweeps its
+device (the `mixed` path: fp64 fill, complex64 LU with tensor-core trailing
+updates, GMRES refinement to fp64 accuracy), --workers points in flight on
+the GPU (one engine context and stream each); timed with CUDA events around
+a device-wide synchronisation on both sides. e2e: the same through the
+public API (Solver construction + sweep(workers=...), host arrays in, S and
+the currents back on the host). Under torchrun each rank sweeps its
 own frequencies (weak scaling, no collective in the path). --impl
 reference times the CPU oracle (numpy restatement of mom25d's own path) on
 the host cores on a bounded sample of each point.
@@ -123,37 +126,67 @@ def run_ours(args, rank, world, local):
             dist.barrier()
         torch.cuda.synchronize()
 
-    # ---- device-resident: geometry, ports uploaded before the timed region
+    # ---- device-resident: geometry, ports uploaded before the timed region;
+    # K workers = K engine contexts (streams), points handed out in order
+    K = max(1, args.workers)
     sol = Solver(mesh, st, verbose=False, precision=args.precision, device=local)
-    sol.geometry()
-    sol.port_data()
-    lib, ctx = sol.ctx.lib, sol.ctx.h
-    for f in my[:args.warmup]:
-        sol.point(f)
+    sols = [sol._sibling(w) for w in range(K)]
+    for s_ in sols:
+        s_.geometry()
+        s_.port_data()
+    warm = my[:args.warmup]
+    for w, s_ in enumerate(sols):
+        for f in warm[w::K] or warm[:1]:
+            s_.point(f)
     import ctypes as C
 
-    ms = (C.c_double * 11)()
-    cnt = (C.c_longlong * 11)()
-    E.check(lib.m25_ctx_timing(ctx, 1, ms, cnt))  # reset + enable the stage timers
+    STAGES = ["greens", "fill", "gather", "via", "lu_panel", "lu_laswp", "lu_trsm", "lu_gemm", "trsv", "refine",
+              "deembed"]
+    ms = [(C.c_double * 11)() for _ in sols]
+    cnt = [(C.c_longlong * 11)() for _ in sols]
+    for s_, m_, c_ in zip(sols, ms, cnt):
+        E.check(s_.ctx.lib.m25_ctx_timing(s_.ctx.h, 1, m_, c_))  # reset + enable the stage timers
+    pts = my[args.warmup:]
+    lock = threading.Lock()
+    nxt = [0]
+    per_worker = [0] * K
+
+    def worker(w):
+        while True:
+            with lock:
+                if nxt[0] >= len(pts):
+                    return
+                f = pts[nxt[0]]
+                nxt[0] += 1
+            sols[w].point(f)
+            per_worker[w] += 1
+
     barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
-        t0 = time.perf_counter()
-        for f in my[args.warmup:]:
-            sol.point(f)
-        sol.ctx.synchronize()
-        barrier()
-        dt = time.perf_counter() - t0
-    E.check(lib.m25_ctx_timing(ctx, 0, ms, cnt))
-    stages = dict(zip(["greens", "fill", "gather", "via", "lu_panel", "lu_laswp", "lu_trsm", "lu_gemm", "trsv",
-                       "refine", "deembed"], [round(v / args.steps, 4) for v in ms]))
-    launches = {k: int(c) for k, c in zip(stages, cnt)}
+        ev0.record()
+        th = [threading.Thread(target=worker, args=(w,)) for w in range(K)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        barrier()  # every worker's stream drained
+        ev1.record()
+        ev1.synchronize()
+    dt = ev0.elapsed_time(ev1) * 1e-3
+    for s_, m_, c_ in zip(sols, ms, cnt):
+        E.check(s_.ctx.lib.m25_ctx_timing(s_.ctx.h, 0, m_, c_))
+    # stage times of worker 0's points (overlapped with the other workers' points)
+    n0 = max(1, per_worker[0])
+    stages = dict(zip(STAGES, [round(v / n0, 4) for v in ms[0]]))
+    launches = sum(int(c) for c_ in cnt for c in c_)
     geo = sol.geometry_stats()
     sol.close()
     # ---- e2e through the public API: host arrays in, S + currents out
     barrier()
     t0 = time.perf_counter()
     sol2 = Solver(mesh, st, verbose=False, precision=args.precision, device=local)
-    r = sol2.sweep(my[args.warmup:], keep_currents=True)
+    r = sol2.sweep(my[args.warmup:], keep_currents=True, workers=K)
     torch.cuda.synchronize()
     barrier()
     dt_e2e = time.perf_counter() - t0
@@ -190,7 +223,7 @@ def run_ours(args, rank, world, local):
         peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
     except OSError:
         pass
-    lu_ms = stages["lu_gemm"]
+    lu_ms = stages["lu_gemm"]  # per point, worker 0, in the timed region (shares the GPU with the other workers)
     gemm_flops = 8.0 / 3.0 * n ** 3  # the trailing updates carry ~all of the LU's flops
     achieved = gemm_flops / (lu_ms * 1e-3) / 1e12 if lu_ms else None
     bf16 = peaks.get("bf16_tflops_sustained") or 1700.0
@@ -207,7 +240,7 @@ def run_ours(args, rank, world, local):
         "config": dict(WORKLOAD, precision=args.precision, l2="inputs > L2 (Z 283 MB, fill scratch 1.2 GB per step)"),
         "e2e": {"value": round(world * args.steps / dt_e2e, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
-        "stages_ms_per_step": stages, "gpu_launches": int(sum(launches.values())),
+        "workers": K, "stages_ms_per_point_worker0": stages, "gpu_launches": int(launches),
         "fp64_ms_per_point": round(t64 * 1e3, 2) if t64 else None,
         "speedup_vs_fp64": round(t64 / (dt / args.steps), 2) if t64 else None,
         "roofline": roof, "clocks": clk.summary(), "geometry": geo,
@@ -293,6 +326,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--fp64-points", type=int, default=2)
+    ap.add_argument("--workers", type=int, default=4, help="frequency points in flight on the GPU")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     rank, world, local = dist_env()

@@ -12,6 +12,7 @@ CPU fallback; without the CUDA library or a device the constructor raises.
 
 import ctypes as C
 import os
+import threading
 import time
 from dataclasses import dataclass
 
@@ -277,9 +278,11 @@ class Solver:
             self.groups.setdefault(key, []).append(p)
         if st.lossless:
             raise ValueError("lossless stacks (bounded beta search) are not supported by this engine")
+        self.device = device
         self.ctx = E.Context(device)
         self._geom = None
         self._ports = None
+        self._siblings = []  # further engine contexts for concurrent points (sweep(workers=...))
 
     # ----------------------------------------------------------- device data
     def geometry(self):
@@ -454,10 +457,28 @@ class Solver:
         return np.array([len(freqs), float(np.sum(freqs)), float(m.n_unknowns), float(np.sum(m.nodes)),
                          float(np.sum(m.nodes ** 2)), float(len(m.tris)), 0.0])
 
-    def sweep(self, freqs, keep_currents=False, interp=None, values=None, checkpoint=None, wait_memory=None):
+    def _sibling(self, i):
+        """Worker i of a concurrent sweep (0: this solver): the same mesh,
+        stack and settings on its own engine context (stream, device data)."""
+        if i == 0:
+            return self
+        while len(self._siblings) < i:
+            s = Solver(self.mesh, self.sub, z0=self.z0_fixed, verbose=False, precision=self.precision,
+                       device=self.device, refine_tol=self.refine_tol, max_refine=self.max_refine,
+                       v_weight=self.v_weight)
+            self._siblings.append(s)
+        return self._siblings[i - 1]
+
+    def sweep(self, freqs, keep_currents=False, interp=None, values=None, checkpoint=None, wait_memory=None,
+              workers=1):
         """S-parameters at freqs (exact fill at every frequency). checkpoint:
         an .npz rewritten atomically after every frequency; a restarted sweep
-        with the same frequencies and mesh resumes from it."""
+        with the same frequencies and mesh resumes from it. workers: frequency
+        points in flight at once on this GPU, each on its own engine context
+        and stream, driven by its own host thread (the latency-bound stages of
+        one point - LU panels, triangular solves, the wave fit - leave most of
+        the GPU to the others); points are handed out in order as workers
+        become free."""
         if interp not in (None, "auto"):
             raise ValueError("this engine fills every frequency exactly (interp=None)")
         freqs = np.atleast_1d(np.asarray(freqs, float))
@@ -481,26 +502,61 @@ class Solver:
                 if self.verbose:
                     print(f" checkpoint: unreadable ({exc}); starting afresh", flush=True)
                 done[:] = False
-        steps = []
+        steps = [None] * nf
+        todo = [fi for fi in range(nf) if not done[fi]]
+        workers = max(1, min(int(workers), len(todo) or 1))
+        lock = threading.Lock()
+        nxt = [0]
+        errors = []
+
+        def work(w):
+            sol = self._sibling(w)
+            while True:
+                with lock:
+                    if errors or nxt[0] >= len(todo):
+                        return
+                    fi = todo[nxt[0]]
+                    nxt[0] += 1
+                try:
+                    out = sol.point(freqs[fi], keep_currents)
+                except Exception as exc:  # noqa: BLE001 - re-raised below in the caller's thread
+                    with lock:
+                        errors.append(exc)
+                    return
+                with lock:
+                    S[fi], zr[fi], gam[fi], zl[fi], res[fi], cur[fi], inf = out
+                    steps[fi] = inf["refine_steps"]
+                    done[fi] = True
+                    if self.verbose:
+                        print(f"PROGRESS {int(done.sum())}/{nf}", flush=True)
+                    if checkpoint:
+                        tmp = checkpoint + ".tmp.npz"
+                        np.savez(tmp, key=key, done=done, S=S, gam=gam, zl=zl, zr=zr, res=res)
+                        os.replace(tmp, checkpoint)
+
         t0 = time.time()
-        for fi, f in enumerate(freqs):
-            if done[fi]:
-                continue
-            S[fi], zr[fi], gam[fi], zl[fi], res[fi], x, inf = self.point(f, keep_currents)
-            steps.append(inf["refine_steps"])
-            cur[fi] = x
-            done[fi] = True
-            if self.verbose:
-                print(f"PROGRESS {int(done.sum())}/{nf}", flush=True)
-            if checkpoint:
-                tmp = checkpoint + ".tmp.npz"
-                np.savez(tmp, key=key, done=done, S=S, gam=gam, zl=zl, zr=zr, res=res)
-                os.replace(tmp, checkpoint)
-        info = dict(seconds=time.time() - t0, refine_steps=steps)
+        for w in range(1, workers):  # set up the contexts before the points start
+            sib = self._sibling(w)
+            sib.geometry()
+            sib.port_data()
+        if workers == 1:
+            work(0)
+        else:
+            th = [threading.Thread(target=work, args=(w,)) for w in range(workers)]
+            for t in th:
+                t.start()
+            for t in th:
+                t.join()
+        if errors:
+            raise errors[0]
+        info = dict(seconds=time.time() - t0, refine_steps=[s for s in steps if s is not None], workers=workers)
         return SweepResult(freqs, S, zr, gam, zl, res, [p.name for p in self.ports],
                            cur if keep_currents else None, info)
 
     def close(self):
+        for sib in self._siblings:
+            sib.close()
+        self._siblings = []
         for h in (self._ports, self._geom):
             if h is not None:
                 h.close()

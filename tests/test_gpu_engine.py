@@ -312,3 +312,20 @@ def test_lu_complex64_tensor_cores_reconstruct(gpu, n):
     print("P L U - A, tensor cores / SIMT:", errs)
     assert errs[0] <= 16 * errs[E.M25_LU_NO_TENSOR_CORES], errs
     ctx.close()
+
+
+# ------------------------------------------------------- concurrent points
+def test_sweep_workers_match_one_worker(gpu):
+    """Points in flight on separate engine contexts give the results of the
+    one-at-a-time sweep (every stage is deterministic)."""
+    lay, st, m, freqs = build("line")
+    f = np.linspace(2e9, 14e9, 5)
+    s1 = Solver(m, st, verbose=False, precision="mixed")
+    r1 = s1.sweep(f)
+    s1.close()
+    s2 = Solver(m, st, verbose=False, precision="mixed")
+    r2 = s2.sweep(f, workers=3)
+    s2.close()
+    assert r2.info["workers"] == 3
+    for a, b in ((r1.S, r2.S), (r1.gamma, r2.gamma), (r1.z0, r2.z0), (r1.fit_residual, r2.fit_residual)):
+        np.testing.assert_allclose(a, b, rtol=1e-15, atol=0)
