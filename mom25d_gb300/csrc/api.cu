@@ -37,7 +37,8 @@ void DevBuf::release() {
 
 // fill.cu
 template <class T>
-int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, void* Z, int64_t ldz, int where);
+int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, void* Z, int64_t ldz, int where,
+                bool far32);
 
 // lu.cu
 template <class T> int lu_factor(m25_ctx*, cx<T>*, int64_t, int, int32_t*, int, bool, int*);
@@ -169,10 +170,12 @@ extern "C" int m25_assemble(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, double
     return M25_ERR_VALUE;
   }
   M25_CUDA(cudaSetDevice(ctx->device));
+  // M25_MIXED: complex128 Z with the far pairs evaluated in fp32 (near / mid in fp64)
   if (precision == M25_FP64 || precision == M25_MIXED)
-    return fill_driver<double>(ctx, geom, gr, zd(zs_re, zs_im), zd(zsv_re, zsv_im), Z, ldz, where);
+    return fill_driver<double>(ctx, geom, gr, zd(zs_re, zs_im), zd(zsv_re, zsv_im), Z, ldz, where,
+                               precision == M25_MIXED);
   if (precision == M25_MIXED_FILL32)
-    return fill_driver<float>(ctx, geom, gr, zd(zs_re, zs_im), zd(zsv_re, zsv_im), Z, ldz, where);
+    return fill_driver<float>(ctx, geom, gr, zd(zs_re, zs_im), zd(zsv_re, zsv_im), Z, ldz, where, false);
   set_error("m25_assemble: unknown precision");
   return M25_ERR_VALUE;
 }

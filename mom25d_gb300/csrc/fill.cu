@@ -43,6 +43,12 @@ struct FillArgs {
   cx<T>* H;            // (3 nt, ldh)
   int64_t ldh;
   cx<T>* IVpad;        // (npad, nt)
+  // fp32 copies for far pairs evaluated in fp32 (fill_tri_kernel<double, true>)
+  const TriData<float>* td32;
+  const float* coef32;
+  cx<float> lead32[kMaxLevSq][2];
+  float dz32[kMaxLevSq];
+  cx<float> jwmu32, inv_jwe32;
 };
 
 // scipy PPoly interval: x[i] <= r < x[i+1], clamped to the end intervals.
@@ -98,7 +104,7 @@ __device__ __forceinline__ void spline_av(const T* __restrict__ xs, const float*
 }
 
 template <class T, int NQ, bool NEAR>
-__device__ __forceinline__ void source_pass(const FillArgs<T>& a, const TriData<T>& S, T dcx, T dcy,
+__device__ __forceinline__ void source_pass(int nrho, const TriData<T>& S, T dcx, T dcy,
                                             const T (&tq)[7][2], const T (&tw)[7], const T* xs, const float* xf,
                                             const T* tab,
                                             cx<T> cA, cx<T> cV, T dz, const T* st, int lane, cx<T> (&Q)[3],
@@ -148,7 +154,7 @@ __device__ __forceinline__ void source_pass(const FillArgs<T>& a, const TriData<
         inv = inv4pi * (dz == T(0) ? ri : rsqrt(R2 + dz * dz));
       }
       cx<T> sa, sv;
-      spline_av(xs, xf, tab, a.nrho, R, sa, sv);
+      spline_av(xs, xf, tab, nrho, R, sa, sv);
       if (!NEAR) {
         sa += cA * inv;
         sv += cV * inv;
@@ -182,7 +188,37 @@ __device__ __forceinline__ void source_pass(const FillArgs<T>& a, const TriData<
   }
 }
 
+// IA[i][j] = Q_i - (b_j - c_s) . P_i ; vals = jw mu cA cA IA + inv_jwe cV cV IV,
+// with the test triangle's factors jw mu cA_i, inv_jwe cV_i applied to Q, P
+// and IV once per i instead of once per (i, j)
 template <class T>
+__device__ __forceinline__ void pair_block(const TriData<T>& S, const T (&tcA)[3], const T (&tcV)[3], cx<T> jwmu,
+                                           cx<T> inv_jwe, const cx<T> (&Q)[3], const cx<T> (&Px)[3],
+                                           const cx<T> (&Py)[3], cx<T> IV, cx<T> (&out)[3][3]) {
+  T scA[3], scV[3], bx[3], by[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    scA[j] = S.cA[j];
+    scV[j] = S.cV[j];
+    bx[j] = S.v[j][0];
+    by[j] = S.v[j][1];
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const cx<T> ja = jwmu * tcA[i], jv = inv_jwe * tcV[i];
+    const cx<T> JQ = ja * Q[i], JPx = ja * Px[i], JPy = ja * Py[i], JV = jv * IV;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) out[i][j] = (JQ - (JPx * bx[j] + JPy * by[j])) * scA[j] + JV * scV[j];
+  }
+}
+
+// FAR32 (T = double, the mixed precision): far pairs (one-point source rule)
+// are evaluated in fp32 - interval search, spline, leading term, test-point
+// sums and the 3x3 block - from fp32 copies of the tables and triangle data;
+// near and mid pairs stay in fp64. The far pairs are ~60 % of the fill's work
+// and carry small, smooth interactions: in the mixed path's error budget
+// (S within 1e-5 of mom25d) their fp32 rounding moves S by ~1e-7.
+template <class T, bool FAR32>
 __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
@@ -192,6 +228,7 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
   T* xs = reinterpret_cast<T*>(smem_raw);
   T* tabs = xs + ((n + 3) & ~3);
   float* xf = reinterpret_cast<float*>(tabs + (size_t)L * (n - 1) * 16);  // radii rounded to fp32
+  float* tabs32 = xf + ((n + 3) & ~3);  // FAR32: fp32 tables, same layout as tabs
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     xs[i] = a.rho[i];
     xf[i] = (float)a.rho[i];
@@ -212,6 +249,16 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
         cx<T> v = src[((size_t)iv * 4 + p) * 3 + which];
         dst[(size_t)iv * 16 + p * 4 + which * 2] = v.re;
         dst[(size_t)iv * 16 + p * 4 + which * 2 + 1] = v.im;
+      }
+      if (FAR32) {
+        const cx<float>* src32 = reinterpret_cast<const cx<float>*>(a.coef32) + (size_t)(lt * L + ls) * (n - 1) * 12;
+        float* dst32 = tabs32 + (size_t)ls * (n - 1) * 16;
+        for (int e = threadIdx.x; e < (n - 1) * 8; e += blockDim.x) {
+          int iv = e >> 3, r = e & 7, p = r >> 1, which = r & 1;
+          cx<float> v = src32[((size_t)iv * 4 + p) * 3 + which];
+          dst32[(size_t)iv * 16 + p * 4 + which * 2] = v.re;
+          dst32[(size_t)iv * 16 + p * 4 + which * 2 + 1] = v.im;
+        }
       }
     }
     __syncthreads();
@@ -254,31 +301,45 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
     const T dz = a.dz[lt * L + ls];
     cx<T> Q[3], Px[3], Py[3], IV;
     if (code >= 0) {
-      source_pass<T, 7, true>(a, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, a.stat + (int64_t)code * 672, lane, Q,
+      source_pass<T, 7, true>(n, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, a.stat + (int64_t)code * 672, lane, Q,
                               Px, Py, IV, tv);
     } else if (code == -1) {
-      source_pass<T, 3, false>(a, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, nullptr, lane, Q, Px, Py, IV, tv);
-    } else {
-      source_pass<T, 1, false>(a, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, nullptr, lane, Q, Px, Py, IV, tv);
+      source_pass<T, 3, false>(n, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, nullptr, lane, Q, Px, Py, IV, tv);
     }
-    // IA[i][j] = Q_i - (b_j - c_s) . P_i ; vals = jw mu cA cA IA + inv_jwe cV cV IV,
-    // with the test triangle's factors jw mu cA_i, inv_jwe cV_i applied to
-    // Q, P and IV once per i instead of once per (i, j)
     cx<T> out[3][3];
-    T scA[3], scV[3], bx[3], by[3];
+    if (FAR32 && code < -1) {
+      // far pair in fp32 (test data re-read from the fp32 copy, L1-resident)
+      const TriData<float>& A32 = a.td32[tt];
+      const TriData<float>& S32 = a.td32[s];
+      float tq32[7][2], tw32[7], tv32[3][2], tcA32[3], tcV32[3];
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      scA[j] = S.cA[j];
-      scV[j] = S.cV[j];
-      bx[j] = S.v[j][0];
-      by[j] = S.v[j][1];
-    }
+      for (int k = 0; k < 7; ++k) {
+        tq32[k][0] = A32.q7[k][0];
+        tq32[k][1] = A32.q7[k][1];
+        tw32[k] = A32.w7[k];
+      }
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      const cx<T> ja = a.jwmu * tcA[i], jv = a.inv_jwe * tcV[i];
-      const cx<T> JQ = ja * Q[i], JPx = ja * Px[i], JPy = ja * Py[i], JV = jv * IV;
+      for (int i = 0; i < 3; ++i) {
+        tv32[i][0] = A32.v[i][0];
+        tv32[i][1] = A32.v[i][1];
+        tcA32[i] = A32.cA[i];
+        tcV32[i] = A32.cV[i];
+      }
+      cx<float> Qf[3], Pxf[3], Pyf[3], IVf, outf[3][3];
+      source_pass<float, 1, false>(n, S32, (float)dcx, (float)dcy, tq32, tw32, xf, xf,
+                                   tabs32 + (size_t)ls * (n - 1) * 16, a.lead32[lt * L + ls][0],
+                                   a.lead32[lt * L + ls][1], a.dz32[lt * L + ls], nullptr, lane, Qf, Pxf, Pyf, IVf,
+                                   tv32);
+      pair_block<float>(S32, tcA32, tcV32, a.jwmu32, a.inv_jwe32, Qf, Pxf, Pyf, IVf, outf);
 #pragma unroll
-      for (int j = 0; j < 3; ++j) out[i][j] = (JQ - (JPx * bx[j] + JPy * by[j])) * scA[j] + JV * scV[j];
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) out[i][j] = cx<T>(outf[i][j]);
+      IV = cx<T>(IVf);
+    } else {
+      if (code < -1)
+        source_pass<T, 1, false>(n, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, nullptr, lane, Q, Px, Py, IV, tv);
+      pair_block<T>(S, tcA, tcV, a.jwmu, a.inv_jwe, Q, Px, Py, IV, out);
     }
     if (active && s == t && (a.zs.re != T(0) || a.zs.im != T(0))) {
       // conductor loss: Zs Int_T (r - a_i).(r - a_j) dS cA_i cA_j
@@ -446,7 +507,8 @@ __global__ void im_gv0_kernel(int L, int nrho, const double* __restrict__ rho, c
 
 // Stage 1 + 2 + 3 on the context's stream; Z is host or device memory.
 template <class T>
-int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, void* Zout, int64_t ldz, int where) {
+int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, void* Zout, int64_t ldz, int where,
+                bool far32) {
   cudaStream_t st = ctx->stream;
   const int nt = geom->nt, nb = geom->nb, nv = geom->nv, L = geom->nlev, n = nb + nv;
   const int nrho = gr->nrho;
@@ -499,14 +561,27 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   a.H = H;
   a.ldh = ldh;
   a.IVpad = IVpad;
-  size_t smem = sizeof(T) * (((nrho + 3) & ~3) + (size_t)L * (nrho - 1) * 16) + sizeof(float) * nrho;
+  const bool f32 = far32 && std::is_same<T, double>::value;
+  a.td32 = geom->td32;
+  a.coef32 = gr->coef32;
+  for (int p = 0; p < L * L; ++p) {
+    zd ca = gr->lead_h[0 * L * L + p], cv = gr->lead_h[1 * L * L + p];
+    a.lead32[p][0] = cx<float>(float(ca.re), float(ca.im));
+    a.lead32[p][1] = cx<float>(float(cv.re), float(cv.im));
+    a.dz32[p] = float(gr->dz_h[p]);
+  }
+  a.jwmu32 = cx<float>(float(jwmu.re), float(jwmu.im));
+  a.inv_jwe32 = cx<float>(float(inv_jwe.re), float(inv_jwe.im));
+  size_t smem = sizeof(T) * (((nrho + 3) & ~3) + (size_t)L * (nrho - 1) * 16) +
+                sizeof(float) * (((nrho + 3) & ~3) + (f32 ? (size_t)L * (nrho - 1) * 16 : 0));
   if (smem > 220 * 1024) {
     set_error("m25_assemble: Green's tables too large for shared memory (reduce rho_max or levels)");
     return M25_ERR_VALUE;
   }
-  M25_CUDA(cudaFuncSetAttribute(fill_tri_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  auto kern = f32 ? fill_tri_kernel<T, true> : fill_tri_kernel<T, false>;
+  M25_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int occ = 1;
-  M25_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fill_tri_kernel<T>, 256, smem));
+  M25_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, smem));
   // persistent grid (a whole number of waves); ~16 work items per CTA of at
   // least 64 sources each keep the round-robin tail short
   const int grid = std::max(1, occ) * ctx->num_sms;
@@ -517,7 +592,7 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   if (nv) M25_CUDA(cudaMemsetAsync(IVpad, 0, sizeof(cx<T>) * (size_t)geom->npad * nt, st));
   {
     StageTimer tm(ctx, ST_FILL);
-    fill_tri_kernel<T><<<std::min(grid, geom->nblocks * nchunk), 256, smem, st>>>(a);
+    kern<<<std::min(grid, geom->nblocks * nchunk), 256, smem, st>>>(a);
   }
   M25_CHECK_LAUNCH();
   {
@@ -560,7 +635,7 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   return M25_OK;
 }
 
-template int fill_driver<double>(m25_ctx*, m25_geom*, m25_greens*, zd, zd, void*, int64_t, int);
-template int fill_driver<float>(m25_ctx*, m25_geom*, m25_greens*, zd, zd, void*, int64_t, int);
+template int fill_driver<double>(m25_ctx*, m25_geom*, m25_greens*, zd, zd, void*, int64_t, int, bool);
+template int fill_driver<float>(m25_ctx*, m25_geom*, m25_greens*, zd, zd, void*, int64_t, int, bool);
 
 }  // namespace m25

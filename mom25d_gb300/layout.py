@@ -400,10 +400,16 @@ class Mesh:
     def cut_edges(self, port, s):
         """RWG edges on the transverse cut at distance s of a feed, signed so
         that positive current flows toward the circuit."""
-        es, _ = port.local(self.nodes[self.edge_nodes])
-        _, tm = port.local(self.edge_mid)
+        # the edges' coordinates in the port frame do not depend on s: once per port
+        cache = self.__dict__.setdefault("_cut_frames", {})
+        key = id(port)
+        if key not in cache or cache[key][0] is not port:
+            es, _ = port.local(self.nodes[self.edge_nodes])
+            _, tm = port.local(self.edge_mid)
+            cand = (np.abs(tm) < port.width / 2) & (self.edge_layer == self.layer_names.index(port.layer))
+            idx = np.nonzero(cand)[0]
+            cache[key] = (port, es[idx], idx, np.sign(self.flow_direction()[idx] @ -port.u))
+        _, es, idx, sign = cache[key]
         tol = 1e-6 * port.width
-        on = (np.abs(es[:, 0] - s) < tol) & (np.abs(es[:, 1] - s) < tol) & (np.abs(tm) < port.width / 2)
-        on &= self.edge_layer == self.layer_names.index(port.layer)
-        idx = np.nonzero(on)[0]
-        return idx, np.sign(self.flow_direction()[idx] @ -port.u)
+        on = (np.abs(es[:, 0] - s) < tol) & (np.abs(es[:, 1] - s) < tol)
+        return idx[on], sign[on]

@@ -283,6 +283,8 @@ class Solver:
         self._geom = None
         self._ports = None
         self._siblings = []  # further engine contexts for concurrent points (sweep(workers=...))
+        self._sib_lock = threading.Lock()
+        self._blocks_host = None  # test blocks (host), shared with the siblings
 
     # ----------------------------------------------------------- device data
     def geometry(self):
@@ -290,7 +292,9 @@ class Solver:
         if self._geom is not None:
             return self._geom
         m, st = self.mesh, self.stack
-        blocks = test_blocks(m)
+        if self._blocks_host is None:
+            self._blocks_host = test_blocks(m)
+        blocks = self._blocks_host
         nt, nb = len(m.tris), m.n_basis
         segs = m.via_segments
         nv = len(segs)
@@ -457,17 +461,32 @@ class Solver:
         return np.array([len(freqs), float(np.sum(freqs)), float(m.n_unknowns), float(np.sum(m.nodes)),
                          float(np.sum(m.nodes ** 2)), float(len(m.tris)), 0.0])
 
+    _DEVICE_STATE = ("ctx", "_geom", "_ports", "_siblings", "_sib_lock")
+
+    def _clone(self):
+        """A solver sharing this one's host-side set-up (mesh, port models,
+        groups, test blocks) with a fresh engine context of its own."""
+        s = object.__new__(Solver)
+        s.__dict__.update({k: v for k, v in self.__dict__.items() if k not in self._DEVICE_STATE})
+        s.verbose = False
+        s.ctx = E.Context(self.device)
+        s._geom = None
+        s._ports = None
+        s._siblings = []
+        s._sib_lock = threading.Lock()
+        return s
+
     def _sibling(self, i):
         """Worker i of a concurrent sweep (0: this solver): the same mesh,
         stack and settings on its own engine context (stream, device data)."""
         if i == 0:
             return self
-        while len(self._siblings) < i:
-            s = Solver(self.mesh, self.sub, z0=self.z0_fixed, verbose=False, precision=self.precision,
-                       device=self.device, refine_tol=self.refine_tol, max_refine=self.max_refine,
-                       v_weight=self.v_weight)
-            self._siblings.append(s)
-        return self._siblings[i - 1]
+        if self._blocks_host is None:
+            self._blocks_host = test_blocks(self.mesh)
+        with self._sib_lock:
+            while len(self._siblings) < i:
+                self._siblings.append(self._clone())
+            return self._siblings[i - 1]
 
     def sweep(self, freqs, keep_currents=False, interp=None, values=None, checkpoint=None, wait_memory=None,
               workers=1):
@@ -510,7 +529,14 @@ class Solver:
         errors = []
 
         def work(w):
-            sol = self._sibling(w)
+            try:  # each worker sets up its own context's device data
+                sol = self._sibling(w)
+                sol.geometry()
+                sol.port_data()
+            except Exception as exc:  # noqa: BLE001 - re-raised below in the caller's thread
+                with lock:
+                    errors.append(exc)
+                return
             while True:
                 with lock:
                     if errors or nxt[0] >= len(todo):
@@ -535,10 +561,6 @@ class Solver:
                         os.replace(tmp, checkpoint)
 
         t0 = time.time()
-        for w in range(1, workers):  # set up the contexts before the points start
-            sib = self._sibling(w)
-            sib.geometry()
-            sib.port_data()
         if workers == 1:
             work(0)
         else:

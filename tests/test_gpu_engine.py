@@ -130,6 +130,18 @@ def test_fill_mixed_close_to_fp64(line):
     assert np.abs(Z32 - Z64).max() <= 3e-6 * np.abs(Z64).max()
 
 
+def test_fill_mixed_far_pairs_in_fp32(line):
+    """precision 'mixed' fills near and mid pairs in fp64 and the far pairs in
+    fp32: a complex128 Z within 1e-6 of the fp64 fill (relative to max |Z|)."""
+    sol, _ = line
+    for f in (2e9, 7e9):
+        Z64 = sol.impedance(f, precision="fp64")
+        Zm = sol.impedance(f, precision="mixed")
+        assert Zm.dtype == np.complex128
+        err = np.abs(Zm - Z64).max() / np.abs(Z64).max()
+        assert 0 < err < 1e-6, err
+
+
 # ----------------------------------------------------------------------- solve
 @pytest.mark.parametrize("n", [1, 2, 63, 65, 130, 700])
 def test_dense_solve_fp64_vs_lapack(gpu, n):
