@@ -42,9 +42,9 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
 
 // lu.cu
 template <class T> int lu_factor(m25_ctx*, cx<T>*, int64_t, int, int32_t*, int, bool, int*);
-int refine(m25_ctx*, int, int, const zf*, const zf*, int64_t, const zf*, const int32_t*, const zd*, zd*, double, int,
-           int*);
-void split_to_z32(m25_ctx*, const zd*, int64_t, zf*, zf*, zf*, int64_t, int, int);
+int refine(m25_ctx*, int, int, const zf*, const zf*, int64_t, const zf*, int64_t, const int32_t*, const zd*, zd*,
+           double, int, int*);
+void split_to_z32(m25_ctx*, const zd*, int64_t, zf*, int64_t, zf*, zf*, int64_t, int, int);
 bool lu_tc_available();
 template <class TF, class TV>
 int lu_solve_wave(m25_ctx*, const cx<TF>*, int64_t, int, const int32_t*, const cx<TV>*, int, cx<TV>*,
@@ -248,7 +248,9 @@ extern "C" int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precis
     if ((rc = lu_solve_wave<double, double>(ctx, Zd, n, n, ctx->ipiv.as<int32_t>(), Bd, nrhs, Xd))) return rc;
   } else if (precision == M25_MIXED || precision == M25_MIXED_FILL32) {
     // M25_MIXED: Z complex128 (cast for the LU); M25_MIXED_FILL32: Z is the complex64 fill
-    if ((rc = ctx->Zlu.ensure(sizeof(zf) * nn))) return rc;
+    // the LU's rows padded to an even length (16-byte rows for the tensor-core update's TMA)
+    const int64_t ldl = (n + 1) & ~1;
+    if ((rc = ctx->Zlu.ensure(sizeof(zf) * (size_t)n * ldl))) return rc;
     zf* LU = ctx->Zlu.as<zf>();
     const void* Zres = Z;
     if (where == M25_ON_HOST) {
@@ -262,22 +264,23 @@ extern "C" int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precis
     const zf* Zh = static_cast<const zf*>(Zres);
     const zf* Zl = nullptr;
     if (precision == M25_MIXED_FILL32) {
-      M25_CUDA(cudaMemcpyAsync(LU, Zres, sizeof(zf) * nn, cudaMemcpyDeviceToDevice, st));
+      M25_CUDA(cudaMemcpy2DAsync(LU, sizeof(zf) * ldl, Zres, sizeof(zf) * n, sizeof(zf) * n, n,
+                                 cudaMemcpyDeviceToDevice, st));
     } else {
       if ((rc = ctx->Zsplit.ensure(sizeof(zf) * 2 * nn))) return rc;
       zf* h = ctx->Zsplit.as<zf>();
-      split_to_z32(ctx, static_cast<const zd*>(Zres), n, LU, h, h + nn, n, n, n);
+      split_to_z32(ctx, static_cast<const zd*>(Zres), n, LU, ldl, h, h + nn, n, n, n);
       Zh = h;
       Zl = h + nn;
     }
-    if ((rc = lu_factor<float>(ctx, LU, n, n, ctx->ipiv.as<int32_t>(), kPanelZ64, lu_tc_available(), &zinfo)))
+    if ((rc = lu_factor<float>(ctx, LU, ldl, n, ctx->ipiv.as<int32_t>(), kPanelZ64, lu_tc_available(), &zinfo)))
       return rc;
     if (zinfo) {
       if (info) { info[0] = 0; info[1] = zinfo; }
       set_error("m25_dense_solve: zero pivot in the complex64 LU");
       return M25_ERR_NUMERIC;
     }
-    rc = refine(ctx, n, nrhs, Zh, Zl, n, LU, ctx->ipiv.as<int32_t>(), Bd, Xd, tol, max_iter, &steps);
+    rc = refine(ctx, n, nrhs, Zh, Zl, n, LU, ldl, ctx->ipiv.as<int32_t>(), Bd, Xd, tol, max_iter, &steps);
     if (rc) return rc;
   } else {
     set_error("m25_dense_solve: unknown precision");

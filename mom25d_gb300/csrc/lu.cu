@@ -663,6 +663,9 @@ bool lu_tc_available();
 template <class T>
 int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb, bool use_tc, int* info_host) {
   cudaStream_t st = ctx->stream;
+  // the tensor-core update reduces into C through a TMA tensor map: rows of
+  // a multiple of 16 bytes and a 16-byte aligned matrix (else SIMT updates)
+  use_tc = use_tc && lda % 2 == 0 && reinterpret_cast<uintptr_t>(A) % 16 == 0 && nb % 2 == 0;
   // panel workspace
   int bps_max = 0;
   size_t panel_smem = 0;
@@ -1378,16 +1381,16 @@ __global__ void split_z64_kernel(int64_t n, const zd* __restrict__ X, zf* __rest
 }
 
 // the same for an n x m block of a matrix (leading dimensions lda / ldb),
-// also writing the hi plane to a second destination (the LU's input)
-__global__ void split_matrix_kernel(const zd* __restrict__ a, int64_t lda, zf* __restrict__ lu, zf* __restrict__ h,
-                                    zf* __restrict__ l, int64_t ldb, int n, int m) {
+// also writing the hi plane to a second destination (the LU's input, ldlu)
+__global__ void split_matrix_kernel(const zd* __restrict__ a, int64_t lda, zf* __restrict__ lu, int64_t ldlu,
+                                    zf* __restrict__ h, zf* __restrict__ l, int64_t ldb, int n, int m) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (int64_t)n * m) return;
   const int64_t r = e / m, c = e % m;
   const zd x = a[r * lda + c];
   const float hr = (float)x.re, hi = (float)x.im;
   const zf hv(hr, hi);
-  lu[r * ldb + c] = hv;
+  lu[r * ldlu + c] = hv;
   h[r * ldb + c] = hv;
   l[r * ldb + c] = zf((float)(x.re - (double)hr), (float)(x.im - (double)hi));
 }
@@ -1552,8 +1555,8 @@ __global__ void maxabs_kernel(int64_t n, const zd* __restrict__ a, double* __res
 // Zl absent when Z is itself complex64). Stops when the normwise backward
 // error |r| / (|Z| |x| + |b|) of every column <= tol; max_iter bounds the
 // total number of GMRES steps.
-int refine(m25_ctx* ctx, int n, int P, const zf* Zh, const zf* Zl, int64_t ldz, const zf* LU, const int32_t* ipiv,
-           const zd* B, zd* X, double tol, int max_iter, int* steps) {
+int refine(m25_ctx* ctx, int n, int P, const zf* Zh, const zf* Zl, int64_t ldz, const zf* LU, int64_t ldlu,
+           const int32_t* ipiv, const zd* B, zd* X, double tol, int max_iter, int* steps) {
   cudaStream_t st = ctx->stream;
   const int m = std::min(30, std::max(1, max_iter));
   const size_t np = (size_t)n * P;
@@ -1580,7 +1583,7 @@ int refine(m25_ctx* ctx, int n, int P, const zf* Zh, const zf* Zl, int64_t ldz, 
   auto precond = [&](const zd* in, zd* out) -> int {
     maxabs_kernel<<<1, 1024, 0, st>>>((int64_t)np, in, pscale);
     z64_to_z32_scaled<<<g1, 256, 0, st>>>((int64_t)np, in, pscale, r32);
-    int r = lu_solve_wave<float, float>(ctx, LU, n, n, ipiv, r32, P, d32, perm);
+    int r = lu_solve_wave<float, float>(ctx, LU, ldlu, n, ipiv, r32, P, d32, perm);
     if (r) return r;
     z32_to_z64_scaled<<<g1, 256, 0, st>>>((int64_t)np, d32, pscale, out);
     return M25_OK;
@@ -1724,9 +1727,10 @@ int refine(m25_ctx* ctx, int n, int P, const zf* Zh, const zf* Zl, int64_t ldz, 
 
 
 
-void split_to_z32(m25_ctx* ctx, const zd* a, int64_t lda, zf* lu, zf* h, zf* l, int64_t ldb, int n, int m) {
+void split_to_z32(m25_ctx* ctx, const zd* a, int64_t lda, zf* lu, int64_t ldlu, zf* h, zf* l, int64_t ldb, int n,
+                  int m) {
   int64_t tot = (int64_t)n * m;
-  split_matrix_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(a, lda, lu, h, l, ldb, n, m);
+  split_matrix_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(a, lda, lu, ldlu, h, l, ldb, n, m);
 }
 
 }  // namespace m25

@@ -18,16 +18,18 @@
 // at the accuracy of the SIMT one.
 //
 // Kernel (persistent, one CTA per SM, 320 threads): warp 0 issues TMA loads of
-// 128B-swizzled K-major tiles (A 128 x 32, B 192 x 32 fp32) into a 3-stage
+// 128B-swizzled K-major tiles (A 128 x 32, B 192 x 32 fp32) into a 4-stage
 // mbarrier ring; warp 1 owns the TMEM (two 128 x 192 fp32 buffers) and one
-// elected thread issues tcgen05.mma (M 128, N 192, K 8); warps 2-9 prefetch
-// the tile of C into shared memory (cp.async) when the tile starts, read the
-// chunk results with tcgen05.ld and sum them, and at the end of the tile
-// apply C -= sum in shared memory and store C with coalesced rows, so that the
-// HBM latency of the read-modify-write of C hides behind the MMAs. Every
-// mbarrier wait is bounded in iterations and wall-clock time; on a timeout
-// the CTA raises an error word, stops all roles, waits (bounded) for its TMA
-// copies and MMAs, frees its TMEM and returns.
+// elected thread issues tcgen05.mma (M 128, N 192, K 8); warps 2-9 read the
+// chunk results with tcgen05.ld and sum them, and at the end of a tile hand
+// the negated sums to the TMA as 32 x 32 blocks (128B-swizzled staging, two
+// buffers per warp) that are reduce-added into C in global memory
+// (cp.reduce.async.bulk.tensor .add), so C is never read by the SMs and the
+// update overlaps the next tile's MMAs. C's rows must be a multiple of 16
+// bytes (an even leading dimension) and C 16-byte aligned. Every mbarrier
+// wait is bounded in iterations and wall-clock time; on a timeout the CTA
+// raises an error word, stops all roles, waits (bounded) for its TMA copies
+// and MMAs, frees its TMEM and returns.
 #include <cuda.h>
 
 #include <algorithm>
@@ -40,12 +42,12 @@ namespace m25 {
 
 namespace {
 
-constexpr int kBM = 128, kBN = 192, kBK = 32, kStages = 3;
+constexpr int kBM = 128, kBN = 192, kBK = 32, kStages = 4;
 constexpr int kTmemCols = 512, kBufStride = 256;  // two accumulators, 256 columns apart
 constexpr int kTileA = kBM * kBK * 4, kTileB = kBN * kBK * 4, kStageBytes = kTileA + kTileB;
 constexpr int kEpiWarps = 8, kThreads = 64 + 32 * kEpiWarps;
-constexpr int kCTileBytes = kBM * kBN * 4;  // the tile of C, prefetched while the MMAs run
-constexpr int kSmemBytes = kStages * kStageBytes + kCTileBytes + 1024;
+constexpr int kOutBlock = 32 * 32 * 4;  // one 32 x 32 fp32 block of C, staged for the TMA reduce
+constexpr int kSmemBytes = kStages * kStageBytes + kEpiWarps * 2 * kOutBlock + 1024;
 constexpr long long kWaitLimit = 1LL << 24;
 constexpr unsigned long long kWaitNs = 200ull * 1000 * 1000;  // 200 ms wall clock per wait
 
@@ -91,6 +93,14 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
+// C += tile (fp32 add) for the box at (c0, c1) of the tensor map, from shared memory
+__device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, const void* src, int c0, int c1) {
+  asm volatile(
+      "cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2}], [%3];\n" ::"l"(map),
+      "r"(c0), "r"(c1), "r"(smem_u32(src))
+      : "memory");
+}
+
 // shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   uint64_t d = 0;
@@ -119,9 +129,7 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 }
 
 struct TcArgs {
-  float* C;        // fp32 view of the complex matrix at the trailing block's origin
-  int64_t ldc;     // in floats
-  int M, N, K3;    // rows, real columns, packed K (multiple of 32)
+  int M, N, K3;    // rows, real columns of C (its fp32 view), packed K (multiple of 32)
   int tiles_m, ntiles;
   int chunk;       // k-blocks accumulated afresh in TMEM before the register sum
   int* err;
@@ -130,11 +138,12 @@ struct TcArgs {
 // one CTA per SM; 10 warps put three on one SM sub-partition, which caps a
 // thread at 168 registers (96 running sums per epilogue thread fit)
 __global__ void __launch_bounds__(kThreads, 1)
-    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a) {
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   const __grid_constant__ CUtensorMap tmC, TcArgs a) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-byte alignment of the swizzled tiles
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  float* ctile = reinterpret_cast<float*>(base + kStages * kStageBytes);  // [kBM][kBN], swizzled
+  float* stage_out = reinterpret_cast<float*>(base + kStages * kStageBytes);  // 2 blocks per epilogue warp
   __shared__ __align__(8) uint64_t full[kStages], empty[kStages], tfull[2], tempty[2], done;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag, n_issued, n_consumed, skip;
@@ -161,6 +170,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     asm volatile("prefetch.tensormap [%0];\n" ::"l"(&tmA) : "memory");
     asm volatile("prefetch.tensormap [%0];\n" ::"l"(&tmB) : "memory");
+    asm volatile("prefetch.tensormap [%0];\n" ::"l"(&tmC) : "memory");
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
@@ -229,30 +239,15 @@ __global__ void __launch_bounds__(kThreads, 1)
       mma_commit(&done);  // arrives once every MMA issued above has completed
     }
   } else {
-    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31, columns h * 96 .. + 95,
-    // and owns that 32 x 96 block of the C tile in shared memory. The block is
-    // stored with its columns XOR-swizzled by the row within each group of 32,
-    // so that both a row per lane and a row per warp are free of bank conflicts.
+    // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows of C), columns
+    // h * 96 .. + 95, and reduce-adds minus their sum into C by TMA, one
+    // 32 x 32 block at a time through two staging buffers
     const int q = warp & 3, h = (warp - 2) >> 2;
-    auto cidx = [&](int r, int c) { return r * kBN + ((c & ~31) | ((c & 31) ^ (r & 31))); };
-    int ch = 0;
+    float* stg = stage_out + (warp - 2) * 2 * (kOutBlock / 4);
+    int ch = 0, nout = 0;
     bool ok = true;
     for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
       const int m0 = (t % a.tiles_m) * kBM, n0 = (t / a.tiles_m) * kBN;
-      // prefetch this warp's block of C (4-byte copies: C rows need only be 8-byte aligned)
-      for (int i = 0; i < 32; ++i) {
-        const int r = q * 32 + i, row = m0 + r;
-#pragma unroll
-        for (int k = 0; k < kBN / 64; ++k) {
-          const int c = h * (kBN / 2) + k * 32 + lane;
-          if (row < a.M && n0 + c < a.N) {
-            const float* src = a.C + (int64_t)row * a.ldc + n0 + c;
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_u32(ctile + cidx(r, c))), "l"(src)
-                         : "memory");
-          }
-        }
-      }
-      asm volatile("cp.async.commit_group;\n" ::: "memory");
       float sum[kBN / 2];
 #pragma unroll
       for (int j = 0; j < kBN / 2; ++j) sum[j] = 0.f;
@@ -280,26 +275,31 @@ __global__ void __launch_bounds__(kThreads, 1)
         __syncwarp();
         if (lane == 0) mbar_arrive(&tempty[b]);
       }
-      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-      __syncwarp();
       if (!ok) break;
-      // C -= sum in shared memory (row per lane), then coalesced stores (row per warp)
-      {
-        const int r = q * 32 + lane;
 #pragma unroll
-        for (int j = 0; j < kBN / 2; ++j) ctile[cidx(r, h * (kBN / 2) + j)] -= sum[j];
-      }
-      __syncwarp();
-      for (int i = 0; i < 32; ++i) {
-        const int r = q * 32 + i, row = m0 + r;
+      for (int g = 0; g < kBN / 64; ++g, ++nout) {
+        float* sb = stg + (nout & 1) * (kOutBlock / 4);
+        // the reduce that last read this buffer (two blocks ago) has finished reading it
+        if (nout >= 2 && lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory");
+        __syncwarp();
+        // row = lane: 8 chunks of 16 bytes at the 128B-swizzle positions c ^ (row % 8)
 #pragma unroll
-        for (int k = 0; k < kBN / 64; ++k) {
-          const int c = h * (kBN / 2) + k * 32 + lane;
-          if (row < a.M && n0 + c < a.N) a.C[(int64_t)row * a.ldc + n0 + c] = ctile[cidx(r, c)];
+        for (int c4 = 0; c4 < 8; ++c4) {
+          float4 v = make_float4(-sum[g * 32 + 4 * c4], -sum[g * 32 + 4 * c4 + 1], -sum[g * 32 + 4 * c4 + 2],
+                                 -sum[g * 32 + 4 * c4 + 3]);
+          *reinterpret_cast<float4*>(sb + lane * 32 + ((c4 ^ (lane & 7)) << 2)) = v;
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // visible to the TMA
+        __syncwarp();
+        if (lane == 0) {
+          tma_reduce_add_2d(&tmC, sb, n0 + h * (kBN / 2) + g * 32, m0 + q * 32);
+          asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
         }
       }
-      __syncwarp();
     }
+    // the reduces are complete before the CTA leaves
+    if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
+    __syncwarp();
     if (!ok) *abort_v = 1;
   }
   __syncthreads();
@@ -391,14 +391,14 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-int make_map(CUtensorMap* map, const float* ptr, int rows, int cols_k, int box_rows) {
+int make_map(CUtensorMap* map, const float* ptr, int rows, int cols_k, int box_rows, int64_t ld = 0) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) {
     set_error("tensor-core LU: cuTensorMapEncodeTiled is not available");
     return M25_ERR_CUDA;
   }
   cuuint64_t dims[2] = {(cuuint64_t)cols_k, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)cols_k * sizeof(float)};
+  cuuint64_t strides[1] = {(cuuint64_t)(ld ? ld : cols_k) * sizeof(float)};
   cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(ptr), dims, strides, box, estr,
@@ -474,6 +474,14 @@ int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w) {
   int rc;
   if ((rc = make_map(&ma, A3, m, K3p, kBM))) return rc;
   if ((rc = make_map(&mb, B3, n2, K3p, kBN))) return rc;
+  // C: the fp32 view of the trailing block, rows 2 lda floats apart, 32 x 32 boxes
+  CUtensorMap mc;
+  const float* C = reinterpret_cast<const float*>(A + (int64_t)(k0 + w) * lda + k0 + w);
+  if ((lda & 1) || (reinterpret_cast<uintptr_t>(C) & 15)) {
+    set_error("tensor-core LU: C needs an even leading dimension and 16-byte alignment");
+    return M25_ERR_VALUE;
+  }
+  if ((rc = make_map(&mc, C, m, n2, 32, 2 * lda))) return rc;
   static int n_sm = 0, chunk = 0;
   if (!n_sm) {
     int dev = 0;
@@ -483,8 +491,6 @@ int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w) {
     chunk = e ? std::max(1, atoi(e)) : 2;
   }
   TcArgs ta;
-  ta.C = reinterpret_cast<float*>(A + (int64_t)(k0 + w) * lda + k0 + w);
-  ta.ldc = 2 * lda;
   ta.M = m;
   ta.N = n2;
   ta.K3 = K3p;
@@ -493,7 +499,7 @@ int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w) {
   ta.chunk = chunk;
   ta.err = err;
   M25_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
-  tc_gemm_kernel<<<std::min(ta.ntiles, n_sm), kThreads, kSmemBytes, st>>>(ma, mb, ta);
+  tc_gemm_kernel<<<std::min(ta.ntiles, n_sm), kThreads, kSmemBytes, st>>>(ma, mb, mc, ta);
   M25_CHECK_LAUNCH();
   return M25_OK;
 }
