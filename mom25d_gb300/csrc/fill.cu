@@ -212,11 +212,12 @@ __device__ __forceinline__ void pair_block(const TriData<T>& S, const T (&tcA)[3
   }
 }
 
-// FAR32 (T = double, the mixed precision): far pairs (one-point source rule)
-// are evaluated in fp32 - interval search, spline, leading term, test-point
-// sums and the 3x3 block - from fp32 copies of the tables and triangle data;
-// near and mid pairs stay in fp64. The far pairs are ~60 % of the fill's work
-// and carry small, smooth interactions: in the mixed path's error budget
+// FAR32 (T = double, the mixed precision): mid and far pairs (three- and
+// one-point source rules) are evaluated in fp32 - interval search, spline,
+// leading term, test-point sums and the 3x3 block - from fp32 copies of the
+// tables and triangle data; near pairs (with their closed-form singular
+// parts) stay in fp64. Mid and far pairs are ~70 % of the fill's work and
+// carry smooth, non-singular interactions: in the mixed path's error budget
 // (S within 1e-5 of mom25d) their fp32 rounding moves S by ~1e-7.
 template <class T, bool FAR32>
 __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
@@ -303,12 +304,12 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
     if (code >= 0) {
       source_pass<T, 7, true>(n, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, a.stat + (int64_t)code * 672, lane, Q,
                               Px, Py, IV, tv);
-    } else if (code == -1) {
+    } else if (code == -1 && !FAR32) {
       source_pass<T, 3, false>(n, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, nullptr, lane, Q, Px, Py, IV, tv);
     }
     cx<T> out[3][3];
-    if (FAR32 && code < -1) {
-      // far pair in fp32 (test data re-read from the fp32 copy, L1-resident)
+    if (FAR32 && code < 0) {
+      // mid or far pair in fp32 (test data re-read from the fp32 copy, L1-resident)
       const TriData<float>& A32 = a.td32[tt];
       const TriData<float>& S32 = a.td32[s];
       float tq32[7][2], tw32[7], tv32[3][2], tcA32[3], tcV32[3];
@@ -326,10 +327,14 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
         tcV32[i] = A32.cV[i];
       }
       cx<float> Qf[3], Pxf[3], Pyf[3], IVf, outf[3][3];
-      source_pass<float, 1, false>(n, S32, (float)dcx, (float)dcy, tq32, tw32, xf, xf,
-                                   tabs32 + (size_t)ls * (n - 1) * 16, a.lead32[lt * L + ls][0],
-                                   a.lead32[lt * L + ls][1], a.dz32[lt * L + ls], nullptr, lane, Qf, Pxf, Pyf, IVf,
-                                   tv32);
+      const float* tab32 = tabs32 + (size_t)ls * (n - 1) * 16;
+      const cx<float> cA32 = a.lead32[lt * L + ls][0], cV32 = a.lead32[lt * L + ls][1];
+      if (code == -1)
+        source_pass<float, 3, false>(n, S32, (float)dcx, (float)dcy, tq32, tw32, xf, xf, tab32, cA32, cV32,
+                                     a.dz32[lt * L + ls], nullptr, lane, Qf, Pxf, Pyf, IVf, tv32);
+      else
+        source_pass<float, 1, false>(n, S32, (float)dcx, (float)dcy, tq32, tw32, xf, xf, tab32, cA32, cV32,
+                                     a.dz32[lt * L + ls], nullptr, lane, Qf, Pxf, Pyf, IVf, tv32);
       pair_block<float>(S32, tcA32, tcV32, a.jwmu32, a.inv_jwe32, Qf, Pxf, Pyf, IVf, outf);
 #pragma unroll
       for (int i = 0; i < 3; ++i)

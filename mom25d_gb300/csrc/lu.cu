@@ -1409,11 +1409,12 @@ void matvec_df(int n, int P, const zf* Zh, const zf* Zl, int64_t ldz, const zd* 
     else                                                                                                       \
       matvec_df_kernel<PP, RR, false><<<g, 256, 0, st>>>(n, Zh, Zl, ldz, Xh, Xl, Y);                           \
   } while (0)
+  // one row per warp: enough warps in flight to cover the HBM latency of Z
   switch (P) {
-    case 1: M25_MVDF(1, 4); break;
-    case 2: M25_MVDF(2, 4); break;
-    case 3: M25_MVDF(3, 2); break;
-    case 4: M25_MVDF(4, 2); break;
+    case 1: M25_MVDF(1, 1); break;
+    case 2: M25_MVDF(2, 1); break;
+    case 3: M25_MVDF(3, 1); break;
+    case 4: M25_MVDF(4, 1); break;
     case 5: M25_MVDF(5, 1); break;
     case 6: M25_MVDF(6, 1); break;
     case 7: M25_MVDF(7, 1); break;
