@@ -188,6 +188,62 @@ __device__ __forceinline__ void source_pass(int nrho, const TriData<T>& S, T dcx
   }
 }
 
+// Near pair of the mixed precision: the closed-form singular parts (fp64,
+// precomputed per sweep) plus the smooth parts S_A, S_V, whose 7 x 7 point
+// evaluations - R, interval search, spline - and sums over the 7 source
+// points run in fp32; the sums join the singular parts and the test-point
+// accumulation in fp64. (On the oracle, near smooth parts in fp32 on top of
+// fp32 mid / far pairs leave S within 1.4e-7 of the fp64 fill.)
+template <class T>
+__device__ __forceinline__ void near_pass_mixed(int nrho, const TriData<float>& S32, T dcx, T dcy,
+                                                const T (&tq)[7][2], const T (&tw)[7], const float* xf,
+                                                const float* tab32, cx<T> cA, cx<T> cV, const T* st, int lane,
+                                                cx<T> (&Q)[3], cx<T> (&Px)[3], cx<T> (&Py)[3], cx<T>& IV,
+                                                const T (&tv)[3][2]) {
+  cx<T> S0, SX, SY, T0, T1, T2;
+  float sq[7][2], sw[7];
+#pragma unroll
+  for (int l = 0; l < 7; ++l) {
+    sq[l][0] = S32.q7[l][0];
+    sq[l][1] = S32.q7[l][1];
+    sw[l] = S32.w7[l];
+  }
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    const T s0 = st[(0 * 7 + k) * 32 + lane], s1x = st[(1 * 7 + k) * 32 + lane], s2y = st[(2 * 7 + k) * 32 + lane];
+    const float rx = (float)(dcx + tq[k][0]), ry = (float)(dcy + tq[k][1]);
+    cx<float> a0, ax, ay, v0;
+#pragma unroll
+    for (int l = 0; l < 7; ++l) {
+      const float ddx = rx - sq[l][0], ddy = ry - sq[l][1];
+      const float R = sqrtf(ddx * ddx + ddy * ddy);  // 0 for coincident points of a self pair
+      cx<float> sa, sv;
+      spline_av<float>(xf, xf, tab32, nrho, R, sa, sv);
+      const cx<float> saw = sa * sw[l];
+      a0 += saw;
+      ax += saw * sq[l][0];
+      ay += saw * sq[l][1];
+      v0 += sv * sw[l];
+    }
+    const cx<T> K0A = cA * s0 + cx<T>(a0), K1x = cA * s1x + cx<T>(ax), K1y = cA * s2y + cx<T>(ay);
+    const cx<T> K0V = cV * s0 + cx<T>(v0);
+    const T wk = tw[k], wx = wk * tq[k][0], wy = wk * tq[k][1];
+    IV += K0V * wk;
+    S0 += K0A * wk;
+    SX += K0A * wx;
+    SY += K0A * wy;
+    T1 += K1x * wk;
+    T2 += K1y * wk;
+    T0 += K1x * wx + K1y * wy;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    Px[i] = SX - S0 * tv[i][0];
+    Py[i] = SY - S0 * tv[i][1];
+    Q[i] = T0 - (T1 * tv[i][0] + T2 * tv[i][1]);
+  }
+}
+
 // IA[i][j] = Q_i - (b_j - c_s) . P_i ; vals = jw mu cA cA IA + inv_jwe cV cV IV,
 // with the test triangle's factors jw mu cA_i, inv_jwe cV_i applied to Q, P
 // and IV once per i instead of once per (i, j)
@@ -215,10 +271,10 @@ __device__ __forceinline__ void pair_block(const TriData<T>& S, const T (&tcA)[3
 // FAR32 (T = double, the mixed precision): mid and far pairs (three- and
 // one-point source rules) are evaluated in fp32 - interval search, spline,
 // leading term, test-point sums and the 3x3 block - from fp32 copies of the
-// tables and triangle data; near pairs (with their closed-form singular
-// parts) stay in fp64. Mid and far pairs are ~70 % of the fill's work and
-// carry smooth, non-singular interactions: in the mixed path's error budget
-// (S within 1e-5 of mom25d) their fp32 rounding moves S by ~1e-7.
+// tables and triangle data; near pairs keep their closed-form singular parts
+// and the accumulation in fp64 with the smooth parts in fp32
+// (near_pass_mixed). In the mixed path's error budget (S within 1e-5 of
+// mom25d) the fp32 rounding moves S by ~1e-7.
 template <class T, bool FAR32>
 __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -302,8 +358,12 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
     const T dz = a.dz[lt * L + ls];
     cx<T> Q[3], Px[3], Py[3], IV;
     if (code >= 0) {
-      source_pass<T, 7, true>(n, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, a.stat + (int64_t)code * 672, lane, Q,
-                              Px, Py, IV, tv);
+      if (FAR32)
+        near_pass_mixed<T>(n, a.td32[s], dcx, dcy, tq, tw, xf, tabs32 + (size_t)ls * (n - 1) * 16, cA, cV,
+                           a.stat + (int64_t)code * 672, lane, Q, Px, Py, IV, tv);
+      else
+        source_pass<T, 7, true>(n, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, a.stat + (int64_t)code * 672, lane,
+                                Q, Px, Py, IV, tv);
     } else if (code == -1 && !FAR32) {
       source_pass<T, 3, false>(n, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, nullptr, lane, Q, Px, Py, IV, tv);
     }

@@ -130,9 +130,10 @@ def test_fill_mixed_close_to_fp64(line):
     assert np.abs(Z32 - Z64).max() <= 3e-6 * np.abs(Z64).max()
 
 
-def test_fill_mixed_far_pairs_in_fp32(line):
-    """precision 'mixed' fills near and mid pairs in fp64 and the far pairs in
-    fp32: a complex128 Z within 1e-6 of the fp64 fill (relative to max |Z|)."""
+def test_fill_mixed_close_to_fp64_fill(line):
+    """precision 'mixed' keeps the near pairs' singular parts and sums in fp64
+    and evaluates their smooth parts and all mid / far pairs in fp32: a
+    complex128 Z within 1e-6 of the fp64 fill (relative to max |Z|)."""
     sol, _ = line
     for f in (2e9, 7e9):
         Z64 = sol.impedance(f, precision="fp64")
