@@ -83,6 +83,16 @@ extern "C" int m25_ctx_create(int device, m25_ctx** out) {
     return M25_ERR_CUDA;
   }
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  {
+    // keep the memory of freed per-frequency tables in the stream-ordered
+    // pool instead of handing it back to the driver at each synchronisation
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      uint64_t keep = 1ull << 30;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+  }
   *out = c;
   return M25_OK;
 }

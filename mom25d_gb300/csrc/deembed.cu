@@ -69,35 +69,26 @@ __device__ inline zd spline_w(const double* __restrict__ rho, int n, const zd* _
   return c[3 * 3 + 2] + c[2 * 3 + 2] * z + c[1 * 3 + 2] * z2 + c[0 * 3 + 2] * z3;
 }
 
-// phi[m][e] = (1/eps0) sum_t [sum_k w_k S_W(|p_m - r_k|) + c_W I0(t, p_m) / 4pi] q[t][e]
-__global__ void line_voltage_kernel(int nt, int P, int L, const double* __restrict__ pts,
-                                    const int32_t* __restrict__ pt_level, const double* __restrict__ cen,
-                                    const TriData<double>* __restrict__ td, const int32_t* __restrict__ tri_layer,
-                                    const double* __restrict__ level_z, int nrho, const double* __restrict__ rho,
-                                    const zd* __restrict__ coef, const zd* __restrict__ cW, const zd* __restrict__ q,
-                                    zd* __restrict__ phi) {
-  int m = blockIdx.x;
-  int li = pt_level[m];
-  double px = pts[2 * m], py = pts[2 * m + 1];
-  zd acc[kMaxPorts];
-  for (int t = threadIdx.x; t < nt; t += blockDim.x) {
-    int ls = tri_layer[t];
-    int pair = li * L + ls;
-    const TriData<double>& T = td[t];
-    double ox = px - cen[2 * t], oy = py - cen[2 * t + 1];
-    zd k0w(0.0);
-    for (int k = 0; k < 7; ++k) {
-      double dx = ox - T.q7[k][0], dy = oy - T.q7[k][1];
-      k0w += spline_w(rho, nrho, coef, pair, sqrt(dx * dx + dy * dy)) * T.w7[k];
-    }
-    zd cw = cW[pair];
-    if (cw.re != 0.0 || cw.im != 0.0) {
-      double I0, I1x, I1y;
-      potential_integrals(T.v, ox, oy, fabs(level_z[li] - level_z[ls]), I0, I1x, I1y);
-      k0w += cw * (I0 / (4.0 * kPi));
-    }
-    for (int e = 0; e < P; ++e) acc[e] += k0w * q[(int64_t)t * P + e];
+// sum_k w_k S_W(|p - r_k|) + c_W I0(t, p) / 4pi of one triangle in fp64
+// (Engine/mom25d/solver.py line voltages: 7-point smooth part plus the
+// closed-form 1/R integral)
+__device__ inline zd lv_tri64(const TriData<double>& T, double ox, double oy, double dz, int nrho,
+                              const double* __restrict__ rho, const zd* __restrict__ coef, int pair, zd cw) {
+  zd k0w(0.0);
+  for (int k = 0; k < 7; ++k) {
+    double dx = ox - T.q7[k][0], dy = oy - T.q7[k][1];
+    k0w += spline_w(rho, nrho, coef, pair, sqrt(dx * dx + dy * dy)) * T.w7[k];
   }
+  if (cw.re != 0.0 || cw.im != 0.0) {
+    double I0, I1x, I1y;
+    potential_integrals(T.v, ox, oy, dz, I0, I1x, I1y);
+    k0w += cw * (I0 / (4.0 * kPi));
+  }
+  return k0w;
+}
+
+// sum of the per-port accumulators over the CTA, times 1/eps0, into phi[m]
+__device__ inline void lv_reduce(int P, zd* acc, zd* __restrict__ phi_m) {
   __shared__ double red[32][2];
   const double ie0 = 1.0 / eps0();
   for (int e = 0; e < P; ++e) {
@@ -117,10 +108,116 @@ __global__ void line_voltage_kernel(int nt, int P, int L, const double* __restri
         sa += red[w][0];
         sb += red[w][1];
       }
-      phi[(int64_t)m * P + e] = zd(sa, sb) * ie0;
+      phi_m[e] = zd(sa, sb) * ie0;
     }
     __syncthreads();
   }
+}
+
+// phi[m][e] = (1/eps0) sum_t [sum_k w_k S_W(|p_m - r_k|) + c_W I0(t, p_m) / 4pi] q[t][e]
+__global__ void line_voltage_kernel(int nt, int P, int L, const double* __restrict__ pts,
+                                    const int32_t* __restrict__ pt_level, const double* __restrict__ cen,
+                                    const TriData<double>* __restrict__ td, const int32_t* __restrict__ tri_layer,
+                                    const double* __restrict__ level_z, int nrho, const double* __restrict__ rho,
+                                    const zd* __restrict__ coef, const zd* __restrict__ cW, const zd* __restrict__ q,
+                                    zd* __restrict__ phi) {
+  int m = blockIdx.x;
+  int li = pt_level[m];
+  double px = pts[2 * m], py = pts[2 * m + 1];
+  zd acc[kMaxPorts];
+  for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+    int ls = tri_layer[t];
+    int pair = li * L + ls;
+    zd k0w = lv_tri64(td[t], px - cen[2 * t], py - cen[2 * t + 1], fabs(level_z[li] - level_z[ls]), nrho, rho, coef,
+                      pair, cW[pair]);
+    for (int e = 0; e < P; ++e) acc[e] += k0w * q[(int64_t)t * P + e];
+  }
+  lv_reduce(P, acc, phi + (int64_t)m * P);
+}
+
+// Mixed precision: a (point, triangle) pair at least kLvFarEdges longest
+// edges apart is summed in fp32 from the fp32 tables, with the 1/R part of
+// the W kernel integrated by the same 7-point rule instead of in closed form
+// (relative error of the rule below 1e-7 at that distance, under the fp32
+// rounding of the rest); nearer pairs as line_voltage_kernel. The products
+// with the charges and the sums over triangles stay in fp64.
+constexpr float kLvFarEdges = 5.0f;
+
+__host__ __device__ inline size_t lv_mixed_smem(int L, int nrho) {
+  return sizeof(float) * (((size_t)nrho + 3) / 4 * 4 + (size_t)L * (nrho - 1) * 8);
+}
+
+__global__ void __launch_bounds__(256) line_voltage_mixed_kernel(
+    int nt, int P, int L, const double* __restrict__ pts, const int32_t* __restrict__ pt_level,
+    const double* __restrict__ cen, const TriData<double>* __restrict__ td, const TriData<float>* __restrict__ td32,
+    const int32_t* __restrict__ tri_layer, const double* __restrict__ level_z, int nrho, const double* __restrict__ rho,
+    const float* __restrict__ rho32, const zd* __restrict__ coef, const zf* __restrict__ coef32,
+    const zd* __restrict__ cW, const zd* __restrict__ q, zd* __restrict__ phi) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* xf = reinterpret_cast<float*>(smem_raw);
+  float* tab = xf + (nrho + 3) / 4 * 4;  // [ls][interval][power 0..3][re, im] of S_W
+  const int m = blockIdx.x;
+  const int li = pt_level[m];
+  const int ni = nrho - 1;
+  for (int i = threadIdx.x; i < nrho; i += blockDim.x) xf[i] = rho32[i];
+  for (int e = threadIdx.x; e < L * ni * 4; e += blockDim.x) {
+    const int ls = e / (ni * 4), r = e - ls * ni * 4, iv = r >> 2, pw = r & 3;
+    const zf v = coef32[(((size_t)(li * L + ls) * ni + iv) * 4 + pw) * 3 + 2];
+    tab[(size_t)e * 2] = v.re;
+    tab[(size_t)e * 2 + 1] = v.im;
+  }
+  __syncthreads();
+  const double px = pts[2 * m], py = pts[2 * m + 1];
+  zd acc[kMaxPorts];
+  for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+    const int ls = tri_layer[t];
+    const int pair = li * L + ls;
+    const double ox = px - cen[2 * t], oy = py - cen[2 * t + 1];
+    const double dz = fabs(level_z[li] - level_z[ls]);
+    const zd cw = cW[pair];
+    const TriData<float>& T = td32[t];
+    const float ox32 = (float)ox, oy32 = (float)oy, far = kLvFarEdges * T.size;
+    zd k0w;
+    if (ox32 * ox32 + oy32 * oy32 >= far * far) {
+      const float* tb = tab + (size_t)ls * ni * 8;
+      const float dz2 = (float)(dz * dz);
+      const float cr = (float)(cw.re * (1.0 / (4.0 * kPi))), ci = (float)(cw.im * (1.0 / (4.0 * kPi)));
+      float sr = 0.f, si = 0.f;
+#pragma unroll
+      for (int k = 0; k < 7; ++k) {
+        const float dx = ox32 - T.q7[k][0], dy = oy32 - T.q7[k][1];
+        const float r2 = dx * dx + dy * dy;
+        const float r = sqrtf(r2);
+        int i;
+        if (r < xf[1]) i = 0;
+        else if (r >= xf[nrho - 2]) i = nrho - 2;
+        else {
+          int lo = 1, hi = nrho - 2;
+          while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (r < xf[mid]) hi = mid; else lo = mid;
+          }
+          i = lo;
+        }
+        const float z = r - xf[i];
+        const float4 c01 = *reinterpret_cast<const float4*>(tb + (size_t)i * 8);
+        const float4 c23 = *reinterpret_cast<const float4*>(tb + (size_t)i * 8 + 4);
+        // powers stored from z^3 down to z^0
+        float vr = fmaf(fmaf(fmaf(c01.x, z, c01.z), z, c23.x), z, c23.z);
+        float vi = fmaf(fmaf(fmaf(c01.y, z, c01.w), z, c23.y), z, c23.w);
+        const float ir = rsqrtf(r2 + dz2);
+        vr = fmaf(cr, ir, vr);
+        vi = fmaf(ci, ir, vi);
+        sr = fmaf(vr, T.w7[k], sr);
+        si = fmaf(vi, T.w7[k], si);
+      }
+      k0w = zd(sr, si);
+    } else {
+      k0w = lv_tri64(td[t], ox, oy, dz, nrho, rho, coef, pair, cw);
+    }
+    for (int e = 0; e < P; ++e) acc[e] += k0w * q[(int64_t)t * P + e];
+  }
+  lv_reduce(P, acc, phi + (int64_t)m * P);
 }
 
 // cut currents I[c][e] = sum sign len x and cut voltages V[c][e] = mean of phi over its 8 points
@@ -629,8 +726,18 @@ extern "C" int m25_ports_destroy(m25_ports* p) {
   return M25_OK;
 }
 
+static int deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, const void* x, int where,
+                   const double* beta0, double* S, double* z0, double* gamma, double* z0_line, double* resid,
+                   bool mixed);
+
 extern "C" int m25_deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, const void* x, int where,
                            const double* beta0, double* S, double* z0, double* gamma, double* z0_line, double* resid) {
+  return deembed(ctx, geom, gr, p, x, where, beta0, S, z0, gamma, z0_line, resid, false);
+}
+
+static int deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, const void* x, int where,
+                   const double* beta0, double* S, double* z0, double* gamma, double* z0_line, double* resid,
+                   bool mixed) {
   if (!ctx || !geom || !gr || !p || !x) {
     set_error("m25_deembed: null argument");
     return M25_ERR_VALUE;
@@ -659,9 +766,23 @@ extern "C" int m25_deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_por
     for (int i = 0; i < L * L; ++i) hc[i] = gr->lead_h[2 * L * L + i];
     M25_CUDA(cudaMemcpyAsync(cW, hc.data(), sizeof(zd) * L * L, cudaMemcpyHostToDevice, st));
   }
-  line_voltage_kernel<<<p->nvpt_tot, 256, 0, st>>>(geom->nt, P, L, p->vpts, p->vpt_level, geom->cen, geom->td64,
-                                                   geom->tri_layer, geom->level_z, gr->nrho, gr->rho,
-                                                   reinterpret_cast<const zd*>(gr->coef), cW, p->q, p->phi);
+  if (mixed) {
+    const size_t smem = lv_mixed_smem(L, gr->nrho);
+    if (smem > 200 * 1024) {
+      set_error("m25_sweep_point: Green's tables too large for shared memory");
+      return M25_ERR_VALUE;
+    }
+    // a fixed limit: the tables' size changes with the frequency (other threads)
+    M25_CUDA(cudaFuncSetAttribute(line_voltage_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    line_voltage_mixed_kernel<<<p->nvpt_tot, 256, smem, st>>>(
+        geom->nt, P, L, p->vpts, p->vpt_level, geom->cen, geom->td64, geom->td32, geom->tri_layer, geom->level_z,
+        gr->nrho, gr->rho, gr->rho32, reinterpret_cast<const zd*>(gr->coef), reinterpret_cast<const zf*>(gr->coef32),
+        cW, p->q, p->phi);
+  } else {
+    line_voltage_kernel<<<p->nvpt_tot, 256, 0, st>>>(geom->nt, P, L, p->vpts, p->vpt_level, geom->cen, geom->td64,
+                                                     geom->tri_layer, geom->level_z, gr->nrho, gr->rho,
+                                                     reinterpret_cast<const zd*>(gr->coef), cW, p->q, p->phi);
+  }
   cuts_kernel<<<(p->ncut * P + 127) / 128, 128, 0, st>>>(p->ncut, P, p->cut_off, p->cut_edge, p->cut_w, xd, p->phi, 8,
                                                          p->I, p->V);
   FitArgs fa;
@@ -752,7 +873,8 @@ extern "C" int m25_sweep_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25
     info[0] = inf[0];
     info[1] = inf[1];
   }
-  if ((rc = m25_deembed(ctx, geom, gr, p, ctx->Xsweep.p, M25_ON_DEVICE, beta0, S, z0, gamma, z0_line, resid)))
+  if ((rc = deembed(ctx, geom, gr, p, ctx->Xsweep.p, M25_ON_DEVICE, beta0, S, z0, gamma, z0_line, resid,
+                    precision != M25_FP64)))
     return rc;
   if (x_out) {
     M25_CUDA(cudaMemcpy(x_out, ctx->Xsweep.p, sizeof(zd) * (size_t)n * P, cudaMemcpyDeviceToHost));

@@ -644,7 +644,9 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
     return M25_ERR_VALUE;
   }
   auto kern = f32 ? fill_tri_kernel<T, true> : fill_tri_kernel<T, false>;
-  M25_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // one fixed limit for every call: the tables' size changes with the
+  // frequency, and concurrent sweeps on other threads launch the same kernel
+  M25_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
   int occ = 1;
   M25_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, smem));
   // persistent grid (a whole number of waves); ~16 work items per CTA of at

@@ -27,6 +27,22 @@ void free_all(std::vector<void*>& list) {
   list.clear();
 }
 
+int alloc_async(std::vector<void*>& list, void** p, size_t bytes, cudaStream_t st) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMallocAsync(p, bytes, st);
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaMallocAsync(") + std::to_string(bytes) + " B): " + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? M25_ERR_MEMORY : M25_ERR_CUDA;
+  }
+  list.push_back(*p);
+  return M25_OK;
+}
+
+void free_all_async(std::vector<void*>& list, cudaStream_t st) {
+  for (void* p : list) cudaFreeAsync(p, st);
+  list.clear();
+}
+
 // Products and sums written out so that nvcc does not contract them into
 // FMAs: the near/mid/far thresholds compare the same rounded values as numpy.
 __device__ inline double mul_rn(double a, double b) { return __dmul_rn(a, b); }

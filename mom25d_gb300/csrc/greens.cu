@@ -429,21 +429,21 @@ extern "C" int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* d, m25_gre
     rc = (x);          \
     if (rc) goto fail; \
   } while (0)
-  TRY(alloc(tmp, (void**)&Sd, sizeof(StackDev)));
-  TRY(alloc(tmp, (void**)&kc, sizeof(double) * 2 * d->nk_c));
-  TRY(alloc(tmp, (void**)&wc, sizeof(double) * 2 * d->nk_c));
-  TRY(alloc(tmp, (void**)&kr, sizeof(double) * d->nk_r));
-  TRY(alloc(tmp, (void**)&wr, sizeof(double) * d->nk_r));
-  TRY(alloc(tmp, (void**)&cc, sizeof(zd) * (size_t)d->nk_c * NC));
-  TRY(alloc(tmp, (void**)&cr, sizeof(zd) * (size_t)d->nk_r * NC));
-  TRY(alloc(tmp, (void**)&res, sizeof(zd) * (size_t)n * NC));
-  TRY(alloc(tmp, (void**)&work, sizeof(zd) * (size_t)NC * 2 * n));
-  TRY(alloc(g->allocs, (void**)&g->rho, sizeof(double) * n));
-  TRY(alloc(g->allocs, (void**)&g->rho32, sizeof(float) * n));
-  TRY(alloc(g->allocs, (void**)&g->S, sizeof(zd) * (size_t)NC * n));
-  TRY(alloc(g->allocs, (void**)&g->coef, sizeof(zd) * (size_t)L * L * (n - 1) * 12));
-  TRY(alloc(g->allocs, (void**)&g->coef32, sizeof(float) * 2 * (size_t)L * L * (n - 1) * 12));
-  TRY(alloc(g->allocs, (void**)&g->lead, sizeof(StackDev)));
+  TRY(alloc_async(tmp, (void**)&Sd, sizeof(StackDev), st));
+  TRY(alloc_async(tmp, (void**)&kc, sizeof(double) * 2 * d->nk_c, st));
+  TRY(alloc_async(tmp, (void**)&wc, sizeof(double) * 2 * d->nk_c, st));
+  TRY(alloc_async(tmp, (void**)&kr, sizeof(double) * d->nk_r, st));
+  TRY(alloc_async(tmp, (void**)&wr, sizeof(double) * d->nk_r, st));
+  TRY(alloc_async(tmp, (void**)&cc, sizeof(zd) * (size_t)d->nk_c * NC, st));
+  TRY(alloc_async(tmp, (void**)&cr, sizeof(zd) * (size_t)d->nk_r * NC, st));
+  TRY(alloc_async(tmp, (void**)&res, sizeof(zd) * (size_t)n * NC, st));
+  TRY(alloc_async(tmp, (void**)&work, sizeof(zd) * (size_t)NC * 2 * n, st));
+  TRY(alloc_async(g->allocs, (void**)&g->rho, sizeof(double) * n, st));
+  TRY(alloc_async(g->allocs, (void**)&g->rho32, sizeof(float) * n, st));
+  TRY(alloc_async(g->allocs, (void**)&g->S, sizeof(zd) * (size_t)NC * n, st));
+  TRY(alloc_async(g->allocs, (void**)&g->coef, sizeof(zd) * (size_t)L * L * (n - 1) * 12, st));
+  TRY(alloc_async(g->allocs, (void**)&g->coef32, sizeof(float) * 2 * (size_t)L * L * (n - 1) * 12, st));
+  TRY(alloc_async(g->allocs, (void**)&g->lead, sizeof(StackDev), st));
   M25_CUDA(cudaMemcpyAsync(Sd, &S, sizeof(StackDev), cudaMemcpyHostToDevice, st));
   M25_CUDA(cudaMemcpyAsync(kc, d->kc, sizeof(double) * 2 * d->nk_c, cudaMemcpyHostToDevice, st));
   M25_CUDA(cudaMemcpyAsync(wc, d->wc, sizeof(double) * 2 * d->nk_c, cudaMemcpyHostToDevice, st));
@@ -473,11 +473,11 @@ extern "C" int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* d, m25_gre
   M25_CUDA(cudaMemcpyAsync(g->lead, Sd, sizeof(StackDev), cudaMemcpyDeviceToDevice, st));
   M25_CHECK_LAUNCH();
   // temporaries are released once the stream has consumed them
-  M25_CUDA(cudaStreamSynchronize(st));
-  free_all(tmp);
+  free_all_async(tmp, st);
   {
     StackDev h;
-    M25_CUDA(cudaMemcpy(&h, g->lead, sizeof(StackDev), cudaMemcpyDeviceToHost));
+    M25_CUDA(cudaMemcpyAsync(&h, g->lead, sizeof(StackDev), cudaMemcpyDeviceToHost, st));
+    M25_CUDA(cudaStreamSynchronize(st));
     g->lead_h.resize(3 * L * L);
     g->dz_h.resize(L * L);
     for (int m = 0; m < 3; ++m)
@@ -490,8 +490,8 @@ extern "C" int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* d, m25_gre
   return M25_OK;
 fail:
   cudaStreamSynchronize(st);
-  free_all(tmp);
-  free_all(g->allocs);
+  free_all_async(tmp, st);
+  free_all_async(g->allocs, st);
   delete g;
   return rc;
 #undef TRY
@@ -499,8 +499,7 @@ fail:
 
 extern "C" int m25_greens_destroy(m25_greens* g) {
   if (!g) return M25_OK;
-  cudaStreamSynchronize(g->ctx->stream);
-  free_all(g->allocs);
+  free_all_async(g->allocs, g->ctx->stream);
   delete g;
   return M25_OK;
 }

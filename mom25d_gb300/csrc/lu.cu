@@ -8,8 +8,8 @@
 //                  rows in shared memory; one bounded grid barrier per
 //                  column (pivot search |re| + |im| as izamax, swap, scale,
 //                  rank-1 update of the panel)
-//   laswp_kernel   the panel's row interchanges on the other columns
-//   trsm_kernel    U12 = L11^-1 A12
+//   swap_trsm_kernel  the panel's row interchanges on the other columns,
+//                  composed into one gather, fused with U12 = L11^-1 A12
 //   gemm_kernel    A22 -= L21 U12 (SIMT), or the tcgen05 tensor-core path
 //                  for complex64 (lu_tc.cu)
 // Solve: permutation, blocked forward / backward substitution. The mixed
@@ -533,48 +533,134 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_cluster_kernel(Cluster
   cluster_sync_all();
 }
 
-// Row interchanges of rows k0..k0+nb-1 applied to the columns outside the panel.
+// The panel's row interchanges applied to the columns outside it, fused with
+// U12 = L11^-1 A12 on the columns to its right (L11 unit lower). One warp owns
+// 32 columns: it gathers the rows the interchanges touch into shared memory
+// and writes them to their final rows; on a right-hand column it first runs
+// the forward substitution on the w panel rows in 8-row blocks. The
+// interchanges are composed, not replayed: the rows touched are the w panel
+// rows and the pivot rows below the panel, and the original row that ends in
+// position x is found by applying the swaps to x in reverse order.
+// (LAPACK zgetrf applies the same swaps one by one through zlaswp.)
+constexpr int kSwapWarps = 2;
+constexpr int kSwapMaxW = 64;
+
 template <class T>
-__global__ void laswp_kernel(cx<T>* A, int64_t lda, int n, int k0, int nb, const int32_t* __restrict__ ipiv) {
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n || (c >= k0 && c < k0 + nb)) return;
-  for (int j = 0; j < nb; ++j) {
-    int r = k0 + j, p = ipiv[r];
-    if (p != r) {
-      cx<T> t = A[(int64_t)r * lda + c];
-      A[(int64_t)r * lda + c] = A[(int64_t)p * lda + c];
-      A[(int64_t)p * lda + c] = t;
-    }
-  }
+__host__ __device__ constexpr size_t swap_trsm_smem() {
+  return sizeof(cx<T>) * ((size_t)kSwapMaxW * kSwapMaxW + (size_t)kSwapWarps * 2 * kSwapMaxW * 32);
 }
 
-// U12 = L11^-1 A12 for a column chunk of 32 per CTA (L11 unit lower).
 template <class T>
-__global__ void __launch_bounds__(256) trsm_kernel(cx<T>* A, int64_t lda, int n, int k0, int nb) {
+__global__ void __launch_bounds__(32 * kSwapWarps) swap_trsm_kernel(cx<T>* A, int64_t lda, int n, int k0, int w,
+                                                                   const int32_t* __restrict__ ipiv) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<T>* Ls = reinterpret_cast<cx<T>*>(smem_raw);  // (nb, nb)
-  cx<T>* X = Ls + (size_t)nb * nb;                  // (nb, 32)
-  const int c0 = k0 + nb + blockIdx.x * 32;
-  const int cw = min(32, n - c0);
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    int r = e / nb, c = e % nb;
-    Ls[e] = A[(int64_t)(k0 + r) * lda + k0 + c];
+  cx<T>* Ls = reinterpret_cast<cx<T>*>(smem_raw);  // Ls[t * 64 + r] = L11[r][t], zero off the strict lower part
+  cx<T>* V = Ls + kSwapMaxW * kSwapMaxW;           // per warp: [2 * 64 rows][32 columns]
+  __shared__ int piv[kSwapMaxW], dst[2 * kSwapMaxW], src[2 * kSwapMaxW];
+  __shared__ int nd_s;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int kend = k0 + w;
+  const int vc0 = blockIdx.x * (32 * kSwapWarps);  // first column of the CTA, counted without the panel's
+  if (warp == 0) {
+    int pr[kSwapMaxW / 32];
+#pragma unroll
+    for (int h = 0; h < kSwapMaxW / 32; ++h) {
+      const int j = lane + 32 * h;
+      pr[h] = j < w ? ipiv[k0 + j] : -1;
+      piv[j] = pr[h];
+    }
+    // positions touched: the panel rows, then each pivot row below the panel once
+    bool first[kSwapMaxW / 32];
+#pragma unroll
+    for (int h = 0; h < kSwapMaxW / 32; ++h) first[h] = pr[h] >= kend;
+#pragma unroll 8
+    for (int q = 0; q < kSwapMaxW; ++q) {
+      const int pq = __shfl_sync(~0u, pr[q >> 5], q & 31);
+#pragma unroll
+      for (int h = 0; h < kSwapMaxW / 32; ++h)
+        if (q < lane + 32 * h && pq == pr[h]) first[h] = false;
+    }
+    int nx = 0;
+#pragma unroll
+    for (int h = 0; h < kSwapMaxW / 32; ++h) {
+      const unsigned b = __ballot_sync(~0u, first[h]);
+      if (first[h]) dst[w + nx + __popc(b & ((1u << lane) - 1u))] = pr[h];
+      nx += __popc(b);
+    }
+    for (int i = lane; i < w; i += 32) dst[i] = k0 + i;
+    __syncwarp();
+    const int nd = w + nx;
+    int y[2 * kSwapMaxW / 32];
+#pragma unroll
+    for (int h = 0; h < 2 * kSwapMaxW / 32; ++h) y[h] = lane + 32 * h < nd ? dst[lane + 32 * h] : -1;
+#pragma unroll 4
+    for (int j = w - 1; j >= 0; --j) {
+      const int r = k0 + j, p = piv[j];
+#pragma unroll
+      for (int h = 0; h < 2 * kSwapMaxW / 32; ++h) y[h] = y[h] == r ? p : (y[h] == p ? r : y[h]);
+    }
+#pragma unroll
+    for (int h = 0; h < 2 * kSwapMaxW / 32; ++h)
+      if (lane + 32 * h < nd) src[lane + 32 * h] = y[h];
+    if (lane == 0) nd_s = nd;
   }
-  for (int e = threadIdx.x; e < nb * 32; e += blockDim.x) {
-    int r = e >> 5, c = e & 31;
-    X[e] = c < cw ? A[(int64_t)(k0 + r) * lda + c0 + c] : cx<T>();
+  const bool any_right = vc0 + 32 * kSwapWarps > k0 && kend < n;
+  // loads are batched into registers before the shared-memory stores: A
+  // is a generic pointer, so the compiler keeps each load behind the
+  // previous store otherwise
+  constexpr int kBatch = 16;
+  if (any_right) {
+    for (int e0 = threadIdx.x; e0 < kSwapMaxW * kSwapMaxW; e0 += kBatch * 32 * kSwapWarps) {
+      cx<T> v[kBatch];
+#pragma unroll
+      for (int k = 0; k < kBatch; ++k) {
+        const int e = e0 + k * 32 * kSwapWarps, t = e >> 6, r = e & 63;
+        v[k] = (t < r && r < w) ? A[(int64_t)(k0 + r) * lda + k0 + t] : cx<T>();
+      }
+#pragma unroll
+      for (int k = 0; k < kBatch; ++k) Ls[e0 + k * 32 * kSwapWarps] = v[k];
+    }
   }
   __syncthreads();
-  for (int t = 0; t < nb - 1; ++t) {
-    for (int e = threadIdx.x; e < (nb - 1 - t) * 32; e += blockDim.x) {
-      int r = t + 1 + (e >> 5), c = e & 31;
-      X[r * 32 + c] -= Ls[r * nb + t] * X[t * 32 + c];
-    }
-    __syncthreads();
+  const int nd = nd_s;
+  const int vc = vc0 + warp * 32 + lane;
+  if (vc >= n - w) return;
+  const int c = vc < k0 ? vc : vc + w;
+  const bool right = c >= kend;
+  cx<T>* Vw = V + (size_t)warp * 2 * kSwapMaxW * 32;
+  // each lane reads and writes only its own column: no barrier between them
+  for (int i0 = 0; i0 < nd; i0 += kBatch) {
+    cx<T> v[kBatch];
+#pragma unroll
+    for (int k = 0; k < kBatch; ++k)
+      if (i0 + k < nd) v[k] = A[(int64_t)src[i0 + k] * lda + c];
+#pragma unroll
+    for (int k = 0; k < kBatch; ++k)
+      if (i0 + k < nd) Vw[(i0 + k) * 32 + lane] = v[k];
   }
-  for (int e = threadIdx.x; e < nb * 32; e += blockDim.x) {
-    int r = e >> 5, c = e & 31;
-    if (c < cw) A[(int64_t)(k0 + r) * lda + c0 + c] = X[e];
+  for (int i = right ? w : 0; i < nd; ++i)
+    if (src[i] != dst[i]) A[(int64_t)dst[i] * lda + c] = Vw[i * 32 + lane];
+  if (!right) return;
+  for (int b = 0; b < w; b += 8) {
+    cx<T> x[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x[i] = b + i < w ? Vw[(b + i) * 32 + lane] : cx<T>();
+    for (int t = 0; t < b; ++t) {
+      const cx<T> xt = Vw[t * 32 + lane];
+      const cx<T>* lt = Ls + t * kSwapMaxW + b;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) x[i] -= lt[i] * xt;
+    }
+#pragma unroll
+    for (int t = 0; t < 7; ++t)
+#pragma unroll
+      for (int i = t + 1; i < 8; ++i) x[i] -= Ls[(b + t) * kSwapMaxW + b + i] * x[t];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (b + i < w) {
+        Vw[(b + i) * 32 + lane] = x[i];
+        A[(int64_t)(k0 + b + i) * lda + c] = x[i];
+      }
   }
 }
 
@@ -678,10 +764,12 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
     return smem <= 200 * 1024;
   };
   M25_CUDA(cudaFuncSetAttribute(panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-  {
-    size_t smem_t = (size_t)nb * nb * sizeof(cx<T>) + (size_t)nb * 32 * sizeof(cx<T>);
-    M25_CUDA(cudaFuncSetAttribute(trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_t));
+  if (nb > kSwapMaxW) {
+    set_error("dense LU: panel width above 64");
+    return M25_ERR_VALUE;
   }
+  M25_CUDA(cudaFuncSetAttribute(swap_trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)swap_trsm_smem<T>()));
   (void)bps_max;
   (void)rows;
   int Gmax = ctx->ext_scratch ? ctx->ext_gmax : 4 * ctx->num_sms;
@@ -707,14 +795,14 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
   // the cluster panel: largest trailing size whose rows fit in 16 CTAs
   int cluster_rows = 0;
   {
-    static int ok = -1;
     int optin = 0;
     M25_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
     const size_t avail = (size_t)optin - 1024;  // static shared variables
     const int R = nb > 64 ? 0
                           : (int)((avail - cluster_panel_smem<T>(0)) / ((size_t)kPanelLd * sizeof(cx<T>)));
-    if (ok < 0) {
-      ok = 0;
+    // decided once (thread-safe initialisation: sweeps on several threads)
+    static const bool ok = [avail] {
+      bool yes = false;
       const char* off = getenv("M25_NO_CLUSTER_PANEL");
       if (!(off && *off == '1') &&
           cudaFuncSetAttribute(panel_cluster_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
@@ -733,12 +821,13 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
         cfg.attrs = at;
         cfg.numAttrs = 1;
         int nclusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&nclusters, panel_cluster_kernel<T>, &cfg) == cudaSuccess && nclusters > 0)
-          ok = 1;
+        yes = cudaOccupancyMaxActiveClusters(&nclusters, panel_cluster_kernel<T>, &cfg) == cudaSuccess &&
+              nclusters > 0;
       }
       cudaGetLastError();  // a refused attribute only means: no cluster panel
-    }
-    if (ok == 1 && R > 0) cluster_rows = kPanelCluster * R;
+      return yes;
+    }();
+    if (ok && R > 0) cluster_rows = kPanelCluster * R;
   }
   for (int k0 = 0; k0 < n; k0 += nb) {
     const int w = std::min(nb, n - k0);
@@ -812,16 +901,12 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
     }
     }
     if (n > w) {
-      StageTimer tm(ctx, ST_LASWP);
-      laswp_kernel<T><<<(n + 255) / 256, 256, 0, st>>>(A, lda, n, k0, w, ipiv);
+      StageTimer tm(ctx, ST_TRSM);
+      const int cols = 32 * kSwapWarps;
+      swap_trsm_kernel<T><<<(n - w + cols - 1) / cols, cols, swap_trsm_smem<T>(), st>>>(A, lda, n, k0, w, ipiv);
     }
     if (k0 + w < n) {
       int ncol = n - k0 - w;
-      size_t smem_t = (size_t)w * w * sizeof(cx<T>) + (size_t)w * 32 * sizeof(cx<T>);
-      {
-        StageTimer tm(ctx, ST_TRSM);
-        trsm_kernel<T><<<(ncol + 31) / 32, 256, smem_t, st>>>(A, lda, n, k0, w);
-      }
       StageTimer tm(ctx, ST_GEMM);
       if (use_tc) {
         int rc = lu_gemm_tc(ctx, reinterpret_cast<zf*>(A), lda, n, k0, w);

@@ -414,16 +414,15 @@ int make_map(CUtensorMap* map, const float* ptr, int rows, int cols_k, int box_r
 }  // namespace
 
 bool lu_tc_available() {
-  static int avail = -1;
-  if (avail < 0) {
+  static const bool avail = [] {  // initialised once, also under concurrent first calls
     int dev = 0, major = 0, minor = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
     cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
     const char* off = getenv("M25_NO_TENSOR_CORES");
-    avail = (major == 10 && minor == 3 && encode_fn() != nullptr && !(off && *off == '1')) ? 1 : 0;
-  }
-  return avail == 1;
+    return major == 10 && minor == 3 && encode_fn() != nullptr && !(off && *off == '1');
+  }();
+  return avail;
 }
 
 // packed width of one plane for a panel of w complex columns
@@ -482,14 +481,11 @@ int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w) {
     return M25_ERR_VALUE;
   }
   if ((rc = make_map(&mc, C, m, n2, 32, 2 * lda))) return rc;
-  static int n_sm = 0, chunk = 0;
-  if (!n_sm) {
-    int dev = 0;
-    M25_CUDA(cudaGetDevice(&dev));
-    M25_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+  const int n_sm = ctx->num_sms;
+  static const int chunk = [] {
     const char* e = getenv("M25_TC_CHUNK");
-    chunk = e ? std::max(1, atoi(e)) : 2;
-  }
+    return e ? std::max(1, atoi(e)) : 2;
+  }();
   TcArgs ta;
   ta.M = m;
   ta.N = n2;

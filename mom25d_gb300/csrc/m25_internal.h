@@ -120,6 +120,10 @@ struct m25_greens {
 namespace m25 {
 int alloc(std::vector<void*>& list, void** p, size_t bytes);
 void free_all(std::vector<void*>& list);
+// Stream-ordered variants for the per-frequency objects: unlike cudaFree,
+// cudaFreeAsync does not wait for the work of every other stream.
+int alloc_async(std::vector<void*>& list, void** p, size_t bytes, cudaStream_t st);
+void free_all_async(std::vector<void*>& list, cudaStream_t st);
 
 cudaEvent_t take_event(m25_ctx* c);
 
