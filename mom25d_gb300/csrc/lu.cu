@@ -534,33 +534,36 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_cluster_kernel(Cluster
 }
 
 // The panel's row interchanges applied to the columns outside it, fused with
-// U12 = L11^-1 A12 on the columns to its right (L11 unit lower). One warp owns
+// U12 = L11^-1 A12 on the columns to its right (L11 unit lower). A CTA owns
 // 32 columns: it gathers the rows the interchanges touch into shared memory
-// and writes them to their final rows; on a right-hand column it first runs
-// the forward substitution on the w panel rows in 8-row blocks. The
-// interchanges are composed, not replayed: the rows touched are the w panel
-// rows and the pivot rows below the panel, and the original row that ends in
-// position x is found by applying the swaps to x in reverse order.
+// (lane = column), writes them to their final rows, and on the right-hand
+// columns runs the forward substitution with 8 lanes per column, each lane
+// holding 8 of the w <= 64 panel rows (rows l, l + 8, ...): at step t the
+// lane of row t passes x[t] to the other 7 by a shuffle. Every element
+// takes its subtractions in the order t = 0, 1, ... as in LAPACK's ztrsm.
+// The interchanges are composed, not replayed: the rows touched are the w
+// panel rows and the pivot rows below the panel, and the original row that
+// ends in position x is found by applying the swaps to x in reverse order.
 // (LAPACK zgetrf applies the same swaps one by one through zlaswp.)
-constexpr int kSwapWarps = 2;
 constexpr int kSwapMaxW = 64;
+constexpr int kSwapLd = 33;  // row stride of the gathered rows (complex elements)
 
 template <class T>
 __host__ __device__ constexpr size_t swap_trsm_smem() {
-  return sizeof(cx<T>) * ((size_t)kSwapMaxW * kSwapMaxW + (size_t)kSwapWarps * 2 * kSwapMaxW * 32);
+  return sizeof(cx<T>) * ((size_t)kSwapMaxW * kSwapMaxW + (size_t)kSwapMaxW * kSwapLd);
 }
 
 template <class T>
-__global__ void __launch_bounds__(32 * kSwapWarps) swap_trsm_kernel(cx<T>* A, int64_t lda, int n, int k0, int w,
-                                                                   const int32_t* __restrict__ ipiv) {
+__global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, int n, int k0, int w,
+                                                        const int32_t* __restrict__ ipiv) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* Ls = reinterpret_cast<cx<T>*>(smem_raw);  // Ls[t * 64 + r] = L11[r][t], zero off the strict lower part
-  cx<T>* V = Ls + kSwapMaxW * kSwapMaxW;           // per warp: [2 * 64 rows][32 columns]
+  cx<T>* V = Ls + kSwapMaxW * kSwapMaxW;           // the w panel rows of the CTA's columns [64][kSwapLd]
   __shared__ int piv[kSwapMaxW], dst[2 * kSwapMaxW], src[2 * kSwapMaxW];
   __shared__ int nd_s;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int kend = k0 + w;
-  const int vc0 = blockIdx.x * (32 * kSwapWarps);  // first column of the CTA, counted without the panel's
+  const int vc0 = blockIdx.x * 32;  // first column of the CTA, counted without the panel's
   if (warp == 0) {
     int pr[kSwapMaxW / 32];
 #pragma unroll
@@ -604,64 +607,79 @@ __global__ void __launch_bounds__(32 * kSwapWarps) swap_trsm_kernel(cx<T>* A, in
       if (lane + 32 * h < nd) src[lane + 32 * h] = y[h];
     if (lane == 0) nd_s = nd;
   }
-  const bool any_right = vc0 + 32 * kSwapWarps > k0 && kend < n;
-  // loads are batched into registers before the shared-memory stores: A
-  // is a generic pointer, so the compiler keeps each load behind the
-  // previous store otherwise
-  constexpr int kBatch = 16;
+  // the CTA's columns vc0 .. vc0 + 31 map to vc (< k0) or vc + w (right of the panel)
+  const bool any_right = kend < n && min(vc0 + 31, n - w - 1) >= k0;
   if (any_right) {
-    for (int e0 = threadIdx.x; e0 < kSwapMaxW * kSwapMaxW; e0 += kBatch * 32 * kSwapWarps) {
-      cx<T> v[kBatch];
+    // 16 elements of L11 per thread, all loads issued before the stores (A is
+    // a generic pointer: the compiler keeps a load behind an earlier store)
+    cx<T> v[16];
 #pragma unroll
-      for (int k = 0; k < kBatch; ++k) {
-        const int e = e0 + k * 32 * kSwapWarps, t = e >> 6, r = e & 63;
-        v[k] = (t < r && r < w) ? A[(int64_t)(k0 + r) * lda + k0 + t] : cx<T>();
-      }
-#pragma unroll
-      for (int k = 0; k < kBatch; ++k) Ls[e0 + k * 32 * kSwapWarps] = v[k];
+    for (int k = 0; k < 16; ++k) {
+      const int e = threadIdx.x + 256 * k, t = e >> 6, r = e & 63;
+      v[k] = (t < r && r < w) ? A[(int64_t)(k0 + r) * lda + k0 + t] : cx<T>();
     }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) Ls[threadIdx.x + 256 * k] = v[k];
   }
   __syncthreads();
   const int nd = nd_s;
-  const int vc = vc0 + warp * 32 + lane;
-  if (vc >= n - w) return;
+  const int vc = vc0 + lane;
+  const bool valid = vc < n - w;
   const int c = vc < k0 ? vc : vc + w;
   const bool right = c >= kend;
-  cx<T>* Vw = V + (size_t)warp * 2 * kSwapMaxW * 32;
-  // each lane reads and writes only its own column: no barrier between them
-  for (int i0 = 0; i0 < nd; i0 += kBatch) {
-    cx<T> v[kBatch];
+  {
+    // warp q gathers rows q, q + 8, ...; every row of the CTA's columns is
+    // read before any is written (the barrier), as rows move between warps
+    cx<T> v[2 * kSwapMaxW / 8];
 #pragma unroll
-    for (int k = 0; k < kBatch; ++k)
-      if (i0 + k < nd) v[k] = A[(int64_t)src[i0 + k] * lda + c];
+    for (int j = 0; j < 2 * kSwapMaxW / 8; ++j) {
+      const int i = warp + 8 * j;
+      v[j] = valid && i < nd ? A[(int64_t)src[i] * lda + c] : cx<T>();
+    }
+    if (any_right)
 #pragma unroll
-    for (int k = 0; k < kBatch; ++k)
-      if (i0 + k < nd) Vw[(i0 + k) * 32 + lane] = v[k];
+      for (int j = 0; j < 2 * kSwapMaxW / 8; ++j) {
+        const int i = warp + 8 * j;
+        if (i < w) V[i * kSwapLd + lane] = v[j];
+      }
+    __syncthreads();
+    // rows that are not solved go straight to their final rows
+#pragma unroll
+    for (int j = 0; j < 2 * kSwapMaxW / 8; ++j) {
+      const int i = warp + 8 * j;
+      if (valid && i < nd && (i >= w || !right) && src[i] != dst[i]) A[(int64_t)dst[i] * lda + c] = v[j];
+    }
   }
-  for (int i = right ? w : 0; i < nd; ++i)
-    if (src[i] != dst[i]) A[(int64_t)dst[i] * lda + c] = Vw[i * 32 + lane];
-  if (!right) return;
-  for (int b = 0; b < w; b += 8) {
+  if (!any_right) return;
+  {
+    const int l8 = lane & 7, col = 4 * warp + (lane >> 3);
     cx<T> x[8];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) x[i] = b + i < w ? Vw[(b + i) * 32 + lane] : cx<T>();
-    for (int t = 0; t < b; ++t) {
-      const cx<T> xt = Vw[t * 32 + lane];
-      const cx<T>* lt = Ls + t * kSwapMaxW + b;
+    for (int k = 0; k < 8; ++k) x[k] = l8 + 8 * k < w ? V[(l8 + 8 * k) * kSwapLd + col] : cx<T>();
 #pragma unroll
-      for (int i = 0; i < 8; ++i) x[i] -= lt[i] * xt;
-    }
+    for (int kb = 0; kb < 8; ++kb)
 #pragma unroll
-    for (int t = 0; t < 7; ++t)
+      for (int j = 0; j < 8; ++j) {
+        const int t = 8 * kb + j;
+        cx<T> xt;
+        xt.re = __shfl_sync(~0u, x[kb].re, (lane & ~7) | j);
+        xt.im = __shfl_sync(~0u, x[kb].im, (lane & ~7) | j);
+        // L11 rows >= w and on / above the diagonal are zero in Ls
 #pragma unroll
-      for (int i = t + 1; i < 8; ++i) x[i] -= Ls[(b + t) * kSwapMaxW + b + i] * x[t];
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-      if (b + i < w) {
-        Vw[(b + i) * 32 + lane] = x[i];
-        A[(int64_t)(k0 + b + i) * lda + c] = x[i];
+        for (int k = kb; k < 8; ++k)
+          if (k > kb || l8 > j) x[k] -= Ls[t * kSwapMaxW + l8 + 8 * k] * xt;
       }
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (l8 + 8 * k < w) V[(l8 + 8 * k) * kSwapLd + col] = x[k];
   }
+  __syncthreads();
+  if (valid && right)
+#pragma unroll
+    for (int j = 0; j < kSwapMaxW / 8; ++j) {
+      const int i = warp + 8 * j;
+      if (i < w) A[(int64_t)(k0 + i) * lda + c] = V[i * kSwapLd + lane];
+    }
 }
 
 // C[r][c] -= sum_t Lp[r][t] Up[t][c] over rows / cols >= off, t < nb:
@@ -902,8 +920,7 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
     }
     if (n > w) {
       StageTimer tm(ctx, ST_TRSM);
-      const int cols = 32 * kSwapWarps;
-      swap_trsm_kernel<T><<<(n - w + cols - 1) / cols, cols, swap_trsm_smem<T>(), st>>>(A, lda, n, k0, w, ipiv);
+      swap_trsm_kernel<T><<<(n - w + 31) / 32, 256, swap_trsm_smem<T>(), st>>>(A, lda, n, k0, w, ipiv);
     }
     if (k0 + w < n) {
       int ncol = n - k0 - w;
