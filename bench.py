@@ -129,7 +129,8 @@ def run_ours(args, rank, world, local):
     # ---- device-resident: geometry, ports uploaded before the timed region;
     # K workers = K engine contexts (streams), points handed out in order
     K = max(1, args.workers)
-    sol = Solver(mesh, st, verbose=False, precision=args.precision, device=local)
+    tol_kw = {} if args.refine_tol is None else {"refine_tol": args.refine_tol}
+    sol = Solver(mesh, st, verbose=False, precision=args.precision, device=local, **tol_kw)
     sols = [sol._sibling(w) for w in range(K)]
     for s_ in sols:
         s_.geometry()
@@ -194,7 +195,7 @@ def run_ours(args, rank, world, local):
     # ---- e2e through the public API: host arrays in, S + currents out
     barrier()
     t0 = time.perf_counter()
-    sol2 = Solver(mesh, st, verbose=False, precision=args.precision, device=local)
+    sol2 = Solver(mesh, st, verbose=False, precision=args.precision, device=local, **tol_kw)
     r = sol2.sweep(my[args.warmup:], keep_currents=True, workers=K)
     torch.cuda.synchronize()
     barrier()
@@ -344,6 +345,7 @@ def main():
     ap.add_argument("--fp64-points", type=int, default=2)
     ap.add_argument("--workers", type=int, default=4, help="frequency points in flight on the GPU")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--refine-tol", type=float, default=None, help="mixed path: backward-error target of the refinement")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":

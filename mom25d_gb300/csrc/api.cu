@@ -102,7 +102,7 @@ extern "C" int m25_ctx_destroy(m25_ctx* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   for (DevBuf* b : {&c->H, &c->Zw, &c->Zlu, &c->Bw, &c->Xw, &c->Rw, &c->Dw, &c->ipiv, &c->scratch, &c->deemb,
-                    &c->Zsweep, &c->Xsweep, &c->flags})
+                    &c->Zsweep, &c->Xsweep, &c->flags, &c->sched})
     b->release();
   cudaStreamDestroy(c->stream);
   delete c;

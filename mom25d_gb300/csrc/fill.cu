@@ -49,6 +49,7 @@ struct FillArgs {
   cx<float> lead32[kMaxLevSq][2];
   float dz32[kMaxLevSq];
   cx<float> jwmu32, inv_jwe32;
+  int* work_counter;   // items handed out beyond the first gridDim.x (zeroed before the launch)
 };
 
 // scipy PPoly interval: x[i] <= r < x[i+1], clamped to the end intervals.
@@ -291,9 +292,12 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
     xf[i] = (float)a.rho[i];
   }
   int loaded = -1;
-  // persistent grid: work items (test block, source chunk) taken round-robin
+  // persistent grid: work items (test block, source chunk) handed out by a
+  // counter, so that CTAs which start late (the SMs busy with the kernels of
+  // concurrent sweeps) take fewer items
+  __shared__ int next_item;
   const int nitems = a.nblocks * a.n_chunks;
-  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+  for (int item = blockIdx.x; item < nitems;) {
   const int blk = item / a.n_chunks, chunk = item % a.n_chunks;
   const int lt = a.block_level[blk];
   if (lt != loaded) {  // same for the whole CTA
@@ -430,6 +434,10 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
       if (pad >= 0) a.IVpad[(int64_t)pad * a.nt + s] = IV;
     }
   }
+  __syncthreads();
+  if (threadIdx.x == 0) next_item = (int)gridDim.x + atomicAdd(a.work_counter, 1);
+  __syncthreads();
+  item = next_item;
   }  // work items
 }
 
@@ -657,6 +665,9 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   nchunk = (nt + a.n_src_chunk - 1) / a.n_src_chunk;
   a.n_chunks = nchunk;
   if (nv) M25_CUDA(cudaMemsetAsync(IVpad, 0, sizeof(cx<T>) * (size_t)geom->npad * nt, st));
+  if ((rc = ctx->sched.ensure(256))) return rc;
+  a.work_counter = ctx->sched.as<int>();
+  M25_CUDA(cudaMemsetAsync(a.work_counter, 0, sizeof(int), st));
   {
     StageTimer tm(ctx, ST_FILL);
     kern<<<std::min(grid, geom->nblocks * nchunk), 256, smem, st>>>(a);

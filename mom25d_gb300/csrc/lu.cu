@@ -759,7 +759,7 @@ __global__ void gather_rows_kernel(int n, int nrhs, const int32_t* __restrict__ 
 }
 
 // ----------------------------------------------------------------- drivers
-int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int nb);  // lu_tc.cu
+int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w, int panel);  // lu_tc.cu
 int lu_tc_prepare(m25_ctx* ctx, int n, int nb);
 int lu_tc_error(m25_ctx* ctx, int* flag);
 bool lu_tc_available();
@@ -926,7 +926,7 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
       int ncol = n - k0 - w;
       StageTimer tm(ctx, ST_GEMM);
       if (use_tc) {
-        int rc = lu_gemm_tc(ctx, reinterpret_cast<zf*>(A), lda, n, k0, w);
+        int rc = lu_gemm_tc(ctx, reinterpret_cast<zf*>(A), lda, n, k0, w, k0 / nb);
         if (rc) return rc;
       } else {
         dim3 grid((ncol + 63) / 64, (ncol + 63) / 64);

@@ -133,7 +133,11 @@ struct TcArgs {
   int tiles_m, ntiles;
   int chunk;       // k-blocks accumulated afresh in TMEM before the register sum
   int* err;
+  int* counter;    // tiles handed out beyond the first gridDim.x (zero at launch)
 };
+
+constexpr int kTileRing = 4;  // tile indices in flight from the producer to the MMA and epilogue warps
+constexpr int kTcHeader = 4096;
 
 // one CTA per SM; 10 warps put three on one SM sub-partition, which caps a
 // thread at 168 registers (96 running sums per epilogue thread fit)
@@ -145,6 +149,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   float* stage_out = reinterpret_cast<float*>(base + kStages * kStageBytes);  // 2 blocks per epilogue warp
   __shared__ __align__(8) uint64_t full[kStages], empty[kStages], tfull[2], tempty[2], done;
+  __shared__ __align__(8) uint64_t tile_full[kTileRing], tile_empty[kTileRing];
+  __shared__ int tile_id[kTileRing];
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag, n_issued, n_consumed, skip;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -162,6 +168,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tfull[b], 1);
       mbar_init(&tempty[b], kEpiWarps);
+    }
+    for (int r = 0; r < kTileRing; ++r) {
+      mbar_init(&tile_full[r], 1);
+      mbar_init(&tile_empty[r], 1 + kEpiWarps);
     }
     mbar_init(&done, 1);
     abort_flag = 0;
@@ -185,9 +195,22 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   if (warp == 0) {
     // TMA producer
+    // tiles are handed out by a counter (CTAs that start late, behind the
+    // kernels of concurrent sweeps, take fewer) and passed on through a ring
+    // of tile indices; -1 ends the CTA's sequence
     if (lane == 0) {
       int it = 0;
-      for (int t = blockIdx.x; t < a.ntiles && !*abort_v; t += gridDim.x) {
+      for (int lt = 0; !*abort_v; ++lt) {
+        const int r = lt % kTileRing;
+        int t = lt == 0 ? (int)blockIdx.x : (int)gridDim.x + atomicAdd(a.counter, 1);
+        if (t >= a.ntiles) t = -1;
+        if (lt >= kTileRing && !mbar_wait(&tile_empty[r], ((lt / kTileRing) - 1) & 1, abort_v)) {
+          *abort_v = 1;
+          break;
+        }
+        tile_id[r] = t;
+        mbar_arrive(&tile_full[r]);
+        if (t < 0) break;
         const int m0 = (t % a.tiles_m) * kBM, n0 = (t / a.tiles_m) * kBN;
         for (int kb = 0; kb < nk; ++kb, ++it) {
           const int s = it % kStages;
@@ -208,7 +231,15 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       int it = 0, ch = 0;
       bool ok = true;
-      for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
+      for (int lt = 0; ok; ++lt) {
+        const int r = lt % kTileRing;
+        if (!mbar_wait(&tile_full[r], (lt / kTileRing) & 1, abort_v)) {
+          ok = false;
+          break;
+        }
+        const int t = *(volatile int*)&tile_id[r];
+        mbar_arrive(&tile_empty[r]);
+        if (t < 0) break;
         for (int c = 0; c < nch && ok; ++c, ++ch) {
           const int b = ch & 1;
           if (ch >= 2 && !mbar_wait(&tempty[b], ((ch >> 1) - 1) & 1, abort_v)) {
@@ -246,7 +277,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     float* stg = stage_out + (warp - 2) * 2 * (kOutBlock / 4);
     int ch = 0, nout = 0;
     bool ok = true;
-    for (int t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
+    for (int lt = 0; ok; ++lt) {
+      const int r = lt % kTileRing;
+      ok = __all_sync(0xffffffffu, mbar_wait(&tile_full[r], (lt / kTileRing) & 1, abort_v));
+      if (!ok) break;
+      const int t = *(volatile int*)&tile_id[r];
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tile_empty[r]);
+      if (t < 0) break;
       const int m0 = (t % a.tiles_m) * kBM, n0 = (t / a.tiles_m) * kBN;
       float sum[kBN / 2];
 #pragma unroll
@@ -429,14 +467,19 @@ bool lu_tc_available() {
 inline int plane_width(int w) { return (2 * w + 63) / 64 * 64; }
 
 // Operand buffer for the factorisation of an n x n matrix with panels of
-// nb: [0, 256) error word, then the packed A3 and B3 of the largest update.
+// nb: a header of kTcHeader bytes (error word, then one tile counter per
+// panel from byte 16), then the packed A3 and B3 of the largest update.
 int lu_tc_prepare(m25_ctx* ctx, int n, int nb) {
   const int m = std::max(n - nb, 1);
   const int K3p = 3 * plane_width(nb);
   const size_t abytes = sizeof(float) * (size_t)m * K3p, bbytes = sizeof(float) * (size_t)2 * m * K3p;
-  int rc = ctx->Dw.ensure(256 + ((abytes + 255) & ~(size_t)255) + bbytes);
+  if (n / nb + 1 > (kTcHeader - 16) / 4) {
+    set_error("tensor-core LU: too many panels");
+    return M25_ERR_VALUE;
+  }
+  int rc = ctx->Dw.ensure(kTcHeader + ((abytes + 255) & ~(size_t)255) + bbytes);
   if (rc) return rc;
-  M25_CUDA(cudaMemsetAsync(ctx->Dw.p, 0, 256, ctx->stream));
+  M25_CUDA(cudaMemsetAsync(ctx->Dw.p, 0, kTcHeader, ctx->stream));
   return M25_OK;
 }
 
@@ -449,19 +492,19 @@ int lu_tc_error(m25_ctx* ctx, int* flag) {
 
 // A22 -= L21 U12 for the panel at k0 of width w (complex64, in place);
 // lu_tc_prepare has sized the operand buffer for this factorisation.
-int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w) {
+int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w, int panel) {
   cudaStream_t st = ctx->stream;
   const int m = n - k0 - w;  // trailing rows = trailing columns
   if (m <= 0) return M25_OK;
   const int P = plane_width(w), K3p = 3 * P;
   const int n2 = 2 * m;
   const size_t abytes = sizeof(float) * (size_t)m * K3p, bbytes = sizeof(float) * (size_t)n2 * K3p;
-  if (256 + ((abytes + 255) & ~(size_t)255) + bbytes > ctx->Dw.bytes) {
+  if (kTcHeader + ((abytes + 255) & ~(size_t)255) + bbytes > ctx->Dw.bytes) {
     set_error("tensor-core LU: operand buffer not prepared for this size");
     return M25_ERR_VALUE;
   }
   int* err = ctx->Dw.as<int>();
-  float* A3 = reinterpret_cast<float*>(ctx->Dw.as<char>() + 256);
+  float* A3 = reinterpret_cast<float*>(ctx->Dw.as<char>() + kTcHeader);
   float* B3 = reinterpret_cast<float*>(reinterpret_cast<char*>(A3) + ((abytes + 255) & ~(size_t)255));
   {
     int64_t ta = (int64_t)m * K3p;
@@ -494,6 +537,7 @@ int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w) {
   ta.ntiles = ta.tiles_m * ((n2 + kBN - 1) / kBN);
   ta.chunk = chunk;
   ta.err = err;
+  ta.counter = reinterpret_cast<int*>(ctx->Dw.as<char>() + 16) + panel;  // zeroed once per factorisation
   M25_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
   tc_gemm_kernel<<<std::min(ta.ntiles, n_sm), kThreads, kSmemBytes, st>>>(ma, mb, mc, ta);
   M25_CHECK_LAUNCH();

@@ -58,6 +58,7 @@ struct m25_ctx {
   long long stage_n[m25::ST_COUNT] = {};
   // workspace reused across calls
   m25::DevBuf H, Zw, Zlu, Zsplit, Bw, Xw, Rw, Dw, ipiv, scratch, deemb, Zsweep, Xsweep, flags;
+  m25::DevBuf sched;  // work counters of the dynamically scheduled kernels
   bool flags_fresh = true;  // the ready flags of the triangular solves need zeroing
   int epoch = 0;            // value of a ready flag in the current sweep
   size_t yt_off = 0;        // offset of the tagged vector copy in the flag buffer (0: not placed yet)

@@ -244,8 +244,8 @@ def test_tee_sweep_matches_reference(gpu):
     g = golden("tee")
     lay, st, m, _ = build("tee")
     idx = [0, 12, 24, 36]
-    # fp64 and mixed (fp64 fill, complex64 LU + fp64 GMRES refinement) are
-    # held to the reference's fit floor; the all-fp32 fill loses the
+    # fp64 and mixed (fp64 singular parts of the fill, complex64 LU + fp64
+    # GMRES refinement) are held to the reference's fit floor; the all-fp32 fill loses the
     # low-frequency scalar-potential cancellation (~1e-4 at 1 GHz)
     for prec, tol in (("fp64", 1e-6), ("mixed", 1e-6), ("mixed_fill32", 3e-4)):
         sol = Solver(m, st, verbose=False, precision=prec)
