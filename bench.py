@@ -127,8 +127,10 @@ def run_ours(args, rank, world, local):
         torch.cuda.synchronize()
 
     # ---- device-resident: geometry, ports uploaded before the timed region;
-    # K workers = K engine contexts (streams), points handed out in order
-    K = max(1, args.workers)
+    # K workers = K engine contexts (streams), points handed out in order;
+    # at least three timed points per worker, so that the pipeline's ramp and
+    # tail stay a small part of the timed region
+    K = max(1, min(args.workers, args.steps // 3))
     tol_kw = {} if args.refine_tol is None else {"refine_tol": args.refine_tol}
     sol = Solver(mesh, st, verbose=False, precision=args.precision, device=local, **tol_kw)
     sols = [sol._sibling(w) for w in range(K)]
@@ -320,7 +322,9 @@ def run_reference(args, rank, world):
 
     lay, st, mesh, freqs = build_workload(G)
     sw = O.Sweep(mesh, st)
-    for i in range(args.warmup):
+    # one untimed point warms the host code (numpy / LAPACK have no later
+    # warm-up effects); more would only lengthen the run by ~7 s each
+    for i in range(min(args.warmup, 1)):
         cpu_sample_point(sw, freqs[i % len(freqs)], block_frac=0.05)
     ts = [cpu_sample_point(sw, freqs[(args.warmup + i) % len(freqs)], block_frac=0.05) for i in range(args.steps)]
     sec = float(np.sum(ts))
@@ -338,12 +342,12 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=12)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=24)
+    ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--fp64-points", type=int, default=2)
-    ap.add_argument("--workers", type=int, default=4, help="frequency points in flight on the GPU")
+    ap.add_argument("--workers", type=int, default=8, help="frequency points in flight on the GPU")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--refine-tol", type=float, default=None, help="mixed path: backward-error target of the refinement")
     args = ap.parse_args()

@@ -20,6 +20,10 @@
  *   m25_deembed          Solver.sweep de-embedding   Engine/mom25d/solver.py:1276-1325
  *                        (charges 1076-1091, line_voltage 1101-1125, PortModel 604-610,
  *                         fit_waves 618-670, _reciprocal_z0 1357-1427)
+ *   m25_mlp_*            (no counterpart: mom25d has no learned part) the
+ *                        network of the learned Green's remainder, which
+ *                        stands in for the Sommerfeld integrals of
+ *                        Engine/mom25d/greens.py:157-173 / layered.py:360-372
  */
 #ifndef M25_H
 #define M25_H
@@ -102,6 +106,7 @@ int m25_geometry_destroy(m25_geom* g);
 int m25_geometry_stats(m25_geom* g, int64_t* out4);
 
 /* ---------------------------------------------------------- Green's tables */
+typedef struct m25_mlp m25_mlp; /* learned remainder network, below */
 typedef struct {
   double freq;
   int32_t nlayer;             /* dielectric layers, bottom to top (air above) */
@@ -122,6 +127,20 @@ typedef struct {
   int32_t nrho;
   const double* rho;          /* (nrho) tabulation radii, rho[0] = 0 */
   double kbig;                /* spectral sample for layered leading terms (15 / t_min) */
+  /* Learned remainder (NULL: the Sommerfeld integral at every radius). The
+   * network maps (2 log1p(rho/a) / log1p(rho_ref/a) - 1, 2 (f - fmin) /
+   * (fmax - fmin) - 1) to the 2 NC scaled real and imaginary parts of the
+   * remainder (NC = 3 nlev^2 columns [A, V, W] x level pairs, res = scale x
+   * output). The Sommerfeld integral at sur_ncheck radii (quadratically
+   * spaced up to the last tabulation radius) corrects it through a cubic
+   * spline of the residual, and at sur_ncheck - 1 midpoints judges it: the
+   * table uses it when the largest error there is <= sur_tol x the largest
+   * |remainder|, else the Sommerfeld integral at every radius. */
+  const m25_mlp* surrogate;
+  double sur_a, sur_rho_ref, sur_fmin, sur_fmax;
+  const double* sur_scale;    /* (2 NC) */
+  int32_t sur_ncheck;         /* 4 .. 64 */
+  double sur_tol;
 } m25_greens_desc;
 
 int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* desc, m25_greens** out);
@@ -130,6 +149,31 @@ int m25_greens_destroy(m25_greens* g);
  * complex128 leading coefficients; coef (nlev*nlev, nrho-1, 4, 3) complex128
  * not-a-knot cubic coefficients (highest power first). Any may be NULL. */
 int m25_greens_tables(m25_greens* g, double* S, double* c, double* coef);
+/* The Sommerfeld remainder the tables were built from: res (nrho, NC)
+ * complex128 (surrogate tables: the corrected network values);
+ * info[0] = 1 if the learned remainder was used, info[1] = the judge's
+ * relative error (0 without a surrogate). Either may be NULL. */
+int m25_greens_remainder(m25_greens* g, double* res, double* info);
+
+/* ------------------------------------------------ learned remainder (MLP) */
+/* A tanh MLP in fp32 on the device: n_in (<= 4) inputs, n_layers (1..4)
+ * hidden layers of width hidden (= 64), n_out (<= 64) linear outputs.
+ * Parameters (one float array, layer by layer: W (out, in) row-major, then b)
+ * start Glorot-uniform from seed, biases zero. */
+int m25_mlp_create(m25_ctx* ctx, int32_t n_in, int32_t hidden, int32_t n_layers, int32_t n_out, uint64_t seed,
+                   m25_mlp** out);
+int m25_mlp_destroy(m25_mlp* m);
+/* *count = parameter count; get / set (host float32, count) may be NULL */
+int m25_mlp_params(m25_mlp* m, int64_t* count, float* get, const float* set);
+/* loss = mean over samples and outputs of (f(X) - Y)^2 and its gradient
+ * (host float32: X (n, n_in), Y (n, n_out), grad (count)) */
+int m25_mlp_loss_grad(m25_mlp* m, int32_t n, const float* X, const float* Y, double* loss, float* grad);
+/* Adam (0.9, 0.999, 1e-8) on minibatches of `batch` rows drawn from (X, Y)
+ * by a counter-based hash of seed, learning rate cosine-decayed from lr to
+ * lr_min over `steps`; loss_out = the loss over all n samples afterwards */
+int m25_mlp_train(m25_mlp* m, int32_t n, const float* X, const float* Y, int32_t steps, int32_t batch, double lr,
+                  double lr_min, uint64_t seed, double* loss_out);
+int m25_mlp_forward(m25_mlp* m, int32_t n, const float* X, float* Y);
 
 /* ----------------------------------------------------------------- fill */
 /* Z (n x n, n = nb + nv) of the MPIE Galerkin fill, symmetrised. precision

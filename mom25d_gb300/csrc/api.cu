@@ -38,7 +38,7 @@ void DevBuf::release() {
 // fill.cu
 template <class T>
 int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, void* Z, int64_t ldz, int where,
-                bool far32);
+                bool far32, const FillSplit* split = nullptr);
 
 // lu.cu
 template <class T> int lu_factor(m25_ctx*, cx<T>*, int64_t, int, int32_t*, int, bool, int*);
@@ -225,9 +225,37 @@ extern "C" int m25_lu_factor(m25_ctx* ctx, int32_t n, int precision, void* A, in
   return M25_OK;
 }
 
+// presplit: Z is already the mixed path's double-float planes and LU input
+static int dense_solve_impl(m25_ctx* ctx, int32_t n, int32_t nrhs, int precision, void* Z, const void* B, void* X,
+                            int where, double tol, int32_t max_iter, int32_t* info, const FillSplit* presplit);
+
 extern "C" int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precision, void* Z, const void* B, void* X,
                                int where, double tol, int32_t max_iter, int32_t* info) {
-  if (!ctx || !Z || !B || !X || n <= 0 || nrhs <= 0 || nrhs > 8) {
+  return dense_solve_impl(ctx, n, nrhs, precision, Z, B, X, where, tol, max_iter, info, nullptr);
+}
+
+namespace m25 {
+// The mixed fill of a mesh without vias straight into the double-float
+// planes of Z and the complex64 LU input (no complex128 Z, no split pass),
+// then the mixed solve: the path of m25_sweep_point for M25_MIXED.
+int fill_solve_mixed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, int nrhs, const zd* B, zd* X,
+                     double tol, int max_iter, int32_t* info) {
+  const int n = geom->nb;
+  const int64_t ldl = (n + 1) & ~1;
+  const size_t nn = (size_t)n * n;
+  int rc;
+  if ((rc = ctx->Zsplit.ensure(sizeof(zf) * 2 * nn))) return rc;
+  if ((rc = ctx->Zlu.ensure(sizeof(zf) * (size_t)n * ldl))) return rc;
+  zf* h = ctx->Zsplit.as<zf>();
+  const FillSplit sp{h, h + nn, ctx->Zlu.as<zf>(), ldl};
+  if ((rc = fill_driver<double>(ctx, geom, gr, zs, zsv, nullptr, n, M25_ON_DEVICE, true, &sp))) return rc;
+  return dense_solve_impl(ctx, n, nrhs, M25_MIXED, nullptr, B, X, M25_ON_DEVICE, tol, max_iter, info, &sp);
+}
+}  // namespace m25
+
+static int dense_solve_impl(m25_ctx* ctx, int32_t n, int32_t nrhs, int precision, void* Z, const void* B, void* X,
+                            int where, double tol, int32_t max_iter, int32_t* info, const FillSplit* presplit) {
+  if (!ctx || !(Z || presplit) || !B || !X || n <= 0 || nrhs <= 0 || nrhs > 8) {
     set_error("m25_dense_solve: bad argument (1 <= nrhs <= 8)");
     return M25_ERR_VALUE;
   }
@@ -259,11 +287,11 @@ extern "C" int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precis
   } else if (precision == M25_MIXED || precision == M25_MIXED_FILL32) {
     // M25_MIXED: Z complex128 (cast for the LU); M25_MIXED_FILL32: Z is the complex64 fill
     // the LU's rows padded to an even length (16-byte rows for the tensor-core update's TMA)
-    const int64_t ldl = (n + 1) & ~1;
-    if ((rc = ctx->Zlu.ensure(sizeof(zf) * (size_t)n * ldl))) return rc;
-    zf* LU = ctx->Zlu.as<zf>();
+    const int64_t ldl = presplit ? presplit->ldl : (n + 1) & ~1;
+    if (!presplit && (rc = ctx->Zlu.ensure(sizeof(zf) * (size_t)n * ldl))) return rc;
+    zf* LU = presplit ? presplit->LU : ctx->Zlu.as<zf>();
     const void* Zres = Z;
-    if (where == M25_ON_HOST) {
+    if (where == M25_ON_HOST && !presplit) {
       size_t zb = (precision == M25_MIXED_FILL32 ? sizeof(zf) : sizeof(zd)) * nn;
       if ((rc = ctx->Zw.ensure(zb))) return rc;
       M25_CUDA(cudaMemcpyAsync(ctx->Zw.p, Z, zb, cudaMemcpyHostToDevice, st));
@@ -273,7 +301,10 @@ extern "C" int m25_dense_solve(m25_ctx* ctx, int32_t n, int32_t nrhs, int precis
     // the fp32 pipes); Zh is also the LU's input
     const zf* Zh = static_cast<const zf*>(Zres);
     const zf* Zl = nullptr;
-    if (precision == M25_MIXED_FILL32) {
+    if (presplit) {
+      Zh = presplit->Zh;
+      Zl = presplit->Zl;
+    } else if (precision == M25_MIXED_FILL32) {
       M25_CUDA(cudaMemcpy2DAsync(LU, sizeof(zf) * ldl, Zres, sizeof(zf) * n, sizeof(zf) * n, n,
                                  cudaMemcpyDeviceToDevice, st));
     } else {

@@ -729,6 +729,10 @@ extern "C" int m25_ports_destroy(m25_ports* p) {
 static int deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, const void* x, int where,
                    const double* beta0, double* S, double* z0, double* gamma, double* z0_line, double* resid,
                    bool mixed);
+namespace m25 {
+int fill_solve_mixed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, int nrhs, const zd* B, zd* X,
+                     double tol, int max_iter, int32_t* info);  // api.cu
+}
 
 extern "C" int m25_deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, const void* x, int where,
                            const double* beta0, double* S, double* z0, double* gamma, double* z0_line, double* resid) {
@@ -861,14 +865,21 @@ extern "C" int m25_sweep_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25
   const int n = geom->nb + geom->nv, P = p->P;
   const size_t esz = precision == M25_MIXED_FILL32 ? sizeof(zf) : sizeof(zd);
   int rc;
-  if ((rc = ctx->Zsweep.ensure(esz * (size_t)n * n))) return rc;
+  if (!(precision == M25_MIXED && geom->nv == 0) && (rc = ctx->Zsweep.ensure(esz * (size_t)n * n))) return rc;
   if ((rc = ctx->Xsweep.ensure(sizeof(zd) * (size_t)n * P))) return rc;
-  if ((rc = m25_assemble(ctx, geom, gr, zs_re, zs_im, zsv_re, zsv_im, precision, ctx->Zsweep.p, n, M25_ON_DEVICE)))
-    return rc;
   int32_t inf[2] = {0, 0};
-  if ((rc = m25_dense_solve(ctx, n, P, precision, ctx->Zsweep.p, p->Bexc, ctx->Xsweep.p, M25_ON_DEVICE, tol, max_iter,
-                            inf)))
-    return rc;
+  if (precision == M25_MIXED && geom->nv == 0) {
+    // fill straight into the solve's double-float planes (no complex128 Z)
+    if ((rc = fill_solve_mixed(ctx, geom, gr, zd(zs_re, zs_im), zd(zsv_re, zsv_im), P, p->Bexc, ctx->Xsweep.as<zd>(),
+                               tol, max_iter, inf)))
+      return rc;
+  } else {
+    if ((rc = m25_assemble(ctx, geom, gr, zs_re, zs_im, zsv_re, zsv_im, precision, ctx->Zsweep.p, n, M25_ON_DEVICE)))
+      return rc;
+    if ((rc = m25_dense_solve(ctx, n, P, precision, ctx->Zsweep.p, p->Bexc, ctx->Xsweep.p, M25_ON_DEVICE, tol,
+                              max_iter, inf)))
+      return rc;
+  }
   if (info) {
     info[0] = inf[0];
     info[1] = inf[1];

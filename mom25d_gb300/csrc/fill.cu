@@ -33,6 +33,7 @@ struct FillArgs {
   const int32_t* block_level;
   const int32_t* cls;
   const T* stat;
+  const double* stat6;  // mixed fill: test-point sums of the near pairs' closed-form parts
   const int32_t* pad_pos;
   int nrho;
   const T* rho;        // (nrho)
@@ -189,19 +190,18 @@ __device__ __forceinline__ void source_pass(int nrho, const TriData<T>& S, T dcx
   }
 }
 
-// Near pair of the mixed precision: the closed-form singular parts (fp64,
-// precomputed per sweep) plus the smooth parts S_A, S_V, whose 7 x 7 point
-// evaluations - R, interval search, spline - and sums over the 7 source
-// points run in fp32; the sums join the singular parts and the test-point
-// accumulation in fp64. (On the oracle, near smooth parts in fp32 on top of
-// fp32 mid / far pairs leave S within 1.4e-7 of the fp64 fill.)
+// Near pair of the mixed precision: the closed-form singular parts enter
+// through their frequency-independent test-point sums (fp64, precomputed per
+// sweep: st6 = [sum w S0, sum w x S0, sum w y S0, sum w S1x, sum w S1y,
+// sum w (x S1x + y S1y)]) times cA, cV; the smooth parts S_A, S_V - their 7 x
+// 7 point evaluations and both sums - run in fp32 and join in fp64.
+// (On the oracle, near smooth parts in fp32 on top of fp32 mid / far pairs
+// leave S within 1.4e-7 of the fp64 fill.)
 template <class T>
-__device__ __forceinline__ void near_pass_mixed(int nrho, const TriData<float>& S32, T dcx, T dcy,
-                                                const T (&tq)[7][2], const T (&tw)[7], const float* xf,
-                                                const float* tab32, cx<T> cA, cx<T> cV, const T* st, int lane,
-                                                cx<T> (&Q)[3], cx<T> (&Px)[3], cx<T> (&Py)[3], cx<T>& IV,
-                                                const T (&tv)[3][2]) {
-  cx<T> S0, SX, SY, T0, T1, T2;
+__device__ __forceinline__ void near_pass_mixed(int nrho, const TriData<float>& S32, const TriData<float>& A32, T dcx,
+                                                T dcy, const float* xf, const float* tab32, cx<T> cA, cx<T> cV,
+                                                const double* st6, int lane, cx<T> (&Q)[3], cx<T> (&Px)[3],
+                                                cx<T> (&Py)[3], cx<T>& IV, const T (&tv)[3][2]) {
   float sq[7][2], sw[7];
 #pragma unroll
   for (int l = 0; l < 7; ++l) {
@@ -209,10 +209,11 @@ __device__ __forceinline__ void near_pass_mixed(int nrho, const TriData<float>& 
     sq[l][1] = S32.q7[l][1];
     sw[l] = S32.w7[l];
   }
+  cx<float> s0, sx, sy, t0, t1, t2, iv;  // the smooth parts' test-point sums
 #pragma unroll
   for (int k = 0; k < 7; ++k) {
-    const T s0 = st[(0 * 7 + k) * 32 + lane], s1x = st[(1 * 7 + k) * 32 + lane], s2y = st[(2 * 7 + k) * 32 + lane];
-    const float rx = (float)(dcx + tq[k][0]), ry = (float)(dcy + tq[k][1]);
+    const float qx = A32.q7[k][0], qy = A32.q7[k][1], wk = A32.w7[k];
+    const float rx = (float)dcx + qx, ry = (float)dcy + qy;
     cx<float> a0, ax, ay, v0;
 #pragma unroll
     for (int l = 0; l < 7; ++l) {
@@ -226,17 +227,20 @@ __device__ __forceinline__ void near_pass_mixed(int nrho, const TriData<float>& 
       ay += saw * sq[l][1];
       v0 += sv * sw[l];
     }
-    const cx<T> K0A = cA * s0 + cx<T>(a0), K1x = cA * s1x + cx<T>(ax), K1y = cA * s2y + cx<T>(ay);
-    const cx<T> K0V = cV * s0 + cx<T>(v0);
-    const T wk = tw[k], wx = wk * tq[k][0], wy = wk * tq[k][1];
-    IV += K0V * wk;
-    S0 += K0A * wk;
-    SX += K0A * wx;
-    SY += K0A * wy;
-    T1 += K1x * wk;
-    T2 += K1y * wk;
-    T0 += K1x * wx + K1y * wy;
+    const float wx = wk * qx, wy = wk * qy;
+    iv += v0 * wk;
+    s0 += a0 * wk;
+    sx += a0 * wx;
+    sy += a0 * wy;
+    t1 += ax * wk;
+    t2 += ay * wk;
+    t0 += ax * wx + ay * wy;
   }
+  const T g0 = st6[0 * 32 + lane], gx = st6[1 * 32 + lane], gy = st6[2 * 32 + lane];
+  const T h1 = st6[3 * 32 + lane], h2 = st6[4 * 32 + lane], h0 = st6[5 * 32 + lane];
+  IV = cV * g0 + cx<T>(iv);
+  const cx<T> S0 = cA * g0 + cx<T>(s0), SX = cA * gx + cx<T>(sx), SY = cA * gy + cx<T>(sy);
+  const cx<T> T1 = cA * h1 + cx<T>(t1), T2 = cA * h2 + cx<T>(t2), T0 = cA * h0 + cx<T>(t0);
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     Px[i] = SX - S0 * tv[i][0];
@@ -276,19 +280,26 @@ __device__ __forceinline__ void pair_block(const TriData<T>& S, const T (&tcA)[3
 // and the accumulation in fp64 with the smooth parts in fp32
 // (near_pass_mixed). In the mixed path's error budget (S within 1e-5 of
 // mom25d) the fp32 rounding moves S by ~1e-7.
-template <class T, bool FAR32>
-__global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
+//
+// PASS (mixed precision): 1 = near pairs only, 2 = mid and far pairs only,
+// two launches over the same work items, each built for two CTAs per SM
+// (the fp64 fill's single pass needs ~240 registers a thread) and staging
+// only the fp32 tables.
+template <class T, bool FAR32, int PASS>
+__global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   const int L = a.nlev;
   const int n = a.nrho;
-  // tables of the pairs (lt, ls): radii, then per source level (n-1) x 16 values [A, V]
-  T* xs = reinterpret_cast<T*>(smem_raw);
-  T* tabs = xs + ((n + 3) & ~3);
-  float* xf = reinterpret_cast<float*>(tabs + (size_t)L * (n - 1) * 16);  // radii rounded to fp32
+  // tables of the pairs (lt, ls): radii, then per source level (n-1) x 16
+  // values [A, V]; FAR32 reads only the fp32 copies (radii and tables)
+  T* xs = FAR32 ? nullptr : reinterpret_cast<T*>(smem_raw);
+  T* tabs = FAR32 ? nullptr : xs + ((n + 3) & ~3);
+  float* xf = FAR32 ? reinterpret_cast<float*>(smem_raw)
+                    : reinterpret_cast<float*>(tabs + (size_t)L * (n - 1) * 16);  // radii rounded to fp32
   float* tabs32 = xf + ((n + 3) & ~3);  // FAR32: fp32 tables, same layout as tabs
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    xs[i] = a.rho[i];
+    if (!FAR32) xs[i] = a.rho[i];
     xf[i] = (float)a.rho[i];
   }
   int loaded = -1;
@@ -304,8 +315,8 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
     __syncthreads();
     for (int ls = 0; ls < L; ++ls) {
       const cx<T>* src = reinterpret_cast<const cx<T>*>(a.coef) + (size_t)(lt * L + ls) * (n - 1) * 12;
-      T* dst = tabs + (size_t)ls * (n - 1) * 16;
-      for (int e = threadIdx.x; e < (n - 1) * 8; e += blockDim.x) {
+      T* dst = FAR32 ? nullptr : tabs + (size_t)ls * (n - 1) * 16;
+      for (int e = threadIdx.x; e < (FAR32 ? 0 : (n - 1) * 8); e += blockDim.x) {
         int iv = e >> 3, r = e & 7, p = r >> 1, which = r & 1;  // power p, kernel A(0) / V(1)
         cx<T> v = src[((size_t)iv * 4 + p) * 3 + which];
         dst[(size_t)iv * 16 + p * 4 + which * 2] = v.re;
@@ -354,17 +365,18 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
   const int s_end = min(a.nt, s_begin + a.n_src_chunk);
   for (int s = s_begin + warp; s < s_end; s += nwarp) {
     const int code = a.cls[(int64_t)blk * a.nt + s];
+    if ((PASS == 1 && code < 0) || (PASS == 2 && code >= 0)) continue;  // the other pass's pair
     const int ls = a.tri_layer[s];
     const TriData<T>& S = a.td[s];
     const T dcx = T(tcx - a.cen[2 * s]), dcy = T(tcy - a.cen[2 * s + 1]);
-    const T* tab = tabs + (size_t)ls * (n - 1) * 16;
+    const T* tab = FAR32 ? nullptr : tabs + (size_t)ls * (n - 1) * 16;
     const cx<T> cA = a.lead[lt * L + ls][0], cV = a.lead[lt * L + ls][1];
     const T dz = a.dz[lt * L + ls];
     cx<T> Q[3], Px[3], Py[3], IV;
     if (code >= 0) {
       if (FAR32)
-        near_pass_mixed<T>(n, a.td32[s], dcx, dcy, tq, tw, xf, tabs32 + (size_t)ls * (n - 1) * 16, cA, cV,
-                           a.stat + (int64_t)code * 672, lane, Q, Px, Py, IV, tv);
+        near_pass_mixed<T>(n, a.td32[s], a.td32[tt], dcx, dcy, xf, tabs32 + (size_t)ls * (n - 1) * 16, cA, cV,
+                           a.stat6 + (int64_t)code * 192, lane, Q, Px, Py, IV, tv);
       else
         source_pass<T, 7, true>(n, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, a.stat + (int64_t)code * 672, lane,
                                 Q, Px, Py, IV, tv);
@@ -410,7 +422,7 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
         source_pass<T, 1, false>(n, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, nullptr, lane, Q, Px, Py, IV, tv);
       pair_block<T>(S, tcA, tcV, a.jwmu, a.inv_jwe, Q, Px, Py, IV, out);
     }
-    if (active && s == t && (a.zs.re != T(0) || a.zs.im != T(0))) {
+    if (PASS != 2 && active && s == t && (a.zs.re != T(0) || a.zs.im != T(0))) {
       // conductor loss: Zs Int_T (r - a_i).(r - a_j) dS cA_i cA_j
 #pragma unroll
       for (int i = 0; i < 3; ++i)
@@ -443,10 +455,14 @@ __global__ void __launch_bounds__(256) fill_tri_kernel(FillArgs<T> a) {
 
 // Z[m][n] = 0.5 (Zr[m][n] + Zr[n][m]), Zr[m][n] = sum over the two triangles
 // of m (test) and of n (source) of H[3 t_n + j_n][slot(t_m) * 3 + i_m].
-template <class T, class TO>
+// SPLIT (mixed precision without vias): Z itself is not stored but its
+// double-float planes Zh = fl32(Z), Zl = fl32(Z - Zh) (rows nb apart) and the
+// complex64 LU input (Zh, rows ldl apart).
+template <class T, class TO, bool SPLIT = false>
 __global__ void gather_kernel(int nb, const cx<T>* __restrict__ H, int64_t ldh, const int32_t* __restrict__ etri,
                               const int32_t* __restrict__ eloc, const int32_t* __restrict__ tpos,
-                              cx<TO>* __restrict__ Z, int64_t ldz) {
+                              cx<TO>* __restrict__ Z, int64_t ldz, zf* __restrict__ Zh = nullptr,
+                              zf* __restrict__ Zl = nullptr, zf* __restrict__ LU = nullptr, int64_t ldl = 0) {
   int nn = blockIdx.x * blockDim.x + threadIdx.x;
   int m = blockIdx.y;
   if (nn >= nb) return;
@@ -469,7 +485,15 @@ __global__ void gather_kernel(int nb, const cx<T>* __restrict__ H, int64_t ldh, 
       s2 += H[rm[a] * ldh + cn[b]];  // test n, source m
     }
   cx<T> z = (s1 + s2) * T(0.5);
-  Z[(int64_t)m * ldz + nn] = cx<TO>(z);
+  if constexpr (SPLIT) {
+    const float hr = (float)z.re, hi = (float)z.im;
+    const zf hv(hr, hi);
+    Zh[(int64_t)m * nb + nn] = hv;
+    Zl[(int64_t)m * nb + nn] = zf((float)(z.re - (double)hr), (float)(z.im - (double)hi));
+    LU[(int64_t)m * ldl + nn] = hv;
+  } else {
+    Z[(int64_t)m * ldz + nn] = cx<TO>(z);
+  }
 }
 
 // Via rows: Zvb[k][n] = inv_jwe sum_pad D[pad][k] sum_{T of n} cV IV(pad, T)
@@ -581,7 +605,7 @@ __global__ void im_gv0_kernel(int L, int nrho, const double* __restrict__ rho, c
 // Stage 1 + 2 + 3 on the context's stream; Z is host or device memory.
 template <class T>
 int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, void* Zout, int64_t ldz, int where,
-                bool far32) {
+                bool far32, const FillSplit* split) {
   cudaStream_t st = ctx->stream;
   const int nt = geom->nt, nb = geom->nb, nv = geom->nv, L = geom->nlev, n = nb + nv;
   const int nrho = gr->nrho;
@@ -614,6 +638,7 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   a.cls = geom->cls;
   a.stat = std::is_same<T, double>::value ? reinterpret_cast<const T*>(geom->stat64)
                                           : reinterpret_cast<const T*>(geom->stat32);
+  a.stat6 = geom->stat6;
   a.pad_pos = geom->pad_pos;
   a.nrho = nrho;
   a.rho = std::is_same<T, double>::value ? reinterpret_cast<const T*>(gr->rho) : reinterpret_cast<const T*>(gr->rho32);
@@ -645,38 +670,56 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   }
   a.jwmu32 = cx<float>(float(jwmu.re), float(jwmu.im));
   a.inv_jwe32 = cx<float>(float(inv_jwe.re), float(inv_jwe.im));
-  size_t smem = sizeof(T) * (((nrho + 3) & ~3) + (size_t)L * (nrho - 1) * 16) +
-                sizeof(float) * (((nrho + 3) & ~3) + (f32 ? (size_t)L * (nrho - 1) * 16 : 0));
+  // fp64 fill: both tables; mixed (f32): the fp32 radii and tables only
+  size_t smem = f32 ? sizeof(float) * (((nrho + 3) & ~3) + (size_t)L * (nrho - 1) * 16)
+                    : sizeof(T) * (((nrho + 3) & ~3) + (size_t)L * (nrho - 1) * 16) + sizeof(float) * ((nrho + 3) & ~3);
   if (smem > 220 * 1024) {
     set_error("m25_assemble: Green's tables too large for shared memory (reduce rho_max or levels)");
     return M25_ERR_VALUE;
   }
-  auto kern = f32 ? fill_tri_kernel<T, true> : fill_tri_kernel<T, false>;
-  // one fixed limit for every call: the tables' size changes with the
-  // frequency, and concurrent sweeps on other threads launch the same kernel
-  M25_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-  int occ = 1;
-  M25_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, smem));
-  // persistent grid (a whole number of waves); ~16 work items per CTA of at
-  // least 64 sources each keep the round-robin tail short
-  const int grid = std::max(1, occ) * ctx->num_sms;
+  // the passes: fp64 = one kernel over all pairs; mixed = near, then mid / far
+  using Kern = void (*)(FillArgs<T>);
+  Kern kerns[2] = {f32 ? fill_tri_kernel<T, true, 1> : fill_tri_kernel<T, false, 0>, fill_tri_kernel<T, true, 2>};
+  const int npass = f32 ? 2 : 1;
+  int grids[2] = {0, 0};
+  for (int k = 0; k < npass; ++k) {
+    // one fixed limit for every call: the tables' size changes with the
+    // frequency, and concurrent sweeps on other threads launch the same kernel
+    M25_CUDA(cudaFuncSetAttribute(kerns[k], cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    int occ = 1;
+    M25_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kerns[k], 256, smem));
+    grids[k] = std::max(1, occ) * ctx->num_sms;  // persistent grid: a whole number of waves
+  }
+  // ~16 work items per CTA of at least 64 sources each keep the tail short
+  const int grid = grids[npass - 1];
   int nchunk = std::max(1, std::min((16 * grid + geom->nblocks - 1) / geom->nblocks, (nt + 63) / 64));
   a.n_src_chunk = (nt + nchunk - 1) / nchunk;
   nchunk = (nt + a.n_src_chunk - 1) / a.n_src_chunk;
   a.n_chunks = nchunk;
   if (nv) M25_CUDA(cudaMemsetAsync(IVpad, 0, sizeof(cx<T>) * (size_t)geom->npad * nt, st));
   if ((rc = ctx->sched.ensure(256))) return rc;
-  a.work_counter = ctx->sched.as<int>();
-  M25_CUDA(cudaMemsetAsync(a.work_counter, 0, sizeof(int), st));
+  M25_CUDA(cudaMemsetAsync(ctx->sched.p, 0, 2 * sizeof(int), st));
   {
     StageTimer tm(ctx, ST_FILL);
-    kern<<<std::min(grid, geom->nblocks * nchunk), 256, smem, st>>>(a);
+    for (int k = 0; k < npass; ++k) {
+      a.work_counter = ctx->sched.as<int>() + k;
+      kerns[k]<<<std::min(grids[k], geom->nblocks * nchunk), 256, smem, st>>>(a);
+    }
   }
   M25_CHECK_LAUNCH();
   {
   StageTimer tm(ctx, ST_GATHER);
-  gather_kernel<T, T><<<dim3((nb + 127) / 128, nb), 128, 0, st>>>(nb, H, ldh, geom->edge_tri, geom->edge_loc,
-                                                                 geom->tpos, Z, ldzd);
+  if (split) {
+    if (nv || !std::is_same<T, double>::value) {
+      set_error("m25_assemble: split output needs the mixed fill without vias");
+      return M25_ERR_VALUE;
+    }
+    gather_kernel<T, T, true><<<dim3((nb + 127) / 128, nb), 128, 0, st>>>(
+        nb, H, ldh, geom->edge_tri, geom->edge_loc, geom->tpos, nullptr, 0, split->Zh, split->Zl, split->LU, split->ldl);
+  } else {
+    gather_kernel<T, T><<<dim3((nb + 127) / 128, nb), 128, 0, st>>>(nb, H, ldh, geom->edge_tri, geom->edge_loc,
+                                                                   geom->tpos, Z, ldzd);
+  }
   }
   M25_CHECK_LAUNCH();
   if (nv) {
@@ -713,7 +756,9 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   return M25_OK;
 }
 
-template int fill_driver<double>(m25_ctx*, m25_geom*, m25_greens*, zd, zd, void*, int64_t, int, bool);
-template int fill_driver<float>(m25_ctx*, m25_geom*, m25_greens*, zd, zd, void*, int64_t, int, bool);
+template int fill_driver<double>(m25_ctx*, m25_geom*, m25_greens*, zd, zd, void*, int64_t, int, bool,
+                                 const FillSplit*);
+template int fill_driver<float>(m25_ctx*, m25_geom*, m25_greens*, zd, zd, void*, int64_t, int, bool,
+                                const FillSplit*);
 
 }  // namespace m25

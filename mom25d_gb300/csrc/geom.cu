@@ -232,6 +232,37 @@ __global__ void static_kernel(int64_t nnear, const int2* __restrict__ near_list,
   st32[o2] = float(S1y);
 }
 
+// The test-point sums of the closed-form parts, per near pair and slot:
+// [sum w S0, sum w x S0, sum w y S0, sum w S1x, sum w S1y, sum w (x S1x +
+// y S1y)] (w, x, y: the test triangle's 7-point weights and points about its
+// centroid). They are frequency independent; the mixed fill multiplies them
+// by the leading coefficients cA, cV of the frequency.
+__global__ void stat_sums_kernel(int64_t nnear, const int2* __restrict__ near_list,
+                                 const int32_t* __restrict__ block_tris, const TriData<double>* __restrict__ td,
+                                 const double* __restrict__ st64, double* __restrict__ st6) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= nnear * 32) return;
+  const int64_t idx = gid >> 5;
+  const int lane = (int)(gid & 31);
+  const int t = block_tris[near_list[idx].x * 32 + lane];
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  if (t >= 0) {
+    const TriData<double>& A = td[t];
+    const double* st = st64 + idx * 672;
+    for (int k = 0; k < 7; ++k) {
+      const double s0 = st[(0 * 7 + k) * 32 + lane], s1x = st[(1 * 7 + k) * 32 + lane], s1y = st[(2 * 7 + k) * 32 + lane];
+      const double w = A.w7[k], wx = w * A.q7[k][0], wy = w * A.q7[k][1];
+      v[0] += w * s0;
+      v[1] += wx * s0;
+      v[2] += wy * s0;
+      v[3] += w * s1x;
+      v[4] += w * s1y;
+      v[5] += wx * s1x + wy * s1y;
+    }
+  }
+  for (int q = 0; q < 6; ++q) st6[(idx * 6 + q) * 32 + lane] = v[q];
+}
+
 __global__ void fill_i32(int32_t* p, int64_t n, int32_t v) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
@@ -391,10 +422,13 @@ extern "C" int m25_geometry_create(m25_ctx* ctx, const m25_mesh_desc* d, m25_geo
     M25_CHECK_LAUNCH();
     TRY(alloc(g->allocs, (void**)&g->stat64, sizeof(double) * std::max<int64_t>(g->nnear, 1) * 672));
     TRY(alloc(g->allocs, (void**)&g->stat32, sizeof(float) * std::max<int64_t>(g->nnear, 1) * 672));
+    TRY(alloc(g->allocs, (void**)&g->stat6, sizeof(double) * std::max<int64_t>(g->nnear, 1) * 192));
     if (g->nnear) {
       int64_t n = g->nnear * 224;
       static_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g->nnear, near_list, g->block_tris, g->tri_layer,
                                                                   g->level_z, g->cen, g->td64, g->stat64, g->stat32);
+      stat_sums_kernel<<<(unsigned)((g->nnear * 32 + 255) / 256), 256, 0, st>>>(g->nnear, near_list, g->block_tris,
+                                                                                g->td64, g->stat64, g->stat6);
       M25_CHECK_LAUNCH();
     }
     // pair statistics (test triangles x source triangles)

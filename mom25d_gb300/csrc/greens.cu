@@ -5,6 +5,7 @@
 // Follows Engine/mom25d/greens.py:111-212 (one grounded slab) and
 // Engine/mom25d/layered.py:238-405 (open multilayer stack, Michalski-Zheng
 // transmission-line form).
+#include <cstring>
 #include <vector>
 
 #include "m25_internal.h"
@@ -220,10 +221,12 @@ __device__ inline zd bessel_j0_complex(zd z) {
 
 // res[rho][c] = sum_k J0(rho k) coef[k][c] over the lifted arc (complex J0)
 // and the real axis (real J0), one CTA per radius.
+// With skip set (the learned remainder was accepted) the CTAs return at once.
 template <int NC>
 __global__ void sommerfeld_kernel(int nrho, const double* __restrict__ rho, int nkc, const double* __restrict__ kc,
                                   const zd* __restrict__ coef_c, int nkr, const double* __restrict__ kr,
-                                  const zd* __restrict__ coef_r, zd* __restrict__ res) {
+                                  const zd* __restrict__ coef_r, zd* __restrict__ res, const int* __restrict__ skip) {
+  if (skip && *skip) return;
   int ir = blockIdx.x;
   double r = rho[ir];
   double acc_re[NC], acc_im[NC];
@@ -372,6 +375,107 @@ __global__ void to_f32_kernel(const double* __restrict__ a, float* __restrict__ 
   if (i < n) b[i] = float(a[i]);
 }
 
+// ------------------------------------------------------ learned remainder
+// network inputs of n radii at frequency f
+__global__ void sur_features_kernel(int n, const double* __restrict__ rho, double a, double rho_ref, double f,
+                                    double fmin, double fmax, float* __restrict__ X) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  X[2 * i] = (float)(2.0 * log1p(rho[i] / a) / log1p(rho_ref / a) - 1.0);
+  X[2 * i + 1] = (float)(2.0 * (f - fmin) / (fmax - fmin) - 1.0);
+}
+
+constexpr int kSurMaxCheck = 48;
+constexpr int kSurMaxCols = 2 * 3 * kMaxLevSq;
+
+// Residual correction and judge (one CTA): natural cubic splines in rho of
+// the Sommerfeld-minus-network residual of every real column through the K
+// check radii; res (table radii) = network + spline; accepted when the
+// largest error at the K - 1 validation radii is <= tol x the largest
+// |remainder| at the check radii.
+__global__ void __launch_bounds__(256) sur_judge_kernel(int NC, int n, const double* __restrict__ rho, int K,
+                                                        const double* __restrict__ rchk, const float* __restrict__ ytab,
+                                                        const float* __restrict__ ychk, const double* __restrict__ scale,
+                                                        const zd* __restrict__ schk, double tol, zd* __restrict__ res,
+                                                        int* __restrict__ flag, double* __restrict__ err_out) {
+  __shared__ double r[kSurMaxCheck][kSurMaxCols], M[kSurMaxCheck][kSurMaxCols];
+  __shared__ double red_e[8], red_s[8];
+  const int ncol = 2 * NC;
+  const int c = threadIdx.x;
+  auto truth = [&](int k, int col) {
+    const zd v = schk[(int64_t)k * NC + (col >> 1)];
+    return (col & 1) ? v.im : v.re;
+  };
+  if (c < ncol) {
+    for (int k = 0; k < K; ++k) r[k][c] = truth(k, c) - scale[c] * (double)ychk[(int64_t)k * ncol + c];
+    // natural spline: M_0 = M_{K-1} = 0, tridiagonal system for the interior (Thomas)
+    double cp[kSurMaxCheck], dp[kSurMaxCheck];
+    cp[0] = 0.0;
+    dp[0] = 0.0;
+    for (int k = 1; k < K - 1; ++k) {
+      const double h0 = rchk[k] - rchk[k - 1], h1 = rchk[k + 1] - rchk[k];
+      const double rhs = 6.0 * ((r[k + 1][c] - r[k][c]) / h1 - (r[k][c] - r[k - 1][c]) / h0);
+      const double den = 2.0 * (h0 + h1) - h0 * cp[k - 1];
+      cp[k] = h1 / den;
+      dp[k] = (rhs - h0 * dp[k - 1]) / den;
+    }
+    M[K - 1][c] = 0.0;
+    for (int k = K - 2; k >= 1; --k) M[k][c] = dp[k] - cp[k] * M[k + 1][c];
+    M[0][c] = 0.0;
+  }
+  __syncthreads();
+  auto spline = [&](double x, int col) {
+    int lo = 0, hi = K - 1;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (x < rchk[mid]) hi = mid; else lo = mid;
+    }
+    const double h = rchk[lo + 1] - rchk[lo], t = x - rchk[lo];
+    const double b = (r[lo + 1][col] - r[lo][col]) / h - h * (2.0 * M[lo][col] + M[lo + 1][col]) / 6.0;
+    return r[lo][col] + t * (b + t * (0.5 * M[lo][col] + t * (M[lo + 1][col] - M[lo][col]) / (6.0 * h)));
+  };
+  // validation radii rchk[K .. 2K-2]
+  double emax = 0.0, smax = 0.0;
+  for (int e = threadIdx.x; e < (K - 1) * ncol; e += blockDim.x) {
+    const int v = K + e / ncol, col = e % ncol;
+    const double pred = scale[col] * (double)ychk[(int64_t)v * ncol + col] + spline(rchk[v], col);
+    emax = fmax(emax, fabs(pred - truth(v, col)));
+  }
+  for (int e = threadIdx.x; e < K * NC; e += blockDim.x) {
+    const zd v = schk[e];
+    smax = fmax(smax, sqrt(v.re * v.re + v.im * v.im));
+  }
+  for (int o = 16; o; o >>= 1) {
+    emax = fmax(emax, __shfl_down_sync(0xffffffffu, emax, o));
+    smax = fmax(smax, __shfl_down_sync(0xffffffffu, smax, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red_e[threadIdx.x >> 5] = emax;
+    red_s[threadIdx.x >> 5] = smax;
+  }
+  // the corrected network values at the table radii
+  for (int e = threadIdx.x; e < n * ncol; e += blockDim.x) {
+    const int i = e / ncol, col = e % ncol;
+    const double v = scale[col] * (double)ytab[(int64_t)i * ncol + col] + spline(rho[i], col);
+    double* out = reinterpret_cast<double*>(res + (int64_t)i * NC + (col >> 1));
+    out[col & 1] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double e = 0, sm = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      e = fmax(e, red_e[w]);
+      sm = fmax(sm, red_s[w]);
+    }
+    const double rel = sm > 0 ? e / sm : INFINITY;
+    *err_out = rel;
+    *flag = rel <= tol ? 1 : 0;
+  }
+}
+
+int mlp_forward_device(const m25_mlp* m, int n, const float* X, float* Y, cudaStream_t st);  // mlp.cu
+int mlp_dims(const m25_mlp* m, int* n_in, int* n_out);
+
 }  // namespace m25
 
 using namespace m25;
@@ -436,7 +540,10 @@ extern "C" int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* d, m25_gre
   TRY(alloc_async(tmp, (void**)&wr, sizeof(double) * d->nk_r, st));
   TRY(alloc_async(tmp, (void**)&cc, sizeof(zd) * (size_t)d->nk_c * NC, st));
   TRY(alloc_async(tmp, (void**)&cr, sizeof(zd) * (size_t)d->nk_r * NC, st));
-  TRY(alloc_async(tmp, (void**)&res, sizeof(zd) * (size_t)n * NC, st));
+  TRY(alloc_async(g->allocs, (void**)&res, sizeof(zd) * (size_t)n * NC, st));
+  g->res = res;
+  TRY(alloc_async(g->allocs, &g->sur, 16, st));
+  M25_CUDA(cudaMemsetAsync(g->sur, 0, 16, st));
   TRY(alloc_async(tmp, (void**)&work, sizeof(zd) * (size_t)NC * 2 * n, st));
   TRY(alloc_async(g->allocs, (void**)&g->rho, sizeof(double) * n, st));
   TRY(alloc_async(g->allocs, (void**)&g->rho32, sizeof(float) * n, st));
@@ -455,11 +562,55 @@ extern "C" int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* d, m25_gre
   leading_kernel<<<1, 1, 0, st>>>(Sd, d->kbig);
   spectral_coef_kernel<<<(d->nk_c + 127) / 128, 128, 0, st>>>(Sd, d->nk_c, kc, wc, 1, cc);
   spectral_coef_kernel<<<(d->nk_r + 127) / 128, 128, 0, st>>>(Sd, d->nk_r, kr, wr, 0, cr);
-  switch (NC) {
-    case 3: sommerfeld_kernel<3><<<n, 256, 0, st>>>(n, g->rho, d->nk_c, kc, cc, d->nk_r, kr, cr, res); break;
-    case 12: sommerfeld_kernel<12><<<n, 256, 0, st>>>(n, g->rho, d->nk_c, kc, cc, d->nk_r, kr, cr, res); break;
-    case 27: sommerfeld_kernel<27><<<n, 256, 0, st>>>(n, g->rho, d->nk_c, kc, cc, d->nk_r, kr, cr, res); break;
-    default: set_error("m25_greens_create: level count"); rc = M25_ERR_VALUE; goto fail;
+  {
+    // the Sommerfeld integral at nr radii (rr) into out; skip: see sommerfeld_kernel
+    auto sommerfeld = [&](int nr, const double* rr, zd* outp, const int* skip) {
+      switch (NC) {
+        case 3: sommerfeld_kernel<3><<<nr, 256, 0, st>>>(nr, rr, d->nk_c, kc, cc, d->nk_r, kr, cr, outp, skip); break;
+        case 12: sommerfeld_kernel<12><<<nr, 256, 0, st>>>(nr, rr, d->nk_c, kc, cc, d->nk_r, kr, cr, outp, skip); break;
+        default: sommerfeld_kernel<27><<<nr, 256, 0, st>>>(nr, rr, d->nk_c, kc, cc, d->nk_r, kr, cr, outp, skip); break;
+      }
+    };
+    if (d->surrogate) {
+      // learned remainder: the network at the table radii and at K check +
+      // K - 1 validation radii, the Sommerfeld integral at the latter only
+      const int K = d->sur_ncheck, nv = 2 * K - 1;
+      int nin = 0, nout = 0;
+      mlp_dims(d->surrogate, &nin, &nout);
+      if (nin != 2 || nout != 2 * NC || K < 4 || K > kSurMaxCheck || !d->sur_scale || !(d->sur_fmax > d->sur_fmin) ||
+          !(d->sur_a > 0) || !(d->sur_rho_ref > 0)) {
+        set_error("m25_greens_create: surrogate does not match the stack (2 inputs, 2 NC outputs, 4-48 check radii)");
+        rc = M25_ERR_VALUE;
+        goto fail;
+      }
+      std::vector<double> hr(nv);
+      const double rlast = d->rho[n - 1];
+      for (int k = 0; k < K; ++k) hr[k] = rlast * ((double)k / (K - 1)) * ((double)k / (K - 1));
+      for (int k = 0; k + 1 < K; ++k) hr[K + k] = rlast * ((k + 0.5) / (K - 1)) * ((k + 0.5) / (K - 1));
+      double *rchk = nullptr, *scl = nullptr;
+      float *X = nullptr, *Y = nullptr;
+      zd* schk = nullptr;
+      TRY(alloc_async(tmp, (void**)&rchk, sizeof(double) * nv, st));
+      TRY(alloc_async(tmp, (void**)&scl, sizeof(double) * 2 * NC, st));
+      TRY(alloc_async(tmp, (void**)&X, sizeof(float) * 2 * (size_t)(n + nv), st));
+      TRY(alloc_async(tmp, (void**)&Y, sizeof(float) * 2 * NC * (size_t)(n + nv), st));
+      TRY(alloc_async(tmp, (void**)&schk, sizeof(zd) * NC * (size_t)nv, st));
+      M25_CUDA(cudaMemcpyAsync(rchk, hr.data(), sizeof(double) * nv, cudaMemcpyHostToDevice, st));
+      M25_CUDA(cudaMemcpyAsync(scl, d->sur_scale, sizeof(double) * 2 * NC, cudaMemcpyHostToDevice, st));
+      sur_features_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, g->rho, d->sur_a, d->sur_rho_ref, d->freq, d->sur_fmin,
+                                                           d->sur_fmax, X);
+      sur_features_kernel<<<(nv + 127) / 128, 128, 0, st>>>(nv, rchk, d->sur_a, d->sur_rho_ref, d->freq, d->sur_fmin,
+                                                            d->sur_fmax, X + 2 * (size_t)n);
+      TRY(mlp_forward_device(d->surrogate, n + nv, X, Y, st));
+      sommerfeld(nv, rchk, schk, nullptr);
+      int* flag = static_cast<int*>(g->sur);
+      double* err = reinterpret_cast<double*>(static_cast<char*>(g->sur) + 8);
+      sur_judge_kernel<<<1, 256, 0, st>>>(NC, n, g->rho, K, rchk, Y, Y + 2 * NC * (size_t)n, scl, schk, d->sur_tol,
+                                          res, flag, err);
+      sommerfeld(n, g->rho, res, flag);  // the full integral unless the judge accepted
+    } else {
+      sommerfeld(n, g->rho, res, nullptr);
+    }
   }
   table_kernel<<<(NC * n + 127) / 128, 128, 0, st>>>(Sd, n, g->rho, res, omega, zd(d->zs_ground_re, d->zs_ground_im),
                                                    reinterpret_cast<zd*>(g->S));
@@ -486,6 +637,14 @@ extern "C" int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* d, m25_gre
     for (int i = 0; i < L; ++i)
       for (int j = 0; j < L; ++j) g->dz_h[i * L + j] = h.dz[i][j];
   }
+  if (d->surrogate) {
+    char hs[16];
+    M25_CUDA(cudaMemcpy(hs, g->sur, 16, cudaMemcpyDeviceToHost));  // the stream is idle here
+    int acc;
+    memcpy(&acc, hs, sizeof(int));
+    memcpy(&g->sur_info[1], hs + 8, sizeof(double));
+    g->sur_info[0] = acc;
+  }
   *out = g;
   return M25_OK;
 fail:
@@ -501,6 +660,21 @@ extern "C" int m25_greens_destroy(m25_greens* g) {
   if (!g) return M25_OK;
   free_all_async(g->allocs, g->ctx->stream);
   delete g;
+  return M25_OK;
+}
+
+extern "C" int m25_greens_remainder(m25_greens* g, double* res, double* info) {
+  if (!g) {
+    set_error("m25_greens_remainder: null greens");
+    return M25_ERR_VALUE;
+  }
+  M25_CUDA(cudaStreamSynchronize(g->ctx->stream));
+  if (res)
+    M25_CUDA(cudaMemcpy(res, g->res, sizeof(zd) * (size_t)g->nrho * 3 * g->nlev * g->nlev, cudaMemcpyDeviceToHost));
+  if (info) {
+    info[0] = g->sur_info[0];
+    info[1] = g->sur_info[1];
+  }
   return M25_OK;
 }
 

@@ -89,6 +89,7 @@ struct m25_geom {
   int32_t* cls = nullptr;                // (nblocks, nt) >= 0 near index, -1 mid, -2 far
   double* stat64 = nullptr;              // (nnear, 3, 7, 32) closed-form S0, S1x, S1y
   float* stat32 = nullptr;
+  double* stat6 = nullptr;               // (nnear, 6, 32) their test-point sums (mixed fill)
   int64_t nnear = 0, npairs[3] = {0, 0, 0};
   // vias
   int32_t* pad_pos = nullptr;            // (nt) pad index or -1
@@ -113,12 +114,20 @@ struct m25_greens {
   float* coef32 = nullptr;     // fp32 copy
   float* rho32 = nullptr;
   double* lead = nullptr;      // (3, nlev, nlev) complex c_A, c_V, c_W (device)
+  m25::zd* res = nullptr;      // (nrho, 3 nlev^2) Sommerfeld remainder (or the learned one)
+  void* sur = nullptr;         // learned remainder: int accepted, then double relative error (device)
+  double sur_info[2] = {0, 0}; // host copy: accepted, error
   std::vector<m25::zd> lead_h; // host copy
   std::vector<double> dz_h;    // (nlev, nlev)
   std::vector<void*> allocs;
 };
 
 namespace m25 {
+// output of the mixed fill as double-float planes and the complex64 LU input
+struct FillSplit {
+  zf *Zh, *Zl, *LU;
+  int64_t ldl;
+};
 int alloc(std::vector<void*>& list, void** p, size_t bytes);
 void free_all(std::vector<void*>& list);
 // Stream-ordered variants for the per-frequency objects: unlike cudaFree,

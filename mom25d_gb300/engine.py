@@ -26,7 +26,8 @@ EXPORTS = ("m25_last_error", "m25_version", "m25_ctx_create", "m25_ctx_destroy",
            "m25_ctx_stream", "m25_geometry_create", "m25_geometry_destroy", "m25_geometry_stats",
            "m25_greens_create", "m25_greens_destroy", "m25_greens_tables", "m25_assemble", "m25_dense_solve",
            "m25_ports_create", "m25_ports_destroy", "m25_deembed", "m25_sweep_point", "m25_deembed_debug",
-           "m25_ctx_timing", "m25_dense_solve_noalloc", "m25_lu_factor")
+           "m25_ctx_timing", "m25_dense_solve_noalloc", "m25_lu_factor", "m25_greens_remainder", "m25_mlp_create",
+           "m25_mlp_destroy", "m25_mlp_params", "m25_mlp_loss_grad", "m25_mlp_train", "m25_mlp_forward")
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
@@ -47,7 +48,10 @@ class GreensDesc(C.Structure):
                 ("layer_tand", _f64p), ("nlev", C.c_int32), ("lev_iface", _i32p), ("lev_z", _f64p),
                 ("single", C.c_int32), ("zs_ground_re", C.c_double), ("zs_ground_im", C.c_double),
                 ("stack_h", C.c_double), ("nk_c", C.c_int32), ("nk_r", C.c_int32), ("kc", _f64p), ("wc", _f64p),
-                ("kr", _f64p), ("wr", _f64p), ("nrho", C.c_int32), ("rho", _f64p), ("kbig", C.c_double)]
+                ("kr", _f64p), ("wr", _f64p), ("nrho", C.c_int32), ("rho", _f64p), ("kbig", C.c_double),
+                ("surrogate", C.c_void_p), ("sur_a", C.c_double), ("sur_rho_ref", C.c_double),
+                ("sur_fmin", C.c_double), ("sur_fmax", C.c_double), ("sur_scale", _f64p), ("sur_ncheck", C.c_int32),
+                ("sur_tol", C.c_double)]
 
 
 class PortDesc(C.Structure):
@@ -94,6 +98,14 @@ def load():
     lib.m25_ctx_timing.argtypes = [vp, C.c_int, _f64p, C.POINTER(C.c_longlong)]
     lib.m25_dense_solve_noalloc.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, vp, vp, _i32p]
     lib.m25_lu_factor.argtypes = [vp, C.c_int32, C.c_int, vp, C.c_int64, _i32p, C.c_int, C.c_int32, _i32p]
+    lib.m25_greens_remainder.argtypes = [vp, _f64p, _f64p]
+    f32p = C.POINTER(C.c_float)
+    lib.m25_mlp_create.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(vp)]
+    lib.m25_mlp_destroy.argtypes = [vp]
+    lib.m25_mlp_params.argtypes = [vp, C.POINTER(C.c_int64), f32p, f32p]
+    lib.m25_mlp_loss_grad.argtypes = [vp, C.c_int32, f32p, f32p, _f64p, f32p]
+    lib.m25_mlp_train.argtypes = [vp, C.c_int32, f32p, f32p, C.c_int32, C.c_int32, d, d, C.c_uint64, _f64p]
+    lib.m25_mlp_forward.argtypes = [vp, C.c_int32, f32p, f32p]
     _lib = lib
     return lib
 

@@ -100,7 +100,9 @@ class Greens:
     """Green's tables of one frequency on the device (GroundedSlabGreens /
     LayeredGreens): rho grid, S_A/S_V/S_W tables, cubic coefficients."""
 
-    def __init__(self, solver, freq):
+    def __init__(self, solver, freq, rho=None, surrogate=True):
+        """rho: tabulation radii (default: mom25d's grid for this frequency);
+        surrogate: use the solver's learned remainder when it covers freq."""
         st, mesh = solver.stack, solver.mesh
         self.freq = float(freq)
         self.omega = 2 * np.pi * freq
@@ -113,7 +115,7 @@ class Greens:
         kref = abs(kk[0]) if single else np.abs(kk).max()
         tmin = t[0] if single else t.min()
         kc, wc, kr, wr = sommerfeld_path(k0, kref, tmin, solver.rho_max)
-        self.rho = tabulation_radii(solver.rho_max, 2 * np.pi / kref, tmin)
+        self.rho = tabulation_radii(solver.rho_max, 2 * np.pi / kref, tmin) if rho is None else np.asarray(rho, float)
         zg = st.surface_impedance(freq) if st.ground_loss else 0.0
         zg = complex(zg)
         self.levels = list(mesh.layer_names)
@@ -126,11 +128,25 @@ class Greens:
                          E.ptr(arrs["il"], C.c_int32), E.ptr(arrs["lz"]), int(single), zg.real, zg.imag,
                          float(st.z[-1]), kc.size, kr.size, E.ptr(arrs["kc"]), E.ptr(arrs["wc"]), E.ptr(arrs["kr"]),
                          E.ptr(arrs["wr"]), self.rho.size, E.ptr(arrs["rho"]), 15.0 / t.min())
+        sur = getattr(solver, "surrogate", None) if surrogate else None
+        self.surrogate_used = None
+        if sur is not None and sur.covers(self.freq):
+            arrs["sur_scale"] = E.f64(sur.scale)
+            sur.fill_desc(d, E.ptr(arrs["sur_scale"]))
         h = C.c_void_p()
         E.check(solver.ctx.lib.m25_greens_create(solver.ctx.h, C.byref(d), C.byref(h)))
         self._h = E.Handle(solver.ctx, h, solver.ctx.lib.m25_greens_destroy)
         self.nlev = L
         self.h = h
+
+    def remainder(self):
+        """(res (nrho, 3 L^2) complex128, info): the Sommerfeld remainder of the
+        tables (columns [A, V, W] x level pairs (i, j)), info = (learned
+        remainder used, its judged relative error)."""
+        res = np.zeros((self.rho.size, 3 * self.nlev ** 2), complex)
+        info = np.zeros(2)
+        E.check(self._h.ctx.lib.m25_greens_remainder(self.h, E.ptr(res.view(np.float64)), E.ptr(info)))
+        return res, (bool(info[0]), float(info[1]))
 
     def tables(self):
         """(S (3,L,L,nrho), c (3,L,L), coef (L*L, nrho-1, 4, 3)) complex128 host copies."""
@@ -273,6 +289,7 @@ class Solver:
         v = mesh.nodes
         self.rho_max = 1.02 * np.hypot(*(v.max(0) - v.min(0)))
         self.verbose = verbose
+        self.surrogate = None  # a GreensSurrogate (mom25d_gb300.surrogate) for the Green's tables
         self.v_weight = 1.0 if v_weight is None else float(v_weight)
         self.pm = [PortModel(mesh, p, st.level_h(p.layer)) for p in self.ports]
         self.groups = {}
