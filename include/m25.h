@@ -67,7 +67,9 @@ void* m25_ctx_stream(m25_ctx* ctx); /* the cudaStream_t every call of this conte
  * accumulated milliseconds and launch counts of the M25_STAGES stages to the
  * outputs (either may be NULL), then enable = 1 / 0 resets and switches the
  * timers on / off, enable = -1 only reads. Stages, in order: greens, fill,
- * gather, via, lu_panel, lu_laswp, lu_trsm, lu_gemm, trsv, refine, deembed. */
+ * gather, via, lu_panel, lu_pack (operand packing of the tensor-core update),
+ * lu_swap_trsm (row interchanges + U12 solve), lu_gemm (trailing update),
+ * trsv, refine, deembed. */
 #define M25_STAGES 11
 int m25_ctx_timing(m25_ctx* ctx, int enable, double* ms_out, long long* count_out);
 

@@ -924,11 +924,11 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
     }
     if (k0 + w < n) {
       int ncol = n - k0 - w;
-      StageTimer tm(ctx, ST_GEMM);
-      if (use_tc) {
+      if (use_tc) {  // times its operand packing (ST_PACK) and its update (ST_GEMM) itself
         int rc = lu_gemm_tc(ctx, reinterpret_cast<zf*>(A), lda, n, k0, w, k0 / nb);
         if (rc) return rc;
       } else {
+        StageTimer tm(ctx, ST_GEMM);
         dim3 grid((ncol + 63) / 64, (ncol + 63) / 64);
         gemm_kernel<T><<<grid, 256, 0, st>>>(A, lda, n, k0, w);
       }

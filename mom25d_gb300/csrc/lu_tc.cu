@@ -5,9 +5,10 @@
 // written as one real GEMM on the interleaved storage: C (m x 2n') -=
 // A (m x 2K) B (2K x 2n') with A the interleaved conj(L21) and B rows
 // (U, -iU) alternating, which gives Re and Im of L U in the even and odd
-// columns of C. Each fp32 operand is split into tf32 hi + lo parts and the
-// three products lo.hi + hi.lo + hi.hi are concatenated along K (3xTF32) so
-// one kind::tf32 GEMM with K3 = 3 P (P = 2K rounded up to 64) does the update.
+// columns of C. Each fp32 operand is split into tf32 hi + lo parts, stored
+// as two planes [hi | lo] of width P (P = 2K rounded up to 64) along K, and
+// every k-block issues the three products hi.lo, lo.hi, hi.hi (3xTF32) from
+// the same staged tiles: the operands are read once, not once per product.
 //
 // The tensor cores round their fp32 accumulation with a bias, so a long
 // accumulation chain loses about four bits against fp32 fused multiply-adds.
@@ -18,9 +19,10 @@
 // at the accuracy of the SIMT one.
 //
 // Kernel (persistent, one CTA per SM, 320 threads): warp 0 issues TMA loads of
-// 128B-swizzled K-major tiles (A 128 x 32, B 192 x 32 fp32) into a 4-stage
-// mbarrier ring; warp 1 owns the TMEM (two 128 x 192 fp32 buffers) and one
-// elected thread issues tcgen05.mma (M 128, N 192, K 8); warps 2-9 read the
+// 128B-swizzled K-major tiles (A hi, A lo 128 x 32, B hi, B lo 192 x 32 fp32)
+// into a 2-stage mbarrier ring of 80 KB stages; warp 1 owns the TMEM (two
+// 128 x 192 fp32 buffers) and one elected thread issues tcgen05.mma (M 128,
+// N 192, K 8; 12 per k-block); warps 2-9 read the
 // chunk results with tcgen05.ld and sum them, and at the end of a tile hand
 // the negated sums to the TMA as 32 x 32 blocks (128B-swizzled staging, two
 // buffers per warp) that are reduce-added into C in global memory
@@ -42,9 +44,10 @@ namespace m25 {
 
 namespace {
 
-constexpr int kBM = 128, kBN = 192, kBK = 32, kStages = 4;
+constexpr int kBM = 128, kBN = 192, kBK = 32, kStages = 2;
 constexpr int kTmemCols = 512, kBufStride = 256;  // two accumulators, 256 columns apart
-constexpr int kTileA = kBM * kBK * 4, kTileB = kBN * kBK * 4, kStageBytes = kTileA + kTileB;
+constexpr int kTileA = kBM * kBK * 4, kTileB = kBN * kBK * 4;
+constexpr int kStageBytes = 2 * (kTileA + kTileB);  // [A hi | A lo | B hi | B lo], each 1024-byte aligned
 constexpr int kEpiWarps = 8, kThreads = 64 + 32 * kEpiWarps;
 constexpr int kOutBlock = 32 * 32 * 4;  // one 32 x 32 fp32 block of C, staged for the TMA reduce
 constexpr int kSmemBytes = kStages * kStageBytes + kEpiWarps * 2 * kOutBlock + 1024;
@@ -129,7 +132,7 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 }
 
 struct TcArgs {
-  int M, N, K3;    // rows, real columns of C (its fp32 view), packed K (multiple of 32)
+  int M, N, P;     // rows, real columns of C (its fp32 view), plane width of the packed K (multiple of 32)
   int tiles_m, ntiles;
   int chunk;       // k-blocks accumulated afresh in TMEM before the register sum
   int* err;
@@ -154,7 +157,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag, n_issued, n_consumed, skip;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nk = a.K3 / kBK;
+  const int nk = a.P / kBK;  // k-blocks of one plane
   const int nch = (nk + a.chunk - 1) / a.chunk;
   // an earlier CTA gave up: leave before taking TMEM
   if (threadIdx.x == 0) skip = *(volatile int*)a.err;
@@ -220,8 +223,10 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           unsigned char* sa = base + s * kStageBytes;
           mbar_expect_tx(&full[s], kStageBytes);
+          tma_load_2d(sa + kTileA, &tmA, a.P + kb * kBK, m0, &full[s]);
+          tma_load_2d(sa + 2 * kTileA + kTileB, &tmB, a.P + kb * kBK, n0, &full[s]);
           tma_load_2d(sa, &tmA, kb * kBK, m0, &full[s]);
-          tma_load_2d(sa + kTileA, &tmB, kb * kBK, n0, &full[s]);
+          tma_load_2d(sa + 2 * kTileA, &tmB, kb * kBK, n0, &full[s]);
           n_issued = it + 1;
         }
       }
@@ -256,10 +261,16 @@ __global__ void __launch_bounds__(kThreads, 1)
               break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const uint32_t sa = smem_u32(base + s * kStageBytes), sb = sa + kTileA;
+            const uint32_t sah = smem_u32(base + s * kStageBytes), sal = sah + kTileA;
+            const uint32_t sbh = sah + 2 * kTileA, sbl = sbh + kTileB;
+            // the two small products first, then hi.hi; 8 tf32 = 32 bytes per MMA
 #pragma unroll
-            for (int k = 0; k < kBK / 8; ++k)  // 8 tf32 = 32 bytes per MMA
-              mma_tf32(acc, smem_desc(sa + 32 * k), smem_desc(sb + 32 * k), (kb > c * a.chunk || k) ? 1u : 0u);
+            for (int k = 0; k < kBK / 8; ++k)
+              mma_tf32(acc, smem_desc(sah + 32 * k), smem_desc(sbl + 32 * k), (kb > c * a.chunk || k) ? 1u : 0u);
+#pragma unroll
+            for (int k = 0; k < kBK / 8; ++k) mma_tf32(acc, smem_desc(sal + 32 * k), smem_desc(sbh + 32 * k), 1u);
+#pragma unroll
+            for (int k = 0; k < kBK / 8; ++k) mma_tf32(acc, smem_desc(sah + 32 * k), smem_desc(sbh + 32 * k), 1u);
             mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
             n_consumed = it + 1;
           }
@@ -365,15 +376,15 @@ __device__ __forceinline__ float tf32_round(float x) {
   return __uint_as_float(r);
 }
 
-// A3[r][s P + j] for the trailing rows, planes s = [hi | lo | hi] of the
+// A2[r][s P + j] for the trailing rows, planes s = [hi | lo] of the
 // interleaved conj(L21) (j = 2 t + f: f = 0 real part, 1 minus imaginary part)
 __global__ void pack_a_kernel(const zf* __restrict__ LU, int64_t lda, int k0, int w, int m, int P,
                               float* __restrict__ A3) {
-  const int K3p = 3 * P;
+  const int K2p = 2 * P;
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (int64_t)m * K3p) return;
-  int r = int(e / K3p), k3 = int(e % K3p);
-  int s = k3 / P, j = k3 % P, t = j >> 1;
+  if (e >= (int64_t)m * K2p) return;
+  int r = int(e / K2p), k2 = int(e % K2p);
+  int s = k2 / P, j = k2 % P, t = j >> 1;
   float out = 0.f;
   if (t < w) {
     zf L = LU[(int64_t)(k0 + w + r) * lda + k0 + t];
@@ -384,14 +395,14 @@ __global__ void pack_a_kernel(const zf* __restrict__ LU, int64_t lda, int k0, in
   A3[e] = out;
 }
 
-// B3t[c2][s P + j] for the trailing real columns c2 = 2 c + e, planes
-// s = [lo | hi | hi] of the rows (U, -iU); the two small products come first.
+// B2t[c2][s P + j] for the trailing real columns c2 = 2 c + e, planes
+// s = [hi | lo] of the rows (U, -iU).
 // One block transposes a 32 (t) x 32 (c) complex tile of U12 through shared
 // memory so that both the reads of U and the writes of B3t are coalesced.
 __global__ void __launch_bounds__(256) pack_b_kernel(const zf* __restrict__ LU, int64_t lda, int k0, int w, int m,
                                                      int P, float* __restrict__ B3) {
   __shared__ zf tile[32][33];
-  const int K3p = 3 * P;
+  const int K2p = 2 * P;
   const int c0 = blockIdx.x * 32, t0 = blockIdx.y * 32;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   for (int i = ty; i < 32; i += 8) {
@@ -399,8 +410,8 @@ __global__ void __launch_bounds__(256) pack_b_kernel(const zf* __restrict__ LU, 
     tile[i][tx] = (t < w && c < m) ? LU[(int64_t)(k0 + t) * lda + k0 + w + c] : zf{0.f, 0.f};
   }
   __syncthreads();
-  // 3 planes x 64 real columns x 64 floats (32 t x 2 parts)
-  for (int idx = threadIdx.x; idx < 3 * 64 * 64; idx += 256) {
+  // 2 planes x 64 real columns x 64 floats (32 t x 2 parts)
+  for (int idx = threadIdx.x; idx < 2 * 64 * 64; idx += 256) {
     const int j = idx & 63, row = idx >> 6;
     const int s = row >> 6, c2l = row & 63;
     const int c = c2l >> 1, ee = c2l & 1, t = j >> 1, f = j & 1;
@@ -408,7 +419,7 @@ __global__ void __launch_bounds__(256) pack_b_kernel(const zf* __restrict__ LU, 
     const zf U = tile[t][c];
     const float v = ee == 0 ? (f == 0 ? U.re : U.im) : (f == 0 ? U.im : -U.re);
     const float hi = tf32_round(v);
-    B3[(int64_t)(2 * c0 + c2l) * K3p + s * P + 2 * t0 + j] = s == 0 ? tf32_round(v - hi) : hi;
+    B3[(int64_t)(2 * c0 + c2l) * K2p + s * P + 2 * t0 + j] = s == 1 ? tf32_round(v - hi) : hi;
   }
 }
 
@@ -471,8 +482,8 @@ inline int plane_width(int w) { return (2 * w + 63) / 64 * 64; }
 // panel from byte 16), then the packed A3 and B3 of the largest update.
 int lu_tc_prepare(m25_ctx* ctx, int n, int nb) {
   const int m = std::max(n - nb, 1);
-  const int K3p = 3 * plane_width(nb);
-  const size_t abytes = sizeof(float) * (size_t)m * K3p, bbytes = sizeof(float) * (size_t)2 * m * K3p;
+  const int K2p = 2 * plane_width(nb);
+  const size_t abytes = sizeof(float) * (size_t)m * K2p, bbytes = sizeof(float) * (size_t)2 * m * K2p;
   if (n / nb + 1 > (kTcHeader - 16) / 4) {
     set_error("tensor-core LU: too many panels");
     return M25_ERR_VALUE;
@@ -496,9 +507,9 @@ int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w, int panel
   cudaStream_t st = ctx->stream;
   const int m = n - k0 - w;  // trailing rows = trailing columns
   if (m <= 0) return M25_OK;
-  const int P = plane_width(w), K3p = 3 * P;
+  const int P = plane_width(w), K2p = 2 * P;
   const int n2 = 2 * m;
-  const size_t abytes = sizeof(float) * (size_t)m * K3p, bbytes = sizeof(float) * (size_t)n2 * K3p;
+  const size_t abytes = sizeof(float) * (size_t)m * K2p, bbytes = sizeof(float) * (size_t)n2 * K2p;
   if (kTcHeader + ((abytes + 255) & ~(size_t)255) + bbytes > ctx->Dw.bytes) {
     set_error("tensor-core LU: operand buffer not prepared for this size");
     return M25_ERR_VALUE;
@@ -507,15 +518,16 @@ int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w, int panel
   float* A3 = reinterpret_cast<float*>(ctx->Dw.as<char>() + kTcHeader);
   float* B3 = reinterpret_cast<float*>(reinterpret_cast<char*>(A3) + ((abytes + 255) & ~(size_t)255));
   {
-    int64_t ta = (int64_t)m * K3p;
+    StageTimer tm(ctx, ST_PACK);
+    int64_t ta = (int64_t)m * K2p;
     pack_a_kernel<<<(unsigned)((ta + 255) / 256), 256, 0, st>>>(A, lda, k0, w, m, P, A3);
     dim3 gb((m + 31) / 32, P / 64);
     pack_b_kernel<<<gb, 256, 0, st>>>(A, lda, k0, w, m, P, B3);
   }
   CUtensorMap ma, mb;
   int rc;
-  if ((rc = make_map(&ma, A3, m, K3p, kBM))) return rc;
-  if ((rc = make_map(&mb, B3, n2, K3p, kBN))) return rc;
+  if ((rc = make_map(&ma, A3, m, K2p, kBM))) return rc;
+  if ((rc = make_map(&mb, B3, n2, K2p, kBN))) return rc;
   // C: the fp32 view of the trailing block, rows 2 lda floats apart, 32 x 32 boxes
   CUtensorMap mc;
   const float* C = reinterpret_cast<const float*>(A + (int64_t)(k0 + w) * lda + k0 + w);
@@ -527,18 +539,19 @@ int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w, int panel
   const int n_sm = ctx->num_sms;
   static const int chunk = [] {
     const char* e = getenv("M25_TC_CHUNK");
-    return e ? std::max(1, atoi(e)) : 2;
+    return e ? std::max(1, atoi(e)) : 1;  // one k-block: 12 MMAs (3 products x K 32) per TMEM accumulation
   }();
   TcArgs ta;
   ta.M = m;
   ta.N = n2;
-  ta.K3 = K3p;
+  ta.P = P;
   ta.tiles_m = (m + kBM - 1) / kBM;
   ta.ntiles = ta.tiles_m * ((n2 + kBN - 1) / kBN);
   ta.chunk = chunk;
   ta.err = err;
   ta.counter = reinterpret_cast<int*>(ctx->Dw.as<char>() + 16) + panel;  // zeroed once per factorisation
   M25_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+  StageTimer tm(ctx, ST_GEMM);
   tc_gemm_kernel<<<std::min(ta.ntiles, n_sm), kThreads, kSmemBytes, st>>>(ma, mb, mc, ta);
   M25_CHECK_LAUNCH();
   return M25_OK;

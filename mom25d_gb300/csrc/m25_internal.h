@@ -42,7 +42,7 @@ struct DevBuf {
 
 namespace m25 {
 // Stages timed with CUDA events on the context's stream (m25_ctx_timing).
-enum Stage { ST_GREENS, ST_FILL, ST_GATHER, ST_VIA, ST_PANEL, ST_LASWP, ST_TRSM, ST_GEMM, ST_TRSV, ST_REFINE,
+enum Stage { ST_GREENS, ST_FILL, ST_GATHER, ST_VIA, ST_PANEL, ST_PACK, ST_TRSM, ST_GEMM, ST_TRSV, ST_REFINE,
              ST_DEEMBED, ST_COUNT };
 }
 
