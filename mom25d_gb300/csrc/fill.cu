@@ -51,6 +51,8 @@ struct FillArgs {
   float dz32[kMaxLevSq];
   cx<float> jwmu32, inv_jwe32;
   int* work_counter;   // items handed out beyond the first gridDim.x (zeroed before the launch)
+  int nbk;             // mixed fill: buckets of the radius index (0: binary search)
+  float bk_scale;      // buckets per unit radius
 };
 
 // scipy PPoly interval: x[i] <= r < x[i+1], clamped to the end intervals.
@@ -70,11 +72,25 @@ __device__ __forceinline__ int find_interval(const T* __restrict__ x, int n, T r
 // radii (the fp64 pipe of this GPU is the fill's bottleneck): rounding is
 // monotone and the radii are far apart against fp32 resolution, so the fp32
 // index is the fp64 one or one above it; one fp64 comparison settles it.
+// Bucket index of the fp32 radii (mixed fill): t[j] = the interval of radius
+// j / scale; buckets are no wider than the smallest radius step, so a radius
+// lies in t[j] or a step or two from it.
+struct Bk {
+  const uint16_t* t = nullptr;
+  float scale = 0.f;
+  int nb = 0;
+};
+
 template <class T>
-__device__ __forceinline__ int find_interval_f(const T* __restrict__ x, const float* __restrict__ xf, int n, T r) {
+__device__ __forceinline__ int find_interval_f(const T* __restrict__ x, const float* __restrict__ xf, int n, T r,
+                                               Bk bk = Bk()) {
   const float rf = (float)r;
   int lo;
-  if (rf < xf[1]) {
+  if (bk.t) {
+    lo = bk.t[min((int)(rf * bk.scale), bk.nb - 1)];
+    if (lo > 0 && rf < xf[lo]) --lo;  // rf * scale rounded into the next bucket
+    while (lo < n - 2 && xf[lo + 1] <= rf) ++lo;
+  } else if (rf < xf[1]) {
     lo = 0;
   } else if (rf >= xf[n - 2]) {
     lo = n - 2;
@@ -94,8 +110,9 @@ __device__ __forceinline__ int find_interval_f(const T* __restrict__ x, const fl
 // sum_p c[3-p] (r - x_i)^p, the order PPoly evaluates.
 template <class T>
 __device__ __forceinline__ void spline_av(const T* __restrict__ xs, const float* __restrict__ xf,
-                                          const T* __restrict__ tab, int n, T r, cx<T>& sa, cx<T>& sv) {
-  int i = find_interval_f(xs, xf, n, r);
+                                          const T* __restrict__ tab, int n, T r, cx<T>& sa, cx<T>& sv,
+                                          Bk bk = Bk()) {
+  int i = find_interval_f(xs, xf, n, r, bk);
   T dx = r - xs[i];
   const T* c = tab + (size_t)i * 16;  // [power 0..3][A re, A im, V re, V im], highest power first
   T z = dx, z2 = dx * dx, z3 = z2 * dx;
@@ -110,7 +127,8 @@ __device__ __forceinline__ void source_pass(int nrho, const TriData<T>& S, T dcx
                                             const T (&tq)[7][2], const T (&tw)[7], const T* xs, const float* xf,
                                             const T* tab,
                                             cx<T> cA, cx<T> cV, T dz, const T* st, int lane, cx<T> (&Q)[3],
-                                            cx<T> (&Px)[3], cx<T> (&Py)[3], cx<T>& IV, const T (&tv)[3][2]) {
+                                            cx<T> (&Px)[3], cx<T> (&Py)[3], cx<T>& IV, const T (&tv)[3][2],
+                                            Bk bk = Bk()) {
   const T inv4pi = T(1.0 / (4.0 * kPi));
   cx<T> S0, SX, SY, T0, T1, T2;  // sums of w_k K over the test points k, weighted by 1, x_k, y_k
   T sq[NQ][2], sw[NQ];
@@ -156,7 +174,7 @@ __device__ __forceinline__ void source_pass(int nrho, const TriData<T>& S, T dcx
         inv = inv4pi * (dz == T(0) ? ri : rsqrt(R2 + dz * dz));
       }
       cx<T> sa, sv;
-      spline_av(xs, xf, tab, nrho, R, sa, sv);
+      spline_av(xs, xf, tab, nrho, R, sa, sv, bk);
       if (!NEAR) {
         sa += cA * inv;
         sv += cV * inv;
@@ -201,7 +219,7 @@ template <class T>
 __device__ __forceinline__ void near_pass_mixed(int nrho, const TriData<float>& S32, const TriData<float>& A32, T dcx,
                                                 T dcy, const float* xf, const float* tab32, cx<T> cA, cx<T> cV,
                                                 const double* st6, int lane, cx<T> (&Q)[3], cx<T> (&Px)[3],
-                                                cx<T> (&Py)[3], cx<T>& IV, const T (&tv)[3][2]) {
+                                                cx<T> (&Py)[3], cx<T>& IV, const T (&tv)[3][2], Bk bk) {
   float sq[7][2], sw[7];
 #pragma unroll
   for (int l = 0; l < 7; ++l) {
@@ -220,7 +238,7 @@ __device__ __forceinline__ void near_pass_mixed(int nrho, const TriData<float>& 
       const float ddx = rx - sq[l][0], ddy = ry - sq[l][1];
       const float R = sqrtf(ddx * ddx + ddy * ddy);  // 0 for coincident points of a self pair
       cx<float> sa, sv;
-      spline_av<float>(xf, xf, tab32, nrho, R, sa, sv);
+      spline_av<float>(xf, xf, tab32, nrho, R, sa, sv, bk);
       const cx<float> saw = sa * sw[l];
       a0 += saw;
       ax += saw * sq[l][0];
@@ -302,6 +320,23 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
     if (!FAR32) xs[i] = a.rho[i];
     xf[i] = (float)a.rho[i];
   }
+  Bk bk;
+  if (FAR32 && a.nbk > 0) {
+    uint16_t* bkt = reinterpret_cast<uint16_t*>(tabs32 + (size_t)L * (n - 1) * 16);
+    __syncthreads();  // xf complete
+    for (int j = threadIdx.x; j < a.nbk; j += blockDim.x) {
+      const float rj = (float)j / a.bk_scale;
+      int lo = 0, hi = n - 2;  // largest i <= n - 2 with xf[i] <= rj
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (xf[mid] <= rj) lo = mid; else hi = mid - 1;
+      }
+      bkt[j] = (uint16_t)lo;
+    }
+    bk.t = bkt;
+    bk.scale = a.bk_scale;
+    bk.nb = a.nbk;
+  }  // the first work item's table load ends with a barrier
   int loaded = -1;
   // persistent grid: work items (test block, source chunk) handed out by a
   // counter, so that CTAs which start late (the SMs busy with the kernels of
@@ -376,7 +411,7 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
     if (code >= 0) {
       if (FAR32)
         near_pass_mixed<T>(n, a.td32[s], a.td32[tt], dcx, dcy, xf, tabs32 + (size_t)ls * (n - 1) * 16, cA, cV,
-                           a.stat6 + (int64_t)code * 192, lane, Q, Px, Py, IV, tv);
+                           a.stat6 + (int64_t)code * 192, lane, Q, Px, Py, IV, tv, bk);
       else
         source_pass<T, 7, true>(n, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, a.stat + (int64_t)code * 672, lane,
                                 Q, Px, Py, IV, tv);
@@ -407,10 +442,10 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
       const cx<float> cA32 = a.lead32[lt * L + ls][0], cV32 = a.lead32[lt * L + ls][1];
       if (code == -1)
         source_pass<float, 3, false>(n, S32, (float)dcx, (float)dcy, tq32, tw32, xf, xf, tab32, cA32, cV32,
-                                     a.dz32[lt * L + ls], nullptr, lane, Qf, Pxf, Pyf, IVf, tv32);
+                                     a.dz32[lt * L + ls], nullptr, lane, Qf, Pxf, Pyf, IVf, tv32, bk);
       else
         source_pass<float, 1, false>(n, S32, (float)dcx, (float)dcy, tq32, tw32, xf, xf, tab32, cA32, cV32,
-                                     a.dz32[lt * L + ls], nullptr, lane, Qf, Pxf, Pyf, IVf, tv32);
+                                     a.dz32[lt * L + ls], nullptr, lane, Qf, Pxf, Pyf, IVf, tv32, bk);
       pair_block<float>(S32, tcA32, tcV32, a.jwmu32, a.inv_jwe32, Qf, Pxf, Pyf, IVf, outf);
 #pragma unroll
       for (int i = 0; i < 3; ++i)
@@ -670,8 +705,23 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   }
   a.jwmu32 = cx<float>(float(jwmu.re), float(jwmu.im));
   a.inv_jwe32 = cx<float>(float(inv_jwe.re), float(inv_jwe.im));
-  // fp64 fill: both tables; mixed (f32): the fp32 radii and tables only
-  size_t smem = f32 ? sizeof(float) * (((nrho + 3) & ~3) + (size_t)L * (nrho - 1) * 16)
+  // mixed fill: bucket index of the fp32 radii, buckets no wider than the
+  // smallest radius step (at most 16384)
+  a.nbk = 0;
+  a.bk_scale = 0.f;
+  if (f32) {
+    const std::vector<double>& hr = gr->rho_h;
+    float gap = INFINITY;
+    for (int i = 0; i + 1 < nrho; ++i) gap = std::min(gap, (float)hr[i + 1] - (float)hr[i]);
+    const float last = (float)hr[nrho - 1];
+    if (gap > 0.f && last > 0.f) {
+      a.nbk = std::min(16384, (int)std::ceil(last / gap) + 1);
+      a.bk_scale = (float)a.nbk / last;
+    }
+  }
+  // fp64 fill: both tables; mixed (f32): the fp32 radii and tables only (+ the bucket index)
+  size_t smem = f32 ? sizeof(float) * (((nrho + 3) & ~3) + (size_t)L * (nrho - 1) * 16) +
+                          sizeof(uint16_t) * (((size_t)a.nbk + 7) & ~(size_t)7)
                     : sizeof(T) * (((nrho + 3) & ~3) + (size_t)L * (nrho - 1) * 16) + sizeof(float) * ((nrho + 3) & ~3);
   if (smem > 220 * 1024) {
     set_error("m25_assemble: Green's tables too large for shared memory (reduce rho_max or levels)");

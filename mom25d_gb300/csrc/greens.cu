@@ -522,6 +522,7 @@ extern "C" int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* d, m25_gre
   g->freq = d->freq;
   g->omega = omega;
   g->stack_h = d->stack_h;
+  g->rho_h.assign(d->rho, d->rho + d->nrho);
   int rc = M25_OK;
   StackDev* Sd = nullptr;
   double *kc = nullptr, *wc = nullptr, *kr = nullptr, *wr = nullptr;

@@ -109,6 +109,7 @@ struct m25_greens {
   int nlev = 0, nrho = 0, single = 0;
   double freq = 0, omega = 0, stack_h = 0;
   double* rho = nullptr;       // (nrho)
+  std::vector<double> rho_h;   // host copy
   double* S = nullptr;         // (3, nlev, nlev, nrho) complex: S_A, S_V, S_W
   double* coef = nullptr;      // (nlev*nlev, nrho-1, 4, 3) complex cubic coefficients
   float* coef32 = nullptr;     // fp32 copy
