@@ -7,7 +7,11 @@
  * of the last error of the calling thread is m25_last_error(). No C++
  * exception crosses this boundary. Array arguments are plain pointers with
  * sizes; "host" arrays are ordinary CPU memory, "device" arrays are CUDA
- * device pointers on the context's device. Complex numbers are interleaved
+ * device pointers on the context's device. The engine works on its own
+ * non-blocking stream (m25_ctx_stream): device inputs written on another
+ * stream must be complete (synchronised, or ordered by an event) before the
+ * call, and device outputs left on that stream (m25_assemble's Z) are
+ * ordered for other streams by m25_ctx_synchronize or an event on it. Complex numbers are interleaved
  * (re, im) pairs of double (complex128) or float (complex64), row-major.
  *
  * Reference interfaces replaced (paths inside the mom25d project):

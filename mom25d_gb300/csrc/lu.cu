@@ -265,7 +265,15 @@ struct ClusterPanelArgs {
   int32_t* ipiv;
   int* info;
   int* err;  // a wait for pushed data ran out
+  float* A2; // tensor-core update: tf32 [hi | lo] planes of conj(L21) (rows of 2 P floats), or null
+  int P;
 };
+
+__device__ __forceinline__ float tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
 
 template <class T>
 struct alignas(16) PivCand {
@@ -529,6 +537,25 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_cluster_kernel(Cluster
     const int r = e >> 6, c = e & 63;
     if (c < nb) a.A[(int64_t)(r0 + r) * a.lda + a.k0 + c] = P[r * kPanelLd + c];
   }
+  if (a.A2) {
+    // the trailing rows as the tensor-core update's A operand: real and minus
+    // imaginary parts of L21 interleaved (j = 2 t + f), split into tf32 hi
+    // and lo planes P floats apart, zero beyond the panel's 2 nb columns
+    for (int e = tid; e < Rq * a.P; e += blockDim.x) {
+      const int r = e / a.P, j = e - r * a.P, t = j >> 1;
+      const int row = r0 + r - (a.k0 + nb);
+      if (row < 0) continue;
+      float hi = 0.f, lo = 0.f;
+      if (t < nb) {
+        const cx<T> L = P[r * kPanelLd + t];
+        const float v = (j & 1) ? -(float)L.im : (float)L.re;
+        hi = tf32_rna(v);
+        lo = tf32_rna(v - hi);
+      }
+      a.A2[(int64_t)row * 2 * a.P + j] = hi;
+      a.A2[(int64_t)row * 2 * a.P + a.P + j] = lo;
+    }
+  }
   // no CTA leaves while a peer may still store into its shared memory
   cluster_sync_all();
 }
@@ -555,7 +582,8 @@ __host__ __device__ constexpr size_t swap_trsm_smem() {
 
 template <class T>
 __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, int n, int k0, int w,
-                                                        const int32_t* __restrict__ ipiv) {
+                                                        const int32_t* __restrict__ ipiv, float* __restrict__ B2,
+                                                        int P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cx<T>* Ls = reinterpret_cast<cx<T>*>(smem_raw);  // Ls[t * 64 + r] = L11[r][t], zero off the strict lower part
   cx<T>* V = Ls + kSwapMaxW * kSwapMaxW;           // the w panel rows of the CTA's columns [64][kSwapLd]
@@ -680,6 +708,28 @@ __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, i
       const int i = warp + 8 * j;
       if (i < w) A[(int64_t)(k0 + i) * lda + c] = V[i * kSwapLd + lane];
     }
+  if (B2) {
+    // U12 as the tensor-core update's B operand: for trailing column cc the
+    // rows 2 cc (re, im) and 2 cc + 1 (im, -re) of (U, -iU), K-major, split
+    // into tf32 hi and lo planes P floats apart, zero beyond 2 w
+    for (int e = threadIdx.x; e < 64 * P; e += blockDim.x) {
+      const int row = e / P, jj = e - row * P;  // row = 2 x (column of the CTA) + part
+      const int cl = row >> 1, part = row & 1;
+      const int vcl = vc0 + cl;
+      if (vcl >= n - w || vcl < k0) continue;  // not a trailing column
+      const int cc = vcl - k0;                  // = (vcl + w) - kend
+      const int t = jj >> 1, f = jj & 1;
+      float hi = 0.f, lo = 0.f;
+      if (t < w) {
+        const cx<T> U = V[t * kSwapLd + cl];
+        const float v = part == 0 ? (f == 0 ? (float)U.re : (float)U.im) : (f == 0 ? (float)U.im : -(float)U.re);
+        hi = tf32_rna(v);
+        lo = tf32_rna(v - hi);
+      }
+      B2[(int64_t)(2 * cc + part) * 2 * P + jj] = hi;
+      B2[(int64_t)(2 * cc + part) * 2 * P + P + jj] = lo;
+    }
+  }
 }
 
 // C[r][c] -= sum_t Lp[r][t] Up[t][c] over rows / cols >= off, t < nb:
@@ -759,8 +809,10 @@ __global__ void gather_rows_kernel(int n, int nrhs, const int32_t* __restrict__ 
 }
 
 // ----------------------------------------------------------------- drivers
-int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w, int panel);  // lu_tc.cu
+int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w, int panel, bool pack_a,
+               bool pack_b);  // lu_tc.cu
 int lu_tc_prepare(m25_ctx* ctx, int n, int nb);
+int lu_tc_operands(m25_ctx* ctx, int n, int k0, int w, float** A2, float** B2, int* P);
 int lu_tc_error(m25_ctx* ctx, int* flag);
 bool lu_tc_available();
 
@@ -850,8 +902,19 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
   for (int k0 = 0; k0 < n; k0 += nb) {
     const int w = std::min(nb, n - k0);
     const int m = n - k0;
-    if (m <= cluster_rows) {
-      ClusterPanelArgs<T> ca{A, lda, n, k0, w, (m + kPanelCluster - 1) / kPanelCluster, ipiv, info, err};
+    // tensor-core update of this panel: its packed operands are written by
+    // the cluster panel (A) and the row-interchange / U12 kernel (B)
+    const bool tc_here = use_tc && k0 + w < n;
+    float *A2 = nullptr, *B2 = nullptr;
+    int P2 = 0;
+    if (tc_here) {
+      int rc = lu_tc_operands(ctx, n, k0, w, &A2, &B2, &P2);
+      if (rc) return rc;
+    }
+    const bool cluster_panel = m <= cluster_rows;
+    if (cluster_panel) {
+      ClusterPanelArgs<T> ca{A,   lda, n, k0, w, (m + kPanelCluster - 1) / kPanelCluster, ipiv, info, err,
+                             A2, P2};
       const size_t smem = cluster_panel_smem<T>(ca.rows_per_cta);
       cudaLaunchConfig_t cfg = {};
       cudaLaunchAttribute at[1];
@@ -920,12 +983,12 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
     }
     if (n > w) {
       StageTimer tm(ctx, ST_TRSM);
-      swap_trsm_kernel<T><<<(n - w + 31) / 32, 256, swap_trsm_smem<T>(), st>>>(A, lda, n, k0, w, ipiv);
+      swap_trsm_kernel<T><<<(n - w + 31) / 32, 256, swap_trsm_smem<T>(), st>>>(A, lda, n, k0, w, ipiv, B2, P2);
     }
     if (k0 + w < n) {
       int ncol = n - k0 - w;
       if (use_tc) {  // times its operand packing (ST_PACK) and its update (ST_GEMM) itself
-        int rc = lu_gemm_tc(ctx, reinterpret_cast<zf*>(A), lda, n, k0, w, k0 / nb);
+        int rc = lu_gemm_tc(ctx, reinterpret_cast<zf*>(A), lda, n, k0, w, k0 / nb, !cluster_panel, false);
         if (rc) return rc;
       } else {
         StageTimer tm(ctx, ST_GEMM);

@@ -503,7 +503,25 @@ int lu_tc_error(m25_ctx* ctx, int* flag) {
 
 // A22 -= L21 U12 for the panel at k0 of width w (complex64, in place);
 // lu_tc_prepare has sized the operand buffer for this factorisation.
-int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w, int panel) {
+// The packed operands of the update of the panel at k0 (width w) in the
+// operand buffer: A2 (m x 2P) and B2 (2m x 2P), m = n - k0 - w trailing rows.
+int lu_tc_operands(m25_ctx* ctx, int n, int k0, int w, float** A2, float** B2, int* Pout) {
+  const int m = n - k0 - w;
+  const int P = plane_width(w), K2p = 2 * P;
+  const size_t abytes = sizeof(float) * (size_t)std::max(m, 1) * K2p, bbytes = sizeof(float) * (size_t)2 * m * K2p;
+  if (kTcHeader + ((abytes + 255) & ~(size_t)255) + bbytes > ctx->Dw.bytes) {
+    set_error("tensor-core LU: operand buffer not prepared for this size");
+    return M25_ERR_VALUE;
+  }
+  *A2 = reinterpret_cast<float*>(ctx->Dw.as<char>() + kTcHeader);
+  *B2 = reinterpret_cast<float*>(reinterpret_cast<char*>(*A2) + ((abytes + 255) & ~(size_t)255));
+  *Pout = P;
+  return M25_OK;
+}
+
+// pack_a / pack_b: the operands still have to be packed (else the panel and
+// the U12 kernel wrote them)
+int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w, int panel, bool pack_a, bool pack_b) {
   cudaStream_t st = ctx->stream;
   const int m = n - k0 - w;  // trailing rows = trailing columns
   if (m <= 0) return M25_OK;
@@ -517,12 +535,12 @@ int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w, int panel
   int* err = ctx->Dw.as<int>();
   float* A3 = reinterpret_cast<float*>(ctx->Dw.as<char>() + kTcHeader);
   float* B3 = reinterpret_cast<float*>(reinterpret_cast<char*>(A3) + ((abytes + 255) & ~(size_t)255));
-  {
+  if (pack_a || pack_b) {
     StageTimer tm(ctx, ST_PACK);
     int64_t ta = (int64_t)m * K2p;
-    pack_a_kernel<<<(unsigned)((ta + 255) / 256), 256, 0, st>>>(A, lda, k0, w, m, P, A3);
+    if (pack_a) pack_a_kernel<<<(unsigned)((ta + 255) / 256), 256, 0, st>>>(A, lda, k0, w, m, P, A3);
     dim3 gb((m + 31) / 32, P / 64);
-    pack_b_kernel<<<gb, 256, 0, st>>>(A, lda, k0, w, m, P, B3);
+    if (pack_b) pack_b_kernel<<<gb, 256, 0, st>>>(A, lda, k0, w, m, P, B3);
   }
   CUtensorMap ma, mb;
   int rc;

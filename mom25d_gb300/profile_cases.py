@@ -73,6 +73,8 @@ def lu_case(args):
     flags = E.M25_LU_NO_TENSOR_CORES if args.simt else 0
     for _ in range(args.reps):
         A = A0.clone()
+        # the engine works on its own stream: torch's copy must have landed
+        torch.cuda.synchronize()
         E.check(ctx.lib.m25_lu_factor(ctx.h, n, E.M25_MIXED, C.c_void_p(A.data_ptr()), n,
                                       C.cast(C.c_void_p(piv.data_ptr()), C.POINTER(C.c_int32)), E.M25_ON_DEVICE, flags,
                                       E.ptr(info, C.c_int32)))
