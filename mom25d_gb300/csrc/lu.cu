@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> a) {
 
 // ------------------------------------------------ panel on one CTA cluster
 // For trailing sizes whose panel fits in the shared memory of one cluster of
-// kPanelCluster CTAs (16, the largest cluster size; about 6500 rows of
+// CL CTAs (16, the largest cluster size: about 6500 rows of
 // 64 complex64 columns), the panel is factored without global barriers. CTA q
 // of the cluster keeps rows k0 + q R .. + R - 1 in shared memory. Per column
 // j, every CTA pushes its pivot candidate (value, row index and the whole
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(256) panel_kernel(PanelArgs<T> a) {
 // it updates. The pushed data is double-buffered by column parity: a CTA can
 // only write column j + 2's buffers after every CTA has passed column j + 1's
 // barrier, that is, after all reads of column j's buffers.
-constexpr int kPanelCluster = 16;
+constexpr int kPanelCluster = 16;  // the largest cluster; smaller trailing blocks take 8 or 4 CTAs
 constexpr int kPanelLd = 65;  // padded row of the panel in shared memory
 
 template <class T>
@@ -281,10 +281,10 @@ struct alignas(16) PivCand {
   int idx;
 };
 
-template <class T>
+template <class T, int CL>
 constexpr size_t cluster_panel_smem(int R) {
-  // rows + candidate rows (2 x 16 x 64) + row j (2 x 64)
-  return sizeof(cx<T>) * ((size_t)R * kPanelLd + 2 * kPanelCluster * 64 + 2 * 64);
+  // rows + candidate rows (2 x CL x 64) + row j (2 x 64)
+  return sizeof(cx<T>) * ((size_t)R * kPanelLd + 2 * CL * 64 + 2 * 64);
 }
 
 __device__ __forceinline__ void cluster_sync_all() {
@@ -367,7 +367,7 @@ __device__ __forceinline__ bool piv_better(T ov, int oi, T v, int i) {
 constexpr int kPanelThreads = 512;
 constexpr int kPanelGroups = kPanelThreads / 64;  // row groups of the update's 2-D map
 
-template <class T>
+template <class T, int CL>
 __global__ void __launch_bounds__(kPanelThreads, 1) panel_cluster_kernel(ClusterPanelArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int q = (int)cluster_rank(), nb = a.nb, R = a.rows_per_cta, tid = threadIdx.x;
@@ -376,8 +376,8 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_cluster_kernel(Cluster
   const int Rq = max(0, r1 - r0);
   cx<T>* P = reinterpret_cast<cx<T>*>(smem_raw);          // (R, kPanelLd) this CTA's rows
   cx<T>* crow = P + (size_t)R * kPanelLd;                   // (2, 16, 64) pushed candidate rows
-  cx<T>* jrow = crow + 2 * kPanelCluster * 64;              // (2, 64) pushed row k0 + j
-  __shared__ PivCand<T> cand[2][kPanelCluster];             // pushed candidates
+  cx<T>* jrow = crow + 2 * CL * 64;              // (2, 64) pushed row k0 + j
+  __shared__ PivCand<T> cand[2][CL];             // pushed candidates
   __shared__ T gmax_v[kPanelGroups];
   __shared__ int gmax_i[kPanelGroups];
   __shared__ __align__(8) uint64_t colbar[2];  // per column parity: completed by the 16 CTAs' pushes
@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_cluster_kernel(Cluster
   __syncthreads();
   cluster_sync_all();  // every CTA runs, with its barriers set up, before the first push
   // bytes pushed into each CTA per column: 16 candidates, 16 rows, row j
-  const uint32_t expect = kPanelCluster * (cand_push_bytes<T>() + nb * (int)sizeof(cx<T>)) + nb * sizeof(cx<T>);
+  const uint32_t expect = CL * (cand_push_bytes<T>() + nb * (int)sizeof(cx<T>)) + nb * sizeof(cx<T>);
   for (int j = 0; j < nb; ++j) {
     const int row_j = a.k0 + j, par = j & 1;
     const int qj = j / R;
@@ -427,15 +427,15 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_cluster_kernel(Cluster
     // from its owner, into all 16 CTAs; each store completes its bytes on
     // the destination's barrier of this column's parity
     if (tid == 0) cl_mbar_expect(&colbar[par], expect);
-    if (tid < kPanelCluster) st_async(dsmem(&cand[par][q], tid), PivCand<T>{bv, bi}, dsmem(&colbar[par], tid));
-    for (int e = tid; e < kPanelCluster * 64; e += blockDim.x) {
+    if (tid < CL) st_async(dsmem(&cand[par][q], tid), PivCand<T>{bv, bi}, dsmem(&colbar[par], tid));
+    for (int e = tid; e < CL * 64; e += blockDim.x) {
       const int dst = e >> 6, c = e & 63;
       if (c < nb)
-        st_async(dsmem(&crow[(par * kPanelCluster + q) * 64 + c], dst),
+        st_async(dsmem(&crow[(par * CL + q) * 64 + c], dst),
                  bi >= 0 ? P[(bi - r0) * kPanelLd + c] : cx<T>(), dsmem(&colbar[par], dst));
     }
     if (q == qj)
-      for (int e = tid; e < kPanelCluster * 64; e += blockDim.x) {
+      for (int e = tid; e < CL * 64; e += blockDim.x) {
         const int dst = e >> 6, c = e & 63;
         if (c < nb)
           st_async(dsmem(&jrow[par * 64 + c], dst), P[(row_j - r0) * kPanelLd + c], dsmem(&colbar[par], dst));
@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_cluster_kernel(Cluster
     T v = T(-1);
     int p = -1, src = -1;
 #pragma unroll
-    for (int k = 0; k < kPanelCluster; ++k) {
+    for (int k = 0; k < CL; ++k) {
       const PivCand<T> c = cand[par][k];
       if (piv_better(c.val, c.idx, v, p)) {
         v = c.val;
@@ -464,7 +464,7 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_cluster_kernel(Cluster
       src = -1;
     }
     if (tid == 0 && q == 0) a.ipiv[row_j] = p;
-    const cx<T>* urow = src >= 0 ? crow + (par * kPanelCluster + src) * 64 : jrow + par * 64;
+    const cx<T>* urow = src >= 0 ? crow + (par * CL + src) * 64 : jrow + par * 64;
     if (p != row_j) {
       if (p >= r0 && p < r1)
         for (int c = tid; c < nb; c += blockDim.x) P[(p - r0) * kPanelLd + c] = jrow[par * 64 + c];
@@ -862,42 +862,60 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
     int rc = lu_tc_prepare(ctx, n, nb);
     if (rc) return rc;
   }
-  // the cluster panel: largest trailing size whose rows fit in 16 CTAs
-  int cluster_rows = 0;
+  // the cluster panel: the smallest cluster (4, 8 or 16 CTAs) whose shared
+  // memory holds the trailing rows; the exchange per column grows with the
+  // square of the cluster size, and small clusters are easier to place next
+  // to the kernels of concurrent sweeps
+  int cl_rows[3] = {0, 0, 0};  // rows that fit in clusters of 4, 8, 16
   {
     int optin = 0;
     M25_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
     const size_t avail = (size_t)optin - 1024;  // static shared variables
-    const int R = nb > 64 ? 0
-                          : (int)((avail - cluster_panel_smem<T>(0)) / ((size_t)kPanelLd * sizeof(cx<T>)));
+    auto rows_of = [&](size_t smem0) {
+      return nb > 64 ? 0 : (int)((avail - smem0) / ((size_t)kPanelLd * sizeof(cx<T>)));
+    };
     // decided once (thread-safe initialisation: sweeps on several threads)
     static const bool ok = [avail] {
       bool yes = false;
       const char* off = getenv("M25_NO_CLUSTER_PANEL");
       if (!(off && *off == '1') &&
-          cudaFuncSetAttribute(panel_cluster_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+          cudaFuncSetAttribute(panel_cluster_kernel<T, 16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
               cudaSuccess &&
-          cudaFuncSetAttribute(panel_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)avail) ==
+          cudaFuncSetAttribute(panel_cluster_kernel<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)avail) ==
+              cudaSuccess &&
+          cudaFuncSetAttribute(panel_cluster_kernel<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)avail) ==
+              cudaSuccess &&
+          cudaFuncSetAttribute(panel_cluster_kernel<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)avail) ==
               cudaSuccess) {
         cudaLaunchConfig_t cfg = {};
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = kPanelCluster;
+        at[0].val.clusterDim.x = 16;
         at[0].val.clusterDim.y = 1;
         at[0].val.clusterDim.z = 1;
-        cfg.gridDim = dim3(kPanelCluster);
+        cfg.gridDim = dim3(16);
         cfg.blockDim = dim3(kPanelThreads);
         cfg.dynamicSmemBytes = avail;
         cfg.attrs = at;
         cfg.numAttrs = 1;
         int nclusters = 0;
-        yes = cudaOccupancyMaxActiveClusters(&nclusters, panel_cluster_kernel<T>, &cfg) == cudaSuccess &&
+        yes = cudaOccupancyMaxActiveClusters(&nclusters, panel_cluster_kernel<T, 16>, &cfg) == cudaSuccess &&
               nclusters > 0;
       }
       cudaGetLastError();  // a refused attribute only means: no cluster panel
       return yes;
     }();
-    if (ok && R > 0) cluster_rows = kPanelCluster * R;
+    // M25_PANEL_CLUSTER_MIN: the smallest cluster size used (4, 8 or 16; a tuning knob)
+    static const int cl_min = [] {
+      const char* e = getenv("M25_PANEL_CLUSTER_MIN");
+      const int v = e ? atoi(e) : 4;
+      return v >= 16 ? 16 : v >= 8 ? 8 : 4;
+    }();
+    if (ok) {
+      cl_rows[0] = cl_min <= 4 ? 4 * rows_of(cluster_panel_smem<T, 4>(0)) : 0;
+      cl_rows[1] = cl_min <= 8 ? 8 * rows_of(cluster_panel_smem<T, 8>(0)) : 0;
+      cl_rows[2] = 16 * rows_of(cluster_panel_smem<T, 16>(0));
+    }
   }
   for (int k0 = 0; k0 < n; k0 += nb) {
     const int w = std::min(nb, n - k0);
@@ -911,25 +929,29 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
       int rc = lu_tc_operands(ctx, n, k0, w, &A2, &B2, &P2);
       if (rc) return rc;
     }
-    const bool cluster_panel = m <= cluster_rows;
+    const int CL = m <= cl_rows[0] ? 4 : m <= cl_rows[1] ? 8 : m <= cl_rows[2] ? 16 : 0;
+    const bool cluster_panel = CL > 0;
     if (cluster_panel) {
-      ClusterPanelArgs<T> ca{A,   lda, n, k0, w, (m + kPanelCluster - 1) / kPanelCluster, ipiv, info, err,
-                             A2, P2};
-      const size_t smem = cluster_panel_smem<T>(ca.rows_per_cta);
+      ClusterPanelArgs<T> ca{A, lda, n, k0, w, (m + CL - 1) / CL, ipiv, info, err, A2, P2};
+      const size_t smem = CL == 4    ? cluster_panel_smem<T, 4>(ca.rows_per_cta)
+                          : CL == 8 ? cluster_panel_smem<T, 8>(ca.rows_per_cta)
+                                    : cluster_panel_smem<T, 16>(ca.rows_per_cta);
       cudaLaunchConfig_t cfg = {};
       cudaLaunchAttribute at[1];
       at[0].id = cudaLaunchAttributeClusterDimension;
-      at[0].val.clusterDim.x = kPanelCluster;
+      at[0].val.clusterDim.x = CL;
       at[0].val.clusterDim.y = 1;
       at[0].val.clusterDim.z = 1;
-      cfg.gridDim = dim3(kPanelCluster);
+      cfg.gridDim = dim3(CL);
       cfg.blockDim = dim3(kPanelThreads);
       cfg.dynamicSmemBytes = smem;
       cfg.stream = st;
       cfg.attrs = at;
       cfg.numAttrs = 1;
       StageTimer tm(ctx, ST_PANEL);
-      M25_CUDA(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T>, ca));
+      if (CL == 4) M25_CUDA(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T, 4>, ca));
+      else if (CL == 8) M25_CUDA(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T, 8>, ca));
+      else M25_CUDA(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T, 16>, ca));
     } else {
     // grid size: as many CTAs as can be co-resident, each with >= 1 row
     int occ = 0;
