@@ -10,7 +10,7 @@
 // a 3x3 block of half-basis values, written to the scratch H laid out
 // [source half-basis][test half-basis slot] so the 32 lanes store one
 // contiguous run per source half-basis.
-// Stage 2 (gather_kernel): each RWG entry sums its 2 x 2 half-basis values
+// Stage 2 (gather_sym_kernel): each RWG entry sums its 2 x 2 half-basis values
 // and the symmetrisation 0.5 (Z + Z^T) is applied, so every Z entry has a
 // single writer (no atomics).
 // Stage 3 (via_rows_kernel, via_block_kernel): rows / columns of the via
@@ -493,41 +493,73 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
 // SPLIT (mixed precision without vias): Z itself is not stored but its
 // double-float planes Zh = fl32(Z), Zl = fl32(Z - Zh) (rows nb apart) and the
 // complex64 LU input (Zh, rows ldl apart).
-template <class T, class TO, bool SPLIT = false>
-__global__ void gather_kernel(int nb, const cx<T>* __restrict__ H, int64_t ldh, const int32_t* __restrict__ etri,
-                              const int32_t* __restrict__ eloc, const int32_t* __restrict__ tpos,
-                              cx<TO>* __restrict__ Z, int64_t ldz, zf* __restrict__ Zh = nullptr,
-                              zf* __restrict__ Zl = nullptr, zf* __restrict__ LU = nullptr, int64_t ldl = 0) {
-  int nn = blockIdx.x * blockDim.x + threadIdx.x;
-  int m = blockIdx.y;
-  if (nn >= nb) return;
-  int64_t rm[2], cm[2], rn[2], cn[2];
+// Each pair (m, n) of the upper triangle is formed once: one
+// CTA per 32 x 32 tile (tile row <= tile column) computes Z[m][n] and writes
+// it to Z[n][m] as well through a shared-memory transpose, which halves the
+// scattered reads of H (Z is symmetric by construction). Diagonal tiles form
+// all their entries directly.
+template <class T, class TO, bool SPLIT>
+__global__ void __launch_bounds__(256) gather_sym_kernel(int nb, const cx<T>* __restrict__ H, int64_t ldh,
+                                                         const int32_t* __restrict__ etri,
+                                                         const int32_t* __restrict__ eloc,
+                                                         const int32_t* __restrict__ tpos, cx<TO>* __restrict__ Z,
+                                                         int64_t ldz, zf* __restrict__ Zh, zf* __restrict__ Zl,
+                                                         zf* __restrict__ LU, int64_t ldl) {
+  const int tm = blockIdx.y, tn = blockIdx.x;
+  if (tm > tn) return;
+  __shared__ cx<T> tile[32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  auto store = [&](int m, int n, cx<T> z) {
+    if constexpr (SPLIT) {
+      const float hr = (float)z.re, hi = (float)z.im;
+      const zf hv(hr, hi);
+      Zh[(int64_t)m * nb + n] = hv;
+      Zl[(int64_t)m * nb + n] = zf((float)(z.re - (double)hr), (float)(z.im - (double)hi));
+      LU[(int64_t)m * ldl + n] = hv;
+    } else {
+      Z[(int64_t)m * ldz + n] = cx<TO>(z);
+    }
+  };
+  const int nn = tn * 32 + tx;
+  const bool nok = nn < nb;
+  int64_t rn[2], cn[2];
 #pragma unroll
   for (int a = 0; a < 2; ++a) {
-    int tmi = etri[2 * m + a], lmi = eloc[2 * m + a];
-    int tni = etri[2 * nn + a], lni = eloc[2 * nn + a];
-    rm[a] = 3 * (int64_t)tmi + lmi;
-    cm[a] = 3 * (int64_t)tpos[tmi] + lmi;
+    const int tni = nok ? etri[2 * nn + a] : 0, lni = nok ? eloc[2 * nn + a] : 0;
     rn[a] = 3 * (int64_t)tni + lni;
-    cn[a] = 3 * (int64_t)tpos[tni] + lni;
+    cn[a] = 3 * (int64_t)(nok ? tpos[tni] : 0) + lni;
   }
-  cx<T> s1, s2;
 #pragma unroll
-  for (int a = 0; a < 2; ++a)
+  for (int k = 0; k < 4; ++k) {
+    const int m = tm * 32 + ty + 8 * k;
+    cx<T> z;
+    if (nok && m < nb) {
+      int64_t rm[2], cm[2];
 #pragma unroll
-    for (int b = 0; b < 2; ++b) {
-      s1 += H[rn[b] * ldh + cm[a]];  // test m, source n
-      s2 += H[rm[a] * ldh + cn[b]];  // test n, source m
+      for (int a = 0; a < 2; ++a) {
+        const int tmi = etri[2 * m + a], lmi = eloc[2 * m + a];
+        rm[a] = 3 * (int64_t)tmi + lmi;
+        cm[a] = 3 * (int64_t)tpos[tmi] + lmi;
+      }
+      cx<T> s1, s2;
+#pragma unroll
+      for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+          s1 += H[rn[b] * ldh + cm[a]];  // test m, source n
+          s2 += H[rm[a] * ldh + cn[b]];  // test n, source m
+        }
+      z = (s1 + s2) * T(0.5);
+      store(m, nn, z);
     }
-  cx<T> z = (s1 + s2) * T(0.5);
-  if constexpr (SPLIT) {
-    const float hr = (float)z.re, hi = (float)z.im;
-    const zf hv(hr, hi);
-    Zh[(int64_t)m * nb + nn] = hv;
-    Zl[(int64_t)m * nb + nn] = zf((float)(z.re - (double)hr), (float)(z.im - (double)hi));
-    LU[(int64_t)m * ldl + nn] = hv;
-  } else {
-    Z[(int64_t)m * ldz + nn] = cx<TO>(z);
+    tile[ty + 8 * k][tx] = z;
+  }
+  if (tm == tn) return;  // uniform over the CTA
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int n2 = tn * 32 + ty + 8 * k, m2 = tm * 32 + tx;
+    if (n2 < nb && m2 < nb) store(n2, m2, tile[tx][ty + 8 * k]);
   }
 }
 
@@ -759,16 +791,17 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   M25_CHECK_LAUNCH();
   {
   StageTimer tm(ctx, ST_GATHER);
+  const dim3 gtiles((nb + 31) / 32, (nb + 31) / 32);
   if (split) {
     if (nv || !std::is_same<T, double>::value) {
       set_error("m25_assemble: split output needs the mixed fill without vias");
       return M25_ERR_VALUE;
     }
-    gather_kernel<T, T, true><<<dim3((nb + 127) / 128, nb), 128, 0, st>>>(
-        nb, H, ldh, geom->edge_tri, geom->edge_loc, geom->tpos, nullptr, 0, split->Zh, split->Zl, split->LU, split->ldl);
+    gather_sym_kernel<T, T, true><<<gtiles, 256, 0, st>>>(nb, H, ldh, geom->edge_tri, geom->edge_loc, geom->tpos,
+                                                          nullptr, 0, split->Zh, split->Zl, split->LU, split->ldl);
   } else {
-    gather_kernel<T, T><<<dim3((nb + 127) / 128, nb), 128, 0, st>>>(nb, H, ldh, geom->edge_tri, geom->edge_loc,
-                                                                   geom->tpos, Z, ldzd);
+    gather_sym_kernel<T, T, false><<<gtiles, 256, 0, st>>>(nb, H, ldh, geom->edge_tri, geom->edge_loc, geom->tpos,
+                                                           Z, ldzd, nullptr, nullptr, nullptr, 0);
   }
   }
   M25_CHECK_LAUNCH();
