@@ -308,63 +308,84 @@ __global__ void table_kernel(const StackDev* __restrict__ Sp, int nrho, const do
 // the nodal slopes, solved by forward elimination / back substitution), as
 // piecewise coefficients c[interval][p] of (r - x_i)^(3-p).
 // coef layout (pair, interval, power, {A, V, W}).
-__global__ void spline_kernel(int L, int nrho, const double* __restrict__ x, const zd* __restrict__ Stab,
-                              zd* __restrict__ work, zd* __restrict__ coef) {
-  int col = blockIdx.x * blockDim.x + threadIdx.x;
-  const int NC = 3 * L * L;
-  if (col >= NC) return;
+// One CTA per column: radii, values and the sweep's arrays in shared memory
+// (the elimination is a chain of dependent steps: it runs on one thread from
+// shared memory), the coefficients of the intervals in parallel.
+__host__ __device__ inline size_t spline_smem(int n) { return (size_t)n * (2 * sizeof(double) + 4 * sizeof(zd)); }
+
+__global__ void __launch_bounds__(128) spline_kernel(int L, int nrho, const double* __restrict__ xg,
+                                                     const zd* __restrict__ Stab, zd* __restrict__ coef) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int col = blockIdx.x;
   const int n = nrho;
-  const zd* y = Stab + (int64_t)col * n;
-  zd* s = work + (int64_t)col * 2 * n;  // slopes
-  zd* cp = s + n;                       // modified upper diagonal (real part only used)
-  // rows: a_i s_{i-1} + b_i s_i + c_i s_{i+1} = d_i
-  auto dxf = [&](int i) { return x[i + 1] - x[i]; };
-  auto slope = [&](int i) { return (y[i + 1] - y[i]) / dxf(i); };
-  // forward sweep
-  double bprev = 0, cprev = 0;
-  for (int i = 0; i < n; ++i) {
-    double a, b, c;
-    zd d;
-    if (i == 0) {
-      double dx0 = dxf(0), dx1 = dxf(1), d0 = x[2] - x[0];
-      a = 0;
-      b = dx1;
-      c = d0;
-      d = (slope(0) * ((dx0 + 2 * d0) * dx1) + slope(1) * (dx0 * dx0)) / d0;
-    } else if (i == n - 1) {
-      double dxl = dxf(n - 2), dxm = dxf(n - 3), d1 = x[n - 1] - x[n - 3];
-      a = d1;
-      b = dxm;
-      c = 0;
-      d = (slope(n - 3) * (dxl * dxl) + slope(n - 2) * ((2 * d1 + dxl) * dxm)) / d1;
-    } else {
-      a = dxf(i);
-      b = 2 * (dxf(i - 1) + dxf(i));
-      c = dxf(i - 1);
-      d = (slope(i - 1) * dxf(i) + slope(i) * dxf(i - 1)) * 3.0;
-    }
-    if (i > 0) {
-      double mlt = a / bprev;
-      b -= mlt * cprev;
-      d -= s[i - 1] * mlt;
-    }
-    s[i] = d;        // holds the modified rhs
-    cp[i] = zd(b);   // modified diagonal
-    bprev = b;
-    cprev = c;
-    if (i < n - 1) cp[i].im = c;
+  zd* y = reinterpret_cast<zd*>(smem_raw);  // (n) values
+  zd* s = y + n;                            // (n) slopes
+  zd* cp = s + n;                           // (n) modified diagonal (re), upper diagonal (im)
+  zd* sl = cp + n;                          // (n - 1) secant slopes
+  double* x = reinterpret_cast<double*>(sl + n);
+  double* dx = x + n;                       // (n - 1) interval widths
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    x[i] = xg[i];
+    y[i] = Stab[(int64_t)col * n + i];
   }
-  // back substitution
-  s[n - 1] = s[n - 1] / cp[n - 1].re;
-  for (int i = n - 2; i >= 0; --i) s[i] = (s[i] - s[i + 1] * cp[i].im) / cp[i].re;
-  int pair = col % (L * L), m = col / (L * L);
-  for (int i = 0; i < n - 1; ++i) {
-    double dx = dxf(i);
-    zd sl = slope(i);
-    zd t = (s[i] + s[i + 1] - sl * 2.0) / dx;
+  __syncthreads();
+  // the widths and secant slopes (independent of the recurrence), in parallel
+  for (int i = threadIdx.x; i < n - 1; i += blockDim.x) {
+    dx[i] = x[i + 1] - x[i];
+    sl[i] = (y[i + 1] - y[i]) / dx[i];
+  }
+  __syncthreads();
+  // rows: a_i s_{i-1} + b_i s_i + c_i s_{i+1} = d_i
+  auto dxf = [&](int i) { return dx[i]; };
+  auto slope = [&](int i) { return sl[i]; };
+  if (threadIdx.x == 0) {
+    // forward sweep
+    double bprev = 0, cprev = 0;
+    for (int i = 0; i < n; ++i) {
+      double a, b, c;
+      zd d;
+      if (i == 0) {
+        double dx0 = dxf(0), dx1 = dxf(1), d0 = x[2] - x[0];
+        a = 0;
+        b = dx1;
+        c = d0;
+        d = (slope(0) * ((dx0 + 2 * d0) * dx1) + slope(1) * (dx0 * dx0)) / d0;
+      } else if (i == n - 1) {
+        double dxl = dxf(n - 2), dxm = dxf(n - 3), d1 = x[n - 1] - x[n - 3];
+        a = d1;
+        b = dxm;
+        c = 0;
+        d = (slope(n - 3) * (dxl * dxl) + slope(n - 2) * ((2 * d1 + dxl) * dxm)) / d1;
+      } else {
+        a = dxf(i);
+        b = 2 * (dxf(i - 1) + dxf(i));
+        c = dxf(i - 1);
+        d = (slope(i - 1) * dxf(i) + slope(i) * dxf(i - 1)) * 3.0;
+      }
+      if (i > 0) {
+        double mlt = a / bprev;
+        b -= mlt * cprev;
+        d -= s[i - 1] * mlt;
+      }
+      s[i] = d;       // holds the modified rhs
+      cp[i] = zd(b);  // modified diagonal
+      bprev = b;
+      cprev = c;
+      if (i < n - 1) cp[i].im = c;
+    }
+    // back substitution
+    s[n - 1] = s[n - 1] / cp[n - 1].re;
+    for (int i = n - 2; i >= 0; --i) s[i] = (s[i] - s[i + 1] * cp[i].im) / cp[i].re;
+  }
+  __syncthreads();
+  const int pair = col % (L * L), m = col / (L * L);
+  for (int i = threadIdx.x; i < n - 1; i += blockDim.x) {
+    const double h = dx[i];
+    const zd si = sl[i];
+    zd t = (s[i] + s[i + 1] - si * 2.0) / h;
     zd* o = coef + (((int64_t)pair * (n - 1) + i) * 4) * 3;
-    o[0 * 3 + m] = t / dx;
-    o[1 * 3 + m] = (sl - s[i]) / dx - t;
+    o[0 * 3 + m] = t / h;
+    o[1 * 3 + m] = (si - s[i]) / h - t;
     o[2 * 3 + m] = s[i];
     o[3 * 3 + m] = y[i];
   }
@@ -526,7 +547,7 @@ extern "C" int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* d, m25_gre
   int rc = M25_OK;
   StackDev* Sd = nullptr;
   double *kc = nullptr, *wc = nullptr, *kr = nullptr, *wr = nullptr;
-  zd *cc = nullptr, *cr = nullptr, *res = nullptr, *work = nullptr;
+  zd *cc = nullptr, *cr = nullptr, *res = nullptr;
   std::vector<void*> tmp;
   const int n = d->nrho;
 #define TRY(x)         \
@@ -545,7 +566,6 @@ extern "C" int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* d, m25_gre
   g->res = res;
   TRY(alloc_async(g->allocs, &g->sur, 16, st));
   M25_CUDA(cudaMemsetAsync(g->sur, 0, 16, st));
-  TRY(alloc_async(tmp, (void**)&work, sizeof(zd) * (size_t)NC * 2 * n, st));
   TRY(alloc_async(g->allocs, (void**)&g->rho, sizeof(double) * n, st));
   TRY(alloc_async(g->allocs, (void**)&g->rho32, sizeof(float) * n, st));
   TRY(alloc_async(g->allocs, (void**)&g->S, sizeof(zd) * (size_t)NC * n, st));
@@ -615,7 +635,14 @@ extern "C" int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* d, m25_gre
   }
   table_kernel<<<(NC * n + 127) / 128, 128, 0, st>>>(Sd, n, g->rho, res, omega, zd(d->zs_ground_re, d->zs_ground_im),
                                                    reinterpret_cast<zd*>(g->S));
-  spline_kernel<<<1, 32, 0, st>>>(L, n, g->rho, reinterpret_cast<zd*>(g->S), work, reinterpret_cast<zd*>(g->coef));
+  if (spline_smem(n) > 200 * 1024) {
+    set_error("m25_greens_create: too many tabulation radii for the spline in shared memory");
+    rc = M25_ERR_VALUE;
+    goto fail;
+  }
+  M25_CUDA(cudaFuncSetAttribute(spline_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+  spline_kernel<<<NC, 128, spline_smem(n), st>>>(L, n, g->rho, reinterpret_cast<zd*>(g->S),
+                                                 reinterpret_cast<zd*>(g->coef));
   {
     int64_t nc = (int64_t)L * L * (n - 1) * 12 * 2;
     to_f32_kernel<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(g->coef, g->coef32, nc);
