@@ -44,7 +44,7 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
 template <class T> int lu_factor(m25_ctx*, cx<T>*, int64_t, int, int32_t*, int, bool, int*);
 int refine(m25_ctx*, int, int, const zf*, const zf*, int64_t, const zf*, int64_t, const int32_t*, const zd*, zd*,
            double, int, int*);
-void split_to_z32(m25_ctx*, const zd*, int64_t, zf*, int64_t, zf*, zf*, int64_t, int, int);
+void split_to_z32(m25_ctx*, const zd*, int64_t, zf*, int64_t, zf*, zf*, int64_t, int, int, double*, zd*, int);
 bool lu_tc_available();
 template <class TF, class TV>
 int lu_solve_wave(m25_ctx*, const cx<TF>*, int64_t, int, const int32_t*, const cx<TV>*, int, cx<TV>*,
@@ -310,7 +310,10 @@ static int dense_solve_impl(m25_ctx* ctx, int32_t n, int32_t nrhs, int precision
     } else {
       if ((rc = ctx->Zsplit.ensure(sizeof(zf) * 2 * nn))) return rc;
       zf* h = ctx->Zsplit.as<zf>();
-      split_to_z32(ctx, static_cast<const zd*>(Zres), n, LU, ldl, h, h + nn, n, n, n);
+      // rows equilibrated by powers of two (B with them; X unchanged)
+      if ((rc = ctx->sched.ensure(256 + sizeof(double) * (size_t)n))) return rc;
+      double* rs = reinterpret_cast<double*>(ctx->sched.as<char>() + 256);
+      split_to_z32(ctx, static_cast<const zd*>(Zres), n, LU, ldl, h, h + nn, n, n, n, rs, Bd, nrhs);
       Zh = h;
       Zl = h + nn;
     }

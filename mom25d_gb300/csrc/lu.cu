@@ -15,6 +15,7 @@
 // Solve: permutation, blocked forward / backward substitution. The mixed
 // path refines in fp64: r = B - Z X, X += LU32^-1 r.
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -1569,12 +1570,41 @@ __global__ void split_z64_kernel(int64_t n, const zd* __restrict__ X, zf* __rest
 
 // the same for an n x m block of a matrix (leading dimensions lda / ldb),
 // also writing the hi plane to a second destination (the LU's input, ldlu)
+// Row equilibration of the mixed solve: rs[r] = 2^-e with max_c |Z[r][c]|
+// (|re| + |im|) in [2^(e-1), 2^e): scaling by powers of two is exact, and
+// rows of very different size (the via unknowns' rows next to the RWG rows)
+// no longer hide the RWG rows' residuals in the normwise backward error.
+__global__ void row_scale_kernel(int n, const zd* __restrict__ a, int64_t lda, double* __restrict__ rs) {
+  const int r = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (r >= n) return;
+  double mx = 0.0;
+  for (int c = lane; c < n; c += 32) {
+    const zd x = a[(int64_t)r * lda + c];
+    mx = fmax(mx, fabs(x.re) + fabs(x.im));
+  }
+  for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) {
+    int e = 0;
+    frexp(mx, &e);
+    rs[r] = mx > 0.0 && isfinite(mx) ? ldexp(1.0, -e) : 1.0;
+  }
+}
+
+__global__ void scale_rows_kernel(int64_t n, int P, const double* __restrict__ rs, zd* __restrict__ B) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * P) return;
+  const double s = rs[e / P];
+  B[e] = zd(B[e].re * s, B[e].im * s);
+}
+
 __global__ void split_matrix_kernel(const zd* __restrict__ a, int64_t lda, zf* __restrict__ lu, int64_t ldlu,
-                                    zf* __restrict__ h, zf* __restrict__ l, int64_t ldb, int n, int m) {
+                                    zf* __restrict__ h, zf* __restrict__ l, int64_t ldb, int n, int m,
+                                    const double* __restrict__ rs) {
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (int64_t)n * m) return;
   const int64_t r = e / m, c = e % m;
-  const zd x = a[r * lda + c];
+  zd x = a[r * lda + c];
+  if (rs) x = zd(x.re * rs[r], x.im * rs[r]);
   const float hr = (float)x.re, hi = (float)x.im;
   const zf hv(hr, hi);
   lu[r * ldlu + c] = hv;
@@ -1814,10 +1844,16 @@ int refine(m25_ctx* ctx, int n, int P, const zf* Zh, const zf* Zl, int64_t ldz, 
     if ((rc = col_norms(X, xn))) return rc;
     double worst = 0;
     std::vector<double> target(P);
+    bool finite = std::isfinite(znorm);
     for (int c = 0; c < P; ++c) {
       double den = znorm * xn[c] + bn[c];
       target[c] = tol * den;
+      finite = finite && std::isfinite(rn[c]) && std::isfinite(xn[c]);
       worst = std::max(worst, den > 0 ? rn[c] / den : 0.0);
+    }
+    if (!finite) {  // an overflow in the complex64 factors or solves: never "converged"
+      set_error("mixed solve: non-finite residual or solution (complex64 LU overflow?)");
+      return M25_ERR_NUMERIC;
     }
     if (worst <= tol) break;
     const bool stalled = worst > 0.5 * prev_worst;
@@ -1915,10 +1951,16 @@ int refine(m25_ctx* ctx, int n, int P, const zf* Zh, const zf* Zl, int64_t ldz, 
 
 
 
+// rs (n doubles, device) or null: the rows are equilibrated by powers of two
+// (row_scale_kernel), and the right-hand sides B (n x P) with them
 void split_to_z32(m25_ctx* ctx, const zd* a, int64_t lda, zf* lu, int64_t ldlu, zf* h, zf* l, int64_t ldb, int n,
-                  int m) {
+                  int m, double* rs, zd* B, int P) {
   int64_t tot = (int64_t)n * m;
-  split_matrix_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(a, lda, lu, ldlu, h, l, ldb, n, m);
+  if (rs) {
+    row_scale_kernel<<<(unsigned)(((int64_t)n * 32 + 255) / 256), 256, 0, ctx->stream>>>(n, a, lda, rs);
+    scale_rows_kernel<<<(unsigned)(((int64_t)n * P + 255) / 256), 256, 0, ctx->stream>>>(n, P, rs, B);
+  }
+  split_matrix_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(a, lda, lu, ldlu, h, l, ldb, n, m, rs);
 }
 
 }  // namespace m25

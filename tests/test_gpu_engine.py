@@ -265,6 +265,18 @@ def test_lpf_headline_workload_matches_reference(gpu):
         sol.close()
 
 
+@pytest.mark.parametrize("name", ["shunt_via", "via"])
+def test_mixed_sweep_with_vias_matches_reference(gpu, name):
+    """The mixed precision with via unknowns (the fill writes a complex128 Z,
+    split for the complex64 LU and the refinement) within 1e-5 of mom25d."""
+    g = golden(name)
+    lay, st, m, _ = build(name)
+    sol = Solver(m, st, verbose=False, precision="mixed")
+    r = sol.sweep(g["freqs"])
+    assert np.abs(r.S - g["S"]).max() < 1e-5
+    sol.close()
+
+
 def test_via_transition_sweep_matches_reference(gpu):
     g = golden("via")
     lay, st, m, _ = build("via")
