@@ -63,6 +63,8 @@ int m25_version(void);
 int m25_ctx_create(int device, m25_ctx** out);
 int m25_ctx_destroy(m25_ctx* ctx);
 int m25_ctx_synchronize(m25_ctx* ctx);
+/* free and total device memory of the context's device, in bytes */
+int m25_ctx_mem_info(m25_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes);
 void* m25_ctx_stream(m25_ctx* ctx); /* the cudaStream_t every call of this context runs on */
 
 /* Stage timers: CUDA events recorded on the context's stream around the

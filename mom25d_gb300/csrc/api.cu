@@ -120,6 +120,19 @@ extern "C" int m25_ctx_synchronize(m25_ctx* c) {
 
 extern "C" void* m25_ctx_stream(m25_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
+extern "C" int m25_ctx_mem_info(m25_ctx* c, uint64_t* free_bytes, uint64_t* total_bytes) {
+  if (!c) {
+    set_error("m25_ctx_mem_info: null context");
+    return M25_ERR_VALUE;
+  }
+  M25_CUDA(cudaSetDevice(c->device));
+  size_t f = 0, t = 0;
+  M25_CUDA(cudaMemGetInfo(&f, &t));
+  if (free_bytes) *free_bytes = f;
+  if (total_bytes) *total_bytes = t;
+  return M25_OK;
+}
+
 namespace m25 {
 cudaEvent_t take_event(m25_ctx* c) {
   if (!c->event_pool.empty()) {

@@ -27,7 +27,8 @@ EXPORTS = ("m25_last_error", "m25_version", "m25_ctx_create", "m25_ctx_destroy",
            "m25_greens_create", "m25_greens_destroy", "m25_greens_tables", "m25_assemble", "m25_dense_solve",
            "m25_ports_create", "m25_ports_destroy", "m25_deembed", "m25_sweep_point", "m25_deembed_debug",
            "m25_ctx_timing", "m25_dense_solve_noalloc", "m25_lu_factor", "m25_greens_remainder", "m25_mlp_create",
-           "m25_mlp_destroy", "m25_mlp_params", "m25_mlp_loss_grad", "m25_mlp_train", "m25_mlp_forward")
+           "m25_mlp_destroy", "m25_mlp_params", "m25_mlp_loss_grad", "m25_mlp_train", "m25_mlp_forward",
+           "m25_ctx_mem_info")
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
@@ -99,6 +100,7 @@ def load():
     lib.m25_dense_solve_noalloc.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, vp, vp, _i32p]
     lib.m25_lu_factor.argtypes = [vp, C.c_int32, C.c_int, vp, C.c_int64, _i32p, C.c_int, C.c_int32, _i32p]
     lib.m25_greens_remainder.argtypes = [vp, _f64p, _f64p]
+    lib.m25_ctx_mem_info.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     f32p = C.POINTER(C.c_float)
     lib.m25_mlp_create.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(vp)]
     lib.m25_mlp_destroy.argtypes = [vp]

@@ -510,6 +510,32 @@ class Solver:
                 self._siblings.append(self._clone())
             return self._siblings[i - 1]
 
+    def _worker_bytes(self):
+        """Device memory of one more worker: fill scratch, the matrix planes
+        and LU copy (or the complex128 Z), geometry and per-point buffers."""
+        mesh = self.mesh
+        nt, N = int(mesh.tri_layer.size), int(mesh.n_unknowns)
+        nv = N - int(mesh.n_basis)
+        nblocks = (nt + 31) // 32 + len(mesh.layer_names)
+        elem = 8 if self.precision == "mixed_fill32" else 16
+        b = elem * 3 * nt * nblocks * 96                # fill scratch H
+        if self.precision == "fp64":
+            b += 16 * N * N                             # Z, factored in place
+        else:
+            b += 24 * N * (N + 1)                       # Zh, Zl, complex64 LU
+            if nv or self.precision == "mixed_fill32":
+                b += elem * N * N                       # Z as filled (split after)
+        b += 4 * nblocks * nt + 48 * 1024 * N           # classes, near-pair data (bound), vectors
+        return b
+
+    def _workers_that_fit(self):
+        """Workers that fit: those that exist already (this solver and its
+        siblings hold their buffers) plus those whose buffers fit in the free
+        device memory."""
+        free, total = C.c_uint64(), C.c_uint64()
+        E.check(self.ctx.lib.m25_ctx_mem_info(self.ctx.h, C.byref(free), C.byref(total)))
+        return 1 + len(self._siblings) + int(0.9 * free.value // max(1, self._worker_bytes()))
+
     def sweep(self, freqs, keep_currents=False, interp=None, values=None, checkpoint=None, wait_memory=None,
               workers=1):
         """S-parameters at freqs (exact fill at every frequency). checkpoint:
@@ -519,7 +545,8 @@ class Solver:
         and stream, driven by its own host thread (the latency-bound stages of
         one point - LU panels, triangular solves, the wave fit - leave most of
         the GPU to the others); points are handed out in order as workers
-        become free."""
+        become free. Fewer workers run when their buffers would not fit in
+        the free device memory (result.info["workers"])."""
         if interp not in (None, "auto"):
             raise ValueError("this engine fills every frequency exactly (interp=None)")
         freqs = np.atleast_1d(np.asarray(freqs, float))
@@ -545,7 +572,7 @@ class Solver:
                 done[:] = False
         steps = [None] * nf
         todo = [fi for fi in range(nf) if not done[fi]]
-        workers = max(1, min(int(workers), len(todo) or 1))
+        workers = max(1, min(int(workers), len(todo) or 1, self._workers_that_fit()))
         lock = threading.Lock()
         nxt = [0]
         errors = []
