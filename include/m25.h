@@ -276,7 +276,9 @@ int m25_deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* ports, 
  * every intermediate on the device: fill (precision), solve of the port
  * excitations, de-embedding. x_out (n, P) complex128 host copy of the
  * currents or NULL; S, z0, gamma, z0_line, resid as m25_deembed; info[0]
- * refinement steps, info[1] zero pivot. */
+ * refinement steps, info[1] zero pivot. When the mixed refinement does not
+ * reach tol (the complex64 LU too inaccurate at that frequency) the point is
+ * recomputed on the fp64 path and info[0] = -1. */
 int m25_sweep_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* ports, double zs_re, double zs_im,
                     double zsv_re, double zsv_im, int precision, const double* beta0, double tol, int32_t max_iter,
                     double* x_out, double* S, double* z0, double* gamma, double* z0_line, double* resid,

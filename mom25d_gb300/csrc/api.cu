@@ -101,7 +101,7 @@ extern "C" int m25_ctx_destroy(m25_ctx* c) {
   if (!c) return M25_OK;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
-  for (DevBuf* b : {&c->H, &c->Zw, &c->Zlu, &c->Bw, &c->Xw, &c->Rw, &c->Dw, &c->ipiv, &c->scratch, &c->deemb,
+  for (DevBuf* b : {&c->H, &c->Zw, &c->Zlu, &c->Zsplit, &c->Bw, &c->Xw, &c->Rw, &c->Dw, &c->ipiv, &c->scratch, &c->deemb,
                     &c->Zsweep, &c->Xsweep, &c->flags, &c->sched})
     b->release();
   cudaStreamDestroy(c->stream);

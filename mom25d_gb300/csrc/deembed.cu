@@ -870,22 +870,42 @@ extern "C" int m25_sweep_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25
   int32_t inf[2] = {0, 0};
   if (precision == M25_MIXED && geom->nv == 0) {
     // fill straight into the solve's double-float planes (no complex128 Z)
-    if ((rc = fill_solve_mixed(ctx, geom, gr, zd(zs_re, zs_im), zd(zsv_re, zsv_im), P, p->Bexc, ctx->Xsweep.as<zd>(),
-                               tol, max_iter, inf)))
-      return rc;
+    rc = fill_solve_mixed(ctx, geom, gr, zd(zs_re, zs_im), zd(zsv_re, zsv_im), P, p->Bexc, ctx->Xsweep.as<zd>(), tol,
+                          max_iter, inf);
   } else {
     if ((rc = m25_assemble(ctx, geom, gr, zs_re, zs_im, zsv_re, zsv_im, precision, ctx->Zsweep.p, n, M25_ON_DEVICE)))
       return rc;
-    if ((rc = m25_dense_solve(ctx, n, P, precision, ctx->Zsweep.p, p->Bexc, ctx->Xsweep.p, M25_ON_DEVICE, tol,
+    rc = m25_dense_solve(ctx, n, P, precision, ctx->Zsweep.p, p->Bexc, ctx->Xsweep.p, M25_ON_DEVICE, tol, max_iter,
+                         inf);
+  }
+  int used = precision;
+  if (rc == M25_ERR_NUMERIC && precision != M25_FP64) {
+    // the refinement with the complex64 LU did not reach the target (or that
+    // LU met a zero pivot): this point goes through the fp64 path
+    // (refinement steps reported as -1). The complex64 planes and LU go
+    // first, so the point's peak memory stays that of the mixed path.
+    M25_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->Zsplit.release();
+    ctx->Zlu.release();
+    if ((rc = ctx->Zsweep.ensure(sizeof(zd) * (size_t)n * n))) return rc;
+    if ((rc = m25_assemble(ctx, geom, gr, zs_re, zs_im, zsv_re, zsv_im, M25_FP64, ctx->Zsweep.p, n, M25_ON_DEVICE)))
+      return rc;
+    inf[0] = inf[1] = 0;
+    if ((rc = m25_dense_solve(ctx, n, P, M25_FP64, ctx->Zsweep.p, p->Bexc, ctx->Xsweep.p, M25_ON_DEVICE, tol,
                               max_iter, inf)))
       return rc;
+    inf[0] = -1;
+    used = M25_FP64;
+    M25_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (geom->nv == 0) ctx->Zsweep.release();
   }
+  if (rc) return rc;
   if (info) {
     info[0] = inf[0];
     info[1] = inf[1];
   }
   if ((rc = deembed(ctx, geom, gr, p, ctx->Xsweep.p, M25_ON_DEVICE, beta0, S, z0, gamma, z0_line, resid,
-                    precision != M25_FP64)))
+                    used != M25_FP64)))
     return rc;
   if (x_out) {
     M25_CUDA(cudaMemcpy(x_out, ctx->Xsweep.p, sizeof(zd) * (size_t)n * P, cudaMemcpyDeviceToHost));

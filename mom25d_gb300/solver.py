@@ -255,7 +255,9 @@ class Solver:
                 fill already moves Z by ~1e-7 relative; at the 1e-12 default
                 the solve adds nothing measurable to S (LPF, N = 5943:
                 max |dS| against the fp64 path 7.8e-7 at 1e-12 and 7.7e-7 at
-                1e-14; 1.0e-5 at 1e-9)
+                1e-14; 1.0e-5 at 1e-9). A point whose refinement stops
+                above the target is recomputed on the fp64 path
+                (refine_steps -1, listed in the sweep's info["fp64_fallback"])
     """
 
     def __init__(self, mesh, substrate, z0=None, verbose=True, method="dense", v_weight=None, precision="fp64",
@@ -461,7 +463,9 @@ class Solver:
             z0 = self.z0_fixed.copy()
             d = np.sqrt(z0)
             S = d[:, None] * SI / d[None, :]
-        return S, z0, gam, zl, res, x, dict(refine_steps=int(info[0]))
+        # refine_steps -1: the mixed refinement did not reach refine_tol and
+        # the point was recomputed on the fp64 path
+        return S, z0, gam, zl, res, x, dict(refine_steps=int(info[0]), fp64_fallback=bool(info[0] < 0))
 
     def last_deembed(self):
         """Intermediates of the last de-embedding on the device: triangle
@@ -483,16 +487,19 @@ class Solver:
         return np.array([len(freqs), float(np.sum(freqs)), float(m.n_unknowns), float(np.sum(m.nodes)),
                          float(np.sum(m.nodes ** 2)), float(len(m.tris)), 0.0])
 
-    _DEVICE_STATE = ("ctx", "_geom", "_ports", "_siblings", "_sib_lock")
+    _DEVICE_STATE = ("ctx", "_geom", "_geom_owner", "_ports", "_siblings", "_sib_lock")
 
     def _clone(self):
         """A solver sharing this one's host-side set-up (mesh, port models,
-        groups, test blocks) with a fresh engine context of its own."""
+        groups, test blocks) and its device geometry (classes, closed-form
+        near-pair data: read-only once built, readable from any stream) with
+        a fresh engine context of its own (stream, per-point buffers, ports)."""
         s = object.__new__(Solver)
         s.__dict__.update({k: v for k, v in self.__dict__.items() if k not in self._DEVICE_STATE})
         s.verbose = False
         s.ctx = E.Context(self.device)
-        s._geom = None
+        s._geom = self.geometry()
+        s._geom_owner = False  # closed by this solver, after its siblings
         s._ports = None
         s._siblings = []
         s._sib_lock = threading.Lock()
@@ -512,7 +519,7 @@ class Solver:
 
     def _worker_bytes(self):
         """Device memory of one more worker: fill scratch, the matrix planes
-        and LU copy (or the complex128 Z), geometry and per-point buffers."""
+        and LU copy (or the complex128 Z) and per-point buffers."""
         mesh = self.mesh
         nt, N = int(mesh.tri_layer.size), int(mesh.n_unknowns)
         nv = N - int(mesh.n_basis)
@@ -525,7 +532,7 @@ class Solver:
             b += 24 * N * (N + 1)                       # Zh, Zl, complex64 LU
             if nv or self.precision == "mixed_fill32":
                 b += elem * N * N                       # Z as filled (split after)
-        b += 4 * nblocks * nt + 48 * 1024 * N           # classes, near-pair data (bound), vectors
+        b += 4096 * N                                   # GMRES vectors, LU scratch (the geometry is shared)
         return b
 
     def _workers_that_fit(self):
@@ -573,6 +580,8 @@ class Solver:
         steps = [None] * nf
         todo = [fi for fi in range(nf) if not done[fi]]
         workers = max(1, min(int(workers), len(todo) or 1, self._workers_that_fit()))
+        if workers > 1:
+            self.geometry()  # built once here, shared by the workers' contexts
         lock = threading.Lock()
         nxt = [0]
         errors = []
@@ -620,7 +629,8 @@ class Solver:
                 t.join()
         if errors:
             raise errors[0]
-        info = dict(seconds=time.time() - t0, refine_steps=[s for s in steps if s is not None], workers=workers)
+        info = dict(seconds=time.time() - t0, refine_steps=[s for s in steps if s is not None], workers=workers,
+                    fp64_fallback=[float(freqs[i]) for i, s in enumerate(steps) if s is not None and s < 0])
         return SweepResult(freqs, S, zr, gam, zl, res, [p.name for p in self.ports],
                            cur if keep_currents else None, info)
 
@@ -628,9 +638,10 @@ class Solver:
         for sib in self._siblings:
             sib.close()
         self._siblings = []
-        for h in (self._ports, self._geom):
-            if h is not None:
-                h.close()
+        if self._ports is not None:
+            self._ports.close()
+        if self._geom is not None and getattr(self, "_geom_owner", True):
+            self._geom.close()
         self._ports = self._geom = None
         self.ctx.close()
 

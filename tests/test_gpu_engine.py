@@ -277,6 +277,24 @@ def test_mixed_sweep_with_vias_matches_reference(gpu, name):
     sol.close()
 
 
+@pytest.mark.parametrize("name", ["line", "via"])
+def test_mixed_point_falls_back_to_fp64(gpu, name):
+    """A refinement target the complex64 LU cannot reach (1e-30 in 8 steps)
+    sends each point through the fp64 fill and LU: the same S as the fp64
+    sweep, refine_steps -1 and every frequency listed as a fallback."""
+    g = golden(name)
+    lay, st, m, _ = build(name)
+    ref = Solver(m, st, verbose=False, precision="fp64")
+    r64 = ref.sweep(g["freqs"])
+    ref.close()
+    sol = Solver(m, st, verbose=False, precision="mixed", refine_tol=1e-30, max_refine=8)
+    r = sol.sweep(g["freqs"])
+    sol.close()
+    assert r.info["refine_steps"] == [-1] * len(g["freqs"])
+    assert r.info["fp64_fallback"] == [float(f) for f in g["freqs"]]
+    assert np.abs(r.S - r64.S).max() < 1e-12
+
+
 def test_via_transition_sweep_matches_reference(gpu):
     g = golden("via")
     lay, st, m, _ = build("via")
