@@ -10,14 +10,21 @@
 //                  rank-1 update of the panel)
 //   swap_trsm_kernel  the panel's row interchanges on the other columns,
 //                  composed into one gather, fused with U12 = L11^-1 A12
-//   gemm_kernel    A22 -= L21 U12 (SIMT), or the tcgen05 tensor-core path
-//                  for complex64 (lu_tc.cu)
+//   gemm_kernel    A22 -= L21 U12 (SIMT)
+// The complex64 factorisation with tensor cores (lu_tc.cu) goes in blocks of
+// 128 columns, each two panels of 64: the first panel's interchanges and
+// U12 on the second panel's columns, their rank-64 update, the second panel,
+// then both panels' interchanges with U12 = L11^-1 A12 (L11 128 x 128) on
+// the trailing columns and one rank-128 update of the trailing matrix. The
+// update is bound by its read-modify-write of the trailing matrix, which
+// this does once per 128 columns.
 // Solve: permutation, blocked forward / backward substitution. The mixed
 // path refines in fp64: r = B - Z X, X += LU32^-1 r.
 #include <algorithm>
 #include <cmath>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "m25_internal.h"
@@ -566,55 +573,84 @@ __global__ void __launch_bounds__(kPanelThreads, 1) panel_cluster_kernel(Cluster
 // 32 columns: it gathers the rows the interchanges touch into shared memory
 // (lane = column), writes them to their final rows, and on the right-hand
 // columns runs the forward substitution with 8 lanes per column, each lane
-// holding 8 of the w <= 64 panel rows (rows l, l + 8, ...): at step t the
+// holding W / 8 of the w <= W panel rows (rows l, l + 8, ...): at step t the
 // lane of row t passes x[t] to the other 7 by a shuffle. Every element
 // takes its subtractions in the order t = 0, 1, ... as in LAPACK's ztrsm.
 // The interchanges are composed, not replayed: the rows touched are the w
 // panel rows and the pivot rows below the panel, and the original row that
 // ends in position x is found by applying the swaps to x in reverse order.
 // (LAPACK zgetrf applies the same swaps one by one through zlaswp.)
+// The CTAs cover the columns vc_begin <= vc < vc_end counted without the
+// panel's (vc < k0: column vc, else column vc + w). W = 128 serves a block
+// of two 64-column panels whose interchanges and L11 are taken together.
 constexpr int kSwapMaxW = 64;
 constexpr int kSwapLd = 33;  // row stride of the gathered rows (complex elements)
 
-template <class T>
+constexpr int kLsLd = 65;  // row stride of a 64 x 64 block of L11 in shared memory (complex elements)
+
+// shared memory: W / 64 blocks of L11 (64 x 64, transposed) and the W gathered rows
+template <class T, int W = kSwapMaxW>
 __host__ __device__ constexpr size_t swap_trsm_smem() {
-  return sizeof(cx<T>) * ((size_t)kSwapMaxW * kSwapMaxW + (size_t)kSwapMaxW * kSwapLd);
+  return sizeof(cx<T>) * ((size_t)(W / 64) * 64 * kLsLd + (size_t)W * kSwapLd);
 }
 
+// Lb[t * kLsLd + r] = L11[r0 + r][c0 + t] for r0 + r < w (strictly below the
+// diagonal on a diagonal block), zero elsewhere; rows of A read coalesced
 template <class T>
+__device__ __forceinline__ void load_l_block(cx<T>* Lb, const cx<T>* A, int64_t lda, int k0, int w, int r0, int c0) {
+  cx<T> v[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const int e = threadIdx.x + 256 * k, t = e & 63, r = e >> 6;
+    const bool keep = r0 + r < w && (r0 != c0 || t < r);
+    v[k] = keep ? A[(int64_t)(k0 + r0 + r) * lda + k0 + c0 + t] : cx<T>();
+  }
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const int e = threadIdx.x + 256 * k, t = e & 63, r = e >> 6;
+    Lb[t * kLsLd + r] = v[k];
+  }
+}
+
+template <class T, int W = kSwapMaxW>
 __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, int n, int k0, int w,
                                                         const int32_t* __restrict__ ipiv, float* __restrict__ B2,
-                                                        int P) {
+                                                        int P, int vc_begin, int vc_end) {
+  static_assert(W == 64 || W == 128, "panel blocks of 64 or 128 columns");
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cx<T>* Ls = reinterpret_cast<cx<T>*>(smem_raw);  // Ls[t * 64 + r] = L11[r][t], zero off the strict lower part
-  cx<T>* V = Ls + kSwapMaxW * kSwapMaxW;           // the w panel rows of the CTA's columns [64][kSwapLd]
-  __shared__ int piv[kSwapMaxW], dst[2 * kSwapMaxW], src[2 * kSwapMaxW];
+  // L11 in 64 x 64 blocks, transposed: for W = 128 first [L11 of rows and
+  // columns 0..63 | rows 64..127 x columns 0..63], then rows and columns 64..127
+  // in the first buffer
+  cx<T>* Ls = reinterpret_cast<cx<T>*>(smem_raw);
+  cx<T>* Ls1 = Ls + (W / 64 - 1) * 64 * kLsLd;
+  cx<T>* V = Ls + (W / 64) * 64 * kLsLd;  // the w panel rows of the CTA's columns [W][kSwapLd]
+  __shared__ int piv[W], dst[2 * W], src[2 * W];
   __shared__ int nd_s;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int kend = k0 + w;
-  const int vc0 = blockIdx.x * 32;  // first column of the CTA, counted without the panel's
+  const int vc0 = vc_begin + blockIdx.x * 32;  // first column of the CTA, counted without the panel's
   if (warp == 0) {
-    int pr[kSwapMaxW / 32];
+    int pr[W / 32];
 #pragma unroll
-    for (int h = 0; h < kSwapMaxW / 32; ++h) {
+    for (int h = 0; h < W / 32; ++h) {
       const int j = lane + 32 * h;
       pr[h] = j < w ? ipiv[k0 + j] : -1;
       piv[j] = pr[h];
     }
     // positions touched: the panel rows, then each pivot row below the panel once
-    bool first[kSwapMaxW / 32];
+    bool first[W / 32];
 #pragma unroll
-    for (int h = 0; h < kSwapMaxW / 32; ++h) first[h] = pr[h] >= kend;
+    for (int h = 0; h < W / 32; ++h) first[h] = pr[h] >= kend;
 #pragma unroll 8
-    for (int q = 0; q < kSwapMaxW; ++q) {
+    for (int q = 0; q < W; ++q) {
       const int pq = __shfl_sync(~0u, pr[q >> 5], q & 31);
 #pragma unroll
-      for (int h = 0; h < kSwapMaxW / 32; ++h)
+      for (int h = 0; h < W / 32; ++h)
         if (q < lane + 32 * h && pq == pr[h]) first[h] = false;
     }
     int nx = 0;
 #pragma unroll
-    for (int h = 0; h < kSwapMaxW / 32; ++h) {
+    for (int h = 0; h < W / 32; ++h) {
       const unsigned b = __ballot_sync(~0u, first[h]);
       if (first[h]) dst[w + nx + __popc(b & ((1u << lane) - 1u))] = pr[h];
       nx += __popc(b);
@@ -622,72 +658,69 @@ __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, i
     for (int i = lane; i < w; i += 32) dst[i] = k0 + i;
     __syncwarp();
     const int nd = w + nx;
-    int y[2 * kSwapMaxW / 32];
+    int y[2 * W / 32];
 #pragma unroll
-    for (int h = 0; h < 2 * kSwapMaxW / 32; ++h) y[h] = lane + 32 * h < nd ? dst[lane + 32 * h] : -1;
+    for (int h = 0; h < 2 * W / 32; ++h) y[h] = lane + 32 * h < nd ? dst[lane + 32 * h] : -1;
 #pragma unroll 4
     for (int j = w - 1; j >= 0; --j) {
       const int r = k0 + j, p = piv[j];
 #pragma unroll
-      for (int h = 0; h < 2 * kSwapMaxW / 32; ++h) y[h] = y[h] == r ? p : (y[h] == p ? r : y[h]);
+      for (int h = 0; h < 2 * W / 32; ++h) y[h] = y[h] == r ? p : (y[h] == p ? r : y[h]);
     }
 #pragma unroll
-    for (int h = 0; h < 2 * kSwapMaxW / 32; ++h)
+    for (int h = 0; h < 2 * W / 32; ++h)
       if (lane + 32 * h < nd) src[lane + 32 * h] = y[h];
     if (lane == 0) nd_s = nd;
   }
   // the CTA's columns vc0 .. vc0 + 31 map to vc (< k0) or vc + w (right of the panel)
-  const bool any_right = kend < n && min(vc0 + 31, n - w - 1) >= k0;
+  const bool any_right = kend < n && min(vc0 + 31, vc_end - 1) >= k0;
   if (any_right) {
-    // 16 elements of L11 per thread, all loads issued before the stores (A is
-    // a generic pointer: the compiler keeps a load behind an earlier store)
-    cx<T> v[16];
-#pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      const int e = threadIdx.x + 256 * k, t = e >> 6, r = e & 63;
-      v[k] = (t < r && r < w) ? A[(int64_t)(k0 + r) * lda + k0 + t] : cx<T>();
-    }
-#pragma unroll
-    for (int k = 0; k < 16; ++k) Ls[threadIdx.x + 256 * k] = v[k];
+    load_l_block(Ls, A, lda, k0, w, 0, 0);
+    if (W == 128) load_l_block(Ls1, A, lda, k0, w, 64, 0);
   }
   __syncthreads();
   const int nd = nd_s;
   const int vc = vc0 + lane;
-  const bool valid = vc < n - w;
+  const bool valid = vc < vc_end;
   const int c = vc < k0 ? vc : vc + w;
   const bool right = c >= kend;
   {
     // warp q gathers rows q, q + 8, ...; every row of the CTA's columns is
     // read before any is written (the barrier), as rows move between warps
-    cx<T> v[2 * kSwapMaxW / 8];
+    cx<T> v[2 * W / 8];
 #pragma unroll
-    for (int j = 0; j < 2 * kSwapMaxW / 8; ++j) {
+    for (int j = 0; j < 2 * W / 8; ++j) {
       const int i = warp + 8 * j;
       v[j] = valid && i < nd ? A[(int64_t)src[i] * lda + c] : cx<T>();
     }
     if (any_right)
 #pragma unroll
-      for (int j = 0; j < 2 * kSwapMaxW / 8; ++j) {
+      for (int j = 0; j < 2 * W / 8; ++j) {
         const int i = warp + 8 * j;
         if (i < w) V[i * kSwapLd + lane] = v[j];
       }
     __syncthreads();
     // rows that are not solved go straight to their final rows
 #pragma unroll
-    for (int j = 0; j < 2 * kSwapMaxW / 8; ++j) {
+    for (int j = 0; j < 2 * W / 8; ++j) {
       const int i = warp + 8 * j;
       if (valid && i < nd && (i >= w || !right) && src[i] != dst[i]) A[(int64_t)dst[i] * lda + c] = v[j];
     }
   }
   if (!any_right) return;
   {
+    constexpr int R = W / 8;  // rows per lane
     const int l8 = lane & 7, col = 4 * warp + (lane >> 3);
-    cx<T> x[8];
+    cx<T> x[R];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) x[k] = l8 + 8 * k < w ? V[(l8 + 8 * k) * kSwapLd + col] : cx<T>();
+    for (int k = 0; k < R; ++k) x[k] = l8 + 8 * k < w ? V[(l8 + 8 * k) * kSwapLd + col] : cx<T>();
+    // rows 0..63 (and, for W = 128, rows 64..127 take their products with
+    // them); the loops over a lane's registers are unrolled, the 8 steps
+    // within a group of rows are not (a fully unrolled substitution is
+    // thousands of instructions, and the warps then wait on instruction fetch)
 #pragma unroll
     for (int kb = 0; kb < 8; ++kb)
-#pragma unroll
+#pragma unroll 1
       for (int j = 0; j < 8; ++j) {
         const int t = 8 * kb + j;
         cx<T> xt;
@@ -696,16 +729,36 @@ __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, i
         // L11 rows >= w and on / above the diagonal are zero in Ls
 #pragma unroll
         for (int k = kb; k < 8; ++k)
-          if (k > kb || l8 > j) x[k] -= Ls[t * kSwapMaxW + l8 + 8 * k] * xt;
-      }
+          if (k > kb || l8 > j) x[k] -= Ls[t * kLsLd + l8 + 8 * k] * xt;
 #pragma unroll
-    for (int k = 0; k < 8; ++k)
+        for (int k = 8; k < R; ++k) x[k] -= Ls1[t * kLsLd + l8 + 8 * (k - 8)] * xt;
+      }
+    if (W == 128) {
+      // rows 64..127 with their own diagonal block, loaded over the first one
+      __syncthreads();
+      load_l_block(Ls, A, lda, k0, w, 64, 64);
+      __syncthreads();
+#pragma unroll
+      for (int kb = 8; kb < R; ++kb)
+#pragma unroll 1
+        for (int j = 0; j < 8; ++j) {
+          const int t = 8 * (kb - 8) + j;
+          cx<T> xt;
+          xt.re = __shfl_sync(~0u, x[kb].re, (lane & ~7) | j);
+          xt.im = __shfl_sync(~0u, x[kb].im, (lane & ~7) | j);
+#pragma unroll
+          for (int k = kb; k < R; ++k)
+            if (k > kb || l8 > j) x[k] -= Ls[t * kLsLd + l8 + 8 * (k - 8)] * xt;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k)
       if (l8 + 8 * k < w) V[(l8 + 8 * k) * kSwapLd + col] = x[k];
   }
   __syncthreads();
   if (valid && right)
 #pragma unroll
-    for (int j = 0; j < kSwapMaxW / 8; ++j) {
+    for (int j = 0; j < W / 8; ++j) {
       const int i = warp + 8 * j;
       if (i < w) A[(int64_t)(k0 + i) * lda + c] = V[i * kSwapLd + lane];
     }
@@ -713,12 +766,12 @@ __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, i
     // U12 as the tensor-core update's B operand: for trailing column cc the
     // rows 2 cc (re, im) and 2 cc + 1 (im, -re) of (U, -iU), K-major, split
     // into tf32 hi and lo planes P floats apart, zero beyond 2 w
-    for (int e = threadIdx.x; e < 64 * P; e += blockDim.x) {
-      const int row = e / P, jj = e - row * P;  // row = 2 x (column of the CTA) + part
+    for (int row = warp; row < 64; row += 8) {  // row = 2 x (column of the CTA) + part
       const int cl = row >> 1, part = row & 1;
       const int vcl = vc0 + cl;
-      if (vcl >= n - w || vcl < k0) continue;  // not a trailing column
+      if (vcl >= vc_end || vcl < k0) continue;  // not a trailing column
       const int cc = vcl - k0;                  // = (vcl + w) - kend
+      for (int jj = lane; jj < P; jj += 32) {
       const int t = jj >> 1, f = jj & 1;
       float hi = 0.f, lo = 0.f;
       if (t < w) {
@@ -729,6 +782,7 @@ __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, i
       }
       B2[(int64_t)(2 * cc + part) * 2 * P + jj] = hi;
       B2[(int64_t)(2 * cc + part) * 2 * P + P + jj] = lo;
+      }
     }
   }
 }
@@ -810,10 +864,12 @@ __global__ void gather_rows_kernel(int n, int nrhs, const int32_t* __restrict__ 
 }
 
 // ----------------------------------------------------------------- drivers
-int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w, int panel, bool pack_a,
-               bool pack_b);  // lu_tc.cu
-int lu_tc_prepare(m25_ctx* ctx, int n, int nb);
-int lu_tc_operands(m25_ctx* ctx, int n, int k0, int w, float** A2, float** B2, int* P);
+// lu_tc.cu
+int lu_tc_prepare(m25_ctx* ctx, int n);
+int lu_tc_buffers(m25_ctx* ctx, int n, float** A3, float** B3, float** Ai, float** Bi);
+int lu_tc_pack_a(m25_ctx* ctx, const zf* A, int64_t lda, int k0, int w, int m, int P, float* A3);
+int lu_tc_update(m25_ctx* ctx, zf* A, int64_t lda, int r0, int m, int nc, int P, const float* A3, const float* B3,
+                 int slot);
 int lu_tc_error(m25_ctx* ctx, int* flag);
 bool lu_tc_available();
 
@@ -822,7 +878,8 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
   cudaStream_t st = ctx->stream;
   // the tensor-core update reduces into C through a TMA tensor map: rows of
   // a multiple of 16 bytes and a 16-byte aligned matrix (else SIMT updates)
-  use_tc = use_tc && lda % 2 == 0 && reinterpret_cast<uintptr_t>(A) % 16 == 0 && nb % 2 == 0;
+  use_tc = use_tc && std::is_same<T, float>::value && lda % 2 == 0 && reinterpret_cast<uintptr_t>(A) % 16 == 0 &&
+           nb == kSwapMaxW;
   // panel workspace
   int bps_max = 0;
   size_t panel_smem = 0;
@@ -841,6 +898,9 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
   }
   M25_CUDA(cudaFuncSetAttribute(swap_trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)swap_trsm_smem<T>()));
+  if constexpr (std::is_same<T, float>::value)
+    M25_CUDA(cudaFuncSetAttribute(swap_trsm_kernel<T, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)swap_trsm_smem<T, 128>()));
   (void)bps_max;
   (void)rows;
   int Gmax = ctx->ext_scratch ? ctx->ext_gmax : 4 * ctx->num_sms;
@@ -860,7 +920,7 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
   cx<T>* rowj = reinterpret_cast<cx<T>*>(candidx + 2 * Gmax);
   M25_CUDA(cudaMemsetAsync(base, 0, 64, st));
   if (use_tc) {
-    int rc = lu_tc_prepare(ctx, n, nb);
+    int rc = lu_tc_prepare(ctx, n);
     if (rc) return rc;
   }
   // the cluster panel: the smallest cluster (4, 8 or 16 CTAs) whose shared
@@ -918,21 +978,14 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
       cl_rows[2] = 16 * rows_of(cluster_panel_smem<T, 16>(0));
     }
   }
-  for (int k0 = 0; k0 < n; k0 += nb) {
-    const int w = std::min(nb, n - k0);
+  // one panel of w <= nb columns at k0 over the rows k0 .. n - 1; A2 / P2:
+  // the tensor-core operand planes of its trailing rows (cluster panel only),
+  // *packed tells whether they were written
+  auto run_panel = [&](int k0, int w, float* A2, int P2, bool* packed) -> int {
     const int m = n - k0;
-    // tensor-core update of this panel: its packed operands are written by
-    // the cluster panel (A) and the row-interchange / U12 kernel (B)
-    const bool tc_here = use_tc && k0 + w < n;
-    float *A2 = nullptr, *B2 = nullptr;
-    int P2 = 0;
-    if (tc_here) {
-      int rc = lu_tc_operands(ctx, n, k0, w, &A2, &B2, &P2);
-      if (rc) return rc;
-    }
     const int CL = m <= cl_rows[0] ? 4 : m <= cl_rows[1] ? 8 : m <= cl_rows[2] ? 16 : 0;
-    const bool cluster_panel = CL > 0;
-    if (cluster_panel) {
+    if (packed) *packed = CL > 0 && A2;
+    if (CL > 0) {
       ClusterPanelArgs<T> ca{A, lda, n, k0, w, (m + CL - 1) / CL, ipiv, info, err, A2, P2};
       const size_t smem = CL == 4    ? cluster_panel_smem<T, 4>(ca.rows_per_cta)
                           : CL == 8 ? cluster_panel_smem<T, 8>(ca.rows_per_cta)
@@ -953,7 +1006,8 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
       if (CL == 4) M25_CUDA(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T, 4>, ca));
       else if (CL == 8) M25_CUDA(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T, 8>, ca));
       else M25_CUDA(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<T, 16>, ca));
-    } else {
+      return M25_OK;
+    }
     // grid size: as many CTAs as can be co-resident, each with >= 1 row
     int occ = 0;
     G = std::min(std::min(m, ctx->num_sms), Gmax);
@@ -999,27 +1053,74 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
     pa.err = err;
     pa.info = info;
     void* args[] = {&pa};
-    {
-      StageTimer tm(ctx, ST_PANEL);
-      M25_CUDA(cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(G), dim3(256), args, panel_smem, st));
-    }
-    }
-    if (n > w) {
-      StageTimer tm(ctx, ST_TRSM);
-      swap_trsm_kernel<T><<<(n - w + 31) / 32, 256, swap_trsm_smem<T>(), st>>>(A, lda, n, k0, w, ipiv, B2, P2);
-    }
-    if (k0 + w < n) {
-      int ncol = n - k0 - w;
-      if (use_tc) {  // times its operand packing (ST_PACK) and its update (ST_GEMM) itself
-        int rc = lu_gemm_tc(ctx, reinterpret_cast<zf*>(A), lda, n, k0, w, k0 / nb, !cluster_panel, false);
-        if (rc) return rc;
-      } else {
+    StageTimer tm(ctx, ST_PANEL);
+    M25_CUDA(cudaLaunchCooperativeKernel((void*)panel_kernel<T>, dim3(G), dim3(256), args, panel_smem, st));
+    return M25_OK;
+  };
+  // interchanges of the panel at k0 (width w) on the columns vc_begin <= vc <
+  // vc_end (counted without the panel's), U12 on those right of it
+  auto swap_trsm = [&](int k0, int w, int vc_begin, int vc_end, float* B2, int P2) -> int {
+    if (vc_end <= vc_begin) return M25_OK;
+    StageTimer tm(ctx, ST_TRSM);
+    swap_trsm_kernel<T><<<(vc_end - vc_begin + 31) / 32, 256, swap_trsm_smem<T>(), st>>>(A, lda, n, k0, w, ipiv, B2,
+                                                                                         P2, vc_begin, vc_end);
+    M25_CHECK_LAUNCH();
+    return M25_OK;
+  };
+  int rc = M25_OK;
+  if (!use_tc) {
+    // right-looking: panel, interchanges and U12, SIMT update of the trailing matrix
+    for (int k0 = 0; k0 < n; k0 += nb) {
+      const int w = std::min(nb, n - k0);
+      if ((rc = run_panel(k0, w, nullptr, 0, nullptr))) return rc;
+      if ((rc = swap_trsm(k0, w, 0, n - w, nullptr, 0))) return rc;
+      if (k0 + w < n) {
+        const int ncol = n - k0 - w;
         StageTimer tm(ctx, ST_GEMM);
         dim3 grid((ncol + 63) / 64, (ncol + 63) / 64);
         gemm_kernel<T><<<grid, 256, 0, st>>>(A, lda, n, k0, w);
+        M25_CHECK_LAUNCH();
       }
     }
-    M25_CHECK_LAUNCH();
+  } else if constexpr (std::is_same<T, float>::value) {
+    // blocks of 128 columns, each factored as two panels of 64: the second
+    // panel's columns get the first panel's rank-64 update, and the trailing
+    // matrix one rank-128 update per block (its read-modify-write of C, the
+    // bound of the update, once per 128 columns instead of once per 64)
+    float *A3, *B3, *Ai, *Bi;
+    if ((rc = lu_tc_buffers(ctx, n, &A3, &B3, &Ai, &Bi))) return rc;
+    constexpr int kHalf = kSwapMaxW, kBlock = 2 * kSwapMaxW;
+    for (int k0 = 0, blk = 0; k0 < n; k0 += kBlock, ++blk) {
+      const int W = std::min(kBlock, n - k0), w1 = std::min(kHalf, W), w2 = W - w1;
+      bool packed = false;
+      if ((rc = run_panel(k0, w1, w2 > 0 ? Ai : nullptr, 128, &packed))) return rc;
+      if (w2 > 0) {
+        // the first panel's interchanges on the columns left of the block and
+        // with U12 on the second panel's; that panel's rank-64 update
+        if ((rc = swap_trsm(k0, w1, 0, k0 + w2, Bi, 128))) return rc;
+        const int m1 = n - k0 - w1;
+        if (!packed && (rc = lu_tc_pack_a(ctx, A, lda, k0, w1, m1, 128, Ai))) return rc;
+        if ((rc = lu_tc_update(ctx, A, lda, k0 + w1, m1, w2, 128, Ai, Bi, 2 * blk))) return rc;
+        if ((rc = run_panel(k0 + w1, w2, nullptr, 0, nullptr))) return rc;
+        // the second panel's interchanges on every column left of it
+        if ((rc = swap_trsm(k0 + w1, w2, 0, k0 + w1, nullptr, 0))) return rc;
+      } else if ((rc = swap_trsm(k0, w1, 0, k0, nullptr, 0))) {
+        return rc;
+      }
+      if (k0 + W < n) {
+        // both panels' interchanges and U12 = L11^-1 A12 (128 rows) on the
+        // trailing columns, then the rank-128 update
+        const int m2 = n - k0 - W;
+        {
+          StageTimer tm(ctx, ST_TRSM);
+          swap_trsm_kernel<T, 128><<<(m2 + 31) / 32, 256, swap_trsm_smem<T, 128>(), st>>>(A, lda, n, k0, W, ipiv, B3,
+                                                                                          256, k0, n - W);
+          M25_CHECK_LAUNCH();
+        }
+        if ((rc = lu_tc_pack_a(ctx, A, lda, k0, W, m2, 256, A3))) return rc;
+        if ((rc = lu_tc_update(ctx, A, lda, k0 + W, m2, m2, 256, A3, B3, 2 * blk + 1))) return rc;
+      }
+    }
   }
   int hflags[3];
   M25_CUDA(cudaMemcpyAsync(hflags, base + 8, 8, cudaMemcpyDeviceToHost, st));

@@ -2,6 +2,9 @@
 //
 //   A22 -= L21 U12          (complex, interleaved re/im, row-major, lda)
 //
+// of rank 128 per block of two panels, and of rank 64 on the second panel's
+// columns (the factorisation's order is in lu.cu).
+//
 // written as one real GEMM on the interleaved storage: C (m x 2n') -=
 // A (m x 2K) B (2K x 2n') with A the interleaved conj(L21) and B rows
 // (U, -iU) alternating, which gives Re and Im of L U in the even and odd
@@ -395,34 +398,6 @@ __global__ void pack_a_kernel(const zf* __restrict__ LU, int64_t lda, int k0, in
   A3[e] = out;
 }
 
-// B2t[c2][s P + j] for the trailing real columns c2 = 2 c + e, planes
-// s = [hi | lo] of the rows (U, -iU).
-// One block transposes a 32 (t) x 32 (c) complex tile of U12 through shared
-// memory so that both the reads of U and the writes of B3t are coalesced.
-__global__ void __launch_bounds__(256) pack_b_kernel(const zf* __restrict__ LU, int64_t lda, int k0, int w, int m,
-                                                     int P, float* __restrict__ B3) {
-  __shared__ zf tile[32][33];
-  const int K2p = 2 * P;
-  const int c0 = blockIdx.x * 32, t0 = blockIdx.y * 32;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  for (int i = ty; i < 32; i += 8) {
-    const int t = t0 + i, c = c0 + tx;
-    tile[i][tx] = (t < w && c < m) ? LU[(int64_t)(k0 + t) * lda + k0 + w + c] : zf{0.f, 0.f};
-  }
-  __syncthreads();
-  // 2 planes x 64 real columns x 64 floats (32 t x 2 parts)
-  for (int idx = threadIdx.x; idx < 2 * 64 * 64; idx += 256) {
-    const int j = idx & 63, row = idx >> 6;
-    const int s = row >> 6, c2l = row & 63;
-    const int c = c2l >> 1, ee = c2l & 1, t = j >> 1, f = j & 1;
-    if (c0 + c >= m) continue;
-    const zf U = tile[t][c];
-    const float v = ee == 0 ? (f == 0 ? U.re : U.im) : (f == 0 ? U.im : -U.re);
-    const float hi = tf32_round(v);
-    B3[(int64_t)(2 * c0 + c2l) * K2p + s * P + 2 * t0 + j] = s == 1 ? tf32_round(v - hi) : hi;
-  }
-}
-
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -474,21 +449,42 @@ bool lu_tc_available() {
   return avail;
 }
 
-// packed width of one plane for a panel of w complex columns
+// packed width of one plane for a panel block of w complex columns
 inline int plane_width(int w) { return (2 * w + 63) / 64 * 64; }
 
-// Operand buffer for the factorisation of an n x n matrix with panels of
-// nb: a header of kTcHeader bytes (error word, then one tile counter per
-// panel from byte 16), then the packed A3 and B3 of the largest update.
-int lu_tc_prepare(m25_ctx* ctx, int n, int nb) {
-  const int m = std::max(n - nb, 1);
-  const int K2p = 2 * plane_width(nb);
-  const size_t abytes = sizeof(float) * (size_t)m * K2p, bbytes = sizeof(float) * (size_t)2 * m * K2p;
-  if (n / nb + 1 > (kTcHeader - 16) / 4) {
+inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Operand buffer of the factorisation of an n x n matrix in blocks of 128
+// columns, each factored as two panels of 64: a header of kTcHeader bytes
+// (error word, then one tile counter per update launch from byte 16), the
+// packed A3 (m x 2 P) and B3 (2 m x 2 P) of a block's rank-128 trailing
+// update (P = 256, m <= n - 128), then Ai and Bi of the rank-64 update of
+// the block's second panel (P = 128, m <= n - 64 rows, 64 columns).
+struct TcLayout {
+  size_t a3, b3, ai, bi, total;
+};
+inline TcLayout tc_layout(int n) {
+  TcLayout t;
+  const size_t m2 = (size_t)std::max(n - 128, 1), m1 = (size_t)std::max(n - 64, 1);
+  size_t off = kTcHeader;
+  t.a3 = off;
+  off += align256(sizeof(float) * m2 * 2 * 256);
+  t.b3 = off;
+  off += align256(sizeof(float) * 2 * m2 * 2 * 256);
+  t.ai = off;
+  off += align256(sizeof(float) * m1 * 2 * 128);
+  t.bi = off;
+  off += align256(sizeof(float) * 128 * 2 * 128);
+  t.total = off;
+  return t;
+}
+
+int lu_tc_prepare(m25_ctx* ctx, int n) {
+  if (2 * ((n + 127) / 128) + 2 > (kTcHeader - 16) / 4) {
     set_error("tensor-core LU: too many panels");
     return M25_ERR_VALUE;
   }
-  int rc = ctx->Dw.ensure(kTcHeader + ((abytes + 255) & ~(size_t)255) + bbytes);
+  int rc = ctx->Dw.ensure(tc_layout(n).total);
   if (rc) return rc;
   M25_CUDA(cudaMemsetAsync(ctx->Dw.p, 0, kTcHeader, ctx->stream));
   return M25_OK;
@@ -501,54 +497,51 @@ int lu_tc_error(m25_ctx* ctx, int* flag) {
   return M25_OK;
 }
 
-// A22 -= L21 U12 for the panel at k0 of width w (complex64, in place);
-// lu_tc_prepare has sized the operand buffer for this factorisation.
-// The packed operands of the update of the panel at k0 (width w) in the
-// operand buffer: A2 (m x 2P) and B2 (2m x 2P), m = n - k0 - w trailing rows.
-int lu_tc_operands(m25_ctx* ctx, int n, int k0, int w, float** A2, float** B2, int* Pout) {
-  const int m = n - k0 - w;
-  const int P = plane_width(w), K2p = 2 * P;
-  const size_t abytes = sizeof(float) * (size_t)std::max(m, 1) * K2p, bbytes = sizeof(float) * (size_t)2 * m * K2p;
-  if (kTcHeader + ((abytes + 255) & ~(size_t)255) + bbytes > ctx->Dw.bytes) {
+// the packed operand planes of a factorisation of order n (lu_tc_prepare first)
+int lu_tc_buffers(m25_ctx* ctx, int n, float** A3, float** B3, float** Ai, float** Bi) {
+  const TcLayout t = tc_layout(n);
+  if (t.total > ctx->Dw.bytes) {
     set_error("tensor-core LU: operand buffer not prepared for this size");
     return M25_ERR_VALUE;
   }
-  *A2 = reinterpret_cast<float*>(ctx->Dw.as<char>() + kTcHeader);
-  *B2 = reinterpret_cast<float*>(reinterpret_cast<char*>(*A2) + ((abytes + 255) & ~(size_t)255));
-  *Pout = P;
+  char* b = ctx->Dw.as<char>();
+  *A3 = reinterpret_cast<float*>(b + t.a3);
+  *B3 = reinterpret_cast<float*>(b + t.b3);
+  *Ai = reinterpret_cast<float*>(b + t.ai);
+  *Bi = reinterpret_cast<float*>(b + t.bi);
   return M25_OK;
 }
 
-// pack_a / pack_b: the operands still have to be packed (else the panel and
-// the U12 kernel wrote them)
-int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w, int panel, bool pack_a, bool pack_b) {
-  cudaStream_t st = ctx->stream;
-  const int m = n - k0 - w;  // trailing rows = trailing columns
+// A3 (m x 2 P) from the rows k0 + w .. k0 + w + m - 1 of the panel block's w columns
+int lu_tc_pack_a(m25_ctx* ctx, const zf* A, int64_t lda, int k0, int w, int m, int P, float* A3) {
   if (m <= 0) return M25_OK;
-  const int P = plane_width(w), K2p = 2 * P;
-  const int n2 = 2 * m;
-  const size_t abytes = sizeof(float) * (size_t)m * K2p, bbytes = sizeof(float) * (size_t)n2 * K2p;
-  if (kTcHeader + ((abytes + 255) & ~(size_t)255) + bbytes > ctx->Dw.bytes) {
-    set_error("tensor-core LU: operand buffer not prepared for this size");
+  StageTimer tm(ctx, ST_PACK);
+  const int64_t ta = (int64_t)m * 2 * P;
+  pack_a_kernel<<<(unsigned)((ta + 255) / 256), 256, 0, ctx->stream>>>(A, lda, k0, w, m, P, A3);
+  M25_CHECK_LAUNCH();
+  return M25_OK;
+}
+
+// C -= A3 B3 for C = A[r0 .. r0 + m - 1][r0 .. r0 + nc - 1] (complex64, in
+// place): A3 (m x 2 P) and B3 (2 nc x 2 P) packed [hi | lo] planes; slot: the
+// header's tile counter of this launch (zeroed by lu_tc_prepare).
+int lu_tc_update(m25_ctx* ctx, zf* A, int64_t lda, int r0, int m, int nc, int P, const float* A3, const float* B3,
+                 int slot) {
+  if (m <= 0 || nc <= 0) return M25_OK;
+  cudaStream_t st = ctx->stream;
+  const int n2 = 2 * nc, K2p = 2 * P;
+  if (P % kBK || 16 + 4 * (size_t)(slot + 1) > (size_t)kTcHeader) {
+    set_error("tensor-core LU: bad update shape");
     return M25_ERR_VALUE;
   }
   int* err = ctx->Dw.as<int>();
-  float* A3 = reinterpret_cast<float*>(ctx->Dw.as<char>() + kTcHeader);
-  float* B3 = reinterpret_cast<float*>(reinterpret_cast<char*>(A3) + ((abytes + 255) & ~(size_t)255));
-  if (pack_a || pack_b) {
-    StageTimer tm(ctx, ST_PACK);
-    int64_t ta = (int64_t)m * K2p;
-    if (pack_a) pack_a_kernel<<<(unsigned)((ta + 255) / 256), 256, 0, st>>>(A, lda, k0, w, m, P, A3);
-    dim3 gb((m + 31) / 32, P / 64);
-    if (pack_b) pack_b_kernel<<<gb, 256, 0, st>>>(A, lda, k0, w, m, P, B3);
-  }
   CUtensorMap ma, mb;
   int rc;
   if ((rc = make_map(&ma, A3, m, K2p, kBM))) return rc;
   if ((rc = make_map(&mb, B3, n2, K2p, kBN))) return rc;
-  // C: the fp32 view of the trailing block, rows 2 lda floats apart, 32 x 32 boxes
+  // C: the fp32 view of the block, rows 2 lda floats apart, 32 x 32 boxes
   CUtensorMap mc;
-  const float* C = reinterpret_cast<const float*>(A + (int64_t)(k0 + w) * lda + k0 + w);
+  const float* C = reinterpret_cast<const float*>(A + (int64_t)r0 * lda + r0);
   if ((lda & 1) || (reinterpret_cast<uintptr_t>(C) & 15)) {
     set_error("tensor-core LU: C needs an even leading dimension and 16-byte alignment");
     return M25_ERR_VALUE;
@@ -567,7 +560,7 @@ int lu_gemm_tc(m25_ctx* ctx, zf* A, int64_t lda, int n, int k0, int w, int panel
   ta.ntiles = ta.tiles_m * ((n2 + kBN - 1) / kBN);
   ta.chunk = chunk;
   ta.err = err;
-  ta.counter = reinterpret_cast<int*>(ctx->Dw.as<char>() + 16) + panel;  // zeroed once per factorisation
+  ta.counter = reinterpret_cast<int*>(ctx->Dw.as<char>() + 16) + slot;
   M25_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
   StageTimer tm(ctx, ST_GEMM);
   tc_gemm_kernel<<<std::min(ta.ntiles, n_sm), kThreads, kSmemBytes, st>>>(ma, mb, mc, ta);

@@ -325,14 +325,16 @@ def _lu_reconstruct(F, piv):
     return L @ U, perm
 
 
-@pytest.mark.parametrize("n", [300, 1000, 1302])
+@pytest.mark.parametrize("n", [300, 1000, 1280, 1302, 1344])
 def test_lu_complex64_tensor_cores_reconstruct(gpu, n):
     """complex64 LU with tcgen05 3xTF32 trailing updates: P L U = A to fp32
     accuracy. The tensor cores' fp32 accumulation rounds differently from
     SIMT fused multiply-adds, so the bound against the SIMT factorisation is
     a factor of 16; a wrong tile or operand split gives O(1) errors. (The
     pivot sequences may part where two candidates tie to rounding, so the
-    factors themselves are not compared.)"""
+    factors themselves are not compared.) The orders end the blocks of 128
+    columns in each way: a second panel of 44, 40 or 22 columns, a full block
+    with no trailing matrix (1280) and a single last panel (1344)."""
     import ctypes as C
 
     from mom25d_gb300 import engine as E
