@@ -252,15 +252,18 @@ def run_ours(args, rank, world, local):
     except OSError:
         pass
     lu_ms = iso_ms["lu_gemm"]  # per point: the update kernels of one LU, GPU to themselves
-    # algorithmic work of the trailing updates: 8 m^2 w real flops per panel
-    # (complex multiply-add = 8 flops), summed over the 64-wide panels
-    gemm_flops = float(sum(8.0 * (n - k0 - 64) ** 2 * 64 for k0 in range(0, n - 64, 64)))
+    # algorithmic work of the updates (complex multiply-add = 8 real flops):
+    # per block of 128 columns the rank-64 update of the second panel's 64
+    # columns (m1 = n - k0 - 64 rows) and the rank-128 update of the m2 x m2
+    # trailing matrix (m2 = n - k0 - 128)
+    gemm_flops = float(sum(8.0 * (n - k0 - 64) * min(64, n - k0 - 64) * 64 + 8.0 * max(n - k0 - 128, 0) ** 2 * 128
+                           for k0 in range(0, n - 64, 128)))
     achieved = gemm_flops / (lu_ms * 1e-3) / 1e12 if lu_ms else None
     bf16 = peaks.get("bf16_tflops") or 1900.0  # burst: the kernel is timed alone
-    # DRAM traffic of the update per flop, from the ncu capture of all trailing
-    # updates of an n = 4096 factorisation (3.84 GB for 1.79e11 flops); bytes and
-    # flops of a panel's update both scale as m^2 at a fixed panel width
-    traffic = 3.844e9 / 1.790e11 * gemm_flops
+    # DRAM traffic of the updates per flop, from the ncu capture of all 63
+    # update launches of an n = 4096 factorisation (2.173 GB for 1.769e11
+    # flops); bytes and flops of a block's update both scale as m^2
+    traffic = 2.173e9 / 1.769e11 * gemm_flops
     roof = {"kernel": "tc_gemm_kernel: LU trailing update (tcgen05 3xTF32, complex64), all launches of one point",
             "bound": "tensor", "achieved": round(achieved, 2) if achieved else None, "peak": bf16, "unit": "TFLOP/s",
             "frac": round(achieved / bf16, 4) if achieved else None, "traffic": round(traffic),
