@@ -284,6 +284,38 @@ int m25_sweep_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* por
                     double* x_out, double* S, double* z0, double* gamma, double* z0_line, double* resid,
                     int32_t* info);
 
+/* ---- Frequency interpolation of Z (FreqInterp, Engine/mom25d/freqinterp.py:27-197).
+ * Anchor matrices W = j w Z exp(+j k_e R) are kept on the device in nslots
+ * slots (complex128, or complex64 when single != 0); at another frequency
+ * Z = (sum_a L[a] W[slot[a]]) exp(-j k_e R) / (j w). R is the distance of the
+ * basis centres pos (n x 3, host float64: RWG edge midpoints on their level,
+ * via segments at mid-span), 0 between two via unknowns (rows and columns
+ * >= nb); k_e = k_ratio w / c0. Z is n x n complex128, rows ldz apart, on the
+ * device or the host per where. */
+typedef struct m25_interp m25_interp;
+int m25_interp_create(m25_ctx* ctx, int32_t n, int32_t nb, const double* pos, int32_t nslots, int32_t single,
+                      m25_interp** out);
+int m25_interp_destroy(m25_interp* ip);
+/* slot <- W of the given Z at freq (FreqInterp._anchor, freqinterp.py:107-122) */
+int m25_interp_store(m25_interp* ip, int32_t slot, const void* Z, int64_t ldz, int where, double freq, double ke);
+/* Z <- the interpolation at freq from nuse <= 8 slots with weights L
+ * (FreqInterp.impedance, freqinterp.py:145-165) */
+int m25_interp_eval(m25_interp* ip, int32_t nuse, const int32_t* slots, const double* L, double freq, double ke,
+                    void* Z, int64_t ldz, int where);
+/* Fill Z at the anchor frequency of gr (precision as m25_assemble; M25_MIXED
+ * and M25_FP64 give complex128) and store it in slot. */
+int m25_interp_anchor(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_interp* ip, int32_t slot, double zs_re,
+                      double zs_im, double zsv_re, double zsv_im, int precision, double ke);
+/* One frequency point as m25_sweep_point with the interpolated Z in place of
+ * the fill (Solver.sweep with a FreqInterp, solver.py:1273-1325 and
+ * solve_currents 1012-1013): solve (precision M25_FP64 or M25_MIXED), then
+ * de-embedding with the tables of gr. A mixed solve that does not reach tol
+ * is redone in fp64 on the same interpolated Z (info[0] = -1). */
+int m25_interp_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* ports, m25_interp* ip, int32_t nuse,
+                     const int32_t* slots, const double* L, double ke, int precision, const double* beta0, double tol,
+                     int32_t max_iter, double* x_out, double* S, double* z0, double* gamma, double* z0_line,
+                     double* resid, int32_t* info);
+
 /* Diagnostics of the last m25_deembed: phi (sum nvpt, P) complex128 line
  * voltages, q (nt, P) complex128 triangle charges, I and V (sum ns, P)
  * complex128 cut currents / voltages. NULL skips an output. */

@@ -912,3 +912,45 @@ extern "C" int m25_sweep_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25
   }
   return M25_OK;
 }
+
+extern "C" int m25_interp_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, m25_interp* ip,
+                                int32_t nuse, const int32_t* slots, const double* L, double ke, int precision,
+                                const double* beta0, double tol, int32_t max_iter, double* x_out, double* S,
+                                double* z0, double* gamma, double* z0_line, double* resid, int32_t* info) {
+  if (!ctx || !geom || !gr || !p || !ip || ip->ctx != ctx || ip->n != geom->nb + geom->nv) {
+    set_error("m25_interp_point: bad argument");
+    return M25_ERR_VALUE;
+  }
+  if (precision != M25_FP64 && precision != M25_MIXED) {
+    set_error("m25_interp_point: precision must be M25_FP64 or M25_MIXED");
+    return M25_ERR_VALUE;
+  }
+  const int n = ip->n, P = p->P;
+  int rc;
+  if ((rc = ctx->Zsweep.ensure(sizeof(zd) * (size_t)n * n))) return rc;
+  if ((rc = ctx->Xsweep.ensure(sizeof(zd) * (size_t)n * P))) return rc;
+  zd* Z = ctx->Zsweep.as<zd>();
+  if ((rc = interp_eval_device(ip, nuse, slots, L, gr->freq, ke, Z, n))) return rc;
+  int32_t inf[2] = {0, 0};
+  rc = m25_dense_solve(ctx, n, P, precision, Z, p->Bexc, ctx->Xsweep.p, M25_ON_DEVICE, tol, max_iter, inf);
+  int used = precision;
+  if (rc == M25_ERR_NUMERIC && precision != M25_FP64) {
+    // the mixed refinement stopped above tol: the same interpolated Z in fp64
+    // (the solve factored a complex64 copy; Z itself is unchanged)
+    inf[0] = inf[1] = 0;
+    if ((rc = m25_dense_solve(ctx, n, P, M25_FP64, Z, p->Bexc, ctx->Xsweep.p, M25_ON_DEVICE, tol, max_iter, inf)))
+      return rc;
+    inf[0] = -1;
+    used = M25_FP64;
+  }
+  if (rc) return rc;
+  if (info) {
+    info[0] = inf[0];
+    info[1] = inf[1];
+  }
+  if ((rc = deembed(ctx, geom, gr, p, ctx->Xsweep.p, M25_ON_DEVICE, beta0, S, z0, gamma, z0_line, resid,
+                    used != M25_FP64)))
+    return rc;
+  if (x_out) M25_CUDA(cudaMemcpy(x_out, ctx->Xsweep.p, sizeof(zd) * (size_t)n * P, cudaMemcpyDeviceToHost));
+  return M25_OK;
+}

@@ -123,7 +123,18 @@ struct m25_greens {
   std::vector<void*> allocs;
 };
 
+struct m25_interp {
+  m25_ctx* ctx = nullptr;
+  int n = 0, nb = 0, single = 0;
+  double* pos = nullptr;          // (n, 3) basis centres
+  std::vector<void*> slots;       // anchor matrices W, n x n complex128 or complex64
+  std::vector<void*> allocs;
+};
+
 namespace m25 {
+// Z (device, complex128, rows ldz apart) <- the interpolation of the anchors
+int interp_eval_device(m25_interp* ip, int nuse, const int32_t* slots, const double* L, double freq, double ke,
+                       zd* Z, int64_t ldz);
 // output of the mixed fill as double-float planes and the complex64 LU input
 struct FillSplit {
   zf *Zh, *Zl, *LU;

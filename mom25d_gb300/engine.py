@@ -28,7 +28,8 @@ EXPORTS = ("m25_last_error", "m25_version", "m25_ctx_create", "m25_ctx_destroy",
            "m25_ports_create", "m25_ports_destroy", "m25_deembed", "m25_sweep_point", "m25_deembed_debug",
            "m25_ctx_timing", "m25_dense_solve_noalloc", "m25_lu_factor", "m25_greens_remainder", "m25_mlp_create",
            "m25_mlp_destroy", "m25_mlp_params", "m25_mlp_loss_grad", "m25_mlp_train", "m25_mlp_forward",
-           "m25_ctx_mem_info")
+           "m25_ctx_mem_info", "m25_interp_create", "m25_interp_destroy", "m25_interp_store", "m25_interp_eval",
+           "m25_interp_anchor", "m25_interp_point")
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
@@ -101,6 +102,13 @@ def load():
     lib.m25_lu_factor.argtypes = [vp, C.c_int32, C.c_int, vp, C.c_int64, _i32p, C.c_int, C.c_int32, _i32p]
     lib.m25_greens_remainder.argtypes = [vp, _f64p, _f64p]
     lib.m25_ctx_mem_info.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+    lib.m25_interp_create.argtypes = [vp, C.c_int32, C.c_int32, _f64p, C.c_int32, C.c_int32, C.POINTER(vp)]
+    lib.m25_interp_destroy.argtypes = [vp]
+    lib.m25_interp_store.argtypes = [vp, C.c_int32, vp, C.c_int64, C.c_int, d, d]
+    lib.m25_interp_eval.argtypes = [vp, C.c_int32, _i32p, _f64p, d, d, vp, C.c_int64, C.c_int]
+    lib.m25_interp_anchor.argtypes = [vp, vp, vp, vp, C.c_int32, d, d, d, d, C.c_int, d]
+    lib.m25_interp_point.argtypes = [vp, vp, vp, vp, vp, C.c_int32, _i32p, _f64p, d, C.c_int, _f64p, d, C.c_int32,
+                                     _f64p, _f64p, _f64p, _f64p, _f64p, _f64p, _i32p]
     f32p = C.POINTER(C.c_float)
     lib.m25_mlp_create.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(vp)]
     lib.m25_mlp_destroy.argtypes = [vp]

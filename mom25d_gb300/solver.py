@@ -457,15 +457,20 @@ class Solver:
             PRECISIONS[self.precision], E.ptr(b0), self.refine_tol, self.max_refine, F(x), F(S), E.ptr(z0), F(gam),
             F(zl), E.ptr(res), E.ptr(info, C.c_int32)))
         g.close()
+        S, z0 = self._fixed_z0(S, z0)
+        # refine_steps -1: the mixed refinement did not reach refine_tol and
+        # the point was recomputed on the fp64 path
+        return S, z0, gam, zl, res, x, dict(refine_steps=int(info[0]), fp64_fallback=bool(info[0] < 0))
+
+    def _fixed_z0(self, S, z0):
+        """S referenced to the fixed port impedances when the solver has them."""
         if self.z0_fixed is not None:
             d0 = np.sqrt(z0)
             SI = S * d0[None, :] / d0[:, None]
             z0 = self.z0_fixed.copy()
             d = np.sqrt(z0)
             S = d[:, None] * SI / d[None, :]
-        # refine_steps -1: the mixed refinement did not reach refine_tol and
-        # the point was recomputed on the fp64 path
-        return S, z0, gam, zl, res, x, dict(refine_steps=int(info[0]), fp64_fallback=bool(info[0] < 0))
+        return S, z0
 
     def last_deembed(self):
         """Intermediates of the last de-embedding on the device: triangle
@@ -545,18 +550,38 @@ class Solver:
 
     def sweep(self, freqs, keep_currents=False, interp=None, values=None, checkpoint=None, wait_memory=None,
               workers=1):
-        """S-parameters at freqs (exact fill at every frequency). checkpoint:
-        an .npz rewritten atomically after every frequency; a restarted sweep
-        with the same frequencies and mesh resumes from it. workers: frequency
+        """S-parameters at freqs. interp: None (default) -> exact fill at
+        every frequency; "auto" -> interpolate Z between anchor fills
+        (FreqInterp with its defaults) when the sweep has at least twice as
+        many frequencies as anchors, else fill every point; a FreqInterp ->
+        use it (Engine/mom25d/solver.py:1189-1223). checkpoint: an .npz
+        rewritten atomically after every frequency; a restarted sweep with
+        the same frequencies and mesh resumes from it. workers: frequency
         points in flight at once on this GPU, each on its own engine context
         and stream, driven by its own host thread (the latency-bound stages of
         one point - LU panels, triangular solves, the wave fit - leave most of
         the GPU to the others); points are handed out in order as workers
         become free. Fewer workers run when their buffers would not fit in
-        the free device memory (result.info["workers"])."""
-        if interp not in (None, "auto"):
-            raise ValueError("this engine fills every frequency exactly (interp=None)")
+        the free device memory (result.info["workers"]). An interpolated
+        sweep runs on one worker, in the order of freqs (its anchors are
+        shared by the points)."""
         freqs = np.atleast_1d(np.asarray(freqs, float))
+        ip = None
+        if isinstance(interp, str):
+            if interp != "auto":
+                raise ValueError("interp must be 'auto', None or a FreqInterp")
+            from .freqinterp import FreqInterp
+
+            ip = FreqInterp().setup(self, freqs)
+            if len(freqs) < 2 * len(ip.anchors):
+                ip = None
+        elif interp is not None:
+            ip = interp.setup(self, freqs)
+        if ip is not None:
+            workers = 1
+            if self.verbose:
+                print(f"  FreqInterp: {len(ip.anchors)} anchor fills for {len(freqs)} frequencies "
+                      f"(order {ip.order}, k_e = {ip.k_ratio:.3f} k0)")
         nf, P = len(freqs), len(self.ports)
         S = np.zeros((nf, P, P), complex)
         gam = np.zeros((nf, P), complex)
@@ -602,7 +627,7 @@ class Solver:
                     fi = todo[nxt[0]]
                     nxt[0] += 1
                 try:
-                    out = sol.point(freqs[fi], keep_currents)
+                    out = ip.point(freqs[fi], keep_currents) if ip is not None else sol.point(freqs[fi], keep_currents)
                 except Exception as exc:  # noqa: BLE001 - re-raised below in the caller's thread
                     with lock:
                         errors.append(exc)
@@ -631,6 +656,10 @@ class Solver:
             raise errors[0]
         info = dict(seconds=time.time() - t0, refine_steps=[s for s in steps if s is not None], workers=workers,
                     fp64_fallback=[float(freqs[i]) for i, s in enumerate(steps) if s is not None and s < 0])
+        if ip is not None:
+            info.update(interp_fills=ip.n_fills, interp_anchors=len(ip.anchors), interp_fill_seconds=ip.fill_time)
+            if interp is not ip:
+                ip.close()  # made here ("auto"); a caller's FreqInterp keeps its anchors
         return SweepResult(freqs, S, zr, gam, zl, res, [p.name for p in self.ports],
                            cur if keep_currents else None, info)
 

@@ -7,7 +7,8 @@ machines without mom25d compare against them:
     python tests/golden/make_golden.py [--quick]
 
 Every case uses the sweep settings the parity tests assume: method="dense"
-(dense LU) and interp=None (an exact fill at every frequency).
+(dense LU) and interp=None (an exact fill at every frequency), except the
+*_interp fixtures (--interp), which record mom25d's FreqInterp.
 """
 
 import argparse
@@ -102,6 +103,37 @@ def case(name, freqs_full=None, zfull=False, zrows=None, sweep_freqs=None, kw=No
     print(f"{name}: N={m.n_unknowns} Nt={len(m.tris)} {len(sf)} freqs {dt:.1f} s ({dt / len(sf):.2f} s/pt)", flush=True)
 
 
+def interp_case(name, interp_kw=None, nfreq=None, zrows=None):
+    """FreqInterp (Engine/mom25d/freqinterp.py) on a case: the anchors, phase
+    ratio, step, basis centres, window and weights of every frequency, rows
+    of the interpolated Z at an off-anchor frequency and the S of the
+    interpolated sweep."""
+    from mom25d.freqinterp import FreqInterp
+
+    lay, stack, mkw, freqs = workloads.BUILDERS[name](ref)
+    if nfreq is not None:
+        freqs = np.linspace(min(freqs), max(freqs), nfreq)
+    m = lay.mesh(**mkw)
+    sol = ref.Solver(m, stack, verbose=False, method="dense")
+    ip = FreqInterp(**(interp_kw or {})).setup(sol, freqs)
+    out = dict(N=m.n_unknowns, mesh_sha=mesh_digest(m), freqs=np.asarray(freqs), anchors=ip.anchors,
+               k_ratio=ip.k_ratio, step=ip.step, order=ip.order, pos=ip.pos, nb=ip.nb)
+    out["windows"] = np.array([ip._window(f) for f in freqs])
+    out["weights"] = np.array([ip.weights(f, ip._window(f)) for f in freqs])
+    # the off-anchor frequency farthest from every anchor
+    fm = max(freqs, key=lambda f: np.min(np.abs(ip.anchors - f)))
+    Zi = ip.impedance(fm)
+    rows = np.unique(np.r_[zrows if zrows is not None else [0], m.n_unknowns - 1])
+    out.update(f_mid=fm, Z_rows_idx=rows, Zi_rows=Zi[rows])
+    t = time.time()
+    r = sol.sweep(freqs, interp=FreqInterp(**(interp_kw or {})))
+    dt = time.time() - t
+    out["sweep_seconds"] = dt
+    out.update(result_arrays(r))
+    np.savez_compressed(os.path.join(HERE, f"{name}_interp.npz"), **out)
+    print(f"{name} interp: N={m.n_unknowns} {len(freqs)} freqs, {len(ip.anchors)} anchors, {dt:.1f} s", flush=True)
+
+
 def kernels():
     """Known-answer vectors for the closed-form integrals and the slab kernels."""
     rng = np.random.default_rng(1)
@@ -131,8 +163,13 @@ def kernels():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true", help="small cases only")
+    ap.add_argument("--interp", action="store_true", help="only the FreqInterp fixtures")
     args = ap.parse_args()
     os.environ.setdefault("OPENBLAS_NUM_THREADS", "4")
+    if args.interp:
+        interp_case("tee", zrows=np.arange(0, 1085, 97))
+        interp_case("shunt_via", interp_kw=dict(step=1.5e9), nfreq=25, zrows=np.arange(0, 492, 41))
+        return
     kernels()
     case("line", zrows=np.arange(0, 546, 37))
     case("shunt_via", zrows=np.arange(0, 492, 41))
