@@ -310,7 +310,9 @@ int m25_interp_anchor(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_interp* 
  * the fill (Solver.sweep with a FreqInterp, solver.py:1273-1325 and
  * solve_currents 1012-1013): solve (precision M25_FP64 or M25_MIXED), then
  * de-embedding with the tables of gr. A mixed solve that does not reach tol
- * is redone in fp64 on the same interpolated Z (info[0] = -1). */
+ * is redone in fp64 on the same interpolated Z (info[0] = -1). ctx may be any
+ * context of the anchors' device: the anchors are read-only here, and the
+ * fills that wrote them must be complete (m25_ctx_synchronize on theirs). */
 int m25_interp_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* ports, m25_interp* ip, int32_t nuse,
                      const int32_t* slots, const double* L, double ke, int precision, const double* beta0, double tol,
                      int32_t max_iter, double* x_out, double* S, double* z0, double* gamma, double* z0_line,

@@ -917,7 +917,7 @@ extern "C" int m25_interp_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m2
                                 int32_t nuse, const int32_t* slots, const double* L, double ke, int precision,
                                 const double* beta0, double tol, int32_t max_iter, double* x_out, double* S,
                                 double* z0, double* gamma, double* z0_line, double* resid, int32_t* info) {
-  if (!ctx || !geom || !gr || !p || !ip || ip->ctx != ctx || ip->n != geom->nb + geom->nv) {
+  if (!ctx || !geom || !gr || !p || !ip || ip->ctx->device != ctx->device || ip->n != geom->nb + geom->nv) {
     set_error("m25_interp_point: bad argument");
     return M25_ERR_VALUE;
   }
@@ -930,7 +930,7 @@ extern "C" int m25_interp_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m2
   if ((rc = ctx->Zsweep.ensure(sizeof(zd) * (size_t)n * n))) return rc;
   if ((rc = ctx->Xsweep.ensure(sizeof(zd) * (size_t)n * P))) return rc;
   zd* Z = ctx->Zsweep.as<zd>();
-  if ((rc = interp_eval_device(ip, nuse, slots, L, gr->freq, ke, Z, n))) return rc;
+  if ((rc = interp_eval_device(ctx, ip, nuse, slots, L, gr->freq, ke, Z, n))) return rc;
   int32_t inf[2] = {0, 0};
   rc = m25_dense_solve(ctx, n, P, precision, Z, p->Bexc, ctx->Xsweep.p, M25_ON_DEVICE, tol, max_iter, inf);
   int used = precision;

@@ -11,8 +11,6 @@
 // carries the Im gV(0) correction, the same for every pair:
 // freqinterp.py:93-101). The anchor window and the weights are host logic
 // (mom25d_gb300/freqinterp.py).
-#include <algorithm>
-
 #include "m25_internal.h"
 
 namespace m25 {
@@ -32,29 +30,29 @@ __device__ __forceinline__ double basis_dist(const double* __restrict__ pos, int
   return sqrt(dx * dx + dy * dy + dz * dz);
 }
 
-// W = (j w) Z exp(+j ke R), in the order of the reference's product
+// W = (j w) Z exp(+j ke R), in the order of the reference's product; one CTA
+// per row (blockIdx.x), its threads along the row
 template <class TW>
 __global__ void interp_store_kernel(int n, int nb, const double* __restrict__ pos, const zd* __restrict__ Z,
                                     int64_t ldz, double w, double ke, cx<TW>* __restrict__ W) {
-  const int64_t tot = (int64_t)n * n;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
-    const int i = int(e / n), j = int(e - (int64_t)i * n);
+  const int i = blockIdx.x;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
     const zd z = Z[(int64_t)i * ldz + j];
     double s, c;
     sincos(ke * basis_dist(pos, nb, i, j), &s, &c);
     const zd jwz(-w * z.im, w * z.re);
     const zd v = jwz * zd(c, s);
-    W[e] = cx<TW>((TW)v.re, (TW)v.im);
+    W[(int64_t)i * n + j] = cx<TW>((TW)v.re, (TW)v.im);
   }
 }
 
-// Z = (sum_a L_a W_a) exp(-j ke R) / (j w)
+// Z = (sum_a L_a W_a) exp(-j ke R) / (j w); one CTA per row
 template <class TW>
 __global__ void interp_eval_kernel(int n, int nb, const double* __restrict__ pos, int nuse, EvalSrc src, double w,
                                    double ke, zd* __restrict__ Z, int64_t ldz) {
-  const int64_t tot = (int64_t)n * n;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
-    const int i = int(e / n), j = int(e - (int64_t)i * n);
+  const int i = blockIdx.x;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    const int64_t e = (int64_t)i * n + j;
     zd acc(0.0, 0.0);
     for (int a = 0; a < nuse; ++a) {
       const cx<TW> v = static_cast<const cx<TW>*>(src.W[a])[e];
@@ -67,14 +65,11 @@ __global__ void interp_eval_kernel(int n, int nb, const double* __restrict__ pos
   }
 }
 
-unsigned grid_for(const m25_ctx* ctx, int64_t tot) {
-  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((tot + 255) / 256, (int64_t)ctx->num_sms * 8));
-}
 
 }  // namespace
 
-int interp_eval_device(m25_interp* ip, int nuse, const int32_t* slots, const double* L, double freq, double ke,
-                       zd* Z, int64_t ldz) {
+int interp_eval_device(m25_ctx* ctx, m25_interp* ip, int nuse, const int32_t* slots, const double* L, double freq,
+                       double ke, zd* Z, int64_t ldz) {
   if (nuse < 1 || nuse > kMaxUse || !slots || !L) {
     set_error("m25_interp_eval: between 1 and 8 anchors");
     return M25_ERR_VALUE;
@@ -88,15 +83,11 @@ int interp_eval_device(m25_interp* ip, int nuse, const int32_t* slots, const dou
     src.W[a] = ip->slots[slots[a]];
     src.L[a] = L[a];
   }
-  const int64_t tot = (int64_t)ip->n * ip->n;
   const double w = 2.0 * kPi * freq;
-  m25_ctx* ctx = ip->ctx;
   if (ip->single)
-    interp_eval_kernel<float><<<grid_for(ctx, tot), 256, 0, ctx->stream>>>(ip->n, ip->nb, ip->pos, nuse, src, w, ke,
-                                                                           Z, ldz);
+    interp_eval_kernel<float><<<ip->n, 256, 0, ctx->stream>>>(ip->n, ip->nb, ip->pos, nuse, src, w, ke, Z, ldz);
   else
-    interp_eval_kernel<double><<<grid_for(ctx, tot), 256, 0, ctx->stream>>>(ip->n, ip->nb, ip->pos, nuse, src, w, ke,
-                                                                            Z, ldz);
+    interp_eval_kernel<double><<<ip->n, 256, 0, ctx->stream>>>(ip->n, ip->nb, ip->pos, nuse, src, w, ke, Z, ldz);
   M25_CHECK_LAUNCH();
   return M25_OK;
 }
@@ -165,14 +156,13 @@ extern "C" int m25_interp_store(m25_interp* ip, int32_t slot, const void* Z, int
     Zd = ctx->Zw.as<zd>();
     ldz = ip->n;
   }
-  const int64_t tot = (int64_t)ip->n * ip->n;
   const double w = 2.0 * kPi * freq;
   if (ip->single)
-    interp_store_kernel<float><<<grid_for(ctx, tot), 256, 0, ctx->stream>>>(
-        ip->n, ip->nb, ip->pos, Zd, ldz, w, ke, static_cast<zf*>(ip->slots[slot]));
+    interp_store_kernel<float><<<ip->n, 256, 0, ctx->stream>>>(ip->n, ip->nb, ip->pos, Zd, ldz, w, ke,
+                                                                 static_cast<zf*>(ip->slots[slot]));
   else
-    interp_store_kernel<double><<<grid_for(ctx, tot), 256, 0, ctx->stream>>>(
-        ip->n, ip->nb, ip->pos, Zd, ldz, w, ke, static_cast<zd*>(ip->slots[slot]));
+    interp_store_kernel<double><<<ip->n, 256, 0, ctx->stream>>>(ip->n, ip->nb, ip->pos, Zd, ldz, w, ke,
+                                                                  static_cast<zd*>(ip->slots[slot]));
   M25_CHECK_LAUNCH();
   if (where == M25_ON_HOST) M25_CUDA(cudaStreamSynchronize(ctx->stream));
   return M25_OK;
@@ -194,7 +184,7 @@ extern "C" int m25_interp_eval(m25_interp* ip, int32_t nuse, const int32_t* slot
     Zd = ctx->Zw.as<zd>();
     ld = ip->n;
   }
-  int rc = interp_eval_device(ip, nuse, slots, L, freq, ke, Zd, ld);
+  int rc = interp_eval_device(ctx, ip, nuse, slots, L, freq, ke, Zd, ld);
   if (rc) return rc;
   if (where == M25_ON_HOST) {
     M25_CUDA(cudaMemcpy2DAsync(Z, sizeof(zd) * ldz, Zd, sizeof(zd) * ip->n, sizeof(zd) * ip->n, ip->n,
@@ -207,7 +197,7 @@ extern "C" int m25_interp_eval(m25_interp* ip, int32_t nuse, const int32_t* slot
 extern "C" int m25_interp_anchor(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_interp* ip, int32_t slot,
                                  double zs_re, double zs_im, double zsv_re, double zsv_im, int precision, double ke) {
   if (!ctx || !geom || !gr || !ip || ip->ctx != ctx || ip->n != geom->nb + geom->nv) {
-    set_error("m25_interp_anchor: bad argument");
+    set_error("m25_interp_anchor: bad argument (the anchors are filled on the context that made them)");
     return M25_ERR_VALUE;
   }
   if (precision != M25_FP64 && precision != M25_MIXED) {

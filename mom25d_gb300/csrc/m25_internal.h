@@ -132,9 +132,10 @@ struct m25_interp {
 };
 
 namespace m25 {
-// Z (device, complex128, rows ldz apart) <- the interpolation of the anchors
-int interp_eval_device(m25_interp* ip, int nuse, const int32_t* slots, const double* L, double freq, double ke,
-                       zd* Z, int64_t ldz);
+// Z (device, complex128, rows ldz apart) <- the interpolation of the anchors,
+// on the stream of ctx (any context of the anchors' device)
+int interp_eval_device(m25_ctx* ctx, m25_interp* ip, int nuse, const int32_t* slots, const double* L, double freq,
+                       double ke, zd* Z, int64_t ldz);
 // output of the mixed fill as double-float planes and the complex64 LU input
 struct FillSplit {
   zf *Zh, *Zl, *LU;

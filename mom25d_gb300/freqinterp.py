@@ -5,12 +5,16 @@ Z is filled exactly at evenly spaced anchor frequencies. With the propagation
 phase between basis functions taken out and the 1/(j w) of the scalar
 potential undone, W = j w Z exp(+j k_e R_mn) is smooth in frequency; between
 anchors it is Lagrange-interpolated from the order + 1 nearest anchors and
-Z = W~ exp(-j k_e R) / (j w). The anchors live on the device (m25_interp: the
-order + 1 matrices in use, complex128 unless that would take more than about
-half the free device memory, then complex64); the interpolation, the solve
-and the de-embedding of a point run there (m25_interp_point). The window,
-the weights and the choice of anchors are the reference's, so an ascending
-sweep fills every anchor once.
+Z = W~ exp(-j k_e R) / (j w). The anchors live on the device (m25_interp,
+complex128 unless that would take more than about half the free device
+memory, then complex64); the interpolation, the solve and the de-embedding of
+a point run there (m25_interp_point). The window, the weights and the choice
+of anchors are the reference's. Where every anchor of the band fits in the
+device memory (a few GB at N ~ 6k) they are all filled first and kept
+("resident"): the points then depend on nothing but the anchors and run on
+the sweep's concurrent workers like exact-fill points. Otherwise the order + 1
+anchors of the window are kept, as in mom25d, and an ascending sweep fills
+every anchor once.
 """
 
 import ctypes as C
@@ -37,12 +41,17 @@ class FreqInterp:
                row blocks; the device kernels need none)
     dtype    : None (complex128 if it fits, else complex64), np.complex128 or
                np.complex64 storage of the anchors
+    resident : None: keep every anchor of the band on the device when they
+               take less than 40 % of the free device memory; True / False
+               force it (an addition to the reference's signature)
     (Engine/mom25d/freqinterp.py:27-88)
     """
 
-    def __init__(self, step=None, order=3, k_ratio=None, check=False, block=1024, dtype=None):
+    def __init__(self, step=None, order=3, k_ratio=None, check=False, block=1024, dtype=None, resident=None):
         self.step, self.order, self.k_ratio, self.check, self.block = step, order, k_ratio, check, block
         self.dtype = dtype
+        self.resident = resident
+        self._resident = False  # this setup's choice
         self.solver = None
         self._ip = None
 
@@ -73,19 +82,36 @@ class FreqInterp:
         if self._ip is None:
             sol = self.solver
             N = len(self.pos)
+            free, total = C.c_uint64(), C.c_uint64()
+            E.check(sol.ctx.lib.m25_ctx_mem_info(sol.ctx.h, C.byref(free), C.byref(total)))
             if self.dtype is None:
-                free, total = C.c_uint64(), C.c_uint64()
-                E.check(sol.ctx.lib.m25_ctx_mem_info(sol.ctx.h, C.byref(free), C.byref(total)))
                 need = (self.order + 1) * N * N * 16 + 3 * N * N * 16  # anchors + Z + LU work
                 self.dtype = np.complex128 if need < 0.5 * free.value else np.complex64
             single = int(np.dtype(self.dtype) == np.complex64)
+            fits = len(self.anchors) * N * N * np.dtype(self.dtype).itemsize < 0.4 * free.value
+            self._resident = fits if self.resident is None else bool(self.resident)
+            nslots = len(self.anchors) if self._resident else self.order + 1
             h = C.c_void_p()
             pos = np.ascontiguousarray(self.pos, np.float64)
-            E.check(sol.ctx.lib.m25_interp_create(sol.ctx.h, N, self.nb, E.ptr(pos), self.order + 1, single,
-                                                  C.byref(h)))
+            E.check(sol.ctx.lib.m25_interp_create(sol.ctx.h, N, self.nb, E.ptr(pos), nslots, single, C.byref(h)))
             self._ip = E.Handle(sol.ctx, h, sol.ctx.lib.m25_interp_destroy)
-            self._free = list(range(self.order + 1))
+            self._free = list(range(nslots))
         return self._ip
+
+    def fill_all(self, freqs=None):
+        """Resident anchors: fill every anchor now (and run the check at the
+        first frequency of freqs between anchors), so that points can then
+        be taken in any order and by several workers."""
+        self._device()
+        if not self._resident:
+            raise RuntimeError("the anchors of this band do not fit in the device memory together")
+        self._slots(list(range(len(self.anchors))))
+        if not self._checked and freqs is not None:
+            for f in freqs:
+                if np.min(np.abs(self.anchors - f)) > 0.25 * self.step:
+                    self.impedance(f)
+                    break
+            self._checked = True
 
     def _window(self, f):
         """Indices of the order+1 anchors used at f: centred on the anchor
@@ -114,9 +140,10 @@ class FreqInterp:
         import time
 
         ip = self._device()
-        for i in list(self._slot_of):
-            if i not in idx:
-                self._free.append(self._slot_of.pop(i))
+        if not self._resident:
+            for i in list(self._slot_of):
+                if i not in idx:
+                    self._free.append(self._slot_of.pop(i))
         sol = self.solver
         for i in idx:
             if i in self._slot_of:
@@ -152,14 +179,21 @@ class FreqInterp:
             self.report_error(f, Z)
         return Z
 
-    def point(self, f, keep_currents=False):
+    def point(self, f, keep_currents=False, solver=None):
         """One sweep point with the interpolated Z: the outputs of
-        Solver.point (S, z0, gamma, z0_line, residual, currents, info)."""
-        sol = self.solver
-        if not self._checked and np.min(np.abs(self.anchors - f)) > 0.25 * self.step:
-            self.impedance(f)  # prints the check
+        Solver.point (S, z0, gamma, z0_line, residual, currents, info).
+        solver: a concurrent worker of the sweep (its own engine context) that
+        reads resident anchors; default the solver of setup."""
+        sol = solver or self.solver
         idx = self._window(f)
-        slots = np.array(self._slots(idx), np.int32)
+        if sol is not self.solver:
+            if not self._resident or any(i not in self._slot_of for i in idx):
+                raise RuntimeError("another worker's point needs resident, filled anchors (fill_all)")
+            slots = np.array([self._slot_of[i] for i in idx], np.int32)
+        else:
+            if not self._checked and np.min(np.abs(self.anchors - f)) > 0.25 * self.step:
+                self.impedance(f)  # prints the check
+            slots = np.array(self._slots(idx), np.int32)
         L = self.weights(f, idx)
         g = sol.greens(f)
         P = len(sol.ports)

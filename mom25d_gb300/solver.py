@@ -563,8 +563,9 @@ class Solver:
         the GPU to the others); points are handed out in order as workers
         become free. Fewer workers run when their buffers would not fit in
         the free device memory (result.info["workers"]). An interpolated
-        sweep runs on one worker, in the order of freqs (its anchors are
-        shared by the points)."""
+        sweep fills its anchors first when they all fit on the device
+        (FreqInterp resident) and then runs its points like an exact one;
+        otherwise it runs on one worker in the order of freqs."""
         freqs = np.atleast_1d(np.asarray(freqs, float))
         ip = None
         if isinstance(interp, str):
@@ -578,10 +579,14 @@ class Solver:
         elif interp is not None:
             ip = interp.setup(self, freqs)
         if ip is not None:
-            workers = 1
             if self.verbose:
                 print(f"  FreqInterp: {len(ip.anchors)} anchor fills for {len(freqs)} frequencies "
                       f"(order {ip.order}, k_e = {ip.k_ratio:.3f} k0)")
+            ip._device()
+            if ip._resident:
+                ip.fill_all(freqs)
+            else:
+                workers = 1
         nf, P = len(freqs), len(self.ports)
         S = np.zeros((nf, P, P), complex)
         gam = np.zeros((nf, P), complex)
@@ -627,7 +632,10 @@ class Solver:
                     fi = todo[nxt[0]]
                     nxt[0] += 1
                 try:
-                    out = ip.point(freqs[fi], keep_currents) if ip is not None else sol.point(freqs[fi], keep_currents)
+                    if ip is not None:
+                        out = ip.point(freqs[fi], keep_currents, solver=sol)
+                    else:
+                        out = sol.point(freqs[fi], keep_currents)
                 except Exception as exc:  # noqa: BLE001 - re-raised below in the caller's thread
                     with lock:
                         errors.append(exc)

@@ -83,3 +83,17 @@ def test_interpolated_sweep_auto_and_mixed(gpu):
     assert r.info["interp_anchors"] == len(g["anchors"])
     assert np.abs(r.S - g["S"]).max() < 1e-5
     sol.close()
+
+
+def test_resident_anchors_on_concurrent_workers(gpu):
+    """Resident anchors (all filled first) read by four workers give the S of
+    the windowed single-worker sweep (the same anchors, the same kernels)."""
+    g = golden("tee_interp")
+    lay, st, m, _ = workloads.build(G, "tee")
+    sol = Solver(m, st, verbose=False)
+    r1 = sol.sweep(g["freqs"], interp=FreqInterp(resident=False))
+    assert r1.info["workers"] == 1
+    r4 = sol.sweep(g["freqs"], interp=FreqInterp(resident=True), workers=4)
+    assert r4.info["workers"] == 4 and r4.info["interp_fills"] == len(g["anchors"])
+    assert np.abs(r4.S - r1.S).max() < 1e-12
+    sol.close()
