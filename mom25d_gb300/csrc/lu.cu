@@ -1530,7 +1530,9 @@ int lu_solve_wave(m25_ctx* ctx, const cx<TF>* A, int64_t lda, int n, const int32
     set_error("dense solve: the triangular-solve kernel does not fit on an SM");
     return M25_ERR_CUDA;
   }
-  const int G = std::min(nblk, ctx->num_sms * occ);
+  // M25_WAVE_CTAS: at most this many CTAs (a tuning knob; 0 or unset = one per block up to the device's fill)
+  static const int wave_cap = getenv("M25_WAVE_CTAS") ? atoi(getenv("M25_WAVE_CTAS")) : 0;
+  const int G = std::min(std::min(nblk, ctx->num_sms * occ), wave_cap > 0 ? wave_cap : nblk);
   StageTimer tm(ctx, ST_TRSV);
   if (!perm) {
     if (ctx->ext_flags) {  // no room for a permutation in a caller-provided flag buffer
