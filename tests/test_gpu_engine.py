@@ -359,6 +359,33 @@ def test_lu_complex64_tensor_cores_reconstruct(gpu, n):
     ctx.close()
 
 
+@pytest.mark.parametrize("n", [40, 64, 65, 127, 128, 129, 193, 257, 511])
+def test_lu_complex64_tensor_cores_small_and_odd_orders(gpu, n):
+    """The blocked tensor-core LU on small and odd orders, rows padded to an
+    even length (16-byte rows, as the mixed solve stores its LU): a single
+    panel, a block without a second panel's full width, blocks that end
+    exactly, and odd trailing sizes of the rank-64 and rank-128 updates."""
+    import ctypes as C
+
+    from mom25d_gb300 import engine as E
+
+    ctx = E.Context(0)
+    rng = np.random.default_rng(1000 + n)
+    lda = n + (n & 1)
+    A = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))).astype(np.complex64)
+    F = np.zeros((n, lda), np.complex64)
+    F[:, :n] = A
+    piv = np.zeros(n, np.int32)
+    info = np.zeros(1, np.int32)
+    E.check(ctx.lib.m25_lu_factor(ctx.h, n, E.M25_MIXED, F.ctypes.data, lda, E.ptr(piv, C.c_int32), E.M25_ON_HOST,
+                                  0, E.ptr(info, C.c_int32)))
+    LU, perm = _lu_reconstruct(F[:, :n].astype(np.complex128), piv)
+    err = np.abs(LU - A[perm]).max() / np.abs(A).max()
+    assert info[0] == 0
+    assert err < 5e-5, err
+    ctx.close()
+
+
 # ------------------------------------------------------- concurrent points
 def test_sweep_workers_match_one_worker(gpu):
     """Points in flight on separate engine contexts give the results of the

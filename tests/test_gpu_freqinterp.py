@@ -97,3 +97,15 @@ def test_resident_anchors_on_concurrent_workers(gpu):
     assert r4.info["workers"] == 4 and r4.info["interp_fills"] == len(g["anchors"])
     assert np.abs(r4.S - r1.S).max() < 1e-12
     sol.close()
+
+
+def test_complex64_anchors(gpu):
+    """complex64 anchors (the reference's choice when complex128 would not
+    fit) stay within its stated ~5e-5 of the complex128 interpolation at low
+    frequency (bound 5e-4 over the tee's band)."""
+    g = golden("tee_interp")
+    lay, st, m, _ = workloads.build(G, "tee")
+    sol = Solver(m, st, verbose=False)
+    r = sol.sweep(g["freqs"], interp=FreqInterp(dtype=np.complex64))
+    assert np.abs(r.S - g["S"]).max() < 5e-4
+    sol.close()
