@@ -318,6 +318,12 @@ int m25_interp_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* po
                      int32_t max_iter, double* x_out, double* S, double* z0, double* gamma, double* z0_line,
                      double* resid, int32_t* info);
 
+/* Incident current-wave amplitudes A (P, P) complex128 host, row = port,
+ * column = excitation, of the last de-embedding on these ports (m25_deembed,
+ * m25_sweep_point, m25_interp_point): SweepResult.waves, solver.py:683,
+ * 1309-1312 (S = D (-B A^-1) D^-1). */
+int m25_deembed_waves(m25_ports* ports, double* A);
+
 /* Diagnostics of the last m25_deembed: phi (sum nvpt, P) complex128 line
  * voltages, q (nt, P) complex128 triangle charges, I and V (sum ns, P)
  * complex128 cut currents / voltages. NULL skips an output. */

@@ -611,6 +611,7 @@ struct m25_ports {
   zd* Bexc = nullptr;  // (n, P) excitation columns
   int* iters = nullptr;
   int nt = 0, n = 0;
+  std::vector<zd> waves;  // (P, P) incident current-wave amplitudes A of the last de-embedding
   std::vector<void*> allocs;
 };
 
@@ -822,6 +823,7 @@ static int deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, c
   const zd* hz = hg + kMaxPorts;
   const double* hr = reinterpret_cast<const double*>(hz + kMaxPorts);
   const double* hz0 = hr + kMaxPorts;
+  p->waves.assign(h.begin(), h.begin() + (size_t)P * P);  // A[port][excitation]
   for (int i = 0; i < P; ++i) {
     for (int j = 0; j < P; ++j) {
       if (S) {
@@ -833,6 +835,22 @@ static int deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, c
     if (z0_line) { z0_line[2 * i] = hz[i].re; z0_line[2 * i + 1] = hz[i].im; }
     if (resid) resid[i] = hr[i];
     if (z0) z0[i] = hz0[i];
+  }
+  return M25_OK;
+}
+
+extern "C" int m25_deembed_waves(m25_ports* p, double* A) {
+  if (!p || !A) {
+    set_error("m25_deembed_waves: null argument");
+    return M25_ERR_VALUE;
+  }
+  if (p->waves.size() != (size_t)p->P * p->P) {
+    set_error("m25_deembed_waves: no de-embedding yet");
+    return M25_ERR_VALUE;
+  }
+  for (size_t k = 0; k < p->waves.size(); ++k) {
+    A[2 * k] = p->waves[k].re;
+    A[2 * k + 1] = p->waves[k].im;
   }
   return M25_OK;
 }

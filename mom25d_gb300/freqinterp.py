@@ -214,7 +214,8 @@ class FreqInterp:
             F(zl), E.ptr(res), E.ptr(info, C.c_int32)))
         g.close()
         return sol._fixed_z0(S, z0) + (gam, zl, res, x, dict(refine_steps=int(info[0]),
-                                                               fp64_fallback=bool(info[0] < 0)))
+                                                               fp64_fallback=bool(info[0] < 0),
+                                                               waves=sol.last_waves()))
 
     def report_error(self, f, Zi=None):
         """Relative interpolation error of Z at f (one exact fill), per block

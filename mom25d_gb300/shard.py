@@ -78,4 +78,5 @@ def sweep_sharded(solver, freqs, rank=0, world=1, group=None):
     return SweepResult(freqs=freqs, S=np.array([r[0] for r in rows]), z0=np.array([r[1] for r in rows]),
                        gamma=np.array([r[2] for r in rows]), z0_line=np.array([r[3] for r in rows]),
                        fit_residual=np.array([r[4] for r in rows]), port_names=[p.name for p in solver.ports],
+                       waves=np.array([r[5]["waves"] for r in rows]) if rows and "waves" in rows[0][5] else None,
                        info=dict(refine_steps=[r[5]["refine_steps"] for r in rows], ranks=world))

@@ -203,7 +203,8 @@ class SweepResult:
     z0_line: np.ndarray  # (F,P)
     fit_residual: np.ndarray  # (F,P)
     port_names: list
-    currents: list = None
+    currents: list = None  # per frequency: (N, P) coefficients (keep_currents=True)
+    waves: np.ndarray = None  # (F, P, P) incident current-wave amplitudes A [port, excitation]
     info: dict = None
 
     @property
@@ -220,6 +221,51 @@ class SweepResult:
             Zm = sq @ (eye + S) @ np.linalg.inv(eye - S) @ sq
             out[f] = (Zm - zref * eye) @ np.linalg.inv(Zm + zref * eye)
         return out
+
+    def matched_currents(self, fi, port):
+        """Coefficients at frequency index fi for a unit incident current wave
+        on `port`, the other ports terminated in their line impedance: the
+        delta-gap solutions combined by the inverse of the wave amplitudes
+        (Engine/mom25d/solver.py:685-694)."""
+        if self.currents is None or self.waves is None:
+            raise ValueError("run sweep(..., keep_currents=True)")
+        e = np.zeros(self.waves.shape[1])
+        e[port] = 1.0
+        return self.currents[fi] @ np.linalg.solve(self.waves[fi], e)
+
+    def wave_currents(self, fi, a50, z0=50.0):
+        """Coefficients at frequency index fi for incident power waves a50
+        (one per port, reference z0) at the ports (solver.py:740-750)."""
+        if self.currents is None or self.waves is None:
+            raise ValueError("run sweep(..., keep_currents=True)")
+        a = np.asarray(a50, complex)
+        b = self.renormalize(z0)[fi] @ a
+        V = np.sqrt(z0) * (a + b)  # port voltage and current into the layout
+        I = (a - b) / np.sqrt(z0)
+        A = 0.5 * (I + V / self.z0[fi])  # incident current waves on the line reference
+        return self.currents[fi] @ np.linalg.solve(self.waves[fi], A)
+
+    def connect(self, model, pairs, z0=None, name=None):
+        """Join S-parameter blocks to ports of this result (solver.py:711-738).
+        model: network.Touchstone or a .sNp path; pairs: [(port name or
+        index, block port 1..n), ...]; z0: common reference (default the
+        block's). Returns a network.Network on the remaining ports: the
+        layout's, then the block's free ports named '<name>.<k>'."""
+        from .network import Network, Touchstone, connect
+
+        if isinstance(model, str):
+            model = Touchstone(model)
+        z0 = z0 or getattr(model, "z0", 50.0)
+        name = name or getattr(model, "path", "block").rsplit("/", 1)[-1].rsplit(".", 1)[0]
+        SA = self.renormalize(z0)
+        SB = np.array([model.s(f) for f in self.freqs])
+        na = SA.shape[-1]
+        pa = [(self.port_names.index(a) if isinstance(a, str) else int(a), int(b) - 1) for a, b in pairs]
+        S, idx = connect(SA, SB, pa)
+        names = [self.port_names[i] if i < na else f"{name}.{i - na + 1}" for i in idx]
+        net = Network(self.freqs, S, names, z0)
+        net._source = (self, model, pa, idx, z0)
+        return net
 
     def db(self, i, j, S=None):
         S = self.S if S is None else S
@@ -460,7 +506,16 @@ class Solver:
         S, z0 = self._fixed_z0(S, z0)
         # refine_steps -1: the mixed refinement did not reach refine_tol and
         # the point was recomputed on the fp64 path
-        return S, z0, gam, zl, res, x, dict(refine_steps=int(info[0]), fp64_fallback=bool(info[0] < 0))
+        return S, z0, gam, zl, res, x, dict(refine_steps=int(info[0]), fp64_fallback=bool(info[0] < 0),
+                                            waves=self.last_waves())
+
+    def last_waves(self):
+        """(P, P) incident current-wave amplitudes A [port, excitation] of the
+        last de-embedding on this solver's context (SweepResult.waves)."""
+        P = len(self.ports)
+        A = np.zeros((P, P), complex)
+        E.check(self.ctx.lib.m25_deembed_waves(self.port_data().h, E.ptr(A.view(np.float64))))
+        return A
 
     def _fixed_z0(self, S, z0):
         """S referenced to the fixed port impedances when the solver has them."""
@@ -594,6 +649,7 @@ class Solver:
         zr = np.zeros((nf, P))
         res = np.zeros((nf, P))
         cur = [None] * nf
+        waves = np.zeros((nf, P, P), complex)
         done = np.zeros(nf, bool)
         key = self._checkpoint_key(freqs) if checkpoint else None
         if checkpoint and os.path.exists(checkpoint) and not keep_currents:
@@ -603,6 +659,8 @@ class Solver:
                         and ck["S"].shape == S.shape:
                     done = ck["done"].astype(bool)
                     S[:], gam[:], zl[:], zr[:], res[:] = (ck[k] for k in ("S", "gam", "zl", "zr", "res"))
+                    if "waves" in ck.files:
+                        waves[:] = ck["waves"]
             except Exception as exc:  # noqa: BLE001 - unreadable: start afresh
                 if self.verbose:
                     print(f" checkpoint: unreadable ({exc}); starting afresh", flush=True)
@@ -642,13 +700,14 @@ class Solver:
                     return
                 with lock:
                     S[fi], zr[fi], gam[fi], zl[fi], res[fi], cur[fi], inf = out
+                    waves[fi] = inf["waves"]
                     steps[fi] = inf["refine_steps"]
                     done[fi] = True
                     if self.verbose:
                         print(f"PROGRESS {int(done.sum())}/{nf}", flush=True)
                     if checkpoint:
                         tmp = checkpoint + ".tmp.npz"
-                        np.savez(tmp, key=key, done=done, S=S, gam=gam, zl=zl, zr=zr, res=res)
+                        np.savez(tmp, key=key, done=done, S=S, gam=gam, zl=zl, zr=zr, res=res, waves=waves)
                         os.replace(tmp, checkpoint)
 
         t0 = time.time()
@@ -669,7 +728,7 @@ class Solver:
             if interp is not ip:
                 ip.close()  # made here ("auto"); a caller's FreqInterp keeps its anchors
         return SweepResult(freqs, S, zr, gam, zl, res, [p.name for p in self.ports],
-                           cur if keep_currents else None, info)
+                           cur if keep_currents else None, waves, info=info)
 
     def close(self):
         for sib in self._siblings:

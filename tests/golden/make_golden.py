@@ -134,6 +134,39 @@ def interp_case(name, interp_kw=None, nfreq=None, zrows=None):
     print(f"{name} interp: N={m.n_unknowns} {len(freqs)} freqs, {len(ip.anchors)} anchors, {dt:.1f} s", flush=True)
 
 
+def write_block(path, freqs):
+    """A synthetic 2-port (attenuator with a phase delay, slightly unmatched)
+    as a Touchstone v1 file in MA format with a GHz axis, 50 ohm."""
+    with open(path, "w") as fh:
+        fh.write("! synthetic 2-port block for the network tests\n# GHZ S MA R 50\n")
+        for f in freqs:
+            ph = -360.0 * f / 4e9
+            s11, s21 = 0.08 * (1 + f / 20e9), 0.7 - 0.01 * f / 1e9
+            # Touchstone v1 2-port order: S11 S21 S12 S22
+            fh.write(f"{f / 1e9:.6f} {s11:.6f} {ph / 3:.4f} {s21:.6f} {ph:.4f} {s21:.6f} {ph:.4f} "
+                     f"{s11 * 1.1:.6f} {ph / 2:.4f}\n")
+
+
+def network_case():
+    """SweepResult waves, matched / wave currents and connect (Engine/mom25d/
+    solver.py:673-765, network.py) on the line case with a synthetic block."""
+    lay, stack, mkw, freqs = workloads.BUILDERS["line"](ref)
+    m = lay.mesh(**mkw)
+    sol = ref.Solver(m, stack, verbose=False, method="dense")
+    g = np.load(os.path.join(HERE, "line.npz"))
+    fr = g["freqs"]
+    r = sol.sweep(fr, interp=None, keep_currents=True)
+    block = os.path.join(HERE, "block.s2p")
+    write_block(block, np.linspace(0.5 * fr.min(), 1.5 * fr.max(), 9))
+    net = r.connect(block, [(1, 1)])
+    out = dict(freqs=fr, S=r.S, z0=r.z0, gamma=r.gamma, z0_line=r.z0_line, fit_residual=r.fit_residual,
+               waves=r.waves, port_names=np.array(r.port_names), matched0=r.matched_currents(0, 0),
+               wave0=r.wave_currents(0, [1.0, 0.5j]), net_S=net.S, net_names=np.array(net.names),
+               net_currents0=net.currents(0, 0))
+    np.savez_compressed(os.path.join(HERE, "line_network.npz"), **out)
+    print("network: done", flush=True)
+
+
 def kernels():
     """Known-answer vectors for the closed-form integrals and the slab kernels."""
     rng = np.random.default_rng(1)
@@ -164,8 +197,12 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true", help="small cases only")
     ap.add_argument("--interp", action="store_true", help="only the FreqInterp fixtures")
+    ap.add_argument("--network", action="store_true", help="only the network / waves fixture")
     args = ap.parse_args()
     os.environ.setdefault("OPENBLAS_NUM_THREADS", "4")
+    if args.network:
+        network_case()
+        return
     if args.interp:
         interp_case("tee", zrows=np.arange(0, 1085, 97))
         interp_case("shunt_via", interp_kw=dict(step=1.5e9), nfreq=25, zrows=np.arange(0, 492, 41))
