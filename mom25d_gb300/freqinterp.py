@@ -185,6 +185,13 @@ class FreqInterp:
         solver: a concurrent worker of the sweep (its own engine context) that
         reads resident anchors; default the solver of setup."""
         sol = solver or self.solver
+        if sol.Lm is not None:  # lumped loads: the interpolated Z through the host solve and Woodbury
+            if sol is not self.solver:
+                raise RuntimeError("lumped loads with an interpolated Z run on the sweep's own solver")
+            g = sol.greens(f)
+            out = sol._lumped_point(f, g, self.impedance(f), keep_currents)
+            g.close()
+            return out
         idx = self._window(f)
         if sol is not self.solver:
             if not self._resident or any(i not in self._slot_of for i in idx):

@@ -177,6 +177,31 @@ class Layout:
         self.vias.extend(p.ground_vias())
         return p
 
+    def add_lumped(self, name, a, b, width, value=None, layer="top"):
+        """Lumped component across a delta gap in the middle of a copper
+        bridge of `width` from pad point a to pad point b (axis-aligned),
+        loaded with `value` (lumped.R / L / C / series / parallel, a number in
+        ohm, a callable f -> Z, a string like 'C 1p' or 'R 10 + L 0.5n'; None:
+        an open gap); voltage a -> b (mom25d/mesh.py:353-378)."""
+        from .lumped import as_value, parse
+
+        a, b = np.asarray(a, float), np.asarray(b, float)
+        d = b - a
+        length = float(np.hypot(*d))
+        if length <= 0:
+            raise ValueError("lumped component: a and b coincide")
+        if any(q.name == name for q in self.lumped) or any(q.name == name for q in self.ports):
+            raise ValueError(f"name {name!r} already used")
+        u = d / length
+        direction = next((k for k, v in _DIRS.items() if np.allclose(u, v, atol=1e-12)), None)
+        if direction is None:
+            raise ValueError(f"lumped {name}: oblique bridges need the triangular mesher (not part of this engine)")
+        g = Port(name, tuple(a), direction, width, length, gap_from_end=0.5 * length, layer=layer)
+        g.value = None if value is None else (parse(value) if isinstance(value, str) else as_value(value))
+        self.lumped.append(g)
+        self.add_rect(*g.rect(), layer=layer)
+        return g
+
     def add_via(self, x, y, drill=0.3e-3, pad=None, name=None, top="top", bottom="gnd"):
         v = Via((x, y), drill, pad, name, top, bottom)
         self.vias.append(v)
@@ -250,6 +275,8 @@ class Mesh:
         fy = [c for r in layout.rects for c in (r[1], r[3])]
         for p in layout.ports:
             (fx if p.axis == 0 else fy).extend([p.coord(0), p.coord(p.s_gap)])
+        for p in layout.lumped:  # a lumped gap and its bridge's ends are grid lines
+            (fx if p.axis == 0 else fy).extend([p.coord(0), p.coord(p.s_gap), p.coord(p.length)])
         rx, ry = [], []
         if edge_cell:
             rx = [c + d for c in fx for d in (-edge_cell, edge_cell)]
@@ -396,6 +423,19 @@ class Mesh:
         s = port.sgn * (g - port.ref[port.axis])
         s = s[(s > -1e-12) & (s <= port.length + 1e-12)]
         return np.sort(s)
+
+    def lumped_vectors(self):
+        """(N, n_lumped) signed edge lengths of each lumped gap's cut: the
+        delta-gap excitation of the gap, and l . x its current a -> b
+        (mom25d/mesh.py:1077-1087)."""
+        gaps = list(getattr(self.layout, "lumped", []))
+        Lm = np.zeros((self.n_unknowns, len(gaps)))
+        for k, p in enumerate(gaps):
+            idx, sgn = self.cut_edges(p, p.s_gap)
+            if idx.size == 0:
+                raise ValueError(f"lumped {p.name}: no mesh edges on its gap")
+            Lm[idx, k] = -sgn * self.edge_len[idx]
+        return Lm
 
     def cut_edges(self, port, s):
         """RWG edges on the transverse cut at distance s of a feed, signed so

@@ -328,8 +328,12 @@ class Solver:
         self.ports = mesh.layout.ports
         if not self.ports:
             raise ValueError("layout has no ports")
-        if getattr(mesh.layout, "lumped", None) or getattr(mesh.layout, "internal_ports", None):
-            raise ValueError("lumped components and internal ports are not part of this engine")
+        if getattr(mesh.layout, "components", None) or getattr(mesh.layout, "internal_ports", None):
+            raise ValueError("multi-port components and internal ports are not part of this engine")
+        # lumped components across delta gaps: loaded after the solve (Woodbury)
+        self.lumped = list(getattr(mesh.layout, "lumped", []))
+        self.Lm = mesh.lumped_vectors() if self.lumped else None
+        self.values = {}  # per-sweep overrides of lumped values
         self.method = "dense"
         self.precision = precision
         self.refine_tol, self.max_refine = refine_tol, max_refine
@@ -483,8 +487,72 @@ class Solver:
         return dense_solve(Z, B, precision=self.precision, ctx=self.ctx, tol=self.refine_tol,
                            max_iter=self.max_refine)
 
+    OPEN = 1e12  # ohm: an unloaded lumped gap
+
+    def lumped_impedance(self, freq):
+        """D (n_lumped, n_lumped): the impedance of the component across each
+        lumped gap at freq, OPEN where none (Engine/mom25d/solver.py:1039-1062
+        without multi-port components and internal ports)."""
+        from .lumped import as_value, parse
+
+        D = np.zeros((len(self.lumped), len(self.lumped)), complex)
+        for k, q in enumerate(self.lumped):
+            v = self.values.get(q.name, getattr(q, "value", None))
+            if isinstance(v, str):
+                v = parse(v)
+            D[k, k] = self.OPEN if v is None else as_value(v).z(freq)
+        return D
+
+    def _load_lumped(self, Xe, Xi, freq):
+        """The solution with the components across the gaps: (Z + L D L^T)^-1 e
+        = Xe - Xi D (I + L^T Xi D)^-1 L^T Xe (Woodbury), Xi = Z^-1 L
+        (solver.py:1064-1070)."""
+        D = self.lumped_impedance(freq)
+        M = self.Lm.T @ Xi
+        y = self.Lm.T @ Xe
+        return Xe - Xi @ (D @ np.linalg.solve(np.eye(len(D)) + M @ D, y))
+
+    def lumped_currents(self, x):
+        """Current a -> b through each lumped gap, (n_lumped, Nexc)."""
+        return self.Lm.T @ x
+
+    def _lumped_point(self, f, g, Z, keep_currents):
+        """A point with lumped loads: one solve for the port and gap
+        excitations, the loads by Woodbury on the host, then the
+        de-embedding of the loaded currents on the device."""
+        P = len(self.ports)
+        E0 = self.port_excitations()
+        B = np.hstack([E0, self.Lm])
+        prec = "fp64" if self.precision == "fp64" else "mixed"
+        steps = 0
+        try:
+            X = dense_solve(Z, B, precision=prec, ctx=self.ctx, tol=self.refine_tol, max_iter=self.max_refine)
+        except RuntimeError:
+            if prec == "fp64":
+                raise
+            X = dense_solve(Z, B, precision="fp64", ctx=self.ctx)
+            steps = -1
+        x = np.ascontiguousarray(self._load_lumped(X[:, :P], X[:, P:], f))
+        S = np.zeros((P, P), complex)
+        z0 = np.zeros(P)
+        gam = np.zeros(P, complex)
+        zl = np.zeros(P, complex)
+        res = np.zeros(P)
+        b0 = E.f64(self.beta0(f))
+        F = lambda a: E.ptr(a.view(np.float64))  # noqa: E731
+        E.check(self.ctx.lib.m25_deembed(self.ctx.h, self.geometry().h, g.h, self.port_data().h, x.ctypes.data,
+                                         E.M25_ON_HOST, E.ptr(b0), F(S), E.ptr(z0), F(gam), F(zl), E.ptr(res)))
+        S, z0 = self._fixed_z0(S, z0)
+        return S, z0, gam, zl, res, (x if keep_currents else None), dict(
+            refine_steps=steps, fp64_fallback=steps < 0, waves=self.last_waves())
+
     def point(self, f, keep_currents=False):
         """One frequency of the sweep on the device: (S, z0, gamma, z0_line, residual, x or None, info)."""
+        if self.Lm is not None:
+            g = self.greens(f)
+            out = self._lumped_point(f, g, self.impedance(f, g), keep_currents)
+            g.close()
+            return out
         g = self.greens(f)
         P = len(self.ports)
         n = self.mesh.n_unknowns
@@ -622,6 +690,8 @@ class Solver:
         (FreqInterp resident) and then runs its points like an exact one;
         otherwise it runs on one worker in the order of freqs."""
         freqs = np.atleast_1d(np.asarray(freqs, float))
+        self.values.clear()  # shared with the sweep's workers
+        self.values.update(values or {})
         ip = None
         if isinstance(interp, str):
             if interp != "auto":
@@ -640,7 +710,7 @@ class Solver:
             ip._device()
             if ip._resident:
                 ip.fill_all(freqs)
-            else:
+            if not ip._resident or self.Lm is not None:
                 workers = 1
         nf, P = len(freqs), len(self.ports)
         S = np.zeros((nf, P, P), complex)

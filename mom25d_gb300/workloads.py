@@ -13,6 +13,7 @@ returns (layout, stack, mesh keyword arguments, frequencies [Hz]).
   gcpw       30 mm grounded CPW with via fences on 0.508 mm eps_r 3.55, 64 f 1-20 GHz
   line       short through line (small N, test case)
   shunt_via  short line with a via to ground (small N, test case)
+  lumped_line  two line sections joined by a lumped component (R 20 + L 0.5n) across a gap
 """
 
 import numpy as np
@@ -123,7 +124,22 @@ def shunt_via(api):
     return lay, sub, dict(max_cell=0.35 * mm, edge_cell=0.08 * mm), np.array([3.0, 9.0]) * GHz
 
 
-BUILDERS = dict(tee=tee, lpf=lpf, bandpass=bandpass, via=via, gcpw=gcpw, line=line, shunt_via=shunt_via)
+def lumped_line(api, value="R 20 + L 0.5n"):
+    """Two line sections joined by a lumped component across a 1 mm bridge
+    (Layout.add_lumped) with a delta gap in its middle."""
+    W = 1.137 * mm
+    lay = api.Layout()
+    lay.add_rect(0, -W / 2, 3 * mm, W / 2)
+    lay.add_rect(4 * mm, -W / 2, 7 * mm, W / 2)
+    lay.add_lumped("Z1", (3 * mm, 0.0), (4 * mm, 0.0), 0.6 * mm, value=value)
+    lay.add_port("P1", (0, 0), "-x", W, 8 * mm)
+    lay.add_port("P2", (7 * mm, 0), "+x", W, 8 * mm)
+    sub = api.Substrate(eps_r=ER, h=H, tand=TAND, sigma=SIGMA)
+    return lay, sub, dict(max_cell=0.5 * mm, edge_cell=0.15 * mm), np.array([2.0, 5.0, 9.0]) * GHz
+
+
+BUILDERS = dict(tee=tee, lpf=lpf, bandpass=bandpass, via=via, gcpw=gcpw, line=line, shunt_via=shunt_via,
+                lumped_line=lumped_line)
 
 
 def build(api, name, **kw):

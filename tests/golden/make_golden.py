@@ -147,6 +147,28 @@ def write_block(path, freqs):
                      f"{s11 * 1.1:.6f} {ph / 2:.4f}\n")
 
 
+def lumped_case():
+    """A lumped component across a gap (Layout.add_lumped, Solver._load_lumped):
+    gap vectors, loads, loaded currents and gap currents at the first
+    frequency, the sweep, and a sweep with the value overridden."""
+    lay, stack, mkw, freqs = workloads.BUILDERS["lumped_line"](ref)
+    m = lay.mesh(**mkw)
+    sol = ref.Solver(m, stack, verbose=False, method="dense")
+    f0 = freqs[0]
+    g = sol.greens(f0)
+    x = sol.solve_currents(f0, greens=g)
+    out = dict(N=m.n_unknowns, mesh_sha=mesh_digest(m), freqs=freqs, Lm=sol.Lm, D0=sol.lumped_impedance(f0),
+               x=x, I_gap=sol.lumped_currents(x))
+    r = sol.sweep(freqs, interp=None)
+    out.update(result_arrays(r))
+    r2 = sol.sweep(freqs, interp=None, values={"Z1": "C 1p"})
+    out.update(result_arrays(r2, "C1p_"))
+    r3 = sol.sweep(freqs, interp=None, values={"Z1": None})
+    out.update(result_arrays(r3, "open_"))
+    np.savez_compressed(os.path.join(HERE, "lumped_line.npz"), **out)
+    print(f"lumped_line: N={m.n_unknowns}", flush=True)
+
+
 def network_case():
     """SweepResult waves, matched / wave currents and connect (Engine/mom25d/
     solver.py:673-765, network.py) on the line case with a synthetic block."""
@@ -198,10 +220,14 @@ def main():
     ap.add_argument("--quick", action="store_true", help="small cases only")
     ap.add_argument("--interp", action="store_true", help="only the FreqInterp fixtures")
     ap.add_argument("--network", action="store_true", help="only the network / waves fixture")
+    ap.add_argument("--lumped", action="store_true", help="only the lumped-component fixture")
     args = ap.parse_args()
     os.environ.setdefault("OPENBLAS_NUM_THREADS", "4")
     if args.network:
         network_case()
+        return
+    if args.lumped:
+        lumped_case()
         return
     if args.interp:
         interp_case("tee", zrows=np.arange(0, 1085, 97))

@@ -1,0 +1,73 @@
+"""CPU tests of lumped components (Layout.add_lumped, mom25d_gb300/lumped.py,
+Solver.lumped_impedance / _load_lumped) against mom25d's own run of the
+lumped_line workload (tests/golden/lumped_line.npz; make_golden.py
+--lumped): the mesh and gap vectors, the loads, and the loaded currents from
+the oracle's fill."""
+
+import hashlib
+from types import SimpleNamespace
+
+import numpy as np
+
+import mom25d_gb300 as G
+from mom25d_gb300 import lumped as LP
+from mom25d_gb300 import workloads
+from mom25d_gb300.solver import Solver
+from oracle import sweep as O
+
+from conftest import golden
+
+
+def digest(m):
+    h = hashlib.sha256()
+    for a in (m.nodes, m.tris, m.tri_basis, m.tri_sign, m.edge_len, m.tri_layer):
+        h.update(np.ascontiguousarray(a).tobytes())
+    for s in m.via_segments:
+        h.update(repr((s["via"], s["top"], s["bottom"])).encode())
+        for k in ("top_tris", "bottom_tris"):
+            if s[k] is not None:
+                h.update(np.asarray(s[k], np.int64).tobytes())
+    return h.hexdigest()
+
+
+def host_solver(m):
+    """What Solver.lumped_impedance and _load_lumped read, without a device."""
+    return SimpleNamespace(lumped=list(m.layout.lumped), values={}, OPEN=Solver.OPEN, Lm=m.lumped_vectors())
+
+
+def test_mesh_and_gap_vectors_match_reference():
+    g = golden("lumped_line")
+    lay, st, m, _ = workloads.build(G, "lumped_line")
+    assert digest(m) == str(g["mesh_sha"])
+    np.testing.assert_array_equal(m.lumped_vectors(), g["Lm"])
+
+
+def test_values_and_loads():
+    f = 3.3e9
+    assert LP.parse("R 20 + L 0.5n").z(f) == 20 + 2j * np.pi * f * 0.5e-9
+    assert abs(LP.parse("C 1p || R 1k").z(f) - 1 / (2j * np.pi * f * 1e-12 + 1e-3)) < 1e-9
+    assert LP.as_value(50).z(f) == 50
+    g = golden("lumped_line")
+    lay, st, m, _ = workloads.build(G, "lumped_line")
+    sol = host_solver(m)
+    np.testing.assert_allclose(Solver.lumped_impedance(sol, float(g["freqs"][0])), g["D0"], rtol=1e-15)
+    sol.values["Z1"] = None
+    assert Solver.lumped_impedance(sol, 1e9)[0, 0] == Solver.OPEN
+
+
+def test_loaded_currents_from_oracle_fill():
+    """The oracle's fill, one solve for the port and gap excitations and the
+    Woodbury loading give mom25d's loaded currents and gap current."""
+    g = golden("lumped_line")
+    lay, st, m, _ = workloads.build(G, "lumped_line")
+    sw = O.Sweep(m, st)
+    f0 = float(g["freqs"][0])
+    Z = sw.impedance(f0)
+    sol = host_solver(m)
+    sol.lumped_impedance = lambda f: Solver.lumped_impedance(sol, f)
+    E0 = sw.excitations()
+    X = O.dense_solve(Z.copy(), np.hstack([E0, sol.Lm]))
+    P = E0.shape[1]
+    x = Solver._load_lumped(sol, X[:, :P], X[:, P:], f0)
+    assert np.abs(x - g["x"]).max() <= 1e-8 * np.abs(g["x"]).max()
+    np.testing.assert_allclose(sol.Lm.T @ x, g["I_gap"], rtol=1e-8)
