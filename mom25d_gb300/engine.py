@@ -121,6 +121,11 @@ def load():
     return lib
 
 
+class NumericError(RuntimeError):
+    """M25_ERR_NUMERIC: a zero pivot, or a refinement that stopped above its
+    target (a RuntimeError, as mom25d raises for a failed iterative solve)."""
+
+
 def check(rc):
     if rc == M25_OK:
         return
@@ -129,6 +134,8 @@ def check(rc):
         raise ValueError(msg)
     if rc == M25_ERR_MEMORY:
         raise MemoryError(msg)
+    if rc == M25_ERR_NUMERIC:
+        raise NumericError(msg)
     raise RuntimeError(msg)
 
 

@@ -527,9 +527,10 @@ class Solver:
         steps = 0
         try:
             X = dense_solve(Z, B, precision=prec, ctx=self.ctx, tol=self.refine_tol, max_iter=self.max_refine)
-        except RuntimeError:
+        except E.NumericError:
             if prec == "fp64":
                 raise
+            # the mixed refinement stopped above its target: this point in fp64
             X = dense_solve(Z, B, precision="fp64", ctx=self.ctx)
             steps = -1
         x = np.ascontiguousarray(self._load_lumped(X[:, :P], X[:, P:], f))
