@@ -160,6 +160,7 @@ class Layout:
     vias: list = field(default_factory=list)
     planes: list = field(default_factory=list)
     lumped: list = field(default_factory=list)
+    components: list = field(default_factory=list)  # (model, [gap names]): multi-port blocks across lumped gaps
     internal_ports: list = field(default_factory=list)
 
     def add_rect(self, x0, y0, x1, y1, layer="top"):
@@ -201,6 +202,23 @@ class Layout:
         self.lumped.append(g)
         self.add_rect(*g.rect(), layer=layer)
         return g
+
+    def add_component(self, model, gaps):
+        """Multi-port component (network.Touchstone or a .sNp path) across the
+        named lumped gaps, in the model's port order; the gaps are added with
+        value=None (mom25d/mesh.py:432-447)."""
+        from .network import Touchstone
+
+        if isinstance(model, str):
+            model = Touchstone(model)
+        names = [q.name for q in self.lumped]
+        for n in gaps:
+            if n not in names:
+                raise ValueError(f"no lumped gap {n!r}")
+        if getattr(model, "n", len(gaps)) != len(gaps):
+            raise ValueError(f"{model} has {model.n} ports, {len(gaps)} gaps given")
+        self.components.append((model, list(gaps)))
+        return self
 
     def add_via(self, x, y, drill=0.3e-3, pad=None, name=None, top="top", bottom="gnd"):
         v = Via((x, y), drill, pad, name, top, bottom)

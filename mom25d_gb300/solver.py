@@ -328,10 +328,12 @@ class Solver:
         self.ports = mesh.layout.ports
         if not self.ports:
             raise ValueError("layout has no ports")
-        if getattr(mesh.layout, "components", None) or getattr(mesh.layout, "internal_ports", None):
-            raise ValueError("multi-port components and internal ports are not part of this engine")
-        # lumped components across delta gaps: loaded after the solve (Woodbury)
+        if getattr(mesh.layout, "internal_ports", None):
+            raise ValueError("internal ports are not part of this engine")
+        # lumped components across delta gaps (one-port values and multi-port
+        # blocks): loaded after the solve (Woodbury)
         self.lumped = list(getattr(mesh.layout, "lumped", []))
+        self.components = list(getattr(mesh.layout, "components", []))
         self.Lm = mesh.lumped_vectors() if self.lumped else None
         self.values = {}  # per-sweep overrides of lumped values
         self.method = "dense"
@@ -490,14 +492,23 @@ class Solver:
     OPEN = 1e12  # ohm: an unloaded lumped gap
 
     def lumped_impedance(self, freq):
-        """D (n_lumped, n_lumped): the impedance of the component across each
-        lumped gap at freq, OPEN where none (Engine/mom25d/solver.py:1039-1062
-        without multi-port components and internal ports)."""
+        """D (n_lumped, n_lumped): the impedance of the components across the
+        lumped gaps at freq: a multi-port block's impedance matrix across its
+        gaps, a one-port value on the diagonal, OPEN where none
+        (Engine/mom25d/solver.py:1039-1062 without internal ports)."""
         from .lumped import as_value, parse
 
         D = np.zeros((len(self.lumped), len(self.lumped)), complex)
+        names = [q.name for q in self.lumped]
+        used = set()
+        for model, gaps in getattr(self, "components", []):
+            ix = [names.index(n) for n in gaps]
+            D[np.ix_(ix, ix)] = model.z(freq)
+            used.update(ix)
         for k, q in enumerate(self.lumped):
             v = self.values.get(q.name, getattr(q, "value", None))
+            if k in used and v is None:
+                continue
             if isinstance(v, str):
                 v = parse(v)
             D[k, k] = self.OPEN if v is None else as_value(v).z(freq)

@@ -14,6 +14,7 @@ returns (layout, stack, mesh keyword arguments, frequencies [Hz]).
   line       short through line (small N, test case)
   shunt_via  short line with a via to ground (small N, test case)
   lumped_line  two line sections joined by a lumped component (R 20 + L 0.5n) across a gap
+  component_line  three line sections, a 2-port S-parameter block across two open gaps
 """
 
 import numpy as np
@@ -138,8 +139,26 @@ def lumped_line(api, value="R 20 + L 0.5n"):
     return lay, sub, dict(max_cell=0.5 * mm, edge_cell=0.15 * mm), np.array([2.0, 5.0, 9.0]) * GHz
 
 
+def component_line(api, block=None):
+    """Three line sections joined by two open lumped gaps with a 2-port
+    S-parameter block (Layout.add_component, a Touchstone file) across them."""
+    W = 1.137 * mm
+    lay = api.Layout()
+    lay.add_rect(0, -W / 2, 3 * mm, W / 2)
+    lay.add_rect(4 * mm, -W / 2, 6 * mm, W / 2)
+    lay.add_rect(7 * mm, -W / 2, 10 * mm, W / 2)
+    lay.add_lumped("G1", (3 * mm, 0.0), (4 * mm, 0.0), 0.6 * mm)
+    lay.add_lumped("G2", (6 * mm, 0.0), (7 * mm, 0.0), 0.6 * mm)
+    if block is not None:
+        lay.add_component(block, ["G1", "G2"])
+    lay.add_port("P1", (0, 0), "-x", W, 8 * mm)
+    lay.add_port("P2", (10 * mm, 0), "+x", W, 8 * mm)
+    sub = api.Substrate(eps_r=ER, h=H, tand=TAND, sigma=SIGMA)
+    return lay, sub, dict(max_cell=0.5 * mm, edge_cell=0.15 * mm), np.array([2.0, 5.0, 9.0]) * GHz
+
+
 BUILDERS = dict(tee=tee, lpf=lpf, bandpass=bandpass, via=via, gcpw=gcpw, line=line, shunt_via=shunt_via,
-                lumped_line=lumped_line)
+                lumped_line=lumped_line, component_line=component_line)
 
 
 def build(api, name, **kw):

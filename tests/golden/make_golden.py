@@ -167,6 +167,15 @@ def lumped_case():
     out.update(result_arrays(r3, "open_"))
     np.savez_compressed(os.path.join(HERE, "lumped_line.npz"), **out)
     print(f"lumped_line: N={m.n_unknowns}", flush=True)
+    # a 2-port block (block.s2p, written by network_case) across two open gaps
+    lay, stack, mkw, freqs = workloads.BUILDERS["component_line"](ref, block=os.path.join(HERE, "block.s2p"))
+    m = lay.mesh(**mkw)
+    sol = ref.Solver(m, stack, verbose=False, method="dense")
+    out = dict(N=m.n_unknowns, mesh_sha=mesh_digest(m), freqs=freqs, Lm=sol.Lm, D0=sol.lumped_impedance(freqs[0]))
+    r = sol.sweep(freqs, interp=None)
+    out.update(result_arrays(r))
+    np.savez_compressed(os.path.join(HERE, "component_line.npz"), **out)
+    print(f"component_line: N={m.n_unknowns}", flush=True)
 
 
 def network_case():

@@ -71,3 +71,19 @@ def test_loaded_currents_from_oracle_fill():
     x = Solver._load_lumped(sol, X[:, :P], X[:, P:], f0)
     assert np.abs(x - g["x"]).max() <= 1e-8 * np.abs(g["x"]).max()
     np.testing.assert_allclose(sol.Lm.T @ x, g["I_gap"], rtol=1e-8)
+
+
+def test_component_mesh_and_loads_match_reference():
+    """A 2-port S-parameter block across two open gaps (Layout.add_component):
+    the mesh, the gap vectors and the block's impedance matrix in D."""
+    import os
+
+    from conftest import GOLDEN
+
+    g = golden("component_line")
+    lay, st, m, _ = workloads.build(G, "component_line", block=os.path.join(GOLDEN, "block.s2p"))
+    assert digest(m) == str(g["mesh_sha"])
+    np.testing.assert_array_equal(m.lumped_vectors(), g["Lm"])
+    sol = host_solver(m)
+    sol.components = list(m.layout.components)
+    np.testing.assert_allclose(Solver.lumped_impedance(sol, float(g["freqs"][0])), g["D0"], rtol=1e-13)

@@ -28,3 +28,16 @@ def test_lumped_sweeps_match_reference(gpu, precision, tol):
     r3 = sol.sweep(g["freqs"], values={"Z1": None})
     assert np.abs(r3.S - g["open_S"]).max() < tol
     sol.close()
+
+
+def test_component_sweep_matches_reference(gpu):
+    import os
+
+    from conftest import GOLDEN
+
+    g = golden("component_line")
+    lay, st, m, _ = workloads.build(G, "component_line", block=os.path.join(GOLDEN, "block.s2p"))
+    sol = Solver(m, st, verbose=False)
+    r = sol.sweep(g["freqs"])
+    assert np.abs(r.S - g["S"]).max() < 1e-6
+    sol.close()
