@@ -64,3 +64,29 @@ def test_wave_currents_of_matched_drive_are_matched_currents():
     r, gn = reference_result(currents=[g["x"]] + [None] * (len(golden("line_network")["freqs"]) - 1))
     np.testing.assert_allclose(r.matched_currents(0, 0), gn["matched0"], rtol=0, atol=1e-12 * np.abs(gn["matched0"]).max())
     np.testing.assert_allclose(r.wave_currents(0, [1.0, 0.5j]), gn["wave0"], rtol=0, atol=1e-12 * np.abs(gn["wave0"]).max())
+
+
+def test_touchstone_formats_units_and_port_order(tmp_path):
+    """DB and RI formats, MHz and Hz axes, comments, a 3-port file (rows in
+    row order; only 2-ports use the column order S11 S21 S12 S22), the
+    interpolation between points and the range check."""
+    p = tmp_path / "a.s2p"
+    p.write_text("! comment\n# MHZ S DB R 75\n100 -6 90 -20 0 -30 0 -1 -90 ! tail\n"
+                 "300 -6 90 -20 0 -30 0 -1 -90\n")
+    t = N.Touchstone(str(p))
+    assert t.z0 == 75.0 and t.n == 2
+    np.testing.assert_allclose(t.f, [1e8, 3e8])
+    s = t.s(2e8)
+    assert abs(s[0, 0] - 10 ** (-6 / 20) * 1j) < 1e-12
+    assert abs(s[1, 0] - 10 ** (-20 / 20)) < 1e-12  # second pair of a 2-port line is S21
+    assert abs(s[0, 1] - 10 ** (-30 / 20)) < 1e-12
+    q = tmp_path / "b.s3p"
+    vals = " ".join(f"{k} {-k}" for k in range(1, 10))
+    q.write_text(f"# HZ S RI\n1e9 {vals}\n2e9 {vals}\n")
+    t3 = N.Touchstone(str(q))
+    s3 = t3.s(1.5e9)
+    assert s3[0, 1] == 2 - 2j and s3[1, 0] == 4 - 4j and s3[2, 2] == 9 - 9j
+    import pytest
+
+    with pytest.raises(ValueError):
+        t3.s(3e9)
