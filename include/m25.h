@@ -24,6 +24,10 @@
  *   m25_deembed          Solver.sweep de-embedding   Engine/mom25d/solver.py:1276-1325
  *                        (charges 1076-1091, line_voltage 1101-1125, PortModel 604-610,
  *                         fit_waves 618-670, _reciprocal_z0 1357-1427)
+ *   m25_sweep_point      one iteration of Solver.sweep Engine/mom25d/solver.py:1273-1325
+ *   m25_deembed_waves    SweepResult.waves           Engine/mom25d/solver.py:683, 1309
+ *   m25_interp_*         FreqInterp                  Engine/mom25d/freqinterp.py:27-197
+ *                        (and solve_currents' interpolated branch, solver.py:1012-1013)
  *   m25_mlp_*            (no counterpart: mom25d has no learned part) the
  *                        network of the learned Green's remainder, which
  *                        stands in for the Sommerfeld integrals of
