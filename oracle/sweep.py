@@ -409,6 +409,12 @@ class Sweep:
     def __init__(self, mesh, stack):
         if not hasattr(stack, "layers"):
             stack = stack.to_stackup()
+        # the levels ordered by height, as Solver.__init__ does before its
+        # geometry (mom25d/solver.py:844-846): the via segments' top / bottom
+        # pads and the level indices follow this order
+        order = sorted(list(mesh.layer_names) + list(getattr(mesh, "planes", [])), key=stack.level_z)
+        if getattr(mesh, "level_order", None) != order:
+            mesh.assign_levels(order)
         self.mesh, self.stack = mesh, stack
         self.single, self.zl = stack_info(stack, mesh)
         v = mesh.nodes

@@ -107,6 +107,25 @@ def test_via_inductance_known_answer():
     np.testing.assert_allclose(L, g["via_L"], rtol=1e-13)
 
 
+@pytest.mark.parametrize("name", ["tee", "bandpass_0", "via"])
+def test_oracle_fill_matches_reference_rows(name):
+    """The oracle's fill against mom25d's Z rows and diagonal on the larger
+    cases: a tee, a band-pass variant and the two-level via transition (its
+    via row, whose entries are small against the RWG self terms, on its own
+    scale: the levels must be ordered by height as Solver does)."""
+    g = golden(name)
+    base = name.split("_")[0]
+    lay, st, m, _ = workloads.build(G, base, **({"k": 0} if base == "bandpass" else {}))
+    sw = O.Sweep(m, st)
+    Z = sw.impedance(float(g["f0"]))
+    rows = g["Z_rows_idx"]
+    assert np.abs(Z[rows] - g["Z_rows"]).max() <= 1e-13 * np.abs(g["Z_rows"]).max()
+    assert np.abs(np.diag(Z) - g["Z_diag"]).max() <= 1e-13 * np.abs(g["Z_diag"]).max()
+    for k, r in enumerate(rows):
+        if r >= m.n_basis:  # via unknowns
+            assert np.abs(Z[r] - g["Z_rows"][k]).max() <= 1e-13 * np.abs(g["Z_rows"][k]).max()
+
+
 @pytest.mark.parametrize("name", ["line", "shunt_via"])
 def test_oracle_fill_and_sweep_match_reference(name):
     g = golden(name)
