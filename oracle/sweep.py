@@ -492,6 +492,59 @@ class Sweep:
         return tuple(np.array([o[k] for o in out]) for k in range(5))
 
 
+OPEN = 1e12  # ohm: an unloaded lumped gap
+
+
+def lumped_value(v, f):
+    """Z [ohm] of a lumped value at f (mom25d/lumped.py:17-90): an object with
+    z(f), a callable, a number, or a string such as 'R 10 + L 0.5n' or
+    'C 1p || R 1k'."""
+    if isinstance(v, str):
+        t = v.strip()
+        if "||" in t:
+            return 1 / sum(1 / lumped_value(p, f) for p in t.split("||"))
+        if "+" in t:
+            return sum(lumped_value(p, f) for p in t.split("+"))
+        kind, num = t.split()
+        mult = dict(f=1e-15, p=1e-12, n=1e-9, u=1e-6, m=1e-3, k=1e3, M=1e6, G=1e9)
+        x = float(num[:-1]) * mult[num[-1]] if num[-1] in mult else float(num)
+        w = 2 * np.pi * f
+        return {"R": complex(x), "L": 1j * w * x, "C": 1 / (1j * w * x)}[kind.upper()]
+    if hasattr(v, "z"):
+        return complex(v.z(f))
+    if callable(v):
+        return complex(v(f))
+    return complex(v)
+
+
+def lumped_loads(mesh, f, values=None):
+    """D (n_lumped, n_lumped): components across the lumped gaps at f, a
+    multi-port block's impedance matrix across its gaps, OPEN where none
+    (mom25d/solver.py:1039-1062 without internal ports)."""
+    gaps = list(getattr(mesh.layout, "lumped", []))
+    names = [q.name for q in gaps]
+    D = np.zeros((len(gaps), len(gaps)), complex)
+    used = set()
+    for model, gn in getattr(mesh.layout, "components", []):
+        ix = [names.index(n) for n in gn]
+        D[np.ix_(ix, ix)] = model.z(f)
+        used.update(ix)
+    for k, q in enumerate(gaps):
+        v = (values or {}).get(q.name, getattr(q, "value", None))
+        if k in used and v is None:
+            continue
+        D[k, k] = OPEN if v is None else lumped_value(v, f)
+    return D
+
+
+def load_lumped(Lm, D, Xe, Xi):
+    """(Z + L D L^T)^-1 e = Xe - Xi D (I + L^T Xi D)^-1 L^T Xe (Woodbury),
+    Xi = Z^-1 L (mom25d/solver.py:1064-1070)."""
+    M = Lm.T @ Xi
+    y = Lm.T @ Xe
+    return Xe - Xi @ (D @ np.linalg.solve(np.eye(len(D)) + M @ D, y))
+
+
 def renormalize(S, z0, zref=50.0):
     out = np.empty_like(S)
     eye = np.eye(S.shape[1])

@@ -87,3 +87,34 @@ def test_component_mesh_and_loads_match_reference():
     sol = host_solver(m)
     sol.components = list(m.layout.components)
     np.testing.assert_allclose(Solver.lumped_impedance(sol, float(g["freqs"][0])), g["D0"], rtol=1e-13)
+
+
+def test_oracle_lumped_sweeps_match_reference():
+    """The oracle's sweep with the loads (its fill, one solve for the port and
+    gap excitations, Woodbury, de-embedding) against mom25d's S for the
+    series R + L, a 1 pF override and an open gap, and a 2-port block across
+    two gaps."""
+    import os
+
+    from conftest import GOLDEN
+
+    cases = [("lumped_line", {}, [("S", None), ("C1p_S", {"Z1": "C 1p"}), ("open_S", {"Z1": None})]),
+             ("component_line", {"block": os.path.join(GOLDEN, "block.s2p")}, [("S", None)])]
+    for name, kw, variants in cases:
+        g = golden(name)
+        lay, st, m, _ = workloads.build(G, name, **kw)
+        sw = O.Sweep(m, st)
+        Lm = m.lumped_vectors()
+        E0 = sw.excitations()
+        P = E0.shape[1]
+        got = {key: [] for key, _ in variants}
+        for f in g["freqs"]:
+            kern = sw.kernels(f)
+            Z = sw.impedance(f, kern)
+            X = O.dense_solve(Z.copy(), np.hstack([E0, Lm]))
+            for key, values in variants:
+                x = O.load_lumped(Lm, O.lumped_loads(m, f, values), X[:, :P], X[:, P:])
+                q = O.charges(m, x, kern.omega)
+                got[key].append(sw.deembed(f, kern, x, q)[0])
+        for key, _ in variants:
+            assert np.abs(np.array(got[key]) - g[key]).max() < 1e-6, (name, key)
