@@ -65,3 +65,25 @@ def test_oracle_interpolated_z_matches_reference():
     rows = g["Z_rows_idx"]
     ref = g["Zi_rows"]
     assert np.abs(Z[rows] - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_oracle_interpolated_sweep_matches_reference():
+    """The oracle's fill at every anchor, the transform, the Lagrange
+    combination at each frequency, solve and de-embedding: mom25d's
+    interpolated S on the shunt via (25 frequencies, 5 anchors)."""
+    g = golden("shunt_via_interp")
+    lay, st, m, _ = workloads.build(G, "shunt_via")
+    sw = O.Sweep(m, st)
+    anchors, order, nb = g["anchors"], int(g["order"]), int(g["nb"])
+    kr = float(g["k_ratio"])
+    ke = lambda f: kr * 2 * np.pi * f / 299792458.0  # noqa: E731
+    W = [OI.store(sw.impedance(float(fa)), g["pos"], nb, float(fa), ke(float(fa))) for fa in anchors]
+    S = []
+    for f in g["freqs"]:
+        idx = OI.window(anchors, order, f)
+        Z = OI.evaluate([W[i] for i in idx], OI.weights(anchors, f, idx), g["pos"], nb, f, ke(f))
+        kern = sw.kernels(f)
+        x = O.dense_solve(Z, sw.excitations())
+        q = O.charges(m, x, kern.omega)
+        S.append(sw.deembed(f, kern, x, q)[0])
+    assert np.abs(np.array(S) - g["S"]).max() < 1e-6
