@@ -48,6 +48,8 @@ class FreqInterp:
     """
 
     def __init__(self, step=None, order=3, k_ratio=None, check=False, block=1024, dtype=None, resident=None):
+        if not 1 <= int(order) <= 7:
+            raise ValueError("FreqInterp: order 1..7 (the device interpolation combines up to 8 anchors)")
         self.step, self.order, self.k_ratio, self.check, self.block = step, order, k_ratio, check, block
         self.dtype = dtype
         self.resident = resident

@@ -87,3 +87,9 @@ def test_oracle_interpolated_sweep_matches_reference():
         q = O.charges(m, x, kern.omega)
         S.append(sw.deembed(f, kern, x, q)[0])
     assert np.abs(np.array(S) - g["S"]).max() < 1e-6
+
+
+def test_order_limit():
+    with pytest.raises(ValueError):
+        FreqInterp(order=8)
+    assert FreqInterp(order=7).order == 7
