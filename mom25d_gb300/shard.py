@@ -59,13 +59,15 @@ def sharded_map(items, costs, fn, rank=0, world=1, group=None):
     return out
 
 
-def sweep_sharded(solver, freqs, rank=0, world=1, group=None):
+def sweep_sharded(solver, freqs, rank=0, world=1, group=None, values=None):
     """Solver.sweep over ranks: rank r runs its share of freqs on its own GPU
     (the solver of each rank holds the same mesh and stack), rank 0 returns
-    the SweepResult of all frequencies in order, the other ranks None."""
-    from .solver import SweepResult
-
+    the SweepResult of all frequencies in order, the other ranks None.
+    values: {lumped name: value} overrides, set on every rank's solver before
+    its points run, as Solver.sweep(values=...) does."""
     freqs = np.asarray(freqs, float)
+    solver.values.clear()
+    solver.values.update(values or {})
     cost = point_cost(solver.mesh.n_unknowns)
 
     def one(f):
@@ -75,8 +77,17 @@ def sweep_sharded(solver, freqs, rank=0, world=1, group=None):
     rows = sharded_map(list(freqs), [cost] * len(freqs), one, rank, world, group)
     if rows is None:
         return None
-    return SweepResult(freqs=freqs, S=np.array([r[0] for r in rows]), z0=np.array([r[1] for r in rows]),
-                       gamma=np.array([r[2] for r in rows]), z0_line=np.array([r[3] for r in rows]),
-                       fit_residual=np.array([r[4] for r in rows]), port_names=[p.name for p in solver.ports],
+    return assemble_result(freqs, rows, [p.name for p in solver.ports], world)
+
+
+def assemble_result(freqs, rows, port_names, world=1):
+    """The SweepResult of a sharded sweep from its rows in frequency order:
+    per frequency (S, z0, gamma, z0_line, residual, info)."""
+    from .solver import SweepResult
+
+    return SweepResult(freqs=np.asarray(freqs, float), S=np.array([r[0] for r in rows]),
+                       z0=np.array([r[1] for r in rows]), gamma=np.array([r[2] for r in rows]),
+                       z0_line=np.array([r[3] for r in rows]), fit_residual=np.array([r[4] for r in rows]),
+                       port_names=list(port_names),
                        waves=np.array([r[5]["waves"] for r in rows]) if rows and "waves" in rows[0][5] else None,
                        info=dict(refine_steps=[r[5]["refine_steps"] for r in rows], ranks=world))

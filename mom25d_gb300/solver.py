@@ -14,6 +14,7 @@ import ctypes as C
 import os
 import threading
 import time
+import zlib
 from dataclasses import dataclass
 
 import numpy as np
@@ -623,9 +624,7 @@ class Solver:
         return q, phi, I, V
 
     def _checkpoint_key(self, freqs):
-        m = self.mesh
-        return np.array([len(freqs), float(np.sum(freqs)), float(m.n_unknowns), float(np.sum(m.nodes)),
-                         float(np.sum(m.nodes ** 2)), float(len(m.tris)), 0.0])
+        return checkpoint_key(self.mesh, freqs, values_digest(self.values, self.lumped, self.components))
 
     _DEVICE_STATE = ("ctx", "_geom", "_geom_owner", "_ports", "_siblings", "_sib_lock")
 
@@ -822,6 +821,31 @@ class Solver:
             self._geom.close()
         self._ports = self._geom = None
         self.ctx.close()
+
+
+def values_digest(values, lumped=(), components=()):
+    """A digest of what the lumped loads of a sweep are: the per-sweep value
+    overrides, the layout's own values and the multi-port blocks (their file
+    name, gaps and S data). CRC-32, so that it is the same in every process
+    (Python's hash of a string is salted per process)."""
+    crc = zlib.crc32(repr(sorted((str(k), repr(v)) for k, v in (values or {}).items())).encode())
+    crc = zlib.crc32(repr([(q.name, repr(getattr(q, "value", None))) for q in lumped]).encode(), crc)
+    for model, gaps in components:
+        crc = zlib.crc32(repr((repr(model), tuple(gaps))).encode(), crc)
+        data = getattr(model, "s_data", None)
+        if data is not None:
+            crc = zlib.crc32(np.ascontiguousarray(data).tobytes(), crc)
+    return float(crc)
+
+
+def checkpoint_key(mesh, freqs, digest=0.0):
+    """The key a sweep checkpoint is resumed under (Engine/mom25d/solver.py:
+    1183-1187): the frequencies, the mesh's size and node sums, and the
+    digest of the lumped loads (values_digest). A checkpoint whose key
+    differs is not resumed."""
+    m = mesh
+    return np.array([len(freqs), float(np.sum(freqs)), float(m.n_unknowns), float(np.sum(m.nodes)),
+                     float(np.sum(m.nodes ** 2)), float(len(m.tris)), float(digest)])
 
 
 def assemble(solver, freq, precision="fp64"):

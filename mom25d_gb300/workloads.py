@@ -8,7 +8,8 @@ returns (layout, stack, mesh keyword arguments, frequencies [Hz]).
   tee        open-stub tee, eps_r 3.55 / 0.508 mm, mesh 0.5/0.08 mm, 37 f 1-10 GHz (N = 1085)
   lpf        7-section stepped-impedance low-pass 4.0/0.3 mm (seeded lengths), 101 f 0.5-8 GHz;
              mesh 0.35/0.05 mm gives N = 5943, the N ~ 6k headline case
-  bandpass   seeded edge-coupled-line band-pass variants, 128 f 1-12 GHz
+  bandpass   16 seeded edge-coupled-line band-pass variants, 128 f 1-12 GHz, each meshed with its own
+             max_cell (BANDPASS_CELL) so that N spreads over 1.5k-5k (BANDPASS_N)
   via        two-layer microstrip -> via -> inner line, 2 x 0.254 mm eps_r 3.66 (N = 3789)
   gcpw       30 mm grounded CPW with via fences on 0.508 mm eps_r 3.55, 64 f 1-20 GHz
   line       short through line (small N, test case)
@@ -50,10 +51,17 @@ def lpf(api, max_cell=0.35 * mm, edge_cell=0.05 * mm, seed=0):
     return lay, sub, dict(max_cell=max_cell, edge_cell=edge_cell), np.linspace(0.5, 8, 101) * GHz
 
 
+# max_cell [mm] of band-pass variant k, picked (0.01 mm steps) so that N comes
+# near 1500 + 3500 k / 15: uneven sizes between 1.5k and 5k unknowns
+BANDPASS_CELL = (0.45, 0.47, 0.44, 0.38, 0.46, 0.40, 0.38, 0.38, 0.32, 0.26, 0.28, 0.28, 0.26, 0.25, 0.22, 0.24)
+BANDPASS_N = (1524, 1800, 1784, 2164, 2434, 2467, 2882, 3064, 3572, 3614, 3722, 3982, 4252, 4452, 4972, 4652)
+
+
 def bandpass(api, k=0, max_cell=None, edge_cell=0.05 * mm):
     """Edge-coupled half-wave band-pass variant k: gap U(0.1, 0.4) mm,
     width U(0.8, 1.4) mm, 3-5 coupled sections, each a pair of
-    quarter-wave-long rectangles offset along x."""
+    quarter-wave-long rectangles offset along x; meshed with
+    BANDPASS_CELL[k] unless max_cell is given."""
     rng = np.random.default_rng(k)
     gap = rng.uniform(0.1, 0.4) * mm
     W = rng.uniform(0.8, 1.4) * mm
@@ -69,7 +77,7 @@ def bandpass(api, k=0, max_cell=None, edge_cell=0.05 * mm):
     lay.add_port("P1", (0.0, 0.0), "-x", W, 8 * mm)
     lay.add_port("P2", (x + L, y - W - gap), "+x", W, 8 * mm)
     sub = api.Substrate(eps_r=ER, h=H, tand=TAND, sigma=SIGMA)
-    mc = max_cell if max_cell is not None else 0.45 * mm
+    mc = max_cell if max_cell is not None else BANDPASS_CELL[k] * mm
     return lay, sub, dict(max_cell=mc, edge_cell=edge_cell), np.linspace(1, 12, 128) * GHz
 
 

@@ -1,10 +1,11 @@
 """Generate the golden fixtures of this directory by running mom25d itself.
 
-Run in a container where the mom25d sources are importable (they are read
-from /root/reference/Engine); the fixtures are committed so that tests on
+Run where the mom25d sources are importable: pass the directory that holds
+mom25d's `mom25d` package (its `Engine` directory) with --ref or in the
+environment variable MOM25D_SRC. The fixtures are committed so that tests on
 machines without mom25d compare against them:
 
-    python tests/golden/make_golden.py [--quick]
+    MOM25D_SRC=<mom25d checkout>/Engine python tests/golden/make_golden.py [--quick]
 
 Every case uses the sweep settings the parity tests assume: method="dense"
 (dense LU) and interp=None (an exact fill at every frequency), except the
@@ -21,13 +22,24 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "..", ".."))
-sys.path.insert(0, "/root/reference/Engine")
-
-import mom25d as ref  # noqa: E402
-from mom25d import solver as ref_solver  # noqa: E402
-from mom25d.integrals import potential_integrals  # noqa: E402
 
 from mom25d_gb300 import workloads  # noqa: E402
+
+ref = ref_solver = potential_integrals = None
+
+
+def import_reference(src):
+    """Import mom25d from the directory `src` (the one holding its package)."""
+    global ref, ref_solver, potential_integrals
+    if not src or not os.path.isdir(os.path.join(src, "mom25d")):
+        raise SystemExit("give mom25d's source directory (the one holding the mom25d package) "
+                         "with --ref or MOM25D_SRC")
+    sys.path.insert(0, src)
+    import mom25d
+    from mom25d import solver
+    from mom25d.integrals import potential_integrals as pint
+
+    ref, ref_solver, potential_integrals = mom25d, solver, pint
 
 
 def mesh_digest(m):
@@ -42,6 +54,30 @@ def mesh_digest(m):
     return h.hexdigest()
 
 
+def cache_points(sol):
+    """Wrap a mom25d Solver's greens / solve_currents so that a frequency's
+    tables and currents are computed once: the sweep then reuses the point
+    computed step by step for the stage fixtures (and the floor runs redo
+    only the de-embedding)."""
+    cache = {}
+    greens, solve = sol.greens, sol.solve_currents
+
+    def cached_greens(f):
+        if ("g", f) not in cache:
+            cache[("g", f)] = greens(f)
+        return cache[("g", f)]
+
+    def cached_solve(f, excitations=None, greens=None, Z=None, interp=None):
+        if excitations is not None or interp is not None:
+            return solve(f, excitations=excitations, greens=greens, Z=Z, interp=interp)
+        if ("x", f) not in cache:
+            cache[("x", f)] = solve(f, greens=greens, Z=Z)
+        return cache[("x", f)]
+
+    sol.greens, sol.solve_currents = cached_greens, cached_solve
+    return cache
+
+
 def solve_point(sol, f):
     """Everything the sweep computes at one frequency, step by step."""
     g = sol.greens(f)
@@ -49,6 +85,23 @@ def solve_point(sol, f):
     x = sol.solve_currents(f, greens=g, Z=Z.copy())
     q = sol.charges(x, g.omega)
     return g, Z, x, q
+
+
+def stage_arrays(sol, g, x, q):
+    """The de-embedding's inputs at one frequency as mom25d's sweep forms them
+    (Engine/mom25d/solver.py:1276-1301): line voltages phi at every port's
+    voltage points (ports in order, (M, P)), cut currents I and cut voltages
+    V of every port ((sum Ns, P))."""
+    npt = len(sol.ports)
+    phi = [None] * npt
+    for lay in dict.fromkeys(p.layer for p in sol.ports):
+        ps = [p for p in range(npt) if sol.ports[p].layer == lay]
+        vp = sol.line_voltage(g, q, np.concatenate([sol.pm[p].vpts for p in ps]), lay)
+        for p, v in zip(ps, np.split(vp, np.cumsum([len(sol.pm[p].vpts) for p in ps])[:-1])):
+            phi[p] = v
+    I = np.concatenate([sol.pm[p].currents(x) for p in range(npt)])
+    V = np.concatenate([sol.pm[p].voltages(phi[p]) for p in range(npt)])
+    return dict(phi=np.concatenate(phi), I=I, V=V)
 
 
 def sweep(sol, freqs):
@@ -62,12 +115,18 @@ def result_arrays(r, prefix=""):
             prefix + "fit_residual": r.fit_residual, prefix + "S50": r.renormalize(50)}
 
 
-def case(name, freqs_full=None, zfull=False, zrows=None, sweep_freqs=None, kw=None):
+def fixture_name(name, kw):
+    return f"{name}{'_' + str(kw['k']) if kw and 'k' in kw else ''}"
+
+
+def case(name, freqs_full=None, zfull=False, zrows=None, sweep_freqs=None, kw=None, tables=True):
     lay, stack, mkw, freqs = workloads.BUILDERS[name](ref, **(kw or {}))
     m = lay.mesh(**mkw)
     sol = ref.Solver(m, stack, verbose=False, method="dense")
+    cache_points(sol)
     out = dict(N=m.n_unknowns, Nt=len(m.tris), mesh_sha=mesh_digest(m), rho_max=sol.rho_max)
     f0 = freqs[0] if sweep_freqs is None else sweep_freqs[0]
+    t = time.time()
     g, Z, x, q = solve_point(sol, f0)
     out["f0"] = f0
     if zfull:
@@ -77,14 +136,17 @@ def case(name, freqs_full=None, zfull=False, zrows=None, sweep_freqs=None, kw=No
         out["Z_rows_idx"] = rows
         out["Z_rows"] = Z[rows]
         out["Z_diag"] = np.diag(Z).copy()
+    del Z
     out["x"] = x
     out["q"] = q
-    if sol.single:
+    out.update(stage_arrays(sol, g, x, q))
+    print(f"{name}: first point {time.time() - t:.1f} s", flush=True)
+    if sol.single and tables:
         out["rho_tab"] = g.rho_tab
         out["SA_tab"], out["SV_tab"], out["SW_tab"] = g.SA_tab, g.SV_tab, g.SW_tab
         out["spl_c"], out["splw_c"] = g._spl.c, g._splw.c
         out["cv"] = g.cv
-    else:
+    elif tables:
         out["rho_tab"] = g.rho_tab
         L = len(g.levels)
         for i in range(L):
@@ -99,8 +161,74 @@ def case(name, freqs_full=None, zfull=False, zrows=None, sweep_freqs=None, kw=No
     out["freqs"] = sf
     out["sweep_seconds"] = dt
     out.update(result_arrays(r))
-    np.savez_compressed(os.path.join(HERE, f"{name}{'_' + str(kw['k']) if kw and 'k' in kw else ''}.npz"), **out)
+    np.savez_compressed(os.path.join(HERE, fixture_name(name, kw) + ".npz"), **out)
     print(f"{name}: N={m.n_unknowns} Nt={len(m.tris)} {len(sf)} freqs {dt:.1f} s ({dt / len(sf):.2f} s/pt)", flush=True)
+
+
+FLOOR_EPS = (1e-15, 1e-14, 1e-13, 1e-12, 1e-11, 1e-10)
+
+
+def floor_case(name, sweep_freqs, seeds=4, kw=None):
+    """The reference's own reproducibility floor: mom25d's sweep at the same
+    frequencies with (a) the inputs of its wave fit (cut currents I and
+    voltages V, Engine/mom25d/solver.py:618-670) and (b) its RWG currents x
+    multiplied by 1 + eps (n1 + j n2), n standard normal, seeded, for eps in
+    FLOOR_EPS. Stored: per eps, the largest |S - S0| over the seeds at each
+    frequency, and the largest relative change of gamma. A re-implementation
+    whose fit inputs differ from mom25d's by eps cannot be expected to match
+    mom25d's S closer than this."""
+    lay, stack, mkw, _ = workloads.BUILDERS[name](ref, **(kw or {}))
+    m = lay.mesh(**mkw)
+    sol = ref.Solver(m, stack, verbose=False, method="dense")
+    cache = cache_points(sol)
+    freqs = np.asarray(sweep_freqs, float)
+    r0 = sol.sweep(freqs, interp=None)
+    fit0 = ref_solver.fit_waves
+    cached = sol.solve_currents
+    out = dict(freqs=freqs, eps=np.array(FLOOR_EPS), S=r0.S, gamma=r0.gamma, N=m.n_unknowns)
+    for mode in ("fit", "x"):
+        dS = np.zeros((len(FLOOR_EPS), len(freqs)))
+        dg = np.zeros((len(FLOOR_EPS), len(freqs)))
+        for ie, eps in enumerate(FLOOR_EPS):
+            for seed in range(seeds):
+                rng = np.random.default_rng(1000 * ie + seed)
+
+                def noisy(a):
+                    return a * (1 + eps * (rng.standard_normal(a.shape) + 1j * rng.standard_normal(a.shape)))
+
+                def fit(s_list, I_list, V_list, gamma0, **k):
+                    return fit0(s_list, [noisy(I) for I in I_list], [noisy(V) for V in V_list], gamma0, **k)
+
+                def solve(f, **k):
+                    return noisy(cached(f, **k))
+
+                try:
+                    if mode == "fit":
+                        ref_solver.fit_waves = fit
+                    else:
+                        sol.solve_currents = solve
+                    r = sol.sweep(freqs, interp=None)
+                finally:
+                    ref_solver.fit_waves = fit0
+                    sol.solve_currents = cached
+                dS[ie] = np.maximum(dS[ie], np.abs(r.S - r0.S).max(axis=(1, 2)))
+                dg[ie] = np.maximum(dg[ie], (np.abs(r.gamma - r0.gamma) / np.abs(r0.gamma)).max(axis=1))
+        out[f"dS_{mode}"], out[f"dgamma_{mode}"] = dS, dg
+        print(f"floor {name} {mode}: max |dS| per eps", dS.max(1), flush=True)
+    del cache
+    return out
+
+
+def floor_all():
+    cases = dict(line=("line", [2e9, 7e9], None), tee=("tee", np.linspace(1, 10, 37)[[0, 12, 24, 36]] * 1e9, None),
+                 via=("via", [2e9, 10e9, 18e9], None), bandpass_0=("bandpass", [3e9, 9e9], dict(k=0)),
+                 lpf=("lpf", [0.5e9, 4e9, 8e9], None))
+    out = {}
+    for key, (name, fr, kw) in cases.items():
+        for k, v in floor_case(name, fr, kw=kw).items():
+            out[f"{key}_{k}"] = v
+    np.savez_compressed(os.path.join(HERE, "fit_floor.npz"), cases=np.array(list(cases)), **out)
+    print("fit floor: done", flush=True)
 
 
 def interp_case(name, interp_kw=None, nfreq=None, zrows=None):
@@ -226,11 +354,18 @@ def kernels():
 
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default=os.environ.get("MOM25D_SRC"),
+                    help="directory holding mom25d's package (default: $MOM25D_SRC)")
     ap.add_argument("--quick", action="store_true", help="small cases only")
     ap.add_argument("--interp", action="store_true", help="only the FreqInterp fixtures")
     ap.add_argument("--network", action="store_true", help="only the network / waves fixture")
     ap.add_argument("--lumped", action="store_true", help="only the lumped-component fixture")
+    ap.add_argument("--floor", action="store_true", help="only the wave-fit floor fixture")
+    ap.add_argument("--variants", action="store_true", help="only band-pass variants 3, 7, 11 and 14")
+    ap.add_argument("--gcpw", action="store_true",
+                    help="only the grounded CPW (N = 25284: ~30 GB of memory, ~20 min per frequency)")
     args = ap.parse_args()
+    import_reference(args.ref)
     os.environ.setdefault("OPENBLAS_NUM_THREADS", "4")
     if args.network:
         network_case()
@@ -242,6 +377,20 @@ def main():
         interp_case("tee", zrows=np.arange(0, 1085, 97))
         interp_case("shunt_via", interp_kw=dict(step=1.5e9), nfreq=25, zrows=np.arange(0, 492, 41))
         return
+    if args.floor:
+        floor_all()
+        return
+    fb = np.linspace(1, 12, 128) * 1e9
+    if args.variants:
+        for k in (3, 7, 11, 14):
+            n = workloads.BANDPASS_N[k]
+            case("bandpass", kw=dict(k=k), zrows=np.arange(0, n, n // 7), sweep_freqs=fb[[10, 60, 115]],
+                 tables=False)
+        return
+    if args.gcpw:
+        fg = np.linspace(1, 20, 64) * 1e9
+        case("gcpw", zrows=np.arange(0, 25284, 4214), sweep_freqs=[fg[0], fg[31]], tables=False)
+        return
     kernels()
     case("line", zrows=np.arange(0, 546, 37))
     case("shunt_via", zrows=np.arange(0, 492, 41))
@@ -250,7 +399,8 @@ def main():
     case("tee", zrows=np.arange(0, 1085, 97))
     case("via", zrows=np.arange(0, 3789, 379), sweep_freqs=[2e9, 10e9, 18e9])
     case("bandpass", kw=dict(k=0), zrows=np.arange(0, 1524, 211), sweep_freqs=[3e9, 9e9])
-    case("lpf", zrows=np.arange(0, 5943, 743), sweep_freqs=[0.5e9, 4e9, 8e9])
+    # 11 of the 101 frequencies, 0.5 GHz (the hardest for the mixed refinement) to 8 GHz
+    case("lpf", zrows=np.arange(0, 5943, 743), sweep_freqs=np.linspace(0.5, 8, 101)[::10] * 1e9)
 
 
 if __name__ == "__main__":

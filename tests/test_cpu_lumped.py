@@ -5,6 +5,7 @@ lumped_line workload (tests/golden/lumped_line.npz; make_golden.py
 the oracle's fill."""
 
 import hashlib
+import os
 from types import SimpleNamespace
 
 import numpy as np
@@ -118,3 +119,33 @@ def test_oracle_lumped_sweeps_match_reference():
                 got[key].append(sw.deembed(f, kern, x, q)[0])
         for key, _ in variants:
             assert np.abs(np.array(got[key]) - g[key]).max() < 1e-6, (name, key)
+
+
+def test_checkpoint_key_depends_on_the_lumped_values():
+    """A checkpoint written under one set of lumped values is not resumed
+    under another: the key's last field is a process-independent digest of
+    the overrides, the layout's values and the multi-port blocks."""
+    import subprocess
+    import sys
+
+    from mom25d_gb300 import workloads
+    from mom25d_gb300.solver import checkpoint_key, values_digest
+
+    lay, st, m, freqs = workloads.build(G, "lumped_line")
+    lumped = list(m.layout.lumped)
+    k0 = checkpoint_key(m, freqs, values_digest({}, lumped))
+    k1 = checkpoint_key(m, freqs, values_digest({"Z1": "C 1p"}, lumped))
+    k2 = checkpoint_key(m, freqs, values_digest({"Z1": None}, lumped))
+    k1b = checkpoint_key(m, freqs, values_digest({"Z1": "C 1p"}, lumped))
+    assert not np.allclose(k0, k1, rtol=1e-12, atol=0)
+    assert not np.allclose(k1, k2, rtol=1e-12, atol=0)
+    assert not np.allclose(k0, k2, rtol=1e-12, atol=0)
+    np.testing.assert_array_equal(k1, k1b)
+    # the same digest in a fresh interpreter (string hashing is salted per process)
+    code = ("from mom25d_gb300 import workloads; import mom25d_gb300 as G; "
+            "from mom25d_gb300.solver import values_digest; "
+            "lay, st, m, f = workloads.build(G, 'lumped_line'); "
+            "print(repr(values_digest({'Z1': 'C 1p'}, list(m.layout.lumped))))")
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, check=True,
+                         cwd=os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    assert float(out.stdout.strip()) == k1[-1]

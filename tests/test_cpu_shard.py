@@ -80,3 +80,76 @@ def test_sharded_map_two_gloo_ranks_matches_one_process(tmp_path):
     got = np.load(out)
     want = np.array([_fake_point(f)[0] for f in items])
     np.testing.assert_array_equal(got, want)
+
+
+class _StubSolver:
+    """Stands in for Solver on a CPU rank (there is no CPU path of the
+    engine): point(f) returns a deterministic 2-port result of f and of the
+    lumped value override "Z1", so the test sees whether values reached every
+    rank."""
+
+    class _Port:
+        def __init__(self, name):
+            self.name = name
+
+    def __init__(self, stale=None):
+        import types
+
+        self.mesh = types.SimpleNamespace(n_unknowns=1500)
+        self.values = dict(stale or {})
+        self.ports = [self._Port("P1"), self._Port("P2")]
+
+    def point(self, f, keep_currents=False):
+        r = float(self.values.get("Z1", 0.0))
+        g = f * 1e-9
+        S = np.array([[np.exp(-1j * g), 0.1 + r], [0.1 + r, np.exp(-2j * g)]])
+        z0 = np.array([50.0, 50.0 + r])
+        return (S, z0, 1j * g * np.ones(2), z0.astype(complex), np.array([1e-3, 2e-3]) * g, None,
+                dict(refine_steps=int(g) % 5, waves=np.eye(2) * g))
+
+
+def _sweep_rank_main(rank, world, port, freqs, values, out_path):
+    import torch.distributed as dist
+
+    from mom25d_gb300.shard import sweep_sharded
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        res = sweep_sharded(_StubSolver(stale={"Z1": 7.0}), freqs, rank, world, values=values)
+        if rank == 0:
+            np.savez(out_path, S=res.S, z0=res.z0, gamma=res.gamma, z0_line=res.z0_line, res=res.fit_residual,
+                     waves=res.waves, steps=np.array(res.info["refine_steps"]), ranks=res.info["ranks"],
+                     names=np.array(res.port_names), freqs=res.freqs)
+        else:
+            assert res is None
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("values", [None, {"Z1": 2.0}])
+def test_sweep_sharded_assembles_the_full_result(tmp_path, values):
+    """sweep_sharded on two gloo ranks: rank 0 gets every frequency's S, z0,
+    gamma, z0_line, residual, waves and refine steps in frequency order, as a
+    one-process sweep_sharded gives them, and the value overrides (or their
+    absence, which clears a stale override) reach both ranks."""
+    import torch.multiprocessing as mp
+
+    from mom25d_gb300.shard import sweep_sharded
+
+    freqs = np.linspace(1e9, 12e9, 9)
+    out = str(tmp_path / "r.npz")
+    mp.start_processes(_sweep_rank_main, args=(2, _free_port(), freqs, values, out), nprocs=2, join=True,
+                       start_method="spawn")
+    got = np.load(out)
+    want = sweep_sharded(_StubSolver(stale={"Z1": 7.0}), freqs, values=values)
+    np.testing.assert_array_equal(got["freqs"], freqs)
+    for k, v in (("S", want.S), ("z0", want.z0), ("gamma", want.gamma), ("z0_line", want.z0_line),
+                 ("res", want.fit_residual), ("waves", want.waves)):
+        np.testing.assert_array_equal(got[k], v, err_msg=k)
+    assert list(got["steps"]) == want.info["refine_steps"]
+    assert int(got["ranks"]) == 2
+    assert list(got["names"]) == ["P1", "P2"]
+    r = 0.0 if values is None else values["Z1"]
+    assert np.all(got["S"][:, 0, 1] == 0.1 + r)

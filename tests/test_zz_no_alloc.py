@@ -5,9 +5,12 @@ framework's caching allocator, a fixed arena) and that cannot let this
 library call cudaMalloc / cudaFree while they run: they hand in device
 buffers for Z, B, X and the pivots, and the library's only scratch is one
 static device array. Checked through the C ABI against m25_dense_solve on
-the same systems, on two calls in a row (the array keeps the previous call's
-contents, which each call must clear). The buffers below are allocated by
-this test, which plays the caller.
+the same systems, on calls in a row (the array keeps the previous call's
+contents, which each call must clear). The third order, 4000, is above what
+the fp64 cluster panel holds (about 2900 trailing rows), so its first panels
+run the cooperative panel kernel, whose grid-barrier words and candidate
+pivot rows live in the static array. The buffers below are allocated by this
+test, which plays the caller.
 
 This file is collected last on purpose, so that a run that stops at the
 first failure has run every other test before it.
@@ -40,7 +43,7 @@ def test_noalloc_solve_matches_dense_solve(gpu):
     lib = E.load()
     ctx = E.Context(0)
     info = np.zeros(2, np.int32)
-    for call, n in enumerate((700, 1301)):
+    for call, n in enumerate((700, 1301, 4000)):
         A, B = system(n, 100 + call)
         # the existing entry point, host buffers
         Xref = np.zeros_like(B)
