@@ -26,25 +26,26 @@ from .constants import C0
 
 
 class FreqInterp:
-    """Interpolated impedance matrices for Solver.sweep(..., interp=FreqInterp(...)).
+    """Z interpolated between exact fills, for Solver.sweep(..., interp=FreqInterp(...)).
 
-    step     : anchor spacing [Hz] (anchors span the requested band evenly);
-               None: 0.35 c / (k_ratio D), D the largest distance between
-               basis functions
-    order    : interpolation order (3 = cubic, 4 anchors per point)
-    k_ratio  : phase-extraction wavenumber k_e = k_ratio * k0; None picks
-               sqrt(eps_eff) of a quasi-static estimate for the stack
-    check    : fill the first frequency that lies between anchors (at least
-               a quarter step from both) exactly as well, and print the
-               relative interpolation error of Z
-    block    : accepted for the reference's signature (its host loop works in
-               row blocks; the device kernels need none)
-    dtype    : None (complex128 if it fits, else complex64), np.complex128 or
-               np.complex64 storage of the anchors
-    resident : None: keep every anchor of the band on the device when they
-               take less than 40 % of the free device memory; True / False
-               force it (an addition to the reference's signature)
-    (Engine/mom25d/freqinterp.py:27-88)
+    The arguments are mom25d's (Engine/mom25d/freqinterp.py:27-88) plus one:
+    step      anchor spacing [Hz]; the anchors cover the swept band at even
+              spacing. None derives it from the layout: 0.35 c / (k_ratio D)
+              with D the largest distance between two basis centres.
+    order     Lagrange order; order + 1 anchors enter each point (1..7 here).
+    k_ratio   the phase taken out before interpolating is exp(-j k_ratio k0 R);
+              None estimates k_ratio as the square root of a quasi-static
+              effective permittivity of the stack.
+    check     also fill exactly the first swept frequency that sits at least
+              a quarter step away from every anchor, and print how far the
+              interpolated Z is from it.
+    block     kept for signature compatibility (the host implementation in
+              mom25d walks the rows in blocks; the device kernels do not).
+    dtype     anchor storage: np.complex128, np.complex64, or None for
+              complex128 when it fits in device memory, else complex64.
+    resident  (not in mom25d) None keeps all anchors of the band on the
+              device when they need under 40 % of its free memory; True or
+              False forces the choice.
     """
 
     def __init__(self, step=None, order=3, k_ratio=None, check=False, block=1024, dtype=None, resident=None):
@@ -227,8 +228,10 @@ class FreqInterp:
                                                                waves=sol.last_waves()))
 
     def report_error(self, f, Zi=None):
-        """Relative interpolation error of Z at f (one exact fill), per block
-        (RWG, RWG-via, via-via); returns the largest (freqinterp.py:170-189)."""
+        """Fill Z exactly at f and compare: the relative Frobenius error of
+        the interpolated Z in each block (RWG-RWG, RWG-via and via-via,
+        taken apart because the via entries are orders of magnitude larger);
+        prints them and returns the worst (Engine/mom25d/freqinterp.py:151-170)."""
         Zi = self.impedance(f) if Zi is None else Zi
         Ze = self.solver.impedance(f, precision="fp64")
         nb = self.nb
@@ -240,9 +243,10 @@ class FreqInterp:
             if ne > 0:
                 errs[k] = np.linalg.norm(Zi[a, b] - Ze[a, b]) / ne
         err = max(errs.values())
-        print(f"  FreqInterp check at {f / 1e9:.4f} GHz: relative error of Z "
-              + ", ".join(f"{k} {v:.1e}" for k, v in errs.items())
-              + f" (anchors every {np.diff(self.anchors).mean() / 1e9:.3g} GHz, order {self.order})")
+        spacing = np.diff(self.anchors).mean() / 1e9
+        parts = "; ".join(f"{k}: {v:.1e}" for k, v in errs.items())
+        print(f"  interpolated Z vs exact fill at {f / 1e9:.4f} GHz -- {parts} "
+              f"[order {self.order}, anchor spacing {spacing:.3g} GHz]")
         self.last_error = err
         return err
 

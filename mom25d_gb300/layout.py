@@ -1,26 +1,62 @@
-"""Manhattan layouts (rectangles, microstrip / GCPW port feeds, vias) and the
-tensor-grid triangulation with RWG edges that the sweep engine consumes.
+"""Layouts on named metal levels and their structured triangle mesh: the
+input side of the sweep path.
 
-This is the input side of the sweep path. The node numbering, the triangle
-order, the RWG edge order and the via segment split must be the same as
-mom25d's grid mesher (mom25d/mesh.py:696-1097) so that impedance matrices and
-currents compare entry by entry; the construction below follows the same
-steps (grid lines from rectangle edges plus edge-cell refinement, one cell
-split into two triangles with a checkerboard diagonal, RWG edges found by
-sorting node-pair keys). Polygons, pours, thick metal, lumped gaps, planes
-and apertures are not part of this engine.
+A layout here is what mom25d's grid mesher accepts for the workloads of this
+engine: axis-aligned copper rectangles per metal level, feed ports along x or
+y (optionally with coplanar side grounds and fence vias), plated round vias
+and lumped gaps with their copper bridges. The public names and the meaning
+of every argument are mom25d's (Layout / Port / Via / CoplanarGround,
+Engine/mom25d/mesh.py:25-460), so a script written for mom25d builds the
+same geometry here.
+
+How the mesh is made (`mesh()`):
+
+1. Grid lines. Every rectangle edge, every feed's reference plane and delta
+   gap, and every lumped gap and bridge end is a grid line of its axis; with
+   an edge cell, lines one edge cell to either side of each of those are
+   added unless another fixed line is nearer than half an edge cell. Lines
+   closer than 1e-9 of the layout's extent are merged, and each interval is
+   cut evenly into cells no longer than max_cell.
+2. Cells to triangles. All levels share the grid. A cell whose centre lies
+   in copper of a level becomes two triangles of that level, split along the
+   diagonal that alternates from cell to cell like a chessboard.
+3. Unknowns. Every edge shared by two triangles is an RWG basis (sorted by
+   its node pair); then one vertical current per via segment, a via being
+   split at every meshed level it passes.
+
+The numbering of nodes, triangles, edges and via segments is the one mom25d
+produces for the same layout, because parity with mom25d compares impedance
+matrices and currents entry by entry; `tests/test_cpu_mesh_oracle.py` checks
+it by hash against meshes made by mom25d. Polygons, pours, thick metal,
+inner planes, antipads and apertures are not part of this engine.
 """
 
 from dataclasses import dataclass, field
 
 import numpy as np
 
-_DIRS = {"+x": (1, 0), "-x": (-1, 0), "+y": (0, 1), "-y": (0, -1)}
+# feed direction -> (axis the feed runs along, sign along that axis)
+_HEADINGS = {"+x": (0, 1), "-x": (0, -1), "+y": (1, 1), "-y": (1, -1)}
+
+
+def _heading(name, direction):
+    try:
+        return _HEADINGS[direction]
+    except (KeyError, TypeError):
+        raise ValueError(f"{name}: this engine meshes feeds that run along an axis; direction must be one of "
+                         f"{sorted(_HEADINGS)}, got {direction!r}") from None
 
 
 @dataclass
 class CoplanarGround:
-    """Side-ground strips of a GCPW feed (mom25d/mesh.py:25-59)."""
+    """Ground strips beside a feed (a grounded coplanar feed) and the vias
+    that tie them down. gap / width: one number for both sides, or a pair
+    (left, right) where left is the side at +t, to the left of the feed's
+    outward direction; a side whose gap is None or whose width is 0 has no
+    strip. via_pitch: spacing of the vias along each strip's centre line
+    (None: no vias); via_drill / via_pad: their drill and pad diameters (pad
+    default: twice the drill, at most 0.9 of the strip width); via_to: the
+    level the vias end on."""
 
     gap: object
     width: object
@@ -31,21 +67,31 @@ class CoplanarGround:
     via_connect: tuple = ()
 
     def sides(self):
-        g = self.gap if isinstance(self.gap, (tuple, list)) else (self.gap, self.gap)
-        w = self.width if isinstance(self.width, (tuple, list)) else (self.width, self.width)
-        return [(sg, float(gi), float(wi)) for sg, gi, wi in zip((1, -1), g, w) if gi is not None and wi]
+        """(sign of t, gap, width) for each side that carries a strip, +t first."""
+        both = lambda v: tuple(v) if isinstance(v, (tuple, list)) else (v, v)  # noqa: E731
+        out = []
+        for sign, g, w in zip((1, -1), both(self.gap), both(self.width)):
+            if g is not None and w:
+                out.append((sign, float(g), float(w)))
+        return out
 
     def key(self, scale):
-        return tuple((sg, round(gi / scale, 6), round(wi / scale, 6)) for sg, gi, wi in self.sides())
+        """The strips' geometry in units of `scale`, rounded: feeds whose
+        keys (and widths and levels) agree share one wave fit."""
+        return tuple((sign, round(g / scale, 6), round(w / scale, 6)) for sign, g, w in self.sides())
 
 
 @dataclass
 class Port:
-    """Axis-aligned feed line with a delta-gap source (mom25d/mesh.py:62-188).
+    """A straight feed line with a delta-gap source near its open end.
 
-    direction points away from the circuit; the S-parameters are referenced
-    to `ref`; the gap sits `gap_from_end` (default: the width) before the
-    open end."""
+    The feed starts at the reference plane `ref` (the point on its centre
+    line where S is referenced) and runs `length` along `direction`, away
+    from the circuit; the gap sits `gap_from_end` (default: the width) short
+    of the open end. `margin` keeps the wave fit that far from the reference
+    plane and from the gap (default max(1.5 width, 4 h)). Positions along
+    the feed are s (0 at the reference plane), across it t (positive to the
+    left of the direction)."""
 
     name: str
     ref: tuple
@@ -60,70 +106,88 @@ class Port:
 
     def __post_init__(self):
         if self.z0_from not in ("voltage", "reciprocity"):
-            raise ValueError("z0_from must be 'voltage' or 'reciprocity'")
-        if self.direction not in _DIRS:
-            raise ValueError(f"direction must be one of {list(_DIRS)} (this engine meshes Manhattan feeds only)")
-        self.u = np.array(_DIRS[self.direction], float)
-        self.n = np.array([-self.u[1], self.u[0]])
+            raise ValueError(f"port {self.name}: z0_from is 'voltage' or 'reciprocity', not {self.z0_from!r}")
+        self.axis, self.sgn = _heading(f"port {self.name}", self.direction)
         self.ref = (float(self.ref[0]), float(self.ref[1]))
         if self.gap_from_end is None:
             self.gap_from_end = self.width
+        # t grows to the left of the direction: +y for +x, -x for +y, ...
+        self.side = self.sgn if self.axis == 0 else -self.sgn
+        self.u = np.zeros(2)
+        self.u[self.axis] = self.sgn
+        self.n = np.zeros(2)
+        self.n[1 - self.axis] = self.side
         self.aligned = True
-        self.axis = 0 if self.direction[1] == "x" else 1
-        self.sgn = _DIRS[self.direction][self.axis]
 
     @property
     def s_gap(self):
+        """Distance of the delta gap from the reference plane."""
         return self.length - self.gap_from_end
 
     def coord(self, s):
+        """Layout coordinate (along the feed's axis) of the cut at s."""
         return self.ref[self.axis] + self.sgn * s
 
     def point(self, s, t=0.0):
+        """(x, y) of the feed-frame points (s, t); broadcasts."""
         s, t = np.broadcast_arrays(np.asarray(s, float), np.asarray(t, float))
-        return np.asarray(self.ref) + s[..., None] * self.u + t[..., None] * self.n
+        xy = np.empty(s.shape + (2,))
+        xy[..., self.axis] = self.ref[self.axis] + self.sgn * s
+        xy[..., 1 - self.axis] = self.ref[1 - self.axis] + self.side * t
+        return xy
 
     def local(self, xy):
-        d = np.asarray(xy, float) - np.asarray(self.ref)
-        return d @ self.u, d @ self.n
+        """Feed-frame (s, t) of layout points (..., 2)."""
+        xy = np.asarray(xy, float)
+        s = self.sgn * (xy[..., self.axis] - self.ref[self.axis])
+        t = self.side * (xy[..., 1 - self.axis] - self.ref[1 - self.axis])
+        return s, t
+
+    def _box(self, t_lo, t_hi):
+        """Layout rectangle over the whole feed length between t_lo < t_hi."""
+        a0, a1 = sorted((self.coord(0.0), self.coord(self.length)))
+        b0, b1 = sorted((self.ref[1 - self.axis] + self.side * t_lo, self.ref[1 - self.axis] + self.side * t_hi))
+        return (a0, b0, a1, b1) if self.axis == 0 else (b0, a0, b1, a1)
 
     def rect(self):
-        a = self.axis
-        c0, c1 = sorted((self.ref[a], self.coord(self.length)))
-        t = self.ref[1 - a]
-        lo, hi = t - self.width / 2, t + self.width / 2
-        return (c0, lo, c1, hi) if a == 0 else (lo, c0, hi, c1)
+        """The feed's copper as (x0, y0, x1, y1)."""
+        return self._box(-self.width / 2, self.width / 2)
 
-    def ground_strips(self):
+    def ground_rects(self):
+        """The side-ground strips' copper, one rectangle per side."""
         if self.ground is None:
             return []
         out = []
-        for sg, g, w in self.ground.sides():
-            t0, t1 = sorted((sg * (self.width / 2 + g), sg * (self.width / 2 + g + w)))
-            out.append([tuple(self.point(s, t)) for s, t in
-                        ((0, t0), (self.length, t0), (self.length, t1), (0, t1))])
+        for sign, g, w in self.ground.sides():
+            t0, t1 = sorted((sign * (self.width / 2 + g), sign * (self.width / 2 + g + w)))
+            out.append(self._box(t0, t1))
         return out
 
     def ground_vias(self):
+        """Fence vias along the centre of each side strip, every via_pitch
+        from half a pitch on, while a whole pad fits on the feed."""
         G = self.ground
         if G is None or not G.via_pitch:
             return []
-        n = int(np.floor(self.length / G.via_pitch))
-        s = (np.arange(n) + 0.5) * G.via_pitch
-        out = []
-        for sg, g, w in G.sides():
+        s = (np.arange(int(np.floor(self.length / G.via_pitch))) + 0.5) * G.via_pitch
+        vias = []
+        for sign, g, w in G.sides():
             pad = min(G.via_pad or 2 * G.via_drill, 0.9 * w)
             if pad < G.via_drill:
-                raise ValueError(f"port {self.name}: ground strip too narrow for its fence vias")
-            t = sg * (self.width / 2 + g + w / 2)
-            out += [Via(tuple(self.point(si, t)), G.via_drill, pad, top=self.layer, bottom=G.via_to,
-                        connect=tuple(G.via_connect)) for si in s[s <= self.length - pad / 2]]
-        return out
+                raise ValueError(f"port {self.name}: a {w * 1e3:g} mm ground strip has no room for "
+                                 f"{G.via_drill * 1e3:g} mm fence vias")
+            t = sign * (self.width / 2 + g + w / 2)
+            for si in s[s <= self.length - pad / 2]:
+                vias.append(Via(tuple(self.point(si, t)), G.via_drill, pad, top=self.layer, bottom=G.via_to,
+                                connect=tuple(G.via_connect)))
+        return vias
 
 
 @dataclass
 class Via:
-    """Plated via between two metal levels ("gnd" = ground plane), mom25d/mesh.py:191-241."""
+    """A plated round via from metal level `top` down to `bottom` ("gnd" is
+    the ground plane), with a round pad (default twice the drill) on each
+    meshed level it ends on."""
 
     xy: tuple
     drill: float
@@ -139,20 +203,26 @@ class Via:
         self.connect = tuple(self.connect)
         if self.pad is None:
             self.pad = 2 * self.drill
+        where = f"via at ({self.xy[0] * 1e3:g}, {self.xy[1] * 1e3:g}) mm"
         if self.pad < self.drill:
-            raise ValueError("via pad smaller than its drill")
+            raise ValueError(f"{where}: its pad ({self.pad * 1e3:g} mm) is narrower than its drill")
         if self.top == self.bottom:
-            raise ValueError("via top and bottom layer are the same")
+            raise ValueError(f"{where}: it starts and ends on {self.top!r}")
         if self.connect or self.antipad is not None:
-            raise ValueError("inner-plane connections and antipads are not part of this engine")
+            raise ValueError(f"{where}: plane connections and antipads need inner planes, which this engine "
+                             "does not model")
 
     def pad_layers(self):
-        return [n for n in (self.top, self.bottom) if n != "gnd"]
+        """The meshed levels the via has a pad on."""
+        return [lv for lv in (self.top, self.bottom) if lv != "gnd"]
 
 
 @dataclass
 class Layout:
-    """Copper rectangles, port feeds and vias on named metal levels."""
+    """Copper on named metal levels: rectangles, feed ports, vias, lumped
+    gaps and multi-port blocks across them. Every add_* takes the level as
+    `layer=` (default "top"); the names are metal levels of the Stackup the
+    layout is solved on."""
 
     rects: list = field(default_factory=list)
     rect_layers: list = field(default_factory=list)
@@ -169,54 +239,56 @@ class Layout:
         return self
 
     def add_port(self, name, ref, direction, width, length, **kw):
-        p = Port(name, tuple(ref), direction, width, length, **kw)
-        self.ports.append(p)
-        self.add_rect(*p.rect(), layer=p.layer)
-        for c in p.ground_strips():
-            xs, ys = zip(*c)
-            self.add_rect(min(xs), min(ys), max(xs), max(ys), layer=p.layer)
-        self.vias.extend(p.ground_vias())
-        return p
+        """A feed port (see Port); its line, side grounds and fence vias
+        become copper of the layout."""
+        port = Port(name, tuple(ref), direction, width, length, **kw)
+        self.ports.append(port)
+        for r in [port.rect()] + port.ground_rects():
+            self.add_rect(*r, layer=port.layer)
+        self.vias.extend(port.ground_vias())
+        return port
 
     def add_lumped(self, name, a, b, width, value=None, layer="top"):
-        """Lumped component across a delta gap in the middle of a copper
-        bridge of `width` from pad point a to pad point b (axis-aligned),
-        loaded with `value` (lumped.R / L / C / series / parallel, a number in
-        ohm, a callable f -> Z, a string like 'C 1p' or 'R 10 + L 0.5n'; None:
-        an open gap); voltage a -> b (mom25d/mesh.py:353-378)."""
+        """A lumped component between pad points a and b (x, y) [m]: a copper
+        bridge of `width` from a to b, along x or y, with a delta gap in its
+        middle, loaded by `value` (lumped.R / L / C / series / parallel, a
+        number in ohm, a callable f -> Z, or text such as 'C 1p' or
+        'R 10 + L 0.5n'; None leaves the gap open, e.g. for a port of a
+        multi-port block). Its voltage is taken from a to b."""
         from .lumped import as_value, parse
 
         a, b = np.asarray(a, float), np.asarray(b, float)
-        d = b - a
-        length = float(np.hypot(*d))
+        span = b - a
+        length = float(np.hypot(*span))
         if length <= 0:
-            raise ValueError("lumped component: a and b coincide")
-        if any(q.name == name for q in self.lumped) or any(q.name == name for q in self.ports):
-            raise ValueError(f"name {name!r} already used")
-        u = d / length
-        direction = next((k for k, v in _DIRS.items() if np.allclose(u, v, atol=1e-12)), None)
-        if direction is None:
-            raise ValueError(f"lumped {name}: oblique bridges need the triangular mesher (not part of this engine)")
-        g = Port(name, tuple(a), direction, width, length, gap_from_end=0.5 * length, layer=layer)
-        g.value = None if value is None else (parse(value) if isinstance(value, str) else as_value(value))
-        self.lumped.append(g)
-        self.add_rect(*g.rect(), layer=layer)
-        return g
+            raise ValueError(f"lumped {name}: its two pad points are the same")
+        taken = {q.name for q in self.lumped} | {q.name for q in self.ports}
+        if name in taken:
+            raise ValueError(f"lumped {name}: the name is already taken by a port or another component")
+        heading = next((k for k, (ax, sg) in _HEADINGS.items()
+                        if span[ax] * sg > 0 and span[1 - ax] == 0), None)
+        if heading is None:
+            raise ValueError(f"lumped {name}: bridges run along x or y in this engine")
+        gap = Port(name, tuple(a), heading, width, length, gap_from_end=0.5 * length, layer=layer)
+        gap.value = None if value is None else (parse(value) if isinstance(value, str) else as_value(value))
+        self.lumped.append(gap)
+        self.add_rect(*gap.rect(), layer=layer)
+        return gap
 
     def add_component(self, model, gaps):
-        """Multi-port component (network.Touchstone or a .sNp path) across the
-        named lumped gaps, in the model's port order; the gaps are added with
-        value=None (mom25d/mesh.py:432-447)."""
+        """A multi-port block (network.Touchstone, or a .sNp path) across the
+        named lumped gaps, port k of the model across gaps[k]; add those gaps
+        with value=None."""
         from .network import Touchstone
 
         if isinstance(model, str):
             model = Touchstone(model)
-        names = [q.name for q in self.lumped]
-        for n in gaps:
-            if n not in names:
-                raise ValueError(f"no lumped gap {n!r}")
+        known = {q.name for q in self.lumped}
+        missing = [g for g in gaps if g not in known]
+        if missing:
+            raise ValueError(f"component {model}: no lumped gaps named {missing}")
         if getattr(model, "n", len(gaps)) != len(gaps):
-            raise ValueError(f"{model} has {model.n} ports, {len(gaps)} gaps given")
+            raise ValueError(f"component {model}: {model.n} ports but {len(gaps)} gaps")
         self.components.append((model, list(gaps)))
         return self
 
@@ -226,28 +298,46 @@ class Layout:
         return v
 
     def layer_names(self):
-        names = list(self.rect_layers) + [n for v in self.vias for n in v.pad_layers()]
-        return [n for n in dict.fromkeys(names) if n not in self.planes]
+        """Meshed levels in order of first use (rectangles, then via pads)."""
+        seen = dict.fromkeys(list(self.rect_layers) + [lv for v in self.vias for lv in v.pad_layers()])
+        return [lv for lv in seen if lv not in self.planes]
 
     def all_vias(self):
         return list(self.vias)
 
     def bbox(self):
-        r = [tuple(q) for q in self.rects]
-        for v in self.vias:
-            r.append((v.xy[0] - v.pad / 2, v.xy[1] - v.pad / 2, v.xy[0] + v.pad / 2, v.xy[1] + v.pad / 2))
-        r = np.array(r)
-        return r[:, 0].min(), r[:, 1].min(), r[:, 2].max(), r[:, 3].max()
+        """(x0, y0, x1, y1) over the rectangles and the via pads."""
+        boxes = [tuple(r) for r in self.rects]
+        boxes += [(v.xy[0] - v.pad / 2, v.xy[1] - v.pad / 2, v.xy[0] + v.pad / 2, v.xy[1] + v.pad / 2)
+                  for v in self.vias]
+        b = np.array(boxes)
+        return b[:, 0].min(), b[:, 1].min(), b[:, 2].max(), b[:, 3].max()
 
     def contains(self, x, y, layer=None):
+        """Whether the points (x, y) lie strictly inside copper (of `layer`,
+        or of any level): a rectangle, or a via's round pad."""
         inside = np.zeros(np.broadcast(x, y).shape, bool)
-        for (x0, y0, x1, y1), n in zip(self.rects, self.rect_layers):
-            if layer is None or n == layer:
+        for (x0, y0, x1, y1), lv in zip(self.rects, self.rect_layers):
+            if layer is None or lv == layer:
                 inside |= (x > x0) & (x < x1) & (y > y0) & (y < y1)
-        for v in self.vias:  # round pads add copper but no grid lines
+        for v in self.vias:  # pads are copper but add no grid lines
             if layer is None or layer in v.pad_layers():
                 inside |= (x - v.xy[0]) ** 2 + (y - v.xy[1]) ** 2 < (v.pad / 2) ** 2
         return inside
+
+    def fixed_lines(self):
+        """Coordinates that must be grid lines, per axis: rectangle edges,
+        every feed's reference plane and gap, every lumped gap and the ends
+        of its bridge."""
+        lines = ([], [])
+        for x0, y0, x1, y1 in self.rects:
+            lines[0].extend((x0, x1))
+            lines[1].extend((y0, y1))
+        for p in self.ports:
+            lines[p.axis].extend((p.coord(0), p.coord(p.s_gap)))
+        for g in self.lumped:
+            lines[g.axis].extend((g.coord(0), g.coord(g.s_gap), g.coord(g.length)))
+        return lines
 
     def mesh(self, max_cell, edge_cell=None, snap=None, kind="grid"):
         if kind != "grid":
@@ -255,21 +345,70 @@ class Layout:
         return Mesh.from_layout(self, max_cell, edge_cell)
 
 
-def _grid_lines(fixed, refine, lo, hi, max_cell, tol):
-    """Sorted grid coordinates: the fixed and refinement lines (merged on a
-    `tol` lattice), each interval subdivided evenly to <= max_cell."""
-    c = np.unique(np.round(np.concatenate([fixed, refine]) / tol) * tol)
-    c = c[(c >= lo - tol) & (c <= hi + tol)]
-    out = [c[0]]
-    for a, b in zip(c[:-1], c[1:]):
-        n = int(np.ceil((b - a) / max_cell - 1e-9))
-        out.extend(np.linspace(a, b, n + 1)[1:])
-    return np.array(out)
+# ------------------------------------------------------------------ mesher
+def axis_lines(fixed, lo, hi, max_cell, edge_cell, tol):
+    """Grid coordinates of one axis: the fixed lines, the edge-cell lines
+    beside them (those at least half an edge cell from every fixed line),
+    merged on a `tol` lattice, clipped to [lo, hi] and cut into cells of at
+    most max_cell."""
+    fixed = np.asarray(fixed, float)
+    lines = fixed
+    if edge_cell:
+        beside = (fixed[:, None] + np.array([-edge_cell, edge_cell])[None, :]).ravel()
+        clear = np.abs(fixed[None, :] - beside[:, None]).min(axis=1) > 0.5 * edge_cell
+        lines = np.concatenate([fixed, beside[clear]])
+    merged = np.unique(np.round(lines / tol) * tol)
+    merged = merged[(merged >= lo - tol) & (merged <= hi + tol)]
+    parts = [merged[:1]]
+    for a, b in zip(merged[:-1], merged[1:]):
+        cells = int(np.ceil((b - a) / max_cell - 1e-9))
+        parts.append(np.linspace(a, b, cells + 1)[1:])
+    return np.concatenate(parts)
+
+
+def cell_triangles(layout, xg, yg, levels):
+    """Two triangles per copper cell of each level. Node (level, i, j) of
+    the grid has the id (level nx + i) ny + j. Per level, the cells in
+    row-major (i, j) order give first all their lower triangles, then all
+    their upper ones. Returns the triangles (ids) and their levels."""
+    nx, ny = len(xg), len(yg)
+    XC, YC = np.meshgrid(0.5 * (xg[1:] + xg[:-1]), 0.5 * (yg[1:] + yg[:-1]), indexing="ij")
+    tris, level = [], []
+    for lv, name in enumerate(levels):
+        i, j = np.nonzero(layout.contains(XC, YC, name))
+        sw = (lv * nx + i) * ny + j
+        se, ne, nw = sw + ny, sw + ny + 1, sw + 1
+        odd = ((i + j) % 2 == 1)[:, None]  # the diagonal runs se-nw on odd cells, sw-ne on even ones
+        tris.append(np.where(odd, np.stack([sw, se, nw], 1), np.stack([sw, se, ne], 1)))
+        tris.append(np.where(odd, np.stack([se, ne, nw], 1), np.stack([sw, ne, nw], 1)))
+        level.append(np.full(2 * i.size, lv))
+    return np.concatenate(tris), np.concatenate(level)
+
+
+def shared_edges(tris, n_nodes):
+    """Edges shared by two triangles, ordered by their (smaller, larger)
+    node pair. Local edge k of a triangle is the one facing its vertex k.
+    Returns the node pairs and, per edge, the triangle listed first (local
+    edges taken 0 for all triangles, then 1, then 2), its local edge, the
+    other triangle and its local edge."""
+    nt = len(tris)
+    facing = ((1, 2), (2, 0), (0, 1))
+    pairs = np.concatenate([np.sort(tris[:, list(f)], axis=1) for f in facing])  # slot = k nt + triangle
+    key = pairs[:, 0] * n_nodes + pairs[:, 1]
+    slot = np.arange(3 * nt)
+    order = np.lexsort((slot, key))
+    k_sorted = key[order]
+    same = k_sorted[1:] == k_sorted[:-1]
+    if np.any(same[1:] & same[:-1]):
+        raise ValueError("mesh edge shared by more than two triangles")
+    a, b = order[:-1][same], order[1:][same]
+    return pairs[a], a % nt, a // nt, b % nt, b // nt
 
 
 class Mesh:
-    """Triangles of all metal levels on one shared tensor grid, RWG edges,
-    via segments and port cut look-ups (the arrays mom25d's Mesh exposes)."""
+    """Triangles of all metal levels on one grid, their RWG bases, the via
+    segments and the look-ups the port models use (the arrays and methods
+    of mom25d's Mesh that the sweep path reads)."""
 
     def __init__(self, nodes, tris, layout, xg, yg, tri_layer, layer_names):
         self.nodes = np.asarray(nodes, float)
@@ -280,194 +419,165 @@ class Mesh:
         self.tri_layer = np.asarray(tri_layer, int)
         self.twin_layer = -np.ones(len(self.layer_names), int)
         self.planes = list(getattr(layout, "planes", []))
-        self._orient()
-        self._edges()
+        self._counter_clockwise()
+        self._rwg()
         self.edge_layer = self.tri_layer[self.tp]
-        self._attach_vias(layout.all_vias())
+        self.vias = layout.all_vias()
+        self.via_attach = [self._via_ends(v) for v in self.vias]
+        self.assign_levels(self.layer_names + self.planes)
 
     @classmethod
     def from_layout(cls, layout, max_cell, edge_cell=None):
         x0, y0, x1, y1 = layout.bbox()
         tol = 1e-9 * max(x1 - x0, y1 - y0)
-        fx = [c for r in layout.rects for c in (r[0], r[2])]
-        fy = [c for r in layout.rects for c in (r[1], r[3])]
-        for p in layout.ports:
-            (fx if p.axis == 0 else fy).extend([p.coord(0), p.coord(p.s_gap)])
-        for p in layout.lumped:  # a lumped gap and its bridge's ends are grid lines
-            (fx if p.axis == 0 else fy).extend([p.coord(0), p.coord(p.s_gap), p.coord(p.length)])
-        rx, ry = [], []
-        if edge_cell:
-            rx = [c + d for c in fx for d in (-edge_cell, edge_cell)]
-            ry = [c + d for c in fy for d in (-edge_cell, edge_cell)]
-            rx = [c for c in rx if np.min(np.abs(np.array(fx) - c)) > 0.5 * edge_cell]
-            ry = [c for c in ry if np.min(np.abs(np.array(fy) - c)) > 0.5 * edge_cell]
-        xg = _grid_lines(fx, rx, x0, x1, max_cell, tol)
-        yg = _grid_lines(fy, ry, y0, y1, max_cell, tol)
-        xc = 0.5 * (xg[1:] + xg[:-1])
-        yc = 0.5 * (yg[1:] + yg[:-1])
-        XC, YC = np.meshgrid(xc, yc, indexing="ij")
-        names = layout.layer_names() or ["top"]
-        ny = len(yg)
-        nxy = len(xg) * ny
-        tris, tl = [], []
-        for li, name in enumerate(names):
-            ii, jj = np.nonzero(layout.contains(XC, YC, name))
-            base = li * nxy
-            a = base + ii * ny + jj
-            b = base + (ii + 1) * ny + jj
-            c = base + (ii + 1) * ny + jj + 1
-            d = base + ii * ny + jj + 1
-            odd = ((ii + jj) % 2 == 1)[:, None]
-            tris.append(np.where(odd, np.stack([a, b, d], 1), np.stack([a, b, c], 1)))
-            tris.append(np.where(odd, np.stack([b, c, d], 1), np.stack([a, c, d], 1)))
-            tl.append(np.full(2 * ii.size, li))
-        tris = np.concatenate(tris)
-        used, inv = np.unique(tris, return_inverse=True)
-        X, Y = np.meshgrid(xg, yg, indexing="ij")
-        nodes = np.stack([np.tile(X.ravel(), len(names))[used], np.tile(Y.ravel(), len(names))[used]], 1)
-        return cls(nodes, inv.reshape(tris.shape), layout, xg, yg, np.concatenate(tl), names)
+        fx, fy = layout.fixed_lines()
+        xg = axis_lines(fx, x0, x1, max_cell, edge_cell, tol)
+        yg = axis_lines(fy, y0, y1, max_cell, edge_cell, tol)
+        levels = layout.layer_names() or ["top"]
+        ids, level = cell_triangles(layout, xg, yg, levels)
+        used, local = np.unique(ids, return_inverse=True)  # keep the grid nodes that triangles use
+        per_level = used % (len(xg) * len(yg))
+        nodes = np.stack([xg[per_level // len(yg)], yg[per_level % len(yg)]], 1)
+        return cls(nodes, local.reshape(ids.shape), layout, xg, yg, level, levels)
 
     # ------------------------------------------------------------ geometry
-    def _orient(self):
-        v = self.nodes[self.tris]
-        e1, e2 = v[:, 1] - v[:, 0], v[:, 2] - v[:, 0]
-        cross = e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0]
-        cw = cross < 0
-        self.tris[cw] = self.tris[cw][:, [0, 2, 1]]
+    def _counter_clockwise(self):
+        p = self.nodes[self.tris]
+        e1, e2 = p[:, 1] - p[:, 0], p[:, 2] - p[:, 0]
+        twice_area = e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0]
+        flip = twice_area < 0
+        self.tris[flip] = self.tris[flip][:, [0, 2, 1]]
         self.verts = self.nodes[self.tris]
-        self.area = 0.5 * np.abs(cross)
+        self.area = 0.5 * np.abs(twice_area)
         self.centroid = self.verts.mean(1)
 
-    def _edges(self):
-        """Interior edges (shared by two triangles) become RWG bases; local
-        edge i of a triangle is the one opposite its vertex i."""
+    def _rwg(self):
+        """One RWG basis per shared edge: + on the triangle listed first, -
+        on the other; tri_basis / tri_sign give each triangle's bases by
+        local edge (-1 / 0 on boundary edges)."""
         nt = len(self.tris)
-        ends = np.concatenate([np.sort(self.tris[:, [1, 2]], 1), np.sort(self.tris[:, [2, 0]], 1),
-                               np.sort(self.tris[:, [0, 1]], 1)])
-        owner = np.tile(np.arange(nt), 3)
-        local = np.repeat(np.arange(3), nt)
-        key = ends[:, 0] * len(self.nodes) + ends[:, 1]
-        order = np.argsort(key, kind="stable")
-        ks = key[order]
-        dup = ks[1:] == ks[:-1]
-        if np.any(dup[1:] & dup[:-1]):
-            raise ValueError("non-manifold edge (more than two triangles)")
-        first, second = order[:-1][dup], order[1:][dup]
-        self.edge_nodes = ends[first]
-        self.tp, self.vp = owner[first], local[first]
-        self.tm, self.vm = owner[second], local[second]
-        d = self.nodes[self.edge_nodes[:, 1]] - self.nodes[self.edge_nodes[:, 0]]
-        self.edge_len = np.hypot(d[:, 0], d[:, 1])
-        self.edge_mid = 0.5 * (self.nodes[self.edge_nodes[:, 0]] + self.nodes[self.edge_nodes[:, 1]])
+        self.edge_nodes, self.tp, self.vp, self.tm, self.vm = shared_edges(self.tris, len(self.nodes))
+        a, b = self.nodes[self.edge_nodes[:, 0]], self.nodes[self.edge_nodes[:, 1]]
+        self.edge_len = np.hypot((b - a)[:, 0], (b - a)[:, 1])
+        self.edge_mid = 0.5 * (a + b)
         self.n_basis = len(self.tp)
         self.wall = np.zeros(self.n_basis, bool)
         self.n_walls = 0
-        self.tri_basis = -np.ones((nt, 3), int)
+        self.tri_basis = np.full((nt, 3), -1)
         self.tri_sign = np.zeros((nt, 3))
-        idx = np.arange(self.n_basis)
-        self.tri_basis[self.tp, self.vp] = idx
+        basis = np.arange(self.n_basis)
+        self.tri_basis[self.tp, self.vp] = basis
+        self.tri_basis[self.tm, self.vm] = basis
         self.tri_sign[self.tp, self.vp] = 1.0
-        self.tri_basis[self.tm, self.vm] = idx
         self.tri_sign[self.tm, self.vm] = -1.0
 
     # ---------------------------------------------------------------- vias
-    def _cell_tris(self, x, y):
-        """Triangles of the grid cell(s) holding (x, y); every cell touching it
-        when it lies on a grid line."""
-        def span(g, c):
-            tol = 1e-6 * (g[-1] - g[0])
-            k = np.nonzero(np.abs(g - c) < tol)[0]
-            if k.size:
-                return g[max(k[0] - 1, 0)], g[min(k[0] + 1, len(g) - 1)]
-            i = np.searchsorted(g, c) - 1
-            return (g[i], g[i + 1]) if 0 <= i < len(g) - 1 else (c, c)
+    def _cells_at(self, x, y):
+        """Triangles whose centroid lies in the grid cell holding (x, y), or
+        in any cell touching it when it lies on a grid line."""
+        def bounds(g, c):
+            on = np.nonzero(np.abs(g - c) < 1e-6 * (g[-1] - g[0]))[0]
+            if on.size:
+                k = on[0]
+                return g[max(k - 1, 0)], g[min(k + 1, len(g) - 1)]
+            k = np.searchsorted(g, c) - 1
+            return (g[k], g[k + 1]) if 0 <= k < len(g) - 1 else (c, c)
 
-        (x0, x1), (y0, y1) = span(self.xg, x), span(self.yg, y)
-        c = self.centroid
-        return np.nonzero((c[:, 0] > x0) & (c[:, 0] < x1) & (c[:, 1] > y0) & (c[:, 1] < y1))[0]
+        (xa, xb), (ya, yb) = bounds(self.xg, x), bounds(self.yg, y)
+        cx, cy = self.centroid[:, 0], self.centroid[:, 1]
+        return np.nonzero((cx > xa) & (cx < xb) & (cy > ya) & (cy < yb))[0]
 
-    def _attach_vias(self, vias):
-        self.vias = list(vias)
-        self.via_attach = []
-        c = self.centroid
-        for v in self.vias:
-            att = {}
-            x, y = v.xy
-            d2 = (c[:, 0] - x) ** 2 + (c[:, 1] - y) ** 2
-            for li, name in enumerate(self.layer_names):
-                on = self.tri_layer == li
-                t = np.nonzero(on & (d2 < (v.drill / 2) ** 2))[0]
-                if t.size == 0:
-                    t = self._cell_tris(x, y)
-                    t = t[on[t]]
-                if t.size:
-                    att[name] = t
-            for n in v.pad_layers():
-                if n in self.layer_names and n not in att:
-                    raise ValueError(f"via at ({x * 1e3:.4g}, {y * 1e3:.4g}) mm: no meshed copper on layer {n}")
-            self.via_attach.append(att)
-        self.assign_levels(self.layer_names + self.planes)
+    def _via_ends(self, via):
+        """{level: triangles the via's current enters or leaves by}: those of
+        the level whose centroid lies within the drill, else those of the
+        grid cell under the via's centre."""
+        x, y = via.xy
+        r2 = (self.centroid[:, 0] - x) ** 2 + (self.centroid[:, 1] - y) ** 2
+        ends = {}
+        for lv, name in enumerate(self.layer_names):
+            on = self.tri_layer == lv
+            t = np.nonzero(on & (r2 < (via.drill / 2) ** 2))[0]
+            if t.size == 0:
+                t = self._cells_at(x, y)
+                t = t[on[t]]
+            if t.size:
+                ends[name] = t
+        bare = [n for n in via.pad_layers() if n in self.layer_names and n not in ends]
+        if bare:
+            raise ValueError(f"via at ({x * 1e3:.4g}, {y * 1e3:.4g}) mm ends on level {bare[0]} "
+                             "where no copper is meshed")
+        return ends
 
     def assign_levels(self, order):
-        """Split every via into vertical segments between the levels it touches
-        (top to bottom); unknown n_basis + k is segment k's downward current."""
-        rank = {n: i for i, n in enumerate(order)}
-        rank["gnd"] = -1
+        """Cut every via into vertical segments at each level it passes that
+        has copper under it, from its upper to its lower end (order: the
+        levels from bottom to top). Unknown n_basis + k is the downward
+        current of segment k."""
+        height = {name: i for i, name in enumerate(order)}
+        height["gnd"] = -1
         self.via_segments = []
-        for k, (v, att) in enumerate(zip(self.vias, self.via_attach)):
-            for n in (v.top, v.bottom):
-                if n not in rank:
-                    raise ValueError(f"via layer {n!r} is not in the stack order {order}")
-            hi, lo = sorted((rank[v.top], rank[v.bottom]), reverse=True)
-            mid = sorted([n for n in order if lo < rank[n] < hi and n in att], key=lambda n: -rank[n])
-            chain = [order[hi]] + mid + [order[lo] if lo >= 0 else "gnd"]
-            for a, b in zip(chain[:-1], chain[1:]):
-                self.via_segments.append(dict(via=k, top=a, bottom=b, top_tris=att.get(a), bottom_tris=att.get(b)))
+        for k, (via, ends) in enumerate(zip(self.vias, self.via_attach)):
+            for name in (via.top, via.bottom):
+                if name not in height:
+                    raise ValueError(f"via ends on {name!r}, which is not one of the levels {order}")
+            upper, lower = max(height[via.top], height[via.bottom]), min(height[via.top], height[via.bottom])
+            stops = [n for n in sorted(order, key=lambda n: -height[n]) if lower < height[n] < upper and n in ends]
+            chain = [order[upper], *stops, order[lower] if lower >= 0 else "gnd"]
+            for top, bottom in zip(chain[:-1], chain[1:]):
+                self.via_segments.append(dict(via=k, top=top, bottom=bottom, top_tris=ends.get(top),
+                                              bottom_tris=ends.get(bottom)))
         self.level_order = list(order)
         self.n_vias = len(self.via_segments)
         self.n_frills = 0
         self.n_ap = 0
-        self.via_tris = [g["top_tris"] for g in self.via_segments]
+        self.via_tris = [seg["top_tris"] for seg in self.via_segments]
         self.n_unknowns = self.n_basis + self.n_vias
 
     # --------------------------------------------------------------- ports
     def flow_direction(self):
+        """Unit vector from each basis' + triangle centroid to its - one."""
         d = self.centroid[self.tm] - self.centroid[self.tp]
-        n = np.linalg.norm(d, axis=1)
-        return d / np.where(n > 0, n, 1.0)[:, None]
+        length = np.linalg.norm(d, axis=1)
+        return d / np.where(length > 0, length, 1.0)[:, None]
 
     def cut_positions(self, port):
-        g = self.xg if port.axis == 0 else self.yg
-        s = port.sgn * (g - port.ref[port.axis])
-        s = s[(s > -1e-12) & (s <= port.length + 1e-12)]
-        return np.sort(s)
+        """The feed positions s in [0, length] that are grid lines, sorted."""
+        grid = self.xg if port.axis == 0 else self.yg
+        s = port.sgn * (grid - port.ref[port.axis])
+        return np.sort(s[(s > -1e-12) & (s <= port.length + 1e-12)])
 
-    def lumped_vectors(self):
-        """(N, n_lumped) signed edge lengths of each lumped gap's cut: the
-        delta-gap excitation of the gap, and l . x its current a -> b
-        (mom25d/mesh.py:1077-1087)."""
-        gaps = list(getattr(self.layout, "lumped", []))
-        Lm = np.zeros((self.n_unknowns, len(gaps)))
-        for k, p in enumerate(gaps):
-            idx, sgn = self.cut_edges(p, p.s_gap)
-            if idx.size == 0:
-                raise ValueError(f"lumped {p.name}: no mesh edges on its gap")
-            Lm[idx, k] = -sgn * self.edge_len[idx]
-        return Lm
+    def _feed_edges(self, port):
+        """The feed's candidate cut edges (on its level, mid-point within its
+        width), the s of both their ends, and the sign that makes a positive
+        coefficient a current toward the circuit. Cached per port object."""
+        cache = self.__dict__.setdefault("_feed_cache", {})
+        hit = cache.get(id(port))
+        if hit is None or hit[0] is not port:
+            s_ends, _ = port.local(self.nodes[self.edge_nodes])
+            _, t_mid = port.local(self.edge_mid)
+            idx = np.nonzero((np.abs(t_mid) < port.width / 2)
+                             & (self.edge_layer == self.layer_names.index(port.layer)))[0]
+            toward = -port.sgn * np.sign(self.flow_direction()[idx, port.axis])
+            hit = cache[id(port)] = (port, idx, s_ends[idx], toward)
+        return hit[1:]
 
     def cut_edges(self, port, s):
-        """RWG edges on the transverse cut at distance s of a feed, signed so
-        that positive current flows toward the circuit."""
-        # the edges' coordinates in the port frame do not depend on s: once per port
-        cache = self.__dict__.setdefault("_cut_frames", {})
-        key = id(port)
-        if key not in cache or cache[key][0] is not port:
-            es, _ = port.local(self.nodes[self.edge_nodes])
-            _, tm = port.local(self.edge_mid)
-            cand = (np.abs(tm) < port.width / 2) & (self.edge_layer == self.layer_names.index(port.layer))
-            idx = np.nonzero(cand)[0]
-            cache[key] = (port, es[idx], idx, np.sign(self.flow_direction()[idx] @ -port.u))
-        _, es, idx, sign = cache[key]
-        tol = 1e-6 * port.width
-        on = (np.abs(es[:, 0] - s) < tol) & (np.abs(es[:, 1] - s) < tol)
-        return idx[on], sign[on]
+        """RWG edges lying on the transverse cut at s of a feed, and their
+        signs: sum(sign * edge_len * x) over them is the current toward the
+        circuit."""
+        idx, s_ends, toward = self._feed_edges(port)
+        on = np.all(np.abs(s_ends - s) < 1e-6 * port.width, axis=1)
+        return idx[on], toward[on]
+
+    def lumped_vectors(self):
+        """(N, n_lumped): column k holds the signed edge lengths of gap k's
+        cut, oriented a -> b; it is the gap's delta-gap excitation, and its
+        dot product with the currents the current from a to b."""
+        gaps = list(getattr(self.layout, "lumped", []))
+        out = np.zeros((self.n_unknowns, len(gaps)))
+        for k, gap in enumerate(gaps):
+            idx, sign = self.cut_edges(gap, gap.s_gap)
+            if idx.size == 0:
+                raise ValueError(f"lumped {gap.name}: no mesh edge lies on its gap")
+            out[idx, k] = -sign * self.edge_len[idx]
+        return out

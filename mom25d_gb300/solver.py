@@ -164,35 +164,51 @@ class Greens:
 
 
 class PortModel:
-    """Delta-gap excitation, fit-window cuts and line-voltage sample points of
-    one feed (Engine/mom25d/solver.py:570-610)."""
+    """The per-feed data of the de-embedding (Engine/mom25d/solver.py:570-610).
+
+    - s: the grid cuts of the feed inside its fitting window, which keeps
+      `margin` (default max(1.5 width, 4 h), h the height of the feed's level
+      over ground) clear of the reference plane and of the delta gap; the
+      wave fit needs at least four.
+    - cuts: per window cut, the RWG edges on it and their signs
+      (Mesh.cut_edges): the current toward the circuit is
+      sum(sign * edge_len * x).
+    - excitation: a 1 V delta gap at the gap cut, i.e. the signed edge
+      lengths of the edges on that cut.
+    - vpts: where the line voltage is sampled, 8 points per window cut: at
+      -0.3, -0.1, 0.1 and 0.3 widths across the strip, on both sides of the
+      cut at half the distance to the nearer neighbouring grid cut (the two
+      sides average out the ripple of the alternating cell diagonals).
+    """
+
+    FRACTIONS = np.array([-0.3, -0.1, 0.1, 0.3])  # across the strip, in widths
 
     def __init__(self, mesh, port, h):
-        margin = port.margin if port.margin is not None else max(1.5 * port.width, 4 * h)
-        s = mesh.cut_positions(port)
-        s = s[(s >= margin - 1e-12) & (s <= port.s_gap - margin + 1e-12)]
-        if s.size < 4:
-            raise ValueError(f"port {port.name}: feed line too short or mesh too coarse "
-                             f"({s.size} sample cuts in the fitting window "
-                             f"[{margin * 1e3:.3g}, {(port.s_gap - margin) * 1e3:.3g}] mm)")
         self.port = port
+        keep = port.margin if port.margin is not None else max(1.5 * port.width, 4 * h)
+        grid_cuts = mesh.cut_positions(port)
+        s = grid_cuts[(grid_cuts >= keep - 1e-12) & (grid_cuts <= port.s_gap - keep + 1e-12)]
+        if s.size < 4:
+            raise ValueError(f"port {port.name}: the wave fit needs 4 grid cuts between {keep * 1e3:.3g} mm "
+                             f"and {(port.s_gap - keep) * 1e3:.3g} mm along the feed and found {s.size}; "
+                             "lengthen the feed or refine the mesh")
         self.s = s
         self.cuts = [mesh.cut_edges(port, si) for si in s]
-        idx, sgn = mesh.cut_edges(port, port.s_gap)
-        if idx.size == 0:
-            raise ValueError(f"port {port.name}: no mesh edges on the gap cut")
+        gap_edges, gap_sign = mesh.cut_edges(port, port.s_gap)
+        if gap_edges.size == 0:
+            raise ValueError(f"port {port.name}: no mesh edge lies on the delta-gap cut")
         self.excitation = np.zeros(mesh.n_unknowns)
-        self.excitation[idx] = sgn * mesh.edge_len[idx]
+        self.excitation[gap_edges] = gap_sign * mesh.edge_len[gap_edges]
         self.len = mesh.edge_len
-        allcuts = mesh.cut_positions(port)
-        k = np.searchsorted(allcuts, s)
-        lo = s - allcuts[np.maximum(k - 1, 0)]
-        hi = allcuts[np.minimum(k + 1, allcuts.size - 1)] - s
-        d = 0.5 * np.minimum(np.where(lo > 0, lo, np.inf), np.where(hi > 0, hi, np.inf))
-        frac = np.array([-0.3, -0.1, 0.1, 0.3])
-        along = np.stack([s - d, s + d], 1)
-        self.vpts = port.point(along[:, :, None], frac * port.width).reshape(-1, 2)
-        self.nper = 2 * frac.size
+        # distance to the nearer neighbouring grid cut (inf on a side that has none)
+        k = np.searchsorted(grid_cuts, s)
+        back = s - grid_cuts[np.maximum(k - 1, 0)]
+        ahead = grid_cuts[np.minimum(k + 1, grid_cuts.size - 1)] - s
+        half = 0.5 * np.minimum(np.where(back > 0, back, np.inf), np.where(ahead > 0, ahead, np.inf))
+        both_sides = np.stack([s - half, s + half], 1)  # (Ns, 2)
+        pts = port.point(both_sides[:, :, None], self.FRACTIONS * port.width)  # (Ns, 2, 4, 2)
+        self.vpts = pts.reshape(-1, 2)
+        self.nper = 2 * self.FRACTIONS.size
 
 
 @dataclass

@@ -47,7 +47,8 @@ def test_noalloc_solve_matches_dense_solve(gpu):
         A, B = system(n, 100 + call)
         # the existing entry point, host buffers
         Xref = np.zeros_like(B)
-        E.check(lib.m25_dense_solve(ctx.h, n, 2, E.M25_FP64, A.copy().ctypes.data, B.ctypes.data, Xref.ctypes.data,
+        Zref = A.copy()  # overwritten by its LU factors; held here until the call returns
+        E.check(lib.m25_dense_solve(ctx.h, n, 2, E.M25_FP64, Zref.ctypes.data, B.ctypes.data, Xref.ctypes.data,
                                     E.M25_ON_HOST, 0.0, 0, E.ptr(info, C.c_int32)))
         # the allocation-free entry point on caller-owned device buffers
         dZ = torch.from_numpy(A.copy()).cuda()
