@@ -15,9 +15,11 @@ the GPU (one engine context and stream each); timed with CUDA events around
 a device-wide synchronisation on both sides. e2e: the same through the
 public API (Solver construction + sweep(workers=...), host arrays in, S and
 the currents back on the host). Under torchrun each rank sweeps its
-own frequencies (weak scaling, no collective in the path). --impl
-reference times the CPU oracle (numpy restatement of mom25d's own path) on
-the host cores on a bounded sample of each point.
+own share of the frequencies (shard.partition; weak scaling, no collective
+in the path). --impl reference times the CPU oracle (numpy restatement of
+mom25d's own path) on full points: the fill's test blocks on one worker
+process per host core, LAPACK on all host threads (oracle/parallel.py), plus
+one point run as mom25d runs it (one process, 4 BLAS threads).
 """
 
 import argparse
@@ -117,7 +119,13 @@ def run_ours(args, rank, world, local):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     lay, st, mesh, freqs = build_workload(G)
     n = mesh.n_unknowns
-    my = [freqs[(rank * args.steps + i) % len(freqs)] for i in range(args.steps + args.warmup)]
+    # every rank sweeps its share of world * steps points (equal costs: the
+    # same mesh), after `warmup` untimed ones
+    from mom25d_gb300.shard import partition, point_cost
+
+    everything = [freqs[(args.warmup + i) % len(freqs)] for i in range(world * args.steps)]
+    mine = partition([point_cost(n)] * len(everything), world)[rank]
+    my = [freqs[i % len(freqs)] for i in range(args.warmup)] + [everything[i] for i in mine]
 
     def barrier():
         if world > 1:
@@ -219,19 +227,24 @@ def run_ours(args, rank, world, local):
     barrier()
     dt_e2e = time.perf_counter() - t0
     sol2.close()
-    # fp64 reference point of the engine itself (same kernels, fp64 fill + LU)
-    t64 = None
+    # the engine's fp64 path (fp64 fill + LU) on the same worker count over
+    # every 4th timed point: its points/s, and the largest |dS| of the mixed
+    # sweep above against it at those frequencies
+    t64 = max_dS = None
+    n64 = 0
     if args.precision != "fp64" and args.fp64_points > 0:
+        step = max(1, len(pts) // args.fp64_points)
+        idx = list(range(0, len(pts), step))[:args.fp64_points]
+        sub = [pts[i] for i in idx]
         s64 = Solver(mesh, st, verbose=False, precision="fp64", device=local)
-        s64.geometry()
-        s64.port_data()
-        s64.point(my[0])
+        s64.sweep(sub[:K], workers=K)  # the workers' contexts and buffers, untimed
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for f in my[1:1 + args.fp64_points]:
-            s64.point(f)
+        r64 = s64.sweep(sub, workers=K)
         torch.cuda.synchronize()
-        t64 = (time.perf_counter() - t0) / args.fp64_points
+        t64 = (time.perf_counter() - t0) / len(sub)
+        n64 = len(sub)
+        max_dS = float(np.abs(r.S[idx] - r64.S).max())
         s64.close()
     # max over ranks
     tt = torch.tensor([dt, dt_e2e], dtype=torch.float64, device="cuda")
@@ -288,93 +301,76 @@ def run_ours(args, rank, world, local):
                 "d2h_bytes_per_step": int(d2h)},
         "workers": K, "stages_ms_per_point_worker0": stages, "gpu_launches": int(launches),
         "fp64_ms_per_point": round(t64 * 1e3, 2) if t64 else None,
+        "fp64_points": n64,
         "speedup_vs_fp64": round(t64 / (dt / args.steps), 2) if t64 else None,
+        "max_dS_vs_fp64": max_dS,
         "roofline": roof, "clocks": clk.summary(), "geometry": geo,
         "refine_steps": r.info["refine_steps"][:4] if r.info else None,
     }
     if world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(samples=1)
+        out["cpu_baseline"] = cpu_baseline()
     return out
 
 
-def cpu_sample_point(sw, f, block_frac=0.2, lu_frac=1.0):
-    """Oracle time of one frequency point: Green's tables + fill of a fraction
-    of the test blocks (scaled to all of them) + LU and solve (lu_frac < 1:
-    of the leading lu_frac n rows and columns, scaled by lu_frac^-3) +
-    de-embedding."""
-    from oracle import sweep as O
-
-    t0 = time.perf_counter()
-    kern = sw.kernels(f)
-    t1 = time.perf_counter()
-    geo = sw.geom
-    nb = len(geo.blocks)
-    k = max(1, int(block_frac * nb))
-    full = geo.blocks
-    geo.blocks = full[:k]
-    try:
-        Z = O.fill(geo, kern, 2 * np.pi * f, sw.stack.surface_impedance(f))
-    finally:
-        geo.blocks = full
-    t2 = time.perf_counter()
-    Z = Z + np.eye(Z.shape[0]) * (1e-3 + np.abs(np.diag(Z)).max())  # partial fill: keep the LU well posed
-    B = sw.excitations()
-    ns = Z.shape[0] if lu_frac >= 1.0 else max(64, int(lu_frac * Z.shape[0]))
-    t25 = time.perf_counter()
-    xs = O.dense_solve(np.ascontiguousarray(Z[:ns, :ns]), B[:ns])
-    t3 = time.perf_counter()
-    x = np.zeros((Z.shape[0], B.shape[1]), complex)
-    x[:ns] = xs
-    lu_t = (t3 - t25) * (Z.shape[0] / ns) ** 3
-    t3b = time.perf_counter()
-    q = O.charges(sw.mesh, x, kern.omega)
-    try:
-        sw.deembed(f, kern, x, q)
-    except Exception:  # noqa: BLE001 - the partial Z gives a meaningless fit; its time still counts
-        pass
-    t4 = time.perf_counter()
-    return (t1 - t0) + (t2 - t1) * nb / k + (t25 - t2) + lu_t + (t4 - t3b)
-
-
-def cpu_baseline(samples=1):
+def cpu_baseline(points=2):
+    """The oracle's full LPF points on all host cores (oracle/parallel.py):
+    one untimed point, then `points` timed ones."""
     import mom25d_gb300 as G
-    from oracle import sweep as O
+    from oracle.parallel import ParallelPoint
 
     lay, st, mesh, freqs = build_workload(G)
-    sw = O.Sweep(mesh, st)
-    ts = [cpu_sample_point(sw, freqs[50 + i]) for i in range(samples)]
+    with ParallelPoint("lpf") as pp:
+        pp.point(freqs[49])
+        ts = [pp.point(freqs[50 + i])[1] for i in range(points)]
+        procs = pp.procs
     sec = float(np.mean(ts))
-    cores = os.cpu_count()
-    return {"value": round(1.0 / sec, 5), "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{samples} point(s) of the workload: Green's tables, LU and de-embedding in full, fill timed "
-                      "on 20% of the 130 test blocks and scaled; numpy/scipy with OpenBLAS on all host threads"}
+    return {"value": round(1.0 / sec, 5), "unit": UNIT, "cores": procs, "kind": "port",
+            "sample": f"{points} full point(s) of the workload after one untimed one (Green's tables, fill, LU + "
+                      f"solve, de-embedding; nothing scaled): the fill's test blocks on {procs} worker processes, "
+                      "LAPACK (OpenBLAS) on all host threads"}
+
+
+def serial_reference_point(f, blas_threads=4):
+    """Seconds of one oracle point run as mom25d runs it (the fill in one
+    Python process, LAPACK with mom25d's default of 4 OpenBLAS threads), in
+    a child process whose BLAS thread count is set before numpy loads."""
+    code = ("import sys, json; sys.path.insert(0, %r); from oracle.parallel import serial_point; "
+            "S, t = serial_point('lpf', %r); print(json.dumps(t))") % (HERE, float(f))
+    env = dict(os.environ, OPENBLAS_NUM_THREADS=str(blas_threads), OMP_NUM_THREADS=str(blas_threads))
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, check=True)
+    return float(out.stdout.strip().splitlines()[-1])
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return None
     import mom25d_gb300 as G
-    from oracle import sweep as O
+    from oracle.parallel import ParallelPoint
 
     lay, st, mesh, freqs = build_workload(G)
-    sw = O.Sweep(mesh, st)
-    # one untimed point warms the host code (numpy / LAPACK have no later
-    # warm-up effects); more would only lengthen the run by ~7 s each
-    for i in range(min(args.warmup, 1)):
-        cpu_sample_point(sw, freqs[i % len(freqs)], block_frac=0.05, lu_frac=0.5)
-    ts = [cpu_sample_point(sw, freqs[(args.warmup + i) % len(freqs)], block_frac=0.05, lu_frac=0.5)
-          for i in range(args.steps)]
+    with ParallelPoint("lpf") as pp:
+        for i in range(args.warmup):
+            pp.point(freqs[i % len(freqs)])
+        ts = [pp.point(freqs[(args.warmup + i) % len(freqs)])[1] for i in range(args.steps)]
+        procs = pp.procs
     sec = float(np.sum(ts))
     value = args.steps / sec
-    return {"metric": METRIC, "value": round(value, 5), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(sec / args.steps * 1e3, 1), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic", "impl": "reference",
-            "config": dict(WORKLOAD, precision="fp64 (numpy / scipy LAPACK)"),
-            "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                             "sample": "per step one frequency point: tables and de-embedding in full, fill on 5% "
-                                       "of the test blocks scaled to all, LU + solve of the leading n/2 block "
-                                       "scaled by 8 (LAPACK zgetrf time ~ n^3)"},
-            "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    out = {"metric": METRIC, "value": round(value, 5), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(sec / args.steps * 1e3, 1), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic", "impl": "reference",
+           "config": dict(WORKLOAD, precision="fp64 (numpy / scipy LAPACK)"),
+           "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": procs, "kind": "port",
+                            "sample": "every step one full frequency point (Green's tables, fill, LU + solve, "
+                                      f"de-embedding; nothing sampled or scaled): the fill's test blocks on {procs} "
+                                      "worker processes, LAPACK (OpenBLAS) on all host threads"},
+           "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if args.serial_points > 0:
+        # as mom25d runs by default: one process, 4 BLAS threads
+        tser = [serial_reference_point(freqs[(args.warmup + i) % len(freqs)]) for i in range(args.serial_points)]
+        out["as_shipped"] = {"s_per_point": round(float(np.mean(tser)), 2), "points": args.serial_points,
+                             "processes": 1, "blas_threads": 4,
+                             "note": "the oracle point as mom25d runs it: fill in one process, OpenBLAS 4 threads"}
+    return out
 
 
 def main():
@@ -384,10 +380,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=8)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--fp64-points", type=int, default=2)
+    ap.add_argument("--fp64-points", type=int, default=16,
+                    help="timed points also run on the fp64 path (same workers): its points/s and max |dS|")
     ap.add_argument("--workers", type=int, default=8, help="frequency points in flight on the GPU")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--refine-tol", type=float, default=None, help="mixed path: backward-error target of the refinement")
+    ap.add_argument("--serial-points", type=int, default=1,
+                    help="reference arm: points also timed as mom25d runs them (one process, 4 BLAS threads)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":

@@ -155,16 +155,15 @@ def via_block_L(vias, spans, z_section):
     return filament_mutual_z(p1, p2, q1, q2, rho) + filament_mutual_z(p1, p2, -q2, -q1, rho)
 
 
-def fill(geom, kern, omega, zs=0.0, zs_via=None):
-    """Galerkin MPIE impedance matrix (N x N complex128), symmetrised."""
-    nt, nb, nv = geom.nt, geom.nb, geom.nv
+def scatter_blocks(geom, kern, omega, blocks, Z, row_map=None, IVpad=None):
+    """Add the Galerkin sums of the given test blocks to Z (mom25d/
+    solver.py:429-509): row m of Z receives row_map[m] when row_map is given
+    (a partial Z holding only some rows), and IVpad the pad rows' scalar
+    potentials when the mesh has vias."""
+    b, cA, cV, V = geom.b, geom.cA, geom.cV, geom.V
     jwmu = 1j * omega * MU0
     inv_jwe = 1 / (1j * omega * EPS0)
-    Z = np.zeros((nb + nv, nb + nv), complex)
-    if nv:
-        IVpad = np.zeros((geom.pad_tris.size, nt), complex)
-    b, cA, cV, V = geom.b, geom.cA, geom.cV, geom.V
-    for lt, pb, r, groups in geom.blocks:
+    for lt, pb, r, groups in blocks:
         npb = pb.size
         rt = r.reshape(npb, 7, 2)
         wo = geom.w7[pb]
@@ -199,25 +198,49 @@ def fill(geom, kern, omega, zs=0.0, zs_via=None):
             rows = np.broadcast_to(b[pb][:, None, :, None], vals.shape)
             cols = np.broadcast_to(b[sel][None, :, None, :], vals.shape)
             ok = (rows >= 0) & (cols >= 0)
-            np.add.at(Z, (rows[ok], cols[ok]), vals[ok])
-            if nv:
+            rr = rows[ok] if row_map is None else row_map[rows[ok]]
+            np.add.at(Z, (rr, cols[ok]), vals[ok])
+            if IVpad is not None:
                 pos = geom.pad_pos[pb]
                 on = pos >= 0
                 if on.any():
                     IVpad[np.ix_(pos[on], sel)] = IV[on]
+
+
+def block_rows(geom, blocks):
+    """The RWG rows the test triangles of `blocks` touch (sorted)."""
+    b = np.concatenate([geom.b[pb].ravel() for _, pb, _, _ in blocks]) if blocks else np.zeros(0, int)
+    return np.unique(b[b >= 0])
+
+
+def finish_fill(geom, kern, omega, Z, zs=0.0, zs_via=None, IVpad=None):
+    """The parts of the fill after the block sums (mom25d/solver.py:
+    510-524): the surface-impedance term, the via rows and the
+    symmetrisation."""
+    b = geom.b
+    nb = geom.nb
     if np.any(zs):
         G = geom.gram
         ii = np.broadcast_to(b[:, :, None], G.shape)
         jj = np.broadcast_to(b[:, None, :], G.shape)
         ok = (ii >= 0) & (jj >= 0)
         np.add.at(Z, (ii[ok], jj[ok]), zs * G[ok])
-    if nv:
+    if geom.nv:
         zv = zs if zs_via is None else zs_via
         Zvb, Zvv = via_blocks(geom, kern, IVpad, omega, zv)
         Z[nb:, :nb] = Zvb
         Z[nb:, nb:] = Zvv
         Z[:nb, nb:] = Zvb.T
     return 0.5 * (Z + Z.T)
+
+
+def fill(geom, kern, omega, zs=0.0, zs_via=None):
+    """Galerkin MPIE impedance matrix (N x N complex128), symmetrised."""
+    nt, nb, nv = geom.nt, geom.nb, geom.nv
+    Z = np.zeros((nb + nv, nb + nv), complex)
+    IVpad = np.zeros((geom.pad_tris.size, nt), complex) if nv else None
+    scatter_blocks(geom, kern, omega, geom.blocks, Z, IVpad=IVpad)
+    return finish_fill(geom, kern, omega, Z, zs, zs_via, IVpad)
 
 
 def via_blocks(geom, kern, IVpad, omega, zs):
