@@ -71,6 +71,15 @@ int m25_ctx_synchronize(m25_ctx* ctx);
 int m25_ctx_mem_info(m25_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes);
 void* m25_ctx_stream(m25_ctx* ctx); /* the cudaStream_t every call of this context runs on */
 
+/* Failure-path hook (no counterpart in mom25d, whose solve has no waits):
+ * bound every ready-flag wait of this context's triangular solves to `polls`
+ * polls (0 restores the default bound, about a second of polling). A solve
+ * whose wait runs out returns M25_ERR_CUDA ("a wait of the triangular solve
+ * ran out") after every block of the kernel has returned; the context stays
+ * usable and its next solve starts with the error word cleared. Lets a test
+ * make a wait run out on purpose without any fault. */
+int m25_ctx_set_wait_limit(m25_ctx* ctx, int64_t polls);
+
 /* Stage timers: CUDA events recorded on the context's stream around the
  * kernels of each stage (the verbose green / fill / solve timers of
  * Engine/mom25d/solver.py:1023-1026, per kernel class). Copies the

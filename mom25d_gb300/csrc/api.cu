@@ -50,6 +50,7 @@ template <class TF, class TV>
 int lu_solve_wave(m25_ctx*, const cx<TF>*, int64_t, int, const int32_t*, const cx<TV>*, int, cx<TV>*,
                   const int32_t* perm = nullptr);
 int lu_wave_error(m25_ctx*, int, int*);
+int lu_wave_reset(m25_ctx*);
 
 // panel width of the complex64 LU: 64 columns keep the panel of up to ~7000
 // trailing rows in the shared memory of one 16-CTA cluster
@@ -130,6 +131,15 @@ extern "C" int m25_ctx_mem_info(m25_ctx* c, uint64_t* free_bytes, uint64_t* tota
   M25_CUDA(cudaMemGetInfo(&f, &t));
   if (free_bytes) *free_bytes = f;
   if (total_bytes) *total_bytes = t;
+  return M25_OK;
+}
+
+extern "C" int m25_ctx_set_wait_limit(m25_ctx* c, int64_t polls) {
+  if (!c || polls < 0) {
+    set_error("m25_ctx_set_wait_limit: null context or negative limit");
+    return M25_ERR_VALUE;
+  }
+  c->wave_spins = polls;
   return M25_OK;
 }
 
@@ -276,6 +286,7 @@ static int dense_solve_impl(m25_ctx* ctx, int32_t n, int32_t nrhs, int precision
   cudaStream_t st = ctx->stream;
   const size_t nn = (size_t)n * n, nr = (size_t)n * nrhs;
   int rc;
+  if ((rc = lu_wave_reset(ctx))) return rc;
   if ((rc = ctx->ipiv.ensure(sizeof(int32_t) * n))) return rc;
   if ((rc = ctx->Bw.ensure(sizeof(zd) * nr))) return rc;
   if ((rc = ctx->Xw.ensure(sizeof(zd) * nr))) return rc;
@@ -338,7 +349,16 @@ static int dense_solve_impl(m25_ctx* ctx, int32_t n, int32_t nrhs, int precision
       return M25_ERR_NUMERIC;
     }
     rc = refine(ctx, n, nrhs, Zh, Zl, n, LU, ldl, ctx->ipiv.as<int32_t>(), Bd, Xd, tol, max_iter, &steps);
-    if (rc) return rc;
+    if (rc) {
+      // a triangular solve that gave up leaves garbage that the refinement
+      // then reports as a numeric failure: name the wait instead
+      int werr = 0;
+      if (lu_wave_error(ctx, n, &werr) == M25_OK && werr) {
+        set_error("dense solve: a wait of the triangular solve ran out");
+        return M25_ERR_CUDA;
+      }
+      return rc;
+    }
   } else {
     set_error("m25_dense_solve: unknown precision");
     return M25_ERR_VALUE;

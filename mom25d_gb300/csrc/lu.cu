@@ -1153,6 +1153,7 @@ struct WaveArgs {
   int* flags;      // (nblk) == epoch once block k of X is final (complex128 vectors)
   int epoch;
   int* err;        // a wait ran out
+  long long spins; // polls per wait before it gives up
   // complex64 vectors: the solved values published with the sweep's epoch in
   // every 8-byte word, (epoch << 32) | bits of re, then the same for im, so
   // a reader can poll the data itself (aligned 8-byte accesses are single-copy
@@ -1370,7 +1371,7 @@ __global__ void __launch_bounds__(256, 1) trsv_wave_kernel(WaveArgs<TF, TV> a) {
               while (true) {
                 v = *g;
                 if ((unsigned)(v >> 32) == tag) break;
-                if (++it > kFlagSpinLimit || *(volatile int*)a.err) {
+                if (++it > a.spins || *(volatile int*)a.err) {
                   bad = true;
                   break;
                 }
@@ -1391,7 +1392,7 @@ __global__ void __launch_bounds__(256, 1) trsv_wave_kernel(WaveArgs<TF, TV> a) {
         if (tid == 0) {
           long long it = 0;
           while (*(volatile int*)&a.flags[j] != a.epoch) {
-            if (++it > kFlagSpinLimit || *(volatile int*)a.err) {
+            if (++it > a.spins || *(volatile int*)a.err) {
               atomicExch(a.err, 1);
               fail = 1;
               break;
@@ -1554,11 +1555,20 @@ int lu_solve_wave(m25_ctx* ctx, const cx<TF>* A, int64_t lda, int n, const int32
       if (Yt) M25_CUDA(cudaMemsetAsync(Yt, 0, sizeof(unsigned long long) * 2 * (size_t)n * 8, st));
       ctx->epoch = 1;
     }
-    WaveArgs<TF, TV> wa{A, lda, n, nrhs, upper, X, flags, ctx->epoch, err, Yt};
+    WaveArgs<TF, TV> wa{A, lda, n, nrhs, upper, X, flags, ctx->epoch, err,
+                        ctx->wave_spins > 0 ? ctx->wave_spins : kFlagSpinLimit, Yt};
     void* args[] = {&wa};
     M25_CUDA(cudaLaunchCooperativeKernel((void*)trsv_wave_kernel<TF, TV>, dim3(G), dim3(256), args, sm, st));
   }
   M25_CHECK_LAUNCH();
+  return M25_OK;
+}
+
+// clear the wait flag of the triangular solves before a solve: a solve whose
+// wait ran out left it set, and every later sweep would give up at once
+int lu_wave_reset(m25_ctx* ctx) {
+  if (ctx->ext_flags) return M25_OK;  // a caller-provided flag buffer is cleared by its owner
+  if (ctx->flags.p) M25_CUDA(cudaMemsetAsync(ctx->flags.p, 0, sizeof(int), ctx->stream));
   return M25_OK;
 }
 

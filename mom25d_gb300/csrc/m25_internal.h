@@ -62,6 +62,7 @@ struct m25_ctx {
   bool flags_fresh = true;  // the ready flags of the triangular solves need zeroing
   int epoch = 0;            // value of a ready flag in the current sweep
   size_t yt_off = 0;        // offset of the tagged vector copy in the flag buffer (0: not placed yet)
+  long long wave_spins = 0; // polls per ready-flag wait of the triangular solves (0: the default bound)
   // caller-provided scratch instead of the workspace buffers (LU panel
   // candidates + barrier words; triangular-solve flags, already zeroed)
   char* ext_scratch = nullptr;
