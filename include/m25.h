@@ -286,6 +286,13 @@ int m25_ports_destroy(m25_ports* p);
 int m25_deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* ports, const void* x, int where,
                 const double* beta0, double* S, double* z0, double* gamma, double* z0_line, double* resid);
 
+/* Per port group, the iterations of the last de-embedding's wave fit
+ * (Nelder-Mead, or for a lossless stack the bounded Brent search over beta);
+ * a lossless fit whose beta ended within 1e-3 |beta0| of its search bound
+ * reports minus its iterations: mom25d warns that gamma, Z0 and S are
+ * unreliable there (fit_waves, Engine/mom25d/solver.py:654-662). */
+int m25_deembed_fit_info(m25_ports* ports, int32_t* iters);
+
 /* One frequency point of Solver.sweep (Engine/mom25d/solver.py:1273-1325) with
  * every intermediate on the device: fill (precision), solve of the port
  * excitations, de-embedding. x_out (n, P) complex128 host copy of the

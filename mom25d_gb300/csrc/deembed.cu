@@ -251,7 +251,9 @@ struct FitArgs {
   zd* gamma;                // (P)
   zd* zline;                // (P)
   double* resid;            // (P)
-  int* iters;               // (ngroup) Nelder-Mead iterations
+  int* iters;               // (ngroup) iterations of the fit; lossless: minus them when beta ended at a bound
+  int lossless;             // 1: gamma = j beta, bounded Brent search over beta / |beta0|
+  double lo[kMaxPorts], hi[kMaxPorts];  // per group: the search interval of beta / |beta0|
   zd* S;                    // (P, P)
   double* z0;               // (P)
 };
@@ -374,6 +376,74 @@ __device__ double wave_objective(const FitArgs& a, int grp, zd g, double Inrm, d
   return res;
 }
 
+// Minimum of f on [lo, hi] by Brent's method (R. P. Brent, "Algorithms for
+// Minimization without Derivatives", 1973, ch. 5, procedure localmin):
+// golden-section steps, replaced by the minimum of the parabola through the
+// three best points whenever that falls inside the bracket and moves less
+// than half the step before last; never closer than tol to a point already
+// evaluated. tol = sqrt(eps) |x| + xatol / 3, the tolerance with which
+// mom25d's minimize_scalar(method="bounded", xatol=...) calls it; stops when
+// the bracket around the best point x is within 2 tol of it, or after
+// maxfun evaluations. *nfun = evaluations made.
+template <class F>
+__device__ double brent_minimize(F f, double lo, double hi, double xatol, int maxfun, int* nfun) {
+  const double cgold = 0.5 * (3.0 - sqrt(5.0));
+  const double reps = 1.4901161193847656e-08;  // sqrt(2^-52)
+  double a = lo, b = hi;
+  double x = a + cgold * (b - a), w = x, v = x;
+  double fx = f(x), fw = fx, fv = fx;
+  double d = 0.0, e = 0.0;
+  int n = 1;
+  while (n < maxfun) {
+    const double m = 0.5 * (a + b);
+    const double tol = reps * fabs(x) + xatol / 3.0, t2 = 2.0 * tol;
+    if (fabs(x - m) <= t2 - 0.5 * (b - a)) break;
+    bool golden = true;
+    if (fabs(e) > tol) {
+      // parabola through (x, fx), (w, fw), (v, fv): its vertex is x + p / q
+      double r = (x - w) * (fx - fv);
+      double q = (x - v) * (fx - fw);
+      double p = (x - v) * q - (x - w) * r;
+      q = 2.0 * (q - r);
+      if (q > 0.0) p = -p;
+      else q = -q;
+      const double e_prev = e;
+      e = d;
+      if (fabs(p) < fabs(0.5 * q * e_prev) && p > q * (a - x) && p < q * (b - x)) {
+        d = p / q;
+        const double u = x + d;
+        if (u - a < t2 || b - u < t2) d = x < m ? tol : -tol;  // not too near the ends
+        golden = false;
+      }
+    }
+    if (golden) {
+      e = (x < m ? b : a) - x;  // into the larger part of the bracket
+      d = cgold * e;
+    }
+    const double u = x + (fabs(d) >= tol ? d : (d > 0.0 ? tol : -tol));
+    const double fu = f(u);
+    ++n;
+    if (fu <= fx) {
+      if (u < x) b = x;
+      else a = x;
+      v = w; fv = fw;
+      w = x; fw = fx;
+      x = u; fx = fu;
+    } else {
+      if (u < x) a = u;
+      else b = u;
+      if (fu <= fw || w == x) {
+        v = w; fv = fw;
+        w = u; fw = fu;
+      } else if (fu <= fv || v == x || v == w) {
+        v = u; fv = fu;
+      }
+    }
+  }
+  *nfun = n;
+  return x;
+}
+
 // One CTA of four warps per port group: Nelder-Mead with scipy's
 // coefficients (reflection 1, expansion 2, contraction 0.5, shrink 0.5),
 // initial simplex 5 % steps, stopping when the simplex spans <= xatol and its
@@ -411,6 +481,27 @@ __global__ void __launch_bounds__(32 * kFitWarps) fit_kernel(FitArgs a) {
     }
     __syncthreads();
   };
+  if (a.lossless) {
+    // gamma = j beta (a bound mode: no attenuation to fit), beta = |beta0| b
+    // with b in [lo, hi] found by Brent's bounded minimisation (one objective
+    // evaluation per step, on warp 0)
+    if (warp != 0) return;
+    auto f = [&](double b) { return wave_objective(a, grp, zd(0.0, scale * b), Inrm, Vnrm, false); };
+    int n = 0;
+    const double b = brent_minimize(f, a.lo[grp], a.hi[grp], 1e-12, 500, &n);
+    const zd g(0.0, scale * b);
+    const double res = wave_objective(a, grp, g, Inrm, Vnrm, true);
+    if (lane == 0) {
+      const bool at_bound = fmin(b - a.lo[grp], a.hi[grp] - b) < 1e-3;
+      a.iters[grp] = at_bound ? -n : n;
+      for (int p = 0; p < a.P; ++p)
+        if (a.group_of[p] == grp) {
+          a.gamma[p] = g;
+          a.resid[p] = sqrt(res);
+        }
+    }
+    return;
+  }
   const double xatol = 1e-10, fatol = 1e-16;
   double sim[3][2], fs[3];
   // gamma0 = 1e-3 b0 + j b0, scaled by |b0|
@@ -600,6 +691,8 @@ struct m25_ports {
   double v_weight = 1.0;
   std::vector<int> group_of, ns, s_off, port_level, nvpt;
   std::vector<double> beta0;
+  std::vector<double> bounds;    // (ngroup, 2) lossless beta search intervals
+  std::vector<int> fit_iters;    // (ngroup) of the last de-embedding
   double* s = nullptr;
   int32_t* cut_off = nullptr;
   int32_t* cut_edge = nullptr;
@@ -625,10 +718,19 @@ extern "C" int m25_ports_create(m25_ctx* ctx, m25_geom* geom, const m25_port_des
     return M25_ERR_VALUE;
   }
   if (d->lossless) {
-    set_error("m25_ports_create: lossless stacks (bounded beta search) are not supported by this engine");
-    return M25_ERR_VALUE;
+    if (!d->bounds) {
+      set_error("m25_ports_create: a lossless stack needs the beta search bounds of every group");
+      return M25_ERR_VALUE;
+    }
+    for (int gi = 0; gi < d->ngroup; ++gi)
+      if (!(d->bounds[2 * gi] > 0.0 && d->bounds[2 * gi + 1] > d->bounds[2 * gi])) {
+        set_error("m25_ports_create: beta search bounds must satisfy 0 < lo < hi");
+        return M25_ERR_VALUE;
+      }
   }
   m25_ports* p = new m25_ports();
+  p->lossless = d->lossless ? 1 : 0;
+  if (p->lossless) p->bounds.assign(d->bounds, d->bounds + 2 * d->ngroup);
   p->ctx = ctx;
   p->P = d->nport;
   p->ngroup = d->ngroup;
@@ -812,11 +914,18 @@ static int deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, c
   fa.resid = reinterpret_cast<double*>(fa.zline + kMaxPorts);
   fa.z0 = fa.resid + kMaxPorts;
   fa.iters = p->iters;
+  fa.lossless = p->lossless;
+  for (int gi = 0; gi < p->ngroup; ++gi) {
+    fa.lo[gi] = p->lossless ? p->bounds[2 * gi] : 0.0;
+    fa.hi[gi] = p->lossless ? p->bounds[2 * gi + 1] : 0.0;
+  }
   fit_kernel<<<p->ngroup, 32 * kFitWarps, 0, st>>>(fa);
   fit_finish_kernel<<<1, 32, 0, st>>>(fa);
   M25_CHECK_LAUNCH();
   std::vector<zd> h(4 * kMaxPorts * kMaxPorts);
   M25_CUDA(cudaMemcpyAsync(h.data(), p->out, sizeof(zd) * h.size(), cudaMemcpyDeviceToHost, st));
+  p->fit_iters.assign(p->ngroup, 0);
+  M25_CUDA(cudaMemcpyAsync(p->fit_iters.data(), p->iters, sizeof(int) * p->ngroup, cudaMemcpyDeviceToHost, st));
   M25_CUDA(cudaStreamSynchronize(st));
   const zd* hS = h.data() + 2 * kMaxPorts * kMaxPorts;
   const zd* hg = h.data() + 3 * kMaxPorts * kMaxPorts;
@@ -836,6 +945,19 @@ static int deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, c
     if (resid) resid[i] = hr[i];
     if (z0) z0[i] = hz0[i];
   }
+  return M25_OK;
+}
+
+extern "C" int m25_deembed_fit_info(m25_ports* p, int32_t* iters) {
+  if (!p || !iters) {
+    set_error("m25_deembed_fit_info: null argument");
+    return M25_ERR_VALUE;
+  }
+  if (p->fit_iters.size() != (size_t)p->ngroup) {
+    set_error("m25_deembed_fit_info: no de-embedding yet");
+    return M25_ERR_VALUE;
+  }
+  for (int gi = 0; gi < p->ngroup; ++gi) iters[gi] = p->fit_iters[gi];
   return M25_OK;
 }
 

@@ -29,7 +29,8 @@ EXPORTS = ("m25_last_error", "m25_version", "m25_ctx_create", "m25_ctx_destroy",
            "m25_ctx_timing", "m25_dense_solve_noalloc", "m25_lu_factor", "m25_greens_remainder", "m25_mlp_create",
            "m25_mlp_destroy", "m25_mlp_params", "m25_mlp_loss_grad", "m25_mlp_train", "m25_mlp_forward",
            "m25_ctx_mem_info", "m25_interp_create", "m25_interp_destroy", "m25_interp_store", "m25_interp_eval",
-           "m25_interp_anchor", "m25_interp_point", "m25_deembed_waves", "m25_ctx_set_wait_limit")
+           "m25_interp_anchor", "m25_interp_point", "m25_deembed_waves", "m25_ctx_set_wait_limit",
+           "m25_deembed_fit_info")
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
@@ -98,6 +99,7 @@ def load():
                                     _f64p, _f64p, _f64p, _i32p]
     lib.m25_deembed_debug.argtypes = [vp, vp, _f64p, _f64p, _f64p, _f64p]
     lib.m25_deembed_waves.argtypes = [vp, _f64p]
+    lib.m25_deembed_fit_info.argtypes = [vp, _i32p]
     lib.m25_ctx_timing.argtypes = [vp, C.c_int, _f64p, C.POINTER(C.c_longlong)]
     lib.m25_dense_solve_noalloc.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, vp, vp, _i32p]
     lib.m25_lu_factor.argtypes = [vp, C.c_int32, C.c_int, vp, C.c_int64, _i32p, C.c_int, C.c_int32, _i32p]

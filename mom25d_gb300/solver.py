@@ -369,8 +369,6 @@ class Solver:
             key = (round(port.width / hp, 9), port.layer,
                    port.ground.key(hp) if port.ground is not None else None, port.z0_from)
             self.groups.setdefault(key, []).append(p)
-        if st.lossless:
-            raise ValueError("lossless stacks (bounded beta search) are not supported by this engine")
         self.device = device
         self.ctx = E.Context(device)
         self._geom = None
@@ -455,11 +453,16 @@ class Solver:
                     w=E.f64(cut_w), nvpt=E.i32([len(pm.vpts) for pm in self.pm]),
                     vpts=E.f64(np.concatenate([pm.vpts for pm in self.pm])),
                     exc=E.f64(np.stack([pm.excitation for pm in self.pm])))
+        # a lossless stack fits gamma = j beta, beta / |beta0| searched in
+        # (0.7, 1.3), or (0.7, 1.8) under a dielectric cover (solver.py:1290-1292)
+        lossless = bool(self.stack.lossless)
+        arrs["bounds"] = E.f64([(0.7, 1.8) if self.stack.covered(self.ports[mem[0]].layer) else (0.7, 1.3)
+                                for mem in groups])
         i = C.c_int32
         d = E.PortDesc(len(self.ports), len(groups), E.ptr(arrs["gid"], i), E.ptr(arrs["lev"], i),
                        E.ptr(arrs["ns"], i), E.ptr(arrs["s"]), E.ptr(arrs["off"], i), E.ptr(arrs["edge"], i),
-                       E.ptr(arrs["w"]), E.ptr(arrs["nvpt"], i), E.ptr(arrs["vpts"]), None, 0, None,
-                       self.v_weight, E.ptr(arrs["exc"]))
+                       E.ptr(arrs["w"]), E.ptr(arrs["nvpt"], i), E.ptr(arrs["vpts"]), None, int(lossless),
+                       E.ptr(arrs["bounds"]) if lossless else None, self.v_weight, E.ptr(arrs["exc"]))
         h = C.c_void_p()
         E.check(self.ctx.lib.m25_ports_create(self.ctx.h, self.geometry().h, C.byref(d), C.byref(h)))
         self._ports = E.Handle(self.ctx, h, self.ctx.lib.m25_ports_destroy)
@@ -571,6 +574,7 @@ class Solver:
         F = lambda a: E.ptr(a.view(np.float64))  # noqa: E731
         E.check(self.ctx.lib.m25_deembed(self.ctx.h, self.geometry().h, g.h, self.port_data().h, x.ctypes.data,
                                          E.M25_ON_HOST, E.ptr(b0), F(S), E.ptr(z0), F(gam), F(zl), E.ptr(res)))
+        self._warn_fit_bounds(f)
         S, z0 = self._fixed_z0(S, z0)
         return S, z0, gam, zl, res, (x if keep_currents else None), dict(
             refine_steps=steps, fp64_fallback=steps < 0, waves=self.last_waves())
@@ -600,11 +604,25 @@ class Solver:
             PRECISIONS[self.precision], E.ptr(b0), self.refine_tol, self.max_refine, F(x), F(S), E.ptr(z0), F(gam),
             F(zl), E.ptr(res), E.ptr(info, C.c_int32)))
         g.close()
+        self._warn_fit_bounds(f)
         S, z0 = self._fixed_z0(S, z0)
         # refine_steps -1: the mixed refinement did not reach refine_tol and
         # the point was recomputed on the fp64 path
         return S, z0, gam, zl, res, x, dict(refine_steps=int(info[0]), fp64_fallback=bool(info[0] < 0),
                                             waves=self.last_waves())
+
+    def _warn_fit_bounds(self, f):
+        """mom25d's warning when a lossless beta fit ends at its search bound
+        (Engine/mom25d/solver.py:658-661)."""
+        if not self.stack.lossless:
+            return
+        it = np.zeros(len(self.groups), np.int32)
+        E.check(self.ctx.lib.m25_deembed_fit_info(self.port_data().h, E.ptr(it, C.c_int32)))
+        if np.any(it < 0):
+            import warnings
+
+            warnings.warn(f"beta fit hit its search bound at {f / 1e9:.4g} GHz: gamma, Z0 and S at this frequency "
+                          "are unreliable", RuntimeWarning, stacklevel=3)
 
     def last_waves(self):
         """(P, P) incident current-wave amplitudes A [port, excitation] of the

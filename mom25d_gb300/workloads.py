@@ -13,6 +13,7 @@ returns (layout, stack, mesh keyword arguments, frequencies [Hz]).
   via        two-layer microstrip -> via -> inner line, 2 x 0.254 mm eps_r 3.66 (N = 3789)
   gcpw       30 mm grounded CPW with via fences on 0.508 mm eps_r 3.55, 64 f 1-20 GHz
   line       short through line (small N, test case)
+  line_lossless  the same line on a lossless substrate (the lossless wave fit)
   shunt_via  short line with a via to ground (small N, test case)
   lumped_line  two line sections joined by a lumped component (R 20 + L 0.5n) across a gap
   component_line  three line sections, a 2-port S-parameter block across two open gaps
@@ -122,6 +123,14 @@ def line(api, length=4 * mm, cell=0.5 * mm):
     return lay, sub, dict(max_cell=cell, edge_cell=0.15 * mm), np.array([2.0, 7.0]) * GHz
 
 
+def line_lossless(api):
+    """The through line on a lossless substrate (tan d = 0, ideal
+    conductors): the wave fit takes mom25d's lossless branch (gamma = j beta
+    by a bounded scalar search)."""
+    lay, _, mkw, freqs = line(api)
+    return lay, api.Substrate(eps_r=ER, h=H), mkw, freqs
+
+
 def shunt_via(api):
     W = 0.5561 * mm
     lay = api.Layout()
@@ -165,7 +174,8 @@ def component_line(api, block=None):
     return lay, sub, dict(max_cell=0.5 * mm, edge_cell=0.15 * mm), np.array([2.0, 5.0, 9.0]) * GHz
 
 
-BUILDERS = dict(tee=tee, lpf=lpf, bandpass=bandpass, via=via, gcpw=gcpw, line=line, shunt_via=shunt_via,
+BUILDERS = dict(tee=tee, lpf=lpf, bandpass=bandpass, via=via, gcpw=gcpw, line=line, line_lossless=line_lossless,
+                shunt_via=shunt_via,
                 lumped_line=lumped_line, component_line=component_line)
 
 

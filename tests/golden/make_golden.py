@@ -362,6 +362,7 @@ def main():
     ap.add_argument("--lumped", action="store_true", help="only the lumped-component fixture")
     ap.add_argument("--floor", action="store_true", help="only the wave-fit floor fixture")
     ap.add_argument("--variants", action="store_true", help="only band-pass variants 3, 7, 11 and 14")
+    ap.add_argument("--lossless", action="store_true", help="only the lossless line (mom25d's bounded beta fit)")
     ap.add_argument("--gcpw", action="store_true",
                     help="only the grounded CPW (N = 25284: ~30 GB of memory, ~20 min per frequency)")
     args = ap.parse_args()
@@ -381,6 +382,9 @@ def main():
         floor_all()
         return
     fb = np.linspace(1, 12, 128) * 1e9
+    if args.lossless:
+        case("line_lossless", zrows=np.arange(0, 546, 37), sweep_freqs=[2e9, 5e9, 7e9])
+        return
     if args.variants:
         for k in (3, 7, 11, 14):
             n = workloads.BANDPASS_N[k]
@@ -394,6 +398,7 @@ def main():
     kernels()
     case("line", zrows=np.arange(0, 546, 37))
     case("shunt_via", zrows=np.arange(0, 492, 41))
+    case("line_lossless", zrows=np.arange(0, 546, 37), sweep_freqs=[2e9, 5e9, 7e9])
     if args.quick:
         return
     case("tee", zrows=np.arange(0, 1085, 97))

@@ -26,11 +26,18 @@ def mesh_digest(m):
     return h.hexdigest()
 
 
-@pytest.mark.parametrize("name", ["line", "shunt_via", "tee", "via", "lpf", "bandpass_0"])
+@pytest.mark.parametrize("name", ["line", "line_lossless", "shunt_via", "tee", "via", "lpf", "bandpass_0",
+                                  "bandpass_3", "bandpass_7", "bandpass_11", "bandpass_14", "gcpw"])
 def test_mesh_identical_to_reference(name):
+    import os
+
+    from conftest import GOLDEN
+
+    if not os.path.exists(os.path.join(GOLDEN, name + ".npz")):
+        pytest.skip(f"no fixture {name}")
     g = golden(name)
-    base = name.split("_")[0] if name.startswith("bandpass") else name
-    kw = {"k": 0} if name.startswith("bandpass") else {}
+    base = "bandpass" if name.startswith("bandpass") else name
+    kw = {"k": int(name.split("_")[1])} if name.startswith("bandpass") else {}
     lay, st, m, _ = workloads.build(G, base, **kw)
     stack = st if hasattr(st, "layers") else st.to_stackup()
     m.assign_levels(sorted(m.layer_names, key=stack.level_z))
@@ -147,3 +154,19 @@ def test_oracle_fill_and_sweep_match_reference(name):
     # perturbations of its inputs: S agrees to that floor, not to 1e-9
     assert np.abs(S - g["S"]).max() < 1e-6
     assert np.abs(gam - g["gamma"]).max() < 1e-6 * np.abs(g["gamma"]).max()
+
+
+def test_oracle_lossless_sweep_matches_reference():
+    """A lossless substrate takes mom25d's bounded search over beta
+    (gamma = j beta, Engine/mom25d/solver.py:654-662): the oracle's sweep
+    gives mom25d's gamma (purely imaginary) and S (lossless line)."""
+    from conftest import fp64_tol
+
+    g = golden("line_lossless")
+    lay, st, m, _ = workloads.build(G, "line_lossless")
+    assert mesh_digest(m) == str(g["mesh_sha"])
+    sw = O.Sweep(m, st)
+    S, z0, gam, zl, res = sw.sweep(g["freqs"])
+    assert np.all(gam.real == 0) and np.all(g["gamma"].real == 0)
+    assert np.abs(gam - g["gamma"]).max() < 1e-9 * np.abs(g["gamma"]).max()
+    assert np.abs(S - g["S"]).max() < fp64_tol("line_lossless")

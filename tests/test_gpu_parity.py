@@ -1,0 +1,131 @@
+"""Parity of every stage of the sweep point against fixtures made by running
+mom25d itself (tests/golden, make_golden.py), on every workload that has one.
+
+Bars:
+- before the wave fit (currents x, charges q, line voltages phi, cut
+  currents I and cut voltages V): 1e-9 relative to the largest entry, fp64
+  path. x is limited by the conditioning of Z: mom25d's own currents move by
+  ~2e-10 relative when its LAPACK runs on another number of threads;
+- S of the fp64 path: three times the floor of mom25d's own wave fit
+  (conftest.fit_floor: 8e-9 to 6e-8 by workload);
+- S of the mixed path: 1e-5.
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+import mom25d_gb300 as G
+from mom25d_gb300 import workloads
+from mom25d_gb300.solver import Solver
+
+from conftest import GOLDEN, fp64_tol, golden
+
+pytestmark = pytest.mark.gpu
+
+STAGE_TOL = 1e-9
+
+
+def _have(name):
+    return os.path.exists(os.path.join(GOLDEN, name + ".npz"))
+
+
+def _build(name):
+    if name.startswith("bandpass_"):
+        return workloads.build(G, "bandpass", k=int(name.split("_")[1]))
+    return workloads.build(G, name)
+
+
+VARIANTS = [f"bandpass_{k}" for k in (0, 3, 7, 11, 14)]
+STAGE_CASES = ["line", "shunt_via", "tee", "via", "lpf"] + VARIANTS
+
+
+@pytest.mark.parametrize("name", STAGE_CASES)
+def test_prefit_stages_match_reference(gpu, name):
+    """x, q, phi, I, V of the fp64 point at the fixture's first frequency."""
+    if not _have(name):
+        pytest.skip(f"no fixture {name}")
+    g = golden(name)
+    if "phi" not in g.files:
+        pytest.skip(f"fixture {name} predates the stage arrays")
+    lay, st, m, _ = _build(name)
+    sol = Solver(m, st, verbose=False, precision="fp64")
+    try:
+        out = sol.point(float(g["f0"]), keep_currents=True)
+        x = out[5]
+        q, phi, I, V = sol.last_deembed()
+        errs = {}
+        for key, got in (("x", x), ("q", q), ("phi", phi), ("I", I), ("V", V)):
+            ref = g[key]
+            assert got.shape == ref.shape, (key, got.shape, ref.shape)
+            errs[key] = np.abs(got - ref).max() / np.abs(ref).max()
+        print(name, {k: f"{v:.1e}" for k, v in errs.items()})
+        assert max(errs.values()) <= STAGE_TOL, errs
+    finally:
+        sol.close()
+
+
+@pytest.mark.parametrize("name", VARIANTS)
+def test_bandpass_variant_sweeps_match_reference(gpu, name):
+    """Coupled-line band-pass variants of N 1524 to 4972: fp64 within three
+    fit floors, mixed within 1e-5, at the fixture's frequencies."""
+    if not _have(name):
+        pytest.skip(f"no fixture {name}")
+    g = golden(name)
+    lay, st, m, _ = _build(name)
+    assert m.n_unknowns == g["N"]
+    for prec, tol in (("fp64", fp64_tol(name)), ("mixed", 1e-5)):
+        sol = Solver(m, st, verbose=False, precision=prec)
+        try:
+            r = sol.sweep(g["freqs"], workers=2)
+            dS = np.abs(r.S - g["S"]).max()
+            print(name, prec, f"max |dS| {dS:.2e}")
+            assert dS < tol, (prec, dS)
+        finally:
+            sol.close()
+
+
+def test_gcpw_large_workload_matches_reference(gpu):
+    """The via-fenced grounded CPW, N = 25284 with 84 vias (the largest
+    workload). Mixed precision: at 10.35 GHz the complex64 LU + refinement
+    within 1e-5; at 1 GHz the refinement stalls (cond(Z) u32 > 1) and the
+    point falls back to the fp64 fill and LU, which must then meet the fp64
+    bar."""
+    if not _have("gcpw"):
+        pytest.skip("no fixture gcpw")
+    g = golden("gcpw")
+    lay, st, m, _ = _build("gcpw")
+    assert m.n_unknowns == g["N"]
+    sol = Solver(m, st, verbose=False, precision="mixed")
+    try:
+        r = sol.sweep(g["freqs"])
+        dS = np.abs(r.S - g["S"]).max(axis=(1, 2))
+        print("gcpw max |dS| per frequency", dS, r.info)
+        fb = set(r.info["fp64_fallback"])
+        for i, f in enumerate(g["freqs"]):
+            assert dS[i] < (fp64_tol("gcpw") if float(f) in fb else 1e-5), (f, dS[i])
+    finally:
+        sol.close()
+
+
+def test_gcpw_prefit_stages_match_reference(gpu):
+    """x, q, phi, I, V of the fp64 point at 1 GHz on the N = 25284 mesh."""
+    if not _have("gcpw"):
+        pytest.skip("no fixture gcpw")
+    g = golden("gcpw")
+    lay, st, m, _ = _build("gcpw")
+    sol = Solver(m, st, verbose=False, precision="fp64")
+    try:
+        x = sol.point(float(g["f0"]), keep_currents=True)[5]
+        q, phi, I, V = sol.last_deembed()
+        errs = {k: np.abs(got - g[k]).max() / np.abs(g[k]).max()
+                for k, got in (("x", x), ("q", q), ("phi", phi), ("I", I), ("V", V))}
+        print("gcpw", {k: f"{v:.1e}" for k, v in errs.items()})
+        assert max(errs.values()) <= STAGE_TOL, errs
+        Z = sol.impedance(float(g["f0"]))
+        rows = g["Z_rows_idx"]
+        assert np.abs(Z[rows] - g["Z_rows"]).max() <= 1e-11 * np.abs(g["Z_rows"]).max()
+        assert np.abs(np.diag(Z) - g["Z_diag"]).max() <= 1e-11 * np.abs(g["Z_diag"]).max()
+    finally:
+        sol.close()
