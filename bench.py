@@ -100,6 +100,33 @@ def build_workload(api):
     return workloads.build(api, "lpf")
 
 
+def update_flops(n):
+    """Algorithmic real flops of the tensor-core updates of one complex64 LU
+    of order n in super-blocks of 256 columns (mom25d_gb300/csrc/lu.cu): per
+    super-block at k0 (width SW = min(256, n - k0), blocks a = min(128, SW)
+    and b = SW - a) each block's rank-64 update of its second panel's
+    columns, block a's rank-128 update of block b's columns, L_ba U_a on
+    block b's rows of the trailing columns and the rank-256 update of the
+    trailing matrix; 8 real flops per complex multiply-add. The sum is the
+    update work of any right-looking complex LU (about 8/3 n^3)."""
+    tot = 0.0
+    for k0 in range(0, n, 256):
+        SW = min(256, n - k0)
+        wa = min(128, SW)
+        wb = SW - wa
+        for c0, W in ((k0, wa), (k0 + wa, wb)):
+            w1 = min(64, W)
+            tot += 8.0 * (n - c0 - w1) * (W - w1) * w1
+        ra = k0 + wa
+        if ra >= n:
+            break
+        tot += 8.0 * (n - ra) * wb * wa
+        nt = n - k0 - SW
+        if nt > 0:
+            tot += 8.0 * wb * nt * wa + 8.0 * nt * nt * SW
+    return tot
+
+
 def lu_flops(n, nrhs=2):
     """Complex LU (8/3 n^3 real flops) + the two triangular solves (8 n^2 nrhs)."""
     return 8.0 / 3.0 * n ** 3 + 8.0 * n * n * nrhs
@@ -265,12 +292,7 @@ def run_ours(args, rank, world, local):
     except OSError:
         pass
     lu_ms = iso_ms["lu_gemm"]  # per point: the update kernels of one LU, GPU to themselves
-    # algorithmic work of the updates (complex multiply-add = 8 real flops):
-    # per block of 128 columns the rank-64 update of the second panel's 64
-    # columns (m1 = n - k0 - 64 rows) and the rank-128 update of the m2 x m2
-    # trailing matrix (m2 = n - k0 - 128)
-    gemm_flops = float(sum(8.0 * (n - k0 - 64) * min(64, n - k0 - 64) * 64 + 8.0 * max(n - k0 - 128, 0) ** 2 * 128
-                           for k0 in range(0, n - 64, 128)))
+    gemm_flops = update_flops(n)
     achieved = gemm_flops / (lu_ms * 1e-3) / 1e12 if lu_ms else None
     bf16 = peaks.get("bf16_tflops") or 1900.0  # burst: the kernel is timed alone
     # DRAM traffic of the updates per flop, from the ncu capture of all 63

@@ -612,10 +612,15 @@ __device__ __forceinline__ void load_l_block(cx<T>* Lb, const cx<T>* A, int64_t 
   }
 }
 
+// ipiv null: no interchanges (the rows are in place already); solve false:
+// the interchanges alone, no U12 (and no B2). B2 rows are 2 P floats long
+// ([hi | lo] planes of width P); this call writes K positions koff ..
+// koff + 2 W - 1 of each plane.
 template <class T, int W = kSwapMaxW>
 __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, int n, int k0, int w,
                                                         const int32_t* __restrict__ ipiv, float* __restrict__ B2,
-                                                        int P, int vc_begin, int vc_end) {
+                                                        int P, int vc_begin, int vc_end, int koff = 0,
+                                                        bool solve = true) {
   static_assert(W == 64 || W == 128, "panel blocks of 64 or 128 columns");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // L11 in 64 x 64 blocks, transposed: for W = 128 first [L11 of rows and
@@ -634,7 +639,7 @@ __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, i
 #pragma unroll
     for (int h = 0; h < W / 32; ++h) {
       const int j = lane + 32 * h;
-      pr[h] = j < w ? ipiv[k0 + j] : -1;
+      pr[h] = j < w ? (ipiv ? ipiv[k0 + j] : k0 + j) : -1;
       piv[j] = pr[h];
     }
     // positions touched: the panel rows, then each pivot row below the panel once
@@ -673,7 +678,7 @@ __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, i
     if (lane == 0) nd_s = nd;
   }
   // the CTA's columns vc0 .. vc0 + 31 map to vc (< k0) or vc + w (right of the panel)
-  const bool any_right = kend < n && min(vc0 + 31, vc_end - 1) >= k0;
+  const bool any_right = solve && kend < n && min(vc0 + 31, vc_end - 1) >= k0;
   if (any_right) {
     load_l_block(Ls, A, lda, k0, w, 0, 0);
     if (W == 128) load_l_block(Ls1, A, lda, k0, w, 64, 0);
@@ -683,7 +688,7 @@ __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, i
   const int vc = vc0 + lane;
   const bool valid = vc < vc_end;
   const int c = vc < k0 ? vc : vc + w;
-  const bool right = c >= kend;
+  const bool right = solve && c >= kend;
   {
     // warp q gathers rows q, q + 8, ...; every row of the CTA's columns is
     // read before any is written (the barrier), as rows move between warps
@@ -771,7 +776,7 @@ __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, i
       const int vcl = vc0 + cl;
       if (vcl >= vc_end || vcl < k0) continue;  // not a trailing column
       const int cc = vcl - k0;                  // = (vcl + w) - kend
-      for (int jj = lane; jj < P; jj += 32) {
+      for (int jj = lane; jj < 2 * W; jj += 32) {
       const int t = jj >> 1, f = jj & 1;
       float hi = 0.f, lo = 0.f;
       if (t < w) {
@@ -780,8 +785,8 @@ __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, i
         hi = tf32_rna(v);
         lo = tf32_rna(v - hi);
       }
-      B2[(int64_t)(2 * cc + part) * 2 * P + jj] = hi;
-      B2[(int64_t)(2 * cc + part) * 2 * P + P + jj] = lo;
+      B2[(int64_t)(2 * cc + part) * 2 * P + koff + jj] = hi;
+      B2[(int64_t)(2 * cc + part) * 2 * P + P + koff + jj] = lo;
       }
     }
   }
@@ -867,9 +872,10 @@ __global__ void gather_rows_kernel(int n, int nrhs, const int32_t* __restrict__ 
 // lu_tc.cu
 int lu_tc_prepare(m25_ctx* ctx, int n);
 int lu_tc_buffers(m25_ctx* ctx, int n, float** A3, float** B3, float** Ai, float** Bi);
-int lu_tc_pack_a(m25_ctx* ctx, const zf* A, int64_t lda, int k0, int w, int m, int P, float* A3);
-int lu_tc_update(m25_ctx* ctx, zf* A, int64_t lda, int r0, int m, int nc, int P, const float* A3, const float* B3,
-                 int slot);
+int lu_tc_pack_a(m25_ctx* ctx, const zf* A, int64_t lda, int k0, int w, int row0, int m, int P, int pw, int koff,
+                 float* A3);
+int lu_tc_update(m25_ctx* ctx, zf* A, int64_t lda, int r0, int c0, int m, int nc, int P, int pw, const float* A3,
+                 const float* B3, int slot);
 int lu_tc_error(m25_ctx* ctx, int* flag);
 bool lu_tc_available();
 
@@ -1063,7 +1069,19 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
     if (vc_end <= vc_begin) return M25_OK;
     StageTimer tm(ctx, ST_TRSM);
     swap_trsm_kernel<T><<<(vc_end - vc_begin + 31) / 32, 256, swap_trsm_smem<T>(), st>>>(A, lda, n, k0, w, ipiv, B2,
-                                                                                         P2, vc_begin, vc_end);
+                                                                                         P2, vc_begin, vc_end, 0, true);
+    M25_CHECK_LAUNCH();
+    return M25_OK;
+  };
+  // the same for a block of w <= 128 columns (two panels' interchanges and a
+  // 128-row L11 at once): piv null skips the interchanges, solve false skips
+  // U12; B planes of width P at K offset koff
+  auto swap_trsm128 = [&](int k0, int w, int vc_begin, int vc_end, float* B2, int P, int koff, const int32_t* piv,
+                          bool solve) -> int {
+    if (vc_end <= vc_begin) return M25_OK;
+    StageTimer tm(ctx, ST_TRSM);
+    swap_trsm_kernel<T, 128><<<(vc_end - vc_begin + 31) / 32, 256, swap_trsm_smem<T, 128>(), st>>>(
+        A, lda, n, k0, w, piv, B2, P, vc_begin, vc_end, koff, solve);
     M25_CHECK_LAUNCH();
     return M25_OK;
   };
@@ -1083,43 +1101,60 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
       }
     }
   } else if constexpr (std::is_same<T, float>::value) {
-    // blocks of 128 columns, each factored as two panels of 64: the second
-    // panel's columns get the first panel's rank-64 update, and the trailing
-    // matrix one rank-128 update per block (its read-modify-write of C, the
-    // bound of the update, once per 128 columns instead of once per 64)
+    // super-blocks of 256 columns: two blocks a, b of 128, each factored as
+    // two panels of 64 (the first panel's rank-64 update of the second's
+    // columns). Block a's interchanges and U_a = L_aa^-1 A_a go to every
+    // column right of it, its rank-128 update only to block b's columns;
+    // block b is factored; on the trailing columns then block b's
+    // interchanges, its rows minus L_ba U_a, U_b = L_bb^-1 of those rows, and
+    // one rank-256 update of the trailing matrix: its read-modify-write of C,
+    // the bound of the update, once per 256 columns. B3 holds U_a at K
+    // 0..255 and U_b at K 256..511 of planes 512 floats wide, for the columns
+    // from the first right of block a (block b's, then the trailing ones).
     float *A3, *B3, *Ai, *Bi;
     if ((rc = lu_tc_buffers(ctx, n, &A3, &B3, &Ai, &Bi))) return rc;
-    constexpr int kHalf = kSwapMaxW, kBlock = 2 * kSwapMaxW;
-    for (int k0 = 0, blk = 0; k0 < n; k0 += kBlock, ++blk) {
-      const int W = std::min(kBlock, n - k0), w1 = std::min(kHalf, W), w2 = W - w1;
+    constexpr int kHalf = kSwapMaxW, kBlock = 2 * kSwapMaxW, kSuper = 2 * kBlock, kPW = 2 * kSuper;
+    int slot = 0;
+    // one block of W <= 128 columns at c0: both panels, the first one's U12
+    // and rank-64 update on the second one's columns, each panel's
+    // interchanges on every column left of it (none on columns right of the block)
+    auto factor_block = [&](int c0, int W) -> int {
+      const int w1 = std::min(kHalf, W), w2 = W - w1;
       bool packed = false;
-      if ((rc = run_panel(k0, w1, w2 > 0 ? Ai : nullptr, 128, &packed))) return rc;
-      if (w2 > 0) {
-        // the first panel's interchanges on the columns left of the block and
-        // with U12 on the second panel's; that panel's rank-64 update
-        if ((rc = swap_trsm(k0, w1, 0, k0 + w2, Bi, 128))) return rc;
-        const int m1 = n - k0 - w1;
-        if (!packed && (rc = lu_tc_pack_a(ctx, A, lda, k0, w1, m1, 128, Ai))) return rc;
-        if ((rc = lu_tc_update(ctx, A, lda, k0 + w1, m1, w2, 128, Ai, Bi, 2 * blk))) return rc;
-        if ((rc = run_panel(k0 + w1, w2, nullptr, 0, nullptr))) return rc;
-        // the second panel's interchanges on every column left of it
-        if ((rc = swap_trsm(k0 + w1, w2, 0, k0 + w1, nullptr, 0))) return rc;
-      } else if ((rc = swap_trsm(k0, w1, 0, k0, nullptr, 0))) {
-        return rc;
-      }
-      if (k0 + W < n) {
-        // both panels' interchanges and U12 = L11^-1 A12 (128 rows) on the
-        // trailing columns, then the rank-128 update
-        const int m2 = n - k0 - W;
-        {
-          StageTimer tm(ctx, ST_TRSM);
-          swap_trsm_kernel<T, 128><<<(m2 + 31) / 32, 256, swap_trsm_smem<T, 128>(), st>>>(A, lda, n, k0, W, ipiv, B3,
-                                                                                          256, k0, n - W);
-          M25_CHECK_LAUNCH();
-        }
-        if ((rc = lu_tc_pack_a(ctx, A, lda, k0, W, m2, 256, A3))) return rc;
-        if ((rc = lu_tc_update(ctx, A, lda, k0 + W, m2, m2, 256, A3, B3, 2 * blk + 1))) return rc;
-      }
+      int r;
+      if ((r = run_panel(c0, w1, w2 > 0 ? Ai : nullptr, 128, &packed))) return r;
+      if (w2 == 0) return swap_trsm(c0, w1, 0, c0, nullptr, 0);
+      if ((r = swap_trsm(c0, w1, 0, c0 + w2, Bi, 128))) return r;
+      const int m1 = n - c0 - w1;
+      if (!packed && (r = lu_tc_pack_a(ctx, A, lda, c0, w1, c0 + w1, m1, 128, 128, 0, Ai))) return r;
+      if ((r = lu_tc_update(ctx, A, lda, c0 + w1, c0 + w1, m1, w2, 128, 128, Ai, Bi, slot++))) return r;
+      if ((r = run_panel(c0 + w1, w2, nullptr, 0, nullptr))) return r;
+      return swap_trsm(c0 + w1, w2, 0, c0 + w1, nullptr, 0);
+    };
+    for (int k0 = 0; k0 < n; k0 += kSuper) {
+      const int SW = std::min(kSuper, n - k0), wa = std::min(kBlock, SW), wb = SW - wa;
+      if ((rc = factor_block(k0, wa))) return rc;
+      const int ra = k0 + wa;  // first column (and row) right of block a
+      if (ra >= n) break;      // (then wb = 0)
+      // block a's interchanges and U_a on every column right of it
+      if ((rc = swap_trsm128(k0, wa, k0, n - wa, B3, kPW, 0, ipiv, true))) return rc;
+      // block a's rank-128 update of block b's columns
+      if ((rc = lu_tc_pack_a(ctx, A, lda, k0, wa, ra, n - ra, 2 * kBlock, kPW, 0, A3))) return rc;
+      if ((rc = lu_tc_update(ctx, A, lda, ra, ra, n - ra, wb, 2 * kBlock, kPW, A3, B3, slot++))) return rc;
+      if ((rc = factor_block(ra, wb))) return rc;
+      const int t0 = k0 + SW, nt = n - t0;  // the trailing columns
+      if (nt <= 0) continue;
+      float* Bt = B3 + (size_t)2 * wb * 2 * kPW;  // B rows of the trailing columns
+      // block b's interchanges on the trailing columns
+      if ((rc = swap_trsm128(ra, wb, ra, ra + nt, nullptr, 0, 0, ipiv, false))) return rc;
+      // block b's rows of the trailing columns minus L_ba U_a
+      if ((rc = lu_tc_pack_a(ctx, A, lda, k0, wa, ra, wb, 2 * kBlock, kPW, 0, A3))) return rc;
+      if ((rc = lu_tc_update(ctx, A, lda, ra, t0, wb, nt, 2 * kBlock, kPW, A3, Bt, slot++))) return rc;
+      // U_b = L_bb^-1 of those rows, its B planes at K 256..511
+      if ((rc = swap_trsm128(ra, wb, ra, ra + nt, Bt, kPW, 2 * kBlock, nullptr, true))) return rc;
+      // the rank-256 update of the trailing matrix
+      if ((rc = lu_tc_pack_a(ctx, A, lda, k0, SW, t0, nt, kPW, kPW, 0, A3))) return rc;
+      if ((rc = lu_tc_update(ctx, A, lda, t0, t0, nt, nt, kPW, kPW, A3, Bt, slot++))) return rc;
     }
   }
   int hflags[3];

@@ -135,7 +135,8 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 }
 
 struct TcArgs {
-  int M, N, P;     // rows, real columns of C (its fp32 view), plane width of the packed K (multiple of 32)
+  int M, N, P;     // rows, real columns of C (its fp32 view), packed K extent per plane (multiple of 32)
+  int pw;          // plane width: the lo plane starts pw floats after the hi plane (pw >= P)
   int tiles_m, ntiles;
   int chunk;       // k-blocks accumulated afresh in TMEM before the register sum
   int* err;
@@ -226,8 +227,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           unsigned char* sa = base + s * kStageBytes;
           mbar_expect_tx(&full[s], kStageBytes);
-          tma_load_2d(sa + kTileA, &tmA, a.P + kb * kBK, m0, &full[s]);
-          tma_load_2d(sa + 2 * kTileA + kTileB, &tmB, a.P + kb * kBK, n0, &full[s]);
+          tma_load_2d(sa + kTileA, &tmA, a.pw + kb * kBK, m0, &full[s]);
+          tma_load_2d(sa + 2 * kTileA + kTileB, &tmB, a.pw + kb * kBK, n0, &full[s]);
           tma_load_2d(sa, &tmA, kb * kBK, m0, &full[s]);
           tma_load_2d(sa + 2 * kTileA, &tmB, kb * kBK, n0, &full[s]);
           n_issued = it + 1;
@@ -308,20 +309,23 @@ __global__ void __launch_bounds__(kThreads, 1)
         ok = __all_sync(0xffffffffu, mbar_wait(&tfull[b], (ch >> 1) & 1, abort_v));
         if (!ok) break;
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        // two batches of three 16-column loads, each batch waited for once (in
+        // the same asm statement, so no use of r can move above the wait)
 #pragma unroll
-        for (int g = 0; g < kBN / 32; ++g) {
-          uint32_t r[16];
+        for (int gb = 0; gb < kBN / 96; ++gb) {
+          uint32_t r[48];
           const uint32_t taddr =
-              tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kBufStride + h * (kBN / 2) + g * 16);
+              tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kBufStride + h * (kBN / 2) + gb * 48);
           asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                "=r"(r[15])
-              : "r"(taddr));
-          asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%48];\n"
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%49];\n"
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47}, [%50];\n"
+              "tcgen05.wait::ld.sync.aligned;\n"
+              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47])
+              : "r"(taddr), "r"(taddr + 16u), "r"(taddr + 32u)
+              : "memory");
 #pragma unroll
-          for (int j = 0; j < 16; ++j) sum[g * 16 + j] += __uint_as_float(r[j]);
+          for (int j = 0; j < 48; ++j) sum[gb * 48 + j] += __uint_as_float(r[j]);
         }
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
         __syncwarp();
@@ -379,10 +383,11 @@ __device__ __forceinline__ float tf32_round(float x) {
   return __uint_as_float(r);
 }
 
-// A2[r][s P + j] for the trailing rows, planes s = [hi | lo] of the
-// interleaved conj(L21) (j = 2 t + f: f = 0 real part, 1 minus imaginary part)
-__global__ void pack_a_kernel(const zf* __restrict__ LU, int64_t lda, int k0, int w, int m, int P,
-                              float* __restrict__ A3) {
+// A3[r][s pw + koff + j] (j < P) for rows row0 + r of the columns k0 .. k0 +
+// w - 1, planes s = [hi | lo] of the interleaved conj(L) (j = 2 t + f: f = 0
+// real part, 1 minus imaginary part), zero for t >= w
+__global__ void pack_a_kernel(const zf* __restrict__ LU, int64_t lda, int k0, int w, int row0, int m, int P, int pw,
+                              int koff, float* __restrict__ A3) {
   const int K2p = 2 * P;
   int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (int64_t)m * K2p) return;
@@ -390,12 +395,12 @@ __global__ void pack_a_kernel(const zf* __restrict__ LU, int64_t lda, int k0, in
   int s = k2 / P, j = k2 % P, t = j >> 1;
   float out = 0.f;
   if (t < w) {
-    zf L = LU[(int64_t)(k0 + w + r) * lda + k0 + t];
+    zf L = LU[(int64_t)(row0 + r) * lda + k0 + t];
     float v = (j & 1) ? -L.im : L.re;
     float hi = tf32_round(v);
     out = s == 1 ? tf32_round(v - hi) : hi;
   }
-  A3[e] = out;
+  A3[(int64_t)r * 2 * pw + s * pw + koff + j] = out;
 }
 
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -454,33 +459,41 @@ inline int plane_width(int w) { return (2 * w + 63) / 64 * 64; }
 
 inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-// Operand buffer of the factorisation of an n x n matrix in blocks of 128
-// columns, each factored as two panels of 64: a header of kTcHeader bytes
-// (error word, then one tile counter per update launch from byte 16), the
-// packed A3 (m x 2 P) and B3 (2 m x 2 P) of a block's rank-128 trailing
-// update (P = 256, m <= n - 128), then Ai and Bi of the rank-64 update of
-// the block's second panel (P = 128, m <= n - 64 rows, 64 columns).
+// Operand buffer of the factorisation of an n x n matrix in super-blocks of
+// 256 columns (two blocks of 128, each two panels of 64): a header of
+// kTcHeader bytes (error word, then one tile counter per update launch from
+// byte 16); A3 (n x 2 x 512) and B3 (2 n x 2 x 512): planes 512 floats wide,
+// K of block a's columns in 0..255 and of block b's in 256..511 (A3 holds, in
+// turn, block a's L for its rank-128 update of block b's columns, L_ba for
+// the product on block b's rows of the trailing columns, and both blocks' L
+// for the rank-256 update of the trailing matrix); then Ai and Bi of the
+// rank-64 update of a block's second panel (plane width 128, m <= n - 64
+// rows, 64 columns).
 struct TcLayout {
   size_t a3, b3, ai, bi, total;
 };
 inline TcLayout tc_layout(int n) {
   TcLayout t;
-  const size_t m2 = (size_t)std::max(n - 128, 1), m1 = (size_t)std::max(n - 64, 1);
+  const size_t m = (size_t)std::max(n, 1);
   size_t off = kTcHeader;
   t.a3 = off;
-  off += align256(sizeof(float) * m2 * 2 * 256);
+  off += align256(sizeof(float) * m * 2 * 512);
   t.b3 = off;
-  off += align256(sizeof(float) * 2 * m2 * 2 * 256);
+  off += align256(sizeof(float) * 2 * m * 2 * 512);
   t.ai = off;
-  off += align256(sizeof(float) * m1 * 2 * 128);
+  off += align256(sizeof(float) * m * 2 * 128);
   t.bi = off;
   off += align256(sizeof(float) * 128 * 2 * 128);
   t.total = off;
   return t;
 }
 
+// update launches per super-block of 256 columns: two rank-64 updates, block
+// a's rank-128 update of block b's columns, L_ba U_a, the rank-256 update
+constexpr int kTcSlotsPerSuper = 5;
+
 int lu_tc_prepare(m25_ctx* ctx, int n) {
-  if (2 * ((n + 127) / 128) + 2 > (kTcHeader - 16) / 4) {
+  if (kTcSlotsPerSuper * ((n + 255) / 256) + 2 > (kTcHeader - 16) / 4) {
     set_error("tensor-core LU: too many panels");
     return M25_ERR_VALUE;
   }
@@ -512,36 +525,39 @@ int lu_tc_buffers(m25_ctx* ctx, int n, float** A3, float** B3, float** Ai, float
   return M25_OK;
 }
 
-// A3 (m x 2 P) from the rows k0 + w .. k0 + w + m - 1 of the panel block's w columns
-int lu_tc_pack_a(m25_ctx* ctx, const zf* A, int64_t lda, int k0, int w, int m, int P, float* A3) {
+// A3 rows 0 .. m - 1 (plane width pw, K offset koff, K extent P per plane)
+// from the rows row0 .. row0 + m - 1 of the w columns k0 .. k0 + w - 1
+int lu_tc_pack_a(m25_ctx* ctx, const zf* A, int64_t lda, int k0, int w, int row0, int m, int P, int pw, int koff,
+                 float* A3) {
   if (m <= 0) return M25_OK;
   StageTimer tm(ctx, ST_PACK);
   const int64_t ta = (int64_t)m * 2 * P;
-  pack_a_kernel<<<(unsigned)((ta + 255) / 256), 256, 0, ctx->stream>>>(A, lda, k0, w, m, P, A3);
+  pack_a_kernel<<<(unsigned)((ta + 255) / 256), 256, 0, ctx->stream>>>(A, lda, k0, w, row0, m, P, pw, koff, A3);
   M25_CHECK_LAUNCH();
   return M25_OK;
 }
 
-// C -= A3 B3 for C = A[r0 .. r0 + m - 1][r0 .. r0 + nc - 1] (complex64, in
-// place): A3 (m x 2 P) and B3 (2 nc x 2 P) packed [hi | lo] planes; slot: the
+// C -= A3 B3 for C = A[r0 .. r0 + m - 1][c0 .. c0 + nc - 1] (complex64, in
+// place): A3 (m rows) and B3 (2 nc rows) packed [hi | lo] planes of width pw
+// floats, of which the first P (a multiple of 32) take part; slot: the
 // header's tile counter of this launch (zeroed by lu_tc_prepare).
-int lu_tc_update(m25_ctx* ctx, zf* A, int64_t lda, int r0, int m, int nc, int P, const float* A3, const float* B3,
-                 int slot) {
+int lu_tc_update(m25_ctx* ctx, zf* A, int64_t lda, int r0, int c0, int m, int nc, int P, int pw, const float* A3,
+                 const float* B3, int slot) {
   if (m <= 0 || nc <= 0) return M25_OK;
   cudaStream_t st = ctx->stream;
-  const int n2 = 2 * nc, K2p = 2 * P;
-  if (P % kBK || 16 + 4 * (size_t)(slot + 1) > (size_t)kTcHeader) {
+  const int n2 = 2 * nc;
+  if (P % kBK || P > pw || pw % kBK || 16 + 4 * (size_t)(slot + 1) > (size_t)kTcHeader) {
     set_error("tensor-core LU: bad update shape");
     return M25_ERR_VALUE;
   }
   int* err = ctx->Dw.as<int>();
   CUtensorMap ma, mb;
   int rc;
-  if ((rc = make_map(&ma, A3, m, K2p, kBM))) return rc;
-  if ((rc = make_map(&mb, B3, n2, K2p, kBN))) return rc;
+  if ((rc = make_map(&ma, A3, m, 2 * pw, kBM))) return rc;
+  if ((rc = make_map(&mb, B3, n2, 2 * pw, kBN))) return rc;
   // C: the fp32 view of the block, rows 2 lda floats apart, 32 x 32 boxes
   CUtensorMap mc;
-  const float* C = reinterpret_cast<const float*>(A + (int64_t)r0 * lda + r0);
+  const float* C = reinterpret_cast<const float*>(A + (int64_t)r0 * lda + c0);
   if ((lda & 1) || (reinterpret_cast<uintptr_t>(C) & 15)) {
     set_error("tensor-core LU: C needs an even leading dimension and 16-byte alignment");
     return M25_ERR_VALUE;
@@ -556,6 +572,7 @@ int lu_tc_update(m25_ctx* ctx, zf* A, int64_t lda, int r0, int m, int nc, int P,
   ta.M = m;
   ta.N = n2;
   ta.P = P;
+  ta.pw = pw;
   ta.tiles_m = (m + kBM - 1) / kBM;
   ta.ntiles = ta.tiles_m * ((n2 + kBN - 1) / kBN);
   ta.chunk = chunk;

@@ -27,6 +27,7 @@ def main():
     ap.add_argument("mode", choices=["fill", "point", "lu"])
     ap.add_argument("--n", type=int, default=4096, help="matrix size of the lu mode")
     ap.add_argument("--simt", action="store_true", help="lu mode: SIMT trailing updates")
+    ap.add_argument("--timing", action="store_true", help="lu mode: print the stage times (CUDA events)")
     ap.add_argument("--workload", default="bandpass")
     ap.add_argument("--precision", default="fp64", choices=list(PRECISIONS))
     ap.add_argument("--reps", type=int, default=2)
@@ -71,6 +72,9 @@ def lu_case(args):
     piv = torch.empty(n, dtype=torch.int32, device="cuda")
     info = np.zeros(1, np.int32)
     flags = E.M25_LU_NO_TENSOR_CORES if args.simt else 0
+    ms = (C.c_double * 11)()
+    if args.timing:
+        E.check(ctx.lib.m25_ctx_timing(ctx.h, 1, None, None))
     for _ in range(args.reps):
         A = A0.clone()
         # the engine works on its own stream: torch's copy must have landed
@@ -79,6 +83,11 @@ def lu_case(args):
                                       C.cast(C.c_void_p(piv.data_ptr()), C.POINTER(C.c_int32)), E.M25_ON_DEVICE, flags,
                                       E.ptr(info, C.c_int32)))
     ctx.synchronize()
+    if args.timing:
+        E.check(ctx.lib.m25_ctx_timing(ctx.h, 0, ms, None))
+        names = ["greens", "fill", "gather", "via", "panel", "pack", "swap_trsm", "update", "trsv", "refine",
+                 "deembed"]
+        print("stage ms per factorisation:", {k: round(v / args.reps, 3) for k, v in zip(names, ms) if v})
     print(f"lu ok: n={n} info={int(info[0])} tensor_cores={not args.simt}")
     ctx.close()
 

@@ -660,17 +660,19 @@ class Solver:
     def _checkpoint_key(self, freqs):
         return checkpoint_key(self.mesh, freqs, values_digest(self.values, self.lumped, self.components))
 
-    _DEVICE_STATE = ("ctx", "_geom", "_geom_owner", "_ports", "_siblings", "_sib_lock")
+    _DEVICE_STATE = ("ctx", "_ctx_owner", "_geom", "_geom_owner", "_ports", "_siblings", "_sib_lock")
 
-    def _clone(self):
+    def _clone(self, ctx=None):
         """A solver sharing this one's host-side set-up (mesh, port models,
         groups, test blocks) and its device geometry (classes, closed-form
         near-pair data: read-only once built, readable from any stream) with
-        a fresh engine context of its own (stream, per-point buffers, ports)."""
+        a fresh engine context of its own (stream, per-point buffers, ports),
+        or on the given context (then owned by the caller, who closes it)."""
         s = object.__new__(Solver)
         s.__dict__.update({k: v for k, v in self.__dict__.items() if k not in self._DEVICE_STATE})
         s.verbose = False
-        s.ctx = E.Context(self.device)
+        s.ctx = E.Context(self.device) if ctx is None else ctx
+        s._ctx_owner = ctx is None
         s._geom = self.geometry()
         s._geom_owner = False  # closed by this solver, after its siblings
         s._ports = None
@@ -854,7 +856,8 @@ class Solver:
         if self._geom is not None and getattr(self, "_geom_owner", True):
             self._geom.close()
         self._ports = self._geom = None
-        self.ctx.close()
+        if getattr(self, "_ctx_owner", True):
+            self.ctx.close()
 
 
 def values_digest(values, lumped=(), components=()):

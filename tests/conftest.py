@@ -50,3 +50,12 @@ def fit_floor(name=None):
 def fp64_tol(name=None):
     """The bar of the fp64 path's S against mom25d's: three times the fit floor."""
     return 3.0 * fit_floor(name)
+
+
+def gamma_floor(name=None):
+    """The same floor for the fitted propagation constant, relative to |gamma|."""
+    d = golden("fit_floor")
+    floors = {str(c): max(float(d[f"{c}_dgamma_fit"].max()), float(d[f"{c}_dgamma_x"].max())) for c in d["cases"]}
+    if name is not None and name in floors:
+        return floors[name]
+    return max(floors.values())

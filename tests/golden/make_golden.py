@@ -219,16 +219,63 @@ def floor_case(name, sweep_freqs, seeds=4, kw=None):
     return out
 
 
-def floor_all():
-    cases = dict(line=("line", [2e9, 7e9], None), tee=("tee", np.linspace(1, 10, 37)[[0, 12, 24, 36]] * 1e9, None),
-                 via=("via", [2e9, 10e9, 18e9], None), bandpass_0=("bandpass", [3e9, 9e9], dict(k=0)),
-                 lpf=("lpf", [0.5e9, 4e9, 8e9], None))
-    out = {}
-    for key, (name, fr, kw) in cases.items():
+FLOOR_CASES = dict(line=("line", [2e9, 7e9], None), tee=("tee", np.linspace(1, 10, 37)[[0, 12, 24, 36]] * 1e9, None),
+                   via=("via", [2e9, 10e9, 18e9], None), bandpass_0=("bandpass", [3e9, 9e9], dict(k=0)),
+                   lpf=("lpf", [0.5e9, 4e9, 8e9], None), line_lossless=("line_lossless", [2e9, 5e9, 7e9], None))
+
+
+def floor_all(only=None):
+    """fit_floor.npz for FLOOR_CASES (only: those keys, merged into the
+    existing file)."""
+    path = os.path.join(HERE, "fit_floor.npz")
+    out, done = {}, []
+    if only and os.path.exists(path):
+        old = np.load(path)
+        done = [str(c) for c in old["cases"] if str(c) not in only]
+        out = {k: old[k] for k in old.files if k != "cases" and any(k.startswith(c + "_") for c in done)}
+    for key, (name, fr, kw) in FLOOR_CASES.items():
+        if only and key not in only:
+            continue
         for k, v in floor_case(name, fr, kw=kw).items():
             out[f"{key}_{k}"] = v
-    np.savez_compressed(os.path.join(HERE, "fit_floor.npz"), cases=np.array(list(cases)), **out)
+        done.append(key)
+    np.savez_compressed(path, cases=np.array(done), **out)
     print("fit floor: done", flush=True)
+
+
+def x_floor_case(name, f, kw=None, eps=1e-13, seeds=2):
+    """The conditioning floor of the currents: mom25d's x at f against its x
+    from the same Z with every entry multiplied by 1 + eps (n1 + j n2)
+    (n standard normal, seeded): max |dx| / max |x| over the seeds. An
+    implementation whose Z agrees with mom25d's to eps cannot be expected to
+    give its x closer than this."""
+    lay, stack, mkw, _ = workloads.BUILDERS[name](ref, **(kw or {}))
+    m = lay.mesh(**mkw)
+    sol = ref.Solver(m, stack, verbose=False, method="dense")
+    g = sol.greens(f)
+    Z = sol.impedance(f, g)
+    B = sol.port_excitations()
+    x0 = ref_solver._dense_solve(Z.copy(), B)
+    worst = 0.0
+    for seed in range(seeds):
+        rng = np.random.default_rng(seed)
+        Zp = Z * (1 + eps * (rng.standard_normal(Z.shape) + 1j * rng.standard_normal(Z.shape)))
+        x = ref_solver._dense_solve(Zp, B)
+        worst = max(worst, float(np.abs(x - x0).max() / np.abs(x0).max()))
+    print(f"x floor {name} {kw or ''}: {worst:.2e}", flush=True)
+    return worst
+
+
+def x_floor_all(names):
+    """x_floor.npz: the conditioning floor of x at each fixture's f0."""
+    path = os.path.join(HERE, "x_floor.npz")
+    out = dict(np.load(path)) if os.path.exists(path) else {}
+    out["eps"] = np.array(1e-13)
+    for key in names:
+        g = np.load(os.path.join(HERE, key + ".npz"))
+        base, kw = (("bandpass", dict(k=int(key.split("_")[1]))) if key.startswith("bandpass_") else (key, None))
+        out[key] = np.array(x_floor_case(base, float(g["f0"]), kw))
+        np.savez_compressed(path, **out)
 
 
 def interp_case(name, interp_kw=None, nfreq=None, zrows=None):
@@ -319,7 +366,7 @@ def network_case():
     write_block(block, np.linspace(0.5 * fr.min(), 1.5 * fr.max(), 9))
     net = r.connect(block, [(1, 1)])
     out = dict(freqs=fr, S=r.S, z0=r.z0, gamma=r.gamma, z0_line=r.z0_line, fit_residual=r.fit_residual,
-               waves=r.waves, port_names=np.array(r.port_names), matched0=r.matched_currents(0, 0),
+               waves=r.waves, x0=r.currents[0], port_names=np.array(r.port_names), matched0=r.matched_currents(0, 0),
                wave0=r.wave_currents(0, [1.0, 0.5j]), net_S=net.S, net_names=np.array(net.names),
                net_currents0=net.currents(0, 0))
     np.savez_compressed(os.path.join(HERE, "line_network.npz"), **out)
@@ -360,7 +407,10 @@ def main():
     ap.add_argument("--interp", action="store_true", help="only the FreqInterp fixtures")
     ap.add_argument("--network", action="store_true", help="only the network / waves fixture")
     ap.add_argument("--lumped", action="store_true", help="only the lumped-component fixture")
-    ap.add_argument("--floor", action="store_true", help="only the wave-fit floor fixture")
+    ap.add_argument("--floor", nargs="*", default=None, metavar="CASE",
+                    help="only the wave-fit floor fixture (of the given FLOOR_CASES keys, merged into the file)")
+    ap.add_argument("--xfloor", nargs="+", default=None, metavar="FIXTURE",
+                    help="only the conditioning floor of x at the f0 of the given fixtures")
     ap.add_argument("--variants", action="store_true", help="only band-pass variants 3, 7, 11 and 14")
     ap.add_argument("--lossless", action="store_true", help="only the lossless line (mom25d's bounded beta fit)")
     ap.add_argument("--gcpw", action="store_true",
@@ -378,8 +428,11 @@ def main():
         interp_case("tee", zrows=np.arange(0, 1085, 97))
         interp_case("shunt_via", interp_kw=dict(step=1.5e9), nfreq=25, zrows=np.arange(0, 492, 41))
         return
-    if args.floor:
-        floor_all()
+    if args.floor is not None:
+        floor_all(args.floor or None)
+        return
+    if args.xfloor:
+        x_floor_all(args.xfloor)
         return
     fb = np.linspace(1, 12, 128) * 1e9
     if args.lossless:

@@ -11,7 +11,7 @@ from conftest import fit_floor, fp64_tol, golden
 
 def test_floor_fixture_covers_the_parity_workloads():
     d = golden("fit_floor")
-    assert set(d["cases"]) == {"line", "tee", "via", "bandpass_0", "lpf"}
+    assert set(d["cases"]) == {"line", "tee", "via", "bandpass_0", "lpf", "line_lossless"}
     for c in d["cases"]:
         for mode in ("fit", "x"):
             dS = d[f"{c}_dS_{mode}"]
@@ -19,7 +19,7 @@ def test_floor_fixture_covers_the_parity_workloads():
             assert np.all(np.isfinite(dS))
 
 
-@pytest.mark.parametrize("case", ["line", "tee", "via", "bandpass_0", "lpf"])
+@pytest.mark.parametrize("case", ["line", "tee", "via", "bandpass_0", "lpf", "line_lossless"])
 def test_floor_does_not_shrink_with_the_perturbation(case):
     """The floor is a property of the fit, not of the perturbation: inputs
     moved by 1e-15 already move S by within a factor of 30 of what 1e-10
@@ -37,7 +37,8 @@ def test_floor_does_not_shrink_with_the_perturbation(case):
 
 
 def test_fp64_bar_is_three_floors():
-    for case in ("line", "tee", "via", "bandpass_0", "lpf"):
+    cases = ("line", "tee", "via", "bandpass_0", "lpf", "line_lossless")
+    for case in cases:
         assert fp64_tol(case) == 3 * fit_floor(case)
     # a workload without its own measurement takes the largest floor
-    assert fit_floor("gcpw") == max(fit_floor(c) for c in ("line", "tee", "via", "bandpass_0", "lpf"))
+    assert fit_floor("gcpw") == max(fit_floor(c) for c in cases)

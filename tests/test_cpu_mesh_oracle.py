@@ -160,7 +160,7 @@ def test_oracle_lossless_sweep_matches_reference():
     """A lossless substrate takes mom25d's bounded search over beta
     (gamma = j beta, Engine/mom25d/solver.py:654-662): the oracle's sweep
     gives mom25d's gamma (purely imaginary) and S (lossless line)."""
-    from conftest import fp64_tol
+    from conftest import fp64_tol, gamma_floor
 
     g = golden("line_lossless")
     lay, st, m, _ = workloads.build(G, "line_lossless")
@@ -168,5 +168,7 @@ def test_oracle_lossless_sweep_matches_reference():
     sw = O.Sweep(m, st)
     S, z0, gam, zl, res = sw.sweep(g["freqs"])
     assert np.all(gam.real == 0) and np.all(g["gamma"].real == 0)
-    assert np.abs(gam - g["gamma"]).max() < 1e-9 * np.abs(g["gamma"]).max()
+    # where the line is short (2 GHz) the objective is flat in beta: even
+    # mom25d's own beta moves within the floor with its BLAS thread count
+    assert (np.abs(gam - g["gamma"]) / np.abs(g["gamma"])).max() < 3 * gamma_floor("line_lossless")
     assert np.abs(S - g["S"]).max() < fp64_tol("line_lossless")

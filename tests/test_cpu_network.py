@@ -58,10 +58,10 @@ def test_innerconnect_of_a_thru_is_identity():
 
 
 def test_wave_currents_of_matched_drive_are_matched_currents():
-    """With x the reference's currents, matched_currents and wave_currents
-    reproduce mom25d's (the waves come from the same fixture)."""
-    g = golden("line")
-    r, gn = reference_result(currents=[g["x"]] + [None] * (len(golden("line_network")["freqs"]) - 1))
+    """With x the reference's currents (those of the same mom25d sweep),
+    matched_currents and wave_currents reproduce mom25d's."""
+    gn0 = golden("line_network")
+    r, gn = reference_result(currents=[gn0["x0"]] + [None] * (len(gn0["freqs"]) - 1))
     np.testing.assert_allclose(r.matched_currents(0, 0), gn["matched0"], rtol=0, atol=1e-12 * np.abs(gn["matched0"]).max())
     np.testing.assert_allclose(r.wave_currents(0, [1.0, 0.5j]), gn["wave0"], rtol=0, atol=1e-12 * np.abs(gn["wave0"]).max())
 

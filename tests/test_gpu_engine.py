@@ -11,7 +11,7 @@ from mom25d_gb300 import workloads
 from mom25d_gb300.solver import Solver, dense_solve
 from oracle import sweep as O
 
-from conftest import fp64_tol, golden
+from conftest import fp64_tol, gamma_floor, golden
 
 pytestmark = pytest.mark.gpu
 
@@ -427,10 +427,15 @@ def test_lossless_line_sweep_matches_reference(gpu, prec):
             warnings.simplefilter("error", RuntimeWarning)
             r = sol.sweep(g["freqs"])
         assert np.all(r.gamma.real == 0)
+        dS = np.abs(r.S - g["S"]).max(axis=(1, 2))
+        dg = (np.abs(r.gamma - g["gamma"]) / np.abs(g["gamma"])).max(axis=1)
+        print(prec, "max |dS|", dS, "gamma", dg)
+        # where the line is electrically short (2 GHz) the fit's objective is
+        # flat in beta and the search stops anywhere within the floor
         if prec == "fp64":
-            assert np.abs(r.gamma - g["gamma"]).max() < 1e-9 * np.abs(g["gamma"]).max()
+            assert dg.max() < 3 * gamma_floor("line_lossless")
         tol = fp64_tol("line_lossless") if prec == "fp64" else 1e-5
-        assert np.abs(r.S - g["S"]).max() < tol
+        assert dS.max() < tol
         it = np.zeros(len(sol.groups), np.int32)
         E.check(sol.ctx.lib.m25_deembed_fit_info(sol.port_data().h, E.ptr(it, C.c_int32)))
         assert np.all(it > 1) and np.all(it < 500), it

@@ -2,10 +2,13 @@
 mom25d itself (tests/golden, make_golden.py), on every workload that has one.
 
 Bars:
-- before the wave fit (currents x, charges q, line voltages phi, cut
-  currents I and cut voltages V): 1e-9 relative to the largest entry, fp64
-  path. x is limited by the conditioning of Z: mom25d's own currents move by
-  ~2e-10 relative when its LAPACK runs on another number of threads;
+- before the wave fit (charges q, line voltages phi, cut currents I and cut
+  voltages V): 1e-9 relative to the largest entry, fp64 path;
+- the currents x: 1e-9, or three times their conditioning floor where that
+  is larger (tests/golden/x_floor.npz: mom25d's own x moves by 5e-10 to
+  2e-8 relative when its Z is perturbed by 1e-13, the level at which the
+  fills agree; the part of x that moves carries no charge, so q, phi, I and
+  V still agree to 1e-12);
 - S of the fp64 path: three times the floor of mom25d's own wave fit
   (conftest.fit_floor: 8e-9 to 6e-8 by workload);
 - S of the mixed path: 1e-5.
@@ -25,6 +28,13 @@ from conftest import GOLDEN, fp64_tol, golden
 pytestmark = pytest.mark.gpu
 
 STAGE_TOL = 1e-9
+
+
+def x_tol(name):
+    """The bar for the currents x of a workload (see the module docstring)."""
+    path = os.path.join(GOLDEN, "x_floor.npz")
+    d = np.load(path) if os.path.exists(path) else {}
+    return max(STAGE_TOL, 3.0 * float(d[name])) if name in d else STAGE_TOL
 
 
 def _have(name):
@@ -60,8 +70,9 @@ def test_prefit_stages_match_reference(gpu, name):
             ref = g[key]
             assert got.shape == ref.shape, (key, got.shape, ref.shape)
             errs[key] = np.abs(got - ref).max() / np.abs(ref).max()
-        print(name, {k: f"{v:.1e}" for k, v in errs.items()})
-        assert max(errs.values()) <= STAGE_TOL, errs
+        print(name, {k: f"{v:.1e}" for k, v in errs.items()}, f"x bar {x_tol(name):.1e}")
+        assert errs["x"] <= x_tol(name), errs
+        assert max(v for k, v in errs.items() if k != "x") <= STAGE_TOL, errs
     finally:
         sol.close()
 
@@ -121,8 +132,9 @@ def test_gcpw_prefit_stages_match_reference(gpu):
         q, phi, I, V = sol.last_deembed()
         errs = {k: np.abs(got - g[k]).max() / np.abs(g[k]).max()
                 for k, got in (("x", x), ("q", q), ("phi", phi), ("I", I), ("V", V))}
-        print("gcpw", {k: f"{v:.1e}" for k, v in errs.items()})
-        assert max(errs.values()) <= STAGE_TOL, errs
+        print("gcpw", {k: f"{v:.1e}" for k, v in errs.items()}, f"x bar {x_tol('gcpw'):.1e}")
+        assert errs["x"] <= x_tol("gcpw"), errs
+        assert max(v for k, v in errs.items() if k != "x") <= STAGE_TOL, errs
         Z = sol.impedance(float(g["f0"]))
         rows = g["Z_rows_idx"]
         assert np.abs(Z[rows] - g["Z_rows"]).max() <= 1e-11 * np.abs(g["Z_rows"]).max()
