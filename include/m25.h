@@ -71,6 +71,17 @@ int m25_ctx_synchronize(m25_ctx* ctx);
 int m25_ctx_mem_info(m25_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes);
 void* m25_ctx_stream(m25_ctx* ctx); /* the cudaStream_t every call of this context runs on */
 
+/* Tuning knobs of this context's calls (no counterpart in mom25d; set per
+ * point by mom25d_gb300/batch.py from the table autotune.py measures), 0
+ * keeping the process default: panel_cluster_min, the smallest cluster (4, 8
+ * or 16 CTAs) the LU panel runs on (default 4, or $M25_PANEL_CLUSTER_MIN);
+ * wave_ctas, the CTA cap of the triangular solves (default one per 64-row
+ * block, or $M25_WAVE_CTAS); tc_chunk, the k-blocks (12 MMAs each) the
+ * tensor-core update accumulates in TMEM before adding into its fp32
+ * registers (1..8; default 1, or $M25_TC_CHUNK: longer chunks round the
+ * accumulation coarser). */
+int m25_ctx_set_tuning(m25_ctx* ctx, int32_t panel_cluster_min, int32_t wave_ctas, int32_t tc_chunk);
+
 /* Failure-path hook (no counterpart in mom25d, whose solve has no waits):
  * bound every ready-flag wait of this context's triangular solves to `polls`
  * polls (0 restores the default bound, about a second of polling). A solve
@@ -285,6 +296,18 @@ int m25_ports_destroy(m25_ports* p);
  * beta0 overrides the per-group initial guess (NULL: from the port desc). */
 int m25_deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* ports, const void* x, int where,
                 const double* beta0, double* S, double* z0, double* gamma, double* z0_line, double* resid);
+
+/* Internal ports (Layout.add_gap_port / add_via_port, Engine/mom25d/
+ * solver.py:1029-1034, 1305-1318): the solutions handed to m25_deembed carry
+ * nexc columns, the P feed excitations then one per internal port. Every
+ * feed's wave fit then takes its currents and voltages under all nexc
+ * excitations (P <= nexc <= 8, at most 16 (port, excitation) datasets per
+ * port group), m25_deembed returns gamma, z0_line and the residual but not
+ * S, and m25_deembed_coefs gives the fitted amplitudes A and B (P x nexc
+ * complex128, [port][excitation]) from which the caller assembles S with the
+ * internal ports' rows. nexc = P restores the feed-only de-embedding. */
+int m25_ports_set_excitations(m25_ports* ports, int32_t nexc);
+int m25_deembed_coefs(m25_ports* ports, double* A, double* B);
 
 /* Per port group, the iterations of the last de-embedding's wave fit
  * (Nelder-Mead, or for a lossless stack the bounded Brent search over beta);

@@ -238,6 +238,7 @@ __global__ void cuts_kernel(int ncut, int P, const int32_t* __restrict__ cut_off
 // ------------------------------------------------------------------ fit
 struct FitArgs {
   int P, ngroup;
+  int E;                    // excitation columns of x (P feeds, then internal ports)
   int group_of[kMaxPorts];
   int ns[kMaxPorts];
   int s_off[kMaxPorts];     // offset of port p's cuts in s / I / V rows
@@ -321,13 +322,13 @@ __device__ double wave_objective(const FitArgs& a, int grp, zd g, double Inrm, d
     const double r22 = sqrt(warp_sum(n22));
 #pragma unroll
     for (int u = 0; u < kPer; ++u) q2[u] = q2[u] / r22;
-    for (int e = 0; e < a.P; ++e, ++nd) {
+    for (int e = 0; e < a.E; ++e, ++nd) {
       zd Iv[kPer];
       zd b1(0.0), b2(0.0);
 #pragma unroll
       for (int u = 0; u < kPer; ++u) {
         int i = lane + 32 * u;
-        Iv[u] = i < ns ? a.I[(int64_t)(off + i) * a.P + e] : zd(0.0);
+        Iv[u] = i < ns ? a.I[(int64_t)(off + i) * a.E + e] : zd(0.0);
         b1 += conj(q1[u]) * Iv[u];
         b2 += conj(q2[u]) * Iv[u];
       }
@@ -342,15 +343,15 @@ __device__ double wave_objective(const FitArgs& a, int grp, zd g, double Inrm, d
         rr += norm2(d);
         U[nd][u] = c0 * ep[u] - c1 * em[u];
         if (lane + 32 * u < ns) {
-          zd Vv = a.V[(int64_t)(off + lane + 32 * u) * a.P + e];
+          zd Vv = a.V[(int64_t)(off + lane + 32 * u) * a.E + e];
           UV += conj(U[nd][u]) * Vv;
           UU += norm2(U[nd][u]);
         }
       }
       res += warp_sum(rr) / Inrm;
       if (store && lane == 0) {
-        a.A[p * a.P + e] = c0;
-        a.B[p * a.P + e] = c1;
+        a.A[p * a.E + e] = c0;
+        a.B[p * a.E + e] = c1;
       }
     }
   }
@@ -360,11 +361,11 @@ __device__ double wave_objective(const FitArgs& a, int grp, zd g, double Inrm, d
   for (int p = 0; p < a.P; ++p) {
     if (a.group_of[p] != grp) continue;
     const int ns = a.ns[p], off = a.s_off[p];
-    for (int e = 0; e < a.P; ++e, ++nd) {
+    for (int e = 0; e < a.E; ++e, ++nd) {
 #pragma unroll
       for (int u = 0; u < kPer; ++u)
         if (lane + 32 * u < ns) {
-          zd Vv = a.V[(int64_t)(off + lane + 32 * u) * a.P + e];
+          zd Vv = a.V[(int64_t)(off + lane + 32 * u) * a.E + e];
           rv += norm2(Vv - z0 * U[nd][u]);
         }
     }
@@ -465,9 +466,9 @@ __global__ void __launch_bounds__(32 * kFitWarps) fit_kernel(FitArgs a) {
   for (int p = 0; p < a.P; ++p) {
     if (a.group_of[p] != grp) continue;
     for (int i = lane; i < a.ns[p]; i += 32)
-      for (int e = 0; e < a.P; ++e) {
-        Inrm += norm2(a.I[(int64_t)(a.s_off[p] + i) * a.P + e]);
-        Vnrm += norm2(a.V[(int64_t)(a.s_off[p] + i) * a.P + e]);
+      for (int e = 0; e < a.E; ++e) {
+        Inrm += norm2(a.I[(int64_t)(a.s_off[p] + i) * a.E + e]);
+        Vnrm += norm2(a.V[(int64_t)(a.s_off[p] + i) * a.E + e]);
       }
   }
   Inrm = warp_sum(Inrm);
@@ -688,6 +689,7 @@ using namespace m25;
 struct m25_ports {
   m25_ctx* ctx = nullptr;
   int P = 0, ngroup = 0, nvpt_tot = 0, ncut = 0, lossless = 0;
+  int E = 0;  // excitation columns of the solutions de-embedded (P, or P + internal ports)
   double v_weight = 1.0;
   std::vector<int> group_of, ns, s_off, port_level, nvpt;
   std::vector<double> beta0;
@@ -704,7 +706,8 @@ struct m25_ports {
   zd* Bexc = nullptr;  // (n, P) excitation columns
   int* iters = nullptr;
   int nt = 0, n = 0;
-  std::vector<zd> waves;  // (P, P) incident current-wave amplitudes A of the last de-embedding
+  std::vector<zd> waves;  // (P, E) incident current-wave amplitudes A of the last de-embedding
+  std::vector<zd> bcoef;  // (P, E) their B (outgoing) amplitudes
   std::vector<void*> allocs;
 };
 
@@ -729,6 +732,7 @@ extern "C" int m25_ports_create(m25_ctx* ctx, m25_geom* geom, const m25_port_des
       }
   }
   m25_ports* p = new m25_ports();
+  p->E = d->nport;
   p->lossless = d->lossless ? 1 : 0;
   if (p->lossless) p->bounds.assign(d->bounds, d->bounds + 2 * d->ngroup);
   p->ctx = ctx;
@@ -789,11 +793,12 @@ extern "C" int m25_ports_create(m25_ctx* ctx, m25_geom* geom, const m25_port_des
   TRY(alloc(p->allocs, (void**)&p->cut_w, sizeof(double) * std::max(nent, 1)));
   TRY(alloc(p->allocs, (void**)&p->vpts, sizeof(double) * 2 * tot_v));
   TRY(alloc(p->allocs, (void**)&p->vpt_level, sizeof(int32_t) * tot_v));
-  TRY(alloc(p->allocs, (void**)&p->q, sizeof(zd) * (size_t)geom->nt * p->P));
-  TRY(alloc(p->allocs, (void**)&p->phi, sizeof(zd) * (size_t)tot_v * p->P));
-  TRY(alloc(p->allocs, (void**)&p->I, sizeof(zd) * (size_t)tot_s * p->P));
-  TRY(alloc(p->allocs, (void**)&p->V, sizeof(zd) * (size_t)tot_s * p->P));
-  TRY(alloc(p->allocs, (void**)&p->x, sizeof(zd) * (size_t)p->n * p->P));
+  // per-call buffers for up to kMaxPorts excitation columns (m25_ports_set_excitations)
+  TRY(alloc(p->allocs, (void**)&p->q, sizeof(zd) * (size_t)geom->nt * kMaxPorts));
+  TRY(alloc(p->allocs, (void**)&p->phi, sizeof(zd) * (size_t)tot_v * kMaxPorts));
+  TRY(alloc(p->allocs, (void**)&p->I, sizeof(zd) * (size_t)tot_s * kMaxPorts));
+  TRY(alloc(p->allocs, (void**)&p->V, sizeof(zd) * (size_t)tot_s * kMaxPorts));
+  TRY(alloc(p->allocs, (void**)&p->x, sizeof(zd) * (size_t)p->n * kMaxPorts));
   TRY(alloc(p->allocs, (void**)&p->out, sizeof(zd) * (size_t)(4 * kMaxPorts * kMaxPorts + 8 * kMaxPorts)));
   TRY(alloc(p->allocs, (void**)&p->iters, sizeof(int) * kMaxPorts));
   TRY(alloc(p->allocs, (void**)&p->Bexc, sizeof(zd) * (size_t)p->n * p->P));
@@ -854,7 +859,7 @@ static int deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, c
     return M25_ERR_VALUE;
   }
   cudaStream_t st = ctx->stream;
-  const int P = p->P, L = geom->nlev;
+  const int P = p->E, L = geom->nlev;  // P: columns of x (feeds, then internal ports)
   const zd* xd = static_cast<const zd*>(x);
   if (where == M25_ON_HOST) {
     M25_CUDA(cudaMemcpyAsync(p->x, x, sizeof(zd) * (size_t)p->n * P, cudaMemcpyHostToDevice, st));
@@ -893,9 +898,10 @@ static int deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, c
   cuts_kernel<<<(p->ncut * P + 127) / 128, 128, 0, st>>>(p->ncut, P, p->cut_off, p->cut_edge, p->cut_w, xd, p->phi, 8,
                                                          p->I, p->V);
   FitArgs fa;
-  fa.P = P;
+  fa.P = p->P;
+  fa.E = P;
   fa.ngroup = p->ngroup;
-  for (int i = 0; i < P; ++i) {
+  for (int i = 0; i < p->P; ++i) {
     fa.group_of[i] = p->group_of[i];
     fa.ns[i] = p->ns[i];
     fa.s_off[i] = p->s_off[i];
@@ -920,7 +926,9 @@ static int deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, c
     fa.hi[gi] = p->lossless ? p->bounds[2 * gi + 1] : 0.0;
   }
   fit_kernel<<<p->ngroup, 32 * kFitWarps, 0, st>>>(fa);
-  fit_finish_kernel<<<1, 32, 0, st>>>(fa);
+  // S of the feeds alone; with internal ports the caller assembles S from
+  // the coefficients (m25_deembed_coefs)
+  if (p->E == p->P) fit_finish_kernel<<<1, 32, 0, st>>>(fa);
   M25_CHECK_LAUNCH();
   std::vector<zd> h(4 * kMaxPorts * kMaxPorts);
   M25_CUDA(cudaMemcpyAsync(h.data(), p->out, sizeof(zd) * h.size(), cudaMemcpyDeviceToHost, st));
@@ -932,10 +940,11 @@ static int deembed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25_ports* p, c
   const zd* hz = hg + kMaxPorts;
   const double* hr = reinterpret_cast<const double*>(hz + kMaxPorts);
   const double* hz0 = hr + kMaxPorts;
-  p->waves.assign(h.begin(), h.begin() + (size_t)P * P);  // A[port][excitation]
-  for (int i = 0; i < P; ++i) {
-    for (int j = 0; j < P; ++j) {
-      if (S) {
+  p->waves.assign(h.begin(), h.begin() + (size_t)p->P * P);  // A[port][excitation]
+  p->bcoef.assign(h.begin() + kMaxPorts * kMaxPorts, h.begin() + kMaxPorts * kMaxPorts + (size_t)p->P * P);
+  for (int i = 0; i < p->P; ++i) {
+    for (int j = 0; j < p->P; ++j) {
+      if (S && p->E == p->P) {
         S[2 * (i * P + j)] = hS[i * P + j].re;
         S[2 * (i * P + j) + 1] = hS[i * P + j].im;
       }
@@ -961,12 +970,49 @@ extern "C" int m25_deembed_fit_info(m25_ports* p, int32_t* iters) {
   return M25_OK;
 }
 
+extern "C" int m25_ports_set_excitations(m25_ports* p, int32_t nexc) {
+  if (!p || nexc < p->P || nexc > kMaxPorts) {
+    set_error("m25_ports_set_excitations: null ports or excitations outside nport..8");
+    return M25_ERR_VALUE;
+  }
+  for (int gi = 0; gi < p->ngroup; ++gi) {
+    int members = 0;
+    for (int i = 0; i < p->P; ++i) members += p->group_of[i] == gi;
+    if (members * nexc > kMaxDatasets) {
+      set_error("m25_ports_set_excitations: more than 16 (port, excitation) datasets in one port group");
+      return M25_ERR_VALUE;
+    }
+  }
+  p->E = nexc;
+  p->waves.clear();
+  p->bcoef.clear();
+  return M25_OK;
+}
+
+extern "C" int m25_deembed_coefs(m25_ports* p, double* A, double* B) {
+  if (!p || !A || !B) {
+    set_error("m25_deembed_coefs: null argument");
+    return M25_ERR_VALUE;
+  }
+  if (p->waves.size() != (size_t)p->P * p->E || p->bcoef.size() != p->waves.size()) {
+    set_error("m25_deembed_coefs: no de-embedding yet");
+    return M25_ERR_VALUE;
+  }
+  for (size_t k = 0; k < p->waves.size(); ++k) {
+    A[2 * k] = p->waves[k].re;
+    A[2 * k + 1] = p->waves[k].im;
+    B[2 * k] = p->bcoef[k].re;
+    B[2 * k + 1] = p->bcoef[k].im;
+  }
+  return M25_OK;
+}
+
 extern "C" int m25_deembed_waves(m25_ports* p, double* A) {
   if (!p || !A) {
     set_error("m25_deembed_waves: null argument");
     return M25_ERR_VALUE;
   }
-  if (p->waves.size() != (size_t)p->P * p->P) {
+  if (p->waves.size() != (size_t)p->P * p->E) {
     set_error("m25_deembed_waves: no de-embedding yet");
     return M25_ERR_VALUE;
   }
@@ -983,10 +1029,10 @@ extern "C" int m25_deembed_debug(m25_ctx* ctx, m25_ports* p, double* phi, double
     return M25_ERR_VALUE;
   }
   M25_CUDA(cudaStreamSynchronize(ctx->stream));
-  if (phi) M25_CUDA(cudaMemcpy(phi, p->phi, sizeof(zd) * (size_t)p->nvpt_tot * p->P, cudaMemcpyDeviceToHost));
-  if (q) M25_CUDA(cudaMemcpy(q, p->q, sizeof(zd) * (size_t)p->nt * p->P, cudaMemcpyDeviceToHost));
-  if (I) M25_CUDA(cudaMemcpy(I, p->I, sizeof(zd) * (size_t)p->ncut * p->P, cudaMemcpyDeviceToHost));
-  if (V) M25_CUDA(cudaMemcpy(V, p->V, sizeof(zd) * (size_t)p->ncut * p->P, cudaMemcpyDeviceToHost));
+  if (phi) M25_CUDA(cudaMemcpy(phi, p->phi, sizeof(zd) * (size_t)p->nvpt_tot * p->E, cudaMemcpyDeviceToHost));
+  if (q) M25_CUDA(cudaMemcpy(q, p->q, sizeof(zd) * (size_t)p->nt * p->E, cudaMemcpyDeviceToHost));
+  if (I) M25_CUDA(cudaMemcpy(I, p->I, sizeof(zd) * (size_t)p->ncut * p->E, cudaMemcpyDeviceToHost));
+  if (V) M25_CUDA(cudaMemcpy(V, p->V, sizeof(zd) * (size_t)p->ncut * p->E, cudaMemcpyDeviceToHost));
   return M25_OK;
 }
 
@@ -1000,6 +1046,10 @@ extern "C" int m25_sweep_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m25
   }
   if (precision != M25_FP64 && precision != M25_MIXED && precision != M25_MIXED_FILL32) {
     set_error("m25_sweep_point: unknown precision");
+    return M25_ERR_VALUE;
+  }
+  if (p->E != p->P) {
+    set_error("m25_sweep_point: ports with internal-port excitations are de-embedded by m25_deembed");
     return M25_ERR_VALUE;
   }
   const int n = geom->nb + geom->nv, P = p->P;
@@ -1057,6 +1107,10 @@ extern "C" int m25_interp_point(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, m2
                                 int32_t nuse, const int32_t* slots, const double* L, double ke, int precision,
                                 const double* beta0, double tol, int32_t max_iter, double* x_out, double* S,
                                 double* z0, double* gamma, double* z0_line, double* resid, int32_t* info) {
+  if (p && p->E != p->P) {
+    set_error("m25_interp_point: ports with internal-port excitations are de-embedded by m25_deembed");
+    return M25_ERR_VALUE;
+  }
   if (!ctx || !geom || !gr || !p || !ip || ip->ctx->device != ctx->device || ip->n != geom->nb + geom->nv) {
     set_error("m25_interp_point: bad argument");
     return M25_ERR_VALUE;

@@ -973,11 +973,16 @@ int lu_factor(m25_ctx* ctx, cx<T>* A, int64_t lda, int n, int32_t* ipiv, int nb,
       return yes;
     }();
     // M25_PANEL_CLUSTER_MIN: the smallest cluster size used (4, 8 or 16; a tuning knob)
-    static const int cl_min = [] {
+    static const int cl_min_env = [] {
       const char* e = getenv("M25_PANEL_CLUSTER_MIN");
       const int v = e ? atoi(e) : 4;
       return v >= 16 ? 16 : v >= 8 ? 8 : 4;
     }();
+    // the context's setting (m25_ctx_set_tuning) over the process default
+    const int cl_min = ctx->tune_cluster_min >= 16 ? 16
+                       : ctx->tune_cluster_min >= 8 ? 8
+                       : ctx->tune_cluster_min > 0  ? 4
+                                                    : cl_min_env;
     if (ok) {
       cl_rows[0] = cl_min <= 4 ? 4 * rows_of(cluster_panel_smem<T, 4>(0)) : 0;
       cl_rows[1] = cl_min <= 8 ? 8 * rows_of(cluster_panel_smem<T, 8>(0)) : 0;
@@ -1567,7 +1572,8 @@ int lu_solve_wave(m25_ctx* ctx, const cx<TF>* A, int64_t lda, int n, const int32
     return M25_ERR_CUDA;
   }
   // M25_WAVE_CTAS: at most this many CTAs (a tuning knob; 0 or unset = one per block up to the device's fill)
-  static const int wave_cap = getenv("M25_WAVE_CTAS") ? atoi(getenv("M25_WAVE_CTAS")) : 0;
+  static const int wave_cap_env = getenv("M25_WAVE_CTAS") ? atoi(getenv("M25_WAVE_CTAS")) : 0;
+  const int wave_cap = ctx->tune_wave_ctas > 0 ? ctx->tune_wave_ctas : wave_cap_env;
   const int G = std::min(std::min(nblk, ctx->num_sms * occ), wave_cap > 0 ? wave_cap : nblk);
   StageTimer tm(ctx, ST_TRSV);
   if (!perm) {

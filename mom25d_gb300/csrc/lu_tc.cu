@@ -575,7 +575,7 @@ int lu_tc_update(m25_ctx* ctx, zf* A, int64_t lda, int r0, int c0, int m, int nc
   ta.pw = pw;
   ta.tiles_m = (m + kBM - 1) / kBM;
   ta.ntiles = ta.tiles_m * ((n2 + kBN - 1) / kBN);
-  ta.chunk = chunk;
+  ta.chunk = ctx->tune_tc_chunk > 0 ? ctx->tune_tc_chunk : chunk;
   ta.err = err;
   ta.counter = reinterpret_cast<int*>(ctx->Dw.as<char>() + 16) + slot;
   M25_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));

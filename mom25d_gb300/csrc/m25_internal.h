@@ -63,6 +63,10 @@ struct m25_ctx {
   int epoch = 0;            // value of a ready flag in the current sweep
   size_t yt_off = 0;        // offset of the tagged vector copy in the flag buffer (0: not placed yet)
   long long wave_spins = 0; // polls per ready-flag wait of the triangular solves (0: the default bound)
+  // tuning knobs (m25_ctx_set_tuning; 0: the process default)
+  int tune_cluster_min = 0; // smallest cluster of the LU panel (4, 8 or 16)
+  int tune_wave_ctas = 0;   // CTA cap of the triangular solves
+  int tune_tc_chunk = 0;    // k-blocks per TMEM accumulation of the tensor-core update
   // caller-provided scratch instead of the workspace buffers (LU panel
   // candidates + barrier words; triangular-solve flags, already zeroed)
   char* ext_scratch = nullptr;

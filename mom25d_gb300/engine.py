@@ -30,7 +30,7 @@ EXPORTS = ("m25_last_error", "m25_version", "m25_ctx_create", "m25_ctx_destroy",
            "m25_mlp_destroy", "m25_mlp_params", "m25_mlp_loss_grad", "m25_mlp_train", "m25_mlp_forward",
            "m25_ctx_mem_info", "m25_interp_create", "m25_interp_destroy", "m25_interp_store", "m25_interp_eval",
            "m25_interp_anchor", "m25_interp_point", "m25_deembed_waves", "m25_ctx_set_wait_limit",
-           "m25_deembed_fit_info")
+           "m25_deembed_fit_info", "m25_ctx_set_tuning", "m25_ports_set_excitations", "m25_deembed_coefs")
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
@@ -100,12 +100,15 @@ def load():
     lib.m25_deembed_debug.argtypes = [vp, vp, _f64p, _f64p, _f64p, _f64p]
     lib.m25_deembed_waves.argtypes = [vp, _f64p]
     lib.m25_deembed_fit_info.argtypes = [vp, _i32p]
+    lib.m25_ports_set_excitations.argtypes = [vp, C.c_int32]
+    lib.m25_deembed_coefs.argtypes = [vp, _f64p, _f64p]
     lib.m25_ctx_timing.argtypes = [vp, C.c_int, _f64p, C.POINTER(C.c_longlong)]
     lib.m25_dense_solve_noalloc.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, vp, vp, _i32p]
     lib.m25_lu_factor.argtypes = [vp, C.c_int32, C.c_int, vp, C.c_int64, _i32p, C.c_int, C.c_int32, _i32p]
     lib.m25_greens_remainder.argtypes = [vp, _f64p, _f64p]
     lib.m25_ctx_mem_info.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     lib.m25_ctx_set_wait_limit.argtypes = [vp, C.c_int64]
+    lib.m25_ctx_set_tuning.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
     lib.m25_interp_create.argtypes = [vp, C.c_int32, C.c_int32, _f64p, C.c_int32, C.c_int32, C.POINTER(vp)]
     lib.m25_interp_destroy.argtypes = [vp]
     lib.m25_interp_store.argtypes = [vp, C.c_int32, vp, C.c_int64, C.c_int, d, d]

@@ -275,6 +275,33 @@ class Layout:
         self.add_rect(*gap.rect(), layer=layer)
         return gap
 
+    def add_gap_port(self, name, a, b, width, layer="top", z_ref=50.0):
+        """An internal S-parameter port of reference impedance z_ref across a
+        delta gap: a copper bridge of `width` from pad point a to pad point b
+        as add_lumped makes it, the port's voltage taken from a to b (e.g. a
+        device pin to its ground pad)."""
+        gap = self.add_lumped(name, a, b, width, None, layer)
+        self.internal_ports.append(dict(kind="gap", name=name, z_ref=float(z_ref)))
+        return gap
+
+    def add_via_port(self, name, via, z_ref=50.0):
+        """An internal S-parameter port at the bottom of a via that ends on
+        the ground plane: a delta gap between the barrel and the plane (the
+        via fed through a hole in the ground), voltage barrel to ground, the
+        port current flowing down the via. `via`: index into vias, or the
+        Via itself."""
+        k = via if isinstance(via, (int, np.integer)) else next(
+            (i for i, v in enumerate(self.vias) if v is via), None)
+        if k is None or not 0 <= k < len(self.vias):
+            raise ValueError(f"via port {name}: no such via in the layout")
+        if self.vias[k].bottom != "gnd":
+            raise ValueError(f"via port {name}: the via must end on the ground plane (bottom 'gnd')")
+        taken = {q.name for q in self.lumped} | {q.name for q in self.ports} | {q["name"] for q in self.internal_ports}
+        if name in taken:
+            raise ValueError(f"via port {name}: the name is already taken")
+        self.internal_ports.append(dict(kind="via", name=name, via=int(k), z_ref=float(z_ref)))
+        return k
+
     def add_component(self, model, gaps):
         """A multi-port block (network.Touchstone, or a .sNp path) across the
         named lumped gaps, port k of the model across gaps[k]; add those gaps
@@ -568,6 +595,25 @@ class Mesh:
         idx, s_ends, toward = self._feed_edges(port)
         on = np.all(np.abs(s_ends - s) < 1e-6 * port.width, axis=1)
         return idx[on], toward[on]
+
+    def internal_port_vectors(self):
+        """(N, n_internal): the delta-gap vector of each internal port of the
+        layout, in order: a gap port's column of lumped_vectors (current a ->
+        b), a via port's unit vector on the via's segment that ends on the
+        ground plane (current flowing down into the plane)."""
+        ports = list(getattr(self.layout, "internal_ports", []))
+        names = [q.name for q in getattr(self.layout, "lumped", [])]
+        Lm = self.lumped_vectors() if names else None
+        out = np.zeros((self.n_unknowns, len(ports)))
+        for k, ip in enumerate(ports):
+            if ip["kind"] == "gap":
+                out[:, k] = Lm[:, names.index(ip["name"])]
+                continue
+            seg = [i for i, g in enumerate(self.via_segments) if g["via"] == ip["via"] and g["bottom"] == "gnd"]
+            if len(seg) != 1:
+                raise ValueError(f"via port {ip['name']}: its via has no segment ending on the ground plane")
+            out[self.n_basis + seg[0], k] = 1.0
+        return out
 
     def lumped_vectors(self):
         """(N, n_lumped): column k holds the signed edge lengths of gap k's

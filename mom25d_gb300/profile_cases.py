@@ -3,13 +3,17 @@
     python -m mom25d_gb300.profile_cases fill  --workload bandpass --precision fp64 [--reps 2]
     python -m mom25d_gb300.profile_cases point --workload lpf --precision mixed [--reps 1]
     python -m mom25d_gb300.profile_cases lu --n 4096 [--simt] [--reps 1]
+    python -m mom25d_gb300.profile_cases batch [--variants 16] [--nfreq 128] [--workers 8]
 
 `fill` builds the mesh geometry and one frequency's Green's tables, then
 runs the impedance fill `reps` times (device output, no host copy);
 `point` runs `reps` full frequency points (tables, fill, LU + solve,
 de-embedding); `lu` factors a seeded random n x n complex64 matrix on the
-device (tensor-core trailing updates unless --simt). Each exits non-zero on
-any engine error.
+device (tensor-core trailing updates unless --simt); `batch` sweeps the
+band-pass variants 0 .. variants - 1 at nfreq frequencies 1-12 GHz (mixed
+precision) once variant by variant (each a concurrent sweep on `workers`
+contexts) and once as one VariantBatch, and prints the points per second of
+both. Each exits non-zero on any engine error.
 """
 
 import argparse
@@ -24,7 +28,10 @@ from .solver import PRECISIONS, Solver
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("mode", choices=["fill", "point", "lu"])
+    ap.add_argument("mode", choices=["fill", "point", "lu", "batch"])
+    ap.add_argument("--variants", type=int, default=16, help="batch mode: band-pass variants")
+    ap.add_argument("--nfreq", type=int, default=128, help="batch mode: frequencies per variant")
+    ap.add_argument("--workers", type=int, default=8, help="batch mode: points in flight")
     ap.add_argument("--n", type=int, default=4096, help="matrix size of the lu mode")
     ap.add_argument("--simt", action="store_true", help="lu mode: SIMT trailing updates")
     ap.add_argument("--timing", action="store_true", help="lu mode: print the stage times (CUDA events)")
@@ -35,6 +42,8 @@ def main():
     args = ap.parse_args()
     if args.mode == "lu":
         return lu_case(args)
+    if args.mode == "batch":
+        return batch_case(args)
     import mom25d_gb300 as G
 
     kw = {"k": 0} if args.workload == "bandpass" else {}
@@ -90,6 +99,40 @@ def lu_case(args):
         print("stage ms per factorisation:", {k: round(v / args.reps, 3) for k, v in zip(names, ms) if v})
     print(f"lu ok: n={n} info={int(info[0])} tensor_cores={not args.simt}")
     ctx.close()
+
+
+def batch_case(args):
+    import json
+    import time
+
+    import mom25d_gb300 as G
+
+    from .batch import VariantBatch
+
+    sols, sizes = [], []
+    for k in range(args.variants):
+        lay, st, mesh, _ = workloads.build(G, "bandpass", k=k)
+        sols.append(Solver(mesh, st, verbose=False, precision="mixed"))
+        sizes.append(mesh.n_unknowns)
+    f = np.linspace(1, 12, args.nfreq) * 1e9
+    for s in sols:  # geometry, contexts and buffers of every variant, untimed
+        s.sweep(f[:args.workers], workers=args.workers)
+    t0 = time.time()
+    seq = [s.sweep(f, workers=args.workers) for s in sols]
+    t_seq = time.time() - t0
+    batch = VariantBatch(sols)
+    batch.sweep(f[:args.workers], workers=args.workers)  # the worker contexts' set-up, untimed
+    res = batch.sweep(f, workers=args.workers)
+    info = res[0].info["batch"]
+    dS = max(float(np.abs(a.S - b.S).max()) for a, b in zip(res, seq))
+    out = dict(variants=args.variants, N=sizes, freqs=args.nfreq, workers=args.workers, points=info["points"],
+               variant_by_variant_points_per_s=round(info["points"] / t_seq, 2),
+               batch_points_per_s=round(info["points_per_s"], 2), batch_workers=info["workers"],
+               max_dS_batch_vs_separate=dS, tuning=batch.tuning is not None)
+    print(json.dumps(out))
+    batch.close()
+    for s in sols:
+        s.close()
 
 
 if __name__ == "__main__":

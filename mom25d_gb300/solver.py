@@ -343,15 +343,27 @@ class Solver:
         if getattr(mesh, "level_order", None) != order:
             mesh.assign_levels(order)
         self.ports = mesh.layout.ports
+        # internal ports (gap and via ports): S-parameter ports of fixed
+        # reference impedance, excited and terminated across a delta gap
+        self.iports = list(getattr(mesh.layout, "internal_ports", []))
         if not self.ports:
-            raise ValueError("layout has no ports")
-        if getattr(mesh.layout, "internal_ports", None):
-            raise ValueError("internal ports are not part of this engine")
+            raise ValueError("layout has no feed ports (this engine de-embeds at least one feed)")
         # lumped components across delta gaps (one-port values and multi-port
-        # blocks): loaded after the solve (Woodbury)
+        # blocks): loaded after the solve (Woodbury); via ports add their
+        # columns after the lumped gaps (a gap port is a lumped gap)
         self.lumped = list(getattr(mesh.layout, "lumped", []))
         self.components = list(getattr(mesh.layout, "components", []))
         self.Lm = mesh.lumped_vectors() if self.lumped else None
+        self.iport_index = []  # column of each internal port in Lm
+        if self.iports:
+            names = [q.name for q in self.lumped]
+            vecs = mesh.internal_port_vectors()
+            vias = [k for k, ip in enumerate(self.iports) if ip["kind"] == "via"]
+            if vias:
+                self.Lm = vecs[:, vias] if self.Lm is None else np.hstack([self.Lm, vecs[:, vias]])
+            col = {k: len(names) + i for i, k in enumerate(vias)}
+            self.iport_index = [names.index(ip["name"]) if ip["kind"] == "gap" else col[k]
+                                for k, ip in enumerate(self.iports)]
         self.values = {}  # per-sweep overrides of lumped values
         self.method = "dense"
         self.precision = precision
@@ -466,6 +478,8 @@ class Solver:
         h = C.c_void_p()
         E.check(self.ctx.lib.m25_ports_create(self.ctx.h, self.geometry().h, C.byref(d), C.byref(h)))
         self._ports = E.Handle(self.ctx, h, self.ctx.lib.m25_ports_destroy)
+        if self.iports:  # the feeds' fits take the internal ports' excitations too
+            E.check(self.ctx.lib.m25_ports_set_excitations(h, len(self.ports) + len(self.iports)))
         return self._ports
 
     # ---------------------------------------------------------------- path
@@ -497,7 +511,10 @@ class Solver:
         return Z
 
     def port_excitations(self):
-        return np.stack([pm.excitation for pm in self.pm], 1)
+        """One column per port: a 1 V delta gap at each feed, then a 1 V
+        source (in series with z_ref) at each internal port."""
+        cols = [pm.excitation for pm in self.pm] + [self.Lm[:, c] for c in self.iport_index]
+        return np.stack(cols, 1)
 
     def solve_currents(self, freq, excitations=None, greens=None, Z=None):
         """RWG (+ via segment) coefficients (N, Nexc) for the given excitations
@@ -513,21 +530,25 @@ class Solver:
 
     def lumped_impedance(self, freq):
         """D (n_lumped, n_lumped): the impedance of the components across the
-        lumped gaps at freq: a multi-port block's impedance matrix across its
-        gaps, a one-port value on the diagonal, OPEN where none
-        (Engine/mom25d/solver.py:1039-1062 without internal ports)."""
+        lumped gaps (and via ports) at freq: an internal port's z_ref, a
+        multi-port block's impedance matrix across its gaps, a one-port value
+        on the diagonal, OPEN where none (Engine/mom25d/solver.py:1039-1062)."""
         from .lumped import as_value, parse
 
-        D = np.zeros((len(self.lumped), len(self.lumped)), complex)
+        nl = 0 if self.Lm is None else self.Lm.shape[1]
+        D = np.zeros((nl, nl), complex)
         names = [q.name for q in self.lumped]
         used = set()
+        for ip, c in zip(self.iports, self.iport_index):  # internal ports: terminated in z_ref
+            D[c, c] = ip["z_ref"]
+            used.add(c)
         for model, gaps in getattr(self, "components", []):
             ix = [names.index(n) for n in gaps]
             D[np.ix_(ix, ix)] = model.z(freq)
             used.update(ix)
         for k, q in enumerate(self.lumped):
             v = self.values.get(q.name, getattr(q, "value", None))
-            if k in used and v is None:
+            if k in used and (v is None or k in self.iport_index):
                 continue
             if isinstance(v, str):
                 v = parse(v)
@@ -548,10 +569,13 @@ class Solver:
         return self.Lm.T @ x
 
     def _lumped_point(self, f, g, Z, keep_currents):
-        """A point with lumped loads: one solve for the port and gap
-        excitations, the loads by Woodbury on the host, then the
-        de-embedding of the loaded currents on the device."""
-        P = len(self.ports)
+        """A point with lumped loads or internal ports: one solve for the
+        port and gap excitations, the loads by Woodbury on the host, then the
+        de-embedding of the loaded currents on the device; with internal
+        ports the feeds' wave fits take every port's excitation and S is
+        assembled here (Engine/mom25d/solver.py:1305-1325)."""
+        P, ni = len(self.ports), len(self.iports)
+        n = P + ni
         E0 = self.port_excitations()
         B = np.hstack([E0, self.Lm])
         prec = "fp64" if self.precision == "fp64" else "mixed"
@@ -564,7 +588,7 @@ class Solver:
             # the mixed refinement stopped above its target: this point in fp64
             X = dense_solve(Z, B, precision="fp64", ctx=self.ctx)
             steps = -1
-        x = np.ascontiguousarray(self._load_lumped(X[:, :P], X[:, P:], f))
+        x = np.ascontiguousarray(self._load_lumped(X[:, :n], X[:, n:], f))
         S = np.zeros((P, P), complex)
         z0 = np.zeros(P)
         gam = np.zeros(P, complex)
@@ -575,9 +599,34 @@ class Solver:
         E.check(self.ctx.lib.m25_deembed(self.ctx.h, self.geometry().h, g.h, self.port_data().h, x.ctypes.data,
                                          E.M25_ON_HOST, E.ptr(b0), F(S), E.ptr(z0), F(gam), F(zl), E.ptr(res)))
         self._warn_fit_bounds(f)
-        S, z0 = self._fixed_z0(S, z0)
-        return S, z0, gam, zl, res, (x if keep_currents else None), dict(
-            refine_steps=steps, fp64_fallback=steps < 0, waves=self.last_waves())
+        info = dict(refine_steps=steps, fp64_fallback=steps < 0)
+        if not ni:
+            S, z0 = self._fixed_z0(S, z0)
+            info["waves"] = self.last_waves()
+            return S, z0, gam, zl, res, (x if keep_currents else None), info
+        # internal ports: their rows of the wave amplitudes from the current
+        # through each source, V = Vs - z_ref I (current-normalised power waves)
+        A, Bc = np.zeros((P, n), complex), np.zeros((P, n), complex)
+        E.check(self.ctx.lib.m25_deembed_coefs(self.port_data().h, F(A), F(Bc)))
+        zi = np.array([ip["z_ref"] for ip in self.iports], float)
+        Ii = self.Lm[:, self.iport_index].T @ x
+        Vs = np.zeros((ni, n))
+        Vs[:, P:] = np.eye(ni)
+        Ac = np.vstack([A, Vs / (2 * zi[:, None])])
+        Bc = np.vstack([Bc, -(Vs - 2 * zi[:, None] * Ii) / (2 * zi[:, None])])
+        SI = -Bc @ np.linalg.inv(Ac)
+        zr = np.zeros(n)
+        if self.z0_fixed is None:
+            zr[:P] = reciprocal_z0(SI[:P, :P], zl.real, list(self.groups.values()))
+            zr[:P] = anchor_z0(SI, zr[:P], zi, list(self.groups.values()))
+        else:
+            zr[:P] = self.z0_fixed
+        zr[P:] = zi
+        d = np.sqrt(zr)
+        S = d[:, None] * SI / d[None, :]
+        info["waves"] = Ac
+        return (S, zr, np.r_[gam, np.zeros(ni)], np.r_[zl, zi.astype(complex)], np.r_[res, np.zeros(ni)],
+                (x if keep_currents else None), info)
 
     def point(self, f, keep_currents=False):
         """One frequency of the sweep on the device: (S, z0, gamma, z0_line, residual, x or None, info)."""
@@ -759,7 +808,7 @@ class Solver:
                 ip.fill_all(freqs)
             if not ip._resident or self.Lm is not None:
                 workers = 1
-        nf, P = len(freqs), len(self.ports)
+        nf, P = len(freqs), len(self.ports) + len(self.iports)
         S = np.zeros((nf, P, P), complex)
         gam = np.zeros((nf, P), complex)
         zl = np.zeros((nf, P), complex)
@@ -844,7 +893,7 @@ class Solver:
             info.update(interp_fills=ip.n_fills, interp_anchors=len(ip.anchors), interp_fill_seconds=ip.fill_time)
             if interp is not ip:
                 ip.close()  # made here ("auto"); a caller's FreqInterp keeps its anchors
-        return SweepResult(freqs, S, zr, gam, zl, res, [p.name for p in self.ports],
+        return SweepResult(freqs, S, zr, gam, zl, res, [p.name for p in self.ports] + [ip["name"] for ip in self.iports],
                            cur if keep_currents else None, waves, info=info)
 
     def close(self):
@@ -858,6 +907,62 @@ class Solver:
         self._ports = self._geom = None
         if getattr(self, "_ctx_owner", True):
             self.ctx.close()
+
+
+def reciprocal_z0(SI, zphi, groups, prior=1e-4):
+    """Reference impedances of the feeds that make S = D SI D^-1 reciprocal
+    (D = diag(sqrt(Z0)): reciprocity fixes Z0_i / Z0_j = |SI_ji / SI_ij|
+    between coupled groups), with the scalar-potential estimates zphi as a
+    weak prior that sets the level and the groups that barely couple: a
+    weighted least-squares fit of log Z0 per group, weights the square of
+    the smaller coupling (Engine/mom25d/solver.py:1357-1427). The same fit
+    as the device's de-embedding, for S assembled on the host."""
+    zphi = np.asarray(zphi, float)
+    if len(groups) == 1:
+        return zphi.copy()
+    gid = np.empty(len(zphi), int)
+    for k, members in enumerate(groups):
+        gid[members] = k
+    rows, rhs, wts = [], [], []
+    for i in range(len(gid)):
+        for j in range(i + 1, len(gid)):
+            w = min(abs(SI[i, j]), abs(SI[j, i])) ** 2
+            if gid[i] != gid[j] and w > 0:
+                r = np.zeros(len(groups))
+                r[gid[i]], r[gid[j]] = 1.0, -1.0
+                rows.append(r)
+                rhs.append(np.log(abs(SI[j, i] / SI[i, j])))
+                wts.append(w)
+    for k, members in enumerate(groups):
+        r = np.zeros(len(groups))
+        r[k] = 1.0
+        rows.append(r)
+        rhs.append(np.log(np.mean(zphi[members])))
+        wts.append(prior)
+    sw = np.sqrt(wts)
+    logz = np.linalg.lstsq(np.array(rows) * sw[:, None], np.array(rhs) * sw, rcond=None)[0]
+    logz += np.mean(np.log(zphi)) - np.mean(logz[gid])  # the scalar-potential level
+    return np.exp(logz[gid])
+
+
+def anchor_z0(SI, zfeed, zi, groups, prior=1e-4):
+    """Feed reference impedances refined by reciprocity with the internal
+    ports, whose z_ref is exact: per feed group the coupling-weighted mean of
+    log(z_i |SI_ij / SI_ji|) over internal ports i and members j, the feed
+    estimate as a weak prior (Engine/mom25d/solver.py:1336-1355)."""
+    P = len(zfeed)
+    z = np.array(zfeed, float)
+    for members in groups:
+        num, den = prior * np.log(np.mean(z[members])), prior
+        for j in members:
+            for k, zk in enumerate(zi):
+                i = P + k
+                w = min(abs(SI[i, j]), abs(SI[j, i])) ** 2
+                if w > 0:
+                    num += w * np.log(zk * abs(SI[i, j] / SI[j, i]))
+                    den += w
+        z[members] = np.exp(num / den)
+    return z
 
 
 def values_digest(values, lumped=(), components=()):

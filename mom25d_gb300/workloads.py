@@ -17,6 +17,8 @@ returns (layout, stack, mesh keyword arguments, frequencies [Hz]).
   shunt_via  short line with a via to ground (small N, test case)
   lumped_line  two line sections joined by a lumped component (R 20 + L 0.5n) across a gap
   component_line  three line sections, a 2-port S-parameter block across two open gaps
+  gap_port_line   a series gap in a line with an internal gap port across it
+  via_port_line   a line with a via to ground fed by an internal via port
 """
 
 import numpy as np
@@ -182,3 +184,34 @@ BUILDERS = dict(tee=tee, lpf=lpf, bandpass=bandpass, via=via, gcpw=gcpw, line=li
 def build(api, name, **kw):
     lay, stack, mkw, freqs = BUILDERS[name](api, **kw)
     return lay, stack, lay.mesh(**mkw), freqs
+
+
+def gap_port_line(api):
+    """A 0.5 mm series gap in a 50 ohm line on 0.254 mm eps_r 3.66 with an
+    internal gap port across it (Layout.add_gap_port, z_ref 50 ohm)."""
+    W, G = 0.5561 * mm, 0.5 * mm
+    lay = api.Layout()
+    lay.add_rect(-5 * mm, -W / 2, -G / 2, W / 2)
+    lay.add_rect(G / 2, -W / 2, 5 * mm, W / 2)
+    lay.add_port("P1", (-5 * mm, 0), "-x", W, 10 * mm)
+    lay.add_port("P2", (5 * mm, 0), "+x", W, 10 * mm)
+    lay.add_gap_port("G", (-G / 2, 0), (G / 2, 0), W)
+    sub = api.Substrate(3.66, 0.254 * mm, 0.003, SIGMA)
+    return lay, sub, dict(max_cell=0.4 * mm, edge_cell=0.05 * mm), np.array([1.0, 4.0, 8.0]) * GHz
+
+
+def via_port_line(api):
+    """A 50 ohm line with a via to ground at its middle, fed at the ground
+    plane by an internal via port (Layout.add_via_port, z_ref 50 ohm)."""
+    W = 0.5561 * mm
+    lay = api.Layout()
+    lay.add_rect(-3 * mm, -W / 2, 3 * mm, W / 2)
+    lay.add_port("P1", (-3 * mm, 0), "-x", W, 6 * mm)
+    lay.add_port("P2", (3 * mm, 0), "+x", W, 6 * mm)
+    lay.add_via(0, 0, drill=0.3 * mm, pad=W)
+    lay.add_via_port("V", 0)
+    sub = api.Substrate(3.66, 0.254 * mm, 0.003, SIGMA)
+    return lay, sub, dict(max_cell=0.4 * mm, edge_cell=0.05 * mm), np.array([3.0, 6.0, 9.0]) * GHz
+
+
+BUILDERS.update(gap_port_line=gap_port_line, via_port_line=via_port_line)

@@ -244,37 +244,61 @@ def floor_all(only=None):
 
 
 def x_floor_case(name, f, kw=None, eps=1e-13, seeds=2):
-    """The conditioning floor of the currents: mom25d's x at f against its x
-    from the same Z with every entry multiplied by 1 + eps (n1 + j n2)
-    (n standard normal, seeded): max |dx| / max |x| over the seeds. An
-    implementation whose Z agrees with mom25d's to eps cannot be expected to
-    give its x closer than this."""
+    """The conditioning floor of every stage of a point: mom25d's currents x
+    from its Z at f, and from the same Z with every entry multiplied by
+    1 + eps (n1 + j n2) (n standard normal, seeded), then the charges q,
+    line voltages phi, cut currents I and voltages V and S of each (its own
+    de-embedding). Returns {stage: max over the seeds of max |d| / max |.|}
+    (S: max |dS|). An implementation whose Z agrees with mom25d's to eps
+    cannot be expected to agree closer than this."""
     lay, stack, mkw, _ = workloads.BUILDERS[name](ref, **(kw or {}))
     m = lay.mesh(**mkw)
     sol = ref.Solver(m, stack, verbose=False, method="dense")
+    cache = cache_points(sol)
     g = sol.greens(f)
     Z = sol.impedance(f, g)
     B = sol.port_excitations()
-    x0 = ref_solver._dense_solve(Z.copy(), B)
-    worst = 0.0
+    solve = sol.solve_currents
+
+    def stages(x):
+        q = sol.charges(x, g.omega)
+        st = stage_arrays(sol, g, x, q)
+        sol.solve_currents = lambda fr, **k: x
+        try:
+            S = sol.sweep([f], interp=None).S[0]
+        finally:
+            sol.solve_currents = solve
+        return dict(x=x, q=q, phi=st["phi"], I=st["I"], V=st["V"], S=S)
+
+    base = stages(ref_solver._dense_solve(Z.copy(), B))
+    worst = {k: 0.0 for k in base}
     for seed in range(seeds):
         rng = np.random.default_rng(seed)
         Zp = Z * (1 + eps * (rng.standard_normal(Z.shape) + 1j * rng.standard_normal(Z.shape)))
-        x = ref_solver._dense_solve(Zp, B)
-        worst = max(worst, float(np.abs(x - x0).max() / np.abs(x0).max()))
-    print(f"x floor {name} {kw or ''}: {worst:.2e}", flush=True)
+        other = stages(ref_solver._dense_solve(Zp, B))
+        del Zp
+        for k in base:
+            d = float(np.abs(other[k] - base[k]).max())
+            worst[k] = max(worst[k], d if k == "S" else d / float(np.abs(base[k]).max()))
+    del cache
+    print(f"stage floors {name} {kw or ''}: " + ", ".join(f"{k} {v:.1e}" for k, v in worst.items()), flush=True)
     return worst
 
 
 def x_floor_all(names):
-    """x_floor.npz: the conditioning floor of x at each fixture's f0."""
+    """x_floor.npz: the conditioning floors of x (key: the fixture's name)
+    and of each stage (key: name_stage) at each fixture's f0."""
     path = os.path.join(HERE, "x_floor.npz")
-    out = dict(np.load(path)) if os.path.exists(path) else {}
-    out["eps"] = np.array(1e-13)
     for key in names:
         g = np.load(os.path.join(HERE, key + ".npz"))
         base, kw = (("bandpass", dict(k=int(key.split("_")[1]))) if key.startswith("bandpass_") else (key, None))
-        out[key] = np.array(x_floor_case(base, float(g["f0"]), kw))
+        floors = x_floor_case(base, float(g["f0"]), kw)
+        # read the file again just before writing: other runs may have added cases
+        out = dict(np.load(path)) if os.path.exists(path) else {}
+        out["eps"] = np.array(1e-13)
+        out[key] = np.array(floors["x"])
+        for k, v in floors.items():
+            out[f"{key}_{k}"] = np.array(v)
         np.savez_compressed(path, **out)
 
 
@@ -307,6 +331,22 @@ def interp_case(name, interp_kw=None, nfreq=None, zrows=None):
     out.update(result_arrays(r))
     np.savez_compressed(os.path.join(HERE, f"{name}_interp.npz"), **out)
     print(f"{name} interp: N={m.n_unknowns} {len(freqs)} freqs, {len(ip.anchors)} anchors, {dt:.1f} s", flush=True)
+
+
+def iport_case(name):
+    """Internal ports (Layout.add_gap_port / add_via_port): mom25d's sweep with
+    the internal ports' excitations, loads and S extension
+    (Engine/mom25d/solver.py:1029-1070, 1305-1356)."""
+    lay, stack, mkw, freqs = workloads.BUILDERS[name](ref)
+    m = lay.mesh(**mkw)
+    sol = ref.Solver(m, stack, verbose=False, method="dense")
+    r = sol.sweep(freqs, interp=None, keep_currents=True)
+    out = dict(N=m.n_unknowns, mesh_sha=mesh_digest(m), freqs=freqs, iport_vectors=m.internal_port_vectors(),
+               Lm=sol.Lm, iport_index=np.array(sol.iport_index), port_names=np.array(r.port_names),
+               x0=r.currents[0], waves=r.waves)
+    out.update(result_arrays(r))
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    print(f"{name}: N={m.n_unknowns} ports {r.port_names}", flush=True)
 
 
 def write_block(path, freqs):
@@ -413,6 +453,7 @@ def main():
                     help="only the conditioning floor of x at the f0 of the given fixtures")
     ap.add_argument("--variants", action="store_true", help="only band-pass variants 3, 7, 11 and 14")
     ap.add_argument("--lossless", action="store_true", help="only the lossless line (mom25d's bounded beta fit)")
+    ap.add_argument("--iports", action="store_true", help="only the internal-port cases (gap port, via port)")
     ap.add_argument("--gcpw", action="store_true",
                     help="only the grounded CPW (N = 25284: ~30 GB of memory, ~20 min per frequency)")
     args = ap.parse_args()
@@ -435,6 +476,10 @@ def main():
         x_floor_all(args.xfloor)
         return
     fb = np.linspace(1, 12, 128) * 1e9
+    if args.iports:
+        iport_case("gap_port_line")
+        iport_case("via_port_line")
+        return
     if args.lossless:
         case("line_lossless", zrows=np.arange(0, 546, 37), sweep_freqs=[2e9, 5e9, 7e9])
         return

@@ -153,3 +153,32 @@ def test_sweep_sharded_assembles_the_full_result(tmp_path, values):
     assert list(got["names"]) == ["P1", "P2"]
     r = 0.0 if values is None else values["Z1"]
     assert np.all(got["S"][:, 0, 1] == 0.1 + r)
+
+
+def test_batch_point_order_is_longest_first():
+    """Batched variants hand out their points largest N first (the LPT rule
+    on the N^3 cost), each variant's frequencies in order."""
+    from mom25d_gb300.batch import point_order
+
+    order = point_order([1524, 4972, 3064], [2, 3, 1])
+    assert order == [(1, 0), (1, 1), (1, 2), (2, 0), (0, 0), (0, 1)]
+
+
+def test_tuning_table_rows_by_size(tmp_path):
+    """A tuning table picks the first row whose n_max covers N (the last one
+    beyond) and round-trips through its JSON file."""
+    import json
+
+    from mom25d_gb300.autotune import Tuning, load_table
+
+    rows = [dict(n_max=None, panel_cluster_min=16, wave_ctas=0, tc_chunk=1),
+            dict(n_max=2000, panel_cluster_min=4, wave_ctas=16, tc_chunk=2)]
+    p = tmp_path / "t.json"
+    p.write_text(json.dumps(dict(rows=rows)))
+    t = load_table(str(p))
+    assert t.knobs(1500) == (4, 16, 2)
+    assert t.knobs(2000) == (4, 16, 2)
+    assert t.knobs(9000) == (16, 0, 1)
+    assert Tuning.fixed(tc_chunk=2).knobs(10 ** 6) == (0, 0, 2)
+    with pytest.raises(ValueError):
+        Tuning([dict(n_max=1)])

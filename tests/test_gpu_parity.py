@@ -2,15 +2,17 @@
 mom25d itself (tests/golden, make_golden.py), on every workload that has one.
 
 Bars:
-- before the wave fit (charges q, line voltages phi, cut currents I and cut
-  voltages V): 1e-9 relative to the largest entry, fp64 path;
-- the currents x: 1e-9, or three times their conditioning floor where that
-  is larger (tests/golden/x_floor.npz: mom25d's own x moves by 5e-10 to
-  2e-8 relative when its Z is perturbed by 1e-13, the level at which the
-  fills agree; the part of x that moves carries no charge, so q, phi, I and
-  V still agree to 1e-12);
+- every stage before the wave fit (currents x, charges q, line voltages phi,
+  cut currents I and cut voltages V), fp64 path: 1e-9 relative to the
+  largest entry, or three times that stage's conditioning floor where that is
+  larger. The floors (tests/golden/x_floor.npz, made by running mom25d) are
+  how far mom25d's own stage moves when its Z is perturbed by 1e-13 relative,
+  the level at which the two fills agree: x by 5e-10 to 3e-7 (the part of x
+  that moves carries almost no charge), q, phi, I and V by far less, except
+  on the ill-conditioned N = 25284 grounded CPW at 1 GHz;
 - S of the fp64 path: three times the floor of mom25d's own wave fit
-  (conftest.fit_floor: 8e-9 to 6e-8 by workload);
+  (conftest.fit_floor: 8e-9 to 6e-8 by workload), or three times the spread
+  of mom25d's S under the same Z perturbation where that is larger;
 - S of the mixed path: 1e-5.
 """
 
@@ -30,11 +32,25 @@ pytestmark = pytest.mark.gpu
 STAGE_TOL = 1e-9
 
 
-def x_tol(name):
-    """The bar for the currents x of a workload (see the module docstring)."""
+def stage_floor(name, stage):
+    """How far mom25d's own value of a stage moves under a 1e-13 relative
+    perturbation of its Z (0 when not measured)."""
     path = os.path.join(GOLDEN, "x_floor.npz")
-    d = np.load(path) if os.path.exists(path) else {}
-    return max(STAGE_TOL, 3.0 * float(d[name])) if name in d else STAGE_TOL
+    if not os.path.exists(path):
+        return 0.0
+    d = np.load(path)
+    key = f"{name}_{stage}" if f"{name}_{stage}" in d.files else (name if stage == "x" and name in d.files else None)
+    return float(d[key]) if key else 0.0
+
+
+def stage_tol(name, stage):
+    """The bar of one pre-fit stage (see the module docstring)."""
+    return max(STAGE_TOL, 3.0 * stage_floor(name, stage))
+
+
+def s_tol(name):
+    """The fp64 bar of S: the wave-fit floor, or the Z-perturbation spread."""
+    return max(fp64_tol(name), 3.0 * stage_floor(name, "S"))
 
 
 def _have(name):
@@ -70,9 +86,9 @@ def test_prefit_stages_match_reference(gpu, name):
             ref = g[key]
             assert got.shape == ref.shape, (key, got.shape, ref.shape)
             errs[key] = np.abs(got - ref).max() / np.abs(ref).max()
-        print(name, {k: f"{v:.1e}" for k, v in errs.items()}, f"x bar {x_tol(name):.1e}")
-        assert errs["x"] <= x_tol(name), errs
-        assert max(v for k, v in errs.items() if k != "x") <= STAGE_TOL, errs
+        bars = {k: stage_tol(name, k) for k in errs}
+        print(name, {k: f"{v:.1e} (bar {bars[k]:.1e})" for k, v in errs.items()})
+        assert all(errs[k] <= bars[k] for k in errs), (errs, bars)
     finally:
         sol.close()
 
@@ -86,7 +102,7 @@ def test_bandpass_variant_sweeps_match_reference(gpu, name):
     g = golden(name)
     lay, st, m, _ = _build(name)
     assert m.n_unknowns == g["N"]
-    for prec, tol in (("fp64", fp64_tol(name)), ("mixed", 1e-5)):
+    for prec, tol in (("fp64", s_tol(name)), ("mixed", 1e-5)):
         sol = Solver(m, st, verbose=False, precision=prec)
         try:
             r = sol.sweep(g["freqs"], workers=2)
@@ -115,7 +131,7 @@ def test_gcpw_large_workload_matches_reference(gpu):
         print("gcpw max |dS| per frequency", dS, r.info)
         fb = set(r.info["fp64_fallback"])
         for i, f in enumerate(g["freqs"]):
-            assert dS[i] < (fp64_tol("gcpw") if float(f) in fb else 1e-5), (f, dS[i])
+            assert dS[i] < (s_tol("gcpw") if float(f) in fb else 1e-5), (f, dS[i])
     finally:
         sol.close()
 
@@ -132,9 +148,9 @@ def test_gcpw_prefit_stages_match_reference(gpu):
         q, phi, I, V = sol.last_deembed()
         errs = {k: np.abs(got - g[k]).max() / np.abs(g[k]).max()
                 for k, got in (("x", x), ("q", q), ("phi", phi), ("I", I), ("V", V))}
-        print("gcpw", {k: f"{v:.1e}" for k, v in errs.items()}, f"x bar {x_tol('gcpw'):.1e}")
-        assert errs["x"] <= x_tol("gcpw"), errs
-        assert max(v for k, v in errs.items() if k != "x") <= STAGE_TOL, errs
+        bars = {k: stage_tol("gcpw", k) for k in errs}
+        print("gcpw", {k: f"{v:.1e} (bar {bars[k]:.1e})" for k, v in errs.items()})
+        assert all(errs[k] <= bars[k] for k in errs), (errs, bars)
         Z = sol.impedance(float(g["f0"]))
         rows = g["Z_rows_idx"]
         assert np.abs(Z[rows] - g["Z_rows"]).max() <= 1e-11 * np.abs(g["Z_rows"]).max()
