@@ -295,10 +295,12 @@ def run_ours(args, rank, world, local):
     gemm_flops = update_flops(n)
     achieved = gemm_flops / (lu_ms * 1e-3) / 1e12 if lu_ms else None
     bf16 = peaks.get("bf16_tflops") or 1900.0  # burst: the kernel is timed alone
-    # DRAM traffic of the updates per flop, from the ncu capture of all 63
-    # update launches of an n = 4096 factorisation (2.173 GB for 1.769e11
-    # flops); bytes and flops of a block's update both scale as m^2
-    traffic = 2.173e9 / 1.769e11 * gemm_flops
+    # DRAM traffic of the updates per flop, from the ncu capture of all 78
+    # update launches of an n = 4096 factorisation in super-blocks of 256
+    # columns (1.553 GB for 1.769e11 flops):
+    # the rank-256 updates, which carry nearly all of it, read and write C
+    # and their operands in proportion to their flops
+    traffic = 1.553e9 / 1.769e11 * gemm_flops
     roof = {"kernel": "tc_gemm_kernel: LU trailing update (tcgen05 3xTF32, complex64), all launches of one point",
             "bound": "tensor", "achieved": round(achieved, 2) if achieved else None, "peak": bf16, "unit": "TFLOP/s",
             "frac": round(achieved / bf16, 4) if achieved else None, "traffic": round(traffic),

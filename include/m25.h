@@ -171,7 +171,7 @@ typedef struct {
   const m25_mlp* surrogate;
   double sur_a, sur_rho_ref, sur_fmin, sur_fmax;
   const double* sur_scale;    /* (2 NC) */
-  int32_t sur_ncheck;         /* 4 .. 64 */
+  int32_t sur_ncheck;         /* 4 .. 128 */
   double sur_tol;
 } m25_greens_desc;
 

@@ -406,8 +406,11 @@ __global__ void sur_features_kernel(int n, const double* __restrict__ rho, doubl
   X[2 * i + 1] = (float)(2.0 * (f - fmin) / (fmax - fmin) - 1.0);
 }
 
-constexpr int kSurMaxCheck = 48;
+constexpr int kSurMaxCheck = 128;
 constexpr int kSurMaxCols = 2 * 3 * kMaxLevSq;
+// dynamic shared memory of the judge: the residuals and spline moments at
+// the K check radii, K x 2 NC doubles each
+inline size_t sur_judge_smem(int K, int NC) { return sizeof(double) * 2 * (size_t)K * 2 * NC; }
 
 // Residual correction and judge (one CTA): natural cubic splines in rho of
 // the Sommerfeld-minus-network residual of every real column through the K
@@ -419,30 +422,34 @@ __global__ void __launch_bounds__(256) sur_judge_kernel(int NC, int n, const dou
                                                         const float* __restrict__ ychk, const double* __restrict__ scale,
                                                         const zd* __restrict__ schk, double tol, zd* __restrict__ res,
                                                         int* __restrict__ flag, double* __restrict__ err_out) {
-  __shared__ double r[kSurMaxCheck][kSurMaxCols], M[kSurMaxCheck][kSurMaxCols];
+  extern __shared__ double judge_smem[];
   __shared__ double red_e[8], red_s[8];
   const int ncol = 2 * NC;
   const int c = threadIdx.x;
+  double* rs = judge_smem;              // residual at check radius k, column c: rs[k ncol + c]
+  double* Ms = judge_smem + K * ncol;   // its spline's second derivative there
+#define r(k, col) rs[(k) * ncol + (col)]
+#define M(k, col) Ms[(k) * ncol + (col)]
   auto truth = [&](int k, int col) {
     const zd v = schk[(int64_t)k * NC + (col >> 1)];
     return (col & 1) ? v.im : v.re;
   };
   if (c < ncol) {
-    for (int k = 0; k < K; ++k) r[k][c] = truth(k, c) - scale[c] * (double)ychk[(int64_t)k * ncol + c];
+    for (int k = 0; k < K; ++k) r(k, c) = truth(k, c) - scale[c] * (double)ychk[(int64_t)k * ncol + c];
     // natural spline: M_0 = M_{K-1} = 0, tridiagonal system for the interior (Thomas)
     double cp[kSurMaxCheck], dp[kSurMaxCheck];
     cp[0] = 0.0;
     dp[0] = 0.0;
     for (int k = 1; k < K - 1; ++k) {
       const double h0 = rchk[k] - rchk[k - 1], h1 = rchk[k + 1] - rchk[k];
-      const double rhs = 6.0 * ((r[k + 1][c] - r[k][c]) / h1 - (r[k][c] - r[k - 1][c]) / h0);
+      const double rhs = 6.0 * ((r(k + 1, c) - r(k, c)) / h1 - (r(k, c) - r(k - 1, c)) / h0);
       const double den = 2.0 * (h0 + h1) - h0 * cp[k - 1];
       cp[k] = h1 / den;
       dp[k] = (rhs - h0 * dp[k - 1]) / den;
     }
-    M[K - 1][c] = 0.0;
-    for (int k = K - 2; k >= 1; --k) M[k][c] = dp[k] - cp[k] * M[k + 1][c];
-    M[0][c] = 0.0;
+    M(K - 1, c) = 0.0;
+    for (int k = K - 2; k >= 1; --k) M(k, c) = dp[k] - cp[k] * M(k + 1, c);
+    M(0, c) = 0.0;
   }
   __syncthreads();
   auto spline = [&](double x, int col) {
@@ -452,8 +459,8 @@ __global__ void __launch_bounds__(256) sur_judge_kernel(int NC, int n, const dou
       if (x < rchk[mid]) hi = mid; else lo = mid;
     }
     const double h = rchk[lo + 1] - rchk[lo], t = x - rchk[lo];
-    const double b = (r[lo + 1][col] - r[lo][col]) / h - h * (2.0 * M[lo][col] + M[lo + 1][col]) / 6.0;
-    return r[lo][col] + t * (b + t * (0.5 * M[lo][col] + t * (M[lo + 1][col] - M[lo][col]) / (6.0 * h)));
+    const double b = (r(lo + 1, col) - r(lo, col)) / h - h * (2.0 * M(lo, col) + M(lo + 1, col)) / 6.0;
+    return r(lo, col) + t * (b + t * (0.5 * M(lo, col) + t * (M(lo + 1, col) - M(lo, col)) / (6.0 * h)));
   };
   // validation radii rchk[K .. 2K-2]
   double emax = 0.0, smax = 0.0;
@@ -492,6 +499,8 @@ __global__ void __launch_bounds__(256) sur_judge_kernel(int NC, int n, const dou
     *err_out = rel;
     *flag = rel <= tol ? 1 : 0;
   }
+#undef r
+#undef M
 }
 
 int mlp_forward_device(const m25_mlp* m, int n, const float* X, float* Y, cudaStream_t st);  // mlp.cu
@@ -600,7 +609,7 @@ extern "C" int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* d, m25_gre
       mlp_dims(d->surrogate, &nin, &nout);
       if (nin != 2 || nout != 2 * NC || K < 4 || K > kSurMaxCheck || !d->sur_scale || !(d->sur_fmax > d->sur_fmin) ||
           !(d->sur_a > 0) || !(d->sur_rho_ref > 0)) {
-        set_error("m25_greens_create: surrogate does not match the stack (2 inputs, 2 NC outputs, 4-48 check radii)");
+        set_error("m25_greens_create: surrogate does not match the stack (2 inputs, 2 NC outputs, 4-128 check radii)");
         rc = M25_ERR_VALUE;
         goto fail;
       }
@@ -626,8 +635,16 @@ extern "C" int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* d, m25_gre
       sommerfeld(nv, rchk, schk, nullptr);
       int* flag = static_cast<int*>(g->sur);
       double* err = reinterpret_cast<double*>(static_cast<char*>(g->sur) + 8);
-      sur_judge_kernel<<<1, 256, 0, st>>>(NC, n, g->rho, K, rchk, Y, Y + 2 * NC * (size_t)n, scl, schk, d->sur_tol,
-                                          res, flag, err);
+      static const bool judge_attr = cudaFuncSetAttribute(sur_judge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                          (int)sur_judge_smem(kSurMaxCheck, kSurMaxCols / 2)) ==
+                                     cudaSuccess;
+      if (!judge_attr) {
+        set_error("m25_greens_create: the surrogate judge's shared memory could not be reserved");
+        rc = M25_ERR_CUDA;
+        goto fail;
+      }
+      sur_judge_kernel<<<1, 256, sur_judge_smem(K, NC), st>>>(NC, n, g->rho, K, rchk, Y, Y + 2 * NC * (size_t)n, scl,
+                                                             schk, d->sur_tol, res, flag, err);
       sommerfeld(n, g->rho, res, flag);  // the full integral unless the judge accepted
     } else {
       sommerfeld(n, g->rho, res, nullptr);
