@@ -163,15 +163,19 @@ typedef struct {
    * network maps (2 log1p(rho/a) / log1p(rho_ref/a) - 1, 2 (f - fmin) /
    * (fmax - fmin) - 1) to the 2 NC scaled real and imaginary parts of the
    * remainder (NC = 3 nlev^2 columns [A, V, W] x level pairs, res = scale x
-   * output). The Sommerfeld integral at sur_ncheck radii (quadratically
-   * spaced up to the last tabulation radius) corrects it through a cubic
-   * spline of the residual, and at sur_ncheck - 1 midpoints judges it: the
-   * table uses it when the largest error there is <= sur_tol x the largest
-   * |remainder|, else the Sommerfeld integral at every radius. */
+   * output). The Sommerfeld integral runs first at the knots (every radius
+   * below sur_near, then every sur_stride-th radius and the last) and at one
+   * validation radius in the middle of each gap between knots. A not-a-knot
+   * spline of the residual (integral - network) through the knots, added to
+   * the network, is judged at the validation radii: when its largest error
+   * there is <= sur_tol x the largest |remainder|, the other radii take the
+   * network plus a not-a-knot spline of the residual through all integrated
+   * radii; else the Sommerfeld integral runs at them too. */
   const m25_mlp* surrogate;
   double sur_a, sur_rho_ref, sur_fmin, sur_fmax;
   const double* sur_scale;    /* (2 NC) */
-  int32_t sur_ncheck;         /* 4 .. 128 */
+  double sur_near;            /* [m] radii below it are always integrated */
+  int32_t sur_stride;         /* 2 .. 64 */
   double sur_tol;
 } m25_greens_desc;
 
@@ -184,7 +188,8 @@ int m25_greens_tables(m25_greens* g, double* S, double* c, double* coef);
 /* The Sommerfeld remainder the tables were built from: res (nrho, NC)
  * complex128 (surrogate tables: the corrected network values);
  * info[0] = 1 if the learned remainder was used, info[1] = the judge's
- * relative error (0 without a surrogate). Either may be NULL. */
+ * relative error (0 without a surrogate), info[2] = the number of radii the
+ * Sommerfeld integral ran at. Either may be NULL. */
 int m25_greens_remainder(m25_greens* g, double* res, double* info);
 
 /* ------------------------------------------------ learned remainder (MLP) */

@@ -5,6 +5,7 @@
 // Follows Engine/mom25d/greens.py:111-212 (one grounded slab) and
 // Engine/mom25d/layered.py:238-405 (open multilayer stack, Michalski-Zheng
 // transmission-line form).
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -105,8 +106,9 @@ __device__ void layered_spectral(const StackDev& S, zd kr, zd g[3][kMaxLev][kMax
   }
 }
 
-// Leading-term coefficients (greens.py:215-224, layered.py:292-331).
-__global__ void leading_kernel(StackDev* S, double kbig) {
+// Leading-term coefficients (greens.py:215-224, layered.py:292-331); gbig:
+// the layered spectral kernels at kbig (spectral_g_kernel's last node).
+__global__ void leading_kernel(StackDev* S, double kbig, const zd* __restrict__ gbig) {
   if (threadIdx.x || blockIdx.x) return;
   StackDev& s = *S;
   const int L = s.nlev, N = s.nlayer;
@@ -124,8 +126,6 @@ __global__ void leading_kernel(StackDev* S, double kbig) {
     s.dz[0][0] = 0.0;
     return;
   }
-  bool have_big = false;
-  zd big[3][kMaxLev][kMaxLev];
   for (int i = 0; i < L; ++i)
     for (int j = 0; j < L; ++j) {
       s.dz[i][j] = fabs(s.zl[i] - s.zl[j]);
@@ -147,14 +147,10 @@ __global__ void leading_kernel(StackDev* S, double kbig) {
         s.kx[1][i][j] = csqrt((eb * (ka * ka) + ea * (kb * kb)) / (ea + eb));
         continue;
       }
-      if (!have_big) {
-        layered_spectral(s, zd(kbig), big);
-        have_big = true;
-      }
       zd ux = csqrt(zd(kbig * kbig - s.k0 * s.k0));
       zd f = ux * 2.0 * cexp(ux * s.dz[i][j]);
       zd c[3];
-      for (int m = 0; m < 3; ++m) c[m] = f * big[m][i][j];
+      for (int m = 0; m < 3; ++m) c[m] = f * gbig[(m * L + i) * L + j];
       if (s.zl[j] < s.zl[i]) c[2] = zd(0.0);
       for (int m = 0; m < 3; ++m) {
         // drop the numerical noise of static coefficients' imaginary parts
@@ -166,31 +162,65 @@ __global__ void leading_kernel(StackDev* S, double kbig) {
     }
 }
 
-// coef[k][(m*L + i)*L + j] = w k g_rem(k) / 2pi at every path point.
-__global__ void spectral_coef_kernel(const StackDev* __restrict__ Sp, int nk, const double* __restrict__ kpts,
-                                     const double* __restrict__ wpts, int complex_path, zd* __restrict__ coef) {
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nk) return;
+// The spectral kernels g[(m*L + i)*L + j] at every path node, in one launch:
+// nodes q < nkc of the lifted arc into gc, the next nkr of the real axis into
+// gr, and (layered stacks) one more node at kbig into gbig for the leading
+// terms. Each node is one thread's fp64 chain of square roots, exponentials
+// and divisions through the layers; small CTAs spread the nodes over the SMs.
+__global__ void __launch_bounds__(64) spectral_g_kernel(const StackDev* __restrict__ Sp, int nkc,
+                                                        const double* __restrict__ kc, int nkr,
+                                                        const double* __restrict__ kr, double kbig,
+                                                        zd* __restrict__ gc, zd* __restrict__ gr,
+                                                        zd* __restrict__ gbig) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const StackDev& S = *Sp;
-  const int L = S.nlev;
-  zd kr = complex_path ? zd(kpts[2 * q], kpts[2 * q + 1]) : zd(kpts[q], 0.0);
-  zd w = complex_path ? zd(wpts[2 * q], wpts[2 * q + 1]) : zd(wpts[q], 0.0);
+  const int L = S.nlev, NC = 3 * L * L;
+  zd k;
+  zd* out;
+  if (q < nkc) {
+    k = zd(kc[2 * q], kc[2 * q + 1]);
+    out = gc + (int64_t)q * NC;
+  } else if (q < nkc + nkr) {
+    k = zd(kr[q - nkc], 0.0);
+    out = gr + (int64_t)(q - nkc) * NC;
+  } else if (q == nkc + nkr && !S.single) {
+    k = zd(kbig, 0.0);
+    out = gbig;
+  } else {
+    return;
+  }
   zd g[3][kMaxLev][kMaxLev];
   if (S.single) {
-    slab_spectral(S, kr, g[0][0][0], g[1][0][0], g[2][0][0]);
+    slab_spectral(S, k, g[0][0][0], g[1][0][0], g[2][0][0]);
   } else {
-    layered_spectral(S, kr, g);
+    layered_spectral(S, k, g);
   }
-  zd kr2 = kr * kr;
-  zd scale = (w * kr) / (2.0 * kPi);
   for (int m = 0; m < 3; ++m)
     for (int i = 0; i < L; ++i)
-      for (int j = 0; j < L; ++j) {
-        zd kx = S.kx[m == 0 ? 0 : 1][i][j];
-        zd ux = csqrt(kr2 - kx * kx);
-        zd lead = S.lead_c[m][i][j] * cexp(ux * (-S.dz[i][j])) / (ux * 2.0);
-        coef[(int64_t)q * (3 * L * L) + (m * L + i) * L + j] = scale * (g[m][i][j] - lead);
-      }
+      for (int j = 0; j < L; ++j) out[(m * L + i) * L + j] = g[m][i][j];
+}
+
+// coef[q][(m*L + i)*L + j] = w k (g - leading term) / 2pi at every path node
+// (in place over the spectral kernels g), one thread per (node, column).
+__global__ void spectral_coef_kernel(const StackDev* __restrict__ Sp, int nkc, const double* __restrict__ kc,
+                                     const double* __restrict__ wc, int nkr, const double* __restrict__ kr,
+                                     const double* __restrict__ wr, zd* __restrict__ cc, zd* __restrict__ cr) {
+  const StackDev& S = *Sp;
+  const int L = S.nlev, NC = 3 * L * L;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)(nkc + nkr) * NC) return;
+  const int q = (int)(t / NC), col = (int)(t % NC);
+  const int m = col / (L * L), i = (col / L) % L, j = col % L;
+  const bool cpath = q < nkc;
+  const int qq = cpath ? q : q - nkc;
+  const zd k = cpath ? zd(kc[2 * qq], kc[2 * qq + 1]) : zd(kr[qq], 0.0);
+  const zd w = cpath ? zd(wc[2 * qq], wc[2 * qq + 1]) : zd(wr[qq], 0.0);
+  zd* c = (cpath ? cc : cr) + (int64_t)qq * NC + col;
+  const zd kx = S.kx[m == 0 ? 0 : 1][i][j];
+  const zd ux = csqrt(k * k - kx * kx);
+  const zd lead = S.lead_c[m][i][j] * cexp(ux * (-S.dz[i][j])) / (ux * 2.0);
+  const zd scale = (w * k) / (2.0 * kPi);
+  *c = scale * (*c - lead);
 }
 
 // J0 of a complex argument: the trapezoidal rule on Bessel's integral
@@ -219,20 +249,32 @@ __device__ inline zd bessel_j0_complex(zd z) {
   return {(2.0 + 2.0 * cr + 4.0 * sr) / M, (2.0 * ci + 4.0 * si) / M};
 }
 
-// res[rho][c] = sum_k J0(rho k) coef[k][c] over the lifted arc (complex J0)
-// and the real axis (real J0), one CTA per radius.
+// Path nodes per CTA of the Sommerfeld integral: each radius's sum over the
+// nk_c + nk_r path nodes is split into ceil(nk / kSomNodes) fixed ranges (at
+// most kSomMaxSplit), whatever the radii launched with it, so that a radius's
+// value does not depend on which radii share its launch.
+constexpr int kSomNodes = 1024;
+constexpr int kSomMaxSplit = 32;
+inline int som_split(int nk) { return std::min(kSomMaxSplit, std::max(1, (nk + kSomNodes - 1) / kSomNodes)); }
+
+// part[s][e][c] = sum over the nodes of range s of J0(rho k) coef[k][c] at
+// radius rho[idx[e]] (idx NULL: rho[e]); complex J0 on the lifted arc, real
+// J0 on the real axis. Grid (ne, nsplit), one CTA per (radius, node range).
 // With skip set (the learned remainder was accepted) the CTAs return at once.
 template <int NC>
-__global__ void sommerfeld_kernel(int nrho, const double* __restrict__ rho, int nkc, const double* __restrict__ kc,
-                                  const zd* __restrict__ coef_c, int nkr, const double* __restrict__ kr,
-                                  const zd* __restrict__ coef_r, zd* __restrict__ res, const int* __restrict__ skip) {
+__global__ void sommerfeld_kernel(int ne, const int* __restrict__ idx, const double* __restrict__ rho, int nsplit,
+                                  int nkc, const double* __restrict__ kc, const zd* __restrict__ coef_c, int nkr,
+                                  const double* __restrict__ kr, const zd* __restrict__ coef_r, zd* __restrict__ part,
+                                  const int* __restrict__ skip) {
   if (skip && *skip) return;
-  int ir = blockIdx.x;
-  double r = rho[ir];
+  const int e = blockIdx.x, s = blockIdx.y;
+  const double r = rho[idx ? idx[e] : e];
+  const int64_t nk = (int64_t)nkc + nkr;
+  const int q0 = (int)(nk * s / nsplit), q1 = (int)(nk * (s + 1) / nsplit);
   double acc_re[NC], acc_im[NC];
 #pragma unroll
   for (int c = 0; c < NC; ++c) acc_re[c] = acc_im[c] = 0.0;
-  for (int q = threadIdx.x; q < nkc; q += blockDim.x) {
+  for (int q = q0 + threadIdx.x; q < min(q1, nkc); q += blockDim.x) {
     zd J = bessel_j0_complex(zd(r * kc[2 * q], r * kc[2 * q + 1]));
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
@@ -241,11 +283,12 @@ __global__ void sommerfeld_kernel(int nrho, const double* __restrict__ rho, int 
       acc_im[c] += v.im;
     }
   }
-  for (int q = threadIdx.x; q < nkr; q += blockDim.x) {
-    double J = j0(r * kr[q]);
+  for (int q = max(q0, nkc) + threadIdx.x; q < q1; q += blockDim.x) {
+    const int qr = q - nkc;
+    double J = j0(r * kr[qr]);
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-      zd v = coef_r[(int64_t)q * NC + c];
+      zd v = coef_r[(int64_t)qr * NC + c];
       acc_re[c] += J * v.re;
       acc_im[c] += J * v.im;
     }
@@ -268,10 +311,23 @@ __global__ void sommerfeld_kernel(int nrho, const double* __restrict__ rho, int 
         sa += red[w][0];
         sb += red[w][1];
       }
-      res[(int64_t)ir * NC + c] = zd(sa, sb);
+      part[((int64_t)s * ne + e) * NC + c] = zd(sa, sb);
     }
     __syncthreads();
   }
+}
+
+// res[idx[e]][c] = sum over the node ranges s (in order) of part[s][e][c].
+__global__ void sommerfeld_sum_kernel(int ne, int NC, const int* __restrict__ idx, int nsplit,
+                                      const zd* __restrict__ part, zd* __restrict__ res,
+                                      const int* __restrict__ skip) {
+  if (skip && *skip) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ne * NC) return;
+  const int e = t / NC, c = t % NC;
+  zd v(0.0, 0.0);
+  for (int s = 0; s < nsplit; ++s) v = v + part[((int64_t)s * ne + e) * NC + c];
+  res[(int64_t)(idx ? idx[e] : e) * NC + c] = v;
 }
 
 // S tables: closed-form expm1 part of the leading term, the Sommerfeld
@@ -311,8 +367,64 @@ __global__ void table_kernel(const StackDev* __restrict__ Sp, int nrho, const do
 // One CTA per column: radii, values and the sweep's arrays in shared memory
 // (the elimination is a chain of dependent steps: it runs on one thread from
 // shared memory), the coefficients of the intervals in parallel.
-__host__ __device__ inline size_t spline_smem(int n) { return (size_t)n * (2 * sizeof(double) + 4 * sizeof(zd)); }
+// Tridiagonal system a_i x_{i-1} + b_i x_i + c_i x_{i+1} = d_i, i < m (a_0 =
+// c_{m-1} = 0), diagonally dominant, solved by parallel cyclic reduction
+// (Hockney) with every thread of the CTA: round r combines each row with the
+// rows 2^r above and below, which removes their couplings; after ceil(log2 m)
+// rounds every row reads b_i x_i = d_i. Shared-memory arrays of m entries:
+// a, b, c, d and the copies a2, b2, c2, d2 (ping-pong); x receives the
+// solution (it may be d). The caller synchronises before the call; the call
+// ends with the CTA synchronised. A serial elimination would chain m
+// dependent fp64 divisions; here the chain is ceil(log2 m) rounds deep.
+template <class T>
+__device__ void pcr_solve(int m, double* a, double* b, double* c, T* d, double* a2, double* b2, double* c2, T* d2,
+                          T* x) {
+  for (int st = 1; st < m; st <<= 1) {
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      double na = 0.0, nc = 0.0, nb = b[i];
+      T nd = d[i];
+      if (i - st >= 0) {
+        const double k1 = a[i] / b[i - st];
+        na = -a[i - st] * k1;
+        nb -= c[i - st] * k1;
+        nd = nd - d[i - st] * k1;
+      }
+      if (i + st < m) {
+        const double k2 = c[i] / b[i + st];
+        nc = -c[i + st] * k2;
+        nb -= a[i + st] * k2;
+        nd = nd - d[i + st] * k2;
+      }
+      a2[i] = na;
+      b2[i] = nb;
+      c2[i] = nc;
+      d2[i] = nd;
+    }
+    __syncthreads();
+    double* t;
+    t = a, a = a2, a2 = t;
+    t = b, b = b2, b2 = t;
+    t = c, c = c2, c2 = t;
+    T* td = d;
+    d = d2, d2 = td;
+  }
+  for (int i = threadIdx.x; i < m; i += blockDim.x) x[i] = d[i] / b[i];
+  __syncthreads();
+}
 
+__host__ __device__ inline size_t spline_smem(int n) { return (size_t)n * (2 * sizeof(double) + 4 * sizeof(zd)); }
+// with the reduced system solved by pcr_solve (n - 2 rows)
+__host__ __device__ inline size_t spline_smem_pcr(int n) {
+  return (size_t)n * (2 * sizeof(double) + 3 * sizeof(zd)) + (size_t)(n - 2) * (6 * sizeof(double) + 2 * sizeof(zd));
+}
+
+// Not-a-knot cubic spline of one table column (scipy CubicSpline's slope
+// form): rows a_i s_{i-1} + b_i s_i + c_i s_{i+1} = d_i for the slopes s,
+// the first and last rows the not-a-knot conditions. PCR: rows 0 and n - 1
+// are eliminated into rows 1 and n - 2, which leaves a strictly diagonally
+// dominant system for s_1 .. s_{n-2} (pcr_solve); else (tables too long for
+// its shared memory) one thread eliminates and substitutes serially.
+template <bool PCR>
 __global__ void __launch_bounds__(128) spline_kernel(int L, int nrho, const double* __restrict__ xg,
                                                      const zd* __restrict__ Stab, zd* __restrict__ coef) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -320,8 +432,7 @@ __global__ void __launch_bounds__(128) spline_kernel(int L, int nrho, const doub
   const int n = nrho;
   zd* y = reinterpret_cast<zd*>(smem_raw);  // (n) values
   zd* s = y + n;                            // (n) slopes
-  zd* cp = s + n;                           // (n) modified diagonal (re), upper diagonal (im)
-  zd* sl = cp + n;                          // (n - 1) secant slopes
+  zd* sl = s + n;                           // (n - 1) secant slopes
   double* x = reinterpret_cast<double*>(sl + n);
   double* dx = x + n;                       // (n - 1) interval widths
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -335,47 +446,96 @@ __global__ void __launch_bounds__(128) spline_kernel(int L, int nrho, const doub
     sl[i] = (y[i + 1] - y[i]) / dx[i];
   }
   __syncthreads();
-  // rows: a_i s_{i-1} + b_i s_i + c_i s_{i+1} = d_i
-  auto dxf = [&](int i) { return dx[i]; };
-  auto slope = [&](int i) { return sl[i]; };
-  if (threadIdx.x == 0) {
-    // forward sweep
-    double bprev = 0, cprev = 0;
-    for (int i = 0; i < n; ++i) {
+  // row i of the slope system
+  auto row = [&](int i, double& a, double& b, double& c, zd& d) {
+    if (i == 0) {
+      const double dx0 = dx[0], dx1 = dx[1], d0 = x[2] - x[0];
+      a = 0;
+      b = dx1;
+      c = d0;
+      d = (sl[0] * ((dx0 + 2 * d0) * dx1) + sl[1] * (dx0 * dx0)) / d0;
+    } else if (i == n - 1) {
+      const double dxl = dx[n - 2], dxm = dx[n - 3], d1 = x[n - 1] - x[n - 3];
+      a = d1;
+      b = dxm;
+      c = 0;
+      d = (sl[n - 3] * (dxl * dxl) + sl[n - 2] * ((2 * d1 + dxl) * dxm)) / d1;
+    } else {
+      a = dx[i];
+      b = 2 * (dx[i - 1] + dx[i]);
+      c = dx[i - 1];
+      d = (sl[i - 1] * dx[i] + sl[i] * dx[i - 1]) * 3.0;
+    }
+  };
+  if constexpr (PCR) {
+    const int m = n - 2;
+    double* ra = dx + n;
+    double* rb = ra + m;
+    double* rc = rb + m;
+    double* ra2 = rc + m;
+    double* rb2 = ra2 + m;
+    double* rc2 = rb2 + m;
+    zd* rd = reinterpret_cast<zd*>(rc2 + m);
+    zd* rd2 = rd + m;
+    for (int i = 1 + threadIdx.x; i <= n - 2; i += blockDim.x) {
       double a, b, c;
       zd d;
-      if (i == 0) {
-        double dx0 = dxf(0), dx1 = dxf(1), d0 = x[2] - x[0];
-        a = 0;
-        b = dx1;
-        c = d0;
-        d = (slope(0) * ((dx0 + 2 * d0) * dx1) + slope(1) * (dx0 * dx0)) / d0;
-      } else if (i == n - 1) {
-        double dxl = dxf(n - 2), dxm = dxf(n - 3), d1 = x[n - 1] - x[n - 3];
-        a = d1;
-        b = dxm;
-        c = 0;
-        d = (slope(n - 3) * (dxl * dxl) + slope(n - 2) * ((2 * d1 + dxl) * dxm)) / d1;
-      } else {
-        a = dxf(i);
-        b = 2 * (dxf(i - 1) + dxf(i));
-        c = dxf(i - 1);
-        d = (slope(i - 1) * dxf(i) + slope(i) * dxf(i - 1)) * 3.0;
+      row(i, a, b, c, d);
+      if (i == 1) {  // s_0 = (d_0 - c_0 s_1) / b_0
+        double a0, b0, c0;
+        zd d0;
+        row(0, a0, b0, c0, d0);
+        b -= a * c0 / b0;
+        d = d - d0 * (a / b0);
+        a = 0.0;
       }
-      if (i > 0) {
-        double mlt = a / bprev;
-        b -= mlt * cprev;
-        d -= s[i - 1] * mlt;
+      if (i == n - 2) {  // s_{n-1} = (d_{n-1} - a_{n-1} s_{n-2}) / b_{n-1}
+        double al, bl, cl;
+        zd dl;
+        row(n - 1, al, bl, cl, dl);
+        b -= c * al / bl;
+        d = d - dl * (c / bl);
+        c = 0.0;
       }
-      s[i] = d;       // holds the modified rhs
-      cp[i] = zd(b);  // modified diagonal
-      bprev = b;
-      cprev = c;
-      if (i < n - 1) cp[i].im = c;
+      ra[i - 1] = a;
+      rb[i - 1] = b;
+      rc[i - 1] = c;
+      rd[i - 1] = d;
     }
-    // back substitution
-    s[n - 1] = s[n - 1] / cp[n - 1].re;
-    for (int i = n - 2; i >= 0; --i) s[i] = (s[i] - s[i + 1] * cp[i].im) / cp[i].re;
+    __syncthreads();
+    pcr_solve<zd>(m, ra, rb, rc, rd, ra2, rb2, rc2, rd2, s + 1);
+    if (threadIdx.x == 0) {
+      double a, b, c;
+      zd d;
+      row(0, a, b, c, d);
+      s[0] = (d - s[1] * c) / b;
+      row(n - 1, a, b, c, d);
+      s[n - 1] = (d - s[n - 2] * a) / b;
+    }
+  } else {
+    zd* cp = reinterpret_cast<zd*>(dx + n);  // (n) modified diagonal (re), upper diagonal (im)
+    if (threadIdx.x == 0) {
+      // forward sweep
+      double bprev = 0, cprev = 0;
+      for (int i = 0; i < n; ++i) {
+        double a, b, c;
+        zd d;
+        row(i, a, b, c, d);
+        if (i > 0) {
+          double mlt = a / bprev;
+          b -= mlt * cprev;
+          d -= s[i - 1] * mlt;
+        }
+        s[i] = d;       // holds the modified rhs
+        cp[i] = zd(b);  // modified diagonal
+        bprev = b;
+        cprev = c;
+        if (i < n - 1) cp[i].im = c;
+      }
+      // back substitution
+      s[n - 1] = s[n - 1] / cp[n - 1].re;
+      for (int i = n - 2; i >= 0; --i) s[i] = (s[i] - s[i + 1] * cp[i].im) / cp[i].re;
+    }
   }
   __syncthreads();
   const int pair = col % (L * L), m = col / (L * L);
@@ -406,72 +566,108 @@ __global__ void sur_features_kernel(int n, const double* __restrict__ rho, doubl
   X[2 * i + 1] = (float)(2.0 * (f - fmin) / (fmax - fmin) - 1.0);
 }
 
-constexpr int kSurMaxCheck = 128;
-constexpr int kSurMaxCols = 2 * 3 * kMaxLevSq;
-// dynamic shared memory of the judge: the residuals and spline moments at
-// the K check radii, K x 2 NC doubles each
-inline size_t sur_judge_smem(int K, int NC) { return sizeof(double) * 2 * (size_t)K * 2 * NC; }
-
-// Residual correction and judge (one CTA): natural cubic splines in rho of
-// the Sommerfeld-minus-network residual of every real column through the K
-// check radii; res (table radii) = network + spline; accepted when the
-// largest error at the K - 1 validation radii is <= tol x the largest
-// |remainder| at the check radii.
-__global__ void __launch_bounds__(256) sur_judge_kernel(int NC, int n, const double* __restrict__ rho, int K,
-                                                        const double* __restrict__ rchk, const float* __restrict__ ytab,
-                                                        const float* __restrict__ ychk, const double* __restrict__ scale,
-                                                        const zd* __restrict__ schk, double tol, zd* __restrict__ res,
-                                                        int* __restrict__ flag, double* __restrict__ err_out) {
-  extern __shared__ double judge_smem[];
-  __shared__ double red_e[8], red_s[8];
-  const int ncol = 2 * NC;
-  const int c = threadIdx.x;
-  double* rs = judge_smem;              // residual at check radius k, column c: rs[k ncol + c]
-  double* Ms = judge_smem + K * ncol;   // its spline's second derivative there
-#define r(k, col) rs[(k) * ncol + (col)]
-#define M(k, col) Ms[(k) * ncol + (col)]
-  auto truth = [&](int k, int col) {
-    const zd v = schk[(int64_t)k * NC + (col >> 1)];
-    return (col & 1) ? v.im : v.re;
-  };
-  if (c < ncol) {
-    for (int k = 0; k < K; ++k) r(k, c) = truth(k, c) - scale[c] * (double)ychk[(int64_t)k * ncol + c];
-    // natural spline: M_0 = M_{K-1} = 0, tridiagonal system for the interior (Thomas)
-    double cp[kSurMaxCheck], dp[kSurMaxCheck];
-    cp[0] = 0.0;
-    dp[0] = 0.0;
-    for (int k = 1; k < K - 1; ++k) {
-      const double h0 = rchk[k] - rchk[k - 1], h1 = rchk[k + 1] - rchk[k];
-      const double rhs = 6.0 * ((r(k + 1, c) - r(k, c)) / h1 - (r(k, c) - r(k - 1, c)) / h0);
-      const double den = 2.0 * (h0 + h1) - h0 * cp[k - 1];
-      cp[k] = h1 / den;
-      dp[k] = (rhs - h0 * dp[k - 1]) / den;
+// Not-a-knot cubic spline through (x_j, y_j), j < K (K >= 4), with every
+// thread of the CTA: the second derivatives M_j. The end conditions (third
+// derivative continuous at x_1 and x_{K-2}) give M_0 and M_{K-1} in terms of
+// their neighbours; substituted into rows 1 and K - 2 they leave a strictly
+// diagonally dominant tridiagonal system for M_1 .. M_{K-2}, solved by
+// pcr_solve. scratch: 8 (K - 2) doubles of shared memory. The caller
+// synchronises before the call; the call ends synchronised.
+template <class XF, class YF>
+__device__ void spline_notaknot(int K, XF x, YF y, double* M, double* scratch) {
+  const int m = K - 2;  // unknowns M_1 .. M_{K-2}
+  double *a = scratch, *b = a + m, *c = b + m, *d = c + m;
+  double *a2 = d + m, *b2 = a2 + m, *c2 = b2 + m, *d2 = c2 + m;
+  auto h = [&](int j) { return x(j + 1) - x(j); };
+  for (int k = 1 + threadIdx.x; k <= m; k += blockDim.x) {
+    double ak = h(k - 1), bk = 2.0 * (h(k - 1) + h(k)), ck = h(k);
+    const double dk = 6.0 * ((y(k + 1) - y(k)) / h(k) - (y(k) - y(k - 1)) / h(k - 1));
+    if (k == 1) {  // M_0 = ((h_0 + h_1) M_1 - h_0 M_2) / h_1
+      bk += h(0) * (h(0) + h(1)) / h(1);
+      ck -= h(0) * h(0) / h(1);
+      ak = 0.0;
     }
-    M(K - 1, c) = 0.0;
-    for (int k = K - 2; k >= 1; --k) M(k, c) = dp[k] - cp[k] * M(k + 1, c);
-    M(0, c) = 0.0;
+    if (k == m) {  // M_{K-1} = ((h_{K-3} + h_{K-2}) M_{K-2} - h_{K-2} M_{K-3}) / h_{K-3}
+      const double p = h(K - 3), q = h(K - 2);
+      ak -= q * q / p;
+      bk += q * (p + q) / p;
+      ck = 0.0;
+    }
+    a[k - 1] = ak;
+    b[k - 1] = bk;
+    c[k - 1] = ck;
+    d[k - 1] = dk;
   }
   __syncthreads();
-  auto spline = [&](double x, int col) {
-    int lo = 0, hi = K - 1;
+  pcr_solve<double>(m, a, b, c, d, a2, b2, c2, d2, M + 1);
+  if (threadIdx.x == 0) {
+    M[0] = ((h(0) + h(1)) * M[1] - h(0) * M[2]) / h(1);
+    M[K - 1] = ((h(K - 3) + h(K - 2)) * M[K - 2] - h(K - 2) * M[K - 3]) / h(K - 3);
+  }
+  __syncthreads();
+}
+
+// The cubic of interval j of a spline with second derivatives M at x.
+__device__ inline double spline_eval(double x0, double x1, double y0, double y1, double M0, double M1, double xv) {
+  const double h = x1 - x0, t = xv - x0;
+  const double b = (y1 - y0) / h - h * (2.0 * M0 + M1) / 6.0;
+  return y0 + t * (b + t * (0.5 * M0 + t * (M1 - M0) / (6.0 * h)));
+}
+
+// Learned remainder. The Sommerfeld integral has been evaluated at the ne
+// radii ie[] (sorted; res holds it there): the knots (every radius below the
+// near limit, then every stride-th radius and the last) at positions kpos[]
+// of ie, and one validation radius in the middle of each gap between knots at
+// positions vpos[]. Y: the network at every table radius (2 NC scaled
+// outputs, res = scale x Y).
+//
+// Judge, one CTA per real column (re / im of each of the NC columns): the
+// residual (integral - network) at the knots is interpolated by a not-a-knot
+// spline, and the network + spline compared with the integral at the
+// validation radii. colerr[2 col] = the largest error there, colerr[2 col +
+// 1] = the largest |remainder| of the column's complex column over the ne
+// radii. Shared memory: (2 ne + 11 nk) doubles.
+__global__ void __launch_bounds__(256) sur_judge_kernel(int NC, const double* __restrict__ rho, int ne,
+                                                        const int* __restrict__ ie, int nk,
+                                                        const int* __restrict__ kpos, int nv,
+                                                        const int* __restrict__ vpos, const float* __restrict__ Y,
+                                                        const double* __restrict__ scale, const zd* __restrict__ res,
+                                                        double* __restrict__ colerr) {
+  extern __shared__ double sm[];
+  __shared__ double red_e[8], red_s[8];
+  const int ncol = 2 * NC, col = blockIdx.x;
+  double* xs = sm;       // radius of integrated radius e
+  double* ys = xs + ne;  // residual there
+  double* xk = ys + ne;
+  double* yk = xk + nk;
+  double* M = yk + nk;
+  double* scratch = M + nk;
+  double smax = 0.0;
+  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+    const int i = ie[e];
+    const zd v = res[(int64_t)i * NC + (col >> 1)];
+    xs[e] = rho[i];
+    ys[e] = ((col & 1) ? v.im : v.re) - scale[col] * (double)Y[(int64_t)i * ncol + col];
+    smax = fmax(smax, sqrt(v.re * v.re + v.im * v.im));
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < nk; j += blockDim.x) {
+    xk[j] = xs[kpos[j]];
+    yk[j] = ys[kpos[j]];
+  }
+  __syncthreads();
+  spline_notaknot(
+      nk, [&](int j) { return xk[j]; }, [&](int j) { return yk[j]; }, M, scratch);
+  double emax = 0.0;
+  for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+    const int e = vpos[v];
+    const double xv = xs[e];
+    int lo = 0, hi = nk - 1;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
-      if (x < rchk[mid]) hi = mid; else lo = mid;
+      if (xv < xk[mid]) hi = mid; else lo = mid;
     }
-    const double h = rchk[lo + 1] - rchk[lo], t = x - rchk[lo];
-    const double b = (r(lo + 1, col) - r(lo, col)) / h - h * (2.0 * M(lo, col) + M(lo + 1, col)) / 6.0;
-    return r(lo, col) + t * (b + t * (0.5 * M(lo, col) + t * (M(lo + 1, col) - M(lo, col)) / (6.0 * h)));
-  };
-  // validation radii rchk[K .. 2K-2]
-  double emax = 0.0, smax = 0.0;
-  for (int e = threadIdx.x; e < (K - 1) * ncol; e += blockDim.x) {
-    const int v = K + e / ncol, col = e % ncol;
-    const double pred = scale[col] * (double)ychk[(int64_t)v * ncol + col] + spline(rchk[v], col);
-    emax = fmax(emax, fabs(pred - truth(v, col)));
-  }
-  for (int e = threadIdx.x; e < K * NC; e += blockDim.x) {
-    const zd v = schk[e];
-    smax = fmax(smax, sqrt(v.re * v.re + v.im * v.im));
+    emax = fmax(emax, fabs(ys[e] - spline_eval(xk[lo], xk[lo + 1], yk[lo], yk[lo + 1], M[lo], M[lo + 1], xv)));
   }
   for (int o = 16; o; o >>= 1) {
     emax = fmax(emax, __shfl_down_sync(0xffffffffu, emax, o));
@@ -481,27 +677,80 @@ __global__ void __launch_bounds__(256) sur_judge_kernel(int NC, int n, const dou
     red_e[threadIdx.x >> 5] = emax;
     red_s[threadIdx.x >> 5] = smax;
   }
-  // the corrected network values at the table radii
-  for (int e = threadIdx.x; e < n * ncol; e += blockDim.x) {
-    const int i = e / ncol, col = e % ncol;
-    const double v = scale[col] * (double)ytab[(int64_t)i * ncol + col] + spline(rho[i], col);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double e = 0, sx = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      e = fmax(e, red_e[w]);
+      sx = fmax(sx, red_s[w]);
+    }
+    colerr[2 * col] = e;
+    colerr[2 * col + 1] = sx;
+  }
+}
+
+// Decision and fill-in, one CTA per real column: accepted when the largest
+// column error <= tol x the largest |remainder| (every CTA forms the same
+// verdict; CTA 0 records it in flag / err_out). When accepted, the table's
+// other radii ir[] get network + a not-a-knot spline of the residual through
+// all ne integrated radii (a denser spline than the judged one). Shared
+// memory: 11 ne doubles.
+__global__ void __launch_bounds__(256) sur_fill_kernel(int NC, const double* __restrict__ rho, int ne,
+                                                       const int* __restrict__ ie, int nr, const int* __restrict__ ir,
+                                                       const float* __restrict__ Y, const double* __restrict__ scale,
+                                                       const double* __restrict__ colerr, double tol,
+                                                       zd* __restrict__ res, int* __restrict__ flag,
+                                                       double* __restrict__ err_out) {
+  extern __shared__ double sm[];
+  __shared__ int accepted;
+  const int ncol = 2 * NC, col = blockIdx.x;
+  if (threadIdx.x == 0) {
+    double e = 0, sx = 0;
+    for (int c = 0; c < ncol; ++c) {
+      e = fmax(e, colerr[2 * c]);
+      sx = fmax(sx, colerr[2 * c + 1]);
+    }
+    const double rel = sx > 0 ? e / sx : INFINITY;
+    accepted = rel <= tol ? 1 : 0;
+    if (blockIdx.x == 0) {
+      *flag = accepted;
+      *err_out = rel;
+    }
+  }
+  __syncthreads();
+  if (!accepted) return;
+  double* xs = sm;
+  double* ys = xs + ne;
+  double* M = ys + ne;
+  double* scratch = M + ne;
+  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+    const int i = ie[e];
+    const zd v = res[(int64_t)i * NC + (col >> 1)];
+    xs[e] = rho[i];
+    ys[e] = ((col & 1) ? v.im : v.re) - scale[col] * (double)Y[(int64_t)i * ncol + col];
+  }
+  __syncthreads();
+  spline_notaknot(
+      ne, [&](int e) { return xs[e]; }, [&](int e) { return ys[e]; }, M, scratch);
+  for (int r = threadIdx.x; r < nr; r += blockDim.x) {
+    const int i = ir[r];
+    const double xv = rho[i];
+    int lo = 0, hi = ne - 1;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (xv < xs[mid]) hi = mid; else lo = mid;
+    }
+    const double v = scale[col] * (double)Y[(int64_t)i * ncol + col] +
+                     spline_eval(xs[lo], xs[lo + 1], ys[lo], ys[lo + 1], M[lo], M[lo + 1], xv);
     double* out = reinterpret_cast<double*>(res + (int64_t)i * NC + (col >> 1));
     out[col & 1] = v;
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double e = 0, sm = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      e = fmax(e, red_e[w]);
-      sm = fmax(sm, red_s[w]);
-    }
-    const double rel = sm > 0 ? e / sm : INFINITY;
-    *err_out = rel;
-    *flag = rel <= tol ? 1 : 0;
-  }
-#undef r
-#undef M
 }
+
+// shared memory of the two kernels above, and its limit
+inline size_t sur_judge_smem(int ne, int nk) { return sizeof(double) * (2 * (size_t)ne + 11 * (size_t)nk); }
+inline size_t sur_fill_smem(int ne) { return sizeof(double) * 11 * (size_t)ne; }
+constexpr size_t kSurSmemMax = 200 * 1024;
 
 int mlp_forward_device(const m25_mlp* m, int n, const float* X, float* Y, cudaStream_t st);  // mlp.cu
 int mlp_dims(const m25_mlp* m, int* n_in, int* n_out);
@@ -589,77 +838,152 @@ extern "C" int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* d, m25_gre
   M25_CUDA(cudaMemcpyAsync(g->rho, d->rho, sizeof(double) * n, cudaMemcpyHostToDevice, st));
   {
   StageTimer tm(ctx, ST_GREENS);
-  leading_kernel<<<1, 1, 0, st>>>(Sd, d->kbig);
-  spectral_coef_kernel<<<(d->nk_c + 127) / 128, 128, 0, st>>>(Sd, d->nk_c, kc, wc, 1, cc);
-  spectral_coef_kernel<<<(d->nk_r + 127) / 128, 128, 0, st>>>(Sd, d->nk_r, kr, wr, 0, cr);
   {
-    // the Sommerfeld integral at nr radii (rr) into out; skip: see sommerfeld_kernel
-    auto sommerfeld = [&](int nr, const double* rr, zd* outp, const int* skip) {
+    zd* gbig = nullptr;
+    TRY(alloc_async(tmp, (void**)&gbig, sizeof(zd) * NC, st));
+    const int nodes = d->nk_c + d->nk_r + 1;
+    spectral_g_kernel<<<(nodes + 63) / 64, 64, 0, st>>>(Sd, d->nk_c, kc, d->nk_r, kr, d->kbig, cc, cr, gbig);
+    leading_kernel<<<1, 1, 0, st>>>(Sd, d->kbig, gbig);
+    const int64_t ncoef = (int64_t)(d->nk_c + d->nk_r) * NC;
+    spectral_coef_kernel<<<(unsigned)((ncoef + 127) / 128), 128, 0, st>>>(Sd, d->nk_c, kc, wc, d->nk_r, kr, wr, cc,
+                                                                          cr);
+  }
+  {
+    // the Sommerfeld integral at the radii rho[idx[e]], e < ne (idx NULL:
+    // all n) into res; skip: see sommerfeld_kernel
+    const int nsplit = som_split(d->nk_c + d->nk_r);
+    zd* part = nullptr;
+    TRY(alloc_async(tmp, (void**)&part, sizeof(zd) * (size_t)nsplit * n * NC, st));
+    auto sommerfeld = [&](int ne, const int* idx, const int* skip) {
+      if (ne <= 0) return;
+      dim3 grid(ne, nsplit);
       switch (NC) {
-        case 3: sommerfeld_kernel<3><<<nr, 256, 0, st>>>(nr, rr, d->nk_c, kc, cc, d->nk_r, kr, cr, outp, skip); break;
-        case 12: sommerfeld_kernel<12><<<nr, 256, 0, st>>>(nr, rr, d->nk_c, kc, cc, d->nk_r, kr, cr, outp, skip); break;
-        default: sommerfeld_kernel<27><<<nr, 256, 0, st>>>(nr, rr, d->nk_c, kc, cc, d->nk_r, kr, cr, outp, skip); break;
+        case 3:
+          sommerfeld_kernel<3><<<grid, 256, 0, st>>>(ne, idx, g->rho, nsplit, d->nk_c, kc, cc, d->nk_r, kr, cr, part,
+                                                     skip);
+          break;
+        case 12:
+          sommerfeld_kernel<12><<<grid, 256, 0, st>>>(ne, idx, g->rho, nsplit, d->nk_c, kc, cc, d->nk_r, kr, cr, part,
+                                                      skip);
+          break;
+        default:
+          sommerfeld_kernel<27><<<grid, 256, 0, st>>>(ne, idx, g->rho, nsplit, d->nk_c, kc, cc, d->nk_r, kr, cr, part,
+                                                      skip);
+          break;
       }
+      sommerfeld_sum_kernel<<<(ne * NC + 255) / 256, 256, 0, st>>>(ne, NC, idx, nsplit, part, res, skip);
     };
+    // learned remainder: which radii get the Sommerfeld integral first
+    std::vector<int> ie, kpos, vpos, ir;
     if (d->surrogate) {
-      // learned remainder: the network at the table radii and at K check +
-      // K - 1 validation radii, the Sommerfeld integral at the latter only
-      const int K = d->sur_ncheck, nv = 2 * K - 1;
       int nin = 0, nout = 0;
       mlp_dims(d->surrogate, &nin, &nout);
-      if (nin != 2 || nout != 2 * NC || K < 4 || K > kSurMaxCheck || !d->sur_scale || !(d->sur_fmax > d->sur_fmin) ||
-          !(d->sur_a > 0) || !(d->sur_rho_ref > 0)) {
-        set_error("m25_greens_create: surrogate does not match the stack (2 inputs, 2 NC outputs, 4-128 check radii)");
+      if (nin != 2 || nout != 2 * NC || d->sur_stride < 2 || d->sur_stride > 64 || !(d->sur_near >= 0) ||
+          !d->sur_scale || !(d->sur_fmax > d->sur_fmin) || !(d->sur_a > 0) || !(d->sur_rho_ref > 0)) {
+        set_error("m25_greens_create: surrogate does not match the stack (2 inputs, 2 NC outputs, stride 2-64)");
         rc = M25_ERR_VALUE;
         goto fail;
       }
-      std::vector<double> hr(nv);
-      const double rlast = d->rho[n - 1];
-      for (int k = 0; k < K; ++k) hr[k] = rlast * ((double)k / (K - 1)) * ((double)k / (K - 1));
-      for (int k = 0; k + 1 < K; ++k) hr[K + k] = rlast * ((k + 0.5) / (K - 1)) * ((k + 0.5) / (K - 1));
-      double *rchk = nullptr, *scl = nullptr;
+      std::vector<int> knots;
+      int n0 = 0;
+      while (n0 < n && d->rho[n0] < d->sur_near) knots.push_back(n0++);
+      for (int i = n0; i < n; i += d->sur_stride) knots.push_back(i);
+      if (knots.back() != n - 1) knots.push_back(n - 1);
+      std::vector<char> exact(n, 0), val(n, 0);
+      for (int i : knots) exact[i] = 1;
+      for (size_t j = 0; j + 1 < knots.size(); ++j)
+        if (knots[j + 1] - knots[j] >= 2) val[(knots[j] + knots[j + 1]) / 2] = 1;
+      for (int i = 0; i < n; ++i) {
+        if (exact[i] || val[i]) {
+          if (exact[i]) kpos.push_back((int)ie.size());
+          if (val[i]) vpos.push_back((int)ie.size());
+          ie.push_back(i);
+        } else {
+          ir.push_back(i);
+        }
+      }
+      if (kpos.size() < 4 || vpos.empty() || ir.empty() ||
+          std::max(sur_judge_smem((int)ie.size(), (int)kpos.size()), sur_fill_smem((int)ie.size())) >
+              kSurSmemMax) {  // the plain tabulation
+        ie.clear();
+        kpos.clear();
+        vpos.clear();
+        ir.clear();
+      }
+    }
+    if (!ie.empty()) {
+      // the network at every radius, the Sommerfeld integral at the knots and
+      // validation radii, the judge, then the integral at the other radii
+      // unless the judge accepted
+      const int ne = (int)ie.size(), nk = (int)kpos.size(), nv = (int)vpos.size(), nr = (int)ir.size();
+      std::vector<int> lists;
+      lists.insert(lists.end(), ie.begin(), ie.end());
+      lists.insert(lists.end(), kpos.begin(), kpos.end());
+      lists.insert(lists.end(), vpos.begin(), vpos.end());
+      lists.insert(lists.end(), ir.begin(), ir.end());
+      int* dl = nullptr;
+      double *scl = nullptr, *colerr = nullptr;
       float *X = nullptr, *Y = nullptr;
-      zd* schk = nullptr;
-      TRY(alloc_async(tmp, (void**)&rchk, sizeof(double) * nv, st));
+      TRY(alloc_async(tmp, (void**)&dl, sizeof(int) * lists.size(), st));
       TRY(alloc_async(tmp, (void**)&scl, sizeof(double) * 2 * NC, st));
-      TRY(alloc_async(tmp, (void**)&X, sizeof(float) * 2 * (size_t)(n + nv), st));
-      TRY(alloc_async(tmp, (void**)&Y, sizeof(float) * 2 * NC * (size_t)(n + nv), st));
-      TRY(alloc_async(tmp, (void**)&schk, sizeof(zd) * NC * (size_t)nv, st));
-      M25_CUDA(cudaMemcpyAsync(rchk, hr.data(), sizeof(double) * nv, cudaMemcpyHostToDevice, st));
+      TRY(alloc_async(tmp, (void**)&X, sizeof(float) * 2 * (size_t)n, st));
+      TRY(alloc_async(tmp, (void**)&Y, sizeof(float) * 2 * NC * (size_t)n, st));
+      TRY(alloc_async(tmp, (void**)&colerr, sizeof(double) * 2 * 2 * NC, st));
+      M25_CUDA(cudaMemcpyAsync(dl, lists.data(), sizeof(int) * lists.size(), cudaMemcpyHostToDevice, st));
       M25_CUDA(cudaMemcpyAsync(scl, d->sur_scale, sizeof(double) * 2 * NC, cudaMemcpyHostToDevice, st));
+      const int *d_ie = dl, *d_kpos = dl + ne, *d_vpos = dl + ne + nk, *d_ir = dl + ne + nk + nv;
       sur_features_kernel<<<(n + 127) / 128, 128, 0, st>>>(n, g->rho, d->sur_a, d->sur_rho_ref, d->freq, d->sur_fmin,
                                                            d->sur_fmax, X);
-      sur_features_kernel<<<(nv + 127) / 128, 128, 0, st>>>(nv, rchk, d->sur_a, d->sur_rho_ref, d->freq, d->sur_fmin,
-                                                            d->sur_fmax, X + 2 * (size_t)n);
-      TRY(mlp_forward_device(d->surrogate, n + nv, X, Y, st));
-      sommerfeld(nv, rchk, schk, nullptr);
+      TRY(mlp_forward_device(d->surrogate, n, X, Y, st));
+      sommerfeld(ne, d_ie, nullptr);
       int* flag = static_cast<int*>(g->sur);
       double* err = reinterpret_cast<double*>(static_cast<char*>(g->sur) + 8);
-      static const bool judge_attr = cudaFuncSetAttribute(sur_judge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                          (int)sur_judge_smem(kSurMaxCheck, kSurMaxCols / 2)) ==
-                                     cudaSuccess;
-      if (!judge_attr) {
-        set_error("m25_greens_create: the surrogate judge's shared memory could not be reserved");
+      static const bool smem_attr =
+          cudaFuncSetAttribute(sur_judge_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSurSmemMax) ==
+              cudaSuccess &&
+          cudaFuncSetAttribute(sur_fill_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSurSmemMax) ==
+              cudaSuccess;
+      if (!smem_attr) {
+        set_error("m25_greens_create: the learned remainder's shared memory could not be reserved");
         rc = M25_ERR_CUDA;
         goto fail;
       }
-      sur_judge_kernel<<<1, 256, sur_judge_smem(K, NC), st>>>(NC, n, g->rho, K, rchk, Y, Y + 2 * NC * (size_t)n, scl,
-                                                             schk, d->sur_tol, res, flag, err);
-      sommerfeld(n, g->rho, res, flag);  // the full integral unless the judge accepted
+      sur_judge_kernel<<<2 * NC, 256, sur_judge_smem(ne, nk), st>>>(NC, g->rho, ne, d_ie, nk, d_kpos, nv, d_vpos, Y,
+                                                                    scl, res, colerr);
+      sur_fill_kernel<<<2 * NC, 256, sur_fill_smem(ne), st>>>(NC, g->rho, ne, d_ie, nr, d_ir, Y, scl, colerr,
+                                                            d->sur_tol, res, flag, err);
+      sommerfeld(nr, d_ir, flag);  // the integral at the other radii unless the judge accepted
+      g->sur_planned = ne;
     } else {
-      sommerfeld(n, g->rho, res, nullptr);
+      sommerfeld(n, nullptr, nullptr);
     }
   }
   table_kernel<<<(NC * n + 127) / 128, 128, 0, st>>>(Sd, n, g->rho, res, omega, zd(d->zs_ground_re, d->zs_ground_im),
                                                    reinterpret_cast<zd*>(g->S));
-  if (spline_smem(n) > 200 * 1024) {
-    set_error("m25_greens_create: too many tabulation radii for the spline in shared memory");
-    rc = M25_ERR_VALUE;
-    goto fail;
+  {
+    const bool pcr = spline_smem_pcr(n) <= 200 * 1024;
+    if (!pcr && spline_smem(n) > 200 * 1024) {
+      set_error("m25_greens_create: too many tabulation radii for the spline in shared memory");
+      rc = M25_ERR_VALUE;
+      goto fail;
+    }
+    static const bool spline_attr =
+        cudaFuncSetAttribute(spline_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) ==
+            cudaSuccess &&
+        cudaFuncSetAttribute(spline_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) ==
+            cudaSuccess;
+    if (!spline_attr) {
+      set_error("m25_greens_create: the spline's shared memory could not be reserved");
+      rc = M25_ERR_CUDA;
+      goto fail;
+    }
+    if (pcr)
+      spline_kernel<true><<<NC, 128, spline_smem_pcr(n), st>>>(L, n, g->rho, reinterpret_cast<zd*>(g->S),
+                                                               reinterpret_cast<zd*>(g->coef));
+    else
+      spline_kernel<false><<<NC, 128, spline_smem(n), st>>>(L, n, g->rho, reinterpret_cast<zd*>(g->S),
+                                                            reinterpret_cast<zd*>(g->coef));
   }
-  M25_CUDA(cudaFuncSetAttribute(spline_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  spline_kernel<<<NC, 128, spline_smem(n), st>>>(L, n, g->rho, reinterpret_cast<zd*>(g->S),
-                                                 reinterpret_cast<zd*>(g->coef));
   {
     int64_t nc = (int64_t)L * L * (n - 1) * 12 * 2;
     to_f32_kernel<<<(unsigned)((nc + 255) / 256), 256, 0, st>>>(g->coef, g->coef32, nc);
@@ -689,6 +1013,9 @@ extern "C" int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* d, m25_gre
     memcpy(&acc, hs, sizeof(int));
     memcpy(&g->sur_info[1], hs + 8, sizeof(double));
     g->sur_info[0] = acc;
+    g->sur_info[2] = acc ? g->sur_planned : n;
+  } else {
+    g->sur_info[2] = n;
   }
   *out = g;
   return M25_OK;
@@ -719,6 +1046,7 @@ extern "C" int m25_greens_remainder(m25_greens* g, double* res, double* info) {
   if (info) {
     info[0] = g->sur_info[0];
     info[1] = g->sur_info[1];
+    info[2] = g->sur_info[2];
   }
   return M25_OK;
 }

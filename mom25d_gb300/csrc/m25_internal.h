@@ -122,7 +122,8 @@ struct m25_greens {
   double* lead = nullptr;      // (3, nlev, nlev) complex c_A, c_V, c_W (device)
   m25::zd* res = nullptr;      // (nrho, 3 nlev^2) Sommerfeld remainder (or the learned one)
   void* sur = nullptr;         // learned remainder: int accepted, then double relative error (device)
-  double sur_info[2] = {0, 0}; // host copy: accepted, error
+  double sur_info[3] = {0, 0, 0};  // host copy: accepted, judged error, radii integrated
+  int sur_planned = 0;              // radii integrated when the learned remainder is accepted
   std::vector<m25::zd> lead_h; // host copy
   std::vector<double> dz_h;    // (nlev, nlev)
   std::vector<void*> allocs;

@@ -5,8 +5,9 @@
 // Parameters live in one float array, layer by layer: W_l (out x in,
 // row-major) then b_l. Training minimises the mean over samples and outputs
 // of (f(x) - y)^2. Every kernel is deterministic: one thread per sample for
-// the forward and backward passes, and the weight gradients are reduced over
-// the samples in a fixed order (no atomics).
+// the training's forward and backward passes, one warp per sample for
+// inference, and the weight gradients are reduced over the samples in a fixed
+// order (no atomics).
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -81,6 +82,72 @@ __global__ void __launch_bounds__(kMlpThreads) mlp_fwd_kernel(MlpDims d, const f
 #pragma unroll
     for (int i = 0; i < kMlpH; ++i) a = fmaf(W[j * kMlpH + i], h[i], a);
     Y[(int64_t)s * d.n_out + j] = a;
+  }
+}
+
+// Y = f(X) for inference, one warp per sample: lane j forms hidden units j
+// and j + 32 of every layer and outputs j, j + 32 (the same fused
+// multiply-adds in the same order as mlp_fwd_kernel, so Y is bit for bit the
+// same), the layer's activations passed through the warp's row of shared
+// memory. The weights are stored transposed in shared memory so that the 32
+// lanes read consecutive words. Shared memory: np + kInferWarps x kMlpH floats.
+constexpr int kInferWarps = 8;
+__global__ void __launch_bounds__(32 * kInferWarps) mlp_infer_kernel(MlpDims d, const float* __restrict__ P,
+                                                                     int64_t np, int n, const float* __restrict__ X,
+                                                                     float* __restrict__ Y) {
+  extern __shared__ float sp[];
+  for (int l = 0; l <= d.n_layers; ++l) {
+    const int nin = mlp_in(d, l), nout = mlp_out(d, l);
+    const float* W = P + d.off[l];
+    float* Wt = sp + d.off[l];
+    for (int e = threadIdx.x; e < nin * nout; e += blockDim.x) Wt[(e % nin) * nout + e / nin] = W[e];
+    for (int e = threadIdx.x; e < nout; e += blockDim.x) Wt[nin * nout + e] = W[nin * nout + e];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* hs = sp + np + warp * kMlpH;
+  for (int s = blockIdx.x * kInferWarps + warp; s < n; s += gridDim.x * kInferWarps) {
+    {
+      const float* Wt = sp + d.off[0];
+      const float* b = Wt + kMlpH * d.n_in;
+      float x[kMlpMaxIn];
+#pragma unroll
+      for (int i = 0; i < kMlpMaxIn; ++i) x[i] = i < d.n_in ? X[(int64_t)s * d.n_in + i] : 0.f;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int j = lane + 32 * h;
+        float a = b[j];
+#pragma unroll
+        for (int i = 0; i < kMlpMaxIn; ++i)
+          if (i < d.n_in) a = fmaf(Wt[i * kMlpH + j], x[i], a);
+        hs[j] = tanhf(a);
+      }
+    }
+    __syncwarp();
+    for (int l = 1; l < d.n_layers; ++l) {
+      const float* Wt = sp + d.off[l];
+      const float* b = Wt + kMlpH * kMlpH;
+      float a0 = b[lane], a1 = b[lane + 32];
+#pragma unroll 16
+      for (int i = 0; i < kMlpH; ++i) {
+        const float hi = hs[i];
+        a0 = fmaf(Wt[i * kMlpH + lane], hi, a0);
+        a1 = fmaf(Wt[i * kMlpH + lane + 32], hi, a1);
+      }
+      __syncwarp();
+      hs[lane] = tanhf(a0);
+      hs[lane + 32] = tanhf(a1);
+      __syncwarp();
+    }
+    const float* Wt = sp + d.off[d.n_layers];
+    const float* b = Wt + (int64_t)d.n_out * kMlpH;
+    for (int j = lane; j < d.n_out; j += 32) {
+      float a = b[j];
+#pragma unroll 16
+      for (int i = 0; i < kMlpH; ++i) a = fmaf(Wt[i * d.n_out + j], hs[i], a);
+      Y[(int64_t)s * d.n_out + j] = a;
+    }
+    __syncwarp();
   }
 }
 
@@ -239,8 +306,9 @@ static size_t mlp_bwd_smem(const m25_mlp* m) {
 // forward pass of n samples already on the device (X (n, n_in), Y (n, n_out))
 int mlp_forward_device(const m25_mlp* m, int n, const float* X, float* Y, cudaStream_t st) {
   if (n <= 0) return M25_OK;
-  mlp_fwd_kernel<false><<<(n + kMlpThreads - 1) / kMlpThreads, kMlpThreads, mlp_fwd_smem(m), st>>>(m->d, m->P, m->np, n,
-                                                                                               X, Y, nullptr);
+  const int64_t blocks = std::min<int64_t>((n + kInferWarps - 1) / kInferWarps, 4096);
+  mlp_infer_kernel<<<(unsigned)blocks, 32 * kInferWarps, sizeof(float) * ((size_t)m->np + kInferWarps * kMlpH), st>>>(
+      m->d, m->P, m->np, n, X, Y);
   M25_CHECK_LAUNCH();
   return M25_OK;
 }
@@ -312,6 +380,7 @@ extern "C" int m25_mlp_create(m25_ctx* ctx, int32_t n_in, int32_t hidden, int32_
   M25_CUDA(cudaMemsetAsync(m->M1, 0, sizeof(float) * off, st));
   M25_CUDA(cudaMemsetAsync(m->M2, 0, sizeof(float) * off, st));
   M25_CUDA(cudaFuncSetAttribute(mlp_fwd_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
+  M25_CUDA(cudaFuncSetAttribute(mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
   M25_CUDA(cudaFuncSetAttribute(mlp_fwd_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
   M25_CUDA(cudaFuncSetAttribute(mlp_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
   if (mlp_bwd_smem(m) > 160 * 1024) {

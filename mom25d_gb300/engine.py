@@ -53,8 +53,8 @@ class GreensDesc(C.Structure):
                 ("stack_h", C.c_double), ("nk_c", C.c_int32), ("nk_r", C.c_int32), ("kc", _f64p), ("wc", _f64p),
                 ("kr", _f64p), ("wr", _f64p), ("nrho", C.c_int32), ("rho", _f64p), ("kbig", C.c_double),
                 ("surrogate", C.c_void_p), ("sur_a", C.c_double), ("sur_rho_ref", C.c_double),
-                ("sur_fmin", C.c_double), ("sur_fmax", C.c_double), ("sur_scale", _f64p), ("sur_ncheck", C.c_int32),
-                ("sur_tol", C.c_double)]
+                ("sur_fmin", C.c_double), ("sur_fmax", C.c_double), ("sur_scale", _f64p), ("sur_near", C.c_double),
+                ("sur_stride", C.c_int32), ("sur_tol", C.c_double)]
 
 
 class PortDesc(C.Structure):

@@ -143,11 +143,12 @@ class Greens:
     def remainder(self):
         """(res (nrho, 3 L^2) complex128, info): the Sommerfeld remainder of the
         tables (columns [A, V, W] x level pairs (i, j)), info = (learned
-        remainder used, its judged relative error)."""
+        remainder used, its judged relative error, number of radii the
+        Sommerfeld integral ran at)."""
         res = np.zeros((self.rho.size, 3 * self.nlev ** 2), complex)
-        info = np.zeros(2)
+        info = np.zeros(3)
         E.check(self._h.ctx.lib.m25_greens_remainder(self.h, E.ptr(res.view(np.float64)), E.ptr(info)))
-        return res, (bool(info[0]), float(info[1]))
+        return res, (bool(info[0]), float(info[1]), int(info[2]))
 
     def tables(self):
         """(S (3,L,L,nrho), c (3,L,L), coef (L*L, nrho-1, 4, 3)) complex128 host copies."""

@@ -3,29 +3,34 @@
 The Green's tables of a frequency are the closed-form leading terms plus a
 remainder, the Sommerfeld integral of the spectral remainder against J0
 (mom25d: Engine/mom25d/greens.py:157-173, layered.py:360-372), evaluated at
-every tabulation radius. GreensSurrogate trains a small network on the
-engine's own Sommerfeld integrals over a frequency band of one stack and
-hands it to the engine, which then
+every tabulation radius; the integral is the cost of a table. GreensSurrogate
+trains a small network (3 x 64 tanh, fp32) on the engine's own Sommerfeld
+integrals over a frequency band of one stack, the inputs a logarithmic radius
+coordinate and the frequency, the outputs the real and imaginary parts of the
+remainder of every kernel and level pair. With it attached the engine
 
-  - evaluates the network at every tabulation radius (inputs: a logarithmic
-    radius coordinate and the frequency; outputs: the real and imaginary parts
-    of the remainder of every kernel and level pair),
-  - corrects it with the Sommerfeld integral at `ncheck` radii (a cubic
-    spline of the residual), and
-  - judges it at ncheck - 1 further radii: the table uses the learned
-    remainder only when the error there is <= tol x max |remainder|; else the
-    Sommerfeld integral at every radius, as without the surrogate.
+  - integrates at the radii below `near` x a (a: the thinnest layer, the
+    scale of the remainder's structure near the source), then at every
+    `stride`-th radius (the knots) and at the middle radius of each gap
+    between knots (validation radii),
+  - corrects the network with a not-a-knot spline of its residual through the
+    knots and judges the corrected network at the validation radii: accepted
+    when the largest error there is <= tol x max |remainder|,
+  - and when accepted fills the other radii with the network plus the spline
+    of its residual through all integrated radii; else integrates there too
+    (the plain tabulation, no integral wasted).
 
 The network (mom25d_gb300/csrc/mlp.cu) is trained on the GPU by the engine's
 forward, backward and Adam kernels; tests/test_gpu_surrogate.py checks their
 gradients against oracle/mlp.py.
 
-Measured on the LPF stack (0.5-8 GHz, 16k samples, 12000 Adam steps in
-~1.6 s on one GB300): the network alone is within 0.4-1 % of the largest
-remainder, 2.6e-5 after the correction; S moves by about the tables' relative
-error (2.8e-5 with tables accepted at 4e-5). The default tol = 5e-6 keeps S
-within 1e-5 of the Sommerfeld tables, where the judge falls back at most
-frequencies of that band.
+Measured on the two-layer via transition on one GB300 (1-20 GHz, 1024 x
+1024 = 1.05e6 samples, 20000 Adam steps in 2.9 s; stride 4, near 8 a,
+tol 5e-6; tests/test_gpu_surrogate.py): accepted at 9 of 10 frequencies;
+judged error 1.9-3.9e-6 of the largest remainder, where a spline of the
+integral alone through the same knots is off by 6.3-8.0e-6; 115-223 of the
+149-365 radii integrated; table time 0.68-1.14 ms against 0.72-1.61 ms
+without the network; S of a sweep within 1.9e-6 of the plain tabulation's.
 """
 
 import ctypes as C
@@ -102,7 +107,7 @@ class GreensSurrogate:
     """
 
     def __init__(self, solver, fmin, fmax, nfreq=64, nrad=256, layers=3, steps=12000, batch=4096, lr=2e-3,
-                 lr_min=1e-5, seed=0, ncheck=48, tol=5e-6):
+                 lr_min=1e-5, seed=0, near=8.0, stride=4, tol=5e-6):
         from .solver import Greens
 
         self.fmin, self.fmax = float(fmin), float(fmax)
@@ -110,7 +115,7 @@ class GreensSurrogate:
         # least accurate at the edges of its inputs
         pad = 0.05 * (self.fmax - self.fmin)
         self.flo, self.fhi = max(self.fmin - pad, 0.5 * self.fmin), self.fmax + pad
-        self.ncheck, self.tol = int(ncheck), float(tol)
+        self.near, self.stride, self.tol = float(near), int(stride), float(tol)
         st = solver.stack
         t = np.array([d.t for d in st.layers], float)
         self.a = float(t[0] if solver.single else t.min())  # the radius scale of the remainder's structure
@@ -159,7 +164,8 @@ class GreensSurrogate:
         d.surrogate = self.net.h.value
         d.sur_a, d.sur_rho_ref, d.sur_fmin, d.sur_fmax = self.a, self.rho_ref, self.flo, self.fhi
         d.sur_scale = scale_ptr
-        d.sur_ncheck = self.ncheck
+        d.sur_near = self.near * self.a
+        d.sur_stride = self.stride
         d.sur_tol = self.tol
 
     def close(self):

@@ -33,7 +33,8 @@ def digest(m):
 
 def host_solver(m):
     """What Solver.lumped_impedance and _load_lumped read, without a device."""
-    return SimpleNamespace(lumped=list(m.layout.lumped), values={}, OPEN=Solver.OPEN, Lm=m.lumped_vectors())
+    return SimpleNamespace(lumped=list(m.layout.lumped), values={}, OPEN=Solver.OPEN, Lm=m.lumped_vectors(),
+                           iports=[], iport_index=[])
 
 
 def test_mesh_and_gap_vectors_match_reference():

@@ -70,39 +70,65 @@ def lpf_surrogate(gpu):
     sol.close()
 
 
+def plan(rho, near, stride):
+    """The radii a learned table integrates (the engine's rule, restated):
+    every radius below `near`, then every stride-th radius and the last (the
+    knots), and the middle radius of each gap between knots (validation).
+    Returns (integrated, knots, validation, rest) index arrays."""
+    n = rho.size
+    n0 = int(np.searchsorted(rho, near, side="left"))
+    knots = list(range(n0)) + list(range(n0, n, stride))
+    if knots[-1] != n - 1:
+        knots.append(n - 1)
+    knots = np.array(knots)
+    val = np.array([(a + b) // 2 for a, b in zip(knots[:-1], knots[1:]) if b - a >= 2], int)
+    ie = np.union1d(knots, val)
+    return ie, knots, val, np.setdiff1d(np.arange(n), ie)
+
+
 def test_surrogate_tables_and_judge(lpf_surrogate):
-    """In-band tables from the learned remainder: the judge's verdict
-    matches the actual error against the full Sommerfeld remainder, and a
-    rejected network leaves the Sommerfeld table untouched."""
+    """Learned tables on the LPF stack: the integrated radii carry the
+    Sommerfeld integral bit for bit; the other radii hold the network plus a
+    not-a-knot spline of its residual through the integrated radii (checked
+    against scipy); the judge's error is the error of the knots-only spline
+    at the validation radii; a rejected table is the plain one bit for bit."""
+    from scipy.interpolate import CubicSpline
+
     sol, sur, freqs = lpf_surrogate
     sol.surrogate = sur
     tol0, sur.tol = sur.tol, 4e-5  # a looser judge, so that some tables take the learned path
     out = []
-    t_sur = t_ref = 0.0
     for f in (0.6e9, 2.3e9, 4.1e9, 7.9e9):
-        t0 = time.perf_counter()
         g = Greens(sol, f)
-        res, (used, err) = g.remainder()
-        t1 = time.perf_counter()
+        res, (used, err, nint) = g.remainder()
         g_ref = Greens(sol, f, surrogate=False)
-        ref, _ = g_ref.remainder()
-        t_sur += t1 - t0
-        t_ref += time.perf_counter() - t1
+        ref, (_, _, nref) = g_ref.remainder()
+        rho = g.rho
+        ie, kn, va, rest = plan(rho, sur.near * sur.a, sur.stride)
+        smax = np.abs(ref[ie]).max()
+        net = sur.predict(rho, f)
+        cs = CubicSpline(rho[kn], ref[kn] - net[kn], bc_type="not-a-knot", axis=0)
+        judged = np.abs(net[va] + cs(rho[va]) - ref[va]).max() / smax
         true_err = np.abs(res - ref).max() / np.abs(ref).max()
-        raw = np.abs(sur.predict(g.rho, f) - ref).max() / np.abs(ref).max()
-        out.append((f, used, err, true_err, raw))
+        out.append((f, used, err, judged, true_err, nint, nref))
+        assert nref == rho.size
+        # the judge, restated (the network's fp32 outputs at the device's features
+        # and at numpy's may differ in the last bit: ~6e-8 of the largest remainder)
+        assert abs(err - judged) <= 0.05 * judged + 1e-7, (err, judged)
+        assert used == (err <= sur.tol)
         if used:
-            assert true_err <= 1.5 * sur.tol, (f, err, true_err)
+            assert nint == ie.size
+            np.testing.assert_array_equal(res[ie], ref[ie])
+            cs2 = CubicSpline(rho[ie], ref[ie] - net[ie], bc_type="not-a-knot", axis=0)
+            fill = net[rest] + cs2(rho[rest])
+            assert np.abs(res[rest] - fill).max() <= 2e-7 * smax
+            assert true_err <= sur.tol
         else:
-            assert true_err == 0.0
-        # the judge's estimate (at radii it did not fit) tracks the actual error
-        if used:
-            assert 0.5 * true_err <= err <= 2 * true_err, (f, err, true_err)
+            assert nint == rho.size
+            np.testing.assert_array_equal(res, ref)
         g.close()
         g_ref.close()
-    print("(f, used, judged error, error vs Sommerfeld, network alone):", out)
-    print(f"Sommerfeld radii per table: {2 * sur.ncheck - 1} with the network, {g_ref.rho.size} without; "
-          f"table time with / without: {t_sur / 4 * 1e3:.2f} / {t_ref / 4 * 1e3:.2f} ms")
+    print("(f, used, judged error, judged error restated, error vs Sommerfeld, radii integrated, radii):", out)
     assert any(o[1] for o in out)
     sur.tol = tol0
     sol.surrogate = None
@@ -120,3 +146,72 @@ def test_surrogate_sweep_within_mixed_bar(lpf_surrogate):
     d = np.abs(r1.S - r0.S).max()
     print("max |dS| with the learned remainder:", d)
     assert d <= 1e-5
+
+
+def _greens_ms(sol, f, surrogate):
+    """Device time of one frequency's Green's tables (CUDA events around the
+    table kernels, the engine's stage timer), the table's remainder info
+    (used, judged error, radii integrated) and its radii."""
+    import ctypes as C
+
+    ms = (C.c_double * 11)()
+    E.check(sol.ctx.lib.m25_ctx_timing(sol.ctx.h, 1, None, None))
+    g = Greens(sol, f, surrogate=surrogate)
+    res, info = g.remainder()
+    sol.ctx.synchronize()
+    E.check(sol.ctx.lib.m25_ctx_timing(sol.ctx.h, 0, ms, None))
+    rho = g.rho
+    g.close()
+    return ms[0], info, rho, res
+
+
+def test_learned_remainder_pays_on_the_via_transition(gpu):
+    """The two-layer via transition (4 level pairs x 3 kernels per radius):
+    a network trained on ~1e6 of the engine's own Sommerfeld remainders over
+    1-20 GHz. At the default judge tolerance it is accepted at most
+    frequencies; each accepted table integrates fewer radii and takes less
+    device time than the plain tabulation; the network's correction through
+    the knots is judged more accurate than a spline of the integral alone
+    through the same knots (what the network adds); and the sweep's S stays
+    within 1e-5 of the plain tabulation's."""
+    from scipy.interpolate import CubicSpline
+
+    lay, st, m, freqs = workloads.build(G, "via")
+    sol = Solver(m, st, verbose=False, precision="mixed")
+    try:
+        sur = GreensSurrogate(sol, 1e9, 20e9, nfreq=1024, nrad=1024, steps=20000)
+        print(f"{sur.nsamples} samples in {sur.sample_seconds:.2f} s, trained in {sur.train_seconds:.2f} s, "
+              f"loss {sur.train_loss:.3e}")
+        assert sur.nsamples >= 1_000_000
+        sol.surrogate = sur
+        fs = np.linspace(1.5e9, 19.5e9, 10)
+        for f in fs[:2]:  # warm-up of both paths
+            _greens_ms(sol, f, True)
+            _greens_ms(sol, f, False)
+        rows = []
+        for f in fs:
+            t_sur, (used, err, nint), rho, _ = _greens_ms(sol, f, True)
+            t_ref, _, _, ref = _greens_ms(sol, f, False)
+            ie, kn, va, rest = plan(rho, sur.near * sur.a, sur.stride)
+            cs = CubicSpline(rho[kn], ref[kn], bc_type="not-a-knot", axis=0)
+            plain_err = np.abs(cs(rho[va]) - ref[va]).max() / np.abs(ref[ie]).max()
+            rows.append((f / 1e9, used, err, plain_err, nint, rho.size, t_sur, t_ref))
+        print("(f GHz, learned table used, judged error, knots-only spline error, radii integrated, radii, "
+              "ms with, ms without):")
+        for r in rows:
+            print("  %.1f %d %.2e %.2e %d %d %.3f %.3f" % r)
+        accepted = [r for r in rows if r[1]]
+        assert len(accepted) >= len(rows) // 2, rows
+        assert all(r[4] < r[5] for r in accepted)  # fewer Sommerfeld radii
+        assert sum(r[6] for r in accepted) < sum(r[7] for r in accepted), rows  # less device time
+        assert np.median([r[2] / r[3] for r in rows]) < 1.0  # the network beats the spline alone
+        f = freqs[::4]
+        r1 = sol.sweep(f)
+        sol.surrogate = None
+        r0 = sol.sweep(f)
+        d = np.abs(r1.S - r0.S).max()
+        print("max |dS| with the learned remainder:", d)
+        assert d <= 1e-5
+        sur.close()
+    finally:
+        sol.close()
