@@ -76,8 +76,8 @@ void* m25_ctx_stream(m25_ctx* ctx); /* the cudaStream_t every call of this conte
  * keeping the process default: panel_cluster_min, the smallest cluster (4, 8
  * or 16 CTAs) the LU panel runs on (default 4, or $M25_PANEL_CLUSTER_MIN);
  * wave_ctas, the CTA cap of the triangular solves (default one per 64-row
- * block, or $M25_WAVE_CTAS); tc_chunk, the k-blocks (12 MMAs each) the
- * tensor-core update accumulates in TMEM before adding into its fp32
+ * block, or $M25_WAVE_CTAS); tc_chunk, the steps of 32 tf32 along K (12 MMAs
+ * each) the tensor-core update accumulates in TMEM before adding into its fp32
  * registers (1..8; default 1, or $M25_TC_CHUNK: longer chunks round the
  * accumulation coarser). */
 int m25_ctx_set_tuning(m25_ctx* ctx, int32_t panel_cluster_min, int32_t wave_ctas, int32_t tc_chunk);

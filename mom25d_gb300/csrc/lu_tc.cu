@@ -47,7 +47,11 @@ namespace m25 {
 
 namespace {
 
+// k-blocks of 32 tf32 (128-byte rows, 128-byte swizzle) in a 2-stage ring (k-blocks
+// of 16 in 4 stages of 40 KB, 64-byte swizzle, measured no faster: 47 % against 50 %
+// tensor pipe on the largest n = 4096 launch)
 constexpr int kBM = 128, kBN = 192, kBK = 32, kStages = 2;
+constexpr int kChunkK = 32;  // tf32 elements per TMEM accumulation per unit of the chunk setting
 constexpr int kTmemCols = 512, kBufStride = 256;  // two accumulators, 256 columns apart
 constexpr int kTileA = kBM * kBK * 4, kTileB = kBN * kBK * 4;
 constexpr int kStageBytes = 2 * (kTileA + kTileB);  // [A hi | A lo | B hi | B lo], each 1024-byte aligned
@@ -112,7 +116,7 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   uint64_t d = 0;
   d |= (uint64_t)((addr & 0x3FFFF) >> 4);
   d |= (uint64_t)1 << 16;            // leading-dimension offset (unused with this swizzle)
-  d |= (uint64_t)(1024 >> 4) << 32;  // stride between 8-row groups
+  d |= (uint64_t)(1024 >> 4) << 32;  // stride between 8-row groups (8 rows of 128 bytes)
   d |= (uint64_t)1 << 46;            // descriptor version
   d |= (uint64_t)2 << 61;            // 128-byte swizzle
   return d;
@@ -138,7 +142,7 @@ struct TcArgs {
   int M, N, P;     // rows, real columns of C (its fp32 view), packed K extent per plane (multiple of 32)
   int pw;          // plane width: the lo plane starts pw floats after the hi plane (pw >= P)
   int tiles_m, ntiles;
-  int chunk;       // k-blocks accumulated afresh in TMEM before the register sum
+  int chunk;       // k-blocks (of kBK) accumulated afresh in TMEM before the register sum
   int* err;
   int* counter;    // tiles handed out beyond the first gridDim.x (zero at launch)
 };
@@ -420,7 +424,8 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-int make_map(CUtensorMap* map, const float* ptr, int rows, int cols_k, int box_rows, int64_t ld = 0) {
+int make_map(CUtensorMap* map, const float* ptr, int rows, int cols_k, int box_cols, int box_rows,
+             CUtensorMapSwizzle swz, int64_t ld = 0) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) {
     set_error("tensor-core LU: cuTensorMapEncodeTiled is not available");
@@ -428,10 +433,10 @@ int make_map(CUtensorMap* map, const float* ptr, int rows, int cols_k, int box_r
   }
   cuuint64_t dims[2] = {(cuuint64_t)cols_k, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)(ld ? ld : cols_k) * sizeof(float)};
-  cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
+  cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(ptr), dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     set_error("tensor-core LU: cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
@@ -553,8 +558,8 @@ int lu_tc_update(m25_ctx* ctx, zf* A, int64_t lda, int r0, int c0, int m, int nc
   int* err = ctx->Dw.as<int>();
   CUtensorMap ma, mb;
   int rc;
-  if ((rc = make_map(&ma, A3, m, 2 * pw, kBM))) return rc;
-  if ((rc = make_map(&mb, B3, n2, 2 * pw, kBN))) return rc;
+  if ((rc = make_map(&ma, A3, m, 2 * pw, kBK, kBM, CU_TENSOR_MAP_SWIZZLE_128B))) return rc;
+  if ((rc = make_map(&mb, B3, n2, 2 * pw, kBK, kBN, CU_TENSOR_MAP_SWIZZLE_128B))) return rc;
   // C: the fp32 view of the block, rows 2 lda floats apart, 32 x 32 boxes
   CUtensorMap mc;
   const float* C = reinterpret_cast<const float*>(A + (int64_t)r0 * lda + c0);
@@ -562,11 +567,11 @@ int lu_tc_update(m25_ctx* ctx, zf* A, int64_t lda, int r0, int c0, int m, int nc
     set_error("tensor-core LU: C needs an even leading dimension and 16-byte alignment");
     return M25_ERR_VALUE;
   }
-  if ((rc = make_map(&mc, C, m, n2, 32, 2 * lda))) return rc;
+  if ((rc = make_map(&mc, C, m, n2, 32, 32, CU_TENSOR_MAP_SWIZZLE_128B, 2 * lda))) return rc;
   const int n_sm = ctx->num_sms;
   static const int chunk = [] {
     const char* e = getenv("M25_TC_CHUNK");
-    return e ? std::max(1, atoi(e)) : 1;  // one k-block: 12 MMAs (3 products x K 32) per TMEM accumulation
+    return e ? std::max(1, atoi(e)) : 1;  // 32 tf32: 12 MMAs (3 products x K 32) per TMEM accumulation
   }();
   TcArgs ta;
   ta.M = m;
@@ -575,7 +580,7 @@ int lu_tc_update(m25_ctx* ctx, zf* A, int64_t lda, int r0, int c0, int m, int nc
   ta.pw = pw;
   ta.tiles_m = (m + kBM - 1) / kBM;
   ta.ntiles = ta.tiles_m * ((n2 + kBN - 1) / kBN);
-  ta.chunk = ctx->tune_tc_chunk > 0 ? ctx->tune_tc_chunk : chunk;
+  ta.chunk = (ctx->tune_tc_chunk > 0 ? ctx->tune_tc_chunk : chunk) * (kChunkK / kBK);  // in k-blocks
   ta.err = err;
   ta.counter = reinterpret_cast<int*>(ctx->Dw.as<char>() + 16) + slot;
   M25_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));

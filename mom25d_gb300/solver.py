@@ -374,6 +374,9 @@ class Solver:
         self.rho_max = 1.02 * np.hypot(*(v.max(0) - v.min(0)))
         self.verbose = verbose
         self.surrogate = None  # a GreensSurrogate (mom25d_gb300.surrogate) for the Green's tables
+        # the engine's knobs of a mixed-precision sweep: "table" -> by N from the table measured
+        # on the device (mom25d_gb300/tuning.json, autotune.py), a Tuning, or None (process defaults)
+        self.tuning = "table"
         self.v_weight = 1.0 if v_weight is None else float(v_weight)
         self.pm = [PortModel(mesh, p, st.level_h(p.layer)) for p in self.ports]
         self.groups = {}
@@ -730,6 +733,21 @@ class Solver:
         s._sib_lock = threading.Lock()
         return s
 
+    def _sweep_tuning(self):
+        """The knob values of this solver's mixed-precision points (None:
+        the process defaults): self.tuning, or the measured table by N."""
+        if self.precision != "mixed" or self.tuning is None:
+            return None
+        if isinstance(self.tuning, str):
+            if self.tuning != "table":
+                raise ValueError('Solver.tuning must be "table", a Tuning or None')
+            from .autotune import load_table
+
+            if not hasattr(Solver, "_table"):
+                Solver._table = load_table()
+            return Solver._table
+        return self.tuning
+
     def _sibling(self, i):
         """Worker i of a concurrent sweep (0: this solver): the same mesh,
         stack and settings on its own engine context (stream, device data)."""
@@ -835,6 +853,7 @@ class Solver:
         steps = [None] * nf
         todo = [fi for fi in range(nf) if not done[fi]]
         workers = max(1, min(int(workers), len(todo) or 1, self._workers_that_fit()))
+        tun = self._sweep_tuning()
         if workers > 1:
             self.geometry()  # built once here, shared by the workers' contexts
         lock = threading.Lock()
@@ -844,6 +863,8 @@ class Solver:
         def work(w):
             try:  # each worker sets up its own context's device data
                 sol = self._sibling(w)
+                if tun is not None:
+                    tun.apply(sol.ctx, self.mesh.n_unknowns)
                 sol.geometry()
                 sol.port_data()
             except Exception as exc:  # noqa: BLE001 - re-raised below in the caller's thread

@@ -182,3 +182,24 @@ def test_tuning_table_rows_by_size(tmp_path):
     assert Tuning.fixed(tc_chunk=2).knobs(10 ** 6) == (0, 0, 2)
     with pytest.raises(ValueError):
         Tuning([dict(n_max=1)])
+
+
+def test_sweep_tuning_choice():
+    """A mixed-precision sweep takes the measured table (by N) unless the
+    solver's tuning says otherwise; fp64 sweeps keep the process defaults."""
+    from mom25d_gb300.autotune import Tuning, load_table
+    from mom25d_gb300.solver import Solver
+
+    s = object.__new__(Solver)
+    s.precision, s.tuning = "mixed", "table"
+    t = s._sweep_tuning()
+    assert t is not None and t.knobs(5943) == load_table().knobs(5943)
+    s.tuning = fixed = Tuning.fixed(panel_cluster_min=8)
+    assert s._sweep_tuning() is fixed
+    s.tuning = None
+    assert s._sweep_tuning() is None
+    s.precision, s.tuning = "fp64", "table"
+    assert s._sweep_tuning() is None
+    s.precision, s.tuning = "mixed", "best"
+    with pytest.raises(ValueError):
+        s._sweep_tuning()
