@@ -41,8 +41,10 @@ struct FillArgs {
   cx<T> lead[kMaxLevSq][2];  // cA, cV of pair (lt*L + ls)
   T dz[kMaxLevSq];
   cx<T> jwmu, inv_jwe, zs;
-  cx<T>* H;            // (3 nt, ldh)
+  cx<T>* H;            // (3 nt, ldh) (fp64 fill)
   int64_t ldh;
+  cx<float>* H32;      // mixed fill: (3 nt, ldh), the mid / far pairs' values (computed in fp32)
+  cx<T>* Hn;           // mixed fill: (nnear, 3 j, 3 i, 32 lanes), the near pairs' values
   cx<T>* IVpad;        // (npad, nt)
   // fp32 copies for far pairs evaluated in fp32 (fill_tri_kernel<double, true>)
   const TriData<float>* td32;
@@ -471,12 +473,29 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
         }
     }
     if (active) {
+      if (FAR32 && code >= 0) {
+        // near pair: [code][j][i][lane], the 32 lanes' words consecutive
+        cx<T>* hn = a.Hn + (int64_t)code * 288 + lane;
 #pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        cx<T>* row = a.H + (int64_t)(3 * s + j) * a.ldh + col0;
-        row[0] = out[0][j];
-        row[1] = out[1][j];
-        row[2] = out[2][j];
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+          for (int i = 0; i < 3; ++i) hn[(j * 3 + i) * 32] = out[i][j];
+      } else if (FAR32) {
+        // mid / far pair: fp32 values, exactly as computed
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          cx<float>* row = a.H32 + (int64_t)(3 * s + j) * a.ldh + col0;
+#pragma unroll
+          for (int i = 0; i < 3; ++i) row[i] = cx<float>(float(out[i][j].re), float(out[i][j].im));
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          cx<T>* row = a.H + (int64_t)(3 * s + j) * a.ldh + col0;
+          row[0] = out[0][j];
+          row[1] = out[1][j];
+          row[2] = out[2][j];
+        }
       }
       if (pad >= 0) a.IVpad[(int64_t)pad * a.nt + s] = IV;
     }
@@ -489,7 +508,13 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
 }
 
 // Z[m][n] = 0.5 (Zr[m][n] + Zr[n][m]), Zr[m][n] = sum over the two triangles
-// of m (test) and of n (source) of H[3 t_n + j_n][slot(t_m) * 3 + i_m].
+// t_m, local edges i_m of m (test) and t_n, j_n of n (source) of the
+// half-basis value h(t_m, i_m; t_n, j_n). The fp64 fill holds every h in H
+// at [3 t_n + j_n][3 slot(t_m) + i_m]; the mixed fill (MIX) holds the mid /
+// far pairs' h in the complex64 H32 at the same place and the near pairs' in
+// Hn at [code][j_n][i_m][lane of t_m], code = the pair's index in the class
+// table cls[block of t_m][t_n] (>= 0 for near pairs). Either way the sums
+// are taken in the same order with the same values.
 // SPLIT (mixed precision without vias): Z itself is not stored but its
 // double-float planes Zh = fl32(Z), Zl = fl32(Z - Zh) (rows nb apart) and the
 // complex64 LU input (Zh, rows ldl apart).
@@ -498,9 +523,11 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
 // it to Z[n][m] as well through a shared-memory transpose, which halves the
 // scattered reads of H (Z is symmetric by construction). Diagonal tiles form
 // all their entries directly.
-template <class T, class TO, bool SPLIT>
-__global__ void __launch_bounds__(256) gather_sym_kernel(int nb, const cx<T>* __restrict__ H, int64_t ldh,
-                                                         const int32_t* __restrict__ etri,
+template <class T, class TO, bool SPLIT, bool MIX>
+__global__ void __launch_bounds__(256) gather_sym_kernel(int nb, const cx<T>* __restrict__ H,
+                                                         const cx<float>* __restrict__ H32,
+                                                         const cx<T>* __restrict__ Hn, const int32_t* __restrict__ cls,
+                                                         int nt, int64_t ldh, const int32_t* __restrict__ etri,
                                                          const int32_t* __restrict__ eloc,
                                                          const int32_t* __restrict__ tpos, cx<TO>* __restrict__ Z,
                                                          int64_t ldz, zf* __restrict__ Zh, zf* __restrict__ Zl,
@@ -520,34 +547,45 @@ __global__ void __launch_bounds__(256) gather_sym_kernel(int nb, const cx<T>* __
       Z[(int64_t)m * ldz + n] = cx<TO>(z);
     }
   };
+  // h(test triangle at slot sl, local i; source triangle s, local j)
+  auto h = [&](int sl, int i, int s, int j) -> cx<T> {
+    if constexpr (MIX) {
+      const int code = cls[(int64_t)(sl >> 5) * nt + s];
+      if (code >= 0) return Hn[(int64_t)code * 288 + (j * 3 + i) * 32 + (sl & 31)];
+      const cx<float> v = H32[(int64_t)(3 * s + j) * ldh + 3 * (int64_t)sl + i];
+      return cx<T>(T(v.re), T(v.im));
+    } else {
+      return H[(int64_t)(3 * s + j) * ldh + 3 * (int64_t)sl + i];
+    }
+  };
   const int nn = tn * 32 + tx;
   const bool nok = nn < nb;
-  int64_t rn[2], cn[2];
+  int tnb[2], lnb[2], snb[2];  // n's triangles, local edges, slots
 #pragma unroll
   for (int a = 0; a < 2; ++a) {
-    const int tni = nok ? etri[2 * nn + a] : 0, lni = nok ? eloc[2 * nn + a] : 0;
-    rn[a] = 3 * (int64_t)tni + lni;
-    cn[a] = 3 * (int64_t)(nok ? tpos[tni] : 0) + lni;
+    tnb[a] = nok ? etri[2 * nn + a] : 0;
+    lnb[a] = nok ? eloc[2 * nn + a] : 0;
+    snb[a] = nok ? tpos[tnb[a]] : 0;
   }
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int m = tm * 32 + ty + 8 * k;
     cx<T> z;
     if (nok && m < nb) {
-      int64_t rm[2], cm[2];
+      int tma[2], lma[2], sma[2];
 #pragma unroll
       for (int a = 0; a < 2; ++a) {
-        const int tmi = etri[2 * m + a], lmi = eloc[2 * m + a];
-        rm[a] = 3 * (int64_t)tmi + lmi;
-        cm[a] = 3 * (int64_t)tpos[tmi] + lmi;
+        tma[a] = etri[2 * m + a];
+        lma[a] = eloc[2 * m + a];
+        sma[a] = tpos[tma[a]];
       }
       cx<T> s1, s2;
 #pragma unroll
       for (int a = 0; a < 2; ++a)
 #pragma unroll
         for (int b = 0; b < 2; ++b) {
-          s1 += H[rn[b] * ldh + cm[a]];  // test m, source n
-          s2 += H[rm[a] * ldh + cn[b]];  // test n, source m
+          s1 += h(sma[a], lma[a], tnb[b], lnb[b]);  // test m, source n
+          s2 += h(snb[b], lnb[b], tma[a], lma[a]);  // test n, source m
         }
       z = (s1 + s2) * T(0.5);
       store(m, nn, z);
@@ -678,11 +716,19 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   const int nrho = gr->nrho;
   const int64_t ldh = (int64_t)geom->nblocks * 96;
   int rc;
-  if ((rc = ctx->H.ensure(sizeof(cx<T>) * (size_t)3 * nt * ldh + sizeof(cx<T>) * (size_t)std::max(geom->npad, 1) * nt +
-                          sizeof(double) * 16)))
+  // scratch: the half-basis values (fp64 fill: H, complex of T; mixed fill:
+  // H32 for the mid / far pairs and Hn for the near pairs), the via pads'
+  // charge integrals and Im gV(0)
+  const bool f32 = far32 && std::is_same<T, double>::value;
+  const size_t hbytes = f32 ? sizeof(cx<float>) * (size_t)3 * nt * ldh +
+                                  sizeof(cx<T>) * 288 * (size_t)std::max<int64_t>(geom->nnear, 1)
+                            : sizeof(cx<T>) * (size_t)3 * nt * ldh;
+  if ((rc = ctx->H.ensure(hbytes + sizeof(cx<T>) * (size_t)std::max(geom->npad, 1) * nt + sizeof(double) * 16)))
     return rc;
-  cx<T>* H = ctx->H.as<cx<T>>();
-  cx<T>* IVpad = H + (size_t)3 * nt * ldh;
+  cx<T>* H = f32 ? nullptr : ctx->H.as<cx<T>>();
+  cx<float>* H32 = f32 ? ctx->H.as<cx<float>>() : nullptr;
+  cx<T>* Hn = f32 ? reinterpret_cast<cx<T>*>(H32 + (size_t)3 * nt * ldh) : nullptr;
+  cx<T>* IVpad = reinterpret_cast<cx<T>*>(ctx->H.as<char>() + hbytes);
   double* imgv = reinterpret_cast<double*>(IVpad + (size_t)std::max(geom->npad, 1) * nt);
   cx<T>* Z = static_cast<cx<T>*>(Zout);
   int64_t ldzd = ldz;
@@ -725,8 +771,9 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   a.zs = cx<T>(T(zs.re), T(zs.im));
   a.H = H;
   a.ldh = ldh;
+  a.H32 = H32;
+  a.Hn = Hn;
   a.IVpad = IVpad;
-  const bool f32 = far32 && std::is_same<T, double>::value;
   a.td32 = geom->td32;
   a.coef32 = gr->coef32;
   for (int p = 0; p < L * L; ++p) {
@@ -797,11 +844,23 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
       set_error("m25_assemble: split output needs the mixed fill without vias");
       return M25_ERR_VALUE;
     }
-    gather_sym_kernel<T, T, true><<<gtiles, 256, 0, st>>>(nb, H, ldh, geom->edge_tri, geom->edge_loc, geom->tpos,
-                                                          nullptr, 0, split->Zh, split->Zl, split->LU, split->ldl);
+    if (f32)
+      gather_sym_kernel<T, T, true, true><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->cls, nt, ldh,
+                                                                  geom->edge_tri, geom->edge_loc, geom->tpos, nullptr,
+                                                                  0, split->Zh, split->Zl, split->LU, split->ldl);
+    else
+      gather_sym_kernel<T, T, true, false><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->cls, nt, ldh,
+                                                                   geom->edge_tri, geom->edge_loc, geom->tpos,
+                                                                   nullptr, 0, split->Zh, split->Zl, split->LU,
+                                                                   split->ldl);
+  } else if (f32) {
+    gather_sym_kernel<T, T, false, true><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->cls, nt, ldh,
+                                                                 geom->edge_tri, geom->edge_loc, geom->tpos, Z,
+                                                                 ldzd, nullptr, nullptr, nullptr, 0);
   } else {
-    gather_sym_kernel<T, T, false><<<gtiles, 256, 0, st>>>(nb, H, ldh, geom->edge_tri, geom->edge_loc, geom->tpos,
-                                                           Z, ldzd, nullptr, nullptr, nullptr, 0);
+    gather_sym_kernel<T, T, false, false><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->cls, nt, ldh,
+                                                                  geom->edge_tri, geom->edge_loc, geom->tpos, Z,
+                                                                  ldzd, nullptr, nullptr, nullptr, 0);
   }
   }
   M25_CHECK_LAUNCH();

@@ -767,8 +767,10 @@ class Solver:
         nt, N = int(mesh.tri_layer.size), int(mesh.n_unknowns)
         nv = N - int(mesh.n_basis)
         nblocks = (nt + 31) // 32 + len(mesh.layer_names)
-        elem = 8 if self.precision == "mixed_fill32" else 16
-        b = elem * 3 * nt * nblocks * 96                # fill scratch H
+        elem = 16 if self.precision == "fp64" else 8
+        b = elem * 3 * nt * nblocks * 96                # fill scratch: H (fp64), H32 (mixed fills)
+        if self.precision == "mixed":
+            b += b // 4                                 # the near pairs' fp64 values (Hn), a bound
         if self.precision == "fp64":
             b += 16 * N * N                             # Z, factored in place
         else:
