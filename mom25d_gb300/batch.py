@@ -108,6 +108,8 @@ class VariantBatch:
         def view(w, v):
             if views[w][v] is None:
                 views[w][v] = self.solvers[v]._clone(ctx=ctxs[w])
+            for k in self.solvers[v]._SETTINGS:  # the variant's settings as they are now
+                setattr(views[w][v], k, getattr(self.solvers[v], k))
             return views[w][v]
 
         def work(w):

@@ -748,9 +748,13 @@ class Solver:
             return Solver._table
         return self.tuning
 
+    # what a caller may change between sweeps; a sweep hands the current values to its workers
+    _SETTINGS = ("precision", "method", "refine_tol", "max_refine", "z0_fixed", "v_weight", "surrogate", "tuning")
+
     def _sibling(self, i):
         """Worker i of a concurrent sweep (0: this solver): the same mesh,
-        stack and settings on its own engine context (stream, device data)."""
+        stack and settings on its own engine context (stream, device data);
+        an existing worker takes this solver's current settings."""
         if i == 0:
             return self
         if self._blocks_host is None:
@@ -758,7 +762,10 @@ class Solver:
         with self._sib_lock:
             while len(self._siblings) < i:
                 self._siblings.append(self._clone())
-            return self._siblings[i - 1]
+            sib = self._siblings[i - 1]
+        for k in self._SETTINGS:
+            setattr(sib, k, getattr(self, k))
+        return sib
 
     def _worker_bytes(self):
         """Device memory of one more worker: fill scratch, the matrix planes

@@ -203,3 +203,22 @@ def test_sweep_tuning_choice():
     s.precision, s.tuning = "mixed", "best"
     with pytest.raises(ValueError):
         s._sweep_tuning()
+
+
+def test_sweep_workers_take_current_settings():
+    """A worker made by an earlier sweep takes the solver's settings as they
+    are now (a learned remainder or tuning attached between sweeps)."""
+    import threading
+    from types import SimpleNamespace
+
+    from mom25d_gb300.solver import Solver
+
+    s = object.__new__(Solver)
+    s._blocks_host = True
+    s._sib_lock = threading.Lock()
+    s._siblings = [SimpleNamespace(**{k: None for k in Solver._SETTINGS})]
+    for k in Solver._SETTINGS:
+        setattr(s, k, "now-" + k)
+    sib = s._sibling(1)
+    assert all(getattr(sib, k) == "now-" + k for k in Solver._SETTINGS)
+    assert s._sibling(0) is s
