@@ -169,7 +169,10 @@ def run_ours(args, rank, world, local):
     tol_kw = {} if args.refine_tol is None else {"refine_tol": args.refine_tol}
     sol = Solver(mesh, st, verbose=False, precision=args.precision, device=local, **tol_kw)
     sols = [sol._sibling(w) for w in range(K)]
+    tun = sol._sweep_tuning()  # the engine's knobs by N, as Solver.sweep sets them
     for s_ in sols:
+        if tun is not None:
+            tun.apply(s_.ctx, n)
         s_.geometry()
         s_.port_data()
     warm = my[:args.warmup]
@@ -273,6 +276,44 @@ def run_ours(args, rank, world, local):
         n64 = len(sub)
         max_dS = float(np.abs(r.S[idx] - r64.S).max())
         s64.close()
+    # the learned remainder (mixed + surrogate): a network trained on this
+    # stack's Sommerfeld remainders over the workload's band before the timed
+    # sweep (its training time reported, not in the points/s), then the same
+    # points through Solver.sweep like e2e, S against the fp64 path
+    sur_arm = None
+    if args.precision == "mixed" and world == 1 and not args.no_surrogate:
+        from mom25d_gb300.solver import Greens
+        from mom25d_gb300.surrogate import GreensSurrogate
+
+        s3 = Solver(mesh, st, verbose=False, precision="mixed", device=local, **tol_kw)
+        t0 = time.perf_counter()
+        sur = GreensSurrogate(s3, float(min(freqs)), float(max(freqs)), nfreq=256, nrad=512, steps=20000)
+        t_train = time.perf_counter() - t0
+        s3.surrogate = sur
+        s3.sweep(pts[:K], workers=K)  # the workers' contexts and buffers, untimed
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r3 = s3.sweep(pts, workers=K)
+        torch.cuda.synchronize()
+        dt3 = time.perf_counter() - t0
+        used = []
+        for f in pts[::max(1, len(pts) // 16)]:
+            g = Greens(s3, f)
+            info = g.remainder()[1]
+            used.append((info[0], info[2], g.rho.size))
+            g.close()
+        sur_arm = {"value": round(len(pts) / dt3, 4), "unit": UNIT,
+                   "timing": "Solver.sweep with the learned remainder attached: the same points, workers, host "
+                             "arrays in and S out as e2e",
+                   "e2e_without": round(world * args.steps / dt_e2e, 4),
+                   "train_seconds": round(t_train, 2), "samples": sur.nsamples,
+                   "tables_learned": f"{sum(u for u, _, _ in used)} of {len(used)} sampled frequencies",
+                   "sommerfeld_radii": f"{sum(k for _, k, _ in used)} of {sum(m for _, _, m in used)}",
+                   "max_dS_vs_mixed": float(np.abs(r3.S - r.S).max())}
+        if args.fp64_points > 0 and max_dS is not None:
+            sur_arm["max_dS_vs_fp64"] = float(np.abs(r3.S[idx] - r64.S).max())
+        sur.close()
+        s3.close()
     # max over ranks
     tt = torch.tensor([dt, dt_e2e], dtype=torch.float64, device="cuda")
     if world > 1:
@@ -320,7 +361,7 @@ def run_ours(args, rank, world, local):
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(step_ms, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64+c128" if args.precision == "mixed" else "c128", "data": "synthetic",
-        "config": dict(WORKLOAD, precision=args.precision, l2="inputs > L2 (Z 283 MB, fill scratch 1.2 GB per step)"),
+        "config": dict(WORKLOAD, precision=args.precision, l2="inputs > L2 (Z 283 MB, fill scratch 1.4 GB per step)"),
         "e2e": {"value": round(world * args.steps / dt_e2e, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "workers": K, "stages_ms_per_point_worker0": stages, "gpu_launches": int(launches),
@@ -331,6 +372,8 @@ def run_ours(args, rank, world, local):
         "roofline": roof, "clocks": clk.summary(), "geometry": geo,
         "refine_steps": r.info["refine_steps"][:4] if r.info else None,
     }
+    if sur_arm is not None:
+        out["surrogate"] = sur_arm
     if world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline()
     return out
@@ -408,6 +451,7 @@ def main():
                     help="timed points also run on the fp64 path (same workers): its points/s and max |dS|")
     ap.add_argument("--workers", type=int, default=8, help="frequency points in flight on the GPU")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the mixed + learned-remainder arm")
     ap.add_argument("--refine-tol", type=float, default=None, help="mixed path: backward-error target of the refinement")
     ap.add_argument("--serial-points", type=int, default=1,
                     help="reference arm: points also timed as mom25d runs them (one process, 4 BLAS threads)")

@@ -23,6 +23,11 @@
 
 namespace m25 {
 
+// mixed fill: H32's entry of a near pair, a quiet NaN carrying the pair's code
+// (< 2^22) in its payload; the gather reads the fp64 value from Hn
+constexpr uint32_t kNearTag = 0x7FC00000u;
+constexpr int64_t kMaxNearTagged = (1 << 22) - 1;
+
 template <class T>
 struct FillArgs {
   int nt, nb, nlev, nblocks, n_src_chunk, n_chunks;
@@ -474,12 +479,19 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
     }
     if (active) {
       if (FAR32 && code >= 0) {
-        // near pair: [code][j][i][lane], the 32 lanes' words consecutive
+        // near pair: [code][j][i][lane], the 32 lanes' words consecutive, and
+        // in H32 a quiet NaN whose payload is the code (kNearTag)
         cx<T>* hn = a.Hn + (int64_t)code * 288 + lane;
+        const cx<float> tag(__uint_as_float(kNearTag | (uint32_t)code), 0.f);
 #pragma unroll
-        for (int j = 0; j < 3; ++j)
+        for (int j = 0; j < 3; ++j) {
+          cx<float>* row = a.H32 + (int64_t)(3 * s + j) * a.ldh + col0;
 #pragma unroll
-          for (int i = 0; i < 3; ++i) hn[(j * 3 + i) * 32] = out[i][j];
+          for (int i = 0; i < 3; ++i) {
+            hn[(j * 3 + i) * 32] = out[i][j];
+            row[i] = tag;
+          }
+        }
       } else if (FAR32) {
         // mid / far pair: fp32 values, exactly as computed
 #pragma unroll
@@ -512,9 +524,9 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
 // half-basis value h(t_m, i_m; t_n, j_n). The fp64 fill holds every h in H
 // at [3 t_n + j_n][3 slot(t_m) + i_m]; the mixed fill (MIX) holds the mid /
 // far pairs' h in the complex64 H32 at the same place and the near pairs' in
-// Hn at [code][j_n][i_m][lane of t_m], code = the pair's index in the class
-// table cls[block of t_m][t_n] (>= 0 for near pairs). Either way the sums
-// are taken in the same order with the same values.
+// Hn at [code][j_n][i_m][lane of t_m], code = the pair's index among the near
+// pairs, which H32 carries in a NaN at the pair's place (kNearTag). Either
+// way the sums are taken in the same order with the same values.
 // SPLIT (mixed precision without vias): Z itself is not stored but its
 // double-float planes Zh = fl32(Z), Zl = fl32(Z - Zh) (rows nb apart) and the
 // complex64 LU input (Zh, rows ldl apart).
@@ -526,8 +538,8 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
 template <class T, class TO, bool SPLIT, bool MIX>
 __global__ void __launch_bounds__(256) gather_sym_kernel(int nb, const cx<T>* __restrict__ H,
                                                          const cx<float>* __restrict__ H32,
-                                                         const cx<T>* __restrict__ Hn, const int32_t* __restrict__ cls,
-                                                         int nt, int64_t ldh, const int32_t* __restrict__ etri,
+                                                         const cx<T>* __restrict__ Hn, int64_t nnear, int64_t ldh,
+                                                         const int32_t* __restrict__ etri,
                                                          const int32_t* __restrict__ eloc,
                                                          const int32_t* __restrict__ tpos, cx<TO>* __restrict__ Z,
                                                          int64_t ldz, zf* __restrict__ Zh, zf* __restrict__ Zl,
@@ -550,44 +562,66 @@ __global__ void __launch_bounds__(256) gather_sym_kernel(int nb, const cx<T>* __
   // h(test triangle at slot sl, local i; source triangle s, local j)
   auto h = [&](int sl, int i, int s, int j) -> cx<T> {
     if constexpr (MIX) {
-      const int code = cls[(int64_t)(sl >> 5) * nt + s];
-      if (code >= 0) return Hn[(int64_t)code * 288 + (j * 3 + i) * 32 + (sl & 31)];
       const cx<float> v = H32[(int64_t)(3 * s + j) * ldh + 3 * (int64_t)sl + i];
+      const uint32_t u = __float_as_uint(v.re);
+      if ((u & 0xFFC00000u) == kNearTag && (int64_t)(u & 0x3FFFFFu) < nnear)
+        return Hn[(int64_t)(u & 0x3FFFFFu) * 288 + (j * 3 + i) * 32 + (sl & 31)];
       return cx<T>(T(v.re), T(v.im));
     } else {
       return H[(int64_t)(3 * s + j) * ldh + 3 * (int64_t)sl + i];
     }
   };
+  // the RWG's two triangles, local edges and slots
+  auto rwg = [&](int e, int (&t)[2], int (&l)[2], int (&sl)[2]) {
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+      t[a] = etri[2 * e + a];
+      l[a] = eloc[2 * e + a];
+      sl[a] = tpos[t[a]];
+    }
+  };
+  // s1[m][n] = sum of h(test m, source n) with the lanes over m: the lanes of
+  // a warp read consecutive test slots of one source row of H (the sum of the
+  // same terms in the same order as below, only the thread that forms it
+  // differs); kept in shared memory as s1t[n][m]
+  __shared__ cx<T> s1t[32][33];
+  {
+    const int m = tm * 32 + tx;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int n = tn * 32 + ty + 8 * k;
+      cx<T> s1;
+      if (m < nb && n < nb) {
+        int tma[2], lma[2], sma[2], tnb[2], lnb[2], snb[2];
+        rwg(m, tma, lma, sma);
+        rwg(n, tnb, lnb, snb);
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+          for (int b = 0; b < 2; ++b) s1 += h(sma[a], lma[a], tnb[b], lnb[b]);  // test m, source n
+      }
+      s1t[ty + 8 * k][tx] = s1;
+    }
+  }
+  __syncthreads();
+  // s2[m][n] = sum of h(test n, source m) with the lanes over n, and Z
   const int nn = tn * 32 + tx;
   const bool nok = nn < nb;
-  int tnb[2], lnb[2], snb[2];  // n's triangles, local edges, slots
-#pragma unroll
-  for (int a = 0; a < 2; ++a) {
-    tnb[a] = nok ? etri[2 * nn + a] : 0;
-    lnb[a] = nok ? eloc[2 * nn + a] : 0;
-    snb[a] = nok ? tpos[tnb[a]] : 0;
-  }
+  int tnb[2], lnb[2], snb[2];
+  if (nok) rwg(nn, tnb, lnb, snb);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int m = tm * 32 + ty + 8 * k;
     cx<T> z;
     if (nok && m < nb) {
       int tma[2], lma[2], sma[2];
-#pragma unroll
-      for (int a = 0; a < 2; ++a) {
-        tma[a] = etri[2 * m + a];
-        lma[a] = eloc[2 * m + a];
-        sma[a] = tpos[tma[a]];
-      }
-      cx<T> s1, s2;
+      rwg(m, tma, lma, sma);
+      cx<T> s2;
 #pragma unroll
       for (int a = 0; a < 2; ++a)
 #pragma unroll
-        for (int b = 0; b < 2; ++b) {
-          s1 += h(sma[a], lma[a], tnb[b], lnb[b]);  // test m, source n
-          s2 += h(snb[b], lnb[b], tma[a], lma[a]);  // test n, source m
-        }
-      z = (s1 + s2) * T(0.5);
+        for (int b = 0; b < 2; ++b) s2 += h(snb[b], lnb[b], tma[a], lma[a]);  // test n, source m
+      z = (s1t[tx][ty + 8 * k] + s2) * T(0.5);
       store(m, nn, z);
     }
     tile[ty + 8 * k][tx] = z;
@@ -725,6 +759,10 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
                             : sizeof(cx<T>) * (size_t)3 * nt * ldh;
   if ((rc = ctx->H.ensure(hbytes + sizeof(cx<T>) * (size_t)std::max(geom->npad, 1) * nt + sizeof(double) * 16)))
     return rc;
+  if (f32 && geom->nnear > kMaxNearTagged) {
+    set_error("m25_assemble: too many near pairs for the mixed fill's tagged scratch");
+    return M25_ERR_VALUE;
+  }
   cx<T>* H = f32 ? nullptr : ctx->H.as<cx<T>>();
   cx<float>* H32 = f32 ? ctx->H.as<cx<float>>() : nullptr;
   cx<T>* Hn = f32 ? reinterpret_cast<cx<T>*>(H32 + (size_t)3 * nt * ldh) : nullptr;
@@ -845,20 +883,20 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
       return M25_ERR_VALUE;
     }
     if (f32)
-      gather_sym_kernel<T, T, true, true><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->cls, nt, ldh,
+      gather_sym_kernel<T, T, true, true><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->nnear, ldh,
                                                                   geom->edge_tri, geom->edge_loc, geom->tpos, nullptr,
                                                                   0, split->Zh, split->Zl, split->LU, split->ldl);
     else
-      gather_sym_kernel<T, T, true, false><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->cls, nt, ldh,
+      gather_sym_kernel<T, T, true, false><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->nnear, ldh,
                                                                    geom->edge_tri, geom->edge_loc, geom->tpos,
                                                                    nullptr, 0, split->Zh, split->Zl, split->LU,
                                                                    split->ldl);
   } else if (f32) {
-    gather_sym_kernel<T, T, false, true><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->cls, nt, ldh,
+    gather_sym_kernel<T, T, false, true><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->nnear, ldh,
                                                                  geom->edge_tri, geom->edge_loc, geom->tpos, Z,
                                                                  ldzd, nullptr, nullptr, nullptr, 0);
   } else {
-    gather_sym_kernel<T, T, false, false><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->cls, nt, ldh,
+    gather_sym_kernel<T, T, false, false><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->nnear, ldh,
                                                                   geom->edge_tri, geom->edge_loc, geom->tpos, Z,
                                                                   ldzd, nullptr, nullptr, nullptr, 0);
   }
