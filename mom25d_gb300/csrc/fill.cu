@@ -521,24 +521,18 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
 
 // Z[m][n] = 0.5 (Zr[m][n] + Zr[n][m]), Zr[m][n] = sum over the two triangles
 // t_m, local edges i_m of m (test) and t_n, j_n of n (source) of the
-// half-basis value h(t_m, i_m; t_n, j_n). The fp64 fill holds every h in H
-// at [3 t_n + j_n][3 slot(t_m) + i_m]; the mixed fill (MIX) holds the mid /
-// far pairs' h in the complex64 H32 at the same place and the near pairs' in
-// Hn at [code][j_n][i_m][lane of t_m], code = the pair's index among the near
-// pairs, which H32 carries in a NaN at the pair's place (kNearTag). Either
-// way the sums are taken in the same order with the same values.
-// SPLIT (mixed precision without vias): Z itself is not stored but its
+// half-basis value h(t_m, i_m; t_n, j_n), held in H at [3 t_n + j_n][3
+// slot(t_m) + i_m] (the fp64 fill). SPLIT: Z itself is not stored but its
 // double-float planes Zh = fl32(Z), Zl = fl32(Z - Zh) (rows nb apart) and the
 // complex64 LU input (Zh, rows ldl apart).
-// Each pair (m, n) of the upper triangle is formed once: one
-// CTA per 32 x 32 tile (tile row <= tile column) computes Z[m][n] and writes
-// it to Z[n][m] as well through a shared-memory transpose, which halves the
-// scattered reads of H (Z is symmetric by construction). Diagonal tiles form
-// all their entries directly.
-template <class T, class TO, bool SPLIT, bool MIX>
-__global__ void __launch_bounds__(256) gather_sym_kernel(int nb, const cx<T>* __restrict__ H,
-                                                         const cx<float>* __restrict__ H32,
-                                                         const cx<T>* __restrict__ Hn, int64_t nnear, int64_t ldh,
+// Each pair (m, n) of the upper triangle is formed once: one CTA per 32 x 32
+// tile (tile row <= tile column) computes Z[m][n] and writes it to Z[n][m] as
+// well through a shared-memory transpose (Z is symmetric by construction).
+// The half-sum over h(test m, source n) is taken with the lanes along m and
+// the one over h(test n, source m) with the lanes along n, so that both read
+// runs of one row of H. Diagonal tiles form all their entries directly.
+template <class T, class TO, bool SPLIT>
+__global__ void __launch_bounds__(256) gather_sym_kernel(int nb, const cx<T>* __restrict__ H, int64_t ldh,
                                                          const int32_t* __restrict__ etri,
                                                          const int32_t* __restrict__ eloc,
                                                          const int32_t* __restrict__ tpos, cx<TO>* __restrict__ Z,
@@ -547,6 +541,7 @@ __global__ void __launch_bounds__(256) gather_sym_kernel(int nb, const cx<T>* __
   const int tm = blockIdx.y, tn = blockIdx.x;
   if (tm > tn) return;
   __shared__ cx<T> tile[32][33];
+  __shared__ cx<T> s1t[32][33];  // s1t[n][m]: the half-sum over h(test m, source n)
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   auto store = [&](int m, int n, cx<T> z) {
     if constexpr (SPLIT) {
@@ -559,19 +554,6 @@ __global__ void __launch_bounds__(256) gather_sym_kernel(int nb, const cx<T>* __
       Z[(int64_t)m * ldz + n] = cx<TO>(z);
     }
   };
-  // h(test triangle at slot sl, local i; source triangle s, local j)
-  auto h = [&](int sl, int i, int s, int j) -> cx<T> {
-    if constexpr (MIX) {
-      const cx<float> v = H32[(int64_t)(3 * s + j) * ldh + 3 * (int64_t)sl + i];
-      const uint32_t u = __float_as_uint(v.re);
-      if ((u & 0xFFC00000u) == kNearTag && (int64_t)(u & 0x3FFFFFu) < nnear)
-        return Hn[(int64_t)(u & 0x3FFFFFu) * 288 + (j * 3 + i) * 32 + (sl & 31)];
-      return cx<T>(T(v.re), T(v.im));
-    } else {
-      return H[(int64_t)(3 * s + j) * ldh + 3 * (int64_t)sl + i];
-    }
-  };
-  // the RWG's two triangles, local edges and slots
   auto rwg = [&](int e, int (&t)[2], int (&l)[2], int (&sl)[2]) {
 #pragma unroll
     for (int a = 0; a < 2; ++a) {
@@ -580,11 +562,7 @@ __global__ void __launch_bounds__(256) gather_sym_kernel(int nb, const cx<T>* __
       sl[a] = tpos[t[a]];
     }
   };
-  // s1[m][n] = sum of h(test m, source n) with the lanes over m: the lanes of
-  // a warp read consecutive test slots of one source row of H (the sum of the
-  // same terms in the same order as below, only the thread that forms it
-  // differs); kept in shared memory as s1t[n][m]
-  __shared__ cx<T> s1t[32][33];
+  auto h = [&](int sl, int i, int s, int j) { return H[(int64_t)(3 * s + j) * ldh + 3 * (int64_t)sl + i]; };
   {
     const int m = tm * 32 + tx;
 #pragma unroll
@@ -604,7 +582,6 @@ __global__ void __launch_bounds__(256) gather_sym_kernel(int nb, const cx<T>* __
     }
   }
   __syncthreads();
-  // s2[m][n] = sum of h(test n, source m) with the lanes over n, and Z
   const int nn = tn * 32 + tx;
   const bool nok = nn < nb;
   int tnb[2], lnb[2], snb[2];
@@ -622,6 +599,129 @@ __global__ void __launch_bounds__(256) gather_sym_kernel(int nb, const cx<T>* __
 #pragma unroll
         for (int b = 0; b < 2; ++b) s2 += h(snb[b], lnb[b], tma[a], lma[a]);  // test n, source m
       z = (s1t[tx][ty + 8 * k] + s2) * T(0.5);
+      store(m, nn, z);
+    }
+    tile[ty + 8 * k][tx] = z;
+  }
+  if (tm == tn) return;  // uniform over the CTA
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int n2 = tn * 32 + ty + 8 * k, m2 = tm * 32 + tx;
+    if (n2 < nb && m2 < nb) store(n2, m2, tile[tx][ty + 8 * k]);
+  }
+}
+
+// Double-float sums on the fp32 pipes (the fp64 pipe of this GPU would bound
+// the gather: ~26 fp64 operations per entry): a running fp32 sum h and its
+// rounding errors (Knuth's two-sum) summed in l.
+struct DF2 {
+  float hr = 0.f, lr = 0.f, hi = 0.f, li = 0.f;  // re = hr + lr, im = hi + li
+};
+__device__ __forceinline__ void df_acc(float& h, float& l, float x) {
+  const float s = h + x, z = s - h;
+  l += (h - (s - z)) + (x - z);
+  h = s;
+}
+
+// The same Z for the mixed fill: the mid / far pairs' h are complex64 in H32
+// (exactly as computed, in fp32), the near pairs' are fp64 in Hn at
+// [code][j_n][i_m][lane of t_m], code = the pair's index among the near pairs,
+// which H32 carries in a NaN at the pair's place (kNearTag). Sums in
+// double-float (DF2), about 2^-46 relative; an fp64 h enters as its fp32
+// rounding and the rounding's remainder. SPLIT writes Zh, Zl (the normalised
+// double-float) and the LU input; else Z in complex128.
+template <bool SPLIT>
+__global__ void __launch_bounds__(256) gather_mix_kernel(int nb, const cx<float>* __restrict__ H32,
+                                                         const zd* __restrict__ Hn, int64_t nnear, int64_t ldh,
+                                                         const int32_t* __restrict__ etri,
+                                                         const int32_t* __restrict__ eloc,
+                                                         const int32_t* __restrict__ tpos, zd* __restrict__ Z,
+                                                         int64_t ldz, zf* __restrict__ Zh, zf* __restrict__ Zl,
+                                                         zf* __restrict__ LU, int64_t ldl) {
+  const int tm = blockIdx.y, tn = blockIdx.x;
+  if (tm > tn) return;
+  __shared__ float4 tile[32][33];  // (Zh re, Zl re, Zh im, Zl im) of the transposed entries
+  __shared__ float4 s1t[32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  auto store = [&](int m, int n, float4 z) {
+    if constexpr (SPLIT) {
+      const zf hv(z.x, z.z);
+      Zh[(int64_t)m * nb + n] = hv;
+      Zl[(int64_t)m * nb + n] = zf(z.y, z.w);
+      LU[(int64_t)m * ldl + n] = hv;
+    } else {
+      Z[(int64_t)m * ldz + n] = zd((double)z.x + (double)z.y, (double)z.z + (double)z.w);
+    }
+  };
+  auto rwg = [&](int e, int (&t)[2], int (&l)[2], int (&sl)[2]) {
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+      t[a] = etri[2 * e + a];
+      l[a] = eloc[2 * e + a];
+      sl[a] = tpos[t[a]];
+    }
+  };
+  // acc += h(test slot sl, local i; source s, local j)
+  auto add = [&](DF2& acc, int sl, int i, int s, int j) {
+    const cx<float> v = H32[(int64_t)(3 * s + j) * ldh + 3 * (int64_t)sl + i];
+    const uint32_t u = __float_as_uint(v.re);
+    if ((u & 0xFFC00000u) == kNearTag && (int64_t)(u & 0x3FFFFFu) < nnear) {
+      const zd w = Hn[(int64_t)(u & 0x3FFFFFu) * 288 + (j * 3 + i) * 32 + (sl & 31)];
+      const float wr = (float)w.re, wi = (float)w.im;
+      df_acc(acc.hr, acc.lr, wr);
+      acc.lr += (float)(w.re - (double)wr);
+      df_acc(acc.hi, acc.li, wi);
+      acc.li += (float)(w.im - (double)wi);
+    } else {
+      df_acc(acc.hr, acc.lr, v.re);
+      df_acc(acc.hi, acc.li, v.im);
+    }
+  };
+  {
+    const int m = tm * 32 + tx;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int n = tn * 32 + ty + 8 * k;
+      DF2 s1;
+      if (m < nb && n < nb) {
+        int tma[2], lma[2], sma[2], tnb[2], lnb[2], snb[2];
+        rwg(m, tma, lma, sma);
+        rwg(n, tnb, lnb, snb);
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+          for (int b = 0; b < 2; ++b) add(s1, sma[a], lma[a], tnb[b], lnb[b]);  // test m, source n
+      }
+      s1t[ty + 8 * k][tx] = make_float4(s1.hr, s1.lr, s1.hi, s1.li);
+    }
+  }
+  __syncthreads();
+  const int nn = tn * 32 + tx;
+  const bool nok = nn < nb;
+  int tnb[2], lnb[2], snb[2];
+  if (nok) rwg(nn, tnb, lnb, snb);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int m = tm * 32 + ty + 8 * k;
+    float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (nok && m < nb) {
+      int tma[2], lma[2], sma[2];
+      rwg(m, tma, lma, sma);
+      const float4 a1 = s1t[tx][ty + 8 * k];
+      DF2 s;
+      s.hr = a1.x;
+      s.lr = a1.y;
+      s.hi = a1.z;
+      s.li = a1.w;
+#pragma unroll
+      for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b) add(s, snb[b], lnb[b], tma[a], lma[a]);  // test n, source m
+      // 0.5 (s1 + s2), normalised: Zh = fl32(h + l), Zl = the remainder
+      const float hr = 0.5f * s.hr, lr = 0.5f * s.lr, hi = 0.5f * s.hi, li = 0.5f * s.li;
+      const float zr = hr + lr, zi = hi + li;
+      z = make_float4(zr, lr - (zr - hr), zi, li - (zi - hi));
       store(m, nn, z);
     }
     tile[ty + 8 * k][tx] = z;
@@ -882,23 +982,23 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
       set_error("m25_assemble: split output needs the mixed fill without vias");
       return M25_ERR_VALUE;
     }
-    if (f32)
-      gather_sym_kernel<T, T, true, true><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->nnear, ldh,
-                                                                  geom->edge_tri, geom->edge_loc, geom->tpos, nullptr,
-                                                                  0, split->Zh, split->Zl, split->LU, split->ldl);
-    else
-      gather_sym_kernel<T, T, true, false><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->nnear, ldh,
-                                                                   geom->edge_tri, geom->edge_loc, geom->tpos,
-                                                                   nullptr, 0, split->Zh, split->Zl, split->LU,
-                                                                   split->ldl);
+    if constexpr (std::is_same<T, double>::value) {
+      if (f32)
+        gather_mix_kernel<true><<<gtiles, 256, 0, st>>>(nb, H32, Hn, geom->nnear, ldh, geom->edge_tri,
+                                                        geom->edge_loc, geom->tpos, nullptr, 0, split->Zh, split->Zl,
+                                                        split->LU, split->ldl);
+      else
+        gather_sym_kernel<T, T, true><<<gtiles, 256, 0, st>>>(nb, H, ldh, geom->edge_tri, geom->edge_loc,
+                                                              geom->tpos, nullptr, 0, split->Zh, split->Zl, split->LU,
+                                                              split->ldl);
+    }
   } else if (f32) {
-    gather_sym_kernel<T, T, false, true><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->nnear, ldh,
-                                                                 geom->edge_tri, geom->edge_loc, geom->tpos, Z,
-                                                                 ldzd, nullptr, nullptr, nullptr, 0);
+    if constexpr (std::is_same<T, double>::value)
+      gather_mix_kernel<false><<<gtiles, 256, 0, st>>>(nb, H32, Hn, geom->nnear, ldh, geom->edge_tri, geom->edge_loc,
+                                                       geom->tpos, Z, ldzd, nullptr, nullptr, nullptr, 0);
   } else {
-    gather_sym_kernel<T, T, false, false><<<gtiles, 256, 0, st>>>(nb, H, H32, Hn, geom->nnear, ldh,
-                                                                  geom->edge_tri, geom->edge_loc, geom->tpos, Z,
-                                                                  ldzd, nullptr, nullptr, nullptr, 0);
+    gather_sym_kernel<T, T, false><<<gtiles, 256, 0, st>>>(nb, H, ldh, geom->edge_tri, geom->edge_loc, geom->tpos, Z,
+                                                           ldzd, nullptr, nullptr, nullptr, 0);
   }
   }
   M25_CHECK_LAUNCH();
