@@ -38,7 +38,8 @@ struct FillArgs {
   const int32_t* block_level;
   const int32_t* cls;
   const T* stat;
-  const double* stat6;  // mixed fill: test-point sums of the near pairs' closed-form parts
+  const float2* stat6;  // mixed fill: test-point sums of the near pairs' closed-form parts (double-float)
+  const TriDF* tddf;    // mixed fill: the triangles' vertices and amplitudes in double-float
   const int32_t* pad_pos;
   int nrho;
   const T* rho;        // (nrho)
@@ -49,7 +50,7 @@ struct FillArgs {
   cx<T>* H;            // (3 nt, ldh) (fp64 fill)
   int64_t ldh;
   cx<float>* H32;      // mixed fill: (3 nt, ldh), the mid / far pairs' values (computed in fp32)
-  cx<T>* Hn;           // mixed fill: (nnear, 3 j, 3 i, 32 lanes), the near pairs' values
+  float4* Hn;          // mixed fill: (nnear, 3 j, 3 i, 32 lanes), the near pairs' values in double-float
   cx<T>* IVpad;        // (npad, nt)
   // fp32 copies for far pairs evaluated in fp32 (fill_tri_kernel<double, true>)
   const TriData<float>* td32;
@@ -57,6 +58,8 @@ struct FillArgs {
   cx<float> lead32[kMaxLevSq][2];
   float dz32[kMaxLevSq];
   cx<float> jwmu32, inv_jwe32;
+  float4 lead_df[kMaxLevSq][2];  // mixed fill, near pairs: cA, cV in double-float
+  float4 jwmu_df, inv_jwe_df;
   int* work_counter;   // items handed out beyond the first gridDim.x (zeroed before the launch)
   int nbk;             // mixed fill: buckets of the radius index (0: binary search)
   float bk_scale;      // buckets per unit radius
@@ -215,18 +218,56 @@ __device__ __forceinline__ void source_pass(int nrho, const TriData<T>& S, T dcx
   }
 }
 
+// ---- double-float arithmetic on the fp32 pipes (GB300 issues fp64 at 1/64
+// of the fp32 rate): a value is h + l with h its fp32 rounding; the error-free
+// sum (Knuth) and product (FMA) keep about 2^-46 relative, against 2^-53 for
+// fp64 and 2^-24 for fp32. The _rn intrinsics keep the compiler from fusing
+// the steps whose rounding the transforms recover.
+struct dff {
+  float h, l;
+};
+struct dfc {
+  dff re, im;
+};
+__device__ __forceinline__ dff df_add(dff a, dff b) {
+  const float s = __fadd_rn(a.h, b.h), z = __fsub_rn(s, a.h);
+  float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, z)), __fsub_rn(b.h, z));
+  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+  const float h = __fadd_rn(s, e);
+  return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ dff df_neg(dff a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ dff df_mul(dff a, dff b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, fmaf(a.l, b.h, e));
+  const float h = __fadd_rn(p, e);
+  return {h, __fsub_rn(e, __fsub_rn(h, p))};
+}
+__device__ __forceinline__ dfc dfc_add(dfc a, dfc b) { return {df_add(a.re, b.re), df_add(a.im, b.im)}; }
+__device__ __forceinline__ dfc dfc_sub(dfc a, dfc b) { return {df_add(a.re, df_neg(b.re)), df_add(a.im, df_neg(b.im))}; }
+__device__ __forceinline__ dfc dfc_mul(dfc a, dff r) { return {df_mul(a.re, r), df_mul(a.im, r)}; }
+__device__ __forceinline__ dfc dfc_mul(dfc a, dfc b) {
+  return {df_add(df_mul(a.re, b.re), df_neg(df_mul(a.im, b.im))), df_add(df_mul(a.re, b.im), df_mul(a.im, b.re))};
+}
+__device__ __forceinline__ dfc dfc_of(cx<float> v) { return {{v.re, 0.f}, {v.im, 0.f}}; }
+__device__ __forceinline__ dfc dfc_of(float4 v) { return {{v.x, v.y}, {v.z, v.w}}; }
+__device__ __forceinline__ float4 dfc_pack(dfc v) { return make_float4(v.re.h, v.re.l, v.im.h, v.im.l); }
+__host__ __device__ inline float4 dfc_split(double re, double im) {
+  const float rh = (float)re, ih = (float)im;
+  return make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
+}
+
 // Near pair of the mixed precision: the closed-form singular parts enter
-// through their frequency-independent test-point sums (fp64, precomputed per
-// sweep: st6 = [sum w S0, sum w x S0, sum w y S0, sum w S1x, sum w S1y,
-// sum w (x S1x + y S1y)]) times cA, cV; the smooth parts S_A, S_V - their 7 x
-// 7 point evaluations and both sums - run in fp32 and join in fp64.
-// (On the oracle, near smooth parts in fp32 on top of fp32 mid / far pairs
-// leave S within 1.4e-7 of the fp64 fill.)
-template <class T>
-__device__ __forceinline__ void near_pass_mixed(int nrho, const TriData<float>& S32, const TriData<float>& A32, T dcx,
-                                                T dcy, const float* xf, const float* tab32, cx<T> cA, cx<T> cV,
-                                                const double* st6, int lane, cx<T> (&Q)[3], cx<T> (&Px)[3],
-                                                cx<T> (&Py)[3], cx<T>& IV, const T (&tv)[3][2], Bk bk) {
+// through their frequency-independent test-point sums (precomputed per sweep
+// in fp64, held in double-float: st6 = [sum w S0, sum w x S0, sum w y S0,
+// sum w S1x, sum w S1y, sum w (x S1x + y S1y)]) times cA, cV; the smooth parts
+// S_A, S_V - their 7 x 7 point evaluations and both sums - run in fp32; they
+// join, and the 3x3 block is formed (pair_block_df), in double-float.
+__device__ __forceinline__ void near_pass_df(int nrho, const TriData<float>& S32, const TriData<float>& A32, float dcx,
+                                             float dcy, const float* xf, const float* tab32, dfc cA, dfc cV,
+                                             const float2* st6, int lane, const TriDF& At, dfc (&Q)[3],
+                                             dfc (&Px)[3], dfc (&Py)[3], dfc& IV, Bk bk) {
   float sq[7][2], sw[7];
 #pragma unroll
   for (int l = 0; l < 7; ++l) {
@@ -238,7 +279,7 @@ __device__ __forceinline__ void near_pass_mixed(int nrho, const TriData<float>& 
 #pragma unroll
   for (int k = 0; k < 7; ++k) {
     const float qx = A32.q7[k][0], qy = A32.q7[k][1], wk = A32.w7[k];
-    const float rx = (float)dcx + qx, ry = (float)dcy + qy;
+    const float rx = dcx + qx, ry = dcy + qy;
     cx<float> a0, ax, ay, v0;
 #pragma unroll
     for (int l = 0; l < 7; ++l) {
@@ -261,16 +302,38 @@ __device__ __forceinline__ void near_pass_mixed(int nrho, const TriData<float>& 
     t2 += ay * wk;
     t0 += ax * wx + ay * wy;
   }
-  const T g0 = st6[0 * 32 + lane], gx = st6[1 * 32 + lane], gy = st6[2 * 32 + lane];
-  const T h1 = st6[3 * 32 + lane], h2 = st6[4 * 32 + lane], h0 = st6[5 * 32 + lane];
-  IV = cV * g0 + cx<T>(iv);
-  const cx<T> S0 = cA * g0 + cx<T>(s0), SX = cA * gx + cx<T>(sx), SY = cA * gy + cx<T>(sy);
-  const cx<T> T1 = cA * h1 + cx<T>(t1), T2 = cA * h2 + cx<T>(t2), T0 = cA * h0 + cx<T>(t0);
+  auto st = [&](int q) {
+    const float2 v = st6[q * 32 + lane];
+    return dff{v.x, v.y};
+  };
+  IV = dfc_add(dfc_mul(cV, st(0)), dfc_of(iv));
+  const dfc S0 = dfc_add(dfc_mul(cA, st(0)), dfc_of(s0)), SX = dfc_add(dfc_mul(cA, st(1)), dfc_of(sx)),
+            SY = dfc_add(dfc_mul(cA, st(2)), dfc_of(sy));
+  const dfc T1 = dfc_add(dfc_mul(cA, st(3)), dfc_of(t1)), T2 = dfc_add(dfc_mul(cA, st(4)), dfc_of(t2)),
+            T0 = dfc_add(dfc_mul(cA, st(5)), dfc_of(t0));
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    Px[i] = SX - S0 * tv[i][0];
-    Py[i] = SY - S0 * tv[i][1];
-    Q[i] = T0 - (T1 * tv[i][0] + T2 * tv[i][1]);
+    const dff tx{At.vh[i][0], At.vl[i][0]}, ty{At.vh[i][1], At.vl[i][1]};
+    Px[i] = dfc_sub(SX, dfc_mul(S0, tx));
+    Py[i] = dfc_sub(SY, dfc_mul(S0, ty));
+    Q[i] = dfc_sub(T0, dfc_add(dfc_mul(T1, tx), dfc_mul(T2, ty)));
+  }
+}
+
+// pair_block (below) in double-float: the near pair's 3x3 block of the mixed fill
+__device__ __forceinline__ void pair_block_df(const TriDF& Sd, const TriDF& At, dfc jwmu, dfc inv_jwe,
+                                              const dfc (&Q)[3], const dfc (&Px)[3], const dfc (&Py)[3], dfc IV,
+                                              dfc (&out)[3][3]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const dfc ja = dfc_mul(jwmu, dff{At.cAh[i], At.cAl[i]}), jv = dfc_mul(inv_jwe, dff{At.cVh[i], At.cVl[i]});
+    const dfc JQ = dfc_mul(ja, Q[i]), JPx = dfc_mul(ja, Px[i]), JPy = dfc_mul(ja, Py[i]), JV = dfc_mul(jv, IV);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const dff bx{Sd.vh[j][0], Sd.vl[j][0]}, by{Sd.vh[j][1], Sd.vl[j][1]};
+      const dfc ia = dfc_sub(JQ, dfc_add(dfc_mul(JPx, bx), dfc_mul(JPy, by)));
+      out[i][j] = dfc_add(dfc_mul(ia, dff{Sd.cAh[j], Sd.cAl[j]}), dfc_mul(JV, dff{Sd.cVh[j], Sd.cVl[j]}));
+    }
   }
 }
 
@@ -409,6 +472,49 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
     const int code = a.cls[(int64_t)blk * a.nt + s];
     if ((PASS == 1 && code < 0) || (PASS == 2 && code >= 0)) continue;  // the other pass's pair
     const int ls = a.tri_layer[s];
+    if constexpr (FAR32 && PASS == 1) {
+      // near pair of the mixed fill, in double-float
+      const float dcx = (float)(tcx - a.cen[2 * s]), dcy = (float)(tcy - a.cen[2 * s + 1]);
+      const TriDF& At = a.tddf[tt];
+      dfc Q[3], Px[3], Py[3], IV, out[3][3];
+      near_pass_df(n, a.td32[s], a.td32[tt], dcx, dcy, xf, tabs32 + (size_t)ls * (n - 1) * 16,
+                   dfc_of(a.lead_df[lt * L + ls][0]), dfc_of(a.lead_df[lt * L + ls][1]), a.stat6 + (int64_t)code * 192,
+                   lane, At, Q, Px, Py, IV, bk);
+      pair_block_df(a.tddf[s], At, dfc_of(a.jwmu_df), dfc_of(a.inv_jwe_df), Q, Px, Py, IV, out);
+      if (active && s == t && (a.zs.re != T(0) || a.zs.im != T(0))) {
+        // conductor loss: Zs Int_T (r - a_i).(r - a_j) dS cA_i cA_j (fp64, the self pair only)
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            T gsum = T(0);
+#pragma unroll
+            for (int k = 0; k < 7; ++k)
+              gsum += tw[k] * ((tq[k][0] - tv[i][0]) * (tq[k][0] - tv[j][0]) + (tq[k][1] - tv[i][1]) * (tq[k][1] - tv[j][1]));
+            const cx<T> zl = a.zs * (gsum * tcA[i] * tcA[j]);
+            out[i][j] = dfc_add(out[i][j], dfc_of(dfc_split((double)zl.re, (double)zl.im)));
+          }
+      }
+      if (active) {
+        // [code][j][i][lane], the 32 lanes' words consecutive; in H32 a quiet
+        // NaN whose payload is the code (kNearTag)
+        float4* hn = a.Hn + (int64_t)code * 288 + lane;
+        const cx<float> tag(__uint_as_float(kNearTag | (uint32_t)code), 0.f);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          cx<float>* row = a.H32 + (int64_t)(3 * s + j) * a.ldh + col0;
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            hn[(j * 3 + i) * 32] = dfc_pack(out[i][j]);
+            row[i] = tag;
+          }
+        }
+        if (pad >= 0)
+          a.IVpad[(int64_t)pad * a.nt + s] =
+              cx<T>(T((double)IV.re.h + (double)IV.re.l), T((double)IV.im.h + (double)IV.im.l));
+      }
+      continue;
+    }
     const TriData<T>& S = a.td[s];
     const T dcx = T(tcx - a.cen[2 * s]), dcy = T(tcy - a.cen[2 * s + 1]);
     const T* tab = FAR32 ? nullptr : tabs + (size_t)ls * (n - 1) * 16;
@@ -416,10 +522,7 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
     const T dz = a.dz[lt * L + ls];
     cx<T> Q[3], Px[3], Py[3], IV;
     if (code >= 0) {
-      if (FAR32)
-        near_pass_mixed<T>(n, a.td32[s], a.td32[tt], dcx, dcy, xf, tabs32 + (size_t)ls * (n - 1) * 16, cA, cV,
-                           a.stat6 + (int64_t)code * 192, lane, Q, Px, Py, IV, tv, bk);
-      else
+      if constexpr (!FAR32)
         source_pass<T, 7, true>(n, S, dcx, dcy, tq, tw, xs, xf, tab, cA, cV, dz, a.stat + (int64_t)code * 672, lane,
                                 Q, Px, Py, IV, tv);
     } else if (code == -1 && !FAR32) {
@@ -478,21 +581,7 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
         }
     }
     if (active) {
-      if (FAR32 && code >= 0) {
-        // near pair: [code][j][i][lane], the 32 lanes' words consecutive, and
-        // in H32 a quiet NaN whose payload is the code (kNearTag)
-        cx<T>* hn = a.Hn + (int64_t)code * 288 + lane;
-        const cx<float> tag(__uint_as_float(kNearTag | (uint32_t)code), 0.f);
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          cx<float>* row = a.H32 + (int64_t)(3 * s + j) * a.ldh + col0;
-#pragma unroll
-          for (int i = 0; i < 3; ++i) {
-            hn[(j * 3 + i) * 32] = out[i][j];
-            row[i] = tag;
-          }
-        }
-      } else if (FAR32) {
+      if (FAR32) {
         // mid / far pair: fp32 values, exactly as computed
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
@@ -625,15 +714,14 @@ __device__ __forceinline__ void df_acc(float& h, float& l, float x) {
 }
 
 // The same Z for the mixed fill: the mid / far pairs' h are complex64 in H32
-// (exactly as computed, in fp32), the near pairs' are fp64 in Hn at
+// (exactly as computed, in fp32), the near pairs' are double-float in Hn at
 // [code][j_n][i_m][lane of t_m], code = the pair's index among the near pairs,
 // which H32 carries in a NaN at the pair's place (kNearTag). Sums in
-// double-float (DF2), about 2^-46 relative; an fp64 h enters as its fp32
-// rounding and the rounding's remainder. SPLIT writes Zh, Zl (the normalised
-// double-float) and the LU input; else Z in complex128.
+// double-float (DF2), about 2^-46 relative. SPLIT writes Zh, Zl (the
+// normalised double-float) and the LU input; else Z in complex128.
 template <bool SPLIT>
 __global__ void __launch_bounds__(256) gather_mix_kernel(int nb, const cx<float>* __restrict__ H32,
-                                                         const zd* __restrict__ Hn, int64_t nnear, int64_t ldh,
+                                                         const float4* __restrict__ Hn, int64_t nnear, int64_t ldh,
                                                          const int32_t* __restrict__ etri,
                                                          const int32_t* __restrict__ eloc,
                                                          const int32_t* __restrict__ tpos, zd* __restrict__ Z,
@@ -667,12 +755,11 @@ __global__ void __launch_bounds__(256) gather_mix_kernel(int nb, const cx<float>
     const cx<float> v = H32[(int64_t)(3 * s + j) * ldh + 3 * (int64_t)sl + i];
     const uint32_t u = __float_as_uint(v.re);
     if ((u & 0xFFC00000u) == kNearTag && (int64_t)(u & 0x3FFFFFu) < nnear) {
-      const zd w = Hn[(int64_t)(u & 0x3FFFFFu) * 288 + (j * 3 + i) * 32 + (sl & 31)];
-      const float wr = (float)w.re, wi = (float)w.im;
-      df_acc(acc.hr, acc.lr, wr);
-      acc.lr += (float)(w.re - (double)wr);
-      df_acc(acc.hi, acc.li, wi);
-      acc.li += (float)(w.im - (double)wi);
+      const float4 w = Hn[(int64_t)(u & 0x3FFFFFu) * 288 + (j * 3 + i) * 32 + (sl & 31)];
+      df_acc(acc.hr, acc.lr, w.x);
+      acc.lr += w.y;
+      df_acc(acc.hi, acc.li, w.z);
+      acc.li += w.w;
     } else {
       df_acc(acc.hr, acc.lr, v.re);
       df_acc(acc.hi, acc.li, v.im);
@@ -855,7 +942,7 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   // charge integrals and Im gV(0)
   const bool f32 = far32 && std::is_same<T, double>::value;
   const size_t hbytes = f32 ? sizeof(cx<float>) * (size_t)3 * nt * ldh +
-                                  sizeof(cx<T>) * 288 * (size_t)std::max<int64_t>(geom->nnear, 1)
+                                  sizeof(float4) * 288 * (size_t)std::max<int64_t>(geom->nnear, 1)
                             : sizeof(cx<T>) * (size_t)3 * nt * ldh;
   if ((rc = ctx->H.ensure(hbytes + sizeof(cx<T>) * (size_t)std::max(geom->npad, 1) * nt + sizeof(double) * 16)))
     return rc;
@@ -865,7 +952,7 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   }
   cx<T>* H = f32 ? nullptr : ctx->H.as<cx<T>>();
   cx<float>* H32 = f32 ? ctx->H.as<cx<float>>() : nullptr;
-  cx<T>* Hn = f32 ? reinterpret_cast<cx<T>*>(H32 + (size_t)3 * nt * ldh) : nullptr;
+  float4* Hn = f32 ? reinterpret_cast<float4*>(H32 + (size_t)3 * nt * ldh) : nullptr;
   cx<T>* IVpad = reinterpret_cast<cx<T>*>(ctx->H.as<char>() + hbytes);
   double* imgv = reinterpret_cast<double*>(IVpad + (size_t)std::max(geom->npad, 1) * nt);
   cx<T>* Z = static_cast<cx<T>*>(Zout);
@@ -890,6 +977,7 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   a.stat = std::is_same<T, double>::value ? reinterpret_cast<const T*>(geom->stat64)
                                           : reinterpret_cast<const T*>(geom->stat32);
   a.stat6 = geom->stat6;
+  a.tddf = geom->tddf;
   a.pad_pos = geom->pad_pos;
   a.nrho = nrho;
   a.rho = std::is_same<T, double>::value ? reinterpret_cast<const T*>(gr->rho) : reinterpret_cast<const T*>(gr->rho32);
@@ -922,6 +1010,13 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   }
   a.jwmu32 = cx<float>(float(jwmu.re), float(jwmu.im));
   a.inv_jwe32 = cx<float>(float(inv_jwe.re), float(inv_jwe.im));
+  for (int p = 0; p < L * L; ++p) {
+    const zd ca = gr->lead_h[0 * L * L + p], cv = gr->lead_h[1 * L * L + p];
+    a.lead_df[p][0] = dfc_split(ca.re, ca.im);
+    a.lead_df[p][1] = dfc_split(cv.re, cv.im);
+  }
+  a.jwmu_df = dfc_split(jwmu.re, jwmu.im);
+  a.inv_jwe_df = dfc_split(inv_jwe.re, inv_jwe.im);
   // mixed fill: bucket index of the fp32 radii, buckets no wider than the
   // smallest radius step (at most 16384)
   a.nbk = 0;

@@ -53,7 +53,7 @@ __device__ inline double hyp_rn(double x, double y) { return sqrt(add_rn(mul_rn(
 __global__ void tri_data_kernel(int nt, const double* __restrict__ verts, const int32_t* __restrict__ tri_basis,
                                 const double* __restrict__ tri_sign, const double* __restrict__ edge_len,
                                 double* __restrict__ cen, TriData<double>* __restrict__ td64,
-                                TriData<float>* __restrict__ td32) {
+                                TriData<float>* __restrict__ td32, TriDF* __restrict__ tddf) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nt) return;
   double V[3][2];
@@ -110,6 +110,18 @@ __global__ void tri_data_kernel(int nt, const double* __restrict__ verts, const 
   float* dst = reinterpret_cast<float*>(&f);
   for (int i = 0; i < int(sizeof(TriData<double>) / sizeof(double)); ++i) dst[i] = float(src[i]);
   td32[t] = f;
+  TriDF g;
+  auto split = [](double x, float& h, float& l) {
+    h = (float)x;
+    l = (float)(x - (double)h);
+  };
+  for (int v = 0; v < 3; ++v)
+    for (int d = 0; d < 2; ++d) split(a.v[v][d], g.vh[v][d], g.vl[v][d]);
+  for (int i = 0; i < 3; ++i) {
+    split(a.cA[i], g.cAh[i], g.cAl[i]);
+    split(a.cV[i], g.cVh[i], g.cVl[i]);
+  }
+  tddf[t] = g;
 }
 
 // class of (test block b, source triangle s): 0 near (< near_factor), 1 mid
@@ -239,7 +251,7 @@ __global__ void static_kernel(int64_t nnear, const int2* __restrict__ near_list,
 // by the leading coefficients cA, cV of the frequency.
 __global__ void stat_sums_kernel(int64_t nnear, const int2* __restrict__ near_list,
                                  const int32_t* __restrict__ block_tris, const TriData<double>* __restrict__ td,
-                                 const double* __restrict__ st64, double* __restrict__ st6) {
+                                 const double* __restrict__ st64, float2* __restrict__ st6) {
   const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= nnear * 32) return;
   const int64_t idx = gid >> 5;
@@ -260,7 +272,10 @@ __global__ void stat_sums_kernel(int64_t nnear, const int2* __restrict__ near_li
       v[5] += wx * s1x + wy * s1y;
     }
   }
-  for (int q = 0; q < 6; ++q) st6[(idx * 6 + q) * 32 + lane] = v[q];
+  for (int q = 0; q < 6; ++q) {  // double-float: the fp32 rounding and its remainder
+    const float h = (float)v[q];
+    st6[(idx * 6 + q) * 32 + lane] = make_float2(h, (float)(v[q] - (double)h));
+  }
 }
 
 __global__ void fill_i32(int32_t* p, int64_t n, int32_t v) {
@@ -393,11 +408,13 @@ extern "C" int m25_geometry_create(m25_ctx* ctx, const m25_mesh_desc* d, m25_geo
   TRY(alloc(g->allocs, (void**)&g->cen, sizeof(double) * 2 * nt));
   TRY(alloc(g->allocs, (void**)&g->td64, sizeof(TriData<double>) * nt));
   TRY(alloc(g->allocs, (void**)&g->td32, sizeof(TriData<float>) * nt));
+  TRY(alloc(g->allocs, (void**)&g->tddf, sizeof(TriDF) * nt));
   TRY(alloc(g->allocs, (void**)&g->tpos, sizeof(int32_t) * nt));
   TRY(alloc(g->allocs, (void**)&g->block_level, sizeof(int32_t) * d->nblocks));
   TRY(alloc(g->allocs, (void**)&g->cls, sizeof(int32_t) * (size_t)d->nblocks * nt));
   TRY(alloc(g->allocs, (void**)&g->pad_pos, sizeof(int32_t) * nt));
-  tri_data_kernel<<<(nt + 127) / 128, 128, 0, st>>>(nt, verts, g->tri_basis, sign, elen, g->cen, g->td64, g->td32);
+  tri_data_kernel<<<(nt + 127) / 128, 128, 0, st>>>(nt, verts, g->tri_basis, sign, elen, g->cen, g->td64, g->td32,
+                                                   g->tddf);
   tpos_kernel<<<(d->nblocks * 32 + 255) / 256, 256, 0, st>>>(d->nblocks, g->block_tris, g->tri_layer, g->tpos,
                                                              g->block_level);
   TRY(alloc(tmp, (void**)&counts, sizeof(int32_t) * d->nblocks));
@@ -422,7 +439,7 @@ extern "C" int m25_geometry_create(m25_ctx* ctx, const m25_mesh_desc* d, m25_geo
     M25_CHECK_LAUNCH();
     TRY(alloc(g->allocs, (void**)&g->stat64, sizeof(double) * std::max<int64_t>(g->nnear, 1) * 672));
     TRY(alloc(g->allocs, (void**)&g->stat32, sizeof(float) * std::max<int64_t>(g->nnear, 1) * 672));
-    TRY(alloc(g->allocs, (void**)&g->stat6, sizeof(double) * std::max<int64_t>(g->nnear, 1) * 192));
+    TRY(alloc(g->allocs, (void**)&g->stat6, sizeof(float2) * std::max<int64_t>(g->nnear, 1) * 192));
     if (g->nnear) {
       int64_t n = g->nnear * 224;
       static_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g->nnear, near_list, g->block_tris, g->tri_layer,

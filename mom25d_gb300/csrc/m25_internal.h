@@ -16,6 +16,14 @@ constexpr int kMaxLevSq = kMaxLev * kMaxLev;
 
 // Per-triangle data of the fill, all lengths relative to the triangle's own
 // centroid (cx, cy) so that fp32 arithmetic keeps its precision.
+// The triangle data the mixed fill's near pairs take in double-float (each
+// value as an fp32 rounding h and its remainder l, h + l within 2^-48).
+struct TriDF {
+  float vh[3][2], vl[3][2];  // vertices about the centroid
+  float cAh[3], cAl[3];      // RWG amplitudes
+  float cVh[3], cVl[3];      // divergences
+};
+
 template <class T>
 struct TriData {
   T v[3][2];   // vertices
@@ -83,6 +91,7 @@ struct m25_geom {
   double* cen = nullptr;                 // (nt,2) absolute centroids
   m25::TriData<double>* td64 = nullptr;  // (nt)
   m25::TriData<float>* td32 = nullptr;   // (nt)
+  m25::TriDF* tddf = nullptr;            // (nt) double-float copy for the mixed near pairs
   int32_t* tri_layer = nullptr;          // (nt)
   int32_t* tri_basis = nullptr;          // (nt,3)
   double* level_z = nullptr;             // (nlev)
@@ -94,7 +103,7 @@ struct m25_geom {
   int32_t* cls = nullptr;                // (nblocks, nt) >= 0 near index, -1 mid, -2 far
   double* stat64 = nullptr;              // (nnear, 3, 7, 32) closed-form S0, S1x, S1y
   float* stat32 = nullptr;
-  double* stat6 = nullptr;               // (nnear, 6, 32) their test-point sums (mixed fill)
+  float2* stat6 = nullptr;               // (nnear, 6, 32) their test-point sums (mixed fill), double-float
   int64_t nnear = 0, npairs[3] = {0, 0, 0};
   // vias
   int32_t* pad_pos = nullptr;            // (nt) pad index or -1
