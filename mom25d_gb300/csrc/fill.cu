@@ -59,7 +59,8 @@ struct FillArgs {
   float dz32[kMaxLevSq];
   cx<float> jwmu32, inv_jwe32;
   float4 lead_df[kMaxLevSq][2];  // mixed fill, near pairs: cA, cV in double-float
-  float4 jwmu_df, inv_jwe_df;
+  float4 jwmu_df, inv_jwe_df, zs_df;  // and the surface impedance (has_zs: not 0)
+  int has_zs;
   int* work_counter;   // items handed out beyond the first gridDim.x (zeroed before the launch)
   int nbk;             // mixed fill: buckets of the radius index (0: binary search)
   float bk_scale;      // buckets per unit radius
@@ -481,19 +482,13 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
                    dfc_of(a.lead_df[lt * L + ls][0]), dfc_of(a.lead_df[lt * L + ls][1]), a.stat6 + (int64_t)code * 192,
                    lane, At, Q, Px, Py, IV, bk);
       pair_block_df(a.tddf[s], At, dfc_of(a.jwmu_df), dfc_of(a.inv_jwe_df), Q, Px, Py, IV, out);
-      if (active && s == t && (a.zs.re != T(0) || a.zs.im != T(0))) {
-        // conductor loss: Zs Int_T (r - a_i).(r - a_j) dS cA_i cA_j (fp64, the self pair only)
+      if (active && s == t && a.has_zs) {
+        // conductor loss of the self pair: Zs x its precomputed factor
+        const dfc zs = dfc_of(a.zs_df);
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
-          for (int j = 0; j < 3; ++j) {
-            T gsum = T(0);
-#pragma unroll
-            for (int k = 0; k < 7; ++k)
-              gsum += tw[k] * ((tq[k][0] - tv[i][0]) * (tq[k][0] - tv[j][0]) + (tq[k][1] - tv[i][1]) * (tq[k][1] - tv[j][1]));
-            const cx<T> zl = a.zs * (gsum * tcA[i] * tcA[j]);
-            out[i][j] = dfc_add(out[i][j], dfc_of(dfc_split((double)zl.re, (double)zl.im)));
-          }
+          for (int j = 0; j < 3; ++j) out[i][j] = dfc_add(out[i][j], dfc_mul(zs, dff{At.gzh[i][j], At.gzl[i][j]}));
       }
       if (active) {
         // [code][j][i][lane], the 32 lanes' words consecutive; in H32 a quiet
@@ -1016,6 +1011,8 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
     a.lead_df[p][1] = dfc_split(cv.re, cv.im);
   }
   a.jwmu_df = dfc_split(jwmu.re, jwmu.im);
+  a.zs_df = dfc_split(zs.re, zs.im);
+  a.has_zs = zs.re != 0.0 || zs.im != 0.0;
   a.inv_jwe_df = dfc_split(inv_jwe.re, inv_jwe.im);
   // mixed fill: bucket index of the fp32 radii, buckets no wider than the
   // smallest radius step (at most 16384)

@@ -121,6 +121,16 @@ __global__ void tri_data_kernel(int nt, const double* __restrict__ verts, const 
     split(a.cA[i], g.cAh[i], g.cAl[i]);
     split(a.cV[i], g.cVh[i], g.cVl[i]);
   }
+  // the conductor-loss factor of the self pair (frequency-independent; the
+  // fill multiplies it by the surface impedance), as the fp64 fill forms it
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double gsum = 0.0;
+      for (int k = 0; k < 7; ++k)
+        gsum += a.w7[k] * ((a.q7[k][0] - a.v[i][0]) * (a.q7[k][0] - a.v[j][0]) +
+                           (a.q7[k][1] - a.v[i][1]) * (a.q7[k][1] - a.v[j][1]));
+      split(gsum * a.cA[i] * a.cA[j], g.gzh[i][j], g.gzl[i][j]);
+    }
   tddf[t] = g;
 }
 

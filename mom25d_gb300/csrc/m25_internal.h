@@ -22,6 +22,7 @@ struct TriDF {
   float vh[3][2], vl[3][2];  // vertices about the centroid
   float cAh[3], cAl[3];      // RWG amplitudes
   float cVh[3], cVl[3];      // divergences
+  float gzh[3][3], gzl[3][3];  // the self pair's conductor-loss factor Int_T (r - a_i).(r - a_j) dS cA_i cA_j
 };
 
 template <class T>
