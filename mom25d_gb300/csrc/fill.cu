@@ -33,6 +33,7 @@ struct FillArgs {
   int nt, nb, nlev, nblocks, n_src_chunk, n_chunks;
   const TriData<T>* td;
   const double* cen;
+  const float4* cen_df;  // mixed fill: the centroids in double-float
   const int32_t* tri_layer;
   const int32_t* block_tris;
   const int32_t* block_level;
@@ -464,6 +465,16 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
     }
   }
   const double tcx = a.cen[2 * tt], tcy = a.cen[2 * tt + 1];
+  float4 tcd = make_float4(0.f, 0.f, 0.f, 0.f);
+  if constexpr (FAR32) tcd = a.cen_df[tt];
+  // mixed fill: the centroid difference to source s in fp32 from the
+  // double-float centroids (the high parts' difference is exact for nearby
+  // triangles, the low parts carry the rest): no fp64 operation per pair
+  auto dcen = [&](int s, float& dx, float& dy) {
+    const float4 sc = a.cen_df[s];
+    dx = __fadd_rn(__fsub_rn(tcd.x, sc.x), __fsub_rn(tcd.y, sc.y));
+    dy = __fadd_rn(__fsub_rn(tcd.z, sc.z), __fsub_rn(tcd.w, sc.w));
+  };
   const int pad = active ? a.pad_pos[tt] : -1;
   const int64_t col0 = (int64_t)(blk * 32 + lane) * 3;
 
@@ -475,7 +486,8 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
     const int ls = a.tri_layer[s];
     if constexpr (FAR32 && PASS == 1) {
       // near pair of the mixed fill, in double-float
-      const float dcx = (float)(tcx - a.cen[2 * s]), dcy = (float)(tcy - a.cen[2 * s + 1]);
+      float dcx, dcy;
+      dcen(s, dcx, dcy);
       const TriDF& At = a.tddf[tt];
       dfc Q[3], Px[3], Py[3], IV, out[3][3];
       near_pass_df(n, a.td32[s], a.td32[tt], dcx, dcy, xf, tabs32 + (size_t)ls * (n - 1) * 16,
@@ -511,7 +523,14 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
       continue;
     }
     const TriData<T>& S = a.td[s];
-    const T dcx = T(tcx - a.cen[2 * s]), dcy = T(tcy - a.cen[2 * s + 1]);
+    T dcx = T(0), dcy = T(0);
+    float fx = 0.f, fy = 0.f;  // mixed fill: the difference in fp32 (dcen)
+    if constexpr (FAR32) {
+      dcen(s, fx, fy);
+    } else {
+      dcx = T(tcx - a.cen[2 * s]);
+      dcy = T(tcy - a.cen[2 * s + 1]);
+    }
     const T* tab = FAR32 ? nullptr : tabs + (size_t)ls * (n - 1) * 16;
     const cx<T> cA = a.lead[lt * L + ls][0], cV = a.lead[lt * L + ls][1];
     const T dz = a.dz[lt * L + ls];
@@ -546,10 +565,10 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
       const float* tab32 = tabs32 + (size_t)ls * (n - 1) * 16;
       const cx<float> cA32 = a.lead32[lt * L + ls][0], cV32 = a.lead32[lt * L + ls][1];
       if (code == -1)
-        source_pass<float, 3, false>(n, S32, (float)dcx, (float)dcy, tq32, tw32, xf, xf, tab32, cA32, cV32,
+        source_pass<float, 3, false>(n, S32, fx, fy, tq32, tw32, xf, xf, tab32, cA32, cV32,
                                      a.dz32[lt * L + ls], nullptr, lane, Qf, Pxf, Pyf, IVf, tv32, bk);
       else
-        source_pass<float, 1, false>(n, S32, (float)dcx, (float)dcy, tq32, tw32, xf, xf, tab32, cA32, cV32,
+        source_pass<float, 1, false>(n, S32, fx, fy, tq32, tw32, xf, xf, tab32, cA32, cV32,
                                      a.dz32[lt * L + ls], nullptr, lane, Qf, Pxf, Pyf, IVf, tv32, bk);
       pair_block<float>(S32, tcA32, tcV32, a.jwmu32, a.inv_jwe32, Qf, Pxf, Pyf, IVf, outf);
 #pragma unroll
@@ -965,6 +984,7 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
   a.td = std::is_same<T, double>::value ? reinterpret_cast<const TriData<T>*>(geom->td64)
                                         : reinterpret_cast<const TriData<T>*>(geom->td32);
   a.cen = geom->cen;
+  a.cen_df = geom->cen_df;
   a.tri_layer = geom->tri_layer;
   a.block_tris = geom->block_tris;
   a.block_level = geom->block_level;

@@ -53,7 +53,8 @@ __device__ inline double hyp_rn(double x, double y) { return sqrt(add_rn(mul_rn(
 __global__ void tri_data_kernel(int nt, const double* __restrict__ verts, const int32_t* __restrict__ tri_basis,
                                 const double* __restrict__ tri_sign, const double* __restrict__ edge_len,
                                 double* __restrict__ cen, TriData<double>* __restrict__ td64,
-                                TriData<float>* __restrict__ td32, TriDF* __restrict__ tddf) {
+                                TriData<float>* __restrict__ td32, TriDF* __restrict__ tddf,
+                                float4* __restrict__ cen_df) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nt) return;
   double V[3][2];
@@ -63,6 +64,10 @@ __global__ void tri_data_kernel(int nt, const double* __restrict__ verts, const 
   double cy = add_rn(add_rn(V[0][1], V[1][1]), V[2][1]) / 3.0;
   cen[2 * t] = cx;
   cen[2 * t + 1] = cy;
+  {
+    const float xh = (float)cx, yh = (float)cy;
+    cen_df[t] = make_float4(xh, (float)(cx - (double)xh), yh, (float)(cy - (double)yh));
+  }
   double e1x = sub_rn(V[1][0], V[0][0]), e1y = sub_rn(V[1][1], V[0][1]);
   double e2x = sub_rn(V[2][0], V[0][0]), e2y = sub_rn(V[2][1], V[0][1]);
   double area = 0.5 * fabs(sub_rn(mul_rn(e1x, e2y), mul_rn(e1y, e2x)));
@@ -419,12 +424,13 @@ extern "C" int m25_geometry_create(m25_ctx* ctx, const m25_mesh_desc* d, m25_geo
   TRY(alloc(g->allocs, (void**)&g->td64, sizeof(TriData<double>) * nt));
   TRY(alloc(g->allocs, (void**)&g->td32, sizeof(TriData<float>) * nt));
   TRY(alloc(g->allocs, (void**)&g->tddf, sizeof(TriDF) * nt));
+  TRY(alloc(g->allocs, (void**)&g->cen_df, sizeof(float4) * nt));
   TRY(alloc(g->allocs, (void**)&g->tpos, sizeof(int32_t) * nt));
   TRY(alloc(g->allocs, (void**)&g->block_level, sizeof(int32_t) * d->nblocks));
   TRY(alloc(g->allocs, (void**)&g->cls, sizeof(int32_t) * (size_t)d->nblocks * nt));
   TRY(alloc(g->allocs, (void**)&g->pad_pos, sizeof(int32_t) * nt));
   tri_data_kernel<<<(nt + 127) / 128, 128, 0, st>>>(nt, verts, g->tri_basis, sign, elen, g->cen, g->td64, g->td32,
-                                                   g->tddf);
+                                                   g->tddf, g->cen_df);
   tpos_kernel<<<(d->nblocks * 32 + 255) / 256, 256, 0, st>>>(d->nblocks, g->block_tris, g->tri_layer, g->tpos,
                                                              g->block_level);
   TRY(alloc(tmp, (void**)&counts, sizeof(int32_t) * d->nblocks));

@@ -90,6 +90,7 @@ struct m25_geom {
   double near_factor = 3.0, far_factor = 10.0;
   // device arrays
   double* cen = nullptr;                 // (nt,2) absolute centroids
+  float4* cen_df = nullptr;              // (nt) the same in double-float (x h, x l, y h, y l), mixed fill
   m25::TriData<double>* td64 = nullptr;  // (nt)
   m25::TriData<float>* td32 = nullptr;   // (nt)
   m25::TriDF* tddf = nullptr;            // (nt) double-float copy for the mixed near pairs
