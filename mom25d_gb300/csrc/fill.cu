@@ -764,9 +764,10 @@ __global__ void __launch_bounds__(256) gather_mix_kernel(int nb, const cx<float>
       sl[a] = tpos[t[a]];
     }
   };
-  // acc += h(test slot sl, local i; source s, local j)
-  auto add = [&](DF2& acc, int sl, int i, int s, int j) {
-    const cx<float> v = H32[(int64_t)(3 * s + j) * ldh + 3 * (int64_t)sl + i];
+  // the scratch entry of h(test slot sl, local i; source s, local j)
+  auto at = [&](int sl, int i, int s, int j) { return H32[(int64_t)(3 * s + j) * ldh + 3 * (int64_t)sl + i]; };
+  // acc += that h, given the entry v read from H32 (a near pair's tag: its double-float value from Hn)
+  auto add = [&](DF2& acc, cx<float> v, int sl, int i, int j) {
     const uint32_t u = __float_as_uint(v.re);
     if ((u & 0xFFC00000u) == kNearTag && (int64_t)(u & 0x3FFFFFu) < nnear) {
       const float4 w = Hn[(int64_t)(u & 0x3FFFFFu) * 288 + (j * 3 + i) * 32 + (sl & 31)];
@@ -779,53 +780,92 @@ __global__ void __launch_bounds__(256) gather_mix_kernel(int nb, const cx<float>
       df_acc(acc.hi, acc.li, v.im);
     }
   };
+  // the four rows' or columns' scratch entries are read before any is summed
+  // (sixteen independent loads in flight per thread: the gather waits on
+  // memory latency)
   {
     const int m = tm * 32 + tx;
+    const bool mok = m < nb;
+    int tma[2] = {0, 0}, lma[2] = {0, 0}, sma[2] = {0, 0};
+    if (mok) rwg(m, tma, lma, sma);
+    int t4[4][2], l4[4][2];
+    bool ok[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const int n = tn * 32 + ty + 8 * k;
+      ok[k] = mok && n < nb;
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        t4[k][b] = ok[k] ? etri[2 * n + b] : 0;
+        l4[k][b] = ok[k] ? eloc[2 * n + b] : 0;
+      }
+    }
+    cx<float> v[4][2][2];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+#pragma unroll
+      for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b) v[k][a][b] = ok[k] ? at(sma[a], lma[a], t4[k][b], l4[k][b]) : cx<float>();
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
       DF2 s1;
-      if (m < nb && n < nb) {
-        int tma[2], lma[2], sma[2], tnb[2], lnb[2], snb[2];
-        rwg(m, tma, lma, sma);
-        rwg(n, tnb, lnb, snb);
+      if (ok[k])
 #pragma unroll
         for (int a = 0; a < 2; ++a)
 #pragma unroll
-          for (int b = 0; b < 2; ++b) add(s1, sma[a], lma[a], tnb[b], lnb[b]);  // test m, source n
-      }
+          for (int b = 0; b < 2; ++b) add(s1, v[k][a][b], sma[a], lma[a], l4[k][b]);  // test m, source n
       s1t[ty + 8 * k][tx] = make_float4(s1.hr, s1.lr, s1.hi, s1.li);
     }
   }
   __syncthreads();
   const int nn = tn * 32 + tx;
   const bool nok = nn < nb;
-  int tnb[2], lnb[2], snb[2];
+  int tnb[2] = {0, 0}, lnb[2] = {0, 0}, snb[2] = {0, 0};
   if (nok) rwg(nn, tnb, lnb, snb);
+  {
+    int t4[4][2], l4[4][2];
+    bool ok[4];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int m = tm * 32 + ty + 8 * k;
-    float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (nok && m < nb) {
-      int tma[2], lma[2], sma[2];
-      rwg(m, tma, lma, sma);
-      const float4 a1 = s1t[tx][ty + 8 * k];
-      DF2 s;
-      s.hr = a1.x;
-      s.lr = a1.y;
-      s.hi = a1.z;
-      s.li = a1.w;
+    for (int k = 0; k < 4; ++k) {
+      const int m = tm * 32 + ty + 8 * k;
+      ok[k] = nok && m < nb;
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        t4[k][a] = ok[k] ? etri[2 * m + a] : 0;
+        l4[k][a] = ok[k] ? eloc[2 * m + a] : 0;
+      }
+    }
+    cx<float> v[4][2][2];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
 #pragma unroll
       for (int a = 0; a < 2; ++a)
 #pragma unroll
-        for (int b = 0; b < 2; ++b) add(s, snb[b], lnb[b], tma[a], lma[a]);  // test n, source m
-      // 0.5 (s1 + s2), normalised: Zh = fl32(h + l), Zl = the remainder
-      const float hr = 0.5f * s.hr, lr = 0.5f * s.lr, hi = 0.5f * s.hi, li = 0.5f * s.li;
-      const float zr = hr + lr, zi = hi + li;
-      z = make_float4(zr, lr - (zr - hr), zi, li - (zi - hi));
-      store(m, nn, z);
+        for (int b = 0; b < 2; ++b) v[k][a][b] = ok[k] ? at(snb[b], lnb[b], t4[k][a], l4[k][a]) : cx<float>();
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int m = tm * 32 + ty + 8 * k;
+      float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (ok[k]) {
+        const float4 a1 = s1t[tx][ty + 8 * k];
+        DF2 s;
+        s.hr = a1.x;
+        s.lr = a1.y;
+        s.hi = a1.z;
+        s.li = a1.w;
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+          for (int b = 0; b < 2; ++b) add(s, v[k][a][b], snb[b], lnb[b], l4[k][a]);  // test n, source m
+        // 0.5 (s1 + s2), normalised: Zh = fl32(h + l), Zl = the remainder
+        const float hr = 0.5f * s.hr, lr = 0.5f * s.lr, hi = 0.5f * s.hi, li = 0.5f * s.li;
+        const float zr = hr + lr, zi = hi + li;
+        z = make_float4(zr, lr - (zr - hr), zi, li - (zi - hi));
+        store(m, nn, z);
+      }
+      tile[ty + 8 * k][tx] = z;
     }
-    tile[ty + 8 * k][tx] = z;
   }
   if (tm == tn) return;  // uniform over the CTA
   __syncthreads();
