@@ -841,13 +841,20 @@ __global__ void __launch_bounds__(256) gemm_kernel(cx<T>* A, int64_t lda, int n,
 // perm from the interchange list: perm[i] = the original row that ends in
 // row i after the interchanges (sequential in shared memory, one thread;
 // built once per factorisation)
+// STAGE: ipiv is first copied to shared memory, so that the serial loop of
+// swaps reads no global memory (n <= 25600)
+template <bool STAGE>
 __global__ void perm_kernel(int n, const int32_t* __restrict__ ipiv, int32_t* __restrict__ perm_out) {
   extern __shared__ int perm[];
-  for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = i;
+  int* piv = perm + n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    perm[i] = i;
+    if (STAGE) piv[i] = ipiv[i];
+  }
   __syncthreads();
   if (threadIdx.x == 0)
     for (int i = 0; i < n; ++i) {
-      int p = ipiv[i];
+      int p = STAGE ? piv[i] : ipiv[i];
       if (p != i && p >= 0 && p < n) {
         int t = perm[i];
         perm[i] = perm[p];
@@ -1513,8 +1520,19 @@ int lu_make_perm(m25_ctx* ctx, int n, const int32_t* ipiv, int32_t* perm) {
     set_error("dense solve: n <= 51200");
     return M25_ERR_VALUE;
   }
-  M25_CUDA(cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-  perm_kernel<<<1, 1024, n * sizeof(int), ctx->stream>>>(n, ipiv, perm);
+  static const bool attr =
+      cudaFuncSetAttribute(perm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) ==
+          cudaSuccess &&
+      cudaFuncSetAttribute(perm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) ==
+          cudaSuccess;
+  if (!attr) {
+    set_error("dense solve: the permutation kernel's shared memory could not be reserved");
+    return M25_ERR_CUDA;
+  }
+  if ((size_t)n * 2 * sizeof(int) <= 200 * 1024)
+    perm_kernel<true><<<1, 1024, 2 * n * sizeof(int), ctx->stream>>>(n, ipiv, perm);
+  else
+    perm_kernel<false><<<1, 1024, n * sizeof(int), ctx->stream>>>(n, ipiv, perm);
   M25_CHECK_LAUNCH();
   return M25_OK;
 }
