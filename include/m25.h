@@ -72,15 +72,18 @@ int m25_ctx_mem_info(m25_ctx* ctx, uint64_t* free_bytes, uint64_t* total_bytes);
 void* m25_ctx_stream(m25_ctx* ctx); /* the cudaStream_t every call of this context runs on */
 
 /* Tuning knobs of this context's calls (no counterpart in mom25d; set per
- * point by mom25d_gb300/batch.py from the table autotune.py measures), 0
- * keeping the process default: panel_cluster_min, the smallest cluster (4, 8
- * or 16 CTAs) the LU panel runs on (default 4, or $M25_PANEL_CLUSTER_MIN);
- * wave_ctas, the CTA cap of the triangular solves (default one per 64-row
- * block, or $M25_WAVE_CTAS); tc_chunk, the steps of 32 tf32 along K (12 MMAs
- * each) the tensor-core update accumulates in TMEM before adding into its fp32
- * registers (1..8; default 1, or $M25_TC_CHUNK: longer chunks round the
- * accumulation coarser). */
-int m25_ctx_set_tuning(m25_ctx* ctx, int32_t panel_cluster_min, int32_t wave_ctas, int32_t tc_chunk);
+ * point by mom25d_gb300/batch.py and Solver.sweep from the table autotune.py
+ * measures), 0 keeping the process default: panel_cluster_min, the smallest
+ * cluster (4, 8 or 16 CTAs) the LU panel runs on (default 4, or
+ * $M25_PANEL_CLUSTER_MIN); wave_ctas, the CTA cap of the triangular solves
+ * (default one per 64-row block, or $M25_WAVE_CTAS); tc_chunk, the steps of
+ * 32 tf32 along K (12 MMAs each) the tensor-core update accumulates in TMEM
+ * before adding into its fp32 registers (1..8; default 1, or $M25_TC_CHUNK:
+ * longer chunks round the accumulation coarser); tc_tile_n, the N of the
+ * tensor-core update's tiles in real columns (128 or 192; default 128 for
+ * updates of at most 64 complex columns, 192 otherwise). */
+int m25_ctx_set_tuning(m25_ctx* ctx, int32_t panel_cluster_min, int32_t wave_ctas, int32_t tc_chunk,
+                       int32_t tc_tile_n);
 
 /* Failure-path hook (no counterpart in mom25d, whose solve has no waits):
  * bound every ready-flag wait of this context's triangular solves to `polls`

@@ -3,10 +3,11 @@ table measured on the device (mom25d has no such knobs: its LU is LAPACK's).
 
 Knobs (m25_ctx_set_tuning): the smallest cluster (4, 8 or 16 CTAs) the LU
 panel runs on, the CTA cap of the triangular solves (0: one CTA per 64-row
-block), and the number of k-blocks the tensor-core update accumulates in
-TMEM before adding into fp32 registers. The best values depend on N: how
-many rows the panel's cluster holds, how long the wavefront is, how much of
-the GPU the points running beside each other leave free.
+block), the number of k-blocks the tensor-core update accumulates in TMEM
+before adding into fp32 registers, and the tile shape of that update (N of
+128 or 192 real columns; 0: by the update's width). The best values depend
+on N: how many rows the panel's cluster holds, how long the wavefront is,
+how much of the GPU the points running beside each other leave free.
 
 `run()` measures, for probe workloads spread over the sizes of the sweeps
 (band-pass variants of N 1524 to 4972, the LPF at 5943), the points per
@@ -28,8 +29,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 TABLE = os.path.join(HERE, "tuning.json")
-KNOBS = ("panel_cluster_min", "wave_ctas", "tc_chunk")
-CANDIDATES = dict(panel_cluster_min=(4, 8, 16), wave_ctas=(0, 16), tc_chunk=(1, 2))
+KNOBS = ("panel_cluster_min", "wave_ctas", "tc_chunk", "tc_tile_n")
+CANDIDATES = dict(panel_cluster_min=(4, 8, 16), wave_ctas=(0, 16), tc_chunk=(1, 2), tc_tile_n=(0, 128))
 PROBES = (("bandpass", dict(k=0)), ("bandpass", dict(k=6)), ("bandpass", dict(k=11)), ("bandpass", dict(k=14)),
           ("lpf", {}))
 
@@ -42,10 +43,11 @@ class Tuning:
         if not rows:
             raise ValueError("a tuning table needs at least one row")
         for r in rows:
-            missing = [k for k in KNOBS + ("n_max",) if k not in r]
+            missing = [k for k in KNOBS[:3] + ("n_max",) if k not in r]
             if missing:
                 raise ValueError(f"tuning row {r} lacks {missing}")
-        self.rows = sorted(rows, key=lambda r: r["n_max"])
+        # a row without a tile shape leaves it to the engine (0)
+        self.rows = sorted(({"tc_tile_n": 0, **r} for r in rows), key=lambda r: r["n_max"])
 
     def knobs(self, n):
         for r in self.rows:

@@ -134,14 +134,17 @@ extern "C" int m25_ctx_mem_info(m25_ctx* c, uint64_t* free_bytes, uint64_t* tota
   return M25_OK;
 }
 
-extern "C" int m25_ctx_set_tuning(m25_ctx* c, int32_t panel_cluster_min, int32_t wave_ctas, int32_t tc_chunk) {
-  if (!c || panel_cluster_min < 0 || wave_ctas < 0 || tc_chunk < 0 || tc_chunk > 8) {
-    set_error("m25_ctx_set_tuning: null context or a knob out of range (>= 0; tc_chunk <= 8)");
+extern "C" int m25_ctx_set_tuning(m25_ctx* c, int32_t panel_cluster_min, int32_t wave_ctas, int32_t tc_chunk,
+                                  int32_t tc_tile_n) {
+  if (!c || panel_cluster_min < 0 || wave_ctas < 0 || tc_chunk < 0 || tc_chunk > 8 ||
+      (tc_tile_n != 0 && tc_tile_n != 128 && tc_tile_n != 192)) {
+    set_error("m25_ctx_set_tuning: null context or a knob out of range (>= 0; tc_chunk <= 8; tc_tile_n 0, 128 or 192)");
     return M25_ERR_VALUE;
   }
   c->tune_cluster_min = panel_cluster_min;
   c->tune_wave_ctas = wave_ctas;
   c->tune_tc_chunk = tc_chunk;
+  c->tune_tc_bn = tc_tile_n;
   return M25_OK;
 }
 

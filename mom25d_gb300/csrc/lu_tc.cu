@@ -50,14 +50,22 @@ namespace {
 // k-blocks of 32 tf32 (128-byte rows, 128-byte swizzle) in a 2-stage ring (k-blocks
 // of 16 in 4 stages of 40 KB, 64-byte swizzle, measured no faster: 47 % against 50 %
 // tensor pipe on the largest n = 4096 launch)
-constexpr int kBM = 128, kBN = 192, kBK = 32, kStages = 2;
+constexpr int kBM = 128, kBK = 32, kStages = 2;
+// N of a tile (real columns of C): 192 by default, 128 for narrow updates (and where
+// the context's tuning asks for it); the kernel is instantiated for both
+constexpr int kBNDefault = 192;
 constexpr int kChunkK = 32;  // tf32 elements per TMEM accumulation per unit of the chunk setting
 constexpr int kTmemCols = 512, kBufStride = 256;  // two accumulators, 256 columns apart
-constexpr int kTileA = kBM * kBK * 4, kTileB = kBN * kBK * 4;
-constexpr int kStageBytes = 2 * (kTileA + kTileB);  // [A hi | A lo | B hi | B lo], each 1024-byte aligned
+constexpr int kTileA = kBM * kBK * 4;
+template <int BN>
+constexpr int tile_b() { return BN * kBK * 4; }
+// [A hi | A lo | B hi | B lo], each 1024-byte aligned
+template <int BN>
+constexpr int stage_bytes() { return 2 * (kTileA + tile_b<BN>()); }
 constexpr int kEpiWarps = 8, kThreads = 64 + 32 * kEpiWarps;
 constexpr int kOutBlock = 32 * 32 * 4;  // one 32 x 32 fp32 block of C, staged for the TMA reduce
-constexpr int kSmemBytes = kStages * kStageBytes + kEpiWarps * 2 * kOutBlock + 1024;
+template <int BN>
+constexpr int smem_bytes() { return kStages * stage_bytes<BN>() + kEpiWarps * 2 * kOutBlock + 1024; }
 constexpr long long kWaitLimit = 1LL << 24;
 constexpr unsigned long long kWaitNs = 200ull * 1000 * 1000;  // 200 ms wall clock per wait
 
@@ -122,15 +130,18 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   return d;
 }
 
-// instruction descriptor: D f32, A and B tf32, both K-major, N = kBN, M = 128
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kBN >> 3) << 17) |
-                            ((uint32_t)(kBM >> 4) << 24);
+// instruction descriptor: D f32, A and B tf32, both K-major, N = BN, M = 128
+template <int BN>
+constexpr uint32_t idesc() {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+}
 
-__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc_v,
+                                         uint32_t accumulate) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
-      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
+      "l"(adesc), "l"(bdesc), "r"(idesc_v), "r"(accumulate));
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -151,10 +162,14 @@ constexpr int kTileRing = 4;  // tile indices in flight from the producer to the
 constexpr int kTcHeader = 4096;
 
 // one CTA per SM; 10 warps put three on one SM sub-partition, which caps a
-// thread at 168 registers (96 running sums per epilogue thread fit)
+// thread at 168 registers (BN / 2 <= 96 running sums per epilogue thread fit)
+template <int BN>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    const __grid_constant__ CUtensorMap tmC, TcArgs a) {
+  static_assert(BN == 128 || BN == 192, "tiles of 128 or 192 real columns");
+  constexpr int kTileB = tile_b<BN>(), kStageBytes = stage_bytes<BN>();
+  constexpr uint32_t kIdesc = idesc<BN>();
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-byte alignment of the swizzled tiles
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -222,7 +237,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         tile_id[r] = t;
         mbar_arrive(&tile_full[r]);
         if (t < 0) break;
-        const int m0 = (t % a.tiles_m) * kBM, n0 = (t / a.tiles_m) * kBN;
+        const int m0 = (t % a.tiles_m) * kBM, n0 = (t / a.tiles_m) * BN;
         for (int kb = 0; kb < nk; ++kb, ++it) {
           const int s = it % kStages;
           if (it >= kStages && !mbar_wait(&empty[s], ((it / kStages) - 1) & 1, abort_v)) {
@@ -274,11 +289,14 @@ __global__ void __launch_bounds__(kThreads, 1)
             // the two small products first, then hi.hi; 8 tf32 = 32 bytes per MMA
 #pragma unroll
             for (int k = 0; k < kBK / 8; ++k)
-              mma_tf32(acc, smem_desc(sah + 32 * k), smem_desc(sbl + 32 * k), (kb > c * a.chunk || k) ? 1u : 0u);
+              mma_tf32(acc, smem_desc(sah + 32 * k), smem_desc(sbl + 32 * k), kIdesc,
+                       (kb > c * a.chunk || k) ? 1u : 0u);
 #pragma unroll
-            for (int k = 0; k < kBK / 8; ++k) mma_tf32(acc, smem_desc(sal + 32 * k), smem_desc(sbh + 32 * k), 1u);
+            for (int k = 0; k < kBK / 8; ++k)
+              mma_tf32(acc, smem_desc(sal + 32 * k), smem_desc(sbh + 32 * k), kIdesc, 1u);
 #pragma unroll
-            for (int k = 0; k < kBK / 8; ++k) mma_tf32(acc, smem_desc(sah + 32 * k), smem_desc(sbh + 32 * k), 1u);
+            for (int k = 0; k < kBK / 8; ++k)
+              mma_tf32(acc, smem_desc(sah + 32 * k), smem_desc(sbh + 32 * k), kIdesc, 1u);
             mma_commit(&empty[s]);  // frees the stage once these MMAs have read it
             n_consumed = it + 1;
           }
@@ -304,32 +322,44 @@ __global__ void __launch_bounds__(kThreads, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(&tile_empty[r]);
       if (t < 0) break;
-      const int m0 = (t % a.tiles_m) * kBM, n0 = (t / a.tiles_m) * kBN;
-      float sum[kBN / 2];
+      const int m0 = (t % a.tiles_m) * kBM, n0 = (t / a.tiles_m) * BN;
+      float sum[BN / 2];
 #pragma unroll
-      for (int j = 0; j < kBN / 2; ++j) sum[j] = 0.f;
+      for (int j = 0; j < BN / 2; ++j) sum[j] = 0.f;
       for (int c = 0; c < nch; ++c, ++ch) {
         const int b = ch & 1;
         ok = __all_sync(0xffffffffu, mbar_wait(&tfull[b], (ch >> 1) & 1, abort_v));
         if (!ok) break;
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        // two batches of three 16-column loads, each batch waited for once (in
-        // the same asm statement, so no use of r can move above the wait)
+        // batches of 16-column loads (three for BN = 192: two batches; two for
+        // BN = 128: two batches), each batch waited for once (in the same asm
+        // statement, so no use of r can move above the wait)
+        constexpr int kPer = (BN / 2) % 48 == 0 ? 3 : 2;
 #pragma unroll
-        for (int gb = 0; gb < kBN / 96; ++gb) {
-          uint32_t r[48];
-          const uint32_t taddr =
-              tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kBufStride + h * (kBN / 2) + gb * 48);
-          asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%48];\n"
-              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%49];\n"
-              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47}, [%50];\n"
-              "tcgen05.wait::ld.sync.aligned;\n"
-              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47])
-              : "r"(taddr), "r"(taddr + 16u), "r"(taddr + 32u)
-              : "memory");
+        for (int gb = 0; gb < (BN / 2) / (16 * kPer); ++gb) {
+          uint32_t r[16 * kPer];
+          const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) +
+                                 (uint32_t)(b * kBufStride + h * (BN / 2) + gb * 16 * kPer);
+          if constexpr (kPer == 3) {
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%48];\n"
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%49];\n"
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47}, [%50];\n"
+                "tcgen05.wait::ld.sync.aligned;\n"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47])
+                : "r"(taddr), "r"(taddr + 16u), "r"(taddr + 32u)
+                : "memory");
+          } else {
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%32];\n"
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%33];\n"
+                "tcgen05.wait::ld.sync.aligned;\n"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                : "r"(taddr), "r"(taddr + 16u)
+                : "memory");
+          }
 #pragma unroll
-          for (int j = 0; j < 48; ++j) sum[gb * 48 + j] += __uint_as_float(r[j]);
+          for (int j = 0; j < 16 * kPer; ++j) sum[gb * 16 * kPer + j] += __uint_as_float(r[j]);
         }
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
         __syncwarp();
@@ -337,7 +367,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       if (!ok) break;
 #pragma unroll
-      for (int g = 0; g < kBN / 64; ++g, ++nout) {
+      for (int g = 0; g < BN / 64; ++g, ++nout) {
         float* sb = stg + (nout & 1) * (kOutBlock / 4);
         // the reduce that last read this buffer (two blocks ago) has finished reading it
         if (nout >= 2 && lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory");
@@ -352,7 +382,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // visible to the TMA
         __syncwarp();
         if (lane == 0) {
-          tma_reduce_add_2d(&tmC, sb, n0 + h * (kBN / 2) + g * 32, m0 + q * 32);
+          tma_reduce_add_2d(&tmC, sb, n0 + h * (BN / 2) + g * 32, m0 + q * 32);
           asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
         }
       }
@@ -558,8 +588,12 @@ int lu_tc_update(m25_ctx* ctx, zf* A, int64_t lda, int r0, int c0, int m, int nc
   int* err = ctx->Dw.as<int>();
   CUtensorMap ma, mb;
   int rc;
+  // tile N: the context's choice, else 128 for updates of at most 64 complex
+  // columns (one tile without the third of a 192-column tile left empty),
+  // 192 otherwise
+  const int bn = ctx->tune_tc_bn == 128 || ctx->tune_tc_bn == 192 ? ctx->tune_tc_bn : (n2 <= 128 ? 128 : kBNDefault);
   if ((rc = make_map(&ma, A3, m, 2 * pw, kBK, kBM, CU_TENSOR_MAP_SWIZZLE_128B))) return rc;
-  if ((rc = make_map(&mb, B3, n2, 2 * pw, kBK, kBN, CU_TENSOR_MAP_SWIZZLE_128B))) return rc;
+  if ((rc = make_map(&mb, B3, n2, 2 * pw, kBK, bn, CU_TENSOR_MAP_SWIZZLE_128B))) return rc;
   // C: the fp32 view of the block, rows 2 lda floats apart, 32 x 32 boxes
   CUtensorMap mc;
   const float* C = reinterpret_cast<const float*>(A + (int64_t)r0 * lda + c0);
@@ -579,13 +613,24 @@ int lu_tc_update(m25_ctx* ctx, zf* A, int64_t lda, int r0, int c0, int m, int nc
   ta.P = P;
   ta.pw = pw;
   ta.tiles_m = (m + kBM - 1) / kBM;
-  ta.ntiles = ta.tiles_m * ((n2 + kBN - 1) / kBN);
+  ta.ntiles = ta.tiles_m * ((n2 + bn - 1) / bn);
   ta.chunk = (ctx->tune_tc_chunk > 0 ? ctx->tune_tc_chunk : chunk) * (kChunkK / kBK);  // in k-blocks
   ta.err = err;
   ta.counter = reinterpret_cast<int*>(ctx->Dw.as<char>() + 16) + slot;
-  M25_CUDA(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+  static const bool attr =
+      cudaFuncSetAttribute(tc_gemm_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes<128>()) ==
+          cudaSuccess &&
+      cudaFuncSetAttribute(tc_gemm_kernel<192>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes<192>()) ==
+          cudaSuccess;
+  if (!attr) {
+    set_error("tensor-core LU: the update's shared memory could not be reserved");
+    return M25_ERR_CUDA;
+  }
   StageTimer tm(ctx, ST_GEMM);
-  tc_gemm_kernel<<<std::min(ta.ntiles, n_sm), kThreads, kSmemBytes, st>>>(ma, mb, mc, ta);
+  if (bn == 128)
+    tc_gemm_kernel<128><<<std::min(ta.ntiles, n_sm), kThreads, smem_bytes<128>(), st>>>(ma, mb, mc, ta);
+  else
+    tc_gemm_kernel<192><<<std::min(ta.ntiles, n_sm), kThreads, smem_bytes<192>(), st>>>(ma, mb, mc, ta);
   M25_CHECK_LAUNCH();
   return M25_OK;
 }

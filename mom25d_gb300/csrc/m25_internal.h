@@ -76,6 +76,7 @@ struct m25_ctx {
   int tune_cluster_min = 0; // smallest cluster of the LU panel (4, 8 or 16)
   int tune_wave_ctas = 0;   // CTA cap of the triangular solves
   int tune_tc_chunk = 0;    // steps of 32 tf32 per TMEM accumulation of the tensor-core update
+  int tune_tc_bn = 0;       // tile N of the tensor-core update (128 or 192; 0: by the update's width)
   // caller-provided scratch instead of the workspace buffers (LU panel
   // candidates + barrier words; triangular-solve flags, already zeroed)
   char* ext_scratch = nullptr;

@@ -108,7 +108,7 @@ def load():
     lib.m25_greens_remainder.argtypes = [vp, _f64p, _f64p]
     lib.m25_ctx_mem_info.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
     lib.m25_ctx_set_wait_limit.argtypes = [vp, C.c_int64]
-    lib.m25_ctx_set_tuning.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
+    lib.m25_ctx_set_tuning.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     lib.m25_interp_create.argtypes = [vp, C.c_int32, C.c_int32, _f64p, C.c_int32, C.c_int32, C.POINTER(vp)]
     lib.m25_interp_destroy.argtypes = [vp]
     lib.m25_interp_store.argtypes = [vp, C.c_int32, vp, C.c_int64, C.c_int, d, d]

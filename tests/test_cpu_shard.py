@@ -176,10 +176,11 @@ def test_tuning_table_rows_by_size(tmp_path):
     p = tmp_path / "t.json"
     p.write_text(json.dumps(dict(rows=rows)))
     t = load_table(str(p))
-    assert t.knobs(1500) == (4, 16, 2)
-    assert t.knobs(2000) == (4, 16, 2)
-    assert t.knobs(9000) == (16, 0, 1)
-    assert Tuning.fixed(tc_chunk=2).knobs(10 ** 6) == (0, 0, 2)
+    assert t.knobs(1500) == (4, 16, 2, 0)
+    assert t.knobs(2000) == (4, 16, 2, 0)
+    assert t.knobs(9000) == (16, 0, 1, 0)
+    assert Tuning.fixed(tc_chunk=2).knobs(10 ** 6) == (0, 0, 2, 0)
+    assert Tuning.fixed(tc_tile_n=128).knobs(1) == (0, 0, 0, 128)
     with pytest.raises(ValueError):
         Tuning([dict(n_max=1)])
 
