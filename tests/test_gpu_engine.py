@@ -390,6 +390,36 @@ def test_lu_complex64_tensor_cores_small_and_odd_orders(gpu, n):
     ctx.close()
 
 
+@pytest.mark.parametrize("tile_n", [128, 192])
+@pytest.mark.parametrize("n", [257, 1302])
+def test_lu_complex64_tensor_cores_each_tile_shape(gpu, n, tile_n):
+    """Every update of the factorisation in tiles of 128 or of 192 real
+    columns (the context's tile-shape knob, which otherwise picks 128 only for
+    the narrow updates): P L U = A to fp32 accuracy either way."""
+    import ctypes as C
+
+    from mom25d_gb300 import engine as E
+
+    ctx = E.Context(0)
+    E.check(ctx.lib.m25_ctx_set_tuning(ctx.h, 0, 0, 0, tile_n))
+    with pytest.raises(ValueError):
+        E.check(ctx.lib.m25_ctx_set_tuning(ctx.h, 0, 0, 0, 96))
+    rng = np.random.default_rng(2000 + n)
+    lda = n + (n & 1)
+    A = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))).astype(np.complex64)
+    F = np.zeros((n, lda), np.complex64)
+    F[:, :n] = A
+    piv = np.zeros(n, np.int32)
+    info = np.zeros(1, np.int32)
+    E.check(ctx.lib.m25_lu_factor(ctx.h, n, E.M25_MIXED, F.ctypes.data, lda, E.ptr(piv, C.c_int32), E.M25_ON_HOST,
+                                  0, E.ptr(info, C.c_int32)))
+    LU, perm = _lu_reconstruct(F[:, :n].astype(np.complex128), piv)
+    err = np.abs(LU - A[perm]).max() / np.abs(A).max()
+    assert info[0] == 0
+    assert err < 5e-5 * np.sqrt(max(n, 300) / 300), err
+    ctx.close()
+
+
 # ------------------------------------------------------- concurrent points
 def test_sweep_workers_match_one_worker(gpu):
     """Points in flight on separate engine contexts give the results of the
