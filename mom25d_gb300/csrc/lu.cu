@@ -661,21 +661,7 @@ __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, i
       nx += __popc(b);
     }
     for (int i = lane; i < w; i += 32) dst[i] = k0 + i;
-    __syncwarp();
-    const int nd = w + nx;
-    int y[2 * W / 32];
-#pragma unroll
-    for (int h = 0; h < 2 * W / 32; ++h) y[h] = lane + 32 * h < nd ? dst[lane + 32 * h] : -1;
-#pragma unroll 4
-    for (int j = w - 1; j >= 0; --j) {
-      const int r = k0 + j, p = piv[j];
-#pragma unroll
-      for (int h = 0; h < 2 * W / 32; ++h) y[h] = y[h] == r ? p : (y[h] == p ? r : y[h]);
-    }
-#pragma unroll
-    for (int h = 0; h < 2 * W / 32; ++h)
-      if (lane + 32 * h < nd) src[lane + 32 * h] = y[h];
-    if (lane == 0) nd_s = nd;
+    if (lane == 0) nd_s = w + nx;
   }
   // the CTA's columns vc0 .. vc0 + 31 map to vc (< k0) or vc + w (right of the panel)
   const bool any_right = solve && kend < n && min(vc0 + 31, vc_end - 1) >= k0;
@@ -685,6 +671,18 @@ __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, i
   }
   __syncthreads();
   const int nd = nd_s;
+  // the original row of each touched position: the swaps applied to it in
+  // reverse order, one position per thread (nd <= 2 W <= the CTA's threads)
+  for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+    int y = dst[i];
+#pragma unroll 4
+    for (int j = w - 1; j >= 0; --j) {
+      const int r = k0 + j, p = piv[j];
+      y = y == r ? p : (y == p ? r : y);
+    }
+    src[i] = y;
+  }
+  __syncthreads();
   const int vc = vc0 + lane;
   const bool valid = vc < vc_end;
   const int c = vc < k0 ? vc : vc + w;
