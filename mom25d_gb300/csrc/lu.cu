@@ -634,34 +634,39 @@ __global__ void __launch_bounds__(256) swap_trsm_kernel(cx<T>* A, int64_t lda, i
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int kend = k0 + w;
   const int vc0 = vc_begin + blockIdx.x * 32;  // first column of the CTA, counted without the panel's
-  if (warp == 0) {
-    int pr[W / 32];
-#pragma unroll
-    for (int h = 0; h < W / 32; ++h) {
-      const int j = lane + 32 * h;
-      pr[h] = j < w ? (ipiv ? ipiv[k0 + j] : k0 + j) : -1;
-      piv[j] = pr[h];
-    }
-    // positions touched: the panel rows, then each pivot row below the panel once
-    bool first[W / 32];
-#pragma unroll
-    for (int h = 0; h < W / 32; ++h) first[h] = pr[h] >= kend;
-#pragma unroll 8
-    for (int q = 0; q < W; ++q) {
-      const int pq = __shfl_sync(~0u, pr[q >> 5], q & 31);
-#pragma unroll
-      for (int h = 0; h < W / 32; ++h)
-        if (q < lane + 32 * h && pq == pr[h]) first[h] = false;
-    }
+  // positions touched: the panel rows, then each pivot row below the panel
+  // once (its first occurrence among the panel's pivots, in order); one
+  // pivot per thread of the first W / 32 warps
+  __shared__ int wcnt[W / 32];
+  int pj = -1;
+  if (threadIdx.x < W) {
+    pj = (int)threadIdx.x < w ? (ipiv ? ipiv[k0 + threadIdx.x] : k0 + (int)threadIdx.x) : -1;
+    piv[threadIdx.x] = pj;
+  }
+  __syncthreads();
+  bool fst = false;
+  if (threadIdx.x < W && pj >= kend) {
+    fst = true;
+    for (int q = 0; q < (int)threadIdx.x; ++q)
+      if (piv[q] == pj) {
+        fst = false;
+        break;
+      }
+  }
+  const unsigned fb = __ballot_sync(~0u, fst);
+  if (warp < W / 32 && lane == 0) wcnt[warp] = __popc(fb);
+  for (int i = threadIdx.x; i < w; i += blockDim.x) dst[i] = k0 + i;
+  __syncthreads();
+  if (fst) {
+    int off = 0;
+    for (int u = 0; u < warp; ++u) off += wcnt[u];
+    dst[w + off + __popc(fb & ((1u << lane) - 1u))] = pj;
+  }
+  if (threadIdx.x == 0) {
     int nx = 0;
 #pragma unroll
-    for (int h = 0; h < W / 32; ++h) {
-      const unsigned b = __ballot_sync(~0u, first[h]);
-      if (first[h]) dst[w + nx + __popc(b & ((1u << lane) - 1u))] = pr[h];
-      nx += __popc(b);
-    }
-    for (int i = lane; i < w; i += 32) dst[i] = k0 + i;
-    if (lane == 0) nd_s = w + nx;
+    for (int u = 0; u < W / 32; ++u) nx += wcnt[u];
+    nd_s = w + nx;
   }
   // the CTA's columns vc0 .. vc0 + 31 map to vc (< k0) or vc + w (right of the panel)
   const bool any_right = solve && kend < n && min(vc0 + 31, vc_end - 1) >= k0;
