@@ -381,6 +381,64 @@ int m25_deembed_waves(m25_ports* ports, double* A);
  * complex128 cut currents / voltages. NULL skips an output. */
 int m25_deembed_debug(m25_ctx* ctx, m25_ports* ports, double* phi, double* q, double* I, double* V);
 
+/* ---- Compressed operator (H-matrix) and its GMRES solve (Engine/mom25d/
+ * hmatrix.py:145-606, HOperator: assemble, matvec, solve). The host builds
+ * the cluster tree and the block partition; every range below is in tree
+ * order (position k holds RWG basis perm[k]; the via unknowns follow at nb).
+ * near: leaf pairs (a0, am, b0, bn), both orders; far: admissible pairs
+ * (r0, m, c0, n), each unordered pair once, far_cen 1 for the centroid rule;
+ * ent: per leaf (CSR ent_off) the items of its rows (type 0 near pair id,
+ * 1 far block whose rows hold the leaf, 2 far block whose columns hold it;
+ * id; the leaf's offset inside the block's rows / columns; 0); keys: the
+ * near field's (test block x nt + source triangle) pairs, sorted; pblk: the
+ * test blocks holding via pad triangles; pc: preconditioner blocks (first,
+ * size <= 1024) with their items (CSR pc_off; type 0 near pair, 1 far block,
+ * 2 the via block; id). rules: per basis 40 values of the far-field rules
+ * (3-point points, w cA (r - a), w cV; centroids, A cA (c - a), A cV). */
+typedef struct m25_hmat m25_hmat;
+typedef struct {
+  int32_t nb, nv;
+  const int32_t* perm;
+  const double* rules;
+  const int32_t* lev;
+  int32_t nleaf;
+  const int32_t* leaf_lo;     /* (nleaf + 1) */
+  int32_t nnear;
+  const int32_t* near;        /* (nnear, 4) */
+  int32_t nfar;
+  const int32_t* far;         /* (nfar, 4) */
+  const int32_t* far_cen;     /* (nfar) */
+  const int64_t* ent_off;     /* (nleaf + 1) */
+  const int32_t* ent;         /* (ent_off[nleaf], 4) */
+  int64_t nkeys;
+  const int64_t* keys;
+  int32_t npblk;
+  const int32_t* pblk;
+  int32_t npc;
+  const int32_t* pc;          /* (npc, 2) */
+  const int64_t* pc_off;      /* (npc + 1) */
+  const int32_t* pc_items;    /* (pc_off[npc], 2) */
+  double tol;                 /* ACA tolerance (1e-4) */
+  int32_t kcap;               /* most ACA terms stored per block */
+} m25_hmat_desc;
+int m25_hmat_create(m25_ctx* ctx, m25_geom* geom, const m25_hmat_desc* desc, m25_hmat** out);
+int m25_hmat_destroy(m25_hmat* h);
+/* Near field (exact entries of the dense fill), far blocks (ACA, or stored
+ * as they are), via blocks and the preconditioner at the tables' frequency.
+ * stats (8, or NULL): near entries, low-rank blocks, far blocks stored as they
+ * are, far entries held, largest rank, sum of ranks, blocks not low rank,
+ * near-field triangle pairs. */
+int m25_hmat_assemble(m25_hmat* h, m25_greens* gr, double zs_re, double zs_im, double zsv_re, double zsv_im,
+                      int64_t* stats);
+/* y = Z x with the compressed operator; x, y host complex128 (n). */
+int m25_hmat_matvec(m25_hmat* h, const double* x, double* y);
+/* X = Z^-1 B by right-preconditioned restarted GMRES, column by column; B, X
+ * host complex128 (n, nrhs) row-major; iters and resid (true relative
+ * residual) per column. A column that does not reach rtol returns M25_OK
+ * with its residual (the caller accepts or raises, as mom25d does). */
+int m25_hmat_solve(m25_hmat* h, int32_t nrhs, const double* B, double* X, double rtol, int32_t restart,
+                   int32_t maxiter, int32_t* iters, double* resid);
+
 #ifdef __cplusplus
 }
 #endif

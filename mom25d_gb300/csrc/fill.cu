@@ -63,6 +63,11 @@ struct FillArgs {
   float4 jwmu_df, inv_jwe_df, zs_df;  // and the surface impedance (has_zs: not 0)
   int has_zs;
   int* work_counter;   // items handed out beyond the first gridDim.x (zeroed before the launch)
+  // listed fill (fp64; the compressed operator's near field): per (test
+  // block, source triangle) -1 skip, -2 compute for the via pads' IVpad
+  // only, >= 0 the slot of the pair's values in Hc; nullptr: every pair, into H
+  const int32_t* cidx = nullptr;
+  cx<T>* Hc = nullptr;  // (slots, 3 j, 3 i, 32 lanes)
   int nbk;             // mixed fill: buckets of the radius index (0: binary search)
   float bk_scale;      // buckets per unit radius
 };
@@ -481,6 +486,13 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
   const int s_begin = chunk * a.n_src_chunk;
   const int s_end = min(a.nt, s_begin + a.n_src_chunk);
   for (int s = s_begin + warp; s < s_end; s += nwarp) {
+    int slot = -1;
+    if constexpr (!FAR32) {
+      if (a.cidx) {
+        slot = a.cidx[(int64_t)blk * a.nt + s];
+        if (slot == -1) continue;
+      }
+    }
     const int code = a.cls[(int64_t)blk * a.nt + s];
     if ((PASS == 1 && code < 0) || (PASS == 2 && code >= 0)) continue;  // the other pass's pair
     const int ls = a.tri_layer[s];
@@ -602,6 +614,14 @@ __global__ void __launch_bounds__(256, PASS != 0 ? 2 : 1) fill_tri_kernel(FillAr
           cx<float>* row = a.H32 + (int64_t)(3 * s + j) * a.ldh + col0;
 #pragma unroll
           for (int i = 0; i < 3; ++i) row[i] = cx<float>(float(out[i][j].re), float(out[i][j].im));
+        }
+      } else if (a.cidx) {
+        if (slot >= 0) {
+          cx<T>* hc = a.Hc + (int64_t)slot * 288 + lane;
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) hc[(j * 3 + i) * 32] = out[i][j];
         }
       } else {
 #pragma unroll
@@ -900,6 +920,28 @@ __global__ void via_rows_kernel(int nb, int nv, int nt, const cx<T>* __restrict_
   Z[(int64_t)nn * ldz + nb + k] = z;
 }
 
+// The same rows for the compressed operator: ZxbT[i][k] = Zvb[k][perm[i]]
+// (tree order of the RWG unknowns, the via index fastest).
+__global__ void via_rows_tree_kernel(int nb, int nv, int nt, const zd* __restrict__ IVpad,
+                                     const int32_t* __restrict__ seg_pad_off, const int32_t* __restrict__ seg_pad,
+                                     const double* __restrict__ seg_pad_w, const int32_t* __restrict__ etri,
+                                     const int32_t* __restrict__ eloc, const TriData<double>* __restrict__ td,
+                                     zd inv_jwe, const int32_t* __restrict__ perm, zd* __restrict__ ZxbT) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;
+  if (i >= nb || k >= nv) return;
+  const int nn = perm[i];
+  const int ta = etri[2 * nn], la = eloc[2 * nn], tb = etri[2 * nn + 1], lb = eloc[2 * nn + 1];
+  const double ca = td[ta].cV[la], cb = td[tb].cV[lb];
+  zd acc;
+  for (int e = seg_pad_off[k]; e < seg_pad_off[k + 1]; ++e) {
+    const int p = seg_pad[e];
+    const zd y = IVpad[(int64_t)p * nt + ta] * ca + IVpad[(int64_t)p * nt + tb] * cb;
+    acc += y * seg_pad_w[e];
+  }
+  ZxbT[(int64_t)i * nv + k] = inv_jwe * acc;
+}
+
 __device__ inline double filament_f(double s, double d) { return s * asinh(s / d) - sqrt(s * s + d * d); }
 
 // Grover's partial mutual inductance of parallel z filaments [a1,a2], [b1,b2]
@@ -982,6 +1024,90 @@ __global__ void im_gv0_kernel(int L, int nrho, const double* __restrict__ rho, c
   out[p] = g.im;
 }
 
+// The fill's arguments shared by the dense and the listed fill: geometry,
+// tables, constants; the scratch pointers are the caller's. smem: the
+// kernel's dynamic shared memory (the tables).
+template <class T>
+static int fill_setup(m25_geom* geom, m25_greens* gr, zd zs, bool f32, FillArgs<T>& a, size_t& smem) {
+  const int nt = geom->nt, nb = geom->nb, L = geom->nlev;
+  const int nrho = gr->nrho;
+  a.nt = nt;
+  a.nb = nb;
+  a.nlev = L;
+  a.nblocks = geom->nblocks;
+  a.td = std::is_same<T, double>::value ? reinterpret_cast<const TriData<T>*>(geom->td64)
+                                        : reinterpret_cast<const TriData<T>*>(geom->td32);
+  a.cen = geom->cen;
+  a.cen_df = geom->cen_df;
+  a.tri_layer = geom->tri_layer;
+  a.block_tris = geom->block_tris;
+  a.block_level = geom->block_level;
+  a.cls = geom->cls;
+  a.stat = std::is_same<T, double>::value ? reinterpret_cast<const T*>(geom->stat64)
+                                          : reinterpret_cast<const T*>(geom->stat32);
+  a.stat6 = geom->stat6;
+  a.tddf = geom->tddf;
+  a.pad_pos = geom->pad_pos;
+  a.nrho = nrho;
+  a.rho = std::is_same<T, double>::value ? reinterpret_cast<const T*>(gr->rho) : reinterpret_cast<const T*>(gr->rho32);
+  a.coef = std::is_same<T, double>::value ? reinterpret_cast<const T*>(gr->coef)
+                                          : reinterpret_cast<const T*>(gr->coef32);
+  for (int p = 0; p < L * L; ++p) {
+    zd ca = gr->lead_h[0 * L * L + p], cv = gr->lead_h[1 * L * L + p];
+    a.lead[p][0] = cx<T>(T(ca.re), T(ca.im));
+    a.lead[p][1] = cx<T>(T(cv.re), T(cv.im));
+    a.dz[p] = T(gr->dz_h[p]);
+  }
+  const double omega = gr->omega;
+  zd jwmu(0.0, omega * kMu0);
+  zd inv_jwe = zd(1.0) / zd(0.0, omega * eps0());
+  a.jwmu = cx<T>(T(jwmu.re), T(jwmu.im));
+  a.inv_jwe = cx<T>(T(inv_jwe.re), T(inv_jwe.im));
+  a.zs = cx<T>(T(zs.re), T(zs.im));
+  a.td32 = geom->td32;
+  a.coef32 = gr->coef32;
+  for (int p = 0; p < L * L; ++p) {
+    zd ca = gr->lead_h[0 * L * L + p], cv = gr->lead_h[1 * L * L + p];
+    a.lead32[p][0] = cx<float>(float(ca.re), float(ca.im));
+    a.lead32[p][1] = cx<float>(float(cv.re), float(cv.im));
+    a.dz32[p] = float(gr->dz_h[p]);
+  }
+  a.jwmu32 = cx<float>(float(jwmu.re), float(jwmu.im));
+  a.inv_jwe32 = cx<float>(float(inv_jwe.re), float(inv_jwe.im));
+  for (int p = 0; p < L * L; ++p) {
+    const zd ca = gr->lead_h[0 * L * L + p], cv = gr->lead_h[1 * L * L + p];
+    a.lead_df[p][0] = dfc_split(ca.re, ca.im);
+    a.lead_df[p][1] = dfc_split(cv.re, cv.im);
+  }
+  a.jwmu_df = dfc_split(jwmu.re, jwmu.im);
+  a.zs_df = dfc_split(zs.re, zs.im);
+  a.has_zs = zs.re != 0.0 || zs.im != 0.0;
+  a.inv_jwe_df = dfc_split(inv_jwe.re, inv_jwe.im);
+  // mixed fill: bucket index of the fp32 radii, buckets no wider than the
+  // smallest radius step (at most 16384)
+  a.nbk = 0;
+  a.bk_scale = 0.f;
+  if (f32) {
+    const std::vector<double>& hr = gr->rho_h;
+    float gap = INFINITY;
+    for (int i = 0; i + 1 < nrho; ++i) gap = std::min(gap, (float)hr[i + 1] - (float)hr[i]);
+    const float last = (float)hr[nrho - 1];
+    if (gap > 0.f && last > 0.f) {
+      a.nbk = std::min(16384, (int)std::ceil(last / gap) + 1);
+      a.bk_scale = (float)a.nbk / last;
+    }
+  }
+  // fp64 fill: both tables; mixed (f32): the fp32 radii and tables only (+ the bucket index)
+  smem = f32 ? sizeof(float) * (((nrho + 3) & ~3) + (size_t)L * (nrho - 1) * 16) +
+                   sizeof(uint16_t) * (((size_t)a.nbk + 7) & ~(size_t)7)
+             : sizeof(T) * (((nrho + 3) & ~3) + (size_t)L * (nrho - 1) * 16) + sizeof(float) * ((nrho + 3) & ~3);
+  if (smem > 220 * 1024) {
+    set_error("m25_assemble: Green's tables too large for shared memory (reduce rho_max or levels)");
+    return M25_ERR_VALUE;
+  }
+  return M25_OK;
+}
+
 // Stage 1 + 2 + 3 on the context's stream; Z is host or device memory.
 template <class T>
 int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, void* Zout, int64_t ldz, int where,
@@ -1017,85 +1143,14 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
     ldzd = n;
   }
   FillArgs<T> a;
-  a.nt = nt;
-  a.nb = nb;
-  a.nlev = L;
-  a.nblocks = geom->nblocks;
-  a.td = std::is_same<T, double>::value ? reinterpret_cast<const TriData<T>*>(geom->td64)
-                                        : reinterpret_cast<const TriData<T>*>(geom->td32);
-  a.cen = geom->cen;
-  a.cen_df = geom->cen_df;
-  a.tri_layer = geom->tri_layer;
-  a.block_tris = geom->block_tris;
-  a.block_level = geom->block_level;
-  a.cls = geom->cls;
-  a.stat = std::is_same<T, double>::value ? reinterpret_cast<const T*>(geom->stat64)
-                                          : reinterpret_cast<const T*>(geom->stat32);
-  a.stat6 = geom->stat6;
-  a.tddf = geom->tddf;
-  a.pad_pos = geom->pad_pos;
-  a.nrho = nrho;
-  a.rho = std::is_same<T, double>::value ? reinterpret_cast<const T*>(gr->rho) : reinterpret_cast<const T*>(gr->rho32);
-  a.coef = std::is_same<T, double>::value ? reinterpret_cast<const T*>(gr->coef)
-                                          : reinterpret_cast<const T*>(gr->coef32);
-  for (int p = 0; p < L * L; ++p) {
-    zd ca = gr->lead_h[0 * L * L + p], cv = gr->lead_h[1 * L * L + p];
-    a.lead[p][0] = cx<T>(T(ca.re), T(ca.im));
-    a.lead[p][1] = cx<T>(T(cv.re), T(cv.im));
-    a.dz[p] = T(gr->dz_h[p]);
-  }
+  size_t smem = 0;
+  if ((rc = fill_setup<T>(geom, gr, zs, f32, a, smem))) return rc;
   const double omega = gr->omega;
-  zd jwmu(0.0, omega * kMu0);
-  zd inv_jwe = zd(1.0) / zd(0.0, omega * eps0());
-  a.jwmu = cx<T>(T(jwmu.re), T(jwmu.im));
-  a.inv_jwe = cx<T>(T(inv_jwe.re), T(inv_jwe.im));
-  a.zs = cx<T>(T(zs.re), T(zs.im));
   a.H = H;
   a.ldh = ldh;
   a.H32 = H32;
   a.Hn = Hn;
   a.IVpad = IVpad;
-  a.td32 = geom->td32;
-  a.coef32 = gr->coef32;
-  for (int p = 0; p < L * L; ++p) {
-    zd ca = gr->lead_h[0 * L * L + p], cv = gr->lead_h[1 * L * L + p];
-    a.lead32[p][0] = cx<float>(float(ca.re), float(ca.im));
-    a.lead32[p][1] = cx<float>(float(cv.re), float(cv.im));
-    a.dz32[p] = float(gr->dz_h[p]);
-  }
-  a.jwmu32 = cx<float>(float(jwmu.re), float(jwmu.im));
-  a.inv_jwe32 = cx<float>(float(inv_jwe.re), float(inv_jwe.im));
-  for (int p = 0; p < L * L; ++p) {
-    const zd ca = gr->lead_h[0 * L * L + p], cv = gr->lead_h[1 * L * L + p];
-    a.lead_df[p][0] = dfc_split(ca.re, ca.im);
-    a.lead_df[p][1] = dfc_split(cv.re, cv.im);
-  }
-  a.jwmu_df = dfc_split(jwmu.re, jwmu.im);
-  a.zs_df = dfc_split(zs.re, zs.im);
-  a.has_zs = zs.re != 0.0 || zs.im != 0.0;
-  a.inv_jwe_df = dfc_split(inv_jwe.re, inv_jwe.im);
-  // mixed fill: bucket index of the fp32 radii, buckets no wider than the
-  // smallest radius step (at most 16384)
-  a.nbk = 0;
-  a.bk_scale = 0.f;
-  if (f32) {
-    const std::vector<double>& hr = gr->rho_h;
-    float gap = INFINITY;
-    for (int i = 0; i + 1 < nrho; ++i) gap = std::min(gap, (float)hr[i + 1] - (float)hr[i]);
-    const float last = (float)hr[nrho - 1];
-    if (gap > 0.f && last > 0.f) {
-      a.nbk = std::min(16384, (int)std::ceil(last / gap) + 1);
-      a.bk_scale = (float)a.nbk / last;
-    }
-  }
-  // fp64 fill: both tables; mixed (f32): the fp32 radii and tables only (+ the bucket index)
-  size_t smem = f32 ? sizeof(float) * (((nrho + 3) & ~3) + (size_t)L * (nrho - 1) * 16) +
-                          sizeof(uint16_t) * (((size_t)a.nbk + 7) & ~(size_t)7)
-                    : sizeof(T) * (((nrho + 3) & ~3) + (size_t)L * (nrho - 1) * 16) + sizeof(float) * ((nrho + 3) & ~3);
-  if (smem > 220 * 1024) {
-    set_error("m25_assemble: Green's tables too large for shared memory (reduce rho_max or levels)");
-    return M25_ERR_VALUE;
-  }
   // the passes: fp64 = one kernel over all pairs; mixed = near, then mid / far
   using Kern = void (*)(FillArgs<T>);
   Kern kerns[2] = {f32 ? fill_tri_kernel<T, true, 1> : fill_tri_kernel<T, false, 0>, fill_tri_kernel<T, true, 2>};
@@ -1184,6 +1239,75 @@ int fill_driver(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, voi
     M25_CUDA(cudaMemcpy2DAsync(Zout, sizeof(cx<T>) * ldz, Z, sizeof(cx<T>) * n, sizeof(cx<T>) * n, n,
                                cudaMemcpyDeviceToHost, st));
     M25_CUDA(cudaStreamSynchronize(st));
+  }
+  return M25_OK;
+}
+
+// The compressed operator's near field (fp64): the listed (test block,
+// source triangle) pairs' half-basis values into Hc, the via pads' charge
+// integrals, then the via unknowns' rows in tree order (ZxbT, nb x nv) and
+// their block (Zxx, nv x nv). cidx: per (block, source) -1 skip, -2 compute
+// for the pads only, >= 0 the slot in Hc.
+int fill_listed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, const int32_t* cidx, zd* Hc,
+                const int32_t* perm, zd* ZxbT, zd* Zxx) {
+  cudaStream_t st = ctx->stream;
+  const int nt = geom->nt, nb = geom->nb, nv = geom->nv, L = geom->nlev;
+  const int nrho = gr->nrho;
+  int rc;
+  if ((rc = ctx->H.ensure(sizeof(zd) * (size_t)std::max(geom->npad, 1) * nt + sizeof(double) * 16))) return rc;
+  zd* IVpad = ctx->H.as<zd>();
+  double* imgv = reinterpret_cast<double*>(IVpad + (size_t)std::max(geom->npad, 1) * nt);
+  FillArgs<double> a;
+  size_t smem = 0;
+  if ((rc = fill_setup<double>(geom, gr, zs, false, a, smem))) return rc;
+  a.H = nullptr;
+  a.ldh = 0;
+  a.H32 = nullptr;
+  a.Hn = nullptr;
+  a.IVpad = IVpad;
+  a.cidx = cidx;
+  a.Hc = Hc;
+  auto kern = fill_tri_kernel<double, false, 0>;
+  M25_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+  int occ = 1;
+  M25_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, smem));
+  const int grid = std::max(1, occ) * ctx->num_sms;
+  int nchunk = std::max(1, std::min((16 * grid + geom->nblocks - 1) / geom->nblocks, (nt + 63) / 64));
+  a.n_src_chunk = (nt + nchunk - 1) / nchunk;
+  nchunk = (nt + a.n_src_chunk - 1) / a.n_src_chunk;
+  a.n_chunks = nchunk;
+  if (nv) M25_CUDA(cudaMemsetAsync(IVpad, 0, sizeof(zd) * (size_t)geom->npad * nt, st));
+  if ((rc = ctx->sched.ensure(256))) return rc;
+  M25_CUDA(cudaMemsetAsync(ctx->sched.p, 0, 2 * sizeof(int), st));
+  a.work_counter = ctx->sched.as<int>();
+  {
+    StageTimer tm(ctx, ST_FILL);
+    kern<<<std::min(grid, geom->nblocks * nchunk), 256, smem, st>>>(a);
+  }
+  M25_CHECK_LAUNCH();
+  if (nv) {
+    std::vector<zd> hv(L * L);
+    std::vector<double> hdz(L * L);
+    for (int p = 0; p < L * L; ++p) {
+      hv[p] = gr->lead_h[1 * L * L + p];
+      hdz[p] = gr->dz_h[p];
+    }
+    if ((rc = ctx->Dw.ensure(sizeof(zd) * 2 * kMaxLevSq))) return rc;
+    zd* dv = ctx->Dw.as<zd>();
+    double* ddz = reinterpret_cast<double*>(dv + kMaxLevSq);
+    M25_CUDA(cudaMemcpyAsync(dv, hv.data(), sizeof(zd) * L * L, cudaMemcpyHostToDevice, st));
+    M25_CUDA(cudaMemcpyAsync(ddz, hdz.data(), sizeof(double) * L * L, cudaMemcpyHostToDevice, st));
+    StageTimer tm(ctx, ST_VIA);
+    im_gv0_kernel<<<1, 32, 0, st>>>(L, nrho, gr->rho, reinterpret_cast<const zd*>(gr->coef), dv, ddz, gr->stack_h,
+                                    imgv);
+    via_rows_tree_kernel<<<dim3((nb + 127) / 128, nv), 128, 0, st>>>(
+        nb, nv, nt, IVpad, geom->seg_pad_off, geom->seg_pad, geom->seg_pad_w, geom->edge_tri, geom->edge_loc,
+        geom->td64, a.inv_jwe, perm, ZxbT);
+    // the via block: via_block_kernel writes Z[(nb + k) ldz + nb + m]; nb = 0, ldz = nv address Zxx
+    via_block_kernel<double, double><<<dim3((nv + 31) / 32, nv), 32, 0, st>>>(
+        0, nv, nt, L, IVpad, geom->pad_tris, geom->seg_pad_off, geom->seg_pad, geom->seg_pad_w, geom->seg_end_lev,
+        geom->seg_span, geom->seg_xy, geom->seg_drill, imgv, gr->omega, zsv, gr->stack_h, Zxx, nv);
+    M25_CHECK_LAUNCH();
   }
   return M25_OK;
 }

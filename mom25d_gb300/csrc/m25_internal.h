@@ -159,6 +159,9 @@ struct FillSplit {
   zf *Zh, *Zl, *LU;
   int64_t ldl;
 };
+// the compressed operator's near field and via rows (fill.cu)
+int fill_listed(m25_ctx* ctx, m25_geom* geom, m25_greens* gr, zd zs, zd zsv, const int32_t* cidx, zd* Hc,
+                const int32_t* perm, zd* ZxbT, zd* Zxx);
 int alloc(std::vector<void*>& list, void** p, size_t bytes);
 void free_all(std::vector<void*>& list);
 // Stream-ordered variants for the per-frequency objects: unlike cudaFree,

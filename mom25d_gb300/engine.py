@@ -30,7 +30,8 @@ EXPORTS = ("m25_last_error", "m25_version", "m25_ctx_create", "m25_ctx_destroy",
            "m25_mlp_destroy", "m25_mlp_params", "m25_mlp_loss_grad", "m25_mlp_train", "m25_mlp_forward",
            "m25_ctx_mem_info", "m25_interp_create", "m25_interp_destroy", "m25_interp_store", "m25_interp_eval",
            "m25_interp_anchor", "m25_interp_point", "m25_deembed_waves", "m25_ctx_set_wait_limit",
-           "m25_deembed_fit_info", "m25_ctx_set_tuning", "m25_ports_set_excitations", "m25_deembed_coefs")
+           "m25_deembed_fit_info", "m25_ctx_set_tuning", "m25_ports_set_excitations", "m25_deembed_coefs",
+           "m25_hmat_create", "m25_hmat_destroy", "m25_hmat_assemble", "m25_hmat_matvec", "m25_hmat_solve")
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
@@ -62,6 +63,17 @@ class PortDesc(C.Structure):
                 ("ns", _i32p), ("s", _f64p), ("cut_off", _i32p), ("cut_edge", _i32p), ("cut_w", _f64p),
                 ("nvpt", _i32p), ("vpts", _f64p), ("beta0", _f64p), ("lossless", C.c_int32), ("bounds", _f64p),
                 ("v_weight", C.c_double), ("excitation", _f64p)]
+
+
+_i64p = C.POINTER(C.c_int64)
+
+
+class HmatDesc(C.Structure):
+    _fields_ = [("nb", C.c_int32), ("nv", C.c_int32), ("perm", _i32p), ("rules", _f64p), ("lev", _i32p),
+                ("nleaf", C.c_int32), ("leaf_lo", _i32p), ("nnear", C.c_int32), ("near", _i32p),
+                ("nfar", C.c_int32), ("far", _i32p), ("far_cen", _i32p), ("ent_off", _i64p), ("ent", _i32p),
+                ("nkeys", C.c_int64), ("keys", _i64p), ("npblk", C.c_int32), ("pblk", _i32p), ("npc", C.c_int32),
+                ("pc", _i32p), ("pc_off", _i64p), ("pc_items", _i32p), ("tol", C.c_double), ("kcap", C.c_int32)]
 
 
 _lib = None
@@ -116,6 +128,11 @@ def load():
     lib.m25_interp_anchor.argtypes = [vp, vp, vp, vp, C.c_int32, d, d, d, d, C.c_int, d]
     lib.m25_interp_point.argtypes = [vp, vp, vp, vp, vp, C.c_int32, _i32p, _f64p, d, C.c_int, _f64p, d, C.c_int32,
                                      _f64p, _f64p, _f64p, _f64p, _f64p, _f64p, _i32p]
+    lib.m25_hmat_create.argtypes = [vp, vp, C.POINTER(HmatDesc), C.POINTER(vp)]
+    lib.m25_hmat_destroy.argtypes = [vp]
+    lib.m25_hmat_assemble.argtypes = [vp, vp, d, d, d, d, _i64p]
+    lib.m25_hmat_matvec.argtypes = [vp, _f64p, _f64p]
+    lib.m25_hmat_solve.argtypes = [vp, C.c_int32, _f64p, _f64p, d, C.c_int32, C.c_int32, _i32p, _f64p]
     f32p = C.POINTER(C.c_float)
     lib.m25_mlp_create.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(vp)]
     lib.m25_mlp_destroy.argtypes = [vp]

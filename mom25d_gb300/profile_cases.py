@@ -4,6 +4,7 @@
     python -m mom25d_gb300.profile_cases point --workload lpf --precision mixed [--reps 1]
     python -m mom25d_gb300.profile_cases lu --n 4096 [--simt] [--reps 1]
     python -m mom25d_gb300.profile_cases batch [--variants 16] [--nfreq 128] [--workers 8]
+    python -m mom25d_gb300.profile_cases hmatrix --workload gcpw [--freq 10e9] [--reps 2]
 
 `fill` builds the mesh geometry and one frequency's Green's tables, then
 runs the impedance fill `reps` times (device output, no host copy);
@@ -13,7 +14,10 @@ device (tensor-core trailing updates unless --simt); `batch` sweeps the
 band-pass variants 0 .. variants - 1 at nfreq frequencies 1-12 GHz (mixed
 precision) once variant by variant (each a concurrent sweep on `workers`
 contexts) and once as one VariantBatch, and prints the points per second of
-both. Each exits non-zero on any engine error.
+both; `hmatrix` runs `reps` points with the compressed operator (method
+"hmatrix") and one with the dense mixed path, and prints the stage times,
+the operator's size and GMRES iterations, and the largest |dS| between the
+two. Each exits non-zero on any engine error.
 """
 
 import argparse
@@ -28,7 +32,7 @@ from .solver import PRECISIONS, Solver
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("mode", choices=["fill", "point", "lu", "batch"])
+    ap.add_argument("mode", choices=["fill", "point", "lu", "batch", "hmatrix"])
     ap.add_argument("--variants", type=int, default=16, help="batch mode: band-pass variants")
     ap.add_argument("--nfreq", type=int, default=128, help="batch mode: frequencies per variant")
     ap.add_argument("--workers", type=int, default=8, help="batch mode: points in flight")
@@ -44,6 +48,8 @@ def main():
         return lu_case(args)
     if args.mode == "batch":
         return batch_case(args)
+    if args.mode == "hmatrix":
+        return hmatrix_case(args)
     import mom25d_gb300 as G
 
     kw = {"k": 0} if args.workload == "bandpass" else {}
@@ -69,6 +75,50 @@ def main():
             S = sol.point(f)[0]
         print(f"point ok: N={mesh.n_unknowns} S11={np.round(S[0, 0], 6)}")
     sol.close()
+
+
+def hmatrix_case(args):
+    import json
+    import time
+
+    import mom25d_gb300 as G
+
+    kw = {"k": 0} if args.workload == "bandpass" else {}
+    lay, st, mesh, freqs = workloads.build(G, args.workload, **kw)
+    f = args.freq or float(freqs[len(freqs) // 2])
+    sol = Solver(mesh, st, verbose=False, method="hmatrix")
+    t = time.perf_counter()
+    hop = sol.hoperator()
+    t_plan = time.perf_counter() - t
+    times = []
+    for _ in range(max(1, args.reps)):
+        t = time.perf_counter()
+        g = sol.greens(f)
+        zs = complex(sol.surface_impedance(f))
+        hop.assemble(g, zs, zs)
+        sol.ctx.synchronize()
+        t1 = time.perf_counter()
+        X = hop.solve(sol.port_excitations())
+        t2 = time.perf_counter()
+        g.close()
+        times.append((t1 - t, t2 - t1))
+    S_h = sol.point(f)[0]
+    sol.close()
+    dense = Solver(mesh, st, verbose=False, precision="mixed")
+    dense.point(f)
+    t = time.perf_counter()
+    S_d = dense.point(f)[0]
+    t_dense = time.perf_counter() - t
+    dense.close()
+    s = dict(hop.stats)
+    out = dict(workload=args.workload, N=mesh.n_unknowns, freq=f, plan_s=round(t_plan, 3),
+               assemble_s=round(min(a for a, _ in times), 4), solve_s=round(min(b for _, b in times), 4),
+               hmatrix_point_s=round(min(a + b for a, b in times), 4), dense_mixed_point_s=round(t_dense, 4),
+               entries_vs_dense=round((s["near_entries"] + s["far_entries"]) / mesh.n_unknowns ** 2, 4),
+               max_dS_vs_dense_mixed=float(np.abs(S_h - S_d).max()),
+               **{k: s[k] for k in ("leaves", "near_pairs", "far_blocks", "lowrank_blocks", "dense_far_blocks",
+                                    "max_rank", "not_low_rank", "near_field_pairs", "gmres_iterations")})
+    print(json.dumps(out))
 
 
 def lu_case(args):

@@ -310,7 +310,10 @@ class Solver:
     mesh      : a Mesh with RWG data, via segments and port cuts (this
                 package's grid mesher, or mom25d's own Mesh object)
     substrate : Substrate or Stackup (open top, no inner planes)
-    method    : "dense" (the only method of this engine; "auto" maps to it)
+    method    : "dense" (Z + LU), "hmatrix" (compressed Z + GMRES,
+                mom25d_gb300/hmatrix.py) or "auto": hmatrix above HMATRIX_N
+                unknowns (where the dense working set no longer fits beside
+                other work on one GPU), else dense
     precision : "fp64" (fill + LU in fp64), "mixed" (fill with fp64 singular
                 parts and fp32 elsewhere, complex64 LU, fp64 GMRES refinement
                 to the normwise backward error refine_tol) or "mixed_fill32"
@@ -324,10 +327,15 @@ class Solver:
                 (refine_steps -1, listed in the sweep's info["fp64_fallback"])
     """
 
+    # "auto": the compressed solver above this many unknowns (mom25d switches at 7000,
+    # Engine/mom25d/solver.py:1037, to fit host memory; one GB300 holds the mixed
+    # path's dense planes of N = 60000 in about 90 GB)
+    HMATRIX_N = 60000
+
     def __init__(self, mesh, substrate, z0=None, verbose=True, method="dense", v_weight=None, precision="fp64",
                  device=0, refine_tol=1e-12, max_refine=60):
-        if method not in ("auto", "dense"):
-            raise ValueError("this engine implements method='dense' only")
+        if method not in ("auto", "dense", "hmatrix"):
+            raise ValueError("method must be 'auto', 'dense' or 'hmatrix'")
         if precision not in PRECISIONS:
             raise ValueError("precision must be 'fp64', 'mixed' or 'mixed_fill32'")
         self.mesh = mesh
@@ -366,7 +374,11 @@ class Solver:
             self.iport_index = [names.index(ip["name"]) if ip["kind"] == "gap" else col[k]
                                 for k, ip in enumerate(self.iports)]
         self.values = {}  # per-sweep overrides of lumped values
-        self.method = "dense"
+        if method == "auto":
+            method = "hmatrix" if mesh.n_unknowns > self.HMATRIX_N else "dense"
+        self.method = method
+        self._hop = None
+        self.hmatrix_options = {}  # HMatrix keyword arguments (leaf, eta, tol, kcap, prec_block)
         self.precision = precision
         self.refine_tol, self.max_refine = refine_tol, max_refine
         self.z0_fixed = None if z0 is None else np.asarray(z0, float)
@@ -524,11 +536,34 @@ class Solver:
         """RWG (+ via segment) coefficients (N, Nexc) for the given excitations
         (default: one 1 V delta gap per port)."""
         g = greens or self.greens(freq)
+        B = self.port_excitations() if excitations is None else excitations
+        if self.method == "hmatrix" and Z is None:
+            return self._hmatrix_solve(freq, g, B)
         if Z is None:
             Z = self.impedance(freq, g)
-        B = self.port_excitations() if excitations is None else excitations
         return dense_solve(Z, B, precision=self.precision, ctx=self.ctx, tol=self.refine_tol,
                            max_iter=self.max_refine)
+
+    def hoperator(self):
+        """The compressed operator of this mesh (built once, on this solver's context)."""
+        if self._hop is None:
+            from .hmatrix import HMatrix
+
+            self._hop = HMatrix(self, **self.hmatrix_options)
+        return self._hop
+
+    def _hmatrix_solve(self, freq, g, B):
+        """Z^-1 B with the compressed operator assembled at freq; each
+        distinct column solved once (Engine/mom25d/solver.py:994-1011)."""
+        hop = self.hoperator()
+        zs = complex(self.surface_impedance(freq))
+        hop.assemble(g, zs, zs)
+        B = np.asarray(B, complex).reshape(self.mesh.n_unknowns, -1)
+        _, first, inv = np.unique(B.T, axis=0, return_index=True, return_inverse=True)
+        X = hop.solve(B[:, first])[:, np.ravel(inv)]
+        if self.verbose:
+            print(f"  f = {freq / 1e9:8.4f} GHz  N = {self.mesh.n_unknowns}  {hop.summary()}", flush=True)
+        return X
 
     OPEN = 1e12  # ohm: an unloaded lumped gap
 
@@ -581,18 +616,21 @@ class Solver:
         P, ni = len(self.ports), len(self.iports)
         n = P + ni
         E0 = self.port_excitations()
-        B = np.hstack([E0, self.Lm])
+        B = E0 if self.Lm is None else np.hstack([E0, self.Lm])
         prec = "fp64" if self.precision == "fp64" else "mixed"
         steps = 0
-        try:
-            X = dense_solve(Z, B, precision=prec, ctx=self.ctx, tol=self.refine_tol, max_iter=self.max_refine)
-        except E.NumericError:
-            if prec == "fp64":
-                raise
-            # the mixed refinement stopped above its target: this point in fp64
-            X = dense_solve(Z, B, precision="fp64", ctx=self.ctx)
-            steps = -1
-        x = np.ascontiguousarray(self._load_lumped(X[:, :n], X[:, n:], f))
+        if Z is None:  # the compressed operator
+            X = self._hmatrix_solve(f, g, B)
+        else:
+            try:
+                X = dense_solve(Z, B, precision=prec, ctx=self.ctx, tol=self.refine_tol, max_iter=self.max_refine)
+            except E.NumericError:
+                if prec == "fp64":
+                    raise
+                # the mixed refinement stopped above its target: this point in fp64
+                X = dense_solve(Z, B, precision="fp64", ctx=self.ctx)
+                steps = -1
+        x = np.ascontiguousarray(X[:, :n] if self.Lm is None else self._load_lumped(X[:, :n], X[:, n:], f))
         S = np.zeros((P, P), complex)
         z0 = np.zeros(P)
         gam = np.zeros(P, complex)
@@ -634,9 +672,11 @@ class Solver:
 
     def point(self, f, keep_currents=False):
         """One frequency of the sweep on the device: (S, z0, gamma, z0_line, residual, x or None, info)."""
-        if self.Lm is not None:
+        if self.Lm is not None or self.method == "hmatrix":
+            # lumped loads, internal ports or the compressed operator: the
+            # solve, then the de-embedding of the currents
             g = self.greens(f)
-            out = self._lumped_point(f, g, self.impedance(f, g), keep_currents)
+            out = self._lumped_point(f, g, None if self.method == "hmatrix" else self.impedance(f, g), keep_currents)
             g.close()
             return out
         g = self.greens(f)
@@ -713,7 +753,7 @@ class Solver:
     def _checkpoint_key(self, freqs):
         return checkpoint_key(self.mesh, freqs, values_digest(self.values, self.lumped, self.components))
 
-    _DEVICE_STATE = ("ctx", "_ctx_owner", "_geom", "_geom_owner", "_ports", "_siblings", "_sib_lock")
+    _DEVICE_STATE = ("ctx", "_ctx_owner", "_geom", "_geom_owner", "_ports", "_siblings", "_sib_lock", "_hop")
 
     def _clone(self, ctx=None):
         """A solver sharing this one's host-side set-up (mesh, port models,
@@ -729,6 +769,7 @@ class Solver:
         s._geom = self.geometry()
         s._geom_owner = False  # closed by this solver, after its siblings
         s._ports = None
+        s._hop = None
         s._siblings = []
         s._sib_lock = threading.Lock()
         return s
@@ -816,6 +857,11 @@ class Solver:
         freqs = np.atleast_1d(np.asarray(freqs, float))
         self.values.clear()  # shared with the sweep's workers
         self.values.update(values or {})
+        if self.method == "hmatrix":
+            # FreqInterp stores dense matrices (Engine/mom25d/solver.py:1208-1209); the
+            # compressed operator is one per solver: its points run one after another
+            interp = None
+            workers = 1
         ip = None
         if isinstance(interp, str):
             if interp != "auto":
@@ -931,6 +977,9 @@ class Solver:
         for sib in self._siblings:
             sib.close()
         self._siblings = []
+        if getattr(self, "_hop", None) is not None:
+            self._hop.close()
+            self._hop = None
         if self._ports is not None:
             self._ports.close()
         if self._geom is not None and getattr(self, "_geom_owner", True):

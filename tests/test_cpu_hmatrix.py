@@ -1,0 +1,144 @@
+"""Host side of the compressed operator (mom25d_gb300/hmatrix.py): the
+cluster tree and block partition against mom25d's own (tests/golden/
+hmatrix.npz, made by make_hmatrix_golden.py), and the index lists that the
+device kernels follow (near-field pairs, per-leaf row items, preconditioner
+blocks), checked entry by entry on small meshes."""
+
+import os
+
+import numpy as np
+import pytest
+
+import mom25d_gb300 as G
+from mom25d_gb300 import hmatrix as H
+from mom25d_gb300 import workloads
+from mom25d_gb300.solver import test_blocks as morton_blocks
+
+from conftest import GOLDEN
+
+
+def _cover(nodes_far_near, n):
+    far, near = nodes_far_near
+    cover = np.zeros((n, n), int)
+    for a, b in near:
+        cover[a.lo:a.hi, b.lo:b.hi] += 1
+    for a, b in H.unique_far(far):
+        cover[a.lo:a.hi, b.lo:b.hi] += 1
+        cover[b.lo:b.hi, a.lo:a.hi] += 1
+    return cover
+
+
+def test_partition_covers_every_entry_once():
+    """Near leaf pairs plus far blocks (each unordered pair once, applied with
+    its transpose) tile the matrix exactly: random points and a regular grid
+    (equal cluster diameters, where the tie-break by id keeps the partition
+    symmetric)."""
+    for pos in (np.random.default_rng(3).random((400, 3)),
+                np.c_[np.mgrid[0:20, 0:20].reshape(2, -1).T * 1.0, np.zeros(400)]):
+        perm, nodes, root = H.cluster_tree(pos, np.full(len(pos), 0.01), 16)
+        assert np.array_equal(np.sort(perm), np.arange(len(pos)))
+        far, near = H.partition(root, 1.0)
+        assert far and np.all(_cover((far, near), len(pos)) == 1)
+
+
+def _golden():
+    path = os.path.join(GOLDEN, "hmatrix.npz")
+    if not os.path.exists(path):
+        pytest.skip("no hmatrix.npz fixture")
+    return np.load(path)
+
+
+@pytest.mark.parametrize("prefix", ["rand_", "grid_", "via_"])
+def test_tree_and_partition_equal_mom25d(prefix):
+    """The clusters (as sets of unknowns, in mom25d's preorder numbering) and
+    the near / far cluster pairs, in mom25d's order, equal those of mom25d's
+    _tree / _partition on the same points."""
+    g = _golden()
+    pos, size, leaf = g[prefix + "pos"], g[prefix + "size"], int(g[prefix + "leaf"])
+    perm, nodes, root = H.cluster_tree(pos, size, leaf)
+    idx = [perm[c.lo:c.hi].astype(np.int64) for c in nodes]
+    assert len(nodes) == len(g[prefix + "cl_n"])
+    assert np.array_equal([i.size for i in idx], g[prefix + "cl_n"])
+    assert np.array_equal([i.sum() for i in idx], g[prefix + "cl_s1"])
+    assert np.array_equal([(i * i).sum() for i in idx], g[prefix + "cl_s2"])
+    far, near = H.partition(root, 1.0)
+    assert np.array_equal(np.array([(a.id, b.id) for a, b in near]), g[prefix + "near"])
+    assert np.array_equal(np.array([(a.id, b.id) for a, b in far]), g[prefix + "far"])
+
+
+def _plan(name, **kw):
+    lay, st, m, _ = workloads.build(G, name)
+    st = st if hasattr(st, "layers") else st.to_stackup()
+    zl = np.array([st.level_z(n) for n in m.layer_names])
+    return m, H.Plan(m, zl, morton_blocks(m), **kw)
+
+
+@pytest.mark.parametrize("name", ["tee", "via"])
+def test_plan_index_lists(name):
+    """What the kernels read is complete and consistent:
+    - every triangle pair a near entry sums (test block of t_m, source t_n)
+      is among the listed near-field pairs;
+    - every row's items (near pairs, far blocks as rows, far blocks as
+      columns) cover each column exactly once;
+    - every preconditioner block's items tile its diagonal block exactly once;
+    - the pad blocks hold every via pad triangle."""
+    m, P = _plan(name)
+    nb, nt = P.nb, P.nt
+    keys = set(P.keys.tolist())
+    perm = P.perm
+    for a0, am, b0, bn in P.near_arr:
+        rows, cols = perm[a0:a0 + am], perm[b0:b0 + bn]
+        tm = np.r_[m.tp[rows], m.tm[rows]]
+        tn = np.unique(np.r_[m.tp[cols], m.tm[cols]])
+        need = np.add.outer(np.unique(P.blk_of[tm]) * nt, tn).ravel()
+        assert all(int(k) in keys for k in need)
+    for k in range(len(P.leaves)):
+        lo, hi = P.leaf_lo[k], P.leaf_lo[k + 1]
+        cnt = np.zeros(nb, int)
+        for t, i, off, _ in P.ent[P.ent_off[k]:P.ent_off[k + 1]]:
+            if t == 0:
+                a0, am, b0, bn = P.near_arr[i]
+                assert a0 == lo and am == hi - lo
+                cnt[b0:b0 + bn] += 1
+            else:
+                r0, mm, c0, nn = P.far_arr[i]
+                if t == 1:
+                    assert r0 + off == lo and off + (hi - lo) <= mm
+                    cnt[c0:c0 + nn] += 1
+                else:
+                    assert c0 + off == lo and off + (hi - lo) <= nn
+                    cnt[r0:r0 + mm] += 1
+        assert np.all(cnt == 1), (k, np.unique(cnt))
+    for k, (p0, s) in enumerate(P.pc):
+        if p0 >= nb:  # the via block
+            assert s == P.nv and P.pc_items[P.pc_off[k]:P.pc_off[k + 1]].tolist() == [[2, 0]]
+            continue
+        cnt = np.zeros((s, s), int)
+        for t, i in P.pc_items[P.pc_off[k]:P.pc_off[k + 1]]:
+            if t == 0:
+                a0, am, b0, bn = P.near_arr[i]
+                cnt[a0 - p0:a0 - p0 + am, b0 - p0:b0 - p0 + bn] += 1
+            else:
+                r0, mm, c0, nn = P.far_arr[i]
+                cnt[r0 - p0:r0 - p0 + mm, c0 - p0:c0 - p0 + nn] += 1
+                cnt[c0 - p0:c0 - p0 + nn, r0 - p0:r0 - p0 + mm] += 1
+        assert np.all(cnt == 1)
+    assert np.array_equal(np.sort(np.concatenate([P.pc[:, 0], [P.n]])[1:] - np.sort(P.pc[:, 0])), np.sort(P.pc[:, 1]))
+    if P.nv:
+        pads = np.unique(np.concatenate([g[e] for g in m.via_segments for e in ("top_tris", "bottom_tris")
+                                         if g[e] is not None]))
+        assert set(P.blk_of[pads].tolist()) <= set(P.pblk.tolist())
+
+
+def test_plan_rules_match_mesh():
+    """The far-field rule data: the 3-point points of both halves average to
+    the triangle centroids, and the weights w cV of a basis' two halves sum
+    to zero (the divergence integrates to zero over the basis)."""
+    m, P = _plan("tee")
+    r = P.rules
+    perm = P.perm
+    pts = r[:, :12].reshape(-1, 2, 3, 2).mean(2)
+    cen = np.stack([m.centroid[m.tp[perm]], m.centroid[m.tm[perm]]], 1)
+    assert np.allclose(pts, cen, rtol=0, atol=1e-15)
+    assert np.allclose(r[:, 24:30].sum(1), 0, atol=1e-12 * np.abs(r[:, 24:30]).max())
+    assert np.allclose(r[:, 38:40].sum(1), 0, atol=1e-12 * np.abs(r[:, 38:40]).max())
