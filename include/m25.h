@@ -391,9 +391,10 @@ int m25_deembed_debug(m25_ctx* ctx, m25_ports* ports, double* phi, double* q, do
  * 1 far block whose rows hold the leaf, 2 far block whose columns hold it;
  * id; the leaf's offset inside the block's rows / columns; 0); keys: the
  * near field's (test block x nt + source triangle) pairs, sorted; pblk: the
- * test blocks holding via pad triangles; pc: preconditioner blocks (first,
- * size <= 1024) with their items (CSR pc_off; type 0 near pair, 1 far block,
- * 2 the via block; id). rules: per basis 40 values of the far-field rules
+ * test blocks holding via pad triangles; pc: preconditioner blocks (first
+ * tree position, RWG unknowns) with their items (CSR pc_off; type 0 near
+ * pair, 1 far block; id) and their via unknowns (CSR pc_via_off; at most
+ * 1024 unknowns per block with its vias). rules: per basis 40 values of the far-field rules
  * (3-point points, w cA (r - a), w cV; centroids, A cA (c - a), A cV). */
 typedef struct m25_hmat m25_hmat;
 typedef struct {
@@ -418,6 +419,8 @@ typedef struct {
   const int32_t* pc;          /* (npc, 2) */
   const int64_t* pc_off;      /* (npc + 1) */
   const int32_t* pc_items;    /* (pc_off[npc], 2) */
+  const int64_t* pc_via_off;  /* (npc + 1) */
+  const int32_t* pc_via;      /* the via unknowns of each block (CSR pc_via_off) */
   double tol;                 /* ACA tolerance (1e-4) */
   int32_t kcap;               /* most ACA terms stored per block */
 } m25_hmat_desc;

@@ -11,15 +11,19 @@
 //                rule on entries of the 3-point (or centroid) rule
 //                (far_entry, hmatrix.py:322-353); far_dense_kernel for the
 //                blocks kept as they are (side <= 64, or not low rank);
-//   matvec       (far_t_kernel, rows_kernel, via_out_kernel): per leaf of
-//                rows, one warp per row sums its near blocks, its far blocks
-//                as rows or as columns, and its via columns; every output
-//                entry has one writer (deterministic, no atomics);
-//   precondition (diag_kernel, plu_kernel, psolve_kernel): block Jacobi over
-//                clusters of <= 256 unknowns and the via block, LU with
-//                partial pivoting in complex64;
-//   GMRES        restarted, right-preconditioned, classical Gram-Schmidt
-//                applied twice, Givens rotations on the host.
+//   matvec       (far_t_kernel, rows_kernel, via_out_kernel): one warp per
+//                low-rank term projects x, then one warp per row sums its
+//                leaf's near blocks, far blocks as rows or as columns, and
+//                its via columns; every output entry has one writer
+//                (deterministic, no atomics);
+//   precondition (diag_kernel, ginv_kernel, psolve_kernel): block Jacobi
+//                over clusters of <= 512 unknowns, each with the vias whose
+//                pads it holds; the blocks scaled to a unit diagonal and
+//                inverted in fp64 (Gauss-Jordan, partial pivoting), applied
+//                as one batched GEMV;
+//   GMRES        restarted, flexible (right-preconditioned, keeping each
+//                M^-1 v_j), classical Gram-Schmidt applied twice, Givens
+//                rotations on the host.
 // Vectors inside are in tree order: RWG unknowns perm[0..nb), then vias.
 #include <algorithm>
 #include <cmath>
@@ -52,15 +56,16 @@ struct m25_hmat {
   // device: structure
   int32_t *perm = nullptr, *lev = nullptr, *leaf_lo = nullptr, *near = nullptr, *ent = nullptr;
   int64_t *near_off = nullptr, *ent_off = nullptr, *keys = nullptr;
-  int32_t *pblk = nullptr, *pc = nullptr, *pc_items = nullptr;
-  int64_t *pc_off = nullptr, *pc_doff = nullptr;
+  int32_t *pblk = nullptr, *pc = nullptr, *pc_items = nullptr, *pc_via = nullptr, *row_leaf = nullptr;
+  int2* terms = nullptr;  // (block, term) of every low-rank term
+  int nterm = 0;
+  int64_t *pc_off = nullptr, *pc_doff = nullptr, *pc_via_off = nullptr;
   double* rules = nullptr;
   FarB* fb = nullptr;  // (nfar) device
   std::vector<FarB> fb_h;
   // device: values
   m25::zd *Zn = nullptr, *pool = nullptr, *tpool = nullptr, *ZxbT = nullptr, *Zxx = nullptr;
-  m25::zf* D = nullptr;       // preconditioner blocks (LU in place)
-  int32_t* piv = nullptr;
+  m25::zf* D = nullptr;       // preconditioner blocks (their inverses, in place)
   uint8_t* flags = nullptr;   // ACA's used rows / columns
   int64_t near_entries = 0, uv_entries = 0, dense_entries = 0, t_entries = 0, flag_bytes = 0, d_entries = 0;
   int32_t *aca_ids = nullptr, *rank = nullptr, *status = nullptr, *dense_ids = nullptr;
@@ -69,7 +74,7 @@ struct m25_hmat {
   size_t dense_bytes = 0;
   bool assembled = false;
   // GMRES workspace
-  m25::zd *Vb = nullptr, *w = nullptr, *xv = nullptr, *zv = nullptr, *bv = nullptr, *hv = nullptr;
+  m25::zd *Vb = nullptr, *Zb = nullptr, *w = nullptr, *xv = nullptr, *zv = nullptr, *bv = nullptr, *hv = nullptr;
   double* nrm = nullptr;
   int restart_cap = 0;
   std::vector<void*> allocs;       // structure (freed on destroy)
@@ -393,29 +398,31 @@ __global__ void __launch_bounds__(256) aca_kernel(Tabs t, const double* __restri
 }
 
 // ------------------------------------------------------------------ matvec
-// per low-rank far block: V^T x[C] and U^T x[R], one warp per term
-__global__ void far_t_kernel(const FarB* __restrict__ fb, const zd* __restrict__ pool, const zd* __restrict__ x,
-                             zd* __restrict__ tpool) {
-  const FarB F = fb[blockIdx.x];
-  if (F.kind != 0) return;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const zd* U = pool + F.uv;
-  const zd* V = U + (int64_t)F.kcap * F.m;
-  for (int l = wid; l < F.rank; l += nw) {
-    zd d1, d2;
-    for (int j = lane; j < F.n; j += 32) d1 += V[(int64_t)l * F.n + j] * x[F.c0 + j];
-    for (int r = lane; r < F.m; r += 32) d2 += U[(int64_t)l * F.m + r] * x[F.r0 + r];
-    d1 = warp_sum(d1);
-    d2 = warp_sum(d2);
-    if (lane == 0) {
-      tpool[F.t + l] = d1;
-      tpool[F.t + F.kcap + l] = d2;
-    }
+// per term l of a low-rank far block: V_l^T x[C] and U_l^T x[R], one warp per (block, term)
+__global__ void far_t_kernel(const int2* __restrict__ terms, int nterm, const FarB* __restrict__ fb,
+                             const zd* __restrict__ pool, const zd* __restrict__ x, zd* __restrict__ tpool) {
+  const int lane = threadIdx.x & 31;
+  const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (q >= nterm) return;
+  const int2 bt = terms[q];
+  const FarB F = fb[bt.x];
+  const int l = bt.y;
+  const zd* U = pool + F.uv + (int64_t)l * F.m;
+  const zd* V = pool + F.uv + (int64_t)F.kcap * F.m + (int64_t)l * F.n;
+  zd d1, d2;
+  for (int j = lane; j < F.n; j += 32) d1 += V[j] * x[F.c0 + j];
+  for (int r = lane; r < F.m; r += 32) d2 += U[r] * x[F.r0 + r];
+  d1 = warp_sum(d1);
+  d2 = warp_sum(d2);
+  if (lane == 0) {
+    tpool[F.t + l] = d1;
+    tpool[F.t + F.kcap + l] = d2;
   }
 }
 
-// y (tree order, RWG rows) for one leaf per CTA, one warp per row
-__global__ void __launch_bounds__(256) rows_kernel(const int32_t* __restrict__ leaf_lo,
+// y (tree order, RWG rows), one warp per row: the items of the row's leaf
+__global__ void __launch_bounds__(256) rows_kernel(const int32_t* __restrict__ row_leaf,
+                                                   const int32_t* __restrict__ leaf_lo,
                                                    const int64_t* __restrict__ ent_off,
                                                    const int32_t* __restrict__ ent, const int32_t* __restrict__ near,
                                                    const int64_t* __restrict__ noff, const zd* __restrict__ Zn,
@@ -423,44 +430,44 @@ __global__ void __launch_bounds__(256) rows_kernel(const int32_t* __restrict__ l
                                                    const zd* __restrict__ dpool, const zd* __restrict__ tpool,
                                                    const zd* __restrict__ ZxbT, int nb, int nv,
                                                    const zd* __restrict__ x, zd* __restrict__ y) {
-  const int leaf = blockIdx.x;
-  const int lo = leaf_lo[leaf], hi = leaf_lo[leaf + 1];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= nb) return;
+  const int leaf = row_leaf[r];
+  const int lo = leaf_lo[leaf];
   const int64_t e0 = ent_off[leaf], e1 = ent_off[leaf + 1];
-  for (int r = lo + wid; r < hi; r += nw) {
-    zd acc;
-    for (int64_t e = e0; e < e1; ++e) {
-      const int type = ent[4 * e], id = ent[4 * e + 1], off = ent[4 * e + 2];
-      if (type == 0) {
-        const int a0 = near[4 * id], b0 = near[4 * id + 2], bn = near[4 * id + 3];
-        const zd* row = Zn + noff[id] + (int64_t)(r - a0) * bn;
-        for (int j = lane; j < bn; j += 32) acc += row[j] * x[b0 + j];
-        continue;
-      }
-      const FarB F = fb[id];
-      const int q = off + (r - lo);  // row of the block (type 1) or of its transpose (type 2)
-      if (F.kind == 0) {
-        const zd* U = pool + F.uv;
-        const zd* V = U + (int64_t)F.kcap * F.m;
-        if (type == 1)
-          for (int l = lane; l < F.rank; l += 32) acc += U[(int64_t)l * F.m + q] * tpool[F.t + l];
-        else
-          for (int l = lane; l < F.rank; l += 32) acc += V[(int64_t)l * F.n + q] * tpool[F.t + F.kcap + l];
+  zd acc;
+  for (int64_t e = e0; e < e1; ++e) {
+    const int type = ent[4 * e], id = ent[4 * e + 1], off = ent[4 * e + 2];
+    if (type == 0) {
+      const int a0 = near[4 * id], b0 = near[4 * id + 2], bn = near[4 * id + 3];
+      const zd* row = Zn + noff[id] + (int64_t)(r - a0) * bn;
+      for (int j = lane; j < bn; j += 32) acc += row[j] * x[b0 + j];
+      continue;
+    }
+    const FarB F = fb[id];
+    const int q = off + (r - lo);  // row of the block (type 1) or of its transpose (type 2)
+    if (F.kind == 0) {
+      const zd* U = pool + F.uv;
+      const zd* V = U + (int64_t)F.kcap * F.m;
+      if (type == 1)
+        for (int l = lane; l < F.rank; l += 32) acc += U[(int64_t)l * F.m + q] * tpool[F.t + l];
+      else
+        for (int l = lane; l < F.rank; l += 32) acc += V[(int64_t)l * F.n + q] * tpool[F.t + F.kcap + l];
+    } else {
+      const zd* B = dpool + F.dense;
+      if (type == 1) {
+        const zd* row = B + (int64_t)q * F.n;
+        for (int j = lane; j < F.n; j += 32) acc += row[j] * x[F.c0 + j];
       } else {
-        const zd* B = dpool + F.dense;
-        if (type == 1) {
-          const zd* row = B + (int64_t)q * F.n;
-          for (int j = lane; j < F.n; j += 32) acc += row[j] * x[F.c0 + j];
-        } else {
-          const zd* row = B + (int64_t)F.m * F.n + (int64_t)q * F.m;
-          for (int j = lane; j < F.m; j += 32) acc += row[j] * x[F.r0 + j];
-        }
+        const zd* row = B + (int64_t)F.m * F.n + (int64_t)q * F.m;
+        for (int j = lane; j < F.m; j += 32) acc += row[j] * x[F.r0 + j];
       }
     }
-    for (int v = lane; v < nv; v += 32) acc += ZxbT[(int64_t)r * nv + v] * x[nb + v];
-    acc = warp_sum(acc);
-    if (lane == 0) y[r] = acc;
   }
+  for (int v = lane; v < nv; v += 32) acc += ZxbT[(int64_t)r * nv + v] * x[nb + v];
+  acc = warp_sum(acc);
+  if (lane == 0) y[r] = acc;
 }
 
 // y of the via unknowns: Zvb x_b + Zvv x_v, one CTA per via row
@@ -488,30 +495,36 @@ __global__ void perm_out_kernel(int nb, int n, const int32_t* __restrict__ perm,
 }
 
 // ---------------------------------------------------------- preconditioner
-// diagonal block k (complex64, row-major s x s) of the compressed operator:
-// its near pairs, its far blocks (both orientations) or the via block
+// Block k holds the RWG unknowns [p0, p0 + s) of a tree cluster, then its nv_k
+// via unknowns (local index s + a): size S = s + nv_k.
+__device__ __forceinline__ int pc_global(int i, int p0, int s, int nb, const int32_t* __restrict__ via, int64_t v0) {
+  return i < s ? p0 + i : nb + via[v0 + (i - s)];
+}
+
+// diagonal block k (row-major S x S) of the compressed operator: its near
+// pairs, its far blocks (both orientations), its via rows / columns
 __global__ void diag_kernel(const int32_t* __restrict__ pc, const int64_t* __restrict__ pc_off,
-                            const int32_t* __restrict__ items, const int64_t* __restrict__ doff,
+                            const int32_t* __restrict__ items, const int64_t* __restrict__ via_off,
+                            const int32_t* __restrict__ via, const int64_t* __restrict__ doff, int nv,
                             const int32_t* __restrict__ near, const int64_t* __restrict__ noff,
                             const zd* __restrict__ Zn, const FarB* __restrict__ fb, const zd* __restrict__ pool,
-                            const zd* __restrict__ dpool, const zd* __restrict__ Zxx, zf* __restrict__ D) {
+                            const zd* __restrict__ dpool, const zd* __restrict__ ZxbT, const zd* __restrict__ Zxx,
+                            zf* __restrict__ D) {
   const int k = blockIdx.x;
   const int p0 = pc[2 * k], s = pc[2 * k + 1];
+  const int64_t v0 = via_off[k];
+  const int nvk = (int)(via_off[k + 1] - v0), S = s + nvk;
   zf* Dk = D + doff[k];
-  for (int64_t e = threadIdx.x; e < (int64_t)s * s; e += blockDim.x) Dk[e] = zf(0.f, 0.f);
+  for (int64_t e = threadIdx.x; e < (int64_t)S * S; e += blockDim.x) Dk[e] = zf(0.f, 0.f);
   __syncthreads();
   for (int64_t it = pc_off[k]; it < pc_off[k + 1]; ++it) {
     const int type = items[2 * it], id = items[2 * it + 1];
-    if (type == 2) {  // the via block
-      for (int64_t e = threadIdx.x; e < (int64_t)s * s; e += blockDim.x) Dk[e] = zf(Zxx[e]);
-      continue;
-    }
     if (type == 0) {
       const int a0 = near[4 * id], am = near[4 * id + 1], b0 = near[4 * id + 2], bn = near[4 * id + 3];
       const zd* blk = Zn + noff[id];
       for (int e = threadIdx.x; e < am * bn; e += blockDim.x) {
         const int i = e / bn, j = e - i * bn;
-        Dk[(int64_t)(a0 - p0 + i) * s + (b0 - p0 + j)] = zf(blk[e]);
+        Dk[(int64_t)(a0 - p0 + i) * S + (b0 - p0 + j)] = zf(blk[e]);
       }
       continue;
     }
@@ -526,95 +539,127 @@ __global__ void diag_kernel(const int32_t* __restrict__ pc, const int64_t* __res
       } else {
         z = dpool[F.dense + e];
       }
-      const zf zz(z);
-      Dk[(int64_t)(F.r0 - p0 + i) * s + (F.c0 - p0 + j)] = zz;
-      Dk[(int64_t)(F.c0 - p0 + j) * s + (F.r0 - p0 + i)] = zz;
+      Dk[(int64_t)(F.r0 - p0 + i) * S + (F.c0 - p0 + j)] = zf(z);
+      Dk[(int64_t)(F.c0 - p0 + j) * S + (F.r0 - p0 + i)] = zf(z);
     }
+  }
+  for (int e = threadIdx.x; e < s * nvk; e += blockDim.x) {  // RWG x via (Z is symmetric)
+    const int i = e / nvk, a = e - i * nvk;
+    const zf z(ZxbT[(int64_t)(p0 + i) * nv + via[v0 + a]]);
+    Dk[(int64_t)i * S + s + a] = z;
+    Dk[(int64_t)(s + a) * S + i] = z;
+  }
+  for (int e = threadIdx.x; e < nvk * nvk; e += blockDim.x) {  // via x via
+    const int a = e / nvk, b = e - a * nvk;
+    Dk[(int64_t)(s + a) * S + s + b] = zf(Zxx[(int64_t)via[v0 + a] * nv + via[v0 + b]]);
   }
 }
 
+// In-place inversion of each diagonal block (one CTA per block, complex64:
+// the flexible GMRES below keeps M^-1 v_j, so the preconditioner need not be
+// exact). The block is first scaled symmetrically to a unit diagonal,
+// D' = W D W with W = diag(|D_ii|^-1/2) (the via rows and the RWG rows
+// differ by many orders of magnitude), then inverted by Gauss-Jordan
+// elimination with partial pivoting (a zero pivot is replaced by 1: the
+// block then preconditions less), the row interchanges undone on the
+// columns, and D^-1 = W D'^-1 W stored in place.
 __device__ __forceinline__ float fabs1(zf a) { return fabsf(a.re) + fabsf(a.im); }
 
-// LU with partial pivoting of each diagonal block (one CTA per block, in
-// place); a zero pivot is replaced by 1 (the block then preconditions less)
-__global__ void __launch_bounds__(256) plu_kernel(const int32_t* __restrict__ pc, const int64_t* __restrict__ doff,
-                                                  zf* __restrict__ D, int32_t* __restrict__ piv) {
+__global__ void __launch_bounds__(256) ginv_kernel(const int32_t* __restrict__ pc, const int64_t* __restrict__ via_off,
+                                                   const int64_t* __restrict__ doff, zf* __restrict__ D) {
   __shared__ double sv[32];
   __shared__ int si[32];
+  __shared__ int pv[1024];
+  __shared__ float w[1024];
+  __shared__ zf fcol[1024];
   const int k = blockIdx.x;
-  const int p0 = pc[2 * k], s = pc[2 * k + 1];
+  const int S = pc[2 * k + 1] + (int)(via_off[k + 1] - via_off[k]);
   zf* A = D + doff[k];
-  int32_t* pv = piv + p0;
-  for (int c = 0; c < s; ++c) {
+  for (int i = threadIdx.x; i < S; i += blockDim.x) {
+    const zf a = A[(int64_t)i * S + i];
+    const float m = hypotf(a.re, a.im);
+    w[i] = m > 0.f ? rsqrtf(m) : 1.f;
+  }
+  __syncthreads();
+  for (int64_t e = threadIdx.x; e < (int64_t)S * S; e += blockDim.x) {
+    const int r = (int)(e / S), j = (int)(e - (int64_t)r * S);
+    A[e] = A[e] * (w[r] * w[j]);
+  }
+  __syncthreads();
+  for (int c = 0; c < S; ++c) {
     double best = -1.0;
     int bi = 0x7fffffff;
-    for (int r = c + threadIdx.x; r < s; r += blockDim.x) {
-      const double a = fabs1(A[(int64_t)r * s + c]);
+    for (int r = c + threadIdx.x; r < S; r += blockDim.x) {
+      const double a = fabs1(A[(int64_t)r * S + c]);
       if (a > best) {
         best = a;
         bi = r;
       }
     }
     block_argmax(best, bi, sv, si);
-    if (bi < c || bi >= s) {  // no finite candidate: no swap, the pivot replaced below
+    if (bi < c || bi >= S) {
       bi = c;
       best = 0.0;
     }
     if (threadIdx.x == 0) pv[c] = bi;
     if (bi != c)
-      for (int j = threadIdx.x; j < s; j += blockDim.x) {
-        const zf t0 = A[(int64_t)c * s + j];
-        A[(int64_t)c * s + j] = A[(int64_t)bi * s + j];
-        A[(int64_t)bi * s + j] = t0;
+      for (int j = threadIdx.x; j < S; j += blockDim.x) {
+        const zf t0 = A[(int64_t)c * S + j];
+        A[(int64_t)c * S + j] = A[(int64_t)bi * S + j];
+        A[(int64_t)bi * S + j] = t0;
       }
     __syncthreads();
-    if (threadIdx.x == 0 && !(best > 0.0)) A[(int64_t)c * s + c] = zf(1.f, 0.f);
+    const zf d = best > 0.0 ? zf(1.f, 0.f) / A[(int64_t)c * S + c] : zf(1.f, 0.f);
     __syncthreads();
-    const zf inv = zf(1.f, 0.f) / A[(int64_t)c * s + c];
-    for (int r = c + 1 + threadIdx.x; r < s; r += blockDim.x) A[(int64_t)r * s + c] = A[(int64_t)r * s + c] * inv;
+    for (int j = threadIdx.x; j < S; j += blockDim.x)
+      A[(int64_t)c * S + j] = j == c ? d : A[(int64_t)c * S + j] * d;
+    for (int r = threadIdx.x; r < S; r += blockDim.x) fcol[r] = A[(int64_t)r * S + c];
     __syncthreads();
-    const int w = s - c - 1;
-    for (int64_t e = threadIdx.x; e < (int64_t)w * w; e += blockDim.x) {
-      const int r = c + 1 + (int)(e / w), j = c + 1 + (int)(e - (e / w) * w);
-      A[(int64_t)r * s + j] -= A[(int64_t)r * s + c] * A[(int64_t)c * s + j];
+    for (int64_t e = threadIdx.x; e < (int64_t)S * S; e += blockDim.x) {
+      const int r = (int)(e / S), j = (int)(e - (int64_t)r * S);
+      if (r == c) continue;
+      const zf f = fcol[r];
+      A[e] = j == c ? -(f * d) : A[e] - f * A[(int64_t)c * S + j];
     }
     __syncthreads();
+  }
+  for (int c = S - 1; c >= 0; --c) {
+    const int p = pv[c];
+    if (p != c)
+      for (int r = threadIdx.x; r < S; r += blockDim.x) {
+        const zf t0 = A[(int64_t)r * S + c];
+        A[(int64_t)r * S + c] = A[(int64_t)r * S + p];
+        A[(int64_t)r * S + p] = t0;
+      }
+    __syncthreads();
+  }
+  for (int64_t e = threadIdx.x; e < (int64_t)S * S; e += blockDim.x) {
+    const int r = (int)(e / S), j = (int)(e - (int64_t)r * S);
+    A[e] = A[e] * (w[r] * w[j]);
   }
 }
 
-// out[p0 .. p0+s) = D_k^-1 in[p0 .. p0+s) (fp64 vectors, complex64 factors)
-__global__ void __launch_bounds__(256) psolve_kernel(const int32_t* __restrict__ pc, const int64_t* __restrict__ doff,
-                                                     const zf* __restrict__ D, const int32_t* __restrict__ piv,
-                                                     const zd* __restrict__ in, zd* __restrict__ out) {
-  __shared__ zf z[1024];
+// out = D_k^-1 in on block k's unknowns (complex64 inverse, fp32 sums), one warp per row
+__global__ void __launch_bounds__(256) psolve_kernel(const int32_t* __restrict__ pc, const int64_t* __restrict__ via_off,
+                                                     const int32_t* __restrict__ via, const int64_t* __restrict__ doff,
+                                                     int nb, const zf* __restrict__ D, const zd* __restrict__ in,
+                                                     zd* __restrict__ out) {
+  __shared__ zf xs[1024];
   const int k = blockIdx.x;
   const int p0 = pc[2 * k], s = pc[2 * k + 1];
+  const int64_t v0 = via_off[k];
+  const int S = s + (int)(via_off[k + 1] - v0);
   const zf* A = D + doff[k];
-  for (int i = threadIdx.x; i < s; i += blockDim.x) z[i] = zf(in[p0 + i]);
+  for (int i = threadIdx.x; i < S; i += blockDim.x) xs[i] = zf(in[pc_global(i, p0, s, nb, via, v0)]);
   __syncthreads();
-  if (threadIdx.x == 0)
-    for (int c = 0; c < s; ++c) {
-      const int p = piv[p0 + c];
-      if (p != c) {
-        const zf t0 = z[c];
-        z[c] = z[p];
-        z[p] = t0;
-      }
-    }
-  __syncthreads();
-  for (int c = 0; c < s; ++c) {  // L (unit diagonal)
-    const zf zc = z[c];
-    for (int r = c + 1 + threadIdx.x; r < s; r += blockDim.x) z[r] -= A[(int64_t)r * s + c] * zc;
-    __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int r = wid; r < S; r += nw) {
+    zf acc(0.f, 0.f);
+    const zf* row = A + (int64_t)r * S;
+    for (int j = lane; j < S; j += 32) acc += row[j] * xs[j];
+    const zd a = warp_sum(zd(double(acc.re), double(acc.im)));
+    if (lane == 0) out[pc_global(r, p0, s, nb, via, v0)] = a;
   }
-  for (int c = s - 1; c >= 0; --c) {  // U
-    if (threadIdx.x == 0) z[c] = z[c] / A[(int64_t)c * s + c];
-    __syncthreads();
-    const zf zc = z[c];
-    for (int r = threadIdx.x; r < c; r += blockDim.x) z[r] -= A[(int64_t)r * s + c] * zc;
-    __syncthreads();
-  }
-  for (int i = threadIdx.x; i < s; i += blockDim.x) out[p0 + i] = zd(double(z[i].re), double(z[i].im));
 }
 
 // ------------------------------------------------------------------ GMRES
@@ -657,11 +702,6 @@ __global__ void sub_kernel(zd* __restrict__ dst, const zd* __restrict__ a, const
   if (i < n) dst[i] = a[i] - b[i];
 }
 
-__global__ void add_kernel(zd* __restrict__ x, const zd* __restrict__ d, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) x[i] += d[i];
-}
-
 template <class T>
 int dalloc(std::vector<void*>& list, T** p, size_t count) {
   return alloc(list, reinterpret_cast<void**>(p), sizeof(T) * std::max<size_t>(count, 1));
@@ -687,8 +727,8 @@ Tabs make_tabs(m25_greens* gr) {
 // y = A x, tree order, device vectors
 int apply(m25_hmat* h, const zd* x, zd* y) {
   cudaStream_t st = h->ctx->stream;
-  if (h->nfar) far_t_kernel<<<h->nfar, 256, 0, st>>>(h->fb, h->pool, x, h->tpool);
-  rows_kernel<<<h->nleaf, 256, 0, st>>>(h->leaf_lo, h->ent_off, h->ent, h->near, h->near_off, h->Zn, h->fb, h->pool,
+  if (h->nterm) far_t_kernel<<<(h->nterm + 7) / 8, 256, 0, st>>>(h->terms, h->nterm, h->fb, h->pool, x, h->tpool);
+  rows_kernel<<<(h->nb + 7) / 8, 256, 0, st>>>(h->row_leaf, h->leaf_lo, h->ent_off, h->ent, h->near, h->near_off, h->Zn, h->fb, h->pool,
                                         h->dense_pool, h->tpool, h->ZxbT, h->nb, h->nv, x, y);
   if (h->nv) via_out_kernel<<<h->nv, 256, 0, st>>>(h->nb, h->nv, h->ZxbT, h->Zxx, x, y);
   M25_CHECK_LAUNCH();
@@ -696,7 +736,8 @@ int apply(m25_hmat* h, const zd* x, zd* y) {
 }
 
 int precond(m25_hmat* h, const zd* in, zd* out) {
-  psolve_kernel<<<h->npc, 256, 0, h->ctx->stream>>>(h->pc, h->pc_doff, h->D, h->piv, in, out);
+  psolve_kernel<<<h->npc, 256, 0, h->ctx->stream>>>(h->pc, h->pc_via_off, h->pc_via, h->pc_doff, h->nb, h->D,
+                                                    in, out);
   M25_CHECK_LAUNCH();
   return M25_OK;
 }
@@ -789,11 +830,18 @@ extern "C" int m25_hmat_create(m25_ctx* ctx, m25_geom* geom, const m25_hmat_desc
   // preconditioner blocks
   h->pc_h.assign(d->pc, d->pc + 2 * (size_t)d->npc);
   std::vector<int64_t> doff(d->npc + 1, 0);
+  if (d->pc_via_off[0] != 0 || d->pc_via_off[d->npc] != d->nv)
+    return fail((set_error("m25_hmat_create: the via unknowns are not split over the blocks"), M25_ERR_VALUE));
   for (int k = 0; k < d->npc; ++k) {
     const int p0 = h->pc_h[2 * k], s = h->pc_h[2 * k + 1];
-    if (s <= 0 || s > 1024 || p0 < 0 || p0 + s > h->n) return fail((set_error("m25_hmat_create: bad preconditioner block"), M25_ERR_VALUE));
-    doff[k + 1] = doff[k] + (int64_t)s * s;
+    const int64_t nvk = d->pc_via_off[k + 1] - d->pc_via_off[k];
+    if (s <= 0 || nvk < 0 || s + nvk > 1024 || p0 < 0 || p0 + s > h->nb)
+      return fail((set_error("m25_hmat_create: bad preconditioner block"), M25_ERR_VALUE));
+    doff[k + 1] = doff[k] + (s + nvk) * (s + nvk);
   }
+  for (int v = 0; v < d->nv; ++v)
+    if (d->pc_via[v] < 0 || d->pc_via[v] >= d->nv)
+      return fail((set_error("m25_hmat_create: bad via index"), M25_ERR_VALUE));
   h->d_entries = doff[d->npc];
   const int64_t nent = d->ent_off[d->nleaf];
   const int64_t nitems = d->pc_off[d->npc];
@@ -805,6 +853,7 @@ extern "C" int m25_hmat_create(m25_ctx* ctx, m25_geom* geom, const m25_hmat_desc
   TRY(dalloc(h->allocs, &h->rules, (size_t)d->nb * kRule));
   TRY(dalloc(h->allocs, &h->lev, d->nb));
   TRY(dalloc(h->allocs, &h->leaf_lo, d->nleaf + 1));
+  TRY(dalloc(h->allocs, &h->row_leaf, d->nb));
   TRY(dalloc(h->allocs, &h->near, 4 * (size_t)d->nnear));
   TRY(dalloc(h->allocs, &h->near_off, d->nnear + 1));
   TRY(dalloc(h->allocs, &h->ent_off, d->nleaf + 1));
@@ -815,15 +864,17 @@ extern "C" int m25_hmat_create(m25_ctx* ctx, m25_geom* geom, const m25_hmat_desc
   TRY(dalloc(h->allocs, &h->pc_off, d->npc + 1));
   TRY(dalloc(h->allocs, &h->pc_items, 2 * (size_t)nitems));
   TRY(dalloc(h->allocs, &h->pc_doff, d->npc + 1));
+  TRY(dalloc(h->allocs, &h->pc_via_off, d->npc + 1));
+  TRY(dalloc(h->allocs, &h->pc_via, std::max(d->nv, 1)));
   TRY(dalloc(h->allocs, &h->fb, d->nfar));
   TRY(dalloc(h->allocs, &h->Zn, h->near_entries));
   TRY(dalloc(h->allocs, &h->pool, uv));
   TRY(dalloc(h->allocs, &h->tpool, tt));
+  TRY(dalloc(h->allocs, &h->terms, std::max<int64_t>(tt / 2, 1)));
   TRY(dalloc(h->allocs, &h->flags, fl));
   TRY(dalloc(h->allocs, &h->ZxbT, (size_t)d->nb * std::max(d->nv, 1)));
   TRY(dalloc(h->allocs, &h->Zxx, (size_t)std::max(d->nv, 1) * std::max(d->nv, 1)));
   TRY(dalloc(h->allocs, &h->D, h->d_entries));
-  TRY(dalloc(h->allocs, &h->piv, h->n));
   TRY(dalloc(h->allocs, &h->aca_ids, std::max(h->naca, 1)));
   TRY(dalloc(h->allocs, &h->rank, std::max(h->naca, 1)));
   TRY(dalloc(h->allocs, &h->status, std::max(h->naca, 1)));
@@ -833,12 +884,18 @@ extern "C" int m25_hmat_create(m25_ctx* ctx, m25_geom* geom, const m25_hmat_desc
     if (bytes) M25_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
     return M25_OK;
   };
+  std::vector<int32_t> row_leaf(d->nb);
+  for (int k = 0; k < d->nleaf; ++k) {
+    if (d->leaf_lo[k + 1] <= d->leaf_lo[k]) return fail((set_error("m25_hmat_create: empty leaf"), M25_ERR_VALUE));
+    for (int r = d->leaf_lo[k]; r < d->leaf_lo[k + 1] && r < d->nb; ++r) row_leaf[r] = k;
+  }
   std::vector<int32_t> aca;
   for (int f = 0; f < d->nfar; ++f)
     if (h->fb_h[f].kind == 0) aca.push_back(f);
   if ((rc = up(h->perm, d->perm, sizeof(int32_t) * d->nb)) || (rc = up(h->rules, d->rules, sizeof(double) * d->nb * kRule)) ||
       (rc = up(h->lev, d->lev, sizeof(int32_t) * d->nb)) ||
       (rc = up(h->leaf_lo, d->leaf_lo, sizeof(int32_t) * (d->nleaf + 1))) ||
+      (rc = up(h->row_leaf, row_leaf.data(), sizeof(int32_t) * d->nb)) ||
       (rc = up(h->near, d->near, sizeof(int32_t) * 4 * d->nnear)) ||
       (rc = up(h->near_off, h->near_off_h.data(), sizeof(int64_t) * (d->nnear + 1))) ||
       (rc = up(h->ent_off, d->ent_off, sizeof(int64_t) * (d->nleaf + 1))) ||
@@ -849,6 +906,8 @@ extern "C" int m25_hmat_create(m25_ctx* ctx, m25_geom* geom, const m25_hmat_desc
       (rc = up(h->pc_off, d->pc_off, sizeof(int64_t) * (d->npc + 1))) ||
       (rc = up(h->pc_items, d->pc_items, sizeof(int32_t) * 2 * nitems)) ||
       (rc = up(h->pc_doff, doff.data(), sizeof(int64_t) * (d->npc + 1))) ||
+      (rc = up(h->pc_via_off, d->pc_via_off, sizeof(int64_t) * (d->npc + 1))) ||
+      (rc = up(h->pc_via, d->pc_via, sizeof(int32_t) * d->nv)) ||
       (rc = up(h->aca_ids, aca.data(), sizeof(int32_t) * aca.size())))
     return fail(rc);
   // index checks of the lists the kernels follow
@@ -859,7 +918,7 @@ extern "C" int m25_hmat_create(m25_ctx* ctx, m25_geom* geom, const m25_hmat_desc
   }
   for (int64_t e = 0; e < nitems; ++e) {
     const int type = d->pc_items[2 * e], id = d->pc_items[2 * e + 1];
-    if (type < 0 || type > 2 || id < 0 || (type == 0 && id >= d->nnear) || (type == 1 && id >= d->nfar))
+    if (type < 0 || type > 1 || id < 0 || (type == 0 && id >= d->nnear) || (type == 1 && id >= d->nfar))
       return fail((set_error("m25_hmat_create: bad preconditioner item"), M25_ERR_VALUE));
   }
   const int64_t cells = (int64_t)geom->nblocks * geom->nt;
@@ -989,6 +1048,19 @@ extern "C" int m25_hmat_assemble(m25_hmat* h, m25_greens* gr, double zs_re, doub
       ++a;
     }
   }
+  // the low-rank terms the matvec projects on, one warp each
+  std::vector<int2> terms;
+  for (int f = 0; f < h->nfar; ++f) {
+    const FarB& F = h->fb_h[f];
+    if (F.kind == 0)
+      for (int l = 0; l < F.rank; ++l) terms.push_back(make_int2(f, l));
+  }
+  h->nterm = (int)terms.size();
+  if (h->nterm && cudaMemcpyAsync(h->terms, terms.data(), sizeof(int2) * terms.size(), cudaMemcpyHostToDevice, st) !=
+                      cudaSuccess) {
+    set_error("m25_hmat_assemble: copy failed");
+    return done(M25_ERR_CUDA);
+  }
   // storage of the blocks kept as they are (B and B^T)
   std::vector<int32_t> dense;
   int64_t doff = 0;
@@ -1008,8 +1080,8 @@ extern "C" int m25_hmat_assemble(m25_hmat* h, m25_greens* gr, double zs_re, doub
     if ((rc = dalloc(h->dense_allocs, &h->dense_pool, (size_t)doff))) return done(rc);
     h->dense_bytes = (size_t)std::max<int64_t>(doff, 1) * sizeof(zd);
   }
-  if (cudaMemcpyAsync(h->fb, h->fb_h.data(), sizeof(FarB) * std::max(h->nfar, 1), cudaMemcpyHostToDevice, st) !=
-          cudaSuccess ||
+  if ((h->nfar && cudaMemcpyAsync(h->fb, h->fb_h.data(), sizeof(FarB) * h->nfar, cudaMemcpyHostToDevice, st) !=
+                     cudaSuccess) ||
       (dense.size() && cudaMemcpyAsync(h->dense_ids, dense.data(), sizeof(int32_t) * dense.size(),
                                        cudaMemcpyHostToDevice, st) != cudaSuccess)) {
     set_error("m25_hmat_assemble: copy failed");
@@ -1018,9 +1090,10 @@ extern "C" int m25_hmat_assemble(m25_hmat* h, m25_greens* gr, double zs_re, doub
   if (!dense.empty())
     far_dense_kernel<<<(unsigned)dense.size(), 256, 0, st>>>(t, h->rules, h->lev, h->fb, h->dense_ids, h->dense_pool);
   // preconditioner: the diagonal blocks and their LU
-  diag_kernel<<<h->npc, 256, 0, st>>>(h->pc, h->pc_off, h->pc_items, h->pc_doff, h->near, h->near_off, h->Zn, h->fb,
-                                      h->pool, h->dense_pool, h->Zxx, h->D);
-  plu_kernel<<<h->npc, 256, 0, st>>>(h->pc, h->pc_doff, h->D, h->piv);
+  diag_kernel<<<h->npc, 256, 0, st>>>(h->pc, h->pc_off, h->pc_items, h->pc_via_off, h->pc_via, h->pc_doff, h->nv,
+                                      h->near, h->near_off, h->Zn, h->fb, h->pool, h->dense_pool, h->ZxbT, h->Zxx,
+                                      h->D);
+  ginv_kernel<<<h->npc, 256, 0, st>>>(h->pc, h->pc_via_off, h->pc_doff, h->D);
   if (cudaGetLastError() != cudaSuccess) {
     set_error("m25_hmat_assemble: launch failed");
     return done(M25_ERR_CUDA);
@@ -1046,11 +1119,12 @@ namespace {
 int ensure_gmres(m25_hmat* h, int restart) {
   if (h->restart_cap >= restart && h->Vb) return M25_OK;
   free_all(h->gm_allocs);
-  h->Vb = h->w = h->xv = h->zv = h->bv = h->hv = nullptr;
+  h->Vb = h->Zb = h->w = h->xv = h->zv = h->bv = h->hv = nullptr;
   h->nrm = nullptr;
   int rc;
   const size_t n = h->n;
-  if ((rc = dalloc(h->gm_allocs, &h->Vb, (size_t)(restart + 1) * n)) || (rc = dalloc(h->gm_allocs, &h->w, n)) ||
+  if ((rc = dalloc(h->gm_allocs, &h->Vb, (size_t)(restart + 1) * n)) ||
+      (rc = dalloc(h->gm_allocs, &h->Zb, (size_t)restart * n)) || (rc = dalloc(h->gm_allocs, &h->w, n)) ||
       (rc = dalloc(h->gm_allocs, &h->xv, n)) || (rc = dalloc(h->gm_allocs, &h->zv, n)) ||
       (rc = dalloc(h->gm_allocs, &h->bv, n)) || (rc = dalloc(h->gm_allocs, &h->hv, 2 * (size_t)(restart + 2))) ||
       (rc = dalloc(h->gm_allocs, &h->nrm, 4)))
@@ -1135,9 +1209,9 @@ extern "C" int m25_hmat_solve(m25_hmat* h, int32_t nrhs, const double* B, double
         gv[0] = beta;
         int j = 0;
         for (; j < restart; ++j) {
-          // w = A M^-1 v_j, orthogonalised twice against v_0 .. v_j
-          if ((rc = precond(h, h->Vb + (int64_t)j * ldv, h->zv))) return rc;
-          if ((rc = apply(h, h->zv, h->w))) return rc;
+          // z_j = M^-1 v_j (kept: flexible GMRES), w = A z_j orthogonalised twice against v_0 .. v_j
+          if ((rc = precond(h, h->Vb + (int64_t)j * ldv, h->Zb + (int64_t)j * ldv))) return rc;
+          if ((rc = apply(h, h->Zb + (int64_t)j * ldv, h->w))) return rc;
           for (int pass = 0; pass < 2; ++pass) {
             dots_kernel<<<j + 1, 256, 0, st>>>(h->Vb, ldv, n, h->w, h->hv + pass * (restart + 2));
             combine_kernel<<<g, 256, 0, st>>>(h->w, h->Vb, ldv, j + 1, n, h->hv + pass * (restart + 2), -1.0);
@@ -1177,7 +1251,7 @@ extern "C" int m25_hmat_solve(m25_hmat* h, int32_t nrhs, const double* B, double
           }
         }
         const int k = std::min(j, restart);
-        // y from the triangle, x += M^-1 (V y)
+        // y from the triangle, x += Z y
         std::vector<cplx> y(k);
         for (int r = k - 1; r >= 0; --r) {
           cplx s = gv[r];
@@ -1185,10 +1259,7 @@ extern "C" int m25_hmat_solve(m25_hmat* h, int32_t nrhs, const double* B, double
           y[r] = s / H[(size_t)r * (restart + 1) + r];
         }
         M25_CUDA(cudaMemcpyAsync(h->hv, y.data(), sizeof(zd) * k, cudaMemcpyHostToDevice, st));
-        M25_CUDA(cudaMemsetAsync(h->w, 0, sizeof(zd) * n, st));
-        combine_kernel<<<g, 256, 0, st>>>(h->w, h->Vb, ldv, k, n, h->hv, 1.0);
-        if ((rc = precond(h, h->w, h->zv))) return rc;
-        add_kernel<<<g, 256, 0, st>>>(h->xv, h->zv, n);
+        combine_kernel<<<g, 256, 0, st>>>(h->xv, h->Zb, ldv, k, n, h->hv, 1.0);
         M25_CHECK_LAUNCH();
       }
       // the true residual

@@ -25,11 +25,13 @@ Here (the host part; the device part is csrc/hmatrix.cu):
   are stored as they are. The ACA factors are not recompressed (QR + SVD,
   hmatrix.py:137-142): that would lower their rank, not their error;
 - preconditioner: block Jacobi over the largest clusters of at most
-  `prec_block` unknowns (their diagonal blocks of the compressed operator,
-  LU in complex64) and the via block, in place of mom25d's sparse LU of the
-  nearest entries (hmatrix.py:523-560); GMRES (restart 200, at most 3
-  restarts, relative residual 1e-6) is right-preconditioned, so the
-  preconditioner's precision does not enter the solution.
+  `prec_block` unknowns, each with the via unknowns whose pads it holds
+  (their diagonal blocks of the compressed operator, scaled to a unit
+  diagonal and inverted in complex64, so that applying it is one batched
+  matrix-vector product), in place of mom25d's sparse LU of the nearest
+  entries (hmatrix.py:523-560); GMRES (restart 200, at most 3 restarts,
+  relative residual 1e-6) is flexible: it keeps M^-1 v_j for every basis
+  vector, so the preconditioner's precision does not enter the solution.
 """
 
 import ctypes as C
@@ -169,7 +171,7 @@ class Plan:
     """The host side of the compressed operator (no device work): the tree,
     the partition and the index lists the device kernels follow."""
 
-    def __init__(self, mesh, zl, blocks, leaf=48, eta=1.0, prec_block=256):
+    def __init__(self, mesh, zl, blocks, leaf=48, eta=1.0, prec_block=512):
         m = mesh
         self.nb, self.nv = nb, nv = m.n_basis, len(m.via_segments)
         self.n = nb + nv
@@ -229,7 +231,7 @@ class Plan:
             tris = np.unique(np.concatenate([g[e] for g in segs for e in ("top_tris", "bottom_tris")
                                              if g[e] is not None]))
             self.pblk = np.unique(blk_of[tris]).astype(np.int32)
-        # preconditioner: the largest clusters of at most prec_block unknowns, then the via block
+        # preconditioner: the largest clusters of at most prec_block unknowns
         pcs = []
         stack = [root]
         while stack:
@@ -254,13 +256,31 @@ class Plan:
             if a.hi <= pcs[k].hi and pcs[k].lo <= b.lo and b.hi <= pcs[k].hi:
                 items[k].append((1, f))
         pc = [(c.lo, c.size) for c in pcs]
+        # each via joins the block holding the RWG unknowns of its pad triangles (the first one's)
+        pcv = [[] for _ in pcs]
         if nv:
-            pc.append((nb, nv))
-            items.append([(2, 0)])
+            ipos = np.empty(nb, np.int64)
+            ipos[perm] = np.arange(nb)
+            for v, g in enumerate(m.via_segments):
+                tris = [t for e in ("top_tris", "bottom_tris") if g[e] is not None for t in np.atleast_1d(g[e])]
+                k = len(pcs) - 1
+                for t in tris:
+                    bs = m.tri_basis[t][m.tri_basis[t] >= 0]
+                    if bs.size:
+                        k = owner(int(ipos[bs[0]]))
+                        break
+                pcv[k].append(v)
+        sizes = [s + len(v) for (_, s), v in zip(pc, pcv)]
+        if max(sizes) > 1024:
+            raise ValueError("a preconditioner block with its vias exceeds 1024 unknowns (lower prec_block)")
         self.pc = np.array(pc, np.int32).reshape(-1, 2)
         self.pc_off = np.zeros(len(pc) + 1, np.int64)
         self.pc_off[1:] = np.cumsum([len(x) for x in items])
         self.pc_items = np.array([x for it in items for x in it], np.int32).reshape(-1, 2)
+        self.pc_via_off = np.zeros(len(pc) + 1, np.int64)
+        self.pc_via_off[1:] = np.cumsum([len(v) for v in pcv])
+        self.pc_via = np.array([v for vs in pcv for v in vs], np.int32)
+        self.prec_sizes = np.array(sizes)
         self.stats = dict(clusters=len(self.nodes), leaves=len(leaves), near_pairs=len(near),
                           far_blocks=len(self.far), near_field_pairs=int(self.keys.size), prec_blocks=len(pc))
 
@@ -269,7 +289,7 @@ class HMatrix:
     """The compressed operator of a Solver's mesh on the solver's engine
     context. assemble(greens, zs) at a frequency, then matvec / solve."""
 
-    def __init__(self, solver, leaf=48, eta=1.0, tol=1e-4, kcap=96, prec_block=256):
+    def __init__(self, solver, leaf=48, eta=1.0, tol=1e-4, kcap=96, prec_block=512):
         if solver._blocks_host is None:
             solver.geometry()
         P = self.plan = Plan(solver.mesh, solver.zl, solver._blocks_host, leaf, eta, prec_block)
@@ -280,7 +300,8 @@ class HMatrix:
             near=E.i32(P.near_arr), far=E.i32(P.far_arr), far_cen=E.i32(P.far_cen),
             ent_off=np.ascontiguousarray(P.ent_off, np.int64), ent=E.i32(P.ent),
             keys=np.ascontiguousarray(P.keys, np.int64), pblk=E.i32(P.pblk), pc=E.i32(P.pc),
-            pc_off=np.ascontiguousarray(P.pc_off, np.int64), pc_items=E.i32(P.pc_items))
+            pc_off=np.ascontiguousarray(P.pc_off, np.int64), pc_items=E.i32(P.pc_items),
+            pc_via_off=np.ascontiguousarray(P.pc_via_off, np.int64), pc_via=E.i32(P.pc_via))
         i32, i64 = C.c_int32, C.c_int64
         d = E.HmatDesc(P.nb, P.nv, E.ptr(arrs["perm"], i32), E.ptr(arrs["rules"]), E.ptr(arrs["lev"], i32),
                        len(P.leaves), E.ptr(arrs["leaf_lo"], i32), len(P.near), E.ptr(arrs["near"], i32),
@@ -288,7 +309,7 @@ class HMatrix:
                        E.ptr(arrs["ent_off"], i64), E.ptr(arrs["ent"], i32), int(P.keys.size),
                        E.ptr(arrs["keys"], i64), int(P.pblk.size), E.ptr(arrs["pblk"], i32), len(P.pc),
                        E.ptr(arrs["pc"], i32), E.ptr(arrs["pc_off"], i64), E.ptr(arrs["pc_items"], i32),
-                       float(tol), int(kcap))
+                       E.ptr(arrs["pc_via_off"], i64), E.ptr(arrs["pc_via"], i32), float(tol), int(kcap))
         self.ctx = solver.ctx
         h = C.c_void_p()
         E.check(self.ctx.lib.m25_hmat_create(self.ctx.h, solver.geometry().h, C.byref(d), C.byref(h)))

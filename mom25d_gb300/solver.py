@@ -379,6 +379,7 @@ class Solver:
         self.method = method
         self._hop = None
         self.hmatrix_options = {}  # HMatrix keyword arguments (leaf, eta, tol, kcap, prec_block)
+        self.gmres_rtol = 1e-6  # relative residual of the compressed solve (mom25d: 1e-6, hmatrix.py:563)
         self.precision = precision
         self.refine_tol, self.max_refine = refine_tol, max_refine
         self.z0_fixed = None if z0 is None else np.asarray(z0, float)
@@ -560,7 +561,7 @@ class Solver:
         hop.assemble(g, zs, zs)
         B = np.asarray(B, complex).reshape(self.mesh.n_unknowns, -1)
         _, first, inv = np.unique(B.T, axis=0, return_index=True, return_inverse=True)
-        X = hop.solve(B[:, first])[:, np.ravel(inv)]
+        X = hop.solve(B[:, first], rtol=self.gmres_rtol)[:, np.ravel(inv)]
         if self.verbose:
             print(f"  f = {freq / 1e9:8.4f} GHz  N = {self.mesh.n_unknowns}  {hop.summary()}", flush=True)
         return X
@@ -790,7 +791,8 @@ class Solver:
         return self.tuning
 
     # what a caller may change between sweeps; a sweep hands the current values to its workers
-    _SETTINGS = ("precision", "method", "refine_tol", "max_refine", "z0_fixed", "v_weight", "surrogate", "tuning")
+    _SETTINGS = ("precision", "method", "refine_tol", "max_refine", "z0_fixed", "v_weight", "surrogate", "tuning",
+                 "gmres_rtol")
 
     def _sibling(self, i):
         """Worker i of a concurrent sweep (0: this solver): the same mesh,

@@ -80,7 +80,8 @@ def test_plan_index_lists(name):
       is among the listed near-field pairs;
     - every row's items (near pairs, far blocks as rows, far blocks as
       columns) cover each column exactly once;
-    - every preconditioner block's items tile its diagonal block exactly once;
+    - every preconditioner block's items tile its diagonal block exactly once,
+      the blocks tile the unknowns and each via joins its pads' block;
     - the pad blocks hold every via pad triangle."""
     m, P = _plan(name)
     nb, nt = P.nb, P.nt
@@ -110,9 +111,6 @@ def test_plan_index_lists(name):
                     cnt[r0:r0 + mm] += 1
         assert np.all(cnt == 1), (k, np.unique(cnt))
     for k, (p0, s) in enumerate(P.pc):
-        if p0 >= nb:  # the via block
-            assert s == P.nv and P.pc_items[P.pc_off[k]:P.pc_off[k + 1]].tolist() == [[2, 0]]
-            continue
         cnt = np.zeros((s, s), int)
         for t, i in P.pc_items[P.pc_off[k]:P.pc_off[k + 1]]:
             if t == 0:
@@ -123,7 +121,21 @@ def test_plan_index_lists(name):
                 cnt[r0 - p0:r0 - p0 + mm, c0 - p0:c0 - p0 + nn] += 1
                 cnt[c0 - p0:c0 - p0 + nn, r0 - p0:r0 - p0 + mm] += 1
         assert np.all(cnt == 1)
-    assert np.array_equal(np.sort(np.concatenate([P.pc[:, 0], [P.n]])[1:] - np.sort(P.pc[:, 0])), np.sort(P.pc[:, 1]))
+    # the blocks' RWG ranges tile the tree order; every via sits in exactly one
+    # block, the one holding an RWG unknown of its first pad triangle
+    order = np.argsort(P.pc[:, 0])
+    starts, sizes = P.pc[order, 0], P.pc[order, 1]
+    assert starts[0] == 0 and np.array_equal(starts[1:], starts[:-1] + sizes[:-1]) and starts[-1] + sizes[-1] == nb
+    assert sorted(P.pc_via.tolist()) == list(range(P.nv))
+    ipos = np.empty(nb, int)
+    ipos[perm] = np.arange(nb)
+    for k, (p0, s) in enumerate(P.pc):
+        for v in P.pc_via[P.pc_via_off[k]:P.pc_via_off[k + 1]]:
+            g = m.via_segments[v]
+            t = next(np.atleast_1d(g[e])[0] for e in ("top_tris", "bottom_tris") if g[e] is not None)
+            bs = m.tri_basis[t][m.tri_basis[t] >= 0]
+            assert p0 <= ipos[bs[0]] < p0 + s
+    assert P.prec_sizes.max() <= 1024
     if P.nv:
         pads = np.unique(np.concatenate([g[e] for g in m.via_segments for e in ("top_tris", "bottom_tris")
                                          if g[e] is not None]))
