@@ -391,10 +391,12 @@ int m25_deembed_debug(m25_ctx* ctx, m25_ports* ports, double* phi, double* q, do
  * 1 far block whose rows hold the leaf, 2 far block whose columns hold it;
  * id; the leaf's offset inside the block's rows / columns; 0); keys: the
  * near field's (test block x nt + source triangle) pairs, sorted; pblk: the
- * test blocks holding via pad triangles; pc: preconditioner blocks (first
- * tree position, RWG unknowns) with their items (CSR pc_off; type 0 near
- * pair, 1 far block; id) and their via unknowns (CSR pc_via_off; at most
- * 1024 unknowns per block with its vias). rules: per basis 40 values of the far-field rules
+ * test blocks holding via pad triangles; preconditioner blocks (restricted
+ * additive Schwarz): per block its unknowns (RWG positions of whole leaves,
+ * then vias; at most 1024), which of them it writes, and per (row leaf,
+ * column leaf) pair of its leaves the source of that sub-block (a near pair
+ * id, or nnear + 2 f for far block f as rows, + 1 as its transpose) with the
+ * sub-block's local row and column. rules: per basis 40 values of the far-field rules
  * (3-point points, w cA (r - a), w cV; centroids, A cA (c - a), A cV). */
 typedef struct m25_hmat m25_hmat;
 typedef struct {
@@ -416,11 +418,11 @@ typedef struct {
   int32_t npblk;
   const int32_t* pblk;
   int32_t npc;
-  const int32_t* pc;          /* (npc, 2) */
-  const int64_t* pc_off;      /* (npc + 1) */
-  const int32_t* pc_items;    /* (pc_off[npc], 2) */
-  const int64_t* pc_via_off;  /* (npc + 1) */
-  const int32_t* pc_via;      /* the via unknowns of each block (CSR pc_via_off) */
+  const int64_t* pc_off;      /* (npc + 1) CSR of the blocks' unknowns */
+  const int32_t* pc_gidx;     /* vector index of each block unknown (tree position, or nb + via) */
+  const int8_t* pc_own;       /* 1: the block writes this unknown (each unknown owned once) */
+  const int64_t* pc_item_off; /* (npc + 1) */
+  const int32_t* pc_items;    /* (pc_item_off[npc], 5): source, row leaf, column leaf, local row, local column */
   double tol;                 /* ACA tolerance (1e-4) */
   int32_t kcap;               /* most ACA terms stored per block */
 } m25_hmat_desc;
@@ -435,10 +437,11 @@ int m25_hmat_assemble(m25_hmat* h, m25_greens* gr, double zs_re, double zs_im, d
                       int64_t* stats);
 /* y = Z x with the compressed operator; x, y host complex128 (n). */
 int m25_hmat_matvec(m25_hmat* h, const double* x, double* y);
-/* X = Z^-1 B by right-preconditioned restarted GMRES, column by column; B, X
- * host complex128 (n, nrhs) row-major; iters and resid (true relative
- * residual) per column. A column that does not reach rtol returns M25_OK
- * with its residual (the caller accepts or raises, as mom25d does). */
+/* X = Z^-1 B by flexible restarted GMRES on the symmetrically scaled system
+ * W Z W (W = |Z_ii|^-1/2), column by column; B, X host complex128 (n, nrhs)
+ * row-major; iters and resid (the scaled system's true relative residual)
+ * per column. A column that does not reach rtol returns M25_OK with its
+ * residual (the caller accepts or raises, as mom25d does). */
 int m25_hmat_solve(m25_hmat* h, int32_t nrhs, const double* B, double* X, double rtol, int32_t restart,
                    int32_t maxiter, int32_t* iters, double* resid);
 

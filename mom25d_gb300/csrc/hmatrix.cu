@@ -16,14 +16,17 @@
 //                leaf's near blocks, far blocks as rows or as columns, and
 //                its via columns; every output entry has one writer
 //                (deterministic, no atomics);
-//   precondition (diag_kernel, ginv_kernel, psolve_kernel): block Jacobi
-//                over clusters of <= 512 unknowns, each with the vias whose
-//                pads it holds; the blocks scaled to a unit diagonal and
-//                inverted in fp64 (Gauss-Jordan, partial pivoting), applied
-//                as one batched GEMV;
-//   GMRES        restarted, flexible (right-preconditioned, keeping each
-//                M^-1 v_j), classical Gram-Schmidt applied twice, Givens
-//                rotations on the host.
+//   precondition (diag_kernel, ginv_kernel, psolve_kernel): restricted
+//                additive Schwarz over clusters of <= 256 unknowns extended
+//                by their near-coupled leaves and the vias whose pads they
+//                hold; the blocks scaled to a unit diagonal and inverted in
+//                complex64 (Gauss-Jordan, partial pivoting), applied as one
+//                batched GEMV that writes each block's own unknowns;
+//   GMRES        on the symmetrically scaled system W Z W, W = |Z_ii|^-1/2
+//                (the via unknowns' diagonal is ~1e10 times the RWG
+//                unknowns'), restarted, flexible (right-preconditioned,
+//                keeping each M^-1 v_j), classical Gram-Schmidt applied
+//                twice, Givens rotations on the host.
 // Vectors inside are in tree order: RWG unknowns perm[0..nb), then vias.
 #include <algorithm>
 #include <cmath>
@@ -51,15 +54,19 @@ struct m25_hmat {
   double tol = 1e-4;
   int kcap = 96;
   // host copies of the block lists
-  std::vector<int32_t> far_h, cen_h, near_h, pc_h;
+  std::vector<int32_t> far_h, cen_h, near_h;
   std::vector<int64_t> near_off_h;
   // device: structure
   int32_t *perm = nullptr, *lev = nullptr, *leaf_lo = nullptr, *near = nullptr, *ent = nullptr;
   int64_t *near_off = nullptr, *ent_off = nullptr, *keys = nullptr;
-  int32_t *pblk = nullptr, *pc = nullptr, *pc_items = nullptr, *pc_via = nullptr, *row_leaf = nullptr;
+  int32_t *pblk = nullptr, *pc_gidx = nullptr, *pc_items = nullptr, *row_leaf = nullptr;
+  int8_t* pc_own = nullptr;
+  int32_t* self_near = nullptr;  // (nleaf) the near pair (a, a) of each leaf
+  double* wsc = nullptr;         // (n) |Z_ii|^-1/2: the GMRES system's symmetric scaling
+  m25::zd* sx = nullptr;         // (n) scratch of the scaled products
   int2* terms = nullptr;  // (block, term) of every low-rank term
   int nterm = 0;
-  int64_t *pc_off = nullptr, *pc_doff = nullptr, *pc_via_off = nullptr;
+  int64_t *pc_off = nullptr, *pc_doff = nullptr, *pc_item_off = nullptr;
   double* rules = nullptr;
   FarB* fb = nullptr;  // (nfar) device
   std::vector<FarB> fb_h;
@@ -495,63 +502,78 @@ __global__ void perm_out_kernel(int nb, int n, const int32_t* __restrict__ perm,
 }
 
 // ---------------------------------------------------------- preconditioner
-// Block k holds the RWG unknowns [p0, p0 + s) of a tree cluster, then its nv_k
-// via unknowns (local index s + a): size S = s + nv_k.
-__device__ __forceinline__ int pc_global(int i, int p0, int s, int nb, const int32_t* __restrict__ via, int64_t v0) {
-  return i < s ? p0 + i : nb + via[v0 + (i - s)];
-}
+// Block k (restricted additive Schwarz) holds S_k unknowns, pc_gidx[pc_off[k]
+// ..]: whole leaves (tree positions) then vias (nb + via); it writes those
+// with pc_own set. Its matrix is the compressed operator on those unknowns.
 
-// diagonal block k (row-major S x S) of the compressed operator: its near
-// pairs, its far blocks (both orientations), its via rows / columns
-__global__ void diag_kernel(const int32_t* __restrict__ pc, const int64_t* __restrict__ pc_off,
-                            const int32_t* __restrict__ items, const int64_t* __restrict__ via_off,
-                            const int32_t* __restrict__ via, const int64_t* __restrict__ doff, int nv,
-                            const int32_t* __restrict__ near, const int64_t* __restrict__ noff,
+// block k's matrix (complex64, row-major S x S): per (row leaf, column leaf)
+// pair the near block or the far block (as rows or as its transpose), then
+// the via rows / columns
+__global__ void diag_kernel(const int64_t* __restrict__ pc_off, const int32_t* __restrict__ gidx,
+                            const int64_t* __restrict__ item_off, const int32_t* __restrict__ items,
+                            const int64_t* __restrict__ doff, int nb, int nv, int nnear,
+                            const int32_t* __restrict__ leaf_lo, const int64_t* __restrict__ noff,
                             const zd* __restrict__ Zn, const FarB* __restrict__ fb, const zd* __restrict__ pool,
                             const zd* __restrict__ dpool, const zd* __restrict__ ZxbT, const zd* __restrict__ Zxx,
                             zf* __restrict__ D) {
+  __shared__ int nr;
   const int k = blockIdx.x;
-  const int p0 = pc[2 * k], s = pc[2 * k + 1];
-  const int64_t v0 = via_off[k];
-  const int nvk = (int)(via_off[k + 1] - v0), S = s + nvk;
+  const int64_t g0 = pc_off[k];
+  const int S = (int)(pc_off[k + 1] - g0);
   zf* Dk = D + doff[k];
+  if (threadIdx.x == 0) nr = 0;
+  __syncthreads();
+  int mine = 0;
+  for (int t = threadIdx.x; t < S; t += blockDim.x) mine += gidx[g0 + t] < nb;
+  atomicAdd(&nr, mine);
   for (int64_t e = threadIdx.x; e < (int64_t)S * S; e += blockDim.x) Dk[e] = zf(0.f, 0.f);
   __syncthreads();
-  for (int64_t it = pc_off[k]; it < pc_off[k + 1]; ++it) {
-    const int type = items[2 * it], id = items[2 * it + 1];
-    if (type == 0) {
-      const int a0 = near[4 * id], am = near[4 * id + 1], b0 = near[4 * id + 2], bn = near[4 * id + 3];
-      const zd* blk = Zn + noff[id];
+  const int R = nr;  // RWG unknowns first, then the vias
+  for (int64_t it = item_off[k]; it < item_off[k + 1]; ++it) {
+    const int src = items[5 * it], li = items[5 * it + 1], lj = items[5 * it + 2];
+    const int lr0 = items[5 * it + 3], lc0 = items[5 * it + 4];
+    const int a0 = leaf_lo[li], am = leaf_lo[li + 1] - a0, b0 = leaf_lo[lj], bn = leaf_lo[lj + 1] - b0;
+    if (src < nnear) {
+      const zd* blk = Zn + noff[src];
       for (int e = threadIdx.x; e < am * bn; e += blockDim.x) {
-        const int i = e / bn, j = e - i * bn;
-        Dk[(int64_t)(a0 - p0 + i) * S + (b0 - p0 + j)] = zf(blk[e]);
+        const int ii = e / bn, jj = e - ii * bn;
+        Dk[(int64_t)(lr0 + ii) * S + lc0 + jj] = zf(blk[e]);
       }
       continue;
     }
-    const FarB F = fb[id];
-    for (int64_t e = threadIdx.x; e < (int64_t)F.m * F.n; e += blockDim.x) {
-      const int i = (int)(e / F.n), j = (int)(e - (int64_t)i * F.n);
-      zd z;
-      if (F.kind == 0) {
-        const zd* U = pool + F.uv;
-        const zd* V = U + (int64_t)F.kcap * F.m;
-        for (int l = 0; l < F.rank; ++l) z += U[(int64_t)l * F.m + i] * V[(int64_t)l * F.n + j];
-      } else {
-        z = dpool[F.dense + e];
+    const int f = (src - nnear) >> 1, o = (src - nnear) & 1;
+    const FarB F = fb[f];
+    const zd* U = F.kind == 0 ? pool + F.uv : nullptr;
+    const zd* V = F.kind == 0 ? U + (int64_t)F.kcap * F.m : nullptr;
+    for (int e = threadIdx.x; e < am * bn; e += blockDim.x) {
+      const int ii = e / bn, jj = e - ii * bn;
+      zf z(0.f, 0.f);
+      if (o == 0) {  // rows in R, columns in C
+        const int ir = a0 - F.r0 + ii, jc = b0 - F.c0 + jj;
+        if (F.kind == 0)
+          for (int l = 0; l < F.rank; ++l) z += zf(U[(int64_t)l * F.m + ir]) * zf(V[(int64_t)l * F.n + jc]);
+        else
+          z = zf(dpool[F.dense + (int64_t)ir * F.n + jc]);
+      } else {  // rows in C, columns in R: the transpose
+        const int ic = a0 - F.c0 + ii, jr = b0 - F.r0 + jj;
+        if (F.kind == 0)
+          for (int l = 0; l < F.rank; ++l) z += zf(V[(int64_t)l * F.n + ic]) * zf(U[(int64_t)l * F.m + jr]);
+        else
+          z = zf(dpool[F.dense + (int64_t)jr * F.n + ic]);
       }
-      Dk[(int64_t)(F.r0 - p0 + i) * S + (F.c0 - p0 + j)] = zf(z);
-      Dk[(int64_t)(F.c0 - p0 + j) * S + (F.r0 - p0 + i)] = zf(z);
+      Dk[(int64_t)(lr0 + ii) * S + lc0 + jj] = z;
     }
   }
-  for (int e = threadIdx.x; e < s * nvk; e += blockDim.x) {  // RWG x via (Z is symmetric)
-    const int i = e / nvk, a = e - i * nvk;
-    const zf z(ZxbT[(int64_t)(p0 + i) * nv + via[v0 + a]]);
-    Dk[(int64_t)i * S + s + a] = z;
-    Dk[(int64_t)(s + a) * S + i] = z;
+  const int nvk = S - R;
+  for (int e = threadIdx.x; e < R * nvk; e += blockDim.x) {  // RWG x via (Z is symmetric)
+    const int t = e / nvk, a = e - t * nvk;
+    const zf z(ZxbT[(int64_t)gidx[g0 + t] * nv + (gidx[g0 + R + a] - nb)]);
+    Dk[(int64_t)t * S + R + a] = z;
+    Dk[(int64_t)(R + a) * S + t] = z;
   }
   for (int e = threadIdx.x; e < nvk * nvk; e += blockDim.x) {  // via x via
     const int a = e / nvk, b = e - a * nvk;
-    Dk[(int64_t)(s + a) * S + s + b] = zf(Zxx[(int64_t)via[v0 + a] * nv + via[v0 + b]]);
+    Dk[(int64_t)(R + a) * S + R + b] = zf(Zxx[(int64_t)(gidx[g0 + R + a] - nb) * nv + (gidx[g0 + R + b] - nb)]);
   }
 }
 
@@ -565,15 +587,15 @@ __global__ void diag_kernel(const int32_t* __restrict__ pc, const int64_t* __res
 // columns, and D^-1 = W D'^-1 W stored in place.
 __device__ __forceinline__ float fabs1(zf a) { return fabsf(a.re) + fabsf(a.im); }
 
-__global__ void __launch_bounds__(256) ginv_kernel(const int32_t* __restrict__ pc, const int64_t* __restrict__ via_off,
-                                                   const int64_t* __restrict__ doff, zf* __restrict__ D) {
+__global__ void __launch_bounds__(256) ginv_kernel(const int64_t* __restrict__ pc_off, const int64_t* __restrict__ doff,
+                                                   zf* __restrict__ D) {
   __shared__ double sv[32];
   __shared__ int si[32];
   __shared__ int pv[1024];
   __shared__ float w[1024];
   __shared__ zf fcol[1024];
   const int k = blockIdx.x;
-  const int S = pc[2 * k + 1] + (int)(via_off[k + 1] - via_off[k]);
+  const int S = (int)(pc_off[k + 1] - pc_off[k]);
   zf* A = D + doff[k];
   for (int i = threadIdx.x; i < S; i += blockDim.x) {
     const zf a = A[(int64_t)i * S + i];
@@ -639,26 +661,26 @@ __global__ void __launch_bounds__(256) ginv_kernel(const int32_t* __restrict__ p
   }
 }
 
-// out = D_k^-1 in on block k's unknowns (complex64 inverse, fp32 sums), one warp per row
-__global__ void __launch_bounds__(256) psolve_kernel(const int32_t* __restrict__ pc, const int64_t* __restrict__ via_off,
-                                                     const int32_t* __restrict__ via, const int64_t* __restrict__ doff,
-                                                     int nb, const zf* __restrict__ D, const zd* __restrict__ in,
+// out = D_k^-1 in on the unknowns block k owns (complex64 inverse, fp32 sums), one warp per row
+__global__ void __launch_bounds__(256) psolve_kernel(const int64_t* __restrict__ pc_off, const int32_t* __restrict__ gidx,
+                                                     const int8_t* __restrict__ own, const int64_t* __restrict__ doff,
+                                                     const zf* __restrict__ D, const zd* __restrict__ in,
                                                      zd* __restrict__ out) {
   __shared__ zf xs[1024];
   const int k = blockIdx.x;
-  const int p0 = pc[2 * k], s = pc[2 * k + 1];
-  const int64_t v0 = via_off[k];
-  const int S = s + (int)(via_off[k + 1] - v0);
+  const int64_t g0 = pc_off[k];
+  const int S = (int)(pc_off[k + 1] - g0);
   const zf* A = D + doff[k];
-  for (int i = threadIdx.x; i < S; i += blockDim.x) xs[i] = zf(in[pc_global(i, p0, s, nb, via, v0)]);
+  for (int i = threadIdx.x; i < S; i += blockDim.x) xs[i] = zf(in[gidx[g0 + i]]);
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int r = wid; r < S; r += nw) {
+    if (!own[g0 + r]) continue;
     zf acc(0.f, 0.f);
     const zf* row = A + (int64_t)r * S;
     for (int j = lane; j < S; j += 32) acc += row[j] * xs[j];
     const zd a = warp_sum(zd(double(acc.re), double(acc.im)));
-    if (lane == 0) out[pc_global(r, p0, s, nb, via, v0)] = a;
+    if (lane == 0) out[gidx[g0 + r]] = a;
   }
 }
 
@@ -724,6 +746,36 @@ Tabs make_tabs(m25_greens* gr) {
   return t;
 }
 
+}  // namespace
+
+// w_i = |Z_ii|^-1/2 from the leaves' own near blocks and the via block
+__global__ void wscale_kernel(int nb, int n, int nv, const int32_t* __restrict__ row_leaf,
+                              const int32_t* __restrict__ self_near, const int32_t* __restrict__ near,
+                              const int64_t* __restrict__ noff, const zd* __restrict__ Zn, const zd* __restrict__ Zxx,
+                              double* __restrict__ w) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  zd d;
+  if (r < nb) {
+    const int p = self_near[row_leaf[r]];
+    const int a0 = near[4 * p], bn = near[4 * p + 3];
+    d = Zn[noff[p] + (int64_t)(r - a0) * bn + (r - a0)];
+  } else {
+    d = Zxx[(int64_t)(r - nb) * nv + (r - nb)];
+  }
+  const double a = cabs(d);
+  w[r] = a > 0.0 ? 1.0 / sqrt(a) : 1.0;
+}
+
+// dst = src w (inv: src / w)
+__global__ void vscale_kernel(zd* __restrict__ dst, const zd* __restrict__ src, const double* __restrict__ w, int n,
+                              int inv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = inv ? src[i] / w[i] : src[i] * w[i];
+}
+
+namespace {
+
 // y = A x, tree order, device vectors
 int apply(m25_hmat* h, const zd* x, zd* y) {
   cudaStream_t st = h->ctx->stream;
@@ -736,8 +788,31 @@ int apply(m25_hmat* h, const zd* x, zd* y) {
 }
 
 int precond(m25_hmat* h, const zd* in, zd* out) {
-  psolve_kernel<<<h->npc, 256, 0, h->ctx->stream>>>(h->pc, h->pc_via_off, h->pc_via, h->pc_doff, h->nb, h->D,
-                                                    in, out);
+  psolve_kernel<<<h->npc, 256, 0, h->ctx->stream>>>(h->pc_off, h->pc_gidx, h->pc_own, h->pc_doff, h->D, in, out);
+  M25_CHECK_LAUNCH();
+  return M25_OK;
+}
+
+// the scaled system W A W: y = W A (W x)
+int sapply(m25_hmat* h, const zd* x, zd* y) {
+  cudaStream_t st = h->ctx->stream;
+  const int g = (h->n + 255) / 256;
+  vscale_kernel<<<g, 256, 0, st>>>(h->sx, x, h->wsc, h->n, 0);
+  int rc = apply(h, h->sx, y);
+  if (rc) return rc;
+  vscale_kernel<<<g, 256, 0, st>>>(y, y, h->wsc, h->n, 0);
+  M25_CHECK_LAUNCH();
+  return M25_OK;
+}
+
+// its preconditioner W^-1 M^-1 W^-1
+int sprecond(m25_hmat* h, const zd* in, zd* out) {
+  cudaStream_t st = h->ctx->stream;
+  const int g = (h->n + 255) / 256;
+  vscale_kernel<<<g, 256, 0, st>>>(h->sx, in, h->wsc, h->n, 1);
+  int rc = precond(h, h->sx, out);
+  if (rc) return rc;
+  vscale_kernel<<<g, 256, 0, st>>>(out, out, h->wsc, h->n, 1);
   M25_CHECK_LAUNCH();
   return M25_OK;
 }
@@ -828,23 +903,53 @@ extern "C" int m25_hmat_create(m25_ctx* ctx, m25_geom* geom, const m25_hmat_desc
   h->t_entries = tt;
   h->flag_bytes = fl;
   // preconditioner blocks
-  h->pc_h.assign(d->pc, d->pc + 2 * (size_t)d->npc);
   std::vector<int64_t> doff(d->npc + 1, 0);
-  if (d->pc_via_off[0] != 0 || d->pc_via_off[d->npc] != d->nv)
-    return fail((set_error("m25_hmat_create: the via unknowns are not split over the blocks"), M25_ERR_VALUE));
-  for (int k = 0; k < d->npc; ++k) {
-    const int p0 = h->pc_h[2 * k], s = h->pc_h[2 * k + 1];
-    const int64_t nvk = d->pc_via_off[k + 1] - d->pc_via_off[k];
-    if (s <= 0 || nvk < 0 || s + nvk > 1024 || p0 < 0 || p0 + s > h->nb)
-      return fail((set_error("m25_hmat_create: bad preconditioner block"), M25_ERR_VALUE));
-    doff[k + 1] = doff[k] + (s + nvk) * (s + nvk);
+  {
+    if (d->pc_off[0] != 0 || d->pc_item_off[0] != 0)
+      return fail((set_error("m25_hmat_create: bad preconditioner offsets"), M25_ERR_VALUE));
+    std::vector<int> owned(h->n, 0);
+    std::vector<int32_t> lsz(d->nleaf);
+    for (int l = 0; l < d->nleaf; ++l) lsz[l] = d->leaf_lo[l + 1] - d->leaf_lo[l];
+    for (int k = 0; k < d->npc; ++k) {
+      const int64_t S = d->pc_off[k + 1] - d->pc_off[k];
+      if (S <= 0 || S > 1024 || d->pc_item_off[k + 1] < d->pc_item_off[k])
+        return fail((set_error("m25_hmat_create: bad preconditioner block"), M25_ERR_VALUE));
+      bool vias = false;
+      for (int64_t t = d->pc_off[k]; t < d->pc_off[k + 1]; ++t) {
+        const int g = d->pc_gidx[t];
+        if (g < 0 || g >= h->n || (vias && g < d->nb))
+          return fail((set_error("m25_hmat_create: bad preconditioner unknown"), M25_ERR_VALUE));
+        vias = vias || g >= d->nb;
+        if (d->pc_own[t]) ++owned[g];
+      }
+      for (int64_t e = d->pc_item_off[k]; e < d->pc_item_off[k + 1]; ++e) {
+        const int32_t* it = d->pc_items + 5 * e;
+        const int src = it[0], li = it[1], lj = it[2], lr0 = it[3], lc0 = it[4];
+        if (li < 0 || li >= d->nleaf || lj < 0 || lj >= d->nleaf || src < 0 || src >= d->nnear + 2 * d->nfar ||
+            lr0 < 0 || lc0 < 0 || lr0 + lsz[li] > S || lc0 + lsz[lj] > S)
+          return fail((set_error("m25_hmat_create: bad preconditioner item"), M25_ERR_VALUE));
+        const int a0 = d->leaf_lo[li], b0 = d->leaf_lo[lj];
+        bool ok;
+        if (src < d->nnear) {
+          const int32_t* q = d->near + 4 * src;
+          ok = q[0] == a0 && q[1] == lsz[li] && q[2] == b0 && q[3] == lsz[lj];
+        } else {
+          const int f = (src - d->nnear) >> 1, o = (src - d->nnear) & 1;
+          const int32_t* q = d->far + 4 * f;
+          const int rr0 = o ? q[2] : q[0], rm = o ? q[3] : q[1], cc0 = o ? q[0] : q[2], cn = o ? q[1] : q[3];
+          ok = a0 >= rr0 && a0 + lsz[li] <= rr0 + rm && b0 >= cc0 && b0 + lsz[lj] <= cc0 + cn;
+        }
+        if (!ok) return fail((set_error("m25_hmat_create: a preconditioner item outside its source block"), M25_ERR_VALUE));
+      }
+      doff[k + 1] = doff[k] + S * S;
+    }
+    for (int g = 0; g < h->n; ++g)
+      if (owned[g] != 1) return fail((set_error("m25_hmat_create: an unknown not owned by exactly one block"), M25_ERR_VALUE));
   }
-  for (int v = 0; v < d->nv; ++v)
-    if (d->pc_via[v] < 0 || d->pc_via[v] >= d->nv)
-      return fail((set_error("m25_hmat_create: bad via index"), M25_ERR_VALUE));
   h->d_entries = doff[d->npc];
   const int64_t nent = d->ent_off[d->nleaf];
-  const int64_t nitems = d->pc_off[d->npc];
+  const int64_t nitems = d->pc_item_off[d->npc];
+  const int64_t npcu = d->pc_off[d->npc];
 #define TRY(x)                 \
   do {                         \
     if ((rc = (x))) return fail(rc); \
@@ -854,18 +959,21 @@ extern "C" int m25_hmat_create(m25_ctx* ctx, m25_geom* geom, const m25_hmat_desc
   TRY(dalloc(h->allocs, &h->lev, d->nb));
   TRY(dalloc(h->allocs, &h->leaf_lo, d->nleaf + 1));
   TRY(dalloc(h->allocs, &h->row_leaf, d->nb));
+  TRY(dalloc(h->allocs, &h->self_near, d->nleaf));
+  TRY(dalloc(h->allocs, &h->wsc, h->n));
+  TRY(dalloc(h->allocs, &h->sx, h->n));
   TRY(dalloc(h->allocs, &h->near, 4 * (size_t)d->nnear));
   TRY(dalloc(h->allocs, &h->near_off, d->nnear + 1));
   TRY(dalloc(h->allocs, &h->ent_off, d->nleaf + 1));
   TRY(dalloc(h->allocs, &h->ent, 4 * (size_t)nent));
   TRY(dalloc(h->allocs, &h->keys, d->nkeys));
   TRY(dalloc(h->allocs, &h->pblk, d->npblk));
-  TRY(dalloc(h->allocs, &h->pc, 2 * (size_t)d->npc));
   TRY(dalloc(h->allocs, &h->pc_off, d->npc + 1));
-  TRY(dalloc(h->allocs, &h->pc_items, 2 * (size_t)nitems));
+  TRY(dalloc(h->allocs, &h->pc_gidx, npcu));
+  TRY(dalloc(h->allocs, &h->pc_own, npcu));
+  TRY(dalloc(h->allocs, &h->pc_item_off, d->npc + 1));
+  TRY(dalloc(h->allocs, &h->pc_items, 5 * (size_t)nitems));
   TRY(dalloc(h->allocs, &h->pc_doff, d->npc + 1));
-  TRY(dalloc(h->allocs, &h->pc_via_off, d->npc + 1));
-  TRY(dalloc(h->allocs, &h->pc_via, std::max(d->nv, 1)));
   TRY(dalloc(h->allocs, &h->fb, d->nfar));
   TRY(dalloc(h->allocs, &h->Zn, h->near_entries));
   TRY(dalloc(h->allocs, &h->pool, uv));
@@ -889,6 +997,14 @@ extern "C" int m25_hmat_create(m25_ctx* ctx, m25_geom* geom, const m25_hmat_desc
     if (d->leaf_lo[k + 1] <= d->leaf_lo[k]) return fail((set_error("m25_hmat_create: empty leaf"), M25_ERR_VALUE));
     for (int r = d->leaf_lo[k]; r < d->leaf_lo[k + 1] && r < d->nb; ++r) row_leaf[r] = k;
   }
+  std::vector<int32_t> self_near(d->nleaf, -1);
+  for (int p = 0; p < d->nnear; ++p)
+    if (d->near[4 * p] == d->near[4 * p + 2]) {
+      const int k = row_leaf[d->near[4 * p]];
+      if (d->leaf_lo[k] == d->near[4 * p]) self_near[k] = p;
+    }
+  for (int k = 0; k < d->nleaf; ++k)
+    if (self_near[k] < 0) return fail((set_error("m25_hmat_create: a leaf without its own near block"), M25_ERR_VALUE));
   std::vector<int32_t> aca;
   for (int f = 0; f < d->nfar; ++f)
     if (h->fb_h[f].kind == 0) aca.push_back(f);
@@ -896,18 +1012,19 @@ extern "C" int m25_hmat_create(m25_ctx* ctx, m25_geom* geom, const m25_hmat_desc
       (rc = up(h->lev, d->lev, sizeof(int32_t) * d->nb)) ||
       (rc = up(h->leaf_lo, d->leaf_lo, sizeof(int32_t) * (d->nleaf + 1))) ||
       (rc = up(h->row_leaf, row_leaf.data(), sizeof(int32_t) * d->nb)) ||
+      (rc = up(h->self_near, self_near.data(), sizeof(int32_t) * d->nleaf)) ||
       (rc = up(h->near, d->near, sizeof(int32_t) * 4 * d->nnear)) ||
       (rc = up(h->near_off, h->near_off_h.data(), sizeof(int64_t) * (d->nnear + 1))) ||
       (rc = up(h->ent_off, d->ent_off, sizeof(int64_t) * (d->nleaf + 1))) ||
       (rc = up(h->ent, d->ent, sizeof(int32_t) * 4 * nent)) ||
       (rc = up(h->keys, d->keys, sizeof(int64_t) * d->nkeys)) ||
       (rc = up(h->pblk, d->pblk, sizeof(int32_t) * d->npblk)) ||
-      (rc = up(h->pc, d->pc, sizeof(int32_t) * 2 * d->npc)) ||
       (rc = up(h->pc_off, d->pc_off, sizeof(int64_t) * (d->npc + 1))) ||
-      (rc = up(h->pc_items, d->pc_items, sizeof(int32_t) * 2 * nitems)) ||
+      (rc = up(h->pc_gidx, d->pc_gidx, sizeof(int32_t) * npcu)) ||
+      (rc = up(h->pc_own, d->pc_own, sizeof(int8_t) * npcu)) ||
+      (rc = up(h->pc_item_off, d->pc_item_off, sizeof(int64_t) * (d->npc + 1))) ||
+      (rc = up(h->pc_items, d->pc_items, sizeof(int32_t) * 5 * nitems)) ||
       (rc = up(h->pc_doff, doff.data(), sizeof(int64_t) * (d->npc + 1))) ||
-      (rc = up(h->pc_via_off, d->pc_via_off, sizeof(int64_t) * (d->npc + 1))) ||
-      (rc = up(h->pc_via, d->pc_via, sizeof(int32_t) * d->nv)) ||
       (rc = up(h->aca_ids, aca.data(), sizeof(int32_t) * aca.size())))
     return fail(rc);
   // index checks of the lists the kernels follow
@@ -915,11 +1032,6 @@ extern "C" int m25_hmat_create(m25_ctx* ctx, m25_geom* geom, const m25_hmat_desc
     const int type = d->ent[4 * e], id = d->ent[4 * e + 1];
     if (type < 0 || type > 2 || id < 0 || id >= (type == 0 ? d->nnear : d->nfar))
       return fail((set_error("m25_hmat_create: bad leaf entry"), M25_ERR_VALUE));
-  }
-  for (int64_t e = 0; e < nitems; ++e) {
-    const int type = d->pc_items[2 * e], id = d->pc_items[2 * e + 1];
-    if (type < 0 || type > 1 || id < 0 || (type == 0 && id >= d->nnear) || (type == 1 && id >= d->nfar))
-      return fail((set_error("m25_hmat_create: bad preconditioner item"), M25_ERR_VALUE));
   }
   const int64_t cells = (int64_t)geom->nblocks * geom->nt;
   for (int64_t q = 0; q < d->nkeys; ++q)
@@ -1090,10 +1202,12 @@ extern "C" int m25_hmat_assemble(m25_hmat* h, m25_greens* gr, double zs_re, doub
   if (!dense.empty())
     far_dense_kernel<<<(unsigned)dense.size(), 256, 0, st>>>(t, h->rules, h->lev, h->fb, h->dense_ids, h->dense_pool);
   // preconditioner: the diagonal blocks and their LU
-  diag_kernel<<<h->npc, 256, 0, st>>>(h->pc, h->pc_off, h->pc_items, h->pc_via_off, h->pc_via, h->pc_doff, h->nv,
-                                      h->near, h->near_off, h->Zn, h->fb, h->pool, h->dense_pool, h->ZxbT, h->Zxx,
-                                      h->D);
-  ginv_kernel<<<h->npc, 256, 0, st>>>(h->pc, h->pc_via_off, h->pc_doff, h->D);
+  wscale_kernel<<<(h->n + 255) / 256, 256, 0, st>>>(h->nb, h->n, h->nv, h->row_leaf, h->self_near, h->near,
+                                                    h->near_off, h->Zn, h->Zxx, h->wsc);
+  diag_kernel<<<h->npc, 256, 0, st>>>(h->pc_off, h->pc_gidx, h->pc_item_off, h->pc_items, h->pc_doff, h->nb, h->nv,
+                                      h->nnear, h->leaf_lo, h->near_off, h->Zn, h->fb, h->pool, h->dense_pool, h->ZxbT,
+                                      h->Zxx, h->D);
+  ginv_kernel<<<h->npc, 256, 0, st>>>(h->pc_off, h->pc_doff, h->D);
   if (cudaGetLastError() != cudaSuccess) {
     set_error("m25_hmat_assemble: launch failed");
     return done(M25_ERR_CUDA);
@@ -1177,7 +1291,8 @@ extern "C" int m25_hmat_solve(m25_hmat* h, int32_t nrhs, const double* B, double
   for (int c = 0; c < nrhs; ++c) {
     for (int i = 0; i < n; ++i) col[i] = cplx(B[2 * ((int64_t)i * nrhs + c)], B[2 * ((int64_t)i * nrhs + c) + 1]);
     M25_CUDA(cudaMemcpyAsync(h->w, col.data(), sizeof(zd) * n, cudaMemcpyHostToDevice, st));
-    perm_in_kernel<<<g, 256, 0, st>>>(h->nb, n, h->perm, h->w, h->bv);
+    perm_in_kernel<<<g, 256, 0, st>>>(h->nb, n, h->perm, h->w, h->zv);
+    vscale_kernel<<<g, 256, 0, st>>>(h->bv, h->zv, h->wsc, n, 0);  // the scaled system's right-hand side W b
     M25_CUDA(cudaMemsetAsync(h->xv, 0, sizeof(zd) * n, st));
     norm_kernel<<<1, 1024, 0, st>>>(h->bv, n, h->nrm);
     double bnorm = 0.0;
@@ -1192,7 +1307,7 @@ extern "C" int m25_hmat_solve(m25_hmat* h, int32_t nrhs, const double* B, double
         if (cyc == 0) {
           M25_CUDA(cudaMemcpyAsync(h->w, h->bv, sizeof(zd) * n, cudaMemcpyDeviceToDevice, st));
         } else {
-          if ((rc = apply(h, h->xv, h->zv))) return rc;
+          if ((rc = sapply(h, h->xv, h->zv))) return rc;
           sub_kernel<<<g, 256, 0, st>>>(h->w, h->bv, h->zv, n);
         }
         norm_kernel<<<1, 1024, 0, st>>>(h->w, n, h->nrm);
@@ -1210,8 +1325,8 @@ extern "C" int m25_hmat_solve(m25_hmat* h, int32_t nrhs, const double* B, double
         int j = 0;
         for (; j < restart; ++j) {
           // z_j = M^-1 v_j (kept: flexible GMRES), w = A z_j orthogonalised twice against v_0 .. v_j
-          if ((rc = precond(h, h->Vb + (int64_t)j * ldv, h->Zb + (int64_t)j * ldv))) return rc;
-          if ((rc = apply(h, h->Zb + (int64_t)j * ldv, h->w))) return rc;
+          if ((rc = sprecond(h, h->Vb + (int64_t)j * ldv, h->Zb + (int64_t)j * ldv))) return rc;
+          if ((rc = sapply(h, h->Zb + (int64_t)j * ldv, h->w))) return rc;
           for (int pass = 0; pass < 2; ++pass) {
             dots_kernel<<<j + 1, 256, 0, st>>>(h->Vb, ldv, n, h->w, h->hv + pass * (restart + 2));
             combine_kernel<<<g, 256, 0, st>>>(h->w, h->Vb, ldv, j + 1, n, h->hv + pass * (restart + 2), -1.0);
@@ -1262,8 +1377,8 @@ extern "C" int m25_hmat_solve(m25_hmat* h, int32_t nrhs, const double* B, double
         combine_kernel<<<g, 256, 0, st>>>(h->xv, h->Zb, ldv, k, n, h->hv, 1.0);
         M25_CHECK_LAUNCH();
       }
-      // the true residual
-      if ((rc = apply(h, h->xv, h->zv))) return rc;
+      // the true residual (of the scaled system)
+      if ((rc = sapply(h, h->xv, h->zv))) return rc;
       sub_kernel<<<g, 256, 0, st>>>(h->w, h->bv, h->zv, n);
       norm_kernel<<<1, 1024, 0, st>>>(h->w, n, h->nrm);
       double rn = 0.0;
@@ -1271,7 +1386,8 @@ extern "C" int m25_hmat_solve(m25_hmat* h, int32_t nrhs, const double* B, double
       M25_CUDA(cudaStreamSynchronize(st));
       rel = rn / bnorm;
     }
-    perm_out_kernel<<<g, 256, 0, st>>>(h->nb, n, h->perm, h->xv, h->zv);
+    vscale_kernel<<<g, 256, 0, st>>>(h->w, h->xv, h->wsc, n, 0);  // x = W x~
+    perm_out_kernel<<<g, 256, 0, st>>>(h->nb, n, h->perm, h->w, h->zv);
     M25_CHECK_LAUNCH();
     M25_CUDA(cudaMemcpyAsync(col.data(), h->zv, sizeof(zd) * n, cudaMemcpyDeviceToHost, st));
     M25_CUDA(cudaStreamSynchronize(st));

@@ -73,8 +73,8 @@ class HmatDesc(C.Structure):
                 ("nleaf", C.c_int32), ("leaf_lo", _i32p), ("nnear", C.c_int32), ("near", _i32p),
                 ("nfar", C.c_int32), ("far", _i32p), ("far_cen", _i32p), ("ent_off", _i64p), ("ent", _i32p),
                 ("nkeys", C.c_int64), ("keys", _i64p), ("npblk", C.c_int32), ("pblk", _i32p), ("npc", C.c_int32),
-                ("pc", _i32p), ("pc_off", _i64p), ("pc_items", _i32p), ("pc_via_off", _i64p), ("pc_via", _i32p),
-                ("tol", C.c_double), ("kcap", C.c_int32)]
+                ("pc_off", _i64p), ("pc_gidx", _i32p), ("pc_own", C.POINTER(C.c_int8)), ("pc_item_off", _i64p),
+                ("pc_items", _i32p), ("tol", C.c_double), ("kcap", C.c_int32)]
 
 
 _lib = None

@@ -24,12 +24,14 @@ Here (the host part; the device part is csrc/hmatrix.cu):
   low rank within min(m, n) / 3 terms (or `kcap` terms, the storage bound)
   are stored as they are. The ACA factors are not recompressed (QR + SVD,
   hmatrix.py:137-142): that would lower their rank, not their error;
-- preconditioner: block Jacobi over the largest clusters of at most
-  `prec_block` unknowns, each with the via unknowns whose pads it holds
-  (their diagonal blocks of the compressed operator, scaled to a unit
-  diagonal and inverted in complex64, so that applying it is one batched
-  matrix-vector product), in place of mom25d's sparse LU of the nearest
-  entries (hmatrix.py:523-560); GMRES (restart 200, at most 3 restarts,
+- preconditioner: restricted additive Schwarz in place of mom25d's sparse
+  LU of the nearest entries (hmatrix.py:523-560): the largest clusters of
+  at most `prec_block` unknowns, each extended by the leaves its own leaves
+  are near-coupled to (the most coupled first) and by the vias whose pads
+  those hold, up to `prec_max` unknowns; each block of the compressed operator is scaled to a unit
+  diagonal and inverted in complex64, so that applying the preconditioner
+  is one batched matrix-vector product, and each block writes only its own
+  unknowns (overlap=False: block Jacobi); GMRES (restart 200, at most 3 restarts,
   relative residual 1e-6) is flexible: it keeps M^-1 v_j for every basis
   vector, so the preconditioner's precision does not enter the solution.
 """
@@ -171,7 +173,7 @@ class Plan:
     """The host side of the compressed operator (no device work): the tree,
     the partition and the index lists the device kernels follow."""
 
-    def __init__(self, mesh, zl, blocks, leaf=48, eta=1.0, prec_block=512):
+    def __init__(self, mesh, zl, blocks, leaf=48, eta=1.0, prec_block=256, overlap=True, prec_max=640):
         m = mesh
         self.nb, self.nv = nb, nv = m.n_basis, len(m.via_segments)
         self.n = nb + nv
@@ -231,7 +233,9 @@ class Plan:
             tris = np.unique(np.concatenate([g[e] for g in segs for e in ("top_tris", "bottom_tris")
                                              if g[e] is not None]))
             self.pblk = np.unique(blk_of[tris]).astype(np.int32)
-        # preconditioner: the largest clusters of at most prec_block unknowns
+        # preconditioner: the largest clusters of at most prec_block unknowns,
+        # each extended by the leaves its own leaves are near-coupled to
+        # (overlap; restricted additive Schwarz: a block writes its own unknowns)
         pcs = []
         stack = [root]
         while stack:
@@ -241,75 +245,111 @@ class Plan:
             else:
                 stack.extend(reversed(c.children))
         pcs.sort(key=lambda c: c.lo)
-        items = [[] for _ in pcs]
-        pc_lo = np.array([c.lo for c in pcs], np.int64)
-
-        def owner(lo):
-            return int(np.searchsorted(pc_lo, lo, side="right")) - 1
-
+        nleaf = len(leaves)
+        # the source of every (row leaf, column leaf) block: near pair p, or far
+        # block f as rows (nnear + 2 f) or as its transpose (nnear + 2 f + 1)
+        srcmap = np.full((nleaf, nleaf), -1, np.int64)
         for p, (a, b) in enumerate(near):
-            k = owner(a.lo)
-            if pcs[k].lo <= b.lo and b.hi <= pcs[k].hi:
-                items[k].append((0, p))
+            srcmap[leaf_index[a.id], leaf_index[b.id]] = p
         for f, (a, b) in enumerate(self.far):
-            k = owner(a.lo)
-            if a.hi <= pcs[k].hi and pcs[k].lo <= b.lo and b.hi <= pcs[k].hi:
-                items[k].append((1, f))
-        pc = [(c.lo, c.size) for c in pcs]
-        # each via joins the block holding the RWG unknowns of its pad triangles (the first one's)
-        pcv = [[] for _ in pcs]
+            r0, r1 = np.searchsorted(lo_sorted, [a.lo, a.hi])
+            c0, c1 = np.searchsorted(lo_sorted, [b.lo, b.hi])
+            srcmap[r0:r1, c0:c1] = len(near) + 2 * f
+            srcmap[c0:c1, r0:r1] = len(near) + 2 * f + 1
+        if (srcmap < 0).any():
+            raise RuntimeError("the block partition does not cover every leaf pair")
+        nbr = [[] for _ in range(nleaf)]
+        for a, b in near:
+            nbr[leaf_index[a.id]].append(leaf_index[b.id])
+        # each via belongs with the RWG unknown of its first pad triangle
+        via_pos = np.full(nv, nb - 1, np.int64)
         if nv:
             ipos = np.empty(nb, np.int64)
             ipos[perm] = np.arange(nb)
             for v, g in enumerate(m.via_segments):
-                tris = [t for e in ("top_tris", "bottom_tris") if g[e] is not None for t in np.atleast_1d(g[e])]
-                k = len(pcs) - 1
-                for t in tris:
+                for t in (t for e in ("top_tris", "bottom_tris") if g[e] is not None for t in np.atleast_1d(g[e])):
                     bs = m.tri_basis[t][m.tri_basis[t] >= 0]
                     if bs.size:
-                        k = owner(int(ipos[bs[0]]))
+                        via_pos[v] = ipos[bs[0]]
                         break
-                pcv[k].append(v)
-        sizes = [s + len(v) for (_, s), v in zip(pc, pcv)]
-        if max(sizes) > 1024:
-            raise ValueError("a preconditioner block with its vias exceeds 1024 unknowns (lower prec_block)")
-        self.pc = np.array(pc, np.int32).reshape(-1, 2)
-        self.pc_off = np.zeros(len(pc) + 1, np.int64)
-        self.pc_off[1:] = np.cumsum([len(x) for x in items])
-        self.pc_items = np.array([x for it in items for x in it], np.int32).reshape(-1, 2)
-        self.pc_via_off = np.zeros(len(pc) + 1, np.int64)
-        self.pc_via_off[1:] = np.cumsum([len(v) for v in pcv])
-        self.pc_via = np.array([v for vs in pcv for v in vs], np.int32)
+        via_leaf = np.searchsorted(lo_sorted, via_pos, side="right") - 1
+        leaf_size = np.diff(self.leaf_lo).astype(np.int64)
+        gidx, own, items, offs, ioffs, sizes, overl = [], [], [], [0], [0], [], []
+        nvia_leaf = np.bincount(via_leaf, minlength=nleaf) if nv else np.zeros(nleaf, np.int64)
+        for c in pcs:
+            k0, k1 = np.searchsorted(lo_sorted, [c.lo, c.hi])
+            mine = list(range(k0, k1))
+            size = int(leaf_size[mine].sum() + nvia_leaf[mine].sum())
+            if size > 1024:
+                raise ValueError("a preconditioner block with its vias exceeds 1024 unknowns (lower prec_block)")
+            ext = set(mine)
+            if overlap:  # the halo: near-coupled leaves, the most coupled first, up to prec_max unknowns
+                cnt = {}
+                for k in mine:
+                    for b in nbr[k]:
+                        if b not in ext:
+                            cnt[b] = cnt.get(b, 0) + 1
+                for b in sorted(cnt, key=lambda b: (-cnt[b], b)):
+                    add = int(leaf_size[b] + nvia_leaf[b])
+                    if size + add <= prec_max:
+                        ext.add(b)
+                        size += add
+            ext = sorted(ext)
+            vias = np.nonzero(np.isin(via_leaf, ext))[0] if nv else np.zeros(0, np.int64)
+            ext = np.array(ext, np.int64)
+            lstart = np.concatenate([[0], np.cumsum(leaf_size[ext])])[:-1]
+            g = np.concatenate([np.arange(self.leaf_lo[k], self.leaf_lo[k + 1]) for k in ext] + [nb + vias])
+            o = np.concatenate([np.full(leaf_size[k], k0 <= k < k1) for k in ext] +
+                               [(via_leaf[vias] >= k0) & (via_leaf[vias] < k1)])
+            I, J = np.meshgrid(np.arange(ext.size), np.arange(ext.size), indexing="ij")
+            it = np.stack([srcmap[ext[I], ext[J]].ravel(), ext[I].ravel(), ext[J].ravel(),
+                           lstart[I].ravel(), lstart[J].ravel()], 1)
+            gidx.append(g)
+            own.append(o)
+            items.append(it)
+            offs.append(offs[-1] + g.size)
+            ioffs.append(ioffs[-1] + it.shape[0])
+            sizes.append(size)
+            overl.append(size - int(o.sum()))
+        self.pc_off = np.array(offs, np.int64)
+        self.pc_gidx = np.concatenate(gidx).astype(np.int32)
+        self.pc_own = np.concatenate(own).astype(np.int8)
+        self.pc_item_off = np.array(ioffs, np.int64)
+        self.pc_items = np.concatenate(items).astype(np.int32)
         self.prec_sizes = np.array(sizes)
+        self.prec_overlap = np.array(overl)
+        self.npc = len(pcs)
         self.stats = dict(clusters=len(self.nodes), leaves=len(leaves), near_pairs=len(near),
-                          far_blocks=len(self.far), near_field_pairs=int(self.keys.size), prec_blocks=len(pc))
+                          far_blocks=len(self.far), near_field_pairs=int(self.keys.size), prec_blocks=len(pcs),
+                          prec_size_max=int(self.prec_sizes.max()), prec_overlap_mean=float(self.prec_overlap.mean()))
 
 
 class HMatrix:
     """The compressed operator of a Solver's mesh on the solver's engine
     context. assemble(greens, zs) at a frequency, then matvec / solve."""
 
-    def __init__(self, solver, leaf=48, eta=1.0, tol=1e-4, kcap=96, prec_block=512):
+    def __init__(self, solver, leaf=48, eta=1.0, tol=1e-4, kcap=96, prec_block=256, overlap=True, prec_max=640):
         if solver._blocks_host is None:
             solver.geometry()
-        P = self.plan = Plan(solver.mesh, solver.zl, solver._blocks_host, leaf, eta, prec_block)
+        P = self.plan = Plan(solver.mesh, solver.zl, solver._blocks_host, leaf, eta, prec_block, overlap, prec_max)
         self.solver, self.tol = solver, tol
         self.nb, self.nv, self.n = P.nb, P.nv, P.n
         self._arrs = arrs = dict(
             perm=E.i32(P.perm), rules=E.f64(P.rules), lev=E.i32(P.lev), leaf_lo=E.i32(P.leaf_lo),
             near=E.i32(P.near_arr), far=E.i32(P.far_arr), far_cen=E.i32(P.far_cen),
             ent_off=np.ascontiguousarray(P.ent_off, np.int64), ent=E.i32(P.ent),
-            keys=np.ascontiguousarray(P.keys, np.int64), pblk=E.i32(P.pblk), pc=E.i32(P.pc),
-            pc_off=np.ascontiguousarray(P.pc_off, np.int64), pc_items=E.i32(P.pc_items),
-            pc_via_off=np.ascontiguousarray(P.pc_via_off, np.int64), pc_via=E.i32(P.pc_via))
-        i32, i64 = C.c_int32, C.c_int64
+            keys=np.ascontiguousarray(P.keys, np.int64), pblk=E.i32(P.pblk),
+            pc_off=np.ascontiguousarray(P.pc_off, np.int64), pc_gidx=E.i32(P.pc_gidx),
+            pc_own=np.ascontiguousarray(P.pc_own, np.int8), pc_item_off=np.ascontiguousarray(P.pc_item_off, np.int64),
+            pc_items=E.i32(P.pc_items))
+        i32, i64, i8 = C.c_int32, C.c_int64, C.c_int8
         d = E.HmatDesc(P.nb, P.nv, E.ptr(arrs["perm"], i32), E.ptr(arrs["rules"]), E.ptr(arrs["lev"], i32),
                        len(P.leaves), E.ptr(arrs["leaf_lo"], i32), len(P.near), E.ptr(arrs["near"], i32),
                        len(P.far), E.ptr(arrs["far"], i32), E.ptr(arrs["far_cen"], i32),
                        E.ptr(arrs["ent_off"], i64), E.ptr(arrs["ent"], i32), int(P.keys.size),
-                       E.ptr(arrs["keys"], i64), int(P.pblk.size), E.ptr(arrs["pblk"], i32), len(P.pc),
-                       E.ptr(arrs["pc"], i32), E.ptr(arrs["pc_off"], i64), E.ptr(arrs["pc_items"], i32),
-                       E.ptr(arrs["pc_via_off"], i64), E.ptr(arrs["pc_via"], i32), float(tol), int(kcap))
+                       E.ptr(arrs["keys"], i64), int(P.pblk.size), E.ptr(arrs["pblk"], i32), P.npc,
+                       E.ptr(arrs["pc_off"], i64), E.ptr(arrs["pc_gidx"], i32), E.ptr(arrs["pc_own"], i8),
+                       E.ptr(arrs["pc_item_off"], i64), E.ptr(arrs["pc_items"], i32), float(tol), int(kcap))
         self.ctx = solver.ctx
         h = C.c_void_p()
         E.check(self.ctx.lib.m25_hmat_create(self.ctx.h, solver.geometry().h, C.byref(d), C.byref(h)))
@@ -341,10 +381,12 @@ class HMatrix:
         return Y.T.reshape(x.shape)
 
     def solve(self, B, rtol=1e-6, restart=200, maxiter=3):
-        """Z^-1 B by preconditioned GMRES, one column at a time. A column
-        that stops above rtol is accepted when its true residual is within
-        the compression's accuracy (ACCEPT x tol, with a warning), else
-        RuntimeError (hmatrix.py:563-597)."""
+        """Z^-1 B by preconditioned GMRES, one column at a time, on the
+        symmetrically scaled system W Z W (W = |Z_ii|^-1/2: the via unknowns'
+        diagonal entries are ~1e10 times the RWG unknowns'), whose relative
+        residual is the stopping test. A column that stops above rtol is
+        accepted when its residual is within the compression's accuracy
+        (ACCEPT x tol, with a warning), else RuntimeError (hmatrix.py:563-597)."""
         B = np.asarray(B, np.complex128)
         Bm = np.ascontiguousarray(B.reshape(self.n, -1))
         X = np.zeros_like(Bm)
@@ -353,6 +395,8 @@ class HMatrix:
         res = np.zeros(k)
         E.check(self.ctx.lib.m25_hmat_solve(self._h.h, k, E.ptr(Bm.view(np.float64)), E.ptr(X.view(np.float64)),
                                             rtol, restart, maxiter, E.ptr(its, C.c_int32), E.ptr(res)))
+        self.stats["gmres_iterations"] = its.tolist()
+        self.stats["gmres_residuals"] = res.tolist()
         for c in range(k):
             if res[c] > rtol:
                 if res[c] > ACCEPT * self.tol:
@@ -361,8 +405,6 @@ class HMatrix:
                 warnings.warn(f"GMRES stopped at residual {res[c]:.1e} (target {rtol:g}) after {its[c]} "
                               f"iterations, rhs {c}: accepted (H-matrix tolerance {self.tol:g})",
                               RuntimeWarning, stacklevel=2)
-        self.stats["gmres_iterations"] = its.tolist()
-        self.stats["gmres_residuals"] = res.tolist()
         return X.reshape(B.shape)
 
     def summary(self):

@@ -43,7 +43,7 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=list(PRECISIONS))
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--freq", type=float, default=None, help="Hz (default: the workload's middle frequency)")
-    ap.add_argument("--prec-block", type=int, default=512, help="hmatrix mode: preconditioner block size")
+    ap.add_argument("--prec-block", type=int, default=256, help="hmatrix mode: preconditioner block size")
     ap.add_argument("--restart", type=int, default=200, help="hmatrix mode: GMRES restart length")
     ap.add_argument("--maxiter", type=int, default=3, help="hmatrix mode: GMRES restarts")
     args = ap.parse_args()

@@ -80,8 +80,8 @@ def test_plan_index_lists(name):
       is among the listed near-field pairs;
     - every row's items (near pairs, far blocks as rows, far blocks as
       columns) cover each column exactly once;
-    - every preconditioner block's items tile its diagonal block exactly once,
-      the blocks tile the unknowns and each via joins its pads' block;
+    - every unknown is written by one preconditioner block, and each block's
+      items tile its RWG part exactly once from blocks that hold them;
     - the pad blocks hold every via pad triangle."""
     m, P = _plan(name)
     nb, nt = P.nb, P.nt
@@ -110,31 +110,33 @@ def test_plan_index_lists(name):
                     assert c0 + off == lo and off + (hi - lo) <= nn
                     cnt[r0:r0 + mm] += 1
         assert np.all(cnt == 1), (k, np.unique(cnt))
-    for k, (p0, s) in enumerate(P.pc):
-        cnt = np.zeros((s, s), int)
-        for t, i in P.pc_items[P.pc_off[k]:P.pc_off[k + 1]]:
-            if t == 0:
-                a0, am, b0, bn = P.near_arr[i]
-                cnt[a0 - p0:a0 - p0 + am, b0 - p0:b0 - p0 + bn] += 1
+    # preconditioner blocks: every unknown written by exactly one block; a
+    # block's (row leaf, column leaf) items tile its RWG part exactly once,
+    # each from a source block that holds it; its vias follow its RWG unknowns
+    owned = np.zeros(P.n, int)
+    np.add.at(owned, P.pc_gidx[P.pc_own == 1], 1)
+    assert np.all(owned == 1)
+    lsz = np.diff(P.leaf_lo)
+    nnear = len(P.near_arr)
+    for k in range(P.npc):
+        g = P.pc_gidx[P.pc_off[k]:P.pc_off[k + 1]]
+        R = int((g < nb).sum())
+        assert np.all(g[:R] < nb) and np.all(g[R:] >= nb) and g.size <= 1024
+        cnt = np.zeros((R, R), int)
+        for src, li, lj, lr0, lc0 in P.pc_items[P.pc_item_off[k]:P.pc_item_off[k + 1]]:
+            assert np.array_equal(g[lr0:lr0 + lsz[li]], np.arange(P.leaf_lo[li], P.leaf_lo[li + 1]))
+            assert np.array_equal(g[lc0:lc0 + lsz[lj]], np.arange(P.leaf_lo[lj], P.leaf_lo[lj + 1]))
+            cnt[lr0:lr0 + lsz[li], lc0:lc0 + lsz[lj]] += 1
+            a0, b0 = P.leaf_lo[li], P.leaf_lo[lj]
+            if src < nnear:
+                assert tuple(P.near_arr[src]) == (a0, lsz[li], b0, lsz[lj])
             else:
-                r0, mm, c0, nn = P.far_arr[i]
-                cnt[r0 - p0:r0 - p0 + mm, c0 - p0:c0 - p0 + nn] += 1
-                cnt[c0 - p0:c0 - p0 + nn, r0 - p0:r0 - p0 + mm] += 1
+                f, o = divmod(src - nnear, 2)
+                r0, mm, c0, nn = P.far_arr[f]
+                if o:
+                    r0, mm, c0, nn = c0, nn, r0, mm
+                assert r0 <= a0 and a0 + lsz[li] <= r0 + mm and c0 <= b0 and b0 + lsz[lj] <= c0 + nn
         assert np.all(cnt == 1)
-    # the blocks' RWG ranges tile the tree order; every via sits in exactly one
-    # block, the one holding an RWG unknown of its first pad triangle
-    order = np.argsort(P.pc[:, 0])
-    starts, sizes = P.pc[order, 0], P.pc[order, 1]
-    assert starts[0] == 0 and np.array_equal(starts[1:], starts[:-1] + sizes[:-1]) and starts[-1] + sizes[-1] == nb
-    assert sorted(P.pc_via.tolist()) == list(range(P.nv))
-    ipos = np.empty(nb, int)
-    ipos[perm] = np.arange(nb)
-    for k, (p0, s) in enumerate(P.pc):
-        for v in P.pc_via[P.pc_via_off[k]:P.pc_via_off[k + 1]]:
-            g = m.via_segments[v]
-            t = next(np.atleast_1d(g[e])[0] for e in ("top_tris", "bottom_tris") if g[e] is not None)
-            bs = m.tri_basis[t][m.tri_basis[t] >= 0]
-            assert p0 <= ipos[bs[0]] < p0 + s
     assert P.prec_sizes.max() <= 1024
     if P.nv:
         pads = np.unique(np.concatenate([g[e] for g in m.via_segments for e in ("top_tris", "bottom_tris")
