@@ -36,7 +36,7 @@ def test_struct_layouts_match_header():
     # the ctypes mirrors follow the C structs field by field
     txt = open(os.path.join(ROOT, "include", "m25.h")).read()
     for cls, name in ((engine.MeshDesc, "m25_mesh_desc"), (engine.GreensDesc, "m25_greens_desc"),
-                      (engine.PortDesc, "m25_port_desc")):
+                      (engine.PortDesc, "m25_port_desc"), (engine.HmatDesc, "m25_hmat_desc")):
         body = re.search(r"typedef struct \{([^}]*)\}\s*" + name, txt, re.S).group(1)
         body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
         fields = []

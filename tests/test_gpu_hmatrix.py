@@ -133,6 +133,31 @@ def test_gmres_converges_on_the_via_transition(gpu):
         dense.close()
 
 
+def test_gcpw_converges_and_matches_reference(gpu):
+    """The via-fenced grounded CPW (N = 25284, 84 vias), mom25d's case for
+    the compressed solver: at 10.35 GHz GMRES reaches 1e-6 within mom25d's
+    600 iterations and S is within 1e-3 of mom25d's dense S (tests/golden/
+    gcpw.npz; the far blocks' 3-point rule moves this via mesh's S by ~4e-4,
+    as on the via transition)."""
+    path = os.path.join(GOLDEN, "gcpw.npz")
+    if not os.path.exists(path):
+        pytest.skip("no gcpw fixture")
+    g = np.load(path)
+    m, st, freqs, sol = _solver("gcpw", method="hmatrix")
+    try:
+        assert m.n_unknowns == int(g["N"])
+        f = g["freqs"][1:2]
+        r = sol.sweep(f)
+        d = np.abs(r.S[0] - g["S"][1]).max()
+        s = sol.hoperator().stats
+        print(f"gcpw: |dS| vs mom25d dense {d:.1e}, GMRES its {s['gmres_iterations']}, "
+              f"residuals {s['gmres_residuals']}, entries {(s['near_entries'] + s['far_entries']) / m.n_unknowns**2:.3f}")
+        assert max(s["gmres_residuals"]) <= 1e-6
+        assert d < 1e-3
+    finally:
+        sol.close()
+
+
 def test_auto_method(gpu):
     """"auto" keeps the dense path below HMATRIX_N unknowns, the compressed one above."""
     lay, st, m, _ = workloads.build(G, "tee")
