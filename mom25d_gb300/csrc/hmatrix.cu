@@ -274,12 +274,13 @@ __global__ void __launch_bounds__(256) far_dense_kernel(Tabs t, const double* __
   const FarB F = fb[ids[blockIdx.x]];
   zd* B = dpool + F.dense;
   zd* BT = B + (int64_t)F.m * F.n;
-  for (int64_t e = threadIdx.x; e < (int64_t)F.m * F.n; e += blockDim.x) {
-    const int i = (int)(e / F.n), j = (int)(e - (int64_t)i * F.n);
-    const zd z = far_entry(t, rules, lev, F.r0 + i, F.c0 + j, F.cen);
-    B[e] = z;
-    BT[(int64_t)j * F.m + i] = z;
-  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = wid; i < F.m; i += nw)  // one warp per row, the lanes along it
+    for (int j = lane; j < F.n; j += 32) {
+      const zd z = far_entry(t, rules, lev, F.r0 + i, F.c0 + j, F.cen);
+      B[(int64_t)i * F.n + j] = z;
+      BT[(int64_t)j * F.m + i] = z;
+    }
 }
 
 // Adaptive cross approximation with partial pivoting (Engine/mom25d/
@@ -603,10 +604,9 @@ __global__ void __launch_bounds__(256) ginv_kernel(const int64_t* __restrict__ p
     w[i] = m > 0.f ? rsqrtf(m) : 1.f;
   }
   __syncthreads();
-  for (int64_t e = threadIdx.x; e < (int64_t)S * S; e += blockDim.x) {
-    const int r = (int)(e / S), j = (int)(e - (int64_t)r * S);
-    A[e] = A[e] * (w[r] * w[j]);
-  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int r = wid; r < S; r += nw)
+    for (int j = lane; j < S; j += 32) A[(int64_t)r * S + j] = A[(int64_t)r * S + j] * (w[r] * w[j]);
   __syncthreads();
   for (int c = 0; c < S; ++c) {
     double best = -1.0;
@@ -637,11 +637,12 @@ __global__ void __launch_bounds__(256) ginv_kernel(const int64_t* __restrict__ p
       A[(int64_t)c * S + j] = j == c ? d : A[(int64_t)c * S + j] * d;
     for (int r = threadIdx.x; r < S; r += blockDim.x) fcol[r] = A[(int64_t)r * S + c];
     __syncthreads();
-    for (int64_t e = threadIdx.x; e < (int64_t)S * S; e += blockDim.x) {
-      const int r = (int)(e / S), j = (int)(e - (int64_t)r * S);
+    for (int r = wid; r < S; r += nw) {  // one warp per row, the lanes along it
       if (r == c) continue;
       const zf f = fcol[r];
-      A[e] = j == c ? -(f * d) : A[e] - f * A[(int64_t)c * S + j];
+      zf* Ar = A + (int64_t)r * S;
+      const zf* Ac = A + (int64_t)c * S;
+      for (int j = lane; j < S; j += 32) Ar[j] = j == c ? -(f * d) : Ar[j] - f * Ac[j];
     }
     __syncthreads();
   }
@@ -655,10 +656,8 @@ __global__ void __launch_bounds__(256) ginv_kernel(const int64_t* __restrict__ p
       }
     __syncthreads();
   }
-  for (int64_t e = threadIdx.x; e < (int64_t)S * S; e += blockDim.x) {
-    const int r = (int)(e / S), j = (int)(e - (int64_t)r * S);
-    A[e] = A[e] * (w[r] * w[j]);
-  }
+  for (int r = wid; r < S; r += nw)
+    for (int j = lane; j < S; j += 32) A[(int64_t)r * S + j] = A[(int64_t)r * S + j] * (w[r] * w[j]);
 }
 
 // out = D_k^-1 in on the unknowns block k owns (complex64 inverse, fp32 sums), one warp per row
