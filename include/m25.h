@@ -263,12 +263,12 @@ int m25_lu_factor(m25_ctx* ctx, int32_t n, int precision, void* A, int64_t lda, 
  * the process exits; it limits n to M25_NOALLOC_MAX_N (larger n is rejected
  * with M25_ERR_VALUE) and the device to at most 192 SMs. The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress, with that
- * device current); make that first call before any stream capture. All calls
- * share the one array: calls that overlap on the GPU (other threads, other
- * streams) race and must be serialised by the caller. info[0] = 0, info[1] =
- * the first zero pivot (1-based) or 0. Every call blocks the calling thread
- * until `stream` has finished the solve: the factorisation reads its pivot
- * flags and the triangular solves their error word on the host. */
+ * device current). All calls share the one array: calls that overlap on the
+ * GPU (other threads, other streams) race and must be serialised by the
+ * caller. info[0] = 0, info[1] = the first zero pivot (1-based) or 0. Every
+ * call blocks the calling thread until `stream` has finished the solve (the
+ * factorisation reads its pivot flags and the triangular solves their error
+ * word on the host), so no call can be captured into a CUDA graph. */
 #define M25_NOALLOC_MAX_N 24576
 #define M25_NOALLOC_SCRATCH_BYTES (512 * 1024)
 int m25_dense_solve_noalloc(int32_t n, int32_t nrhs, void* Z, const void* B, void* X, int32_t* ipiv, void* stream,
