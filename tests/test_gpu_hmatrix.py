@@ -158,6 +158,24 @@ def test_gcpw_converges_and_matches_reference(gpu):
         sol.close()
 
 
+@pytest.mark.parametrize("name", ["lumped_line", "gap_port_line", "via_port_line"])
+def test_loads_and_internal_ports_through_the_compressed_solve(gpu, name):
+    """Lumped loads (Woodbury on the host) and internal ports take the
+    compressed solve's columns as they take the dense solve's: S within 2e-4
+    of mom25d's dense S (tests/golden), as the compressed sweep's bar."""
+    from conftest import golden
+
+    g = golden(name)
+    m, st, freqs, sol = _solver(name, method="hmatrix")
+    try:
+        r = sol.sweep(g["freqs"])
+        d = np.abs(r.S - g["S"]).max()
+        print(name, f"|dS| vs mom25d dense {d:.1e}", sol.hoperator().stats["gmres_iterations"])
+        assert r.S.shape == g["S"].shape and d < 2e-4
+    finally:
+        sol.close()
+
+
 def test_auto_method(gpu):
     """"auto" keeps the dense path below HMATRIX_N unknowns, the compressed one above."""
     lay, st, m, _ = workloads.build(G, "tee")
