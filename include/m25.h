@@ -180,6 +180,7 @@ typedef struct {
   double sur_near;            /* [m] radii below it are always integrated */
   int32_t sur_stride;         /* 2 .. 64 */
   double sur_tol;
+  int32_t top_pec;            /* 1: a PEC cover on the top layer (no level on it); 0: air above */
 } m25_greens_desc;
 
 int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* desc, m25_greens** out);

@@ -22,6 +22,7 @@ struct StackDev {
   int il[kMaxLev];
   double zl[kMaxLev];
   double k0, h;
+  int top_pec;                     // a PEC cover on the top layer (layered.py:257-275)
   zd lead_c[3][kMaxLev][kMaxLev];  // c_A, c_V, c_W per (observer, source)
   zd kx[2][kMaxLev][kMaxLev];      // k of the A and the V/W leading terms
   double dz[kMaxLev][kMaxLev];
@@ -77,10 +78,15 @@ __device__ void layered_spectral(const StackDev& S, zd kr, zd g[3][kMaxLev][kMax
       zd yl = ydn[k - 1], yk = y[k - 1], tk = T[k - 1];
       ydn[k] = yk * (yl + yk * tk) / (yk + yl * tk);
     }
-    yup[N] = yair;
+    yup[N] = S.top_pec ? zd(0.0) : yair;  // (unused under a cover: no level on it)
     for (int k = N - 1; k >= 1; --k) {
-      zd yk = y[k], tk = T[k], yl = yup[k + 1];
-      yup[k] = yk * (yl + yk * tk) / (yk + yl * tk);
+      zd yk = y[k], tk = T[k];
+      if (S.top_pec && k == N - 1) {
+        yup[k] = yk / tk;  // layer N shorted by the cover
+      } else {
+        zd yl = yup[k + 1];
+        yup[k] = yk * (yl + yk * tk) / (yk + yl * tk);
+      }
     }
     for (int l = 0; l < L; ++l) {
       zd* V = Vmode[mode][l];
@@ -88,7 +94,10 @@ __device__ void layered_spectral(const StackDev& S, zd kr, zd g[3][kMaxLev][kMax
       int s = S.il[l];
       V[s] = zd(1.0) / (ydn[s] + yup[s]);
       for (int k = s; k >= 2; --k) V[k - 1] = V[k] * Sh[k - 1] / (zd(1.0) + ydn[k - 1] / y[k - 1] * T[k - 1]);
-      for (int k = s; k < N; ++k) V[k + 1] = V[k] * Sh[k] / (zd(1.0) + yup[k + 1] / y[k] * T[k]);
+      for (int k = s; k < N; ++k) {
+        if (S.top_pec && k + 1 == N) break;  // V_N = 0 on the cover
+        V[k + 1] = V[k] * Sh[k] / (zd(1.0) + yup[k + 1] / y[k] * T[k]);
+      }
     }
   }
   const double k02 = S.k0 * S.k0;
@@ -770,16 +779,21 @@ extern "C" int m25_greens_create(m25_ctx* ctx, const m25_greens_desc* d, m25_gre
     return M25_ERR_VALUE;
   }
   for (int l = 0; l < d->nlev; ++l)
-    if (d->lev_iface[l] < 1 || d->lev_iface[l] > d->nlayer) {
-      set_error("m25_greens_create: level interface out of range");
+    if (d->lev_iface[l] < 1 || d->lev_iface[l] > d->nlayer || (d->top_pec && d->lev_iface[l] == d->nlayer)) {
+      set_error("m25_greens_create: level interface out of range (or on the PEC cover)");
       return M25_ERR_VALUE;
     }
+  if (d->top_pec && (d->single || d->nlayer < 2)) {
+    set_error("m25_greens_create: a PEC cover needs a layer above the metal");
+    return M25_ERR_VALUE;
+  }
   M25_CUDA(cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
   StackDev S{};
   S.nlayer = d->nlayer;
   S.nlev = d->nlev;
   S.single = d->single;
+  S.top_pec = d->top_pec ? 1 : 0;
   double omega = 2.0 * kPi * d->freq;
   S.k0 = omega / kC0;
   S.h = d->stack_h;

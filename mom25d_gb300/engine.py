@@ -55,7 +55,7 @@ class GreensDesc(C.Structure):
                 ("kr", _f64p), ("wr", _f64p), ("nrho", C.c_int32), ("rho", _f64p), ("kbig", C.c_double),
                 ("surrogate", C.c_void_p), ("sur_a", C.c_double), ("sur_rho_ref", C.c_double),
                 ("sur_fmin", C.c_double), ("sur_fmax", C.c_double), ("sur_scale", _f64p), ("sur_near", C.c_double),
-                ("sur_stride", C.c_int32), ("sur_tol", C.c_double)]
+                ("sur_stride", C.c_int32), ("sur_tol", C.c_double), ("top_pec", C.c_int32)]
 
 
 class PortDesc(C.Structure):

@@ -129,6 +129,7 @@ class Greens:
                          E.ptr(arrs["il"], C.c_int32), E.ptr(arrs["lz"]), int(single), zg.real, zg.imag,
                          float(st.z[-1]), kc.size, kr.size, E.ptr(arrs["kc"]), E.ptr(arrs["wc"]), E.ptr(arrs["kr"]),
                          E.ptr(arrs["wr"]), self.rho.size, E.ptr(arrs["rho"]), 15.0 / t.min())
+        d.top_pec = int(getattr(st, "top", "air") == "pec")
         sur = getattr(solver, "surrogate", None) if surrogate else None
         self.surrogate_used = None
         if sur is not None and sur.covers(self.freq):
@@ -309,7 +310,7 @@ class Solver:
 
     mesh      : a Mesh with RWG data, via segments and port cuts (this
                 package's grid mesher, or mom25d's own Mesh object)
-    substrate : Substrate or Stackup (open top, no inner planes)
+    substrate : Substrate or Stackup (air above or a PEC cover; no inner planes)
     method    : "dense" (Z + LU), "hmatrix" (compressed Z + GMRES,
                 mom25d_gb300/hmatrix.py) or "auto": hmatrix above HMATRIX_N
                 unknowns (where the dense working set no longer fits beside
@@ -346,6 +347,9 @@ class Solver:
             raise ValueError(f"mesh layers {missing} are not metal levels of the stackup {list(st.metals)}")
         if getattr(mesh, "n_frills", 0) or getattr(mesh, "n_ap", 0) or getattr(mesh, "n_walls", 0):
             raise ValueError("antipads, plane apertures and thick metal are not part of this engine")
+        if st.top == "pec" and len(getattr(mesh, "via_segments", [])):
+            raise ValueError("vias under a PEC cover (a closed section: parallel-plate via modes, "
+                             "mom25d solver.py:181-188) are not part of this engine")
         self.single = len(st.layers) == 1 and st.top == "air" and list(mesh.layer_names) == ["top"]
         self.zl = np.array([st.level_z(n) for n in mesh.layer_names])
         order = sorted(list(mesh.layer_names), key=st.level_z)

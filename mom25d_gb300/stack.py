@@ -1,7 +1,8 @@
 """Dielectric stack descriptions: Substrate (one grounded slab) and Stackup
 (layers bottom to top with named metal levels), as mom25d/solver.py:42-76
-and mom25d/layered.py:52-180 define them. Inner PEC planes are not part of
-this engine (every configuration it serves is an open, air-topped stack)."""
+and mom25d/layered.py:52-180 define them: air above the top layer
+(top="air") or a PEC cover on it (top="pec", e.g. a stripline). Inner PEC
+planes (sections) are not part of this engine."""
 
 from dataclasses import dataclass
 
@@ -46,13 +47,15 @@ class Stackup:
         n = len(self.layers)
         if self.metals is None:
             self.metals = {"top": n}
-        if self.top != "air":
-            raise ValueError("this engine supports open (top='air') stacks only")
+        if self.top not in ("air", "pec"):
+            raise ValueError("top must be 'air' or 'pec'")
         for name, k in self.metals.items():
             if name == GND:
                 raise ValueError("'gnd' is reserved for the ground plane")
             if not 1 <= k <= n:
                 raise ValueError(f"metal level {name}: interface {k} not in 1..{n}")
+            if k == n and self.top == "pec":
+                raise ValueError(f"metal level {name} would lie on the PEC cover")
         self.planes = dict(self.planes or {})
         if self.planes:
             raise ValueError("inner PEC planes are not part of this engine")
@@ -85,7 +88,7 @@ class Stackup:
         return float(t @ e / t.sum())
 
     def covered(self, name):
-        return self.metals[name] < len(self.layers)
+        return self.metals[name] < len(self.layers) or self.top == "pec"
 
     def surface_impedance(self, freq, t=None):
         return surface_impedance(freq, self.sigma, self.t if t is None else t)

@@ -19,6 +19,8 @@ returns (layout, stack, mesh keyword arguments, frequencies [Hz]).
   component_line  three line sections, a 2-port S-parameter block across two open gaps
   gap_port_line   a series gap in a line with an internal gap port across it
   via_port_line   a line with a via to ground fed by an internal via port
+  stripline  a centred 0.4 mm stripline under a PEC cover, 2 x 0.254 mm eps_r 3.66 (mom25d's
+             Engine/tests/test_multilayer.py:59-76 geometry), 2 and 10 GHz
 """
 
 import numpy as np
@@ -215,3 +217,20 @@ def via_port_line(api):
 
 
 BUILDERS.update(gap_port_line=gap_port_line, via_port_line=via_port_line)
+
+
+def stripline(api):
+    """A 4 mm centred stripline under a PEC cover: the 0.4 mm strip on the
+    interface of two 0.254 mm eps_r 3.66 layers (mom25d's stripline check,
+    Engine/tests/test_multilayer.py:59-76: eps_eff = eps_r, Z0 of the
+    zero-thickness strip from K(k) / K(k'))."""
+    er, hh, W = 3.66, 0.254 * mm, 0.4 * mm
+    lay = api.Layout()
+    lay.add_rect(-2 * mm, -W / 2, 2 * mm, W / 2, layer="mid")
+    lay.add_port("P1", (-2 * mm, 0), "-x", W, 6 * mm, layer="mid")
+    lay.add_port("P2", (2 * mm, 0), "+x", W, 6 * mm, layer="mid")
+    st = api.Stackup([api.Dielectric(hh, er), api.Dielectric(hh, er)], {"mid": 1}, top="pec")
+    return lay, st, dict(max_cell=0.25 * mm, edge_cell=0.04 * mm), np.array([2.0, 10.0]) * GHz
+
+
+BUILDERS.update(stripline=stripline)

@@ -208,9 +208,11 @@ class LayeredKernels:
     (mom25d/layered.py:217-405): TE/TM line voltages per level, leading
     c e^{-jkR}/(4 pi R) terms, remainder tabulated per level pair."""
 
-    def __init__(self, freq, layers, il, zl, rho_max=0.1, zs_ground=0.0):
+    def __init__(self, freq, layers, il, zl, rho_max=0.1, zs_ground=0.0, top="air"):
         """layers [(t, eps_r, tand)] bottom to top; il: interface index of each
-        mesh level (1..N); zl: its height."""
+        mesh level (1..N); zl: its height; top: "air" or "pec" (a cover on
+        the top layer, mom25d/layered.py:257-275)."""
+        self.pec_top = top == "pec"
         self.freq = freq
         self.omega = 2 * np.pi * freq
         self.k0 = k0 = self.omega / C0
@@ -266,16 +268,23 @@ class LayeredKernels:
                 yl, yk, tk = ydn[k - 1], y[k - 1], T[k - 1]
                 ydn[k] = yk * (yl + yk * tk) / (yk + yl * tk)
             yup = np.empty((N + 1, K), complex)
-            yup[N] = yair
+            if not self.pec_top:
+                yup[N] = yair
             for k in range(N - 1, 0, -1):
-                yk, tk, yl = y[k], T[k], yup[k + 1]
-                yup[k] = yk * (yl + yk * tk) / (yk + yl * tk)
+                yk, tk = y[k], T[k]
+                if k == N - 1 and self.pec_top:  # layer N shorted by the cover
+                    yup[k] = yk / tk
+                else:
+                    yl = yup[k + 1]
+                    yup[k] = yk * (yl + yk * tk) / (yk + yl * tk)
             V = np.zeros((L, N + 1, K), complex)
             for l, s in enumerate(self.il):
                 V[l, s] = 1.0 / (ydn[s] + yup[s])
                 for k in range(s, 1, -1):
                     V[l, k - 1] = V[l, k] * Sh[k - 1] / (1 + ydn[k - 1] / y[k - 1] * T[k - 1])
                 for k in range(s, N):
+                    if k + 1 == N and self.pec_top:
+                        break  # V_N = 0 on the cover
                     V[l, k + 1] = V[l, k] * Sh[k] / (1 + yup[k + 1] / y[k] * T[k])
             out.append(V)
         return out[0], out[1], u

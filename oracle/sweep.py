@@ -51,7 +51,8 @@ def make_kernels(stack, mesh, freq, rho_max):
         d = stack.layers[0]
         return K.SlabKernels(freq, d.eps_r, d.t, d.tand, rho_max, zs_ground=zg)
     il = [stack.metals[n] for n in mesh.layer_names]
-    return K.LayeredKernels(freq, [(d.t, d.eps_r, d.tand) for d in stack.layers], il, zl, rho_max, zs_ground=zg)
+    return K.LayeredKernels(freq, [(d.t, d.eps_r, d.tand) for d in stack.layers], il, zl, rho_max, zs_ground=zg,
+                            top=getattr(stack, "top", "air"))
 
 
 class Geometry:

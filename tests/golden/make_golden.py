@@ -454,6 +454,7 @@ def main():
     ap.add_argument("--variants", action="store_true", help="only band-pass variants 3, 7, 11 and 14")
     ap.add_argument("--lossless", action="store_true", help="only the lossless line (mom25d's bounded beta fit)")
     ap.add_argument("--iports", action="store_true", help="only the internal-port cases (gap port, via port)")
+    ap.add_argument("--stripline", action="store_true", help="only the stripline under a PEC cover")
     ap.add_argument("--gcpw", action="store_true",
                     help="only the grounded CPW (N = 25284: ~30 GB of memory, ~20 min per frequency)")
     args = ap.parse_args()
@@ -482,6 +483,9 @@ def main():
         return
     if args.lossless:
         case("line_lossless", zrows=np.arange(0, 546, 37), sweep_freqs=[2e9, 5e9, 7e9])
+        return
+    if args.stripline:
+        case("stripline", zrows=np.arange(0, 200, 23))
         return
     if args.variants:
         for k in (3, 7, 11, 14):

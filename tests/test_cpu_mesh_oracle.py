@@ -27,7 +27,7 @@ def mesh_digest(m):
 
 
 @pytest.mark.parametrize("name", ["line", "line_lossless", "shunt_via", "tee", "via", "lpf", "bandpass_0",
-                                  "bandpass_3", "bandpass_7", "bandpass_11", "bandpass_14", "gcpw"])
+                                  "bandpass_3", "bandpass_7", "bandpass_11", "bandpass_14", "gcpw", "stripline"])
 def test_mesh_identical_to_reference(name):
     import os
 
@@ -172,3 +172,30 @@ def test_oracle_lossless_sweep_matches_reference():
     # mom25d's own beta moves within the floor with its BLAS thread count
     assert (np.abs(gam - g["gamma"]) / np.abs(g["gamma"])).max() < 3 * gamma_floor("line_lossless")
     assert np.abs(S - g["S"]).max() < fp64_tol("line_lossless")
+
+
+def test_stripline_tables_equal_reference():
+    """The oracle's layered kernels under a PEC cover (a shorted top layer,
+    V = 0 on the cover; mom25d/layered.py:257-275) against mom25d's own
+    tables of the stripline stack (tests/golden/stripline.npz): the leading
+    coefficients and the smooth parts' spline values at the radii."""
+    import os
+
+    from conftest import GOLDEN
+
+    if not os.path.exists(os.path.join(GOLDEN, "stripline.npz")):
+        pytest.skip("no stripline fixture")
+    g = golden("stripline")
+    lay, st, m, _ = workloads.build(G, "stripline")
+    zl = [st.level_z(n) for n in m.layer_names]
+    lk = K.LayeredKernels(float(g["f0"]), [(d.t, d.eps_r, d.tand) for d in st.layers],
+                          [st.metals[n] for n in m.layer_names], zl, rho_max=float(g["rho_max"]), top="pec")
+    np.testing.assert_array_equal(lk.rho_tab, g["rho_tab"])
+    p = lk.pairs[0, 0]
+    np.testing.assert_allclose([p.cA, p.cV, p.cW], g["pair00_c"], rtol=1e-12, atol=1e-15)
+    # mom25d's spline coefficients evaluated at the knots: the tabulated smooth parts
+    c = g["pair00_spl_c"]  # (4, n - 1, 2) PPoly coefficients of [S_A, S_V]
+    ref_SA, ref_SV = c[3, :, 0], c[3, :, 1]
+    mine = p.spl(g["rho_tab"][:-1])
+    for k, ref in ((0, ref_SA), (1, ref_SV)):
+        assert np.abs(mine[:, k] - ref).max() <= 1e-10 * np.abs(ref).max(), k

@@ -64,8 +64,11 @@ def test_slab_tables_match_oracle(line, f):
     g.close()
 
 
-def test_layered_tables_match_oracle(gpu):
-    lay, st, m, _ = build("via")
+@pytest.mark.parametrize("name", ["via", "stripline"])
+def test_layered_tables_match_oracle(gpu, name):
+    """Two levels with air above (via transition), and one level under a PEC
+    cover (stripline)."""
+    lay, st, m, _ = build(name)
     sol = Solver(m, st, verbose=False)
     ref = O.Sweep(m, st)
     f = 10e9

@@ -64,7 +64,7 @@ def _build(name):
 
 
 VARIANTS = [f"bandpass_{k}" for k in (0, 3, 7, 11, 14)]
-STAGE_CASES = ["line", "shunt_via", "tee", "via", "lpf"] + VARIANTS
+STAGE_CASES = ["line", "shunt_via", "tee", "via", "lpf", "stripline"] + VARIANTS
 
 
 @pytest.mark.parametrize("name", STAGE_CASES)
@@ -157,3 +157,34 @@ def test_gcpw_prefit_stages_match_reference(gpu):
         assert np.abs(np.diag(Z) - g["Z_diag"]).max() <= 1e-11 * np.abs(g["Z_diag"]).max()
     finally:
         sol.close()
+
+
+def test_stripline_under_a_pec_cover(gpu):
+    """The centred stripline under a PEC cover (mom25d's Engine/tests/
+    test_multilayer.py:59-76): S of the fp64 path within three fit floors of
+    mom25d's and the mixed path within 1e-5 (tests/golden/stripline.npz), and
+    mom25d's physics checks: eps_eff = eps_r within 3e-3, the line impedance
+    within 1.5 % of the zero-thickness formula eta0 / (4 sqrt(eps_r)) K(k) /
+    K(k'), k = sech(pi W / 2 b), and |S11| < 5e-3."""
+    from scipy.special import ellipk
+
+    if not _have("stripline"):
+        pytest.skip("no fixture stripline")
+    g = golden("stripline")
+    lay, st, m, _ = _build("stripline")
+    er, hh, W = 3.66, 0.254e-3, 0.4e-3
+    b = 2 * hh
+    k = 1 / np.cosh(np.pi * W / (2 * b))
+    z0 = 376.730313668 / (4 * np.sqrt(er)) * ellipk(k ** 2) / ellipk(1 - k ** 2)
+    for prec, tol in (("fp64", s_tol("stripline")), ("mixed", 1e-5)):
+        sol = Solver(m, st, verbose=False, precision=prec)
+        try:
+            r = sol.sweep(g["freqs"])
+            dS = np.abs(r.S - g["S"]).max()
+            print("stripline", prec, f"|dS| {dS:.1e}", r.eeff[:, 0], r.z0_line[:, 0].real, z0)
+            assert dS < tol, (prec, dS)
+            np.testing.assert_allclose(r.eeff[:, 0], er, rtol=3e-3)
+            np.testing.assert_allclose(r.z0_line[:, 0].real, z0, rtol=0.015)
+            assert np.all(np.abs(r.S[:, 0, 0]) < 5e-3)
+        finally:
+            sol.close()
