@@ -319,6 +319,31 @@ def run_ours(args, rank, world, local):
             sur_arm["max_dS_vs_fp64"] = float(np.abs(r3.S[idx] - r64.S).max())
         sur.close()
         s3.close()
+    # the compressed operator (method="hmatrix") on the same mesh: one point
+    # at the band's middle frequency after one untimed point (its tree,
+    # partition and index lists built then), against the mixed path's S there
+    hm_arm = None
+    if world == 1 and not args.no_hmatrix:
+        fm = float(freqs[len(freqs) // 2])
+        sh = Solver(mesh, st, verbose=False, method="hmatrix", device=local)
+        sh.point(fm)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Sh = sh.point(fm)[0]
+        torch.cuda.synchronize()
+        th = time.perf_counter() - t0
+        hs = sh.hoperator().stats
+        sm = Solver(mesh, st, verbose=False, precision="mixed", device=local, **tol_kw)
+        Sm = sm.point(fm)[0]
+        hm_arm = {"value": round(1.0 / th, 4), "unit": UNIT, "freq": fm,
+                  "timing": "one Solver.point with method='hmatrix' (tables, near field, ACA, preconditioner, "
+                            "GMRES on both port columns, de-embedding), after one untimed point",
+                  "gmres_iterations": hs["gmres_iterations"], "entries_vs_dense":
+                      round((hs["near_entries"] + hs["far_entries"]) / mesh.n_unknowns ** 2, 4),
+                  "lowrank_blocks": hs["lowrank_blocks"], "max_rank": hs["max_rank"],
+                  "max_dS_vs_mixed": float(np.abs(Sh - Sm).max())}
+        sm.close()
+        sh.close()
     # max over ranks
     tt = torch.tensor([dt, dt_e2e], dtype=torch.float64, device="cuda")
     if world > 1:
@@ -379,6 +404,8 @@ def run_ours(args, rank, world, local):
     }
     if sur_arm is not None:
         out["surrogate"] = sur_arm
+    if hm_arm is not None:
+        out["hmatrix"] = hm_arm
     if world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline()
     return out
@@ -457,6 +484,7 @@ def main():
     ap.add_argument("--workers", type=int, default=8, help="frequency points in flight on the GPU")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the mixed + learned-remainder arm")
+    ap.add_argument("--no-hmatrix", action="store_true", help="skip the compressed-operator point")
     ap.add_argument("--refine-tol", type=float, default=None, help="mixed path: backward-error target of the refinement")
     ap.add_argument("--serial-points", type=int, default=1,
                     help="reference arm: points also timed as mom25d runs them (one process, 4 BLAS threads)")
