@@ -699,8 +699,8 @@ __global__ void __launch_bounds__(256) sur_judge_kernel(int NC, const double* __
 }
 
 // Decision and fill-in, one CTA per real column: accepted when the largest
-// column error <= tol x the largest |remainder| (every CTA forms the same
-// verdict; CTA 0 records it in flag / err_out). When accepted, the table's
+// column error <= tol x the largest |remainder| (every CTA reaches the same
+// decision; CTA 0 records it in flag / err_out). When accepted, the table's
 // other radii ir[] get network + a not-a-knot spline of the residual through
 // all ne integrated radii (a denser spline than the judged one). Shared
 // memory: 11 ne doubles.
