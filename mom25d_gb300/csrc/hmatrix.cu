@@ -588,7 +588,7 @@ __global__ void diag_kernel(const int64_t* __restrict__ pc_off, const int32_t* _
 // columns, and D^-1 = W D'^-1 W stored in place.
 __device__ __forceinline__ float fabs1(zf a) { return fabsf(a.re) + fabsf(a.im); }
 
-__global__ void __launch_bounds__(256) ginv_kernel(const int64_t* __restrict__ pc_off, const int64_t* __restrict__ doff,
+__global__ void __launch_bounds__(1024) ginv_kernel(const int64_t* __restrict__ pc_off, const int64_t* __restrict__ doff,
                                                    zf* __restrict__ D) {
   __shared__ double sv[32];
   __shared__ int si[32];
@@ -1206,7 +1206,7 @@ extern "C" int m25_hmat_assemble(m25_hmat* h, m25_greens* gr, double zs_re, doub
   diag_kernel<<<h->npc, 256, 0, st>>>(h->pc_off, h->pc_gidx, h->pc_item_off, h->pc_items, h->pc_doff, h->nb, h->nv,
                                       h->nnear, h->leaf_lo, h->near_off, h->Zn, h->fb, h->pool, h->dense_pool, h->ZxbT,
                                       h->Zxx, h->D);
-  ginv_kernel<<<h->npc, 256, 0, st>>>(h->pc_off, h->pc_doff, h->D);
+  ginv_kernel<<<h->npc, 1024, 0, st>>>(h->pc_off, h->pc_doff, h->D);  // 32 warps: the sweeps wait on L2
   if (cudaGetLastError() != cudaSuccess) {
     set_error("m25_hmat_assemble: launch failed");
     return done(M25_ERR_CUDA);
