@@ -14,8 +14,8 @@
 //   matvec       (far_t_kernel, rows_kernel, via_out_kernel): one warp per
 //                low-rank term projects x, then one warp per row sums its
 //                leaf's near blocks, far blocks as rows or as columns, and
-//                its via columns; every output entry has one writer
-//                (deterministic, no atomics);
+//                its via columns, in double-float on the fp32 pipes; every
+//                output entry has one writer (deterministic, no atomics);
 //   precondition (diag_kernel, ginv_kernel, psolve_kernel): restricted
 //                additive Schwarz over clusters of <= 256 unknowns extended
 //                by their near-coupled leaves and the vias whose pads they
@@ -42,7 +42,7 @@ struct FarB {
   int rank, kcap, cen;
   int64_t uv;     // U at pool + uv (kcap x m, term-major), V after it (kcap x n)
   int64_t dense;  // B at dense_pool + dense (m x n), B^T after it
-  int64_t t;      // the matvec's V^T x (kcap) then U^T x (kcap) at tpool + t
+  int64_t t;      // the matvec's V^T x (kcap) then U^T x (kcap) at t_df + t
   int64_t flag;   // ACA's used rows (m) then columns (n)
 };
 
@@ -71,13 +71,15 @@ struct m25_hmat {
   FarB* fb = nullptr;  // (nfar) device
   std::vector<FarB> fb_h;
   // device: values
-  m25::zd *Zn = nullptr, *pool = nullptr, *tpool = nullptr, *ZxbT = nullptr, *Zxx = nullptr;
+  m25::zd *Zn = nullptr, *pool = nullptr, *ZxbT = nullptr, *Zxx = nullptr;
   m25::zf* D = nullptr;       // preconditioner blocks (their inverses, in place)
   uint8_t* flags = nullptr;   // ACA's used rows / columns
   int64_t near_entries = 0, uv_entries = 0, dense_entries = 0, t_entries = 0, flag_bytes = 0, d_entries = 0;
   int32_t *aca_ids = nullptr, *rank = nullptr, *status = nullptr, *dense_ids = nullptr;
   int naca = 0;
   m25::zd* dense_pool = nullptr;  // far blocks kept as they are (B, then B^T)
+  float4* dense_df = nullptr;     // the same in double-float (the matvec's)
+  float4 *Zn_df = nullptr, *pool_df = nullptr, *ZxbT_df = nullptr, *x_df = nullptr, *t_df = nullptr;
   size_t dense_bytes = 0;
   bool assembled = false;
   // GMRES workspace
@@ -406,25 +408,77 @@ __global__ void __launch_bounds__(256) aca_kernel(Tabs t, const double* __restri
 }
 
 // ------------------------------------------------------------------ matvec
+// The matvec sums in double-float on the fp32 pipes (GB300 issues fp64 at
+// 1/64 of the fp32 rate; the fp64 form of these sums kept the fp64 pipe 86 %
+// busy): the operator and x are held as (hi, lo) fp32 pairs per real and
+// imaginary part (float4: re h, re l, im h, im l), products are exact to
+// fp32 x fp32 by FMA plus the low parts' cross terms, running sums by
+// Knuth's two-sum (~2^-48 relative). Warp results are combined in fp64.
+__device__ __forceinline__ float4 df_split(zd z) {
+  const float rh = (float)z.re, ih = (float)z.im;
+  return make_float4(rh, (float)(z.re - (double)rh), ih, (float)(z.im - (double)ih));
+}
+
+__global__ void df_split_kernel(const zd* __restrict__ src, float4* __restrict__ dst, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = df_split(src[i]);
+}
+
+struct DfAcc {
+  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+};
+
+__device__ __forceinline__ void two_sum(float& h, float& l, float x) {
+  const float s = __fadd_rn(h, x), z = __fsub_rn(s, h);
+  l = __fadd_rn(l, __fadd_rn(__fsub_rn(h, __fsub_rn(s, z)), __fsub_rn(x, z)));
+  h = s;
+}
+
+// p + e = a b for double-float reals a = (ah, al), b = (bh, bl)
+__device__ __forceinline__ float two_prod(float ah, float al, float bh, float bl, float& e) {
+  const float p = __fmul_rn(ah, bh);
+  e = __fadd_rn(fmaf(ah, bh, -p), __fadd_rn(__fmul_rn(ah, bl), __fmul_rn(al, bh)));
+  return p;
+}
+
+// acc += a b (complex, double-float)
+__device__ __forceinline__ void df_cmac(DfAcc& acc, float4 a, float4 b) {
+  float e1, e2, e3, e4;
+  const float p1 = two_prod(a.x, a.y, b.x, b.y, e1);  // ar br
+  const float p2 = two_prod(a.z, a.w, b.z, b.w, e2);  // ai bi
+  const float p3 = two_prod(a.x, a.y, b.z, b.w, e3);  // ar bi
+  const float p4 = two_prod(a.z, a.w, b.x, b.y, e4);  // ai br
+  two_sum(acc.rh, acc.rl, p1);
+  two_sum(acc.rh, acc.rl, -p2);
+  acc.rl = __fadd_rn(acc.rl, __fsub_rn(e1, e2));
+  two_sum(acc.ih, acc.il, p3);
+  two_sum(acc.ih, acc.il, p4);
+  acc.il = __fadd_rn(acc.il, __fadd_rn(e3, e4));
+}
+
+__device__ __forceinline__ zd df_value(const DfAcc& a) {
+  return zd((double)a.rh + (double)a.rl, (double)a.ih + (double)a.il);
+}
+
 // per term l of a low-rank far block: V_l^T x[C] and U_l^T x[R], one warp per (block, term)
 __global__ void far_t_kernel(const int2* __restrict__ terms, int nterm, const FarB* __restrict__ fb,
-                             const zd* __restrict__ pool, const zd* __restrict__ x, zd* __restrict__ tpool) {
+                             const float4* __restrict__ pool, const float4* __restrict__ x,
+                             float4* __restrict__ tpool) {
   const int lane = threadIdx.x & 31;
   const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (q >= nterm) return;
   const int2 bt = terms[q];
   const FarB F = fb[bt.x];
   const int l = bt.y;
-  const zd* U = pool + F.uv + (int64_t)l * F.m;
-  const zd* V = pool + F.uv + (int64_t)F.kcap * F.m + (int64_t)l * F.n;
-  zd d1, d2;
-  for (int j = lane; j < F.n; j += 32) d1 += V[j] * x[F.c0 + j];
-  for (int r = lane; r < F.m; r += 32) d2 += U[r] * x[F.r0 + r];
-  d1 = warp_sum(d1);
-  d2 = warp_sum(d2);
+  const float4* U = pool + F.uv + (int64_t)l * F.m;
+  const float4* V = pool + F.uv + (int64_t)F.kcap * F.m + (int64_t)l * F.n;
+  DfAcc a1, a2;
+  for (int j = lane; j < F.n; j += 32) df_cmac(a1, V[j], x[F.c0 + j]);
+  for (int r = lane; r < F.m; r += 32) df_cmac(a2, U[r], x[F.r0 + r]);
+  const zd d1 = warp_sum(df_value(a1)), d2 = warp_sum(df_value(a2));
   if (lane == 0) {
-    tpool[F.t + l] = d1;
-    tpool[F.t + F.kcap + l] = d2;
+    tpool[F.t + l] = df_split(d1);
+    tpool[F.t + F.kcap + l] = df_split(d2);
   }
 }
 
@@ -433,49 +487,49 @@ __global__ void __launch_bounds__(256) rows_kernel(const int32_t* __restrict__ r
                                                    const int32_t* __restrict__ leaf_lo,
                                                    const int64_t* __restrict__ ent_off,
                                                    const int32_t* __restrict__ ent, const int32_t* __restrict__ near,
-                                                   const int64_t* __restrict__ noff, const zd* __restrict__ Zn,
-                                                   const FarB* __restrict__ fb, const zd* __restrict__ pool,
-                                                   const zd* __restrict__ dpool, const zd* __restrict__ tpool,
-                                                   const zd* __restrict__ ZxbT, int nb, int nv,
-                                                   const zd* __restrict__ x, zd* __restrict__ y) {
+                                                   const int64_t* __restrict__ noff, const float4* __restrict__ Zn,
+                                                   const FarB* __restrict__ fb, const float4* __restrict__ pool,
+                                                   const float4* __restrict__ dpool, const float4* __restrict__ tpool,
+                                                   const float4* __restrict__ ZxbT, int nb, int nv,
+                                                   const float4* __restrict__ x, zd* __restrict__ y) {
   const int lane = threadIdx.x & 31;
   const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (r >= nb) return;
   const int leaf = row_leaf[r];
   const int lo = leaf_lo[leaf];
   const int64_t e0 = ent_off[leaf], e1 = ent_off[leaf + 1];
-  zd acc;
+  DfAcc acc;
   for (int64_t e = e0; e < e1; ++e) {
     const int type = ent[4 * e], id = ent[4 * e + 1], off = ent[4 * e + 2];
     if (type == 0) {
       const int a0 = near[4 * id], b0 = near[4 * id + 2], bn = near[4 * id + 3];
-      const zd* row = Zn + noff[id] + (int64_t)(r - a0) * bn;
-      for (int j = lane; j < bn; j += 32) acc += row[j] * x[b0 + j];
+      const float4* row = Zn + noff[id] + (int64_t)(r - a0) * bn;
+      for (int j = lane; j < bn; j += 32) df_cmac(acc, row[j], x[b0 + j]);
       continue;
     }
     const FarB F = fb[id];
     const int q = off + (r - lo);  // row of the block (type 1) or of its transpose (type 2)
     if (F.kind == 0) {
-      const zd* U = pool + F.uv;
-      const zd* V = U + (int64_t)F.kcap * F.m;
+      const float4* U = pool + F.uv;
+      const float4* V = U + (int64_t)F.kcap * F.m;
       if (type == 1)
-        for (int l = lane; l < F.rank; l += 32) acc += U[(int64_t)l * F.m + q] * tpool[F.t + l];
+        for (int l = lane; l < F.rank; l += 32) df_cmac(acc, U[(int64_t)l * F.m + q], tpool[F.t + l]);
       else
-        for (int l = lane; l < F.rank; l += 32) acc += V[(int64_t)l * F.n + q] * tpool[F.t + F.kcap + l];
+        for (int l = lane; l < F.rank; l += 32) df_cmac(acc, V[(int64_t)l * F.n + q], tpool[F.t + F.kcap + l]);
     } else {
-      const zd* B = dpool + F.dense;
+      const float4* B = dpool + F.dense;
       if (type == 1) {
-        const zd* row = B + (int64_t)q * F.n;
-        for (int j = lane; j < F.n; j += 32) acc += row[j] * x[F.c0 + j];
+        const float4* row = B + (int64_t)q * F.n;
+        for (int j = lane; j < F.n; j += 32) df_cmac(acc, row[j], x[F.c0 + j]);
       } else {
-        const zd* row = B + (int64_t)F.m * F.n + (int64_t)q * F.m;
-        for (int j = lane; j < F.m; j += 32) acc += row[j] * x[F.r0 + j];
+        const float4* row = B + (int64_t)F.m * F.n + (int64_t)q * F.m;
+        for (int j = lane; j < F.m; j += 32) df_cmac(acc, row[j], x[F.r0 + j]);
       }
     }
   }
-  for (int v = lane; v < nv; v += 32) acc += ZxbT[(int64_t)r * nv + v] * x[nb + v];
-  acc = warp_sum(acc);
-  if (lane == 0) y[r] = acc;
+  for (int v = lane; v < nv; v += 32) df_cmac(acc, ZxbT[(int64_t)r * nv + v], x[nb + v]);
+  const zd a = warp_sum(df_value(acc));
+  if (lane == 0) y[r] = a;
 }
 
 // y of the via unknowns: Zvb x_b + Zvv x_v, one CTA per via row
@@ -778,9 +832,11 @@ namespace {
 // y = A x, tree order, device vectors
 int apply(m25_hmat* h, const zd* x, zd* y) {
   cudaStream_t st = h->ctx->stream;
-  if (h->nterm) far_t_kernel<<<(h->nterm + 7) / 8, 256, 0, st>>>(h->terms, h->nterm, h->fb, h->pool, x, h->tpool);
-  rows_kernel<<<(h->nb + 7) / 8, 256, 0, st>>>(h->row_leaf, h->leaf_lo, h->ent_off, h->ent, h->near, h->near_off, h->Zn, h->fb, h->pool,
-                                        h->dense_pool, h->tpool, h->ZxbT, h->nb, h->nv, x, y);
+  df_split_kernel<<<(h->n + 255) / 256, 256, 0, st>>>(x, h->x_df, h->n);
+  if (h->nterm) far_t_kernel<<<(h->nterm + 7) / 8, 256, 0, st>>>(h->terms, h->nterm, h->fb, h->pool_df, h->x_df, h->t_df);
+  rows_kernel<<<(h->nb + 7) / 8, 256, 0, st>>>(h->row_leaf, h->leaf_lo, h->ent_off, h->ent, h->near, h->near_off,
+                                               h->Zn_df, h->fb, h->pool_df, h->dense_df, h->t_df, h->ZxbT_df, h->nb,
+                                               h->nv, h->x_df, y);
   if (h->nv) via_out_kernel<<<h->nv, 256, 0, st>>>(h->nb, h->nv, h->ZxbT, h->Zxx, x, y);
   M25_CHECK_LAUNCH();
   return M25_OK;
@@ -960,6 +1016,11 @@ extern "C" int m25_hmat_create(m25_ctx* ctx, m25_geom* geom, const m25_hmat_desc
   TRY(dalloc(h->allocs, &h->row_leaf, d->nb));
   TRY(dalloc(h->allocs, &h->self_near, d->nleaf));
   TRY(dalloc(h->allocs, &h->wsc, h->n));
+  TRY(dalloc(h->allocs, &h->Zn_df, h->near_entries));
+  TRY(dalloc(h->allocs, &h->pool_df, uv));
+  TRY(dalloc(h->allocs, &h->ZxbT_df, (size_t)d->nb * std::max(d->nv, 1)));
+  TRY(dalloc(h->allocs, &h->x_df, h->n));
+  TRY(dalloc(h->allocs, &h->t_df, tt));
   TRY(dalloc(h->allocs, &h->sx, h->n));
   TRY(dalloc(h->allocs, &h->near, 4 * (size_t)d->nnear));
   TRY(dalloc(h->allocs, &h->near_off, d->nnear + 1));
@@ -976,7 +1037,6 @@ extern "C" int m25_hmat_create(m25_ctx* ctx, m25_geom* geom, const m25_hmat_desc
   TRY(dalloc(h->allocs, &h->fb, d->nfar));
   TRY(dalloc(h->allocs, &h->Zn, h->near_entries));
   TRY(dalloc(h->allocs, &h->pool, uv));
-  TRY(dalloc(h->allocs, &h->tpool, tt));
   TRY(dalloc(h->allocs, &h->terms, std::max<int64_t>(tt / 2, 1)));
   TRY(dalloc(h->allocs, &h->flags, fl));
   TRY(dalloc(h->allocs, &h->ZxbT, (size_t)d->nb * std::max(d->nv, 1)));
@@ -1187,8 +1247,11 @@ extern "C" int m25_hmat_assemble(m25_hmat* h, m25_greens* gr, double zs_re, doub
   if ((size_t)doff * sizeof(zd) > h->dense_bytes) {
     free_all(h->dense_allocs);
     h->dense_pool = nullptr;
+    h->dense_df = nullptr;
     h->dense_bytes = 0;
-    if ((rc = dalloc(h->dense_allocs, &h->dense_pool, (size_t)doff))) return done(rc);
+    if ((rc = dalloc(h->dense_allocs, &h->dense_pool, (size_t)doff)) ||
+        (rc = dalloc(h->dense_allocs, &h->dense_df, (size_t)doff)))
+      return done(rc);
     h->dense_bytes = (size_t)std::max<int64_t>(doff, 1) * sizeof(zd);
   }
   if ((h->nfar && cudaMemcpyAsync(h->fb, h->fb_h.data(), sizeof(FarB) * h->nfar, cudaMemcpyHostToDevice, st) !=
@@ -1201,6 +1264,15 @@ extern "C" int m25_hmat_assemble(m25_hmat* h, m25_greens* gr, double zs_re, doub
   if (!dense.empty())
     far_dense_kernel<<<(unsigned)dense.size(), 256, 0, st>>>(t, h->rules, h->lev, h->fb, h->dense_ids, h->dense_pool);
   // preconditioner: the diagonal blocks and their LU
+  {  // the matvec's double-float copies of the operator
+    auto split = [&](const zd* src, float4* dst, int64_t n) {
+      if (n > 0) df_split_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, st>>>(src, dst, n);
+    };
+    split(h->Zn, h->Zn_df, h->near_entries);
+    split(h->pool, h->pool_df, h->uv_entries);
+    split(h->ZxbT, h->ZxbT_df, (int64_t)h->nb * h->nv);
+    split(h->dense_pool, h->dense_df, doff);
+  }
   wscale_kernel<<<(h->n + 255) / 256, 256, 0, st>>>(h->nb, h->n, h->nv, h->row_leaf, h->self_near, h->near,
                                                     h->near_off, h->Zn, h->Zxx, h->wsc);
   diag_kernel<<<h->npc, 256, 0, st>>>(h->pc_off, h->pc_gidx, h->pc_item_off, h->pc_items, h->pc_doff, h->nb, h->nv,
