@@ -156,3 +156,23 @@ def test_plan_rules_match_mesh():
     assert np.allclose(pts, cen, rtol=0, atol=1e-15)
     assert np.allclose(r[:, 24:30].sum(1), 0, atol=1e-12 * np.abs(r[:, 24:30]).max())
     assert np.allclose(r[:, 38:40].sum(1), 0, atol=1e-12 * np.abs(r[:, 38:40]).max())
+
+
+def test_plan_block_jacobi_and_overlap_cap():
+    """overlap=False: each preconditioner block holds exactly its own leaves
+    (and vias) and writes all of them; with overlap every block stays within
+    prec_max unknowns unless its own part is larger, and grows by whole
+    near-coupled leaves only."""
+    m, P = _plan("via", overlap=False)
+    assert np.all(P.pc_own == 1)
+    m, P2 = _plan("via", prec_max=400)
+    own = [int(P2.pc_own[P2.pc_off[k]:P2.pc_off[k + 1]].sum()) for k in range(P2.npc)]
+    for k in range(P2.npc):
+        assert P2.prec_sizes[k] <= max(400, own[k])
+        g = P2.pc_gidx[P2.pc_off[k]:P2.pc_off[k + 1]]
+        g = g[g < P2.nb]
+        starts = set(P2.leaf_lo[:-1].tolist())
+        # whole leaves: every run of consecutive positions starts at a leaf start
+        runs = np.r_[0, np.nonzero(np.diff(g) != 1)[0] + 1]
+        assert all(int(g[r]) in starts for r in runs)
+    assert P2.prec_sizes.max() <= P.prec_sizes.max() + 400
