@@ -56,11 +56,7 @@ TRI3_W = np.full(3, 1 / 3)
 class Cluster:
     """A node of the cluster tree: positions [lo, hi) of the tree order."""
 
-    __slots__ = ("id", "lo", "hi", "bmin", "bmax", "smax", "children")
-
-    @property
-    def diam(self):
-        return float(np.linalg.norm(self.bmax - self.bmin))
+    __slots__ = ("id", "lo", "hi", "bmin", "bmax", "lo3", "hi3", "smax", "children", "diam")
 
     @property
     def size(self):
@@ -87,6 +83,8 @@ def cluster_tree(pos, size, leaf):
         c.lo, c.hi = lo, lo + idx.size
         p = pos[idx]
         c.bmin, c.bmax = p.min(0), p.max(0)
+        c.lo3, c.hi3 = tuple(float(v) for v in c.bmin), tuple(float(v) for v in c.bmax)
+        c.diam = float(np.linalg.norm(c.bmax - c.bmin))  # as mom25d's _Cluster.diam, once
         c.smax = float(size[idx].max())
         c.children = []
         if parent is None:
@@ -107,8 +105,13 @@ def cluster_tree(pos, size, leaf):
 
 
 def _dist(a, b):
-    gap = np.maximum(0.0, np.maximum(a.bmin - b.bmax, b.bmin - a.bmax))
-    return float(np.linalg.norm(gap))
+    """Distance of the bounding boxes (hmatrix.py:65-67): the gap per axis
+    (exact in floats), its norm by numpy as mom25d takes it; overlapping
+    boxes at once."""
+    gap = [max(0.0, max(x0 - y1, y0 - x1)) for x0, x1, y0, y1 in zip(a.lo3, a.hi3, b.lo3, b.hi3)]
+    if gap[0] == 0.0 and gap[1] == 0.0 and gap[2] == 0.0:
+        return 0.0
+    return float(np.linalg.norm(np.array(gap)))
 
 
 def partition(root, eta):
