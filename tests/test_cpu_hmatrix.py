@@ -176,3 +176,50 @@ def test_plan_block_jacobi_and_overlap_cap():
         runs = np.r_[0, np.nonzero(np.diff(g) != 1)[0] + 1]
         assert all(int(g[r]) in starts for r in runs)
     assert P2.prec_sizes.max() <= P.prec_sizes.max() + 400
+
+
+class _FakeLib:
+    """Stands in for the engine's m25_hmat_solve: X = B, with the given
+    iterations and residuals per column."""
+
+    def __init__(self, resid):
+        self.resid = resid
+
+    def m25_hmat_solve(self, h, k, B, X, rtol, restart, maxiter, its, res):
+        import ctypes
+
+        n2 = 2 * k * self.n
+        ctypes.memmove(X, B, 8 * n2)
+        for c in range(k):
+            its[c] = 600
+            res[c] = self.resid[c]
+        return 0
+
+
+def _fake_hmatrix(resid, n=6, tol=1e-4):
+    from types import SimpleNamespace
+
+    hm = object.__new__(H.HMatrix)
+    lib = _FakeLib(resid)
+    lib.n = n
+    hm.ctx = SimpleNamespace(lib=lib)
+    hm._h = SimpleNamespace(h=None)
+    hm.n, hm.tol, hm.stats = n, tol, {}
+    return hm
+
+
+def test_stalled_gmres_accepted_within_the_compression_tolerance():
+    """mom25d's acceptance (hmatrix.py:583-591): a column that stops above
+    rtol is accepted with a RuntimeWarning when its residual is within
+    ACCEPT x tol, and raises RuntimeError above it."""
+    B = np.arange(12.0).reshape(6, 2) + 1j
+    hm = _fake_hmatrix([1e-7, 1e-7])
+    X = hm.solve(B, rtol=1e-6)
+    assert np.array_equal(X, B) and hm.stats["gmres_iterations"] == [600, 600]
+    hm = _fake_hmatrix([5e-5, 1e-7])
+    with pytest.warns(RuntimeWarning, match="accepted"):
+        hm.solve(B, rtol=1e-6)
+    hm = _fake_hmatrix([1e-7, 2e-4])
+    with pytest.raises(RuntimeError, match="did not converge"):
+        hm.solve(B, rtol=1e-6)
+    assert hm.stats["gmres_residuals"] == [1e-7, 2e-4]
